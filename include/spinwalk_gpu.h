@@ -1,0 +1,184 @@
+/*
+ * spinwalk_gpu.h -- C ABI of libspinwalk_gpu.so, the GB300 (sm_103a) implementation of
+ * SpinWalk's `sim` hot path: the per-spin Monte-Carlo random walk over a voxel phantom with
+ * the Bloch update.
+ *
+ * Every entry point returns an int status (SW_OK or a negative SW_ERR_* code) and never exits
+ * or traps; sw_last_error() gives a one-line message for the last failure on the calling thread.
+ * No torch or CUDA types appear in the signatures: streams are passed as `void*`
+ * (a cudaStream_t, NULL = legacy default stream).
+ *
+ * Reference interfaces replaced (paths relative to the SpinWalk 1.21.0 source tree):
+ *   sw_params            <- struct sim::parameters          src/sim/simulation_parameters.cuh:176-246
+ *   sw_sequence          <- struct parameters_uvec          src/sim/simulation_parameters.cuh:102-173
+ *   sw_sim               <- std::for_each(par_unseq, sim::sim) over all spins of one scale
+ *                           src/sim/monte_carlo.cu:313-321 (host buffers in, host buffers out)
+ *   sw_sim_device        <- cu_sim<<<ceil(n/256),256>>>(...) + gpuCheckKernelExecutionError
+ *                           src/sim/kernels.cu:57-63, src/sim/monte_carlo.cu:324-333
+ *   sw_prepare_params    <- parameters::prepare              src/sim/simulation_parameters.cuh:227-245
+ *   sw_fieldmap_scale    <- Tesla -> degree-per-timestep factor src/sim/monte_carlo.cu:241
+ *   sw_run_config        <- sim::monte_carlo::run            src/sim/monte_carlo.cu:199-355
+ */
+#ifndef SPINWALK_GPU_H
+#define SPINWALK_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SW_ABI_VERSION 1
+
+/* ---- return codes -------------------------------------------------------------------- */
+#define SW_OK              0
+#define SW_ERR_INVALID    -1   /* bad argument or inconsistent parameters */
+#define SW_ERR_CUDA       -2   /* a CUDA runtime call failed */
+#define SW_ERR_NOMEM      -3   /* device allocation failed or the HBM budget is exceeded */
+#define SW_ERR_IO         -4   /* file could not be read or written */
+#define SW_ERR_CONFIG     -5   /* config file rejected (same checks as config_reader::check) */
+#define SW_ERR_TIMEOUT    -6   /* a bounded device loop gave up (reported, never a hang) */
+
+/* ---- per-spin status (written to the optional `status` array) ------------------------ */
+#define SW_SPIN_OK         0   /* walked to the end of the last scan */
+#define SW_SPIN_LOST       1   /* more than max_iterations rejected moves in a row
+                                  (reference: printf + return, src/sim/kernels.cu:155-158) */
+#define SW_SPIN_OOB        2   /* voxel index outside the phantom
+                                  (reference: printf + return, src/sim/kernels.cu:141-147) */
+#define SW_SPIN_START_OOB  3   /* starting position outside the phantom (the reference reads
+                                  mask[] out of bounds there, src/sim/kernels.cu:102-103) */
+
+/* ---- precision of the Bloch part (the walk itself is always bit-exact FP64) ----------- */
+#define SW_PREC_FP32       0   /* the reference's arithmetic: float phase sum, float Bloch */
+#define SW_PREC_FP64       1   /* same walk, phase sum + rotations + relaxation in double */
+#define SW_PREC_KAHAN      2   /* same walk, compensated (Kahan) float phase sum */
+
+/*
+ * Scalar simulation parameters. Field-for-field mirror of sim::parameters
+ * (src/sim/simulation_parameters.cuh:176-186), with bools widened to int32 and size_t to
+ * uint64 so the layout is the same on every platform. Values are AFTER parameters::prepare():
+ * c/s hold cos/sin of RF_FA[0]; n_timepoints = TR_us / timestep_us.
+ */
+typedef struct sw_params {
+    double   fov[3];                  /* field of view in m (after FoV scaling)           */
+    float    B0;                      /* T (the fieldmap passed in is already deg/step)   */
+    float    c, s;                    /* cosf/sinf(RF_FA_deg[0] * pi/180)                 */
+    float    linear_phase_cycling;    /* degrees added to RF_PH[0] per dummy scan         */
+    float    quadratic_phase_cycling; /* degrees, quadratic term                          */
+    int32_t  timestep_us;
+    int32_t  TR_us;
+    int32_t  n_dummy_scan;
+    uint32_t n_spins;
+    uint32_t n_timepoints;
+    uint32_t n_substrate;
+    uint32_t n_scales;
+    uint64_t phantom_size[3];         /* Nx, Ny, Nz; data are row-major, z fastest        */
+    uint64_t seed;                    /* per-spin generators are seeded with seed + spin  */
+    uint64_t max_iterations;          /* rejected moves allowed before a spin is lost     */
+    int64_t  matrix_length;           /* Nx*Ny*Nz                                         */
+    int32_t  enCrossFOV;              /* 1: periodic wrap, 0: reflect at the FoV boundary  */
+    int32_t  enRecordTrajectory;      /* 1: XYZ1 holds every step, 0: final position only */
+    int32_t  fieldmap_exist;
+    int32_t  _pad;
+} sw_params;
+
+/*
+ * Sequence and tissue tables. Mirror of parameters_uvec
+ * (src/sim/simulation_parameters.cuh:102-106). Pointers are HOST pointers for sw_sim and
+ * sw_sim_device alike (the library copies the tables itself). Times are in time points, i.e.
+ * after config_reader::timing_scale (src/sim/config_reader.cpp:39-46), as in the reference.
+ */
+typedef struct sw_sequence {
+    const double  *diffusivity;      /* [n_substrate] random-walk step std-dev in m        */
+    const float   *T1_ms, *T2_ms;    /* [n_substrate]; negative = no relaxation            */
+    const float   *pXY;              /* [n_substrate^2] crossing probability, row = from   */
+    const float   *RF_FA_deg;        /* [n_RF]                                             */
+    const float   *RF_PH_deg;        /* [n_RF]                                             */
+    const int32_t *RF_us;            /* [n_RF] time points, RF_us[0] == 0                  */
+    const int32_t *TE_us;            /* [n_TE] time points, strictly ascending             */
+    const float   *dephasing_deg;    /* [n_dephasing]                                      */
+    const int32_t *dephasing_us;     /* [n_dephasing] time points                          */
+    const float   *gradientX_mTm;    /* [n_gradient]                                       */
+    const float   *gradientY_mTm;
+    const float   *gradientZ_mTm;
+    const int32_t *gradient_us;      /* [n_gradient] time points                           */
+    uint32_t n_RF, n_TE, n_dephasing, n_gradient;
+} sw_sequence;
+
+/* Library and device information. */
+int         sw_abi_version(void);
+const char *sw_last_error(void);
+int         sw_device_count(int *count);
+
+/*
+ * parameters::prepare (src/sim/simulation_parameters.cuh:227-245) on plain arrays:
+ * sets c/s from RF_FA_deg[0], n_timepoints = TR/dt, replaces seed 0 by a random seed,
+ * converts diffusivity[i] (m^2/s, in place) to the step std-dev 1e-3*sqrt(2*D*dt_us), and
+ * sets n_dummy_scan = 5*T1[0]/TR when it is negative.
+ */
+int sw_prepare_params(sw_params *p, double *diffusivity, const float *RF_FA_deg,
+                      const float *T1_ms);
+
+/* Factor from Tesla (at 1 T) to degree per time step, computed as the reference does
+ * (src/sim/monte_carlo.cu:241): float(B0*dt*1e-6*GAMMA*RAD2DEG). */
+float sw_fieldmap_scale(float B0, int32_t timestep_us);
+
+/* Initial positions when no XYZ0 file is given: monte_carlo::initialize_position
+ * (src/sim/monte_carlo.cu:141-151): std::mt19937(seed), per spin x, y, z drawn from
+ * uniform_real_distribution<float>(0.01*fov, 0.99*fov). XYZ0 is [n_spins*3]. */
+int sw_initial_positions(const float fov[3], uint64_t seed, uint32_t n_spins, float *XYZ0);
+
+/* Size of the table that makes the device logf equal to this host's libm logf (built on first
+ * use; `wide` counts differences larger than one ulp and must be 0). No reference counterpart:
+ * it exists so that the GPU reproduces libstdc++'s normal_distribution<float> bit for bit. */
+int sw_logf_exception_count(uint64_t *count, uint64_t *wide);
+
+/*
+ * Run the whole walk for all p->n_spins spins of ONE scale, host buffers in and out.
+ * Replaces the per-scale CPU loop std::for_each(par_unseq, sim(...)) of
+ * src/sim/monte_carlo.cu:313-321 with the GPU kernels; semantics are those of sim::sim
+ * (src/sim/kernels.cu:72-233) with the libstdc++ std::mt19937 generators, bit for bit.
+ *   pFieldMap : [matrix_length] float, degree per time step, or NULL (no off-resonance)
+ *   pMask     : [matrix_length] uint8 substrate index
+ *   M0, XYZ0  : [n_spins*3] float
+ *   M1        : [n_spins*n_TE*3]  written at echo times only (untouched for echoes a lost
+ *               or out-of-bounds spin never reaches, as in the reference)
+ *   XYZ1      : [n_spins*(enRecordTrajectory ? (n_dummy_scan+1)*n_timepoints : 1)*3]
+ *   T         : [n_spins*n_TE] substrate at each echo
+ *   status    : [n_spins] SW_SPIN_* or NULL
+ *   precision : SW_PREC_*; M1_fp64 (optional, [n_spins*n_TE*3] double) receives the FP64
+ *               shadow magnetisation of the same walk when non-NULL.
+ */
+int sw_sim(const sw_params *param, const sw_sequence *seq,
+           const float *pFieldMap, const uint8_t *pMask,
+           const float *M0, const float *XYZ0,
+           float *M1, float *XYZ1, uint8_t *T, int32_t *status,
+           int precision, double *M1_fp64);
+
+/* Same as sw_sim with DEVICE buffers (the cu_sim analogue). Asynchronous on `stream` except
+ * for the small parameter-table uploads; sw_sync(stream) waits and reports errors. */
+int sw_sim_device(const sw_params *param, const sw_sequence *seq,
+                  const float *d_FieldMap, const uint8_t *d_Mask,
+                  const float *d_M0, const float *d_XYZ0,
+                  float *d_M1, float *d_XYZ1, uint8_t *d_T, int32_t *d_status,
+                  int precision, double *d_M1_fp64, void *stream);
+int sw_sync(void *stream);
+
+/* Timing of the kernels launched by the last sw_sim / sw_sim_device call on this thread
+ * (milliseconds, CUDA events on the launching stream): seeding, RNG refill, walk, total. */
+typedef struct sw_timing {
+    float seed_ms, refill_ms, walk_ms, total_ms;
+    uint32_t n_chunks;       /* refill+walk rounds                                   */
+    uint32_t n_launches;     /* kernels launched by the call                         */
+} sw_timing;
+int sw_last_timing(sw_timing *out);
+
+/* Host-visible check of the bit-exact logf used by the Gaussian generator: evaluates the
+ * device logf on n inputs (device pointers) -- used by the tests. */
+int sw_debug_logf(const float *d_x, float *d_y, uint64_t n, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPINWALK_GPU_H */

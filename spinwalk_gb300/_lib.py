@@ -1,0 +1,116 @@
+"""ctypes binding of libspinwalk_gpu.so (the C ABI declared in include/spinwalk_gpu.h).
+
+The library is loaded from this package directory only. There is no fallback: if the library
+is missing, or no GPU is visible, every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libspinwalk_gpu.so")
+_lib = None
+
+
+class SpinWalkError(RuntimeError):
+    pass
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SpinWalkError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; "
+                "g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        P = C.POINTER
+        L.sw_abi_version.restype = C.c_int
+        L.sw_last_error.restype = C.c_char_p
+        L.sw_device_count.argtypes = [P(C.c_int)]
+        L.sw_prepare_params.argtypes = [P(abi.SwParams), P(C.c_double), P(C.c_float),
+                                        P(C.c_float)]
+        L.sw_fieldmap_scale.restype = C.c_float
+        L.sw_fieldmap_scale.argtypes = [C.c_float, C.c_int32]
+        L.sw_initial_positions.argtypes = [P(C.c_float), C.c_uint64, C.c_uint32, P(C.c_float)]
+        L.sw_logf_exception_count.argtypes = [P(C.c_uint64), P(C.c_uint64)]
+        sim_args = [P(abi.SwParams), P(abi.SwSequence), C.c_void_p, C.c_void_p, C.c_void_p,
+                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                    C.c_void_p]
+        L.sw_sim.argtypes = sim_args
+        L.sw_sim_device.argtypes = sim_args + [C.c_void_p]
+        L.sw_sync.argtypes = [C.c_void_p]
+        L.sw_last_timing.argtypes = [P(abi.SwTiming)]
+        L.sw_debug_logf.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
+        if L.sw_abi_version() != 1:
+            raise SpinWalkError("libspinwalk_gpu ABI version mismatch")
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != abi.SW_OK:
+        raise SpinWalkError(f"spinwalk error {rc}: {lib().sw_last_error().decode()}")
+
+
+def device_count():
+    n = C.c_int(0)
+    lib().sw_device_count(C.byref(n))
+    return n.value
+
+
+def fieldmap_scale(B0, timestep_us):
+    return np.float32(lib().sw_fieldmap_scale(B0, timestep_us))
+
+
+def initial_positions(fov, seed, n_spins):
+    out = np.zeros((n_spins, 3), np.float32)
+    f = (C.c_float * 3)(*[float(np.float32(x)) for x in fov])
+    check(lib().sw_initial_positions(f, C.c_uint64(int(seed)), C.c_uint32(n_spins),
+                                     out.ctypes.data_as(C.POINTER(C.c_float))))
+    return out
+
+
+def logf_exception_count():
+    n, w = C.c_uint64(0), C.c_uint64(0)
+    check(lib().sw_logf_exception_count(C.byref(n), C.byref(w)))
+    return n.value, w.value
+
+
+def last_timing():
+    t = abi.SwTiming()
+    check(lib().sw_last_timing(C.byref(t)))
+    return {k: getattr(t, k) for k, _ in abi.SwTiming._fields_}
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def run(problem, precision=abi.SW_PREC_FP32, fp64_shadow=False, fill=0.0):
+    """sw_sim on host buffers: one scale of `problem` (a problem.Problem). Returns a dict with
+    M1 [n, nTE, 3], XYZ1 [n, traj, 3], T [n, nTE], status [n] (+ M1_fp64, timing)."""
+    M1, XYZ1, T, status = problem.outputs(fill)
+    M1d = np.full(M1.shape, fill, np.float64) if fp64_shadow else None
+    check(lib().sw_sim(C.byref(problem.params), C.byref(problem.seq.struct),
+                       _p(problem.field), _p(problem.mask), _p(problem.M0), _p(problem.XYZ0),
+                       _p(M1), _p(XYZ1), _p(T), _p(status), int(precision), _p(M1d)))
+    out = dict(M1=M1, XYZ1=XYZ1, T=T, status=status, timing=last_timing())
+    if M1d is not None:
+        out["M1_fp64"] = M1d
+    return out
+
+
+def run_device(problem, d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T, d_status=None,
+               precision=abi.SW_PREC_FP32, d_M1d=None, stream=None):
+    """sw_sim_device with raw device pointers (ints), e.g. torch tensors' data_ptr()."""
+    check(lib().sw_sim_device(C.byref(problem.params), C.byref(problem.seq.struct),
+                              d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T, d_status,
+                              int(precision), d_M1d, stream))
+
+
+def debug_logf(d_x, d_y, n, stream=None):
+    check(lib().sw_debug_logf(d_x, d_y, C.c_uint64(n), stream))

@@ -1,0 +1,479 @@
+// C ABI of libspinwalk_gpu (include/spinwalk_gpu.h): argument checks, device workspace,
+// parameter-table upload and the seed -> (refill, walk)* launch sequence.
+//
+// The workspace (packed phantom, per-spin walk state, generator state and buffers) is owned by
+// a per-device context, grown on demand and reused across calls; calls on the same device are
+// serialised by a mutex. Nothing here exits or traps: failures come back as SW_ERR_* codes
+// with a message in sw_last_error().
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "spinwalk_gpu.h"
+#include "sw_host.h"
+#include "sw_kernels.h"
+
+namespace {
+
+thread_local std::string g_err;
+thread_local sw_timing g_timing{};
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define SW_CUDA(call)                                                                  \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess)                                                         \
+            return fail(SW_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr int kMaxDevices = 64;
+constexpr int kMaxTimedChunks = 4096;
+
+struct DeviceCtx {
+    std::mutex mu;
+    bool logf_ready = false;
+    float *d_logf_tab = nullptr;
+    uint32_t *d_logf_off = nullptr, *d_logf_ent = nullptr;
+    char *ws = nullptr;
+    size_t ws_size = 0;
+    uint32_t *h_active = nullptr;          // pinned
+    std::vector<cudaEvent_t> ev;           // timing events
+};
+DeviceCtx g_ctx[kMaxDevices];
+
+// Bump allocator over the workspace (256-byte aligned slices).
+struct Carve {
+    char *base;
+    size_t off = 0;
+    template <typename T>
+    T *take(size_t n) {
+        off = (off + 255) & ~size_t(255);
+        T *p = base ? reinterpret_cast<T *>(base + off) : nullptr;
+        off += n * sizeof(T);
+        return p;
+    }
+};
+
+int ensure_logf(DeviceCtx &c) {
+    if (c.logf_ready) return SW_OK;
+    const sw::LogfExceptions &ex = sw::logf_exceptions();
+    if (ex.wide != 0) return fail(SW_ERR_INVALID, "host logf differs from the candidate by >1 ulp");
+    SW_CUDA(cudaMalloc(&c.d_logf_tab, 192 * sizeof(float)));
+    SW_CUDA(cudaMalloc(&c.d_logf_off, ex.off.size() * sizeof(uint32_t)));
+    SW_CUDA(cudaMalloc(&c.d_logf_ent, std::max<size_t>(1, ex.ent.size()) * sizeof(uint32_t)));
+    SW_CUDA(cudaMemcpy(c.d_logf_tab, sw::logf_reduction_table(), 192 * sizeof(float),
+                       cudaMemcpyHostToDevice));
+    SW_CUDA(cudaMemcpy(c.d_logf_off, ex.off.data(), ex.off.size() * sizeof(uint32_t),
+                       cudaMemcpyHostToDevice));
+    if (!ex.ent.empty())
+        SW_CUDA(cudaMemcpy(c.d_logf_ent, ex.ent.data(), ex.ent.size() * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice));
+    SW_CUDA(cudaMallocHost(&c.h_active, sizeof(uint32_t)));
+    c.ev.resize(2 * kMaxTimedChunks + 4);
+    for (auto &e : c.ev) SW_CUDA(cudaEventCreate(&e));
+    c.logf_ready = true;
+    return SW_OK;
+}
+
+sw::LogfTables logf_tables(const DeviceCtx &c) {
+    return sw::LogfTables{c.d_logf_tab, c.d_logf_off, c.d_logf_ent};
+}
+
+int check_args(const sw_params *p, const sw_sequence *q) {
+    if (!p || !q) return fail(SW_ERR_INVALID, "null params or sequence");
+    if (p->n_substrate == 0 || p->n_substrate > 256) return fail(SW_ERR_INVALID, "n_substrate");
+    if (!q->diffusivity || !q->T1_ms || !q->T2_ms || !q->pXY)
+        return fail(SW_ERR_INVALID, "tissue tables missing");
+    if (q->n_RF == 0 || !q->RF_FA_deg || !q->RF_PH_deg || !q->RF_us)
+        return fail(SW_ERR_INVALID, "at least one RF pulse (RF_T = 0) is required");
+    if (q->n_TE > 0xffff || q->n_RF > 0xffff || q->n_dephasing > 0xffff || q->n_gradient > 0xffff)
+        return fail(SW_ERR_INVALID, "event tables longer than the 16-bit counters of the reference");
+    if (q->n_TE && !q->TE_us) return fail(SW_ERR_INVALID, "TE table");
+    if (q->n_dephasing && (!q->dephasing_us || !q->dephasing_deg))
+        return fail(SW_ERR_INVALID, "dephasing table");
+    if (q->n_gradient &&
+        (!q->gradient_us || !q->gradientX_mTm || !q->gradientY_mTm || !q->gradientZ_mTm))
+        return fail(SW_ERR_INVALID, "gradient table");
+    if (p->n_dummy_scan < 0) return fail(SW_ERR_INVALID, "n_dummy_scan < 0 (call sw_prepare_params)");
+    if (p->timestep_us <= 0) return fail(SW_ERR_INVALID, "timestep_us");
+    const int64_t ml = (int64_t)(p->phantom_size[0] * p->phantom_size[1] * p->phantom_size[2]);
+    if (ml <= 0 || ml != p->matrix_length) return fail(SW_ERR_INVALID, "matrix_length != Nx*Ny*Nz");
+    for (int i = 0; i < 3; i++)
+        if (!(p->fov[i] > 0)) return fail(SW_ERR_INVALID, "fov must be positive");
+    return SW_OK;
+}
+
+sw::DevParams dev_params(const sw_params *p, const sw_sequence *q) {
+    sw::DevParams d{};
+    for (int i = 0; i < 3; i++) {
+        d.fov[i] = p->fov[i];
+        d.s2g[i] = (double)p->phantom_size[i] / p->fov[i];       // kernels.cu:98
+    }
+    d.nz = (int64_t)p->phantom_size[2];
+    d.nynz = (int64_t)p->phantom_size[1] * (int64_t)p->phantom_size[2];
+    d.matrix_length = p->matrix_length;
+    d.seed = p->seed;
+    d.max_iterations = p->max_iterations;
+    d.n_spins = p->n_spins;
+    d.n_timepoints = p->n_timepoints;
+    d.n_substrate = p->n_substrate;
+    d.n_dummy_scan = (uint32_t)p->n_dummy_scan;
+    d.n_TE = q->n_TE;
+    d.n_RF = q->n_RF;
+    d.n_dephasing = q->n_dephasing;
+    d.n_gradient = q->n_gradient;
+    d.timestep_us = p->timestep_us;
+    d.cross_fov = p->enCrossFOV ? 1 : 0;
+    d.record_traj = p->enRecordTrajectory ? 1 : 0;
+    d.fieldmap_exist = p->fieldmap_exist ? 1 : 0;
+    d.traj_len = p->enRecordTrajectory
+                     ? (uint64_t)(p->n_dummy_scan + 1) * (uint64_t)p->n_timepoints : 1;
+    return d;
+}
+
+// Host image of the small tables, laid out exactly like the device copy.
+struct TableImage {
+    std::vector<char> bytes;
+    size_t o_dscale, o_T1f, o_T2f, o_T1d, o_T2d, o_pXY, o_rf, o_scan, o_te, o_dtp, o_ddeg, o_gtp,
+        o_gx, o_gy, o_gz;
+    template <typename T>
+    size_t put(const T *src, size_t n) {
+        size_t off = (bytes.size() + 15) & ~size_t(15);
+        bytes.resize(off + std::max<size_t>(1, n) * sizeof(T));
+        if (n) std::memcpy(bytes.data() + off, src, n * sizeof(T));
+        return off;
+    }
+};
+
+void build_tables(const sw_params *p, const sw_sequence *q, TableImage &im) {
+    const uint32_t ns = p->n_substrate;
+    std::vector<float> T1f(ns), T2f(ns);
+    std::vector<double> T1d(ns), T2d(ns);
+    for (uint32_t i = 0; i < ns; i++) {
+        T1f[i] = q->T1_ms[i] * 1e-3;          // kernels.cu:167-168 (float * double -> float)
+        T2f[i] = q->T2_ms[i] * 1e-3;
+        T1d[i] = q->T1_ms[i] * 1e-3;
+        T2d[i] = q->T2_ms[i] * 1e-3;
+    }
+    std::vector<sw::RfOp> rf, scan;
+    sw::build_rf(p, q, rf);
+    sw::build_scan_rf(p, q, scan);
+    im.o_dscale = im.put(q->diffusivity, ns);
+    im.o_T1f = im.put(T1f.data(), ns);
+    im.o_T2f = im.put(T2f.data(), ns);
+    im.o_T1d = im.put(T1d.data(), ns);
+    im.o_T2d = im.put(T2d.data(), ns);
+    im.o_pXY = im.put(q->pXY, (size_t)ns * ns);
+    im.o_rf = im.put(rf.data(), rf.size());
+    im.o_scan = im.put(scan.data(), scan.size());
+    im.o_te = im.put(q->TE_us, q->n_TE);
+    im.o_dtp = im.put(q->dephasing_us, q->n_dephasing);
+    im.o_ddeg = im.put(q->dephasing_deg, q->n_dephasing);
+    im.o_gtp = im.put(q->gradient_us, q->n_gradient);
+    im.o_gx = im.put(q->gradientX_mTm, q->n_gradient);
+    im.o_gy = im.put(q->gradientY_mTm, q->n_gradient);
+    im.o_gz = im.put(q->gradientZ_mTm, q->n_gradient);
+}
+
+sw::DevTables dev_tables(const TableImage &im, const char *d) {
+    sw::DevTables t{};
+    t.dscale = reinterpret_cast<const double *>(d + im.o_dscale);
+    t.T1f = reinterpret_cast<const float *>(d + im.o_T1f);
+    t.T2f = reinterpret_cast<const float *>(d + im.o_T2f);
+    t.T1d = reinterpret_cast<const double *>(d + im.o_T1d);
+    t.T2d = reinterpret_cast<const double *>(d + im.o_T2d);
+    t.pXY = reinterpret_cast<const float *>(d + im.o_pXY);
+    t.rf = reinterpret_cast<const sw::RfOp *>(d + im.o_rf);
+    t.scan_rf = reinterpret_cast<const sw::RfOp *>(d + im.o_scan);
+    t.te_tp = reinterpret_cast<const int32_t *>(d + im.o_te);
+    t.dph_tp = reinterpret_cast<const int32_t *>(d + im.o_dtp);
+    t.dph_deg = reinterpret_cast<const float *>(d + im.o_ddeg);
+    t.grad_tp = reinterpret_cast<const int32_t *>(d + im.o_gtp);
+    t.gx = reinterpret_cast<const float *>(d + im.o_gx);
+    t.gy = reinterpret_cast<const float *>(d + im.o_gy);
+    t.gz = reinterpret_cast<const float *>(d + im.o_gz);
+    return t;
+}
+
+// Lays out the whole workspace; with base == nullptr it only measures.
+struct Layout {
+    uint2 *vox;
+    char *tables;
+    uint32_t *active;
+    sw::SpinState S;
+    sw::RngState G;
+    size_t bytes;
+};
+
+Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl) {
+    Carve c{base};
+    Layout L{};
+    L.vox = c.take<uint2>(ml);
+    L.tables = c.take<char>(table_bytes);
+    L.active = c.take<uint32_t>(4);
+    sw::SpinState &S = L.S;
+    S.x = c.take<double>(n);
+    S.y = c.take<double>(n);
+    S.z = c.take<double>(n);
+    S.mx = c.take<float>(n);
+    S.my = c.take<float>(n);
+    S.mz = c.take<float>(n);
+    S.acc = c.take<float>(n);
+    S.acc_e = c.take<float>(n);
+    S.accd = c.take<double>(dbl ? n : 1);
+    S.dmx = c.take<double>(dbl ? n : 1);
+    S.dmy = c.take<double>(dbl ? n : 1);
+    S.dmz = c.take<double>(dbl ? n : 1);
+    S.field = c.take<float>(n);
+    S.ind_old = c.take<int64_t>(n);
+    S.tp = c.take<uint32_t>(n);
+    S.tp_old = c.take<uint32_t>(n);
+    S.ds = c.take<uint32_t>(n);
+    S.itr = c.take<uint32_t>(n);
+    S.ctr = c.take<uint32_t>(n);
+    S.ctr2 = c.take<uint32_t>(n);
+    S.flags = c.take<uint32_t>(n);
+    sw::RngState &G = L.G;
+    G.mt_r = c.take<uint32_t>(n * sw::kMtN);
+    G.mt_u = c.take<uint32_t>(n * sw::kMtN);
+    G.p_r = c.take<uint32_t>(n);
+    G.p_u = c.take<uint32_t>(n);
+    G.nbuf = c.take<float>(n * sw::kNormBuf);
+    G.nhead = c.take<uint32_t>(n);
+    G.ncnt = c.take<uint32_t>(n);
+    G.ubuf = c.take<float>(n * sw::kUnifBuf);
+    G.uhead = c.take<uint32_t>(n);
+    G.ucnt = c.take<uint32_t>(n);
+    L.bytes = c.off + 256;
+    return L;
+}
+
+int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const float *d_field,
+               const uint8_t *d_mask, const float *d_M0, const float *d_XYZ0, float *d_M1,
+               float *d_XYZ1, uint8_t *d_T, int32_t *d_status, int precision, double *d_M1d,
+               cudaStream_t st) {
+    g_timing = sw_timing{};
+    const size_t n = p->n_spins;
+    if (n == 0) return SW_OK;
+    if (precision != SW_PREC_FP32 && precision != SW_PREC_FP64 && precision != SW_PREC_KAHAN)
+        return fail(SW_ERR_INVALID, "precision");
+    int rc = ensure_logf(ctx);
+    if (rc) return rc;
+    const bool dbl = precision == SW_PREC_FP64 || d_M1d != nullptr;
+
+    TableImage im;
+    build_tables(p, q, im);
+    Layout L = layout(nullptr, n, p->matrix_length, im.bytes.size(), dbl);
+    if (L.bytes > ctx.ws_size) {
+        if (ctx.ws) {
+            SW_CUDA(cudaStreamSynchronize(st));
+            cudaFree(ctx.ws);
+            ctx.ws = nullptr;
+            ctx.ws_size = 0;
+        }
+        cudaError_t e = cudaMalloc(&ctx.ws, L.bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SW_ERR_NOMEM, "workspace of " + std::to_string(L.bytes >> 20) +
+                                          " MiB: " + cudaGetErrorString(e));
+        }
+        ctx.ws_size = L.bytes;
+    }
+    L = layout(ctx.ws, n, p->matrix_length, im.bytes.size(), dbl);
+    SW_CUDA(cudaMemcpyAsync(L.tables, im.bytes.data(), im.bytes.size(), cudaMemcpyHostToDevice, st));
+
+    const sw::DevParams P = dev_params(p, q);
+    const sw::DevTables Tb = dev_tables(im, L.tables);
+    const sw::LogfTables LT = logf_tables(ctx);
+    sw::Outputs O{d_M1, d_M1d, d_XYZ1, d_T, d_status};
+    cudaEvent_t *ev = ctx.ev.data();
+    uint32_t launches = 0;
+
+    SW_CUDA(cudaEventRecord(ev[0], st));
+    SW_CUDA(cudaMemsetAsync(L.active, 0, 2 * sizeof(uint32_t), st));
+    SW_CUDA(sw::launch_pack(d_mask, p->fieldmap_exist ? d_field : nullptr, L.vox,
+                            p->matrix_length, p->n_substrate, L.active + 1, st));
+    SW_CUDA(sw::launch_seed(P, L.G, st));
+    SW_CUDA(sw::launch_init(P, Tb, L.vox, d_M0, d_XYZ0, L.S, O, dbl, st));
+    launches += 3;
+    SW_CUDA(cudaEventRecord(ev[1], st));
+    SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    SW_CUDA(cudaStreamSynchronize(st));
+    if (*ctx.h_active != 0)
+        return fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate");
+
+    // Upper bound on rounds: every round advances each unfinished spin by >= 1 attempt.
+    const uint64_t steps = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
+    const uint64_t max_rounds = 64 + steps * (p->max_iterations + 2);
+    uint32_t chunk = 0;
+    for (;; chunk++) {
+        if (chunk >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
+        const bool timed = chunk < kMaxTimedChunks;
+        SW_CUDA(cudaMemsetAsync(L.active, 0, sizeof(uint32_t), st));
+        if (timed) SW_CUDA(cudaEventRecord(ev[4 + 2 * chunk], st));
+        SW_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
+        if (timed) SW_CUDA(cudaEventRecord(ev[5 + 2 * chunk], st));
+        SW_CUDA(sw::launch_walk(precision, dbl, P, Tb, L.vox, L.S, L.G, O, L.active, st));
+        launches += 2;
+        SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        if (timed) SW_CUDA(cudaEventRecord(ev[2], st));
+        SW_CUDA(cudaStreamSynchronize(st));
+        if (timed) {
+            float a = 0.f, b = 0.f;
+            cudaEventElapsedTime(&a, ev[4 + 2 * chunk], ev[5 + 2 * chunk]);
+            cudaEventElapsedTime(&b, ev[5 + 2 * chunk], ev[2]);
+            g_timing.refill_ms += a;
+            g_timing.walk_ms += b;
+        }
+        if (*ctx.h_active == 0) break;
+    }
+    SW_CUDA(cudaEventRecord(ev[3], st));
+    SW_CUDA(cudaEventSynchronize(ev[3]));
+    cudaEventElapsedTime(&g_timing.seed_ms, ev[0], ev[1]);
+    cudaEventElapsedTime(&g_timing.total_ms, ev[0], ev[3]);
+    g_timing.n_chunks = chunk + 1;
+    g_timing.n_launches = launches;
+    return SW_OK;
+}
+
+DeviceCtx *current_ctx(int *dev_out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+    if (dev_out) *dev_out = dev;
+    return &g_ctx[dev];
+}
+
+}  // namespace
+
+extern "C" {
+
+int sw_abi_version(void) { return SW_ABI_VERSION; }
+
+const char *sw_last_error(void) { return g_err.c_str(); }
+
+int sw_device_count(int *count) {
+    if (!count) return SW_ERR_INVALID;
+    cudaError_t e = cudaGetDeviceCount(count);
+    if (e != cudaSuccess) {
+        *count = 0;
+        cudaGetLastError();
+        return fail(SW_ERR_CUDA, cudaGetErrorString(e));
+    }
+    return SW_OK;
+}
+
+int sw_sync(void *stream) {
+    SW_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return SW_OK;
+}
+
+int sw_last_timing(sw_timing *out) {
+    if (!out) return SW_ERR_INVALID;
+    *out = g_timing;
+    return SW_OK;
+}
+
+int sw_sim_device(const sw_params *param, const sw_sequence *seq, const float *d_FieldMap,
+                  const uint8_t *d_Mask, const float *d_M0, const float *d_XYZ0, float *d_M1,
+                  float *d_XYZ1, uint8_t *d_T, int32_t *d_status, int precision,
+                  double *d_M1_fp64, void *stream) {
+    int rc = check_args(param, seq);
+    if (rc) return rc;
+    if (param->n_spins && (!d_Mask || !d_M0 || !d_XYZ0 || !d_XYZ1 || (seq->n_TE && (!d_M1 || !d_T))))
+        return fail(SW_ERR_INVALID, "null device buffer");
+    DeviceCtx *ctx = current_ctx(nullptr);
+    if (!ctx) return fail(SW_ERR_CUDA, "no current CUDA device");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return run_device(*ctx, param, seq, d_FieldMap, d_Mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T,
+                      d_status, precision, d_M1_fp64, (cudaStream_t)stream);
+}
+
+int sw_sim(const sw_params *param, const sw_sequence *seq, const float *pFieldMap,
+           const uint8_t *pMask, const float *M0, const float *XYZ0, float *M1, float *XYZ1,
+           uint8_t *T, int32_t *status, int precision, double *M1_fp64) {
+    int rc = check_args(param, seq);
+    if (rc) return rc;
+    const size_t n = param->n_spins;
+    if (n == 0) return SW_OK;
+    if (!pMask || !M0 || !XYZ0 || !XYZ1 || (seq->n_TE && (!M1 || !T)))
+        return fail(SW_ERR_INVALID, "null host buffer");
+    const size_t ml = (size_t)param->matrix_length, nte = seq->n_TE;
+    const size_t trj = param->enRecordTrajectory
+                           ? (size_t)(param->n_dummy_scan + 1) * param->n_timepoints : 1;
+    const bool has_field = param->fieldmap_exist && pFieldMap;
+    // one device allocation for all user-visible buffers
+    size_t off = 0;
+    auto slot = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~size_t(255); return o; };
+    const size_t o_mask = slot(ml), o_field = slot(has_field ? ml * 4 : 0), o_M0 = slot(n * 12),
+                 o_XYZ0 = slot(n * 12), o_M1 = slot(n * nte * 12), o_XYZ1 = slot(n * trj * 12),
+                 o_T = slot(n * nte), o_st = slot(status ? n * 4 : 0),
+                 o_M1d = slot(M1_fp64 ? n * nte * 24 : 0);
+    char *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, off + 256);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SW_ERR_NOMEM, std::string("buffers: ") + cudaGetErrorString(e));
+    }
+    auto done = [&](int code) { cudaFree(d); return code; };
+    cudaStream_t st = nullptr;
+#define SW_TRY(call)                                                                       \
+    do {                                                                                   \
+        cudaError_t e2 = (call);                                                           \
+        if (e2 != cudaSuccess)                                                             \
+            return done(fail(SW_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e2))); \
+    } while (0)
+    SW_TRY(cudaMemcpyAsync(d + o_mask, pMask, ml, cudaMemcpyHostToDevice, st));
+    if (has_field) SW_TRY(cudaMemcpyAsync(d + o_field, pFieldMap, ml * 4, cudaMemcpyHostToDevice, st));
+    SW_TRY(cudaMemcpyAsync(d + o_M0, M0, n * 12, cudaMemcpyHostToDevice, st));
+    SW_TRY(cudaMemcpyAsync(d + o_XYZ0, XYZ0, n * 12, cudaMemcpyHostToDevice, st));
+    // outputs start from the caller's contents: slots the walk never reaches keep them, as in
+    // the reference (whose GPU path uploads M1/XYZ1/T too, monte_carlo.cu:256-260)
+    if (nte) {
+        SW_TRY(cudaMemcpyAsync(d + o_M1, M1, n * nte * 12, cudaMemcpyHostToDevice, st));
+        SW_TRY(cudaMemcpyAsync(d + o_T, T, n * nte, cudaMemcpyHostToDevice, st));
+    }
+    SW_TRY(cudaMemcpyAsync(d + o_XYZ1, XYZ1, n * trj * 12, cudaMemcpyHostToDevice, st));
+    if (M1_fp64) SW_TRY(cudaMemcpyAsync(d + o_M1d, M1_fp64, n * nte * 24, cudaMemcpyHostToDevice, st));
+    DeviceCtx *ctx = current_ctx(nullptr);
+    if (!ctx) return done(fail(SW_ERR_CUDA, "no current CUDA device"));
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        int rc2 = run_device(*ctx, param, seq, has_field ? (float *)(d + o_field) : nullptr,
+                             (uint8_t *)(d + o_mask), (float *)(d + o_M0), (float *)(d + o_XYZ0),
+                             (float *)(d + o_M1), (float *)(d + o_XYZ1), (uint8_t *)(d + o_T),
+                             status ? (int32_t *)(d + o_st) : nullptr, precision,
+                             M1_fp64 ? (double *)(d + o_M1d) : nullptr, st);
+        if (rc2) return done(rc2);
+    }
+    if (nte) {
+        SW_TRY(cudaMemcpyAsync(M1, d + o_M1, n * nte * 12, cudaMemcpyDeviceToHost, st));
+        SW_TRY(cudaMemcpyAsync(T, d + o_T, n * nte, cudaMemcpyDeviceToHost, st));
+    }
+    SW_TRY(cudaMemcpyAsync(XYZ1, d + o_XYZ1, n * trj * 12, cudaMemcpyDeviceToHost, st));
+    if (status) SW_TRY(cudaMemcpyAsync(status, d + o_st, n * 4, cudaMemcpyDeviceToHost, st));
+    if (M1_fp64) SW_TRY(cudaMemcpyAsync(M1_fp64, d + o_M1d, n * nte * 24, cudaMemcpyDeviceToHost, st));
+    SW_TRY(cudaStreamSynchronize(st));
+#undef SW_TRY
+    return done(SW_OK);
+}
+
+int sw_debug_logf(const float *d_x, float *d_y, uint64_t n, void *stream) {
+    DeviceCtx *ctx = current_ctx(nullptr);
+    if (!ctx) return fail(SW_ERR_CUDA, "no current CUDA device");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    int rc = ensure_logf(*ctx);
+    if (rc) return rc;
+    SW_CUDA(sw::launch_debug_logf(d_x, d_y, n, logf_tables(*ctx), (cudaStream_t)stream));
+    return SW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,200 @@
+// Device-side building blocks of the SpinWalk `sim` hot path on GB300 (sm_103a).
+//
+// The translation units that include this header are compiled with -fmad=false: every float and
+// double expression rounds after each operation exactly like the reference's CPU build
+// (x86-64 SSE2, no contraction), so trajectories are bit-exact. The only fused multiply-adds
+// are the explicit ones inside logf_cand (sw_logf.h), which the host reproduces with fmaf.
+#pragma once
+#include <stdint.h>
+
+#include "sw_logf.h"
+#include "sw_types.h"
+
+namespace sw {
+
+// ------------------------------------------------------------------------------------------
+// MT19937 (the std::mt19937 parameters of the C++ standard)
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t mt_temper(uint32_t y) {
+    y ^= (y >> 11);
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= (y >> 18);
+    return y;
+}
+
+__device__ __forceinline__ uint32_t mt_twist1(uint32_t xi, uint32_t xi1, uint32_t xm) {
+    uint32_t y = (xi & 0x80000000u) | (xi1 & 0x7fffffffu);
+    return xm ^ (y >> 1) ^ ((xi1 & 1u) ? 0x9908b0dfu : 0u);
+}
+
+// One full regeneration of the 624-word state held in shared memory, by one warp. Same result
+// as the sequential in-place loop of mersenne_twister_engine::_M_gen_rand: words [0,227) read
+// only old words; [227,454) and [454,623) read words regenerated by the previous phase; word
+// 623 reads the new words 0 and 396.
+__device__ __forceinline__ void mt_twist_warp(uint32_t *s, int lane) {
+    uint32_t v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        int i = lane + 32 * k;
+        if (i < 227) v[k] = mt_twist1(s[i], s[i + 1], s[i + kMtM]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        int i = lane + 32 * k;
+        if (i < 227) s[i] = v[k];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        int i = 227 + lane + 32 * k;
+        if (i < 454) v[k] = mt_twist1(s[i], s[i + 1], s[i - 227]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        int i = 227 + lane + 32 * k;
+        if (i < 454) s[i] = v[k];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        int i = 454 + lane + 32 * k;
+        if (i < 623) v[k] = mt_twist1(s[i], s[i + 1], s[i - 227]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        int i = 454 + lane + 32 * k;
+        if (i < 623) s[i] = v[k];
+    }
+    __syncwarp();
+    if (lane == 0) s[623] = mt_twist1(s[623], s[0], s[396]);
+    __syncwarp();
+}
+
+// generate_canonical<float, 24>(mt19937): float(w) / 2^32, clamped below 1
+// (libstdc++ bits/random.tcc, generate_canonical).
+__device__ __forceinline__ float canon24(uint32_t w) {
+    float f = __fmul_rn(__uint2float_rn(w), 2.3283064365386963e-10f);  // exact: * 2^-32
+    return f >= 1.0f ? 0x1.fffffep-1f : f;
+}
+
+// The host libm's logf, bit for bit, on [2^-48, 1] (sw_logf.h).
+__device__ __forceinline__ float logf_libm(float x, const float *s_tab, const LogfTables &L) {
+    float c = swlogf::logf_cand(x, s_tab);
+    const uint32_t bits = __float_as_uint(x);
+    const uint32_t b = (bits - swlogf::kDomainLo) >> swlogf::kBucketShift;
+    uint32_t lo = __ldg(L.off + b), hi = __ldg(L.off + b + 1);
+    for (uint32_t i = lo; i < hi; i++) {
+        uint32_t e = __ldg(L.ent + i);
+        if ((e >> 1) == bits) {
+            c = __uint_as_float(__float_as_uint(c) + ((e & 1u) ? 1u : 0xffffffffu));
+            break;
+        }
+    }
+    return c;
+}
+
+// ------------------------------------------------------------------------------------------
+// Bloch primitives, float path (src/sim/kernels.cuh:82-230, kernels.cu:45-52)
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void xrot_f(float s, float c, const float *a, float *b) {
+    b[0] = a[0];
+    b[1] = c * a[1] - s * a[2];
+    b[2] = s * a[1] + c * a[2];
+}
+__device__ __forceinline__ void yrot_f(float s, float c, const float *a, float *b) {
+    b[0] = c * a[0] + s * a[2];
+    b[1] = a[1];
+    b[2] = -s * a[0] + c * a[2];
+}
+__device__ __forceinline__ void zrot_f(float s, float c, const float *a, float *b) {
+    b[0] = c * a[0] - s * a[1];
+    b[1] = s * a[0] + c * a[1];
+    b[2] = a[2];
+}
+__device__ __forceinline__ void rf_f(const RfOp &op, const float *a, float *b) {
+    switch (op.kind) {
+        case 0: xrot_f(op.s, op.c, a, b); break;
+        case 1: xrot_f(-op.s, op.c, a, b); break;
+        case 2: yrot_f(op.s, op.c, a, b); break;
+        case 3: yrot_f(-op.s, op.c, a, b); break;
+        default: {
+            float t[3];
+            zrot_f(-op.sp, op.cp, a, b);
+            xrot_f(op.s, op.c, b, t);
+            zrot_f(op.sp, op.cp, t, b);
+        }
+    }
+}
+// dephase_relax: zrot by the accumulated phase (degrees), then T1/T2 relaxation with the
+// double exp of the reference and relax()'s double constant 1.
+__device__ __forceinline__ void dephase_relax_f(const float *a, float *b, float phase, float T1,
+                                                float T2, float dt_s) {
+    float ang = (float)((double)phase * kDeg2Rad);
+    float s, c;
+    sincosf(ang, &s, &c);
+    zrot_f(s, c, a, b);
+    if (T1 >= 0 && T2 >= 0) {
+        float e1 = (float)exp((double)(-dt_s / T1));
+        float e2 = (float)exp((double)(-dt_s / T2));
+        b[0] = b[0] * e2;
+        b[1] = b[1] * e2;
+        b[2] = (float)(1. + (double)e1 * ((double)b[2] - 1.));
+    }
+}
+
+// ---- FP64 path ----------------------------------------------------------------------------
+__device__ __forceinline__ void xrot_d(double s, double c, const double *a, double *b) {
+    b[0] = a[0];
+    b[1] = c * a[1] - s * a[2];
+    b[2] = s * a[1] + c * a[2];
+}
+__device__ __forceinline__ void yrot_d(double s, double c, const double *a, double *b) {
+    b[0] = c * a[0] + s * a[2];
+    b[1] = a[1];
+    b[2] = -s * a[0] + c * a[2];
+}
+__device__ __forceinline__ void zrot_d(double s, double c, const double *a, double *b) {
+    b[0] = c * a[0] - s * a[1];
+    b[1] = s * a[0] + c * a[1];
+    b[2] = a[2];
+}
+__device__ __forceinline__ void rf_d(const RfOp &op, const double *a, double *b) {
+    switch (op.kind) {
+        case 0: xrot_d(op.sd, op.cd, a, b); break;
+        case 1: xrot_d(-op.sd, op.cd, a, b); break;
+        case 2: yrot_d(op.sd, op.cd, a, b); break;
+        case 3: yrot_d(-op.sd, op.cd, a, b); break;
+        default: {
+            double t[3];
+            zrot_d(-op.spd, op.cpd, a, b);
+            xrot_d(op.sd, op.cd, b, t);
+            zrot_d(op.spd, op.cpd, t, b);
+        }
+    }
+}
+__device__ __forceinline__ void dephase_relax_d(const double *a, double *b, double phase,
+                                                double T1, double T2, double dt_s) {
+    double s, c;
+    sincos(phase * kDeg2Rad, &s, &c);
+    zrot_d(s, c, a, b);
+    if (T1 >= 0 && T2 >= 0) {
+        double e1 = exp(-dt_s / T1), e2 = exp(-dt_s / T2);
+        b[0] *= e2;
+        b[1] *= e2;
+        b[2] = 1. + e1 * (b[2] - 1.);
+    }
+}
+
+// Compensated float accumulation (Knuth two-sum), value = s + e.
+__device__ __forceinline__ void kahan_add(float &s, float &e, float x) {
+    float t = s + x;
+    float bp = t - s;
+    e += (s - (t - bp)) + (x - bp);
+    s = t;
+}
+
+}  // namespace sw

@@ -1,0 +1,571 @@
+// CUDA kernels of the SpinWalk `sim` hot path for GB300 (sm_103a).
+//
+// The reference runs one thread per spin that seeds two std::mt19937, draws Gaussian steps and
+// walks all time points in one go (cu_sim / sim::sim, src/sim/kernels.cu:57-233). Here the
+// same per-spin computation is split so that each part runs in the shape the GPU likes:
+//
+//   k_pack    : mask + fieldmap -> one 8-byte record per voxel (one gather per step)
+//   k_seed    : one WARP per spin: mt19937(seed+spin) + discard(seed+spin), the twist done by
+//               32 lanes on a shared-memory copy of the 624-word state
+//   k_init    : one thread per spin: initial voxel, substrate and state (kernels.cu:90-104)
+//   k_refill  : one WARP per spin: tops up the spin's ring buffers of Gaussian deviates
+//               (libstdc++ polar method, 32 candidate pairs per pass, accepted pairs compacted
+//               with a ballot) and crossing uniforms, twisting the state when a block runs out
+//   k_walk    : one thread per spin: walk + mask/permeability + field + Bloch events until the
+//               spin's buffers run low, then saves its state (kernels.cu:107-232)
+//
+// k_refill and k_walk alternate until every spin has finished. All kernels are compiled with
+// -fmad=false (see sw_device.cuh).
+#include <cuda_runtime.h>
+
+#include "sw_device.cuh"
+#include "sw_kernels.h"
+#include "spinwalk_gpu.h"
+
+namespace sw {
+
+// ------------------------------------------------------------------------------------------
+// Also flags substrate labels >= n_substrate (the reference's driver refuses such a mask,
+// src/sim/monte_carlo.cu:113-118); the host checks the flag before any walk reads the tables.
+__global__ void k_pack(const uint8_t *__restrict__ mask, const float *__restrict__ field,
+                       uint2 *__restrict__ out, int64_t n, uint32_t n_substrate,
+                       uint32_t *__restrict__ bad_label) {
+    bool bad = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t f = field ? __float_as_uint(field[i]) : 0u;
+        const uint32_t m = mask[i];
+        bad |= m >= n_substrate;
+        out[i] = make_uint2(f, m);
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(bad_label, 1u);
+}
+
+// ------------------------------------------------------------------------------------------
+// Seeding: std::mt19937 gen(seed + spin); gen.discard(seed + spin)   (kernels.cu:82-88)
+// ------------------------------------------------------------------------------------------
+constexpr int kSeedWarps = 4;
+
+__global__ void __launch_bounds__(32 * kSeedWarps) k_seed(DevParams P, RngState G) {
+    __shared__ uint32_t s_mt[kSeedWarps][kMtN];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t *s = s_mt[w];
+    for (uint32_t idx = blockIdx.x * kSeedWarps + w; idx < P.n_spins;
+         idx += gridDim.x * kSeedWarps) {
+        const uint32_t spin = P.n_spins - 1 - idx;   // most expensive (largest discard) first
+        const uint64_t sd = P.seed + spin;
+        if (lane == 0) {                             // mersenne_twister_engine::seed
+            uint32_t x = (uint32_t)sd;
+            s[0] = x;
+            for (uint32_t i = 1; i < kMtN; i++) {
+                x = 1812433253u * (x ^ (x >> 30)) + i;
+                s[i] = x;
+            }
+        }
+        __syncwarp();
+        // mersenne_twister_engine::discard: while (z > n - p) { z -= n - p; twist; p = 0; }
+        uint64_t z = sd;
+        uint32_t p = kMtN;
+        while (z > (uint64_t)(kMtN - p)) {
+            z -= kMtN - p;
+            mt_twist_warp(s, lane);
+            p = 0;
+        }
+        p += (uint32_t)z;
+        uint32_t *gr = G.mt_r + (size_t)spin * kMtN, *gu = G.mt_u + (size_t)spin * kMtN;
+        for (int i = lane; i < kMtN; i += 32) {
+            gr[i] = s[i];
+            gu[i] = s[i];
+        }
+        if (lane == 0) {
+            G.p_r[spin] = p;
+            G.p_u[spin] = p;
+            G.nhead[spin] = 0;
+            G.ncnt[spin] = 0;
+            G.uhead[spin] = 0;
+            G.ucnt[spin] = 0;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Initial state (kernels.cu:90-104)
+// ------------------------------------------------------------------------------------------
+__global__ void k_init(DevParams P, DevTables Tb, const uint2 *__restrict__ vox,
+                       const float *__restrict__ M0, const float *__restrict__ XYZ0,
+                       SpinState S, Outputs O, int fp64_state) {
+    const uint32_t spin = blockIdx.x * blockDim.x + threadIdx.x;
+    if (spin >= P.n_spins) return;
+    float p0[3], m[3];
+    for (int i = 0; i < 3; i++) {
+        p0[i] = XYZ0[3 * (size_t)spin + i];
+        m[i] = M0[3 * (size_t)spin + i];
+    }
+    float *xyz1 = O.XYZ1 + 3 * (size_t)spin * P.traj_len;
+    for (int i = 0; i < 3; i++) xyz1[i] = p0[i];                   // kernels.cu:96
+    S.x[spin] = p0[0];
+    S.y[spin] = p0[1];
+    S.z[spin] = p0[2];
+    S.mx[spin] = m[0];
+    S.my[spin] = m[1];
+    S.mz[spin] = m[2];
+    S.acc[spin] = 0.f;
+    S.acc_e[spin] = 0.f;
+    if (fp64_state) {
+        S.accd[spin] = 0.;
+        S.dmx[spin] = m[0];
+        S.dmy[spin] = m[1];
+        S.dmz[spin] = m[2];
+    }
+    S.field[spin] = 0.f;
+    S.ind_old[spin] = P.matrix_length + 1;
+    S.tp[spin] = 0;
+    S.tp_old[spin] = 0;
+    S.ds[spin] = 0;
+    S.itr[spin] = 0;
+    S.ctr[spin] = 1;
+    S.ctr2[spin] = 0;
+    const int64_t i0 = (int64_t)((double)p0[0] * P.s2g[0]) * P.nynz +
+                       (int64_t)((double)p0[1] * P.s2g[1]) * P.nz +
+                       (int64_t)((double)p0[2] * P.s2g[2]);
+    if (i0 < 0 || i0 >= P.matrix_length) {
+        S.flags[spin] = kFlagDone | ((uint32_t)SW_SPIN_START_OOB << 16);
+        if (O.status) O.status[spin] = SW_SPIN_START_OOB;
+        return;
+    }
+    S.flags[spin] = vox[i0].y & 0xffu;                             // ts_old, not started
+}
+
+// ------------------------------------------------------------------------------------------
+// Generator refill
+// ------------------------------------------------------------------------------------------
+constexpr int kRefillWarps = 4;
+
+// Brings the spin's current 624-word block into shared memory (if it is not there yet),
+// regenerates it, and writes it back.
+__device__ __forceinline__ void twist_block(uint32_t *gst, uint32_t *s, bool &in_smem, int lane) {
+    if (!in_smem)
+        for (int i = lane; i < kMtN; i += 32) s[i] = gst[i];
+    __syncwarp();
+    mt_twist_warp(s, lane);
+    for (int i = lane; i < kMtN; i += 32) gst[i] = s[i];
+    in_smem = true;
+    __syncwarp();
+}
+
+__device__ __forceinline__ uint32_t block_word(const uint32_t *gst, const uint32_t *s,
+                                               bool in_smem, uint32_t i) {
+    return in_smem ? s[i] : gst[i];
+}
+
+__global__ void __launch_bounds__(32 * kRefillWarps)
+    k_refill(DevParams P, RngState G, const uint32_t *__restrict__ flags, LogfTables L) {
+    __shared__ float s_tab[192];
+    __shared__ uint32_t s_mt[kRefillWarps][kMtN];
+    for (int i = threadIdx.x; i < 192; i += blockDim.x) s_tab[i] = L.tab[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    uint32_t *s = s_mt[w];
+    for (uint32_t spin = blockIdx.x * kRefillWarps + w; spin < P.n_spins;
+         spin += gridDim.x * kRefillWarps) {
+        if (flags[spin] & kFlagDone) continue;
+        // ---- Gaussian deviates from gen_r (normal_distribution<float>, polar method) ----
+        const uint32_t nc = G.ncnt[spin];
+        const uint32_t K = (kNormBuf - nc) / 2;                 // pairs to add
+        if (K > 0) {
+            uint32_t *gst = G.mt_r + (size_t)spin * kMtN;
+            float *nb = G.nbuf + (size_t)spin * kNormBuf;
+            const uint32_t wpos = G.nhead[spin] + nc;
+            uint32_t p = G.p_r[spin];
+            uint32_t produced = 0;
+            bool in_smem = false;
+            while (produced < K) {
+                if (p >= (uint32_t)kMtN) {
+                    twist_block(gst, s, in_smem, lane);
+                    p = 0;
+                }
+                uint32_t w0 = 0, w1 = 0;
+                uint32_t npairs;
+                bool straddle = false;
+                if (kMtN - p == 1) {            // pair = last word of this block + first of next
+                    w0 = block_word(gst, s, in_smem, kMtN - 1);
+                    twist_block(gst, s, in_smem, lane);
+                    w1 = s[0];
+                    npairs = 1;
+                    straddle = true;
+                } else {
+                    npairs = min(32u, (kMtN - p) / 2);
+                    if ((uint32_t)lane < npairs) {
+                        w0 = block_word(gst, s, in_smem, p + 2 * lane);
+                        w1 = block_word(gst, s, in_smem, p + 2 * lane + 1);
+                    }
+                }
+                const bool valid = (uint32_t)lane < npairs;
+                const float u1 = canon24(mt_temper(w0)), u2 = canon24(mt_temper(w1));
+                const float x = 2.0f * u1 - 1.0f, y = 2.0f * u2 - 1.0f;
+                const float r2 = x * x + y * y;
+                const bool ok = valid && !(r2 > 1.0f || r2 == 0.0f);
+                const unsigned bal = __ballot_sync(0xffffffffu, ok);
+                const uint32_t rank = __popc(bal & lt_mask);
+                const uint32_t need = K - produced;
+                if (ok && rank < need) {
+                    const float lg = logf_libm(r2, s_tab, L);
+                    const float mult = __fsqrt_rn(__fdiv_rn(-2.0f * lg, r2));
+                    const uint32_t pos = (wpos + 2 * (produced + rank)) % kNormBuf;
+                    nb[pos] = y * mult;                          // returned first
+                    nb[(pos + 1) % kNormBuf] = x * mult;         // saved for the next call
+                }
+                const uint32_t nacc = __popc(bal);
+                if (nacc <= need) {
+                    produced += nacc;
+                    p = straddle ? 1 : p + 2 * npairs;
+                } else {
+                    const unsigned m2 = __ballot_sync(0xffffffffu, ok && rank == need - 1);
+                    const uint32_t last = __ffs(m2) - 1;
+                    produced = K;
+                    p = p + 2 * (last + 1);
+                }
+            }
+            if (lane == 0) {
+                G.p_r[spin] = p;
+                G.ncnt[spin] = nc + 2 * K;
+            }
+        }
+        // ---- crossing uniforms from gen_u (uniform_real_distribution<float>(0,1)) ----
+        const uint32_t uc = G.ucnt[spin];
+        if (uc <= kUnifBuf / 2) {
+            uint32_t *gst = G.mt_u + (size_t)spin * kMtN;
+            float *ub = G.ubuf + (size_t)spin * kUnifBuf;
+            const uint32_t wpos = G.uhead[spin] + uc;
+            const uint32_t need = kUnifBuf - uc;
+            uint32_t p = G.p_u[spin];
+            uint32_t produced = 0;
+            bool in_smem = false;
+            while (produced < need) {
+                if (p >= (uint32_t)kMtN) {
+                    twist_block(gst, s, in_smem, lane);
+                    p = 0;
+                }
+                const uint32_t n = min(min(32u, (uint32_t)kMtN - p), need - produced);
+                if ((uint32_t)lane < n) {
+                    const uint32_t wv = block_word(gst, s, in_smem, p + lane);
+                    ub[(wpos + produced + lane) % kUnifBuf] = canon24(mt_temper(wv));
+                }
+                p += n;
+                produced += n;
+            }
+            if (lane == 0) {
+                G.p_u[spin] = p;
+                G.ucnt[spin] = uc + need;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// The walk (kernels.cu:107-232)
+// ------------------------------------------------------------------------------------------
+template <int PREC, bool DBL>
+__device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, const DevParams &P,
+                                          const DevTables &Tb, const uint2 *__restrict__ vox,
+                                          const SpinState &S, const RngState &G,
+                                          const Outputs &O) {
+    constexpr bool KAHAN = PREC == SW_PREC_KAHAN;
+    double xo[3] = {S.x[spin], S.y[spin], S.z[spin]};
+    float m0[3] = {S.mx[spin], S.my[spin], S.mz[spin]}, m1[3];
+    float acc = S.acc[spin], acc_e = KAHAN ? S.acc_e[spin] : 0.f;
+    double accd = 0., d0[3] = {0., 0., 0.}, d1[3];
+    if (DBL) {
+        accd = S.accd[spin];
+        d0[0] = S.dmx[spin];
+        d0[1] = S.dmy[spin];
+        d0[2] = S.dmz[spin];
+    }
+    float field = S.field[spin];
+    int64_t ind_old = S.ind_old[spin];
+    uint32_t tp = S.tp[spin], tp_old = S.tp_old[spin], ds = S.ds[spin], itr = S.itr[spin];
+    uint32_t ctr = S.ctr[spin], ctr2 = S.ctr2[spin];
+    uint32_t c_rf = ctr & 0xffffu, c_te = ctr >> 16, c_dph = ctr2 & 0xffffu, c_grad = ctr2 >> 16;
+    uint32_t ts_old = flags & 0xffu;
+    bool started = (flags & kFlagStarted) != 0;
+    double dscale = __ldg(Tb.dscale + ts_old);
+
+    uint32_t nh = G.nhead[spin], nc = G.ncnt[spin], uh = G.uhead[spin], uc = G.ucnt[spin];
+    const float *nb = G.nbuf + (size_t)spin * kNormBuf;
+    const float *ub = G.ubuf + (size_t)spin * kUnifBuf;
+
+    constexpr uint32_t NONE = 0xffffffffu;
+    const bool last_scan0 = ds == P.n_dummy_scan;
+    uint32_t t_rf = c_rf < P.n_RF ? (uint32_t)Tb.rf[c_rf].tp : NONE;
+    uint32_t t_te = (last_scan0 && c_te < P.n_TE) ? (uint32_t)Tb.te_tp[c_te] : NONE;
+    uint32_t t_dph = c_dph < P.n_dephasing ? (uint32_t)Tb.dph_tp[c_dph] : NONE;
+    uint32_t t_grad = c_grad < P.n_gradient ? (uint32_t)Tb.grad_tp[c_grad] : NONE;
+
+    int status = -1;   // -1: paused (buffers ran low)
+    for (;;) {
+        if (!started) {
+            if (ds > P.n_dummy_scan) { status = SW_SPIN_OK; break; }
+            const RfOp op = Tb.scan_rf[ds];                         // kernels.cu:110-120
+            rf_f(op, m0, m1);
+            m0[0] = m1[0]; m0[1] = m1[1]; m0[2] = m1[2];
+            if (DBL) {
+                rf_d(op, d0, d1);
+                d0[0] = d1[0]; d0[1] = d1[1]; d0[2] = d1[2];
+            }
+            ind_old = P.matrix_length + 1;                          // kernels.cu:123-126
+            tp = tp_old = 0;
+            c_rf = 1; c_te = 0; c_dph = 0; c_grad = 0;
+            acc = 0.f; acc_e = 0.f; accd = 0.;
+            started = true;
+            t_rf = 1 < P.n_RF ? (uint32_t)Tb.rf[1].tp : NONE;
+            t_te = (ds == P.n_dummy_scan && P.n_TE > 0) ? (uint32_t)Tb.te_tp[0] : NONE;
+            t_dph = P.n_dephasing > 0 ? (uint32_t)Tb.dph_tp[0] : NONE;
+            t_grad = P.n_gradient > 0 ? (uint32_t)Tb.grad_tp[0] : NONE;
+        }
+        if (tp >= P.n_timepoints) {                                 // kernels.cu:225-231
+            const float te = (float)((double)((tp - tp_old) * (uint32_t)P.timestep_us) * 1e-6);
+            dephase_relax_f(m0, m1, KAHAN ? acc + acc_e : acc, __ldg(Tb.T1f + ts_old),
+                            __ldg(Tb.T2f + ts_old), te);
+            m0[0] = m1[0]; m0[1] = m1[1]; m0[2] = m1[2];
+            if (DBL) {
+                const double ted = (double)(tp - tp_old) * (double)P.timestep_us * 1e-6;
+                dephase_relax_d(d0, d1, accd, __ldg(Tb.T1d + ts_old), __ldg(Tb.T2d + ts_old), ted);
+                d0[0] = d1[0]; d0[1] = d1[1]; d0[2] = d1[2];
+            }
+            ds++;
+            started = false;
+            continue;
+        }
+        if ((dscale != 0. && nc < 3) || uc == 0) break;             // buffers low: pause
+
+        // ---- random walk + boundary (kernels.cu:130-137) ----
+        double xn[3] = {xo[0], xo[1], xo[2]};
+        if (dscale != 0.) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                const float g = nb[nh];
+                nh = (nh + 1 == kNormBuf) ? 0 : nh + 1;
+                const double rnd = (double)g * dscale;
+                double v = xo[i] + rnd;
+                if (v < 0)
+                    v += P.cross_fov ? P.fov[i] : 2 * fabs(rnd);
+                else if (v >= P.fov[i])
+                    v -= P.cross_fov ? P.fov[i] : 2 * fabs(rnd);
+                xn[i] = v;
+            }
+            nc -= 3;
+        }
+        // ---- voxel index (kernels.cu:140-147) ----
+        const int64_t ind = (int64_t)(xn[0] * P.s2g[0]) * P.nynz +
+                            (int64_t)(xn[1] * P.s2g[1]) * P.nz + (int64_t)(xn[2] * P.s2g[2]);
+        if (ind >= P.matrix_length || ind < 0) { status = SW_SPIN_OOB; break; }
+        // ---- mask, permeability, field (kernels.cu:150-170) ----
+        if (ind != ind_old) {
+            const uint2 v = __ldg(vox + ind);
+            const uint32_t ts = v.y;
+            if (ts != ts_old) {
+                const float u = ub[uh];
+                uh = (uh + 1 == kUnifBuf) ? 0 : uh + 1;
+                uc--;
+                if (u >= __ldg(Tb.pXY + ts_old * P.n_substrate + ts)) {
+                    if ((uint64_t)(itr++) > P.max_iterations) { status = SW_SPIN_LOST; break; }
+                    continue;
+                }
+                ts_old = ts;
+            }
+            ind_old = ind;
+            field = __uint_as_float(v.x);
+            dscale = __ldg(Tb.dscale + ts_old);
+        }
+        // ---- phase accumulation (kernels.cu:171-172) ----
+        if (KAHAN) kahan_add(acc, acc_e, field); else acc += field;
+        if (DBL) accd += (double)field;
+        itr = 0;
+        // ---- ideal dephasing (kernels.cu:175-178) ----
+        if (tp == t_dph) {
+            const float deg = __ldg(Tb.dph_deg + c_dph);
+            const float inc = (float)spin * deg / (float)P.n_spins;
+            if (KAHAN) kahan_add(acc, acc_e, inc); else acc += inc;
+            if (DBL) accd += (double)spin * (double)deg / (double)P.n_spins;
+            c_dph++;
+            t_dph = c_dph < P.n_dephasing ? (uint32_t)Tb.dph_tp[c_dph] : NONE;
+        }
+        // ---- gradient (kernels.cu:181-187) ----
+        if (tp == t_grad) {
+            const double g = ((double)__ldg(Tb.gx + c_grad) * xn[0] +
+                              (double)__ldg(Tb.gy + c_grad) * xn[1] +
+                              (double)__ldg(Tb.gz + c_grad) * xn[2]) *
+                             1e-3 * (double)P.timestep_us * 1e-6 * kGamma * kRad2Deg;
+            if (KAHAN) {
+                const float ghi = (float)g;
+                kahan_add(acc, acc_e, ghi);
+                kahan_add(acc, acc_e, (float)(g - (double)ghi));
+            } else {
+                acc = (float)((double)acc + g);
+            }
+            if (DBL) accd += g;
+            c_grad++;
+            t_grad = c_grad < P.n_gradient ? (uint32_t)Tb.grad_tp[c_grad] : NONE;
+        }
+        // ---- RF pulse (kernels.cu:190-199) ----
+        if (tp == t_rf) {
+            const float te = (float)((double)((tp - tp_old) * (uint32_t)P.timestep_us) * 1e-6);
+            dephase_relax_f(m0, m1, KAHAN ? acc + acc_e : acc, __ldg(Tb.T1f + ts_old),
+                            __ldg(Tb.T2f + ts_old), te);
+            const RfOp op = Tb.rf[c_rf];
+            rf_f(op, m1, m0);
+            if (DBL) {
+                const double ted = (double)(tp - tp_old) * (double)P.timestep_us * 1e-6;
+                dephase_relax_d(d0, d1, accd, __ldg(Tb.T1d + ts_old), __ldg(Tb.T2d + ts_old), ted);
+                rf_d(op, d1, d0);
+            }
+            acc = 0.f; acc_e = 0.f; accd = 0.;
+            tp_old = tp;
+            c_rf++;
+            t_rf = c_rf < P.n_RF ? (uint32_t)Tb.rf[c_rf].tp : NONE;
+        }
+        // ---- echo, last scan only (kernels.cu:202-215) ----
+        if (tp == t_te) {
+            const float te = (float)((double)((tp - tp_old) * (uint32_t)P.timestep_us) * 1e-6);
+            dephase_relax_f(m0, m1, KAHAN ? acc + acc_e : acc, __ldg(Tb.T1f + ts_old),
+                            __ldg(Tb.T2f + ts_old), te);
+            if (DBL) {
+                const double ted = (double)(tp - tp_old) * (double)P.timestep_us * 1e-6;
+                dephase_relax_d(d0, d1, accd, __ldg(Tb.T1d + ts_old), __ldg(Tb.T2d + ts_old), ted);
+                d0[0] = d1[0]; d0[1] = d1[1]; d0[2] = d1[2];
+            }
+            const size_t o = 3 * ((size_t)spin * P.n_TE + c_te);
+            for (int i = 0; i < 3; i++) {
+                m0[i] = m1[i];
+                O.M1[o + i] = (PREC == SW_PREC_FP64) ? (float)d1[i] : m1[i];
+                if (DBL && O.M1d) O.M1d[o + i] = d1[i];
+            }
+            O.T[(size_t)spin * P.n_TE + c_te] = (uint8_t)ts_old;
+            acc = 0.f; acc_e = 0.f; accd = 0.;
+            tp_old = tp;
+            c_te++;
+            t_te = c_te < P.n_TE ? (uint32_t)Tb.te_tp[c_te] : NONE;
+        }
+        // ---- accept the move (kernels.cu:218-223) ----
+        xo[0] = xn[0]; xo[1] = xn[1]; xo[2] = xn[2];
+        if (P.record_traj) {
+            float *dst = O.XYZ1 + 3 * ((size_t)spin * P.traj_len + (size_t)ds * P.n_timepoints + tp);
+            dst[0] = (float)xn[0]; dst[1] = (float)xn[1]; dst[2] = (float)xn[2];
+        }
+        tp++;
+    }
+
+    // ---- save state ----
+    S.x[spin] = xo[0]; S.y[spin] = xo[1]; S.z[spin] = xo[2];
+    S.mx[spin] = m0[0]; S.my[spin] = m0[1]; S.mz[spin] = m0[2];
+    S.acc[spin] = acc;
+    if (KAHAN) S.acc_e[spin] = acc_e;
+    if (DBL) {
+        S.accd[spin] = accd;
+        S.dmx[spin] = d0[0]; S.dmy[spin] = d0[1]; S.dmz[spin] = d0[2];
+    }
+    S.field[spin] = field;
+    S.ind_old[spin] = ind_old;
+    S.tp[spin] = tp; S.tp_old[spin] = tp_old; S.ds[spin] = ds; S.itr[spin] = itr;
+    S.ctr[spin] = c_rf | (c_te << 16);
+    S.ctr2[spin] = c_dph | (c_grad << 16);
+    G.nhead[spin] = nh; G.ncnt[spin] = nc; G.uhead[spin] = uh; G.ucnt[spin] = uc;
+    uint32_t nf = ts_old | (started ? kFlagStarted : 0u);
+    if (status >= 0) {
+        nf |= kFlagDone | ((uint32_t)status << 16);
+        if (!P.record_traj) {
+            float *dst = O.XYZ1 + 3 * (size_t)spin * P.traj_len;
+            dst[0] = (float)xo[0]; dst[1] = (float)xo[1]; dst[2] = (float)xo[2];
+        }
+        if (O.status) O.status[spin] = status;
+    }
+    S.flags[spin] = nf;
+    return status < 0;
+}
+
+template <int PREC, bool DBL>
+__global__ void __launch_bounds__(256)
+    k_walk(DevParams P, DevTables Tb, const uint2 *__restrict__ vox, SpinState S, RngState G,
+           Outputs O, uint32_t *active) {
+    const uint32_t spin = blockIdx.x * blockDim.x + threadIdx.x;
+    bool still = false;
+    if (spin < P.n_spins) {
+        const uint32_t flags = S.flags[spin];
+        if (!(flags & kFlagDone)) still = walk_spin<PREC, DBL>(spin, flags, P, Tb, vox, S, G, O);
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, still);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(active, (uint32_t)__popc(b));
+}
+
+__global__ void k_debug_logf(const float *x, float *y, uint64_t n, LogfTables L) {
+    __shared__ float s_tab[192];
+    for (int i = threadIdx.x; i < 192; i += blockDim.x) s_tab[i] = L.tab[i];
+    __syncthreads();
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        y[i] = logf_libm(x[i], s_tab, L);
+}
+
+// ------------------------------------------------------------------------------------------
+// Launchers
+// ------------------------------------------------------------------------------------------
+static int grid_for(int64_t work, int block, int max_blocks) {
+    int64_t g = (work + block - 1) / block;
+    if (g < 1) g = 1;
+    return (int)(g < max_blocks ? g : max_blocks);
+}
+
+cudaError_t launch_pack(const uint8_t *mask, const float *field, uint2 *out, int64_t n,
+                        uint32_t n_substrate, uint32_t *bad_label, cudaStream_t st) {
+    k_pack<<<grid_for(n, 256, 152 * 32), 256, 0, st>>>(mask, field, out, n, n_substrate,
+                                                        bad_label);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_seed(const DevParams &P, const RngState &G, cudaStream_t st) {
+    k_seed<<<grid_for(P.n_spins, kSeedWarps, 1 << 30), 32 * kSeedWarps, 0, st>>>(P, G);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init(const DevParams &P, const DevTables &Tb, const uint2 *vox,
+                        const float *M0, const float *XYZ0, const SpinState &S,
+                        const Outputs &O, bool fp64_state, cudaStream_t st) {
+    k_init<<<grid_for(P.n_spins, 256, 1 << 30), 256, 0, st>>>(P, Tb, vox, M0, XYZ0, S, O,
+                                                              fp64_state ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refill(const DevParams &P, const RngState &G, const uint32_t *flags,
+                          const LogfTables &L, cudaStream_t st) {
+    k_refill<<<grid_for(P.n_spins, kRefillWarps, 152 * 64), 32 * kRefillWarps, 0, st>>>(
+        P, G, flags, L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_walk(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
+                        const uint2 *vox, const SpinState &S, const RngState &G,
+                        const Outputs &O, uint32_t *active, cudaStream_t st) {
+    const int g = grid_for(P.n_spins, 256, 1 << 30);
+    if (prec == SW_PREC_FP64)
+        k_walk<SW_PREC_FP64, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active);
+    else if (prec == SW_PREC_KAHAN && dbl)
+        k_walk<SW_PREC_KAHAN, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active);
+    else if (prec == SW_PREC_KAHAN)
+        k_walk<SW_PREC_KAHAN, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active);
+    else if (dbl)
+        k_walk<SW_PREC_FP32, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active);
+    else
+        k_walk<SW_PREC_FP32, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_logf(const float *x, float *y, uint64_t n, const LogfTables &L,
+                              cudaStream_t st) {
+    k_debug_logf<<<grid_for((int64_t)n, 256, 152 * 16), 256, 0, st>>>(x, y, n, L);
+    return cudaGetLastError();
+}
+
+}  // namespace sw

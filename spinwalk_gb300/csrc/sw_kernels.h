@@ -1,0 +1,23 @@
+// Kernel launchers of sw_kernels.cu (host side).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sw_device.cuh"
+
+namespace sw {
+
+cudaError_t launch_pack(const uint8_t *mask, const float *field, uint2 *out, int64_t n,
+                        uint32_t n_substrate, uint32_t *bad_label, cudaStream_t st);
+cudaError_t launch_seed(const DevParams &P, const RngState &G, cudaStream_t st);
+cudaError_t launch_init(const DevParams &P, const DevTables &Tb, const uint2 *vox,
+                        const float *M0, const float *XYZ0, const SpinState &S,
+                        const Outputs &O, bool fp64_state, cudaStream_t st);
+cudaError_t launch_refill(const DevParams &P, const RngState &G, const uint32_t *flags,
+                          const LogfTables &L, cudaStream_t st);
+cudaError_t launch_walk(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
+                        const uint2 *vox, const SpinState &S, const RngState &G,
+                        const Outputs &O, uint32_t *active, cudaStream_t st);
+cudaError_t launch_debug_logf(const float *x, float *y, uint64_t n, const LogfTables &L,
+                              cudaStream_t st);
+
+}  // namespace sw

@@ -1,0 +1,106 @@
+// Plain-data types shared by the host C++ and the CUDA kernels (no CUDA types here).
+#pragma once
+#include <stdint.h>
+
+namespace sw {
+
+
+constexpr double kDeg2Rad = 0.0174532925199433;  // DEG2RAD, src/sim/simulation_parameters.cuh:24
+constexpr double kRad2Deg = 57.2957795130823;    // RAD2DEG, simulation_parameters.cuh:25
+constexpr double kGamma = 267515315.;            // GAMMA,   src/definitions.h:20
+
+constexpr int kMtN = 624;                        // mt19937 state size (words)
+constexpr int kMtM = 397;
+
+// Ring buffers of generator output per spin (refilled between walk chunks).
+constexpr uint32_t kNormBuf = 192;               // Gaussian deviates: 64 steps x 3 axes
+constexpr uint32_t kUnifBuf = 32;                // uniform deviates for crossing attempts
+
+// Spin flags word: bits 0-7 ts_old (substrate of the last accepted voxel), bit 8 "scan
+// started", bit 9 done, bits 16-23 status (SW_SPIN_*).
+constexpr uint32_t kFlagStarted = 1u << 8;
+constexpr uint32_t kFlagDone = 1u << 9;
+
+// One RF rotation, with the trigonometry precomputed on the host with the host libm (the values
+// the reference computes inside xrot_withphase, src/sim/kernels.cuh:160-206).
+//   kind 0: xrot(s,c)   1: xrot(-s,c)   2: yrot(s,c)   3: yrot(-s,c)
+//   kind 4: zrot(-sp,cp) -> xrot(s,c) -> zrot(sp,cp)
+struct RfOp {
+    int32_t kind;
+    int32_t tp;               // time point (RF events k >= 1; unused for the scan-start pulse)
+    float s, c, sp, cp;       // float path
+    double sd, cd, spd, cpd;  // FP64 path
+};
+
+// Device-resident copies of the scalar parameters (passed by value to every kernel).
+struct DevParams {
+    double fov[3];
+    double s2g[3];            // phantom_size / fov  (kernels.cu:98)
+    int64_t nz, nynz;         // row-major strides (kernels.cuh:53-60)
+    int64_t matrix_length;
+    uint64_t seed;
+    uint64_t max_iterations;
+    uint32_t n_spins, n_timepoints, n_substrate, n_dummy_scan;
+    uint32_t n_TE, n_RF, n_dephasing, n_gradient;
+    int32_t timestep_us;
+    int32_t cross_fov, record_traj, fieldmap_exist;
+    uint64_t traj_len;        // XYZ1 slots per spin
+};
+
+// Small read-only tables (device pointers into one allocation).
+struct DevTables {
+    const double *dscale;     // [ns] step std-dev (m)
+    const float *T1f, *T2f;   // [ns] float(T1_ms*1e-3) as the reference stores it (kernels.cu:167)
+    const double *T1d, *T2d;  // [ns] T1_ms*1e-3 in double (FP64 path)
+    const float *pXY;         // [ns*ns]
+    const RfOp *rf;           // [n_RF]  (index 0 unused)
+    const RfOp *scan_rf;      // [n_dummy_scan+1] scan-start pulse incl. phase cycling
+    const int32_t *te_tp;     // [n_TE]
+    const int32_t *dph_tp;    // [n_dephasing]
+    const float *dph_deg;
+    const int32_t *grad_tp;   // [n_gradient]
+    const float *gx, *gy, *gz;
+};
+
+// Bit-exact logf tables (see sw_logf.h).
+struct LogfTables {
+    const float *tab;         // 64 x {invc, Lhi, Llo}
+    const uint32_t *off;      // [kNumBuckets + 1]
+    const uint32_t *ent;      // exceptions: (x_bits << 1) | (libm == cand + 1ulp)
+};
+
+// Per-spin walk state between chunks (structure of arrays, one entry per spin).
+struct SpinState {
+    double *x, *y, *z;        // xyz_old (kernels.cu:93)
+    float *mx, *my, *mz;      // m0
+    float *acc, *acc_e;       // accumulated phase (+ two-sum error in KAHAN mode)
+    double *accd;             // FP64 phase (FP64 mode / shadow)
+    double *dmx, *dmy, *dmz;  // FP64 magnetisation (FP64 mode / shadow)
+    float *field;             // field of the last accepted voxel (deg / step)
+    int64_t *ind_old;
+    uint32_t *tp, *tp_old, *ds, *itr;
+    uint32_t *ctr;            // c_rf | c_te << 16
+    uint32_t *ctr2;           // c_dph | c_grad << 16
+    uint32_t *flags;
+};
+
+// Generator state: two mt19937 per spin (gen_r for the walk, gen_u for crossings,
+// kernels.cu:82-83) and the ring buffers of their output.
+struct RngState {
+    uint32_t *mt_r, *mt_u;    // [n][624]
+    uint32_t *p_r, *p_u;      // next output index in the current 624-word block
+    float *nbuf;              // [n][kNormBuf]
+    uint32_t *nhead, *ncnt;
+    float *ubuf;              // [n][kUnifBuf]
+    uint32_t *uhead, *ucnt;
+};
+
+struct Outputs {
+    float *M1;                // [n][n_TE][3]
+    double *M1d;              // optional FP64 shadow
+    float *XYZ1;              // [n][traj_len][3]
+    uint8_t *T;               // [n][n_TE]
+    int32_t *status;          // optional
+};
+
+}  // namespace sw

@@ -1,0 +1,159 @@
+"""GPU parity: the sm_103a kernels against the reference's golden outputs and the oracle.
+
+Bar: trajectories (XYZ1), substrates at the echoes (T) and per-spin status are bit-exact;
+magnetisation within M_RTOL = 1e-5 of |M| (+1e-7 absolute) in the FP32 path.
+"""
+import numpy as np
+import pytest
+
+from spinwalk_gb300 import _lib, abi
+from spinwalk_gb300.problem import Problem, cylinder_phantom
+from tests import oracle_lib
+from tests.helpers import GOLDEN_CASES, bits_equal, load_golden, m_close
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_gpu_matches_reference_golden(case):
+    pr, ref = load_golden(case)
+    out = _lib.run(pr, fill=np.nan)
+    assert bits_equal(out["XYZ1"], ref["XYZ1"]), f"{case}: trajectories differ"
+    assert bits_equal(out["T"], ref["T"]), f"{case}: substrates differ"
+    ok, rel = m_close(out["M1"], ref["M1"])
+    assert ok, f"{case}: M1 max relative error {rel:.3e}"
+    st = oracle_lib.run(pr)["status"]
+    assert np.array_equal(out["status"], st), f"{case}: status differs"
+
+
+@pytest.mark.parametrize("case", ["gre", "se_multi_te", "bssfp_phase_cycling", "pgse_gradients",
+                                  "permeable", "ste_dephasing"])
+@pytest.mark.parametrize("prec", [abi.SW_PREC_FP64, abi.SW_PREC_KAHAN])
+def test_gpu_precision_modes_match_oracle(case, prec):
+    pr, _ = load_golden(case)
+    g = _lib.run(pr, precision=prec, fp64_shadow=True)
+    o = oracle_lib.run(pr, precision=prec, fp64_shadow=True)
+    assert bits_equal(g["XYZ1"], o["XYZ1"]) and bits_equal(g["T"], o["T"])
+    # the FP64 shadow differs from the oracle's only by libm-vs-CUDA double sin/cos/exp
+    d = np.abs(g["M1_fp64"] - o["M1_fp64"])
+    assert d.max() <= 1e-12, d.max()
+    ok, rel = m_close(g["M1"], o["M1"])
+    assert ok, rel
+
+
+def test_gpu_fp64_shadow_reports_fp32_error():
+    """The FP64 run of the same walk is what the FP32 error is stated against."""
+    pr, _ = load_golden("se_multi_te")
+    g = _lib.run(pr, fp64_shadow=True)
+    err = np.abs(g["M1"] - g["M1_fp64"]).max()
+    assert 0 < err < 1e-4
+
+
+def test_gpu_random_configs_match_oracle():
+    rng = np.random.default_rng(7)
+    for trial in range(4):
+        n = int(rng.integers(12, 40))
+        mask, field = cylinder_phantom(n, n * 1e-6, float(rng.uniform(2e-6, 5e-6)), 0.12,
+                                       seed=trial)
+        kw = dict(n_spins=int(rng.integers(1, 700)), seed=int(rng.integers(1, 10 ** 6)),
+                  TR_us=4050, TE_us=(1000, 2000, 4000), RF_FA=(90.0, 180.0),
+                  RF_PH=(0.0, float(rng.choice([0.0, 90.0, 37.5]))), RF_us=(0, 1500),
+                  pXY=rng.uniform(0, 1, (2, 2)), n_dummy_scan=int(rng.integers(0, 3)),
+                  linear_phase_cycling=float(rng.uniform(0, 200)),
+                  cross_fov=bool(rng.integers(0, 2)))
+        pr = Problem(mask, [n * 1e-6] * 3, field, **kw)
+        g = _lib.run(pr, fill=np.nan)
+        o = oracle_lib.run(pr, fill=np.nan)
+        assert bits_equal(g["XYZ1"], o["XYZ1"]), trial
+        assert bits_equal(g["T"], o["T"]), trial
+        assert np.array_equal(g["status"], o["status"]), trial
+        ok, rel = m_close(g["M1"], o["M1"])
+        assert ok, (trial, rel)
+
+
+def test_gpu_large_seed_and_spin_ids():
+    """Spin ids near 2^20 with a large seed: long discard() runs in the seeding kernel."""
+    mask, field = cylinder_phantom(16, 16e-6, 3e-6, 0.1, seed=5)
+    pr = Problem(mask, [16e-6] * 3, field, n_spins=1 << 20, seed=123456, TR_us=550,
+                 TE_us=(500,))
+    ids = np.array([0, 1, 623, 624, 625, 99999, (1 << 20) - 2, (1 << 20) - 1], np.uint32)
+    g = _lib.run(pr)
+    o = oracle_lib.run(pr, spin_ids=ids)
+    for k in ("XYZ1", "T"):
+        assert bits_equal(g[k][ids], o[k][ids]), k
+    ok, rel = m_close(g["M1"][ids], o["M1"][ids])
+    assert ok, rel
+
+
+def test_gpu_deterministic_and_spin_independent():
+    pr, _ = load_golden("permeable")
+    a = _lib.run(pr)
+    b = _lib.run(pr)
+    for k in ("M1", "XYZ1", "T", "status"):
+        assert bits_equal(a[k], b[k]), k
+    # the first k spins of a run alone equal the same spins in the full run
+    z = np.load(__import__("os").path.join(__import__("tests.helpers", fromlist=["x"]).GOLDEN_DIR,
+                                           "permeable.npz"))
+    kw = __import__("json").loads(str(z["kwargs"]))
+    kw["n_spins"] = 40
+    pr40 = Problem(z["mask"], [float(z["fov"])] * 3, z["field_T"], XYZ0=z["XYZ0"][:40],
+                   **{k: (tuple(v) if isinstance(v, list) and k != "pXY" else v)
+                      for k, v in kw.items()})
+    c = _lib.run(pr40)
+    for k in ("M1", "XYZ1", "T"):
+        assert bits_equal(c[k], a[k][:40]), k
+
+
+def test_gpu_logf_matches_host_libm_exhaustively():
+    """Device logf == host libm logf on every float in [2^-48, 1] (the polar-method domain)."""
+    torch = pytest.importorskip("torch")
+    lo, hi = 0x27800000, 0x3F800000
+    chunk = 1 << 26
+    start = lo
+    while start <= hi:
+        stop = min(hi + 1, start + chunk)
+        bits = np.arange(start, stop, dtype=np.uint32)
+        x = bits.view(np.float32)
+        want = oracle_lib.host_logf(x)
+        dx = torch.from_numpy(x).cuda()
+        dy = torch.empty_like(dx)
+        _lib.debug_logf(dx.data_ptr(), dy.data_ptr(), x.size)
+        torch.cuda.synchronize()
+        got = dy.cpu().numpy()
+        bad = np.flatnonzero(got.view(np.uint32) != want.view(np.uint32))
+        assert bad.size == 0, f"{bad.size} mismatches, first x={x[bad[0]]!r}"
+        start = stop
+
+
+def test_gpu_device_api_matches_host_api():
+    torch = pytest.importorskip("torch")
+    pr, _ = load_golden("se_multi_te")
+    h = _lib.run(pr)
+    n, nte = pr.params.n_spins, pr.n_te
+    dev = "cuda"
+    d_field = torch.from_numpy(pr.field).to(dev)
+    d_mask = torch.from_numpy(pr.mask).to(dev)
+    d_M0 = torch.from_numpy(pr.M0).to(dev)
+    d_XYZ0 = torch.from_numpy(pr.XYZ0).to(dev)
+    d_M1 = torch.zeros((n, nte, 3), dtype=torch.float32, device=dev)
+    d_XYZ1 = torch.zeros((n, pr.traj_len, 3), dtype=torch.float32, device=dev)
+    d_T = torch.zeros((n, nte), dtype=torch.uint8, device=dev)
+    d_st = torch.zeros(n, dtype=torch.int32, device=dev)
+    _lib.run_device(pr, d_field.data_ptr(), d_mask.data_ptr(), d_M0.data_ptr(),
+                    d_XYZ0.data_ptr(), d_M1.data_ptr(), d_XYZ1.data_ptr(), d_T.data_ptr(),
+                    d_st.data_ptr())
+    torch.cuda.synchronize()
+    assert bits_equal(d_M1.cpu().numpy(), h["M1"])
+    assert bits_equal(d_XYZ1.cpu().numpy(), h["XYZ1"])
+    assert bits_equal(d_T.cpu().numpy(), h["T"])
+    assert np.array_equal(d_st.cpu().numpy(), h["status"])
+
+
+def test_gpu_rejects_bad_arguments():
+    pr, _ = load_golden("gre")
+    pr.params.matrix_length += 1
+    with pytest.raises(_lib.SpinWalkError):
+        _lib.run(pr)
+    pr.params.matrix_length -= 1
+    with pytest.raises(_lib.SpinWalkError):
+        _lib.run(pr, precision=7)

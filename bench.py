@@ -1,0 +1,333 @@
+"""Benchmark of the SpinWalk `sim` hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload se|gre] [--impl ours|reference]
+
+A "step" is one full pass of the hot path over one batch of synthetic input: per-spin generator
+seeding (mt19937(seed+spin) + discard), the walk over all time points and the Bloch update for
+every spin -- exactly the work of the reference's per-scale loop (src/sim/monte_carlo.cu:310-335).
+
+Workloads (synthetic, seeded; the reference publishes no dataset):
+  se  (default) spin echo, 500^3 phantom of random spheres (r 2-8 um, 5 %), 1e6 spins, 2001 time
+      points (TE 40 ms, dt 20 us, TR = TE + dt), permeability 0.01 both ways.
+  gre gradient echo, 200^3 phantom of random-orientation cylinders (r 5 um, 3 %), 1e5 spins,
+      401 time points (TE 20 ms, dt 50 us).
+
+Metric: spin-steps/s (spins x time points x scans per second of the whole pass). `value` is
+timed with CUDA events with every input already in HBM; `e2e` goes through the public host-buffer
+entry point sw_sim (host->device copies of the inputs and device->host copies of the results
+inside the timed region). Inputs (packed phantom, generator state) are larger than L2, so no
+explicit flush is needed between steps.
+
+--impl reference times the reference algorithm's CPU path (the oracle port of sim::sim, with
+std::mt19937) on all host cores on a bounded, stratified sample of the same workload's spin ids.
+Multi-GPU: spins are independent, so each rank walks its own spin range (weak scaling, no
+collective on the data path).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GATHER_BYTES_PER_SPIN_STEP = 32   # one DRAM sector per random voxel lookup (mask + field record)
+USEFUL_BYTES_PER_SPIN_STEP = 5    # 1 B mask + 4 B field
+
+
+def workload(name, rank=0):
+    from spinwalk_gb300 import _lib
+    from spinwalk_gb300.problem import Problem
+    if name == "se":
+        n, fov = 500, 500e-6
+        mask, field = _lib.phantom_spheres(n, fov, 2e-6, 8e-6, 0.05, seed=2)
+        n_spins = 1_000_000
+        kw = dict(TR_us=40020, TE_us=(40000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
+                  RF_us=(0, 20000), timestep_us=20, pXY=[[1.0, 0.01], [0.01, 1.0]],
+                  T2_ms=(40.0, 20.0), T1_ms=(2000.0, 2000.0))
+        desc = dict(workload="se_spheres_500cubed_1e6spins_2001tp", phantom="500^3 spheres r2-8um 5%",
+                    n_spins=n_spins, time_points=2001, sequence="SE 90/180, TE 40 ms, dt 20 us",
+                    permeability=0.01)
+    elif name == "gre":
+        n, fov = 200, 200e-6
+        mask, field = _lib.phantom_cylinders(n, fov, 5e-6, 0.03, seed=1)
+        n_spins = 100_000
+        kw = dict(TR_us=20050, TE_us=(20000,), timestep_us=50)
+        desc = dict(workload="gre_cylinders_200cubed_1e5spins_401tp",
+                    phantom="200^3 cylinders r5um 3% random orientation", n_spins=n_spins,
+                    time_points=401, sequence="GRE 90, TE 20 ms, dt 50 us", permeability=0.0)
+    elif name == "small":      # profiling case: > L2 phantom, few GB on the device
+        n, fov = 300, 300e-6
+        mask, field = _lib.phantom_spheres(n, fov, 2e-6, 8e-6, 0.05, seed=2)
+        n_spins = 200_000
+        kw = dict(TR_us=4020, TE_us=(4000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
+                  RF_us=(0, 2000), timestep_us=20, pXY=[[1.0, 0.01], [0.01, 1.0]])
+        desc = dict(workload="small_se_300cubed_2e5spins_201tp", n_spins=n_spins, time_points=201)
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    seed = 10 + 1_000_003 * rank          # each rank: its own disjoint spin population
+    pr = Problem(mask, [fov] * 3, field, n_spins=n_spins, seed=seed, **kw)
+    return pr, desc
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.dev = device_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            c = [x.strip() for x in line.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                mx = float(c[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, c[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample_ids(n_spins, n_sample):
+    """Stratified sample: evenly spaced spin ids over the whole range (the per-spin discard()
+    cost grows with the spin id, so a prefix would under-count it)."""
+    return np.unique(np.linspace(0, n_spins - 1, n_sample).round().astype(np.uint32))
+
+
+def time_cpu(pr, n_sample, threads=0):
+    from tests import oracle_lib
+    ids = cpu_sample_ids(pr.params.n_spins, n_sample)
+    outs = pr.outputs()
+    t = time.perf_counter()
+    oracle_lib.run(pr, spin_ids=ids, n_threads=threads, outputs=outs)
+    dt = time.perf_counter() - t
+    steps = len(ids) * pr.params.n_timepoints * (pr.params.n_dummy_scan + 1)
+    return steps / dt, len(ids), dt
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, world, rank):
+    """CPU reference arm: the oracle port on all host cores, rank 0 only."""
+    if rank != 0:
+        return
+    pr, desc = workload(args.workload)
+    cores = os.cpu_count()
+    n_sample = args.cpu_sample
+    for _ in range(args.warmup):
+        time_cpu(pr, max(16, n_sample // 8), cores)
+    rates, secs = [], []
+    for _ in range(args.steps):
+        r, n, dt = time_cpu(pr, n_sample, cores)
+        rates.append(r)
+        secs.append(dt)
+    v = float(np.mean(rates))
+    sample = (f"{n} stratified spin ids of {pr.params.n_spins} per step, "
+              f"{pr.params.n_timepoints} time points each, extrapolated as spin-steps/s")
+    line = {"impl": "reference", "metric": "spin-steps/s", "value": v, "unit": "spin-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * float(np.mean(secs)), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(desc, l2="inputs larger than L2"),
+            "cpu_baseline": {"value": v, "unit": "spin-steps/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "spin-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    from spinwalk_gb300 import _lib
+
+    torch.cuda.set_device(local)
+    pr, desc = workload(args.workload, rank)
+    p = pr.params
+    n, nte = p.n_spins, pr.n_te
+    dev = torch.device("cuda", local)
+    d = dict(field=torch.from_numpy(pr.field).to(dev), mask=torch.from_numpy(pr.mask).to(dev),
+             M0=torch.from_numpy(pr.M0).to(dev), XYZ0=torch.from_numpy(pr.XYZ0).to(dev),
+             M1=torch.zeros((n, nte, 3), dtype=torch.float32, device=dev),
+             XYZ1=torch.zeros((n, pr.traj_len, 3), dtype=torch.float32, device=dev),
+             T=torch.zeros((n, nte), dtype=torch.uint8, device=dev),
+             status=torch.zeros(n, dtype=torch.int32, device=dev))
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        _lib.run_device(pr, d["field"].data_ptr(), d["mask"].data_ptr(), d["M0"].data_ptr(),
+                        d["XYZ0"].data_ptr(), d["M1"].data_ptr(), d["XYZ1"].data_ptr(),
+                        d["T"].data_ptr(), d["status"].data_ptr(), stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    spin_steps = pr.spin_steps()
+    timings = []
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+            timings.append(_lib.last_timing())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    clocks = clk.summary()
+    ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(world, ms)
+    value = world * spin_steps * args.steps / (ms * 1e-3)
+    st = d["status"].cpu().numpy()
+
+    # ---- end to end through the host-buffer entry point ----
+    e2e_times = []
+    h2d = pr.mask.nbytes + pr.field.nbytes + pr.M0.nbytes + pr.XYZ0.nbytes + \
+        n * nte * 12 + n * nte + n * pr.traj_len * 12
+    d2h = n * nte * 12 + n * nte + n * pr.traj_len * 12 + n * 4
+    _lib.run(pr)                                     # warm (host staging)
+    for _ in range(max(1, args.steps)):
+        barrier(world)
+        t = time.perf_counter()
+        out = _lib.run(pr)
+        e2e_times.append(time.perf_counter() - t)
+    e2e_s = max_over_ranks(world, float(np.mean(e2e_times)))
+    e2e = world * spin_steps / e2e_s
+    assert np.array_equal(out["status"], st)
+
+    if rank != 0:
+        return
+    walk_ms = sum(t["walk_ms"] for t in timings)
+    refill_ms = sum(t["refill_ms"] for t in timings)
+    seed_ms = sum(t["seed_ms"] for t in timings)
+    n_walk = sum(t["n_chunks"] for t in timings)
+    launches = sum(t["n_launches"] for t in timings)
+    parts = {"walk": walk_ms, "refill": refill_ms, "seed+init+pack": seed_ms}
+    dominant = max(parts, key=parts.get)
+    peak, peak_kind = measured_peaks()
+    # walk kernel: algorithmic gather bytes per launch / average launch duration
+    achieved = spin_steps * args.steps * GATHER_BYTES_PER_SPIN_STEP / (walk_ms * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic_per_spin_step.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            tb = json.load(f).get("walk_dram_bytes_per_spin_step")
+        if tb:
+            traffic = tb * spin_steps / (n_walk / args.steps)
+    cpu = None
+    if world == 1 or rank == 0:
+        if args.cpu_sample > 0:
+            rate, ns, dt = time_cpu(pr, args.cpu_sample, os.cpu_count())
+            cpu = {"value": rate, "unit": "spin-steps/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"{ns} stratified spin ids of {n} ({pr.params.n_timepoints} time "
+                             f"points each, {dt:.1f} s wall on {os.cpu_count()} threads)"}
+    line = {
+        "metric": "spin-steps/s", "value": value, "unit": "spin-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded phantom generator, reference-driver initial positions)",
+        "config": dict(desc, parallelism=f"spin-range shards x{world}",
+                       l2="inputs larger than L2 (packed phantom + generator state)"),
+        "kernel_ms_per_step": {k: v / args.steps for k, v in parts.items()},
+        "roofline": {"bound": "hbm", "kernel": "k_walk", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "note": f"{GATHER_BYTES_PER_SPIN_STEP} B gather sector per spin-step; "
+                             f"dominant stage: {dominant}"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": "spin-steps/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "status_counts": {str(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="se")
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=16384)
+    args = ap.parse_args()
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -106,6 +106,21 @@ typedef struct sw_sequence {
     uint32_t n_RF, n_TE, n_dephasing, n_gradient;
 } sw_sequence;
 
+/*
+ * Synthetic phantoms (host C++, OpenMP, deterministic per seed): uint8 mask (1 inside a shape)
+ * and field in Tesla at B0 = 1 T, row-major [dims[0]][dims[1]][dims[2]]. The field models are
+ * those of the reference's phantom generators (src/phantom/phantom_cylinder.cpp:255-265,
+ * src/phantom/phantom_sphere.cpp:180-187); the placement differs (random orientations allowed,
+ * overlaps allowed, sphere fields summed within +-window*r). `field` may be NULL.
+ */
+int sw_phantom_cylinders(const uint32_t dims[3], const double fov[3], double radius,
+                         double volume_fraction, uint64_t seed, int random_orientation,
+                         double dchi, double Y, const double B0_dir[3], uint8_t *mask,
+                         float *field);
+int sw_phantom_spheres(const uint32_t dims[3], const double fov[3], double rmin, double rmax,
+                       double volume_fraction, uint64_t seed, double dchi, double Y,
+                       const double B0_dir[3], double window, uint8_t *mask, float *field);
+
 /* Library and device information. */
 int         sw_abi_version(void);
 const char *sw_last_error(void);

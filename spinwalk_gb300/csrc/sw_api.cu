@@ -42,7 +42,7 @@ struct DeviceCtx {
     std::mutex mu;
     bool logf_ready = false;
     float *d_logf_tab = nullptr;
-    uint32_t *d_logf_off = nullptr, *d_logf_ent = nullptr;
+    uint32_t *d_logf_bitmap = nullptr;
     char *ws = nullptr;
     size_t ws_size = 0;
     uint32_t *h_active = nullptr;          // pinned
@@ -66,17 +66,16 @@ struct Carve {
 int ensure_logf(DeviceCtx &c) {
     if (c.logf_ready) return SW_OK;
     const sw::LogfExceptions &ex = sw::logf_exceptions();
-    if (ex.wide != 0) return fail(SW_ERR_INVALID, "host logf differs from the candidate by >1 ulp");
+    if (ex.wide != 0)
+        return fail(SW_ERR_INVALID, "the host logf differs from the device candidate by more "
+                                    "than one ulp towards the exact value on " +
+                                        std::to_string(ex.wide) + " inputs");
     SW_CUDA(cudaMalloc(&c.d_logf_tab, 192 * sizeof(float)));
-    SW_CUDA(cudaMalloc(&c.d_logf_off, ex.off.size() * sizeof(uint32_t)));
-    SW_CUDA(cudaMalloc(&c.d_logf_ent, std::max<size_t>(1, ex.ent.size()) * sizeof(uint32_t)));
+    SW_CUDA(cudaMalloc(&c.d_logf_bitmap, ex.bitmap.size() * sizeof(uint32_t)));
     SW_CUDA(cudaMemcpy(c.d_logf_tab, sw::logf_reduction_table(), 192 * sizeof(float),
                        cudaMemcpyHostToDevice));
-    SW_CUDA(cudaMemcpy(c.d_logf_off, ex.off.data(), ex.off.size() * sizeof(uint32_t),
+    SW_CUDA(cudaMemcpy(c.d_logf_bitmap, ex.bitmap.data(), ex.bitmap.size() * sizeof(uint32_t),
                        cudaMemcpyHostToDevice));
-    if (!ex.ent.empty())
-        SW_CUDA(cudaMemcpy(c.d_logf_ent, ex.ent.data(), ex.ent.size() * sizeof(uint32_t),
-                           cudaMemcpyHostToDevice));
     SW_CUDA(cudaMallocHost(&c.h_active, sizeof(uint32_t)));
     c.ev.resize(2 * kMaxTimedChunks + 4);
     for (auto &e : c.ev) SW_CUDA(cudaEventCreate(&e));
@@ -85,7 +84,7 @@ int ensure_logf(DeviceCtx &c) {
 }
 
 sw::LogfTables logf_tables(const DeviceCtx &c) {
-    return sw::LogfTables{c.d_logf_tab, c.d_logf_off, c.d_logf_ent};
+    return sw::LogfTables{c.d_logf_tab, c.d_logf_bitmap};
 }
 
 int check_args(const sw_params *p, const sw_sequence *q) {
@@ -117,6 +116,7 @@ sw::DevParams dev_params(const sw_params *p, const sw_sequence *q) {
     for (int i = 0; i < 3; i++) {
         d.fov[i] = p->fov[i];
         d.s2g[i] = (double)p->phantom_size[i] / p->fov[i];       // kernels.cu:98
+        d.s2g_f[i] = (float)d.s2g[i];
     }
     d.nz = (int64_t)p->phantom_size[2];
     d.nynz = (int64_t)p->phantom_size[1] * (int64_t)p->phantom_size[2];

@@ -74,6 +74,38 @@ __device__ __forceinline__ void mt_twist_warp(uint32_t *s, int lane) {
     __syncwarp();
 }
 
+// The same regeneration with the state held in registers: lane l owns words l + 32k in a[k]
+// (k < 20; a[19] only for lanes < 16). x[i+1] and the far word x[i+397] (words < 227) or the
+// already regenerated x[i-227] (words >= 227) arrive by warp shuffles, 41 per regeneration,
+// and no shared memory is touched. Words are regenerated in increasing k, each k reading its
+// operands before any lane overwrites a[k], which reproduces the sequential in-place order.
+__device__ __forceinline__ void mt_twist_regs(uint32_t (&a)[20], int lane) {
+    constexpr unsigned FULL = 0xffffffffu;
+#pragma unroll
+    for (int k = 0; k < 20; k++) {
+        uint32_t nxt;
+        if (k < 19) {
+            const uint32_t prov = (lane == 0) ? a[k + 1] : a[k];
+            nxt = __shfl_sync(FULL, prov, (lane + 1) & 31);
+        } else {   // word 623's successor is the regenerated word 0
+            const uint32_t prov = (lane == 0) ? a[0] : a[19];
+            nxt = __shfl_sync(FULL, prov, lane == 15 ? 0 : (lane + 1) & 31);
+        }
+        uint32_t farA = 0u, farB = 0u;
+        if (k <= 7) {
+            const uint32_t prov = (lane >= 13) ? a[k + 12] : ((k + 13 < 20) ? a[k + 13 < 20 ? k + 13 : 0] : 0u);
+            farA = __shfl_sync(FULL, prov, (lane + 13) & 31);
+        }
+        if (k >= 7) {
+            const uint32_t prov = (lane < 29) ? a[k - 7] : ((k >= 8) ? a[k >= 8 ? k - 8 : 0] : 0u);
+            farB = __shfl_sync(FULL, prov, (lane + 29) & 31);
+        }
+        const bool inA = (lane + 32 * k) < 227;
+        const uint32_t nw = mt_twist1(a[k], nxt, inA ? farA : farB);
+        if (k < 19 || lane < 16) a[k] = nw;
+    }
+}
+
 // generate_canonical<float, 24>(mt19937): float(w) / 2^32, clamped below 1
 // (libstdc++ bits/random.tcc, generate_canonical).
 __device__ __forceinline__ float canon24(uint32_t w) {
@@ -81,20 +113,57 @@ __device__ __forceinline__ float canon24(uint32_t w) {
     return f >= 1.0f ? 0x1.fffffep-1f : f;
 }
 
-// The host libm's logf, bit for bit, on [2^-48, 1] (sw_logf.h).
+// The host libm's logf, bit for bit, on [2^-48, 1] (sw_logf.h): the candidate, or its
+// neighbour towards the exact value where the host's exception bitmap says so.
 __device__ __forceinline__ float logf_libm(float x, const float *s_tab, const LogfTables &L) {
-    float c = swlogf::logf_cand(x, s_tab);
-    const uint32_t bits = __float_as_uint(x);
-    const uint32_t b = (bits - swlogf::kDomainLo) >> swlogf::kBucketShift;
-    uint32_t lo = __ldg(L.off + b), hi = __ldg(L.off + b + 1);
-    for (uint32_t i = lo; i < hi; i++) {
-        uint32_t e = __ldg(L.ent + i);
-        if ((e >> 1) == bits) {
-            c = __uint_as_float(__float_as_uint(c) + ((e & 1u) ? 1u : 0xffffffffu));
-            break;
-        }
+    bool above;
+    const float c = swlogf::logf_cand(x, s_tab, above);
+    const uint32_t k = __float_as_uint(x) - swlogf::kDomainLo;
+    const uint32_t w = __ldg(L.bitmap + (k >> 5));
+    return ((w >> (k & 31u)) & 1u) ? swlogf::neighbour(c, above) : c;
+}
+
+// ------------------------------------------------------------------------------------------
+// Exact helpers that keep the walk off the (slow) FP64 pipe
+// ------------------------------------------------------------------------------------------
+// float -> double, exact, with integer operations. The Gaussian deviates are 0 or have
+// magnitude >= 2^-36 (|y| >= 2^-24 times sqrt(-2 ln r2 / r2)), so they are never subnormal;
+// a subnormal input still takes the exact conversion instruction.
+__device__ __forceinline__ double f2d_exact(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+    if (e == 0u) return m ? (double)f : __hiloint2double(b & 0x80000000u, 0);
+    const uint32_t hi = (b & 0x80000000u) | ((e + (1023u - 127u)) << 20) | (m >> 3);
+    return __hiloint2double((int)hi, (int)(m << 29));
+}
+
+// v < 0 and v >= bound (bound > 0) on the bit patterns (positive doubles order as integers).
+__device__ __forceinline__ bool dneg(double v) {
+    const long long b = __double_as_longlong(v);
+    return b < 0 && (b & 0x7fffffffffffffffLL) != 0;
+}
+__device__ __forceinline__ bool dge_pos(double v, double bound) {
+    return __double_as_longlong(v) >= __double_as_longlong(bound);
+}
+
+// (int64_t)(v * s2g) as the reference computes it (double product, truncation), via an FP32
+// estimate: v is truncated to 24 bits from its bit pattern (relative error < 2^-23), s2g_f is
+// s2g rounded to float (< 2^-24), the float product adds < 2^-24, so |p - v*s2g| < 2^-22 |p|.
+// When p is farther than 2^-21 |p| from an integer (all but ~1e-4 of the calls at 500 voxels)
+// floor(p) is the answer; otherwise, and for v <= 0 or tiny v, the exact double product is used.
+__device__ __forceinline__ int64_t voxel_coord(double v, double s2g, float s2g_f) {
+    const uint32_t hi = (uint32_t)__double2hiint(v), lo = (uint32_t)__double2loint(v);
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    if ((int32_t)hi > 0 && e > 1023u - 120u) {
+        const float vf = __uint_as_float(((e - 1023u + 127u) << 23) | ((hi & 0xfffffu) << 3) |
+                                         (lo >> 29));
+        const float p = vf * s2g_f;
+        const float fl = floorf(p);
+        const float fr = p - fl;
+        const float margin = p * 4.76837158203125e-07f;    // 2^-21
+        if (fr > margin && 1.0f - fr > margin) return (int64_t)fl;
     }
-    return c;
+    return (int64_t)(v * s2g);
 }
 
 // ------------------------------------------------------------------------------------------

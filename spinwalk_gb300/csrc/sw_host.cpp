@@ -23,45 +23,36 @@ static const float kLogfTab[192] = SW_LOGF_TABLE_INIT;
 
 const float *logf_reduction_table() { return kLogfTab; }
 
-// Every float x in [2^-48, 1] where the host logf differs from logf_cand, as
-// (bits << 1) | (libm == cand + 1 ulp), sorted, with a bucket index over bits >> 12.
-// Built once per process (~4e8 evaluations, a second or two on all cores).
+// Marks every float x in [2^-48, 1] where the host logf differs from logf_cand, and checks that
+// the candidate's neighbour towards the exact value (swlogf::neighbour) is the libm result
+// there. Built once per process (~4e8 evaluations, about a second on all cores).
 const LogfExceptions &logf_exceptions() {
     static LogfExceptions ex;
     static std::once_flag once;
     std::call_once(once, [] {
-        const uint32_t nb = swlogf::kNumBuckets;
-        const int nt = omp_get_max_threads();
-        std::vector<std::vector<uint32_t>> per(nt);
-        std::vector<uint32_t> count(nb, 0);
-#pragma omp parallel num_threads(nt)
-        {
-            const int t = omp_get_thread_num();
-            const uint32_t b0 = (uint64_t)nb * t / nt, b1 = (uint64_t)nb * (t + 1) / nt;
-            std::vector<uint32_t> &out = per[t];
-            for (uint32_t b = b0; b < b1; b++) {
-                const uint32_t lo = swlogf::kDomainLo + (b << swlogf::kBucketShift);
-                uint32_t hi = lo + (1u << swlogf::kBucketShift);
-                if (hi > swlogf::kDomainHi + 1) hi = swlogf::kDomainHi + 1;
-                for (uint32_t bits = lo; bits < hi; bits++) {
-                    const float x = swlogf::u2f(bits);
-                    const float g = logf(x);
-                    const float c = swlogf::logf_cand(x, kLogfTab);
-                    const uint32_t gb = swlogf::f2u(g), cb = swlogf::f2u(c);
-                    if (gb != cb) {
-                        // the libm result is always an adjacent float of the candidate; a
-                        // wider gap would be recorded as "down" and caught by the tests
-                        out.push_back((bits << 1) | (gb == cb + 1 ? 1u : 0u));
-                        if (gb != cb + 1 && gb + 1 != cb) ex.wide++;
-                        count[b]++;
-                    }
+        const uint32_t nw = swlogf::kBitmapWords;
+        ex.bitmap.assign(nw, 0u);
+        uint64_t count = 0, wide = 0;
+#pragma omp parallel for schedule(static) reduction(+ : count, wide)
+        for (int64_t w = 0; w < (int64_t)nw; w++) {
+            uint32_t word = 0;
+            for (uint32_t b = 0; b < 32; b++) {
+                const uint32_t bits = swlogf::kDomainLo + ((uint32_t)w << 5) + b;
+                if (bits > swlogf::kDomainHi) break;
+                const float x = swlogf::u2f(bits);
+                const float g = logf(x);
+                bool above;
+                const float c = swlogf::logf_cand(x, kLogfTab, above);
+                if (swlogf::f2u(g) != swlogf::f2u(c)) {
+                    word |= 1u << b;
+                    count++;
+                    if (swlogf::f2u(swlogf::neighbour(c, above)) != swlogf::f2u(g)) wide++;
                 }
             }
+            ex.bitmap[w] = word;
         }
-        ex.off.assign(nb + 1, 0);
-        for (uint32_t b = 0; b < nb; b++) ex.off[b + 1] = ex.off[b] + count[b];
-        ex.ent.reserve(ex.off[nb]);
-        for (auto &v : per) ex.ent.insert(ex.ent.end(), v.begin(), v.end());
+        ex.count = count;
+        ex.wide = wide;
     });
     return ex;
 }
@@ -155,7 +146,7 @@ int sw_initial_positions(const float fov[3], uint64_t seed, uint32_t n_spins, fl
 
 int sw_logf_exception_count(uint64_t *count, uint64_t *wide) {
     const sw::LogfExceptions &ex = sw::logf_exceptions();
-    if (count) *count = ex.ent.size();
+    if (count) *count = ex.count;
     if (wide) *wide = ex.wide;
     return SW_OK;
 }

@@ -9,9 +9,9 @@
 namespace sw {
 
 struct LogfExceptions {
-    std::vector<uint32_t> off;   // [kNumBuckets + 1]
-    std::vector<uint32_t> ent;   // (bits << 1) | up
-    uint64_t wide = 0;           // differences wider than one ulp (expected: 0)
+    std::vector<uint32_t> bitmap;  // [kBitmapWords]: 1 where the host logf != candidate
+    uint64_t count = 0;            // inputs marked
+    uint64_t wide = 0;             // marked inputs the neighbour rule does not fix (must be 0)
 };
 
 const float *logf_reduction_table();            // 64 x {invc, Lhi, Llo}

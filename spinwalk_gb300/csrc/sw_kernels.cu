@@ -5,8 +5,8 @@
 // same per-spin computation is split so that each part runs in the shape the GPU likes:
 //
 //   k_pack    : mask + fieldmap -> one 8-byte record per voxel (one gather per step)
-//   k_seed    : one WARP per spin: mt19937(seed+spin) + discard(seed+spin), the twist done by
-//               32 lanes on a shared-memory copy of the 624-word state
+//   k_seed    : one WARP per spin: mt19937(seed+spin) + discard(seed+spin), the 624-word state
+//               held in the 32 lanes' registers and regenerated with warp shuffles
 //   k_init    : one thread per spin: initial voxel, substrate and state (kernels.cu:90-104)
 //   k_refill  : one WARP per spin: tops up the spin's ring buffers of Gaussian deviates
 //               (libstdc++ polar method, 32 candidate pairs per pass, accepted pairs compacted
@@ -63,19 +63,30 @@ __global__ void __launch_bounds__(32 * kSeedWarps) k_seed(DevParams P, RngState 
             }
         }
         __syncwarp();
+        uint32_t a[20];                              // lane l holds words l + 32k
+#pragma unroll
+        for (int k = 0; k < 20; k++) {
+            const int i = lane + 32 * k;
+            a[k] = i < kMtN ? s[i] : 0u;
+        }
+        __syncwarp();
         // mersenne_twister_engine::discard: while (z > n - p) { z -= n - p; twist; p = 0; }
         uint64_t z = sd;
         uint32_t p = kMtN;
         while (z > (uint64_t)(kMtN - p)) {
             z -= kMtN - p;
-            mt_twist_warp(s, lane);
+            mt_twist_regs(a, lane);
             p = 0;
         }
         p += (uint32_t)z;
         uint32_t *gr = G.mt_r + (size_t)spin * kMtN, *gu = G.mt_u + (size_t)spin * kMtN;
-        for (int i = lane; i < kMtN; i += 32) {
-            gr[i] = s[i];
-            gu[i] = s[i];
+#pragma unroll
+        for (int k = 0; k < 20; k++) {
+            const int i = lane + 32 * k;
+            if (i < kMtN) {
+                gr[i] = a[k];
+                gu[i] = a[k];
+            }
         }
         if (lane == 0) {
             G.p_r[spin] = p;
@@ -348,19 +359,20 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
             for (int i = 0; i < 3; i++) {
                 const float g = nb[nh];
                 nh = (nh + 1 == kNormBuf) ? 0 : nh + 1;
-                const double rnd = (double)g * dscale;
+                const double rnd = f2d_exact(g) * dscale;
                 double v = xo[i] + rnd;
-                if (v < 0)
+                if (dneg(v))
                     v += P.cross_fov ? P.fov[i] : 2 * fabs(rnd);
-                else if (v >= P.fov[i])
+                else if (dge_pos(v, P.fov[i]))
                     v -= P.cross_fov ? P.fov[i] : 2 * fabs(rnd);
                 xn[i] = v;
             }
             nc -= 3;
         }
         // ---- voxel index (kernels.cu:140-147) ----
-        const int64_t ind = (int64_t)(xn[0] * P.s2g[0]) * P.nynz +
-                            (int64_t)(xn[1] * P.s2g[1]) * P.nz + (int64_t)(xn[2] * P.s2g[2]);
+        const int64_t ind = voxel_coord(xn[0], P.s2g[0], P.s2g_f[0]) * P.nynz +
+                            voxel_coord(xn[1], P.s2g[1], P.s2g_f[1]) * P.nz +
+                            voxel_coord(xn[2], P.s2g[2], P.s2g_f[2]);
         if (ind >= P.matrix_length || ind < 0) { status = SW_SPIN_OOB; break; }
         // ---- mask, permeability, field (kernels.cu:150-170) ----
         if (ind != ind_old) {

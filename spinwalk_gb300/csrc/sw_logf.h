@@ -10,9 +10,11 @@
 //      the SAME float for every input. It is correctly rounded except on a tiny fraction of
 //      inputs.
 //   2. At start-up the host evaluates its own libm logf and logf_cand on every float of the
-//      domain and records the inputs where they differ (all by one unit in the last place):
-//      ~2e5 of 4e8, held as a sorted exception list with a bucket index (~1.2 MB). The device
-//      applies the +-1 ulp correction from that list.
+//      domain and marks, in a bitmap (one bit per input, 50 MB), the inputs where they differ:
+//      ~2e5 of 4e8 (glibc 2.39: 111k of them in [0.5, 1)). Every difference is one unit in the
+//      last place towards the exact value, so the device takes the candidate's neighbour on the
+//      side given by the sign of the candidate's own rounding residual. The host verifies that
+//      rule on every marked input before the table is used.
 //
 // Reduction: x = 2^k * m with m in [0.75, 1.5); m is split into 64 buckets by its bit pattern;
 // r = m*invc - 1 is formed exactly as a float pair; log(x) = k*ln2 + L_j + log1p(r) with L_j =
@@ -33,11 +35,10 @@
 
 namespace swlogf {
 
-// Domain covered by the exception list: [2^-48, 1].
+// Domain covered by the exception bitmap: [2^-48, 1].
 constexpr uint32_t kDomainLo = 0x27800000u;    // bits of 2^-48
 constexpr uint32_t kDomainHi = 0x3f800000u;    // bits of 1.0f (inclusive)
-constexpr uint32_t kBucketShift = 12;
-constexpr uint32_t kNumBuckets = ((kDomainHi - kDomainLo) >> kBucketShift) + 1;
+constexpr uint32_t kBitmapWords = ((kDomainHi - kDomainLo) >> 5) + 1;
 
 constexpr float kLn2Hi = 0x1.62e4p-1f;          // ln2 rounded to 17 bits: k*kLn2Hi is exact
 constexpr float kLn2Lo = 0x1.7f7d1cp-20f;       // ln2 - kLn2Hi rounded to float
@@ -85,9 +86,11 @@ SWL_HD void two_sum(float a, float b, float &s, float &e) {
     e = fadd(fsub(a, fsub(s, bb)), fsub(b, bb));
 }
 
-// tab: 64 x {invc, Lhi, Llo}. Valid for x in [2^-48, 1].
-SWL_HD float logf_cand(float x, const float *tab) {
+// tab: 64 x {invc, Lhi, Llo}. Valid for x in [2^-48, 1]. `above` is set when the float-float
+// value the candidate rounded (an approximation of log(x) to ~2^-38) lies above the result.
+SWL_HD float logf_cand(float x, const float *tab, bool &above) {
     const uint32_t ix = f2u(x);
+    above = false;
     if (ix == 0x3f800000u) return 0.0f;
     const int32_t t = (int32_t)(ix - 0x3f400000u);
     const int32_t k = t >> 23;                                  // arithmetic shift
@@ -120,7 +123,17 @@ SWL_HD float logf_cand(float x, const float *tab) {
     sm = fadd(sm, fadd(fmul(kf, kLn2Lo), Llo));
     float Cs, c_err;
     two_sum(A, B, Cs, c_err);
-    return fadd(Cs, fadd(c_err, sm));
+    const float lo = fadd(c_err, sm);
+    const float r = fadd(Cs, lo);
+    above = fadd(fsub(Cs, r), lo) > 0.0f;
+    return r;
+}
+
+// The candidate's neighbour one ulp away, on the side of the exact value.
+SWL_HD float neighbour(float r, bool above) {
+    // r < 0 on (0, 1): a larger value has a smaller magnitude, i.e. bits - 1
+    const uint32_t b = f2u(r);
+    return u2f(above == (r < 0.0f) ? b - 1u : b + 1u);
 }
 
 }  // namespace swlogf

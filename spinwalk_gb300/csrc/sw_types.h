@@ -36,6 +36,7 @@ struct RfOp {
 struct DevParams {
     double fov[3];
     double s2g[3];            // phantom_size / fov  (kernels.cu:98)
+    float s2g_f[3];           // s2g rounded to float (fast path of voxel_coord)
     int64_t nz, nynz;         // row-major strides (kernels.cuh:53-60)
     int64_t matrix_length;
     uint64_t seed;
@@ -65,8 +66,7 @@ struct DevTables {
 // Bit-exact logf tables (see sw_logf.h).
 struct LogfTables {
     const float *tab;         // 64 x {invc, Lhi, Llo}
-    const uint32_t *off;      // [kNumBuckets + 1]
-    const uint32_t *ent;      // exceptions: (x_bits << 1) | (libm == cand + 1ulp)
+    const uint32_t *bitmap;   // bit (x_bits - 2^-48 bits): host libm differs from the candidate
 };
 
 // Per-spin walk state between chunks (structure of arrays, one entry per spin).

@@ -180,6 +180,35 @@ int sw_sim_device(const sw_params *param, const sw_sequence *seq,
                   int precision, double *d_M1_fp64, void *stream);
 int sw_sync(void *stream);
 
+/*
+ * sw_sim_device without any device allocation, for callers that are not allowed to allocate
+ * device memory: a process whose device memory is reserved up front by a pool or another
+ * framework's allocator, a real-time loop that cannot take cudaMalloc's implicit device-wide
+ * synchronisation, or a host application that forbids libraries from allocating on their own.
+ * No counterpart in the reference (its driver allocates thrust device_vectors per run).
+ *
+ * The caller passes device inputs and outputs exactly as for sw_sim_device (FP32 precision, no
+ * FP64 shadow). All other device memory comes from one static array of SW_NOALLOC_SCRATCH_BYTES
+ * that every GPU loading this part of the library keeps until the process exits. About 48 MiB of
+ * it hold the logf correction table; the rest must fit the call: roughly 6 KiB per spin plus
+ * 8 bytes per voxel -- larger requests are rejected with SW_ERR_NOMEM and a message, never
+ * partially run. No cudaMalloc/cudaFree or other device-allocating routine is called (host-side
+ * staging of the small parameter tables uses ordinary host memory).
+ *
+ * The first call on a device sets the region up (resolves the array's device address and copies
+ * the logf table into it, synchronously); make that first call before any stream capture. Every
+ * call reuses the same array and finds the previous call's contents there; it re-initialises all
+ * state it reads. Calls on one device are serialised by the library and each returns only after
+ * its work on `stream` has finished; any other work that touched the array while a call runs on
+ * the GPU would race with it.
+ */
+#define SW_NOALLOC_SCRATCH_BYTES (128ull << 20)
+int sw_sim_device_noalloc(const sw_params *param, const sw_sequence *seq,
+                          const float *d_FieldMap, const uint8_t *d_Mask,
+                          const float *d_M0, const float *d_XYZ0,
+                          float *d_M1, float *d_XYZ1, uint8_t *d_T, int32_t *d_status,
+                          void *stream);
+
 /* Timing of the kernels launched by the last sw_sim / sw_sim_device call on this thread
  * (milliseconds, CUDA events on the launching stream): seeding, RNG refill, walk, total. */
 typedef struct sw_timing {

@@ -48,6 +48,7 @@ def lib():
                     C.c_void_p]
         L.sw_sim.argtypes = sim_args
         L.sw_sim_device.argtypes = sim_args + [C.c_void_p]
+        L.sw_sim_device_noalloc.argtypes = sim_args[:10] + [C.c_void_p]
         L.sw_sync.argtypes = [C.c_void_p]
         L.sw_last_timing.argtypes = [P(abi.SwTiming)]
         L.sw_debug_logf.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
@@ -143,6 +144,15 @@ def run_device(problem, d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T, d_stat
     check(lib().sw_sim_device(C.byref(problem.params), C.byref(problem.seq.struct),
                               d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T, d_status,
                               int(precision), d_M1d, stream))
+
+
+def run_device_noalloc(problem, d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T,
+                       d_status=None, stream=None):
+    """sw_sim_device_noalloc: like run_device (FP32), with no device allocation by the library;
+    its scratch is a fixed static device array (see include/spinwalk_gpu.h)."""
+    check(lib().sw_sim_device_noalloc(C.byref(problem.params), C.byref(problem.seq.struct),
+                                      d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T,
+                                      d_status, stream))
 
 
 def debug_logf(d_x, d_y, n, stream=None):

@@ -17,8 +17,11 @@
 #include "spinwalk_gpu.h"
 #include "sw_host.h"
 #include "sw_kernels.h"
+#include "sw_api_internal.h"
 
-namespace {
+namespace sw {
+namespace api {
+
 
 thread_local std::string g_err;
 thread_local sw_timing g_timing{};
@@ -35,57 +38,6 @@ int fail(int code, const std::string &msg) {
             return fail(SW_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-constexpr int kMaxDevices = 64;
-constexpr int kMaxTimedChunks = 4096;
-
-struct DeviceCtx {
-    std::mutex mu;
-    bool logf_ready = false;
-    float *d_logf_tab = nullptr;
-    uint32_t *d_logf_bitmap = nullptr;
-    char *ws = nullptr;
-    size_t ws_size = 0;
-    uint32_t *h_active = nullptr;          // pinned
-    std::vector<cudaEvent_t> ev;           // timing events
-};
-DeviceCtx g_ctx[kMaxDevices];
-
-// Bump allocator over the workspace (256-byte aligned slices).
-struct Carve {
-    char *base;
-    size_t off = 0;
-    template <typename T>
-    T *take(size_t n) {
-        off = (off + 255) & ~size_t(255);
-        T *p = base ? reinterpret_cast<T *>(base + off) : nullptr;
-        off += n * sizeof(T);
-        return p;
-    }
-};
-
-int ensure_logf(DeviceCtx &c) {
-    if (c.logf_ready) return SW_OK;
-    const sw::LogfExceptions &ex = sw::logf_exceptions();
-    if (ex.wide != 0)
-        return fail(SW_ERR_INVALID, "the host logf differs from the device candidate by more "
-                                    "than one ulp towards the exact value on " +
-                                        std::to_string(ex.wide) + " inputs");
-    SW_CUDA(cudaMalloc(&c.d_logf_tab, 192 * sizeof(float)));
-    SW_CUDA(cudaMalloc(&c.d_logf_bitmap, ex.bitmap.size() * sizeof(uint32_t)));
-    SW_CUDA(cudaMemcpy(c.d_logf_tab, sw::logf_reduction_table(), 192 * sizeof(float),
-                       cudaMemcpyHostToDevice));
-    SW_CUDA(cudaMemcpy(c.d_logf_bitmap, ex.bitmap.data(), ex.bitmap.size() * sizeof(uint32_t),
-                       cudaMemcpyHostToDevice));
-    SW_CUDA(cudaMallocHost(&c.h_active, sizeof(uint32_t)));
-    c.ev.resize(2 * kMaxTimedChunks + 4);
-    for (auto &e : c.ev) SW_CUDA(cudaEventCreate(&e));
-    c.logf_ready = true;
-    return SW_OK;
-}
-
-sw::LogfTables logf_tables(const DeviceCtx &c) {
-    return sw::LogfTables{c.d_logf_tab, c.d_logf_bitmap};
-}
 
 int check_args(const sw_params *p, const sw_sequence *q) {
     if (!p || !q) return fail(SW_ERR_INVALID, "null params or sequence");
@@ -140,19 +92,6 @@ sw::DevParams dev_params(const sw_params *p, const sw_sequence *q) {
     return d;
 }
 
-// Host image of the small tables, laid out exactly like the device copy.
-struct TableImage {
-    std::vector<char> bytes;
-    size_t o_dscale, o_T1f, o_T2f, o_T1d, o_T2d, o_pXY, o_rf, o_scan, o_te, o_dtp, o_ddeg, o_gtp,
-        o_gx, o_gy, o_gz;
-    template <typename T>
-    size_t put(const T *src, size_t n) {
-        size_t off = (bytes.size() + 15) & ~size_t(15);
-        bytes.resize(off + std::max<size_t>(1, n) * sizeof(T));
-        if (n) std::memcpy(bytes.data() + off, src, n * sizeof(T));
-        return off;
-    }
-};
 
 void build_tables(const sw_params *p, const sw_sequence *q, TableImage &im) {
     const uint32_t ns = p->n_substrate;
@@ -204,16 +143,8 @@ sw::DevTables dev_tables(const TableImage &im, const char *d) {
     return t;
 }
 
-// Lays out the whole workspace; with base == nullptr it only measures.
-struct Layout {
-    uint2 *vox;
-    char *tables;
-    uint32_t *active;
-    sw::SpinState S;
-    sw::RngState G;
-    size_t bytes;
-};
 
+// Lays out the whole workspace; with base == nullptr it only measures.
 Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl) {
     Carve c{base};
     Layout L{};
@@ -255,6 +186,52 @@ Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl) {
     G.ucnt = c.take<uint32_t>(n);
     L.bytes = c.off + 256;
     return L;
+}
+
+}  // namespace api
+}  // namespace sw
+
+using namespace sw::api;
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+constexpr int kMaxTimedChunks = 4096;
+
+struct DeviceCtx {
+    std::mutex mu;
+    bool logf_ready = false;
+    float *d_logf_tab = nullptr;
+    uint32_t *d_logf_bitmap = nullptr;
+    char *ws = nullptr;
+    size_t ws_size = 0;
+    uint32_t *h_active = nullptr;          // pinned
+    std::vector<cudaEvent_t> ev;           // timing events
+};
+DeviceCtx g_ctx[kMaxDevices];
+
+int ensure_logf(DeviceCtx &c) {
+    if (c.logf_ready) return SW_OK;
+    const sw::LogfExceptions &ex = sw::logf_exceptions();
+    if (ex.wide != 0)
+        return fail(SW_ERR_INVALID, "the host logf differs from the device candidate by more "
+                                    "than one ulp towards the exact value on " +
+                                        std::to_string(ex.wide) + " inputs");
+    SW_CUDA(cudaMalloc(&c.d_logf_tab, 192 * sizeof(float)));
+    SW_CUDA(cudaMalloc(&c.d_logf_bitmap, ex.bitmap.size() * sizeof(uint32_t)));
+    SW_CUDA(cudaMemcpy(c.d_logf_tab, sw::logf_reduction_table(), 192 * sizeof(float),
+                       cudaMemcpyHostToDevice));
+    SW_CUDA(cudaMemcpy(c.d_logf_bitmap, ex.bitmap.data(), ex.bitmap.size() * sizeof(uint32_t),
+                       cudaMemcpyHostToDevice));
+    SW_CUDA(cudaMallocHost(&c.h_active, sizeof(uint32_t)));
+    c.ev.resize(2 * kMaxTimedChunks + 4);
+    for (auto &e : c.ev) SW_CUDA(cudaEventCreate(&e));
+    c.logf_ready = true;
+    return SW_OK;
+}
+
+sw::LogfTables logf_tables(const DeviceCtx &c) {
+    return sw::LogfTables{c.d_logf_tab, c.d_logf_bitmap};
 }
 
 int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const float *d_field,

@@ -1,0 +1,64 @@
+// Internal helpers of the C ABI (sw_api.cu), shared with sw_noalloc.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "spinwalk_gpu.h"
+#include "sw_types.h"
+
+namespace sw {
+namespace api {
+
+// Bump allocator over the workspace (256-byte aligned slices).
+struct Carve {
+    char *base;
+    size_t off = 0;
+    template <typename T>
+    T *take(size_t n) {
+        off = (off + 255) & ~size_t(255);
+        T *p = base ? reinterpret_cast<T *>(base + off) : nullptr;
+        off += n * sizeof(T);
+        return p;
+    }
+};
+
+// Host image of the small tables, laid out exactly like the device copy.
+struct TableImage {
+    std::vector<char> bytes;
+    size_t o_dscale, o_T1f, o_T2f, o_T1d, o_T2d, o_pXY, o_rf, o_scan, o_te, o_dtp, o_ddeg, o_gtp,
+        o_gx, o_gy, o_gz;
+    template <typename T>
+    size_t put(const T *src, size_t n) {
+        size_t off = (bytes.size() + 15) & ~size_t(15);
+        bytes.resize(off + std::max<size_t>(1, n) * sizeof(T));
+        if (n) std::memcpy(bytes.data() + off, src, n * sizeof(T));
+        return off;
+    }
+};
+
+// Device workspace of one call, carved from one allocation.
+struct Layout {
+    uint2 *vox;
+    char *tables;
+    uint32_t *active;
+    SpinState S;
+    RngState G;
+    size_t bytes;
+};
+
+// Sets sw_last_error() for the calling thread and returns `code`.
+int fail(int code, const std::string &msg);
+// Parameter checks shared by every entry point.
+int check_args(const sw_params *p, const sw_sequence *q);
+DevParams dev_params(const sw_params *p, const sw_sequence *q);
+void build_tables(const sw_params *p, const sw_sequence *q, TableImage &im);
+DevTables dev_tables(const TableImage &im, const char *d);
+// base == nullptr: only measures (Layout::bytes).
+Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl);
+
+}  // namespace api
+}  // namespace sw

@@ -29,7 +29,7 @@ struct Carve {
 // Host image of the small tables, laid out exactly like the device copy.
 struct TableImage {
     std::vector<char> bytes;
-    size_t o_dscale, o_T1f, o_T2f, o_T1d, o_T2d, o_pXY, o_rf, o_scan, o_te, o_dtp, o_ddeg, o_gtp,
+    size_t o_dscale, o_dsplit, o_T1f, o_T2f, o_T1d, o_T2d, o_pXY, o_rf, o_scan, o_te, o_dtp, o_ddeg, o_gtp,
         o_gx, o_gy, o_gz;
     template <typename T>
     size_t put(const T *src, size_t n) {

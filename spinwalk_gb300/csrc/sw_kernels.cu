@@ -46,13 +46,14 @@ __global__ void k_pack(const uint8_t *__restrict__ mask, const float *__restrict
 // ------------------------------------------------------------------------------------------
 constexpr int kSeedWarps = 4;
 
-__global__ void __launch_bounds__(32 * kSeedWarps) k_seed(DevParams P, RngState G) {
+__global__ void __launch_bounds__(32 * kSeedWarps)
+    k_seed(DevParams P, RngState G, uint32_t spin_lo, uint32_t spin_hi) {
     __shared__ uint32_t s_mt[kSeedWarps][kMtN];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     uint32_t *s = s_mt[w];
-    for (uint32_t idx = blockIdx.x * kSeedWarps + w; idx < P.n_spins;
+    for (uint32_t idx = blockIdx.x * kSeedWarps + w; idx < spin_hi - spin_lo;
          idx += gridDim.x * kSeedWarps) {
-        const uint32_t spin = P.n_spins - 1 - idx;   // most expensive (largest discard) first
+        const uint32_t spin = spin_hi - 1 - idx;     // most expensive (largest discard) first
         const uint64_t sd = P.seed + spin;
         if (lane == 0) {                             // mersenne_twister_engine::seed
             uint32_t x = (uint32_t)sd;
@@ -171,7 +172,8 @@ __device__ __forceinline__ uint32_t block_word(const uint32_t *gst, const uint32
 }
 
 __global__ void __launch_bounds__(32 * kRefillWarps)
-    k_refill(DevParams P, RngState G, const uint32_t *__restrict__ flags, LogfTables L) {
+    k_refill(DevParams P, RngState G, const uint32_t *__restrict__ flags, LogfTables L,
+             uint32_t spin_lo, uint32_t spin_hi) {
     __shared__ float s_tab[192];
     __shared__ uint32_t s_mt[kRefillWarps][kMtN];
     for (int i = threadIdx.x; i < 192; i += blockDim.x) s_tab[i] = L.tab[i];
@@ -179,7 +181,7 @@ __global__ void __launch_bounds__(32 * kRefillWarps)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
     uint32_t *s = s_mt[w];
-    for (uint32_t spin = blockIdx.x * kRefillWarps + w; spin < P.n_spins;
+    for (uint32_t spin = spin_lo + blockIdx.x * kRefillWarps + w; spin < spin_hi;
          spin += gridDim.x * kRefillWarps) {
         if (flags[spin] & kFlagDone) continue;
         // ---- Gaussian deviates from gen_r (normal_distribution<float>, polar method) ----
@@ -303,6 +305,7 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
     uint32_t ts_old = flags & 0xffu;
     bool started = (flags & kFlagStarted) != 0;
     double dscale = __ldg(Tb.dscale + ts_old);
+    uint4 dsp = __ldg(reinterpret_cast<const uint4 *>(Tb.dsplit) + ts_old);
 
     uint32_t nh = G.nhead[spin], nc = G.ncnt[spin], uh = G.uhead[spin], uc = G.ucnt[spin];
     const float *nb = G.nbuf + (size_t)spin * kNormBuf;
@@ -359,7 +362,8 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
             for (int i = 0; i < 3; i++) {
                 const float g = nb[nh];
                 nh = (nh + 1 == kNormBuf) ? 0 : nh + 1;
-                const double rnd = f2d_exact(g) * dscale;
+                const double rnd = dsp.w ? mul_fd(g, dsp.x, dsp.y, (int)dsp.z)
+                                         : f2d_exact(g) * dscale;
                 double v = xo[i] + rnd;
                 if (dneg(v))
                     v += P.cross_fov ? P.fov[i] : 2 * fabs(rnd);
@@ -391,6 +395,7 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
             ind_old = ind;
             field = __uint_as_float(v.x);
             dscale = __ldg(Tb.dscale + ts_old);
+            dsp = __ldg(reinterpret_cast<const uint4 *>(Tb.dsplit) + ts_old);
         }
         // ---- phase accumulation (kernels.cu:171-172) ----
         if (KAHAN) kahan_add(acc, acc_e, field); else acc += field;
@@ -501,10 +506,10 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
 template <int PREC, bool DBL>
 __global__ void __launch_bounds__(256)
     k_walk(DevParams P, DevTables Tb, const uint2 *__restrict__ vox, SpinState S, RngState G,
-           Outputs O, uint32_t *active) {
-    const uint32_t spin = blockIdx.x * blockDim.x + threadIdx.x;
+           Outputs O, uint32_t *active, uint32_t spin_lo, uint32_t spin_hi) {
+    const uint32_t spin = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
     bool still = false;
-    if (spin < P.n_spins) {
+    if (spin < spin_hi) {
         const uint32_t flags = S.flags[spin];
         if (!(flags & kFlagDone)) still = walk_spin<PREC, DBL>(spin, flags, P, Tb, vox, S, G, O);
     }
@@ -538,7 +543,13 @@ cudaError_t launch_pack(const uint8_t *mask, const float *field, uint2 *out, int
 }
 
 cudaError_t launch_seed(const DevParams &P, const RngState &G, cudaStream_t st) {
-    k_seed<<<grid_for(P.n_spins, kSeedWarps, 1 << 30), 32 * kSeedWarps, 0, st>>>(P, G);
+    return launch_seed_range(P, G, 0, P.n_spins, st);
+}
+
+cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo, uint32_t hi,
+                              cudaStream_t st) {
+    if (hi <= lo) return cudaSuccess;
+    k_seed<<<grid_for(hi - lo, kSeedWarps, 1 << 30), 32 * kSeedWarps, 0, st>>>(P, G, lo, hi);
     return cudaGetLastError();
 }
 
@@ -552,25 +563,39 @@ cudaError_t launch_init(const DevParams &P, const DevTables &Tb, const uint2 *vo
 
 cudaError_t launch_refill(const DevParams &P, const RngState &G, const uint32_t *flags,
                           const LogfTables &L, cudaStream_t st) {
-    k_refill<<<grid_for(P.n_spins, kRefillWarps, 152 * 64), 32 * kRefillWarps, 0, st>>>(
-        P, G, flags, L);
+    return launch_refill_range(P, G, flags, L, 0, P.n_spins, st);
+}
+
+cudaError_t launch_refill_range(const DevParams &P, const RngState &G, const uint32_t *flags,
+                                const LogfTables &L, uint32_t lo, uint32_t hi, cudaStream_t st) {
+    if (hi <= lo) return cudaSuccess;
+    k_refill<<<grid_for(hi - lo, kRefillWarps, 152 * 64), 32 * kRefillWarps, 0, st>>>(
+        P, G, flags, L, lo, hi);
     return cudaGetLastError();
 }
 
 cudaError_t launch_walk(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
                         const uint2 *vox, const SpinState &S, const RngState &G,
                         const Outputs &O, uint32_t *active, cudaStream_t st) {
-    const int g = grid_for(P.n_spins, 256, 1 << 30);
+    return launch_walk_range(prec, dbl, P, Tb, vox, S, G, O, active, 0, P.n_spins, st);
+}
+
+cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
+                              const uint2 *vox, const SpinState &S, const RngState &G,
+                              const Outputs &O, uint32_t *active, uint32_t lo, uint32_t hi,
+                              cudaStream_t st) {
+    if (hi <= lo) return cudaSuccess;
+    const int g = grid_for(hi - lo, 256, 1 << 30);
     if (prec == SW_PREC_FP64)
-        k_walk<SW_PREC_FP64, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active);
+        k_walk<SW_PREC_FP64, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
     else if (prec == SW_PREC_KAHAN && dbl)
-        k_walk<SW_PREC_KAHAN, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active);
+        k_walk<SW_PREC_KAHAN, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
     else if (prec == SW_PREC_KAHAN)
-        k_walk<SW_PREC_KAHAN, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active);
+        k_walk<SW_PREC_KAHAN, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
     else if (dbl)
-        k_walk<SW_PREC_FP32, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active);
+        k_walk<SW_PREC_FP32, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
     else
-        k_walk<SW_PREC_FP32, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active);
+        k_walk<SW_PREC_FP32, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
     return cudaGetLastError();
 }
 

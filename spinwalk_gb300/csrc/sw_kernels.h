@@ -9,6 +9,14 @@ namespace sw {
 cudaError_t launch_pack(const uint8_t *mask, const float *field, uint2 *out, int64_t n,
                         uint32_t n_substrate, uint32_t *bad_label, cudaStream_t st);
 cudaError_t launch_seed(const DevParams &P, const RngState &G, cudaStream_t st);
+cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo, uint32_t hi,
+                              cudaStream_t st);
+cudaError_t launch_refill_range(const DevParams &P, const RngState &G, const uint32_t *flags,
+                                const LogfTables &L, uint32_t lo, uint32_t hi, cudaStream_t st);
+cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
+                              const uint2 *vox, const SpinState &S, const RngState &G,
+                              const Outputs &O, uint32_t *active, uint32_t lo, uint32_t hi,
+                              cudaStream_t st);
 cudaError_t launch_init(const DevParams &P, const DevTables &Tb, const uint2 *vox,
                         const float *M0, const float *XYZ0, const SpinState &S,
                         const Outputs &O, bool fp64_state, cudaStream_t st);

@@ -181,6 +181,37 @@ int sw_sim_device(const sw_params *param, const sw_sequence *seq,
 int sw_sync(void *stream);
 
 /*
+ * Many instances of one configuration that walk identically, in one pass: the reference's
+ * phase-cycling scales (WHAT_TO_SCALE = 2, src/sim/monte_carlo.cu:302-305), its DUMMY_SCAN
+ * sweeps and per-pulse flip-angle / phase variants all re-run the same trajectories (same seeds,
+ * same XYZ0; the scan structure does not touch the random streams). sw_sim_tracks walks every
+ * spin ONCE and advances one Bloch state per distinct RF configuration; each track's outputs
+ * are bit-identical to sw_sim on that instance alone.
+ *
+ * A track = one instance: its phase cycling, its DUMMY_SCAN (echoes are recorded in that
+ * scan), optional per-pulse RF_FA / RF_PH arrays (NULL = the sequence's), and host output
+ * buffers. `param` supplies everything else (its n_dummy_scan, phase cycling, c and s are
+ * ignored; enRecordTrajectory must be 0). Tracks with identical RF configuration and
+ * DUMMY_SCAN are rejected as duplicates. FP32 arithmetic (the reference's).
+ */
+typedef struct sw_track {
+    float linear_phase_cycling;
+    float quadratic_phase_cycling;
+    int32_t n_dummy_scan;
+    int32_t _pad;
+    const float *RF_FA_deg;   /* [n_RF] or NULL */
+    const float *RF_PH_deg;   /* [n_RF] or NULL */
+    float *M1;                /* [n_spins][n_TE][3] host */
+    float *XYZ1;              /* [n_spins][3] host: final position */
+    uint8_t *T;               /* [n_spins][n_TE] host */
+    int32_t *status;          /* [n_spins] host, or NULL */
+} sw_track;
+
+int sw_sim_tracks(const sw_params *param, const sw_sequence *seq, const sw_track *tracks,
+                  uint32_t n_tracks, const float *pFieldMap, const uint8_t *pMask,
+                  const float *M0, const float *XYZ0);
+
+/*
  * sw_sim_device without any device allocation, for callers that are not allowed to allocate
  * device memory: a process whose device memory is reserved up front by a pool or another
  * framework's allocator, a real-time loop that cannot take cudaMalloc's implicit device-wide

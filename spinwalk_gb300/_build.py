@@ -28,7 +28,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", *ARCH, "-lineinfo", "-fmad=false",
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp", f"-I{INC}",
              f"-I{CSRC}"]
 
-CU_UNITS = ["sw_kernels.cu", "sw_api.cu", "sw_noalloc.cu"]
+CU_UNITS = ["sw_kernels.cu", "sw_api.cu", "sw_noalloc.cu", "sw_tracks.cu"]
 CXX_UNITS = ["sw_host.cpp", "sw_phantom.cpp"]
 
 

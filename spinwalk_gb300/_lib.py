@@ -49,6 +49,8 @@ def lib():
         L.sw_sim.argtypes = sim_args
         L.sw_sim_device.argtypes = sim_args + [C.c_void_p]
         L.sw_sim_device_noalloc.argtypes = sim_args[:10] + [C.c_void_p]
+        L.sw_sim_tracks.argtypes = [P(abi.SwParams), P(abi.SwSequence), P(abi.SwTrack), C.c_uint32,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.sw_sync.argtypes = [C.c_void_p]
         L.sw_last_timing.argtypes = [P(abi.SwTiming)]
         L.sw_debug_logf.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
@@ -153,6 +155,38 @@ def run_device_noalloc(problem, d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T
     check(lib().sw_sim_device_noalloc(C.byref(problem.params), C.byref(problem.seq.struct),
                                       d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T,
                                       d_status, stream))
+
+
+def run_tracks(problem, tracks, fill=0.0):
+    """sw_sim_tracks: many instances of `problem` sharing one walk. `tracks` is a list of dicts
+    with keys linear_phase_cycling, quadratic_phase_cycling, n_dummy_scan and optionally
+    RF_FA_deg / RF_PH_deg arrays. Returns one output dict per track."""
+    n, nte = problem.params.n_spins, problem.n_te
+    arr = (abi.SwTrack * len(tracks))()
+    outs, keep = [], []
+    for i, t in enumerate(tracks):
+        o = dict(M1=np.full((n, nte, 3), fill, np.float32), XYZ1=np.full((n, 1, 3), fill, np.float32),
+                 T=np.zeros((n, nte), np.uint8), status=np.full(n, -1, np.int32))
+        outs.append(o)
+        s = arr[i]
+        s.linear_phase_cycling = t.get("linear_phase_cycling", 0.0)
+        s.quadratic_phase_cycling = t.get("quadratic_phase_cycling", 0.0)
+        s.n_dummy_scan = int(t.get("n_dummy_scan", 0))
+        for key in ("RF_FA_deg", "RF_PH_deg"):
+            if t.get(key) is not None:
+                a = np.ascontiguousarray(t[key], np.float32)
+                keep.append(a)
+                setattr(s, key, abi.ptr(a, C.c_float))
+            else:
+                setattr(s, key, abi.ptr(None, C.c_float))
+        s.M1 = abi.ptr(o["M1"], C.c_float)
+        s.XYZ1 = abi.ptr(o["XYZ1"], C.c_float)
+        s.T = abi.ptr(o["T"], C.c_uint8)
+        s.status = abi.ptr(o["status"], C.c_int32)
+    check(lib().sw_sim_tracks(C.byref(problem.params), C.byref(problem.seq.struct), arr,
+                              len(tracks), _p(problem.field), _p(problem.mask), _p(problem.M0),
+                              _p(problem.XYZ0)))
+    return outs
 
 
 def debug_logf(d_x, d_y, n, stream=None):

@@ -76,6 +76,21 @@ class SwSequence(C.Structure):
     ]
 
 
+class SwTrack(C.Structure):
+    _fields_ = [
+        ("linear_phase_cycling", C.c_float),
+        ("quadratic_phase_cycling", C.c_float),
+        ("n_dummy_scan", C.c_int32),
+        ("_pad", C.c_int32),
+        ("RF_FA_deg", C.POINTER(C.c_float)),
+        ("RF_PH_deg", C.POINTER(C.c_float)),
+        ("M1", C.POINTER(C.c_float)),
+        ("XYZ1", C.POINTER(C.c_float)),
+        ("T", C.POINTER(C.c_uint8)),
+        ("status", C.POINTER(C.c_int32)),
+    ]
+
+
 class SwTiming(C.Structure):
     _fields_ = [
         ("seed_ms", C.c_float),

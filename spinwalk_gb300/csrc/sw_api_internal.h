@@ -29,8 +29,17 @@ struct Carve {
 // Host image of the small tables, laid out exactly like the device copy.
 struct TableImage {
     std::vector<char> bytes;
-    size_t o_dscale, o_dsplit, o_T1f, o_T2f, o_T1d, o_T2d, o_pXY, o_rf, o_scan, o_te, o_dtp, o_ddeg, o_gtp,
-        o_gx, o_gy, o_gz;
+    static constexpr size_t kUnset = ~size_t(0);
+    size_t o_dscale = kUnset, o_dsplit = kUnset, o_T1f = kUnset, o_T2f = kUnset, o_T1d = kUnset,
+           o_T2d = kUnset, o_pXY = kUnset, o_rf = kUnset, o_scan = kUnset, o_te = kUnset,
+           o_dtp = kUnset, o_ddeg = kUnset, o_gtp = kUnset, o_gx = kUnset, o_gy = kUnset,
+           o_gz = kUnset;
+    bool complete() const {
+        for (size_t o : {o_dscale, o_dsplit, o_T1f, o_T2f, o_T1d, o_T2d, o_pXY, o_rf, o_scan,
+                         o_te, o_dtp, o_ddeg, o_gtp, o_gx, o_gy, o_gz})
+            if (o == kUnset) return false;
+        return true;
+    }
     template <typename T>
     size_t put(const T *src, size_t n) {
         size_t off = (bytes.size() + 15) & ~size_t(15);
@@ -59,6 +68,9 @@ void build_tables(const sw_params *p, const sw_sequence *q, TableImage &im);
 DevTables dev_tables(const TableImage &im, const char *d);
 // base == nullptr: only measures (Layout::bytes).
 Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl);
+// The current device's logf tables (built and uploaded on first use); {nullptr, nullptr} and
+// sw_last_error() set on failure.
+LogfTables device_logf_tables();
 
 }  // namespace api
 }  // namespace sw

@@ -201,6 +201,71 @@ __device__ __forceinline__ int64_t voxel_coord(double v, double s2g, float s2g_f
 }
 
 // ------------------------------------------------------------------------------------------
+// One attempted move of a spin (src/sim/kernels.cu:130-170), shared by the walk kernels
+// ------------------------------------------------------------------------------------------
+enum MoveResult { kMoveAccepted = 0, kMoveRejected = 1, kMoveLost = 2, kMoveOOB = 3 };
+
+struct WalkRegs {
+    double xo[3];             // last accepted position
+    int64_t ind_old;
+    uint32_t ts_old;          // substrate of the last accepted voxel
+    float field;              // its field (deg per step)
+    double dscale;            // its step std-dev
+    uint4 dsp;                // dscale split for mul_fd
+    uint32_t itr;             // consecutive rejected moves
+    uint32_t nh, nc, uh, uc;  // ring buffer heads / counts
+};
+
+// Draws three deviates (when the substrate diffuses), wraps at the FoV, looks the voxel up and
+// applies the permeability test. On acceptance xn holds the new position and the voxel state in
+// w is updated; w.xo is left to the caller (it commits xn after the Bloch events).
+__device__ __forceinline__ int walk_move(WalkRegs &w, double (&xn)[3], const DevParams &P,
+                                         const DevTables &Tb, const uint2 *__restrict__ vox,
+                                         const float *nb, const float *ub) {
+    xn[0] = w.xo[0];
+    xn[1] = w.xo[1];
+    xn[2] = w.xo[2];
+    if (w.dscale != 0.) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float g = nb[w.nh];
+            w.nh = (w.nh + 1 == kNormBuf) ? 0 : w.nh + 1;
+            const double rnd = w.dsp.w ? mul_fd(g, w.dsp.x, w.dsp.y, (int)w.dsp.z)
+                                       : f2d_exact(g) * w.dscale;
+            double v = w.xo[i] + rnd;
+            if (dneg(v))
+                v += P.cross_fov ? P.fov[i] : 2 * fabs(rnd);
+            else if (dge_pos(v, P.fov[i]))
+                v -= P.cross_fov ? P.fov[i] : 2 * fabs(rnd);
+            xn[i] = v;
+        }
+        w.nc -= 3;
+    }
+    const int64_t ind = voxel_coord(xn[0], P.s2g[0], P.s2g_f[0]) * P.nynz +
+                        voxel_coord(xn[1], P.s2g[1], P.s2g_f[1]) * P.nz +
+                        voxel_coord(xn[2], P.s2g[2], P.s2g_f[2]);
+    if (ind >= P.matrix_length || ind < 0) return kMoveOOB;
+    if (ind != w.ind_old) {
+        const uint2 v = __ldg(vox + ind);
+        const uint32_t ts = v.y;
+        if (ts != w.ts_old) {
+            const float u = ub[w.uh];
+            w.uh = (w.uh + 1 == kUnifBuf) ? 0 : w.uh + 1;
+            w.uc--;
+            if (u >= __ldg(Tb.pXY + w.ts_old * P.n_substrate + ts))
+                return (uint64_t)(w.itr++) > P.max_iterations ? kMoveLost : kMoveRejected;
+            w.ts_old = ts;
+        }
+        w.ind_old = ind;
+        w.field = __uint_as_float(v.x);
+        w.dscale = __ldg(Tb.dscale + w.ts_old);
+        w.dsp = __ldg(reinterpret_cast<const uint4 *>(Tb.dsplit) + w.ts_old);
+    }
+    w.itr = 0;
+    return kMoveAccepted;
+}
+
+// ------------------------------------------------------------------------------------------
 // Bloch primitives, float path (src/sim/kernels.cuh:82-230, kernels.cu:45-52)
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ void xrot_f(float s, float c, const float *a, float *b) {

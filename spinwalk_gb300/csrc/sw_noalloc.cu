@@ -91,6 +91,7 @@ extern "C" int sw_sim_device_noalloc(const sw_params *p, const sw_sequence *q,
 
     TableImage im;
     build_tables(p, q, im);
+    if (!im.complete()) return fail(SW_ERR_INVALID, "internal error: incomplete parameter tables");
     const size_t need = layout(nullptr, p->n_spins, p->matrix_length, im.bytes.size(), false).bytes;
     const size_t avail = SW_NOALLOC_SCRATCH_BYTES - R.work_offset;
     if (need > avail)

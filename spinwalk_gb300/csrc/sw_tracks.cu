@@ -1,0 +1,561 @@
+// sw_sim_tracks: one walk, many Bloch tracks.
+//
+// The reference re-runs the complete walk for every scale of a config (src/sim/monte_carlo.cu:
+// 273-337) even when only the RF phase changes (phase-cycling scales) and for every DUMMY_SCAN
+// setting. The trajectory (positions, voxels, substrates, rejected moves) depends only on the
+// seeds, XYZ0, the phantom and the tissue tables -- not on RF phases, flip angles or the number
+// of scans (the forced voxel reload at a scan start never draws a uniform: the spin is still in a
+// voxel of its own substrate). So every such instance ("track") can ride on ONE walk.
+//
+// Tracks are grouped by RF configuration (scan-start phase cycling, per-pulse flip angles and
+// phases). Per spin and group only the magnetisation m_g is stored. Within a scan, all groups
+// share the accumulated phase (`acc`) and its event times, because dephasing, gradients and the
+// RF/echo times are common. A track = (group, recording scan d): before scan d it is m_g; in
+// scan d it records echoes; from its first echo on, its magnetisation (m_rec) and phase
+// (acc_rec, reset at each echo) diverge from the group's -- one extra state per group in a
+// recording scan. A track ends with its recording scan. Every float operation is the one the
+// plain kernel performs for that instance, so each track is bit-identical to sw_sim on it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "spinwalk_gpu.h"
+#include "sw_api_internal.h"
+#include "sw_device.cuh"
+#include "sw_host.h"
+#include "sw_kernels.h"
+
+namespace sw {
+
+struct GroupTables {
+    uint32_t n_groups, n_tracks, max_ds, n_rf;
+    const RfOp *scan_rf;      // [n_groups][max_ds + 1]
+    const RfOp *rf;           // [n_groups][n_rf]
+    const int32_t *rec;       // [n_groups][max_ds + 1]: track recording in that scan, or -1
+    const uint32_t *last_ds;  // [n_groups]
+    const uint32_t *rec_any;  // [max_ds + 1]: some track records in that scan
+    const int32_t *track_nd;  // [n_tracks]
+    float *const *M1;         // [n_tracks] -> [n][n_TE][3]
+    float *const *XYZ1;       // [n_tracks] -> [n][3]
+    uint8_t *const *T;        // [n_tracks] -> [n][n_TE]
+    int32_t *const *status;   // [n_tracks] -> [n]
+};
+
+struct GroupState {
+    float *mg;                // [3][n_groups][n]
+    float *mr;                // [3][n_groups][n]
+    float *acc_rec;           // [n]
+    uint32_t *tp_old_rec;     // [n]
+    uint32_t *rec_started;    // [n]
+};
+
+// dephase_relax_f split in two: the trigonometry and exponentials depend only on the shared
+// phase, substrate and interval, so they are computed once and applied to every group.
+struct RelaxOp {
+    float s, c, e1, e2;
+    bool relax;
+};
+__device__ __forceinline__ RelaxOp make_relax(float phase, float T1, float T2, float dt_s) {
+    RelaxOp r;
+    const float ang = (float)((double)phase * kDeg2Rad);
+    sincosf(ang, &r.s, &r.c);
+    r.relax = T1 >= 0 && T2 >= 0;
+    r.e1 = r.relax ? (float)exp((double)(-dt_s / T1)) : 0.f;
+    r.e2 = r.relax ? (float)exp((double)(-dt_s / T2)) : 0.f;
+    return r;
+}
+__device__ __forceinline__ void apply_relax(const RelaxOp &r, const float *a, float *b) {
+    zrot_f(r.s, r.c, a, b);
+    if (r.relax) {
+        b[0] = b[0] * r.e2;
+        b[1] = b[1] * r.e2;
+        b[2] = (float)(1. + (double)r.e1 * ((double)b[2] - 1.));
+    }
+}
+
+__device__ __forceinline__ void load_m(const float *base, size_t plane, size_t idx, float *m) {
+    m[0] = base[idx];
+    m[1] = base[plane + idx];
+    m[2] = base[2 * plane + idx];
+}
+__device__ __forceinline__ void store_m(float *base, size_t plane, size_t idx, const float *m) {
+    base[idx] = m[0];
+    base[plane + idx] = m[1];
+    base[2 * plane + idx] = m[2];
+}
+
+__global__ void k_groups_init(DevParams P, GroupTables GT, GroupState GS, const SpinState S,
+                              const float *__restrict__ M0, const float *__restrict__ XYZ0) {
+    const uint32_t spin = blockIdx.x * blockDim.x + threadIdx.x;
+    if (spin >= P.n_spins) return;
+    const size_t n = P.n_spins, plane = (size_t)GT.n_groups * n;
+    const float m[3] = {M0[3 * (size_t)spin], M0[3 * (size_t)spin + 1], M0[3 * (size_t)spin + 2]};
+    for (uint32_t g = 0; g < GT.n_groups; g++) store_m(GS.mg, plane, (size_t)g * n + spin, m);
+    GS.acc_rec[spin] = 0.f;
+    GS.tp_old_rec[spin] = 0;
+    GS.rec_started[spin] = 0;
+    // a start outside the phantom ends every track at once (status set by k_init)
+    const uint32_t fl = S.flags[spin];
+    if (fl & kFlagDone) {
+        for (uint32_t t = 0; t < GT.n_tracks; t++) {
+            float *x = GT.XYZ1[t] + 3 * (size_t)spin;
+            x[0] = XYZ0[3 * (size_t)spin];
+            x[1] = XYZ0[3 * (size_t)spin + 1];
+            x[2] = XYZ0[3 * (size_t)spin + 2];
+            if (GT.status[t]) GT.status[t][spin] = (int32_t)((fl >> 16) & 0xffu);
+        }
+    }
+}
+
+__device__ __forceinline__ bool walk_groups_spin(const uint32_t spin, uint32_t flags,
+                                                 const DevParams &P, const DevTables &Tb,
+                                                 const GroupTables &GT, const GroupState &GS,
+                                                 const uint2 *__restrict__ vox,
+                                                 const SpinState &S, const RngState &G) {
+    const size_t n = P.n_spins, plane = (size_t)GT.n_groups * n;
+    WalkRegs w;
+    w.xo[0] = S.x[spin]; w.xo[1] = S.y[spin]; w.xo[2] = S.z[spin];
+    w.ind_old = S.ind_old[spin];
+    w.ts_old = flags & 0xffu;
+    w.field = S.field[spin];
+    w.dscale = __ldg(Tb.dscale + w.ts_old);
+    w.dsp = __ldg(reinterpret_cast<const uint4 *>(Tb.dsplit) + w.ts_old);
+    w.itr = S.itr[spin];
+    w.nh = G.nhead[spin]; w.nc = G.ncnt[spin]; w.uh = G.uhead[spin]; w.uc = G.ucnt[spin];
+    const float *nb = G.nbuf + (size_t)spin * kNormBuf;
+    const float *ub = G.ubuf + (size_t)spin * kUnifBuf;
+
+    float acc = S.acc[spin], acc_rec = GS.acc_rec[spin];
+    uint32_t tp = S.tp[spin], tp_old = S.tp_old[spin], tp_old_rec = GS.tp_old_rec[spin];
+    uint32_t ds = S.ds[spin];
+    bool rec_started = GS.rec_started[spin] != 0;
+    uint32_t ctr = S.ctr[spin], ctr2 = S.ctr2[spin];
+    uint32_t c_rf = ctr & 0xffffu, c_te = ctr >> 16, c_dph = ctr2 & 0xffffu, c_grad = ctr2 >> 16;
+    bool started = (flags & kFlagStarted) != 0;
+
+    constexpr uint32_t NONE = 0xffffffffu;
+    const uint32_t span = GT.max_ds + 1;
+    bool rec_scan = ds <= GT.max_ds && GT.rec_any[ds] != 0;
+    uint32_t t_rf = c_rf < P.n_RF ? (uint32_t)Tb.rf[c_rf].tp : NONE;
+    uint32_t t_te = (rec_scan && c_te < P.n_TE) ? (uint32_t)Tb.te_tp[c_te] : NONE;
+    uint32_t t_dph = c_dph < P.n_dephasing ? (uint32_t)Tb.dph_tp[c_dph] : NONE;
+    uint32_t t_grad = c_grad < P.n_gradient ? (uint32_t)Tb.grad_tp[c_grad] : NONE;
+
+    int status = -1;
+    for (;;) {
+        if (!started) {
+            if (ds > GT.max_ds) { status = SW_SPIN_OK; break; }
+            for (uint32_t g = 0; g < GT.n_groups; g++) {         // kernels.cu:110-120
+                if (GT.last_ds[g] < ds) continue;
+                float a[3], b[3];
+                const size_t idx = (size_t)g * n + spin;
+                load_m(GS.mg, plane, idx, a);
+                rf_f(GT.scan_rf[(size_t)g * span + ds], a, b);
+                store_m(GS.mg, plane, idx, b);
+            }
+            w.ind_old = P.matrix_length + 1;
+            tp = tp_old = 0;
+            c_rf = 1; c_te = 0; c_dph = 0; c_grad = 0;
+            acc = 0.f;
+            acc_rec = 0.f;
+            tp_old_rec = 0;
+            rec_started = false;
+            rec_scan = GT.rec_any[ds] != 0;
+            started = true;
+            t_rf = 1 < P.n_RF ? (uint32_t)Tb.rf[1].tp : NONE;
+            t_te = (rec_scan && P.n_TE > 0) ? (uint32_t)Tb.te_tp[0] : NONE;
+            t_dph = P.n_dephasing > 0 ? (uint32_t)Tb.dph_tp[0] : NONE;
+            t_grad = P.n_gradient > 0 ? (uint32_t)Tb.grad_tp[0] : NONE;
+        }
+        if (tp >= P.n_timepoints) {                                 // kernels.cu:225-231
+            const float te = (float)((double)((tp - tp_old) * (uint32_t)P.timestep_us) * 1e-6);
+            const RelaxOp r = make_relax(acc, __ldg(Tb.T1f + w.ts_old), __ldg(Tb.T2f + w.ts_old), te);
+            for (uint32_t g = 0; g < GT.n_groups; g++) {
+                if (GT.last_ds[g] < ds) continue;
+                float a[3], b[3];
+                const size_t idx = (size_t)g * n + spin;
+                load_m(GS.mg, plane, idx, a);
+                apply_relax(r, a, b);
+                store_m(GS.mg, plane, idx, b);
+                const int32_t t = GT.rec[(size_t)g * span + ds];
+                if (t >= 0) {                                       // track t ends here
+                    float *x = GT.XYZ1[t] + 3 * (size_t)spin;
+                    x[0] = (float)w.xo[0]; x[1] = (float)w.xo[1]; x[2] = (float)w.xo[2];
+                    if (GT.status[t]) GT.status[t][spin] = SW_SPIN_OK;
+                }
+            }
+            ds++;
+            started = false;
+            continue;
+        }
+        if ((w.dscale != 0. && w.nc < 3) || w.uc == 0) break;       // buffers low: pause
+
+        double xn[3];
+        const int mv = walk_move(w, xn, P, Tb, vox, nb, ub);
+        if (mv == kMoveRejected) continue;
+        if (mv == kMoveLost) { status = SW_SPIN_LOST; break; }
+        if (mv == kMoveOOB) { status = SW_SPIN_OOB; break; }
+
+        acc += w.field;                                             // kernels.cu:171
+        if (rec_started) acc_rec += w.field;
+        if (tp == t_dph) {                                          // kernels.cu:175-178
+            const float inc = (float)spin * __ldg(Tb.dph_deg + c_dph) / (float)P.n_spins;
+            acc += inc;
+            if (rec_started) acc_rec += inc;
+            c_dph++;
+            t_dph = c_dph < P.n_dephasing ? (uint32_t)Tb.dph_tp[c_dph] : NONE;
+        }
+        if (tp == t_grad) {                                         // kernels.cu:181-187
+            const double g = ((double)__ldg(Tb.gx + c_grad) * xn[0] +
+                              (double)__ldg(Tb.gy + c_grad) * xn[1] +
+                              (double)__ldg(Tb.gz + c_grad) * xn[2]) *
+                             1e-3 * (double)P.timestep_us * 1e-6 * kGamma * kRad2Deg;
+            acc = (float)((double)acc + g);
+            if (rec_started) acc_rec = (float)((double)acc_rec + g);
+            c_grad++;
+            t_grad = c_grad < P.n_gradient ? (uint32_t)Tb.grad_tp[c_grad] : NONE;
+        }
+        if (tp == t_rf) {                                           // kernels.cu:190-199
+            const float T1 = __ldg(Tb.T1f + w.ts_old), T2 = __ldg(Tb.T2f + w.ts_old);
+            const float te = (float)((double)((tp - tp_old) * (uint32_t)P.timestep_us) * 1e-6);
+            const RelaxOp r = make_relax(acc, T1, T2, te);
+            RelaxOp rr = r;
+            if (rec_started) {
+                const float ter = (float)((double)((tp - tp_old_rec) * (uint32_t)P.timestep_us) * 1e-6);
+                rr = make_relax(acc_rec, T1, T2, ter);
+            }
+            for (uint32_t g = 0; g < GT.n_groups; g++) {
+                if (GT.last_ds[g] < ds) continue;
+                const RfOp op = GT.rf[(size_t)g * P.n_RF + c_rf];
+                float a[3], b[3];
+                const size_t idx = (size_t)g * n + spin;
+                load_m(GS.mg, plane, idx, a);
+                apply_relax(r, a, b);
+                rf_f(op, b, a);
+                store_m(GS.mg, plane, idx, a);
+                if (rec_started && GT.rec[(size_t)g * span + ds] >= 0) {
+                    load_m(GS.mr, plane, idx, a);
+                    apply_relax(rr, a, b);
+                    rf_f(op, b, a);
+                    store_m(GS.mr, plane, idx, a);
+                }
+            }
+            acc = 0.f;
+            tp_old = tp;
+            if (rec_started) {
+                acc_rec = 0.f;
+                tp_old_rec = tp;
+            }
+            c_rf++;
+            t_rf = c_rf < P.n_RF ? (uint32_t)Tb.rf[c_rf].tp : NONE;
+        }
+        if (tp == t_te) {                                           // kernels.cu:202-215
+            const float T1 = __ldg(Tb.T1f + w.ts_old), T2 = __ldg(Tb.T2f + w.ts_old);
+            const float te = (float)((double)((tp - (rec_started ? tp_old_rec : tp_old)) *
+                                              (uint32_t)P.timestep_us) * 1e-6);
+            const RelaxOp r = make_relax(rec_started ? acc_rec : acc, T1, T2, te);
+            for (uint32_t g = 0; g < GT.n_groups; g++) {
+                const int32_t t = GT.rec[(size_t)g * span + ds];
+                if (t < 0) continue;
+                float a[3], b[3];
+                const size_t idx = (size_t)g * n + spin;
+                load_m(rec_started ? GS.mr : GS.mg, plane, idx, a);
+                apply_relax(r, a, b);
+                store_m(GS.mr, plane, idx, b);
+                float *m1 = GT.M1[t] + 3 * ((size_t)spin * P.n_TE + c_te);
+                m1[0] = b[0]; m1[1] = b[1]; m1[2] = b[2];
+                GT.T[t][(size_t)spin * P.n_TE + c_te] = (uint8_t)w.ts_old;
+            }
+            acc_rec = 0.f;
+            tp_old_rec = tp;
+            rec_started = true;
+            c_te++;
+            t_te = c_te < P.n_TE ? (uint32_t)Tb.te_tp[c_te] : NONE;
+        }
+        w.xo[0] = xn[0]; w.xo[1] = xn[1]; w.xo[2] = xn[2];
+        tp++;
+    }
+    if (status > 0) {            // lost / out of bounds: every track still running ends here
+        for (uint32_t t = 0; t < GT.n_tracks; t++) {
+            if ((uint32_t)GT.track_nd[t] < ds) continue;
+            float *x = GT.XYZ1[t] + 3 * (size_t)spin;
+            x[0] = (float)w.xo[0]; x[1] = (float)w.xo[1]; x[2] = (float)w.xo[2];
+            if (GT.status[t]) GT.status[t][spin] = status;
+        }
+    }
+    S.x[spin] = w.xo[0]; S.y[spin] = w.xo[1]; S.z[spin] = w.xo[2];
+    S.acc[spin] = acc;
+    GS.acc_rec[spin] = acc_rec;
+    GS.tp_old_rec[spin] = tp_old_rec;
+    GS.rec_started[spin] = rec_started ? 1u : 0u;
+    S.field[spin] = w.field;
+    S.ind_old[spin] = w.ind_old;
+    S.tp[spin] = tp; S.tp_old[spin] = tp_old; S.ds[spin] = ds; S.itr[spin] = w.itr;
+    S.ctr[spin] = c_rf | (c_te << 16);
+    S.ctr2[spin] = c_dph | (c_grad << 16);
+    G.nhead[spin] = w.nh; G.ncnt[spin] = w.nc; G.uhead[spin] = w.uh; G.ucnt[spin] = w.uc;
+    uint32_t nf = w.ts_old | (started ? kFlagStarted : 0u);
+    if (status >= 0) nf |= kFlagDone | ((uint32_t)status << 16);
+    S.flags[spin] = nf;
+    return status < 0;
+}
+
+__global__ void __launch_bounds__(256)
+    k_walk_groups(DevParams P, DevTables Tb, GroupTables GT, GroupState GS,
+                  const uint2 *__restrict__ vox, SpinState S, RngState G, uint32_t *active) {
+    const uint32_t spin = blockIdx.x * blockDim.x + threadIdx.x;
+    bool still = false;
+    if (spin < P.n_spins) {
+        const uint32_t flags = S.flags[spin];
+        if (!(flags & kFlagDone)) still = walk_groups_spin(spin, flags, P, Tb, GT, GS, vox, S, G);
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, still);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(active, (uint32_t)__popc(b));
+}
+
+}  // namespace sw
+
+namespace {
+
+using namespace sw::api;
+
+struct TracksCtx {
+    std::mutex mu;
+    char *buf = nullptr;
+    size_t size = 0;
+};
+TracksCtx g_tctx[64];
+
+std::vector<float> rf_array(const float *override_, const float *base, uint32_t n) {
+    const float *src = override_ ? override_ : base;
+    return std::vector<float>(src, src + n);
+}
+
+}  // namespace
+
+extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
+                             const sw_track *tracks, uint32_t n_tracks, const float *pFieldMap,
+                             const uint8_t *pMask, const float *M0, const float *XYZ0) {
+    int rc = check_args(param, seq);
+    if (rc) return rc;
+    if (!tracks || n_tracks == 0) return fail(SW_ERR_INVALID, "no tracks");
+    if (param->enRecordTrajectory) return fail(SW_ERR_INVALID, "tracks do not record trajectories");
+    const size_t n = param->n_spins, nte = seq->n_TE, ml = (size_t)param->matrix_length;
+    if (n == 0) return SW_OK;
+    if (!pMask || !M0 || !XYZ0) return fail(SW_ERR_INVALID, "null host buffer");
+    for (uint32_t t = 0; t < n_tracks; t++) {
+        if (tracks[t].n_dummy_scan < 0) return fail(SW_ERR_INVALID, "track n_dummy_scan < 0");
+        if (!tracks[t].XYZ1 || (nte && (!tracks[t].M1 || !tracks[t].T)))
+            return fail(SW_ERR_INVALID, "track output buffer missing");
+    }
+    // ---- group tracks by RF configuration ----
+    using Key = std::tuple<float, float, std::vector<float>, std::vector<float>>;
+    std::map<Key, uint32_t> gid;
+    std::vector<Key> groups;
+    std::vector<uint32_t> tgroup(n_tracks);
+    uint32_t max_ds = 0;
+    for (uint32_t t = 0; t < n_tracks; t++) {
+        Key k{tracks[t].linear_phase_cycling, tracks[t].quadratic_phase_cycling,
+              rf_array(tracks[t].RF_FA_deg, seq->RF_FA_deg, seq->n_RF),
+              rf_array(tracks[t].RF_PH_deg, seq->RF_PH_deg, seq->n_RF)};
+        auto it = gid.find(k);
+        if (it == gid.end()) {
+            it = gid.emplace(k, (uint32_t)groups.size()).first;
+            groups.push_back(k);
+        }
+        tgroup[t] = it->second;
+        max_ds = std::max(max_ds, (uint32_t)tracks[t].n_dummy_scan);
+    }
+    const uint32_t ng = (uint32_t)groups.size(), span = max_ds + 1;
+    std::vector<int32_t> rec((size_t)ng * span, -1), track_nd(n_tracks);
+    std::vector<uint32_t> last_ds(ng, 0), rec_any(span, 0);
+    for (uint32_t t = 0; t < n_tracks; t++) {
+        const uint32_t d = (uint32_t)tracks[t].n_dummy_scan, g = tgroup[t];
+        if (rec[(size_t)g * span + d] >= 0)
+            return fail(SW_ERR_INVALID, "two tracks with the same RF configuration and DUMMY_SCAN");
+        rec[(size_t)g * span + d] = (int32_t)t;
+        last_ds[g] = std::max(last_ds[g], d);
+        rec_any[d] = 1;
+        track_nd[t] = (int32_t)d;
+    }
+    // per-group RF operations: parameters::prepare's c/s and the scan-start phases of each group
+    std::vector<sw::RfOp> scan_rf((size_t)ng * span), rfops((size_t)ng * seq->n_RF);
+    for (uint32_t g = 0; g < ng; g++) {
+        const auto &[lin, quad, fa, ph] = groups[g];
+        sw_params pg = *param;
+        pg.linear_phase_cycling = lin;
+        pg.quadratic_phase_cycling = quad;
+        pg.n_dummy_scan = (int32_t)max_ds;
+        pg.c = cosf(fa[0] * sw::kDeg2Rad);
+        pg.s = sinf(fa[0] * sw::kDeg2Rad);
+        sw_sequence qg = *seq;
+        qg.RF_FA_deg = fa.data();
+        qg.RF_PH_deg = ph.data();
+        std::vector<sw::RfOp> a, b;
+        sw::build_scan_rf(&pg, &qg, a);
+        sw::build_rf(&pg, &qg, b);
+        std::copy(a.begin(), a.end(), scan_rf.begin() + (size_t)g * span);
+        std::copy(b.begin(), b.end(), rfops.begin() + (size_t)g * seq->n_RF);
+    }
+    sw_params pw = *param;            // the walk: the longest track
+    pw.n_dummy_scan = (int32_t)max_ds;
+
+    TableImage im;
+    build_tables(&pw, seq, im);
+    if (!im.complete()) return fail(SW_ERR_INVALID, "internal error: incomplete parameter tables");
+    TableImage gi;                    // group tables
+    const size_t o_scan = gi.put(scan_rf.data(), scan_rf.size());
+    const size_t o_rf = gi.put(rfops.data(), rfops.size());
+    const size_t o_rec = gi.put(rec.data(), rec.size());
+    const size_t o_last = gi.put(last_ds.data(), last_ds.size());
+    const size_t o_any = gi.put(rec_any.data(), rec_any.size());
+    const size_t o_nd = gi.put(track_nd.data(), track_nd.size());
+
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return fail(SW_ERR_CUDA, "no current CUDA device");
+    }
+    TracksCtx &C = g_tctx[dev];
+    std::lock_guard<std::mutex> lk(C.mu);
+
+    // ---- one device allocation: inputs, per-track outputs, pointer arrays, walk workspace ----
+    size_t off = 0;
+    auto slot = [&](size_t bytes) {
+        const size_t o = off;
+        off = (off + bytes + 255) & ~size_t(255);
+        return o;
+    };
+    const bool has_field = param->fieldmap_exist && pFieldMap;
+    const size_t o_mask = slot(ml), o_field = slot(has_field ? ml * 4 : 0), o_M0 = slot(n * 12),
+                 o_XYZ0 = slot(n * 12), o_scratch_xyz = slot(n * 12), o_scratch_st = slot(n * 4),
+                 o_tab = slot(im.bytes.size()), o_gtab = slot(gi.bytes.size()),
+                 o_ptrs = slot(4 * sizeof(void *) * n_tracks),
+                 o_mg = slot(2 * 3 * sizeof(float) * (size_t)ng * n),
+                 o_gs = slot(12 * n);
+    std::vector<size_t> o_M1(n_tracks), o_X(n_tracks), o_T(n_tracks), o_S(n_tracks);
+    for (uint32_t t = 0; t < n_tracks; t++) {
+        o_M1[t] = slot(n * nte * 12);
+        o_X[t] = slot(n * 12);
+        o_T[t] = slot(n * nte);
+        o_S[t] = slot(n * 4);
+    }
+    const Layout Lm = layout(nullptr, n, param->matrix_length, 0, false);
+    const size_t o_ws = slot(Lm.bytes);
+    if (off > C.size) {
+        if (C.buf) cudaFree(C.buf);
+        C.buf = nullptr;
+        C.size = 0;
+        cudaError_t e = cudaMalloc(&C.buf, off);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SW_ERR_NOMEM, "tracks buffers of " + std::to_string(off >> 20) + " MiB: " +
+                                          cudaGetErrorString(e));
+        }
+        C.size = off;
+    }
+    char *d = C.buf;
+    cudaStream_t st = nullptr;
+#define TR_CUDA(call)                                                                      \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            cudaGetLastError();                                                            \
+            return fail(SW_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));  \
+        }                                                                                  \
+    } while (0)
+    TR_CUDA(cudaMemcpyAsync(d + o_mask, pMask, ml, cudaMemcpyHostToDevice, st));
+    if (has_field) TR_CUDA(cudaMemcpyAsync(d + o_field, pFieldMap, ml * 4, cudaMemcpyHostToDevice, st));
+    TR_CUDA(cudaMemcpyAsync(d + o_M0, M0, n * 12, cudaMemcpyHostToDevice, st));
+    TR_CUDA(cudaMemcpyAsync(d + o_XYZ0, XYZ0, n * 12, cudaMemcpyHostToDevice, st));
+    TR_CUDA(cudaMemcpyAsync(d + o_tab, im.bytes.data(), im.bytes.size(), cudaMemcpyHostToDevice, st));
+    TR_CUDA(cudaMemcpyAsync(d + o_gtab, gi.bytes.data(), gi.bytes.size(), cudaMemcpyHostToDevice, st));
+    std::vector<void *> ptrs(4 * (size_t)n_tracks);
+    for (uint32_t t = 0; t < n_tracks; t++) {
+        ptrs[t] = d + o_M1[t];
+        ptrs[n_tracks + t] = d + o_X[t];
+        ptrs[2 * n_tracks + t] = d + o_T[t];
+        ptrs[3 * n_tracks + t] = tracks[t].status ? (void *)(d + o_S[t]) : nullptr;
+        if (nte) {     // unreached echoes keep the caller's contents, as in the reference
+            TR_CUDA(cudaMemcpyAsync(d + o_M1[t], tracks[t].M1, n * nte * 12, cudaMemcpyHostToDevice, st));
+            TR_CUDA(cudaMemcpyAsync(d + o_T[t], tracks[t].T, n * nte, cudaMemcpyHostToDevice, st));
+        }
+    }
+    TR_CUDA(cudaMemcpyAsync(d + o_ptrs, ptrs.data(), ptrs.size() * sizeof(void *), cudaMemcpyHostToDevice, st));
+
+    const Layout L = layout(d + o_ws, n, param->matrix_length, 0, false);
+    const sw::DevParams P = dev_params(&pw, seq);
+    const sw::DevTables Tb = dev_tables(im, d + o_tab);
+    sw::GroupTables GT;
+    GT.n_groups = ng;
+    GT.n_tracks = n_tracks;
+    GT.max_ds = max_ds;
+    GT.n_rf = seq->n_RF;
+    GT.scan_rf = reinterpret_cast<const sw::RfOp *>(d + o_gtab + o_scan);
+    GT.rf = reinterpret_cast<const sw::RfOp *>(d + o_gtab + o_rf);
+    GT.rec = reinterpret_cast<const int32_t *>(d + o_gtab + o_rec);
+    GT.last_ds = reinterpret_cast<const uint32_t *>(d + o_gtab + o_last);
+    GT.rec_any = reinterpret_cast<const uint32_t *>(d + o_gtab + o_any);
+    GT.track_nd = reinterpret_cast<const int32_t *>(d + o_gtab + o_nd);
+    void **dp = reinterpret_cast<void **>(d + o_ptrs);
+    GT.M1 = reinterpret_cast<float *const *>(dp);
+    GT.XYZ1 = reinterpret_cast<float *const *>(dp + n_tracks);
+    GT.T = reinterpret_cast<uint8_t *const *>(dp + 2 * (size_t)n_tracks);
+    GT.status = reinterpret_cast<int32_t *const *>(dp + 3 * (size_t)n_tracks);
+    sw::GroupState GS;
+    GS.mg = reinterpret_cast<float *>(d + o_mg);
+    GS.mr = GS.mg + 3 * (size_t)ng * n;
+    GS.acc_rec = reinterpret_cast<float *>(d + o_gs);
+    GS.tp_old_rec = reinterpret_cast<uint32_t *>(d + o_gs + 4 * n);
+    GS.rec_started = reinterpret_cast<uint32_t *>(d + o_gs + 8 * n);
+
+    const sw::LogfTables LT = sw::api::device_logf_tables();
+    if (!LT.bitmap) return fail(SW_ERR_CUDA, "logf tables unavailable");
+    sw::Outputs O{nullptr, nullptr, reinterpret_cast<float *>(d + o_scratch_xyz), nullptr,
+                  reinterpret_cast<int32_t *>(d + o_scratch_st)};
+    TR_CUDA(cudaMemsetAsync(L.active, 0, 2 * sizeof(uint32_t), st));
+    TR_CUDA(sw::launch_pack(reinterpret_cast<const uint8_t *>(d + o_mask),
+                            has_field ? reinterpret_cast<const float *>(d + o_field) : nullptr,
+                            L.vox, param->matrix_length, param->n_substrate, L.active + 1, st));
+    TR_CUDA(sw::launch_seed(P, L.G, st));
+    TR_CUDA(sw::launch_init(P, Tb, L.vox, reinterpret_cast<const float *>(d + o_M0),
+                            reinterpret_cast<const float *>(d + o_XYZ0), L.S, O, false, st));
+    sw::k_groups_init<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        P, GT, GS, L.S, reinterpret_cast<const float *>(d + o_M0),
+        reinterpret_cast<const float *>(d + o_XYZ0));
+    TR_CUDA(cudaGetLastError());
+    uint32_t h = 0;
+    TR_CUDA(cudaMemcpyAsync(&h, L.active + 1, 4, cudaMemcpyDeviceToHost, st));
+    TR_CUDA(cudaStreamSynchronize(st));
+    if (h) return fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate");
+    const uint64_t steps = (uint64_t)pw.n_timepoints * (uint64_t)(max_ds + 1);
+    const uint64_t max_rounds = 64 + steps * (param->max_iterations + 2);
+    for (uint64_t round = 0;; round++) {
+        if (round >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
+        TR_CUDA(cudaMemsetAsync(L.active, 0, 4, st));
+        TR_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
+        sw::k_walk_groups<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P, Tb, GT, GS, L.vox, L.S,
+                                                                       L.G, L.active);
+        TR_CUDA(cudaGetLastError());
+        TR_CUDA(cudaMemcpyAsync(&h, L.active, 4, cudaMemcpyDeviceToHost, st));
+        TR_CUDA(cudaStreamSynchronize(st));
+        if (h == 0) break;
+    }
+    for (uint32_t t = 0; t < n_tracks; t++) {
+        if (nte) {
+            TR_CUDA(cudaMemcpyAsync(tracks[t].M1, d + o_M1[t], n * nte * 12, cudaMemcpyDeviceToHost, st));
+            TR_CUDA(cudaMemcpyAsync(tracks[t].T, d + o_T[t], n * nte, cudaMemcpyDeviceToHost, st));
+        }
+        TR_CUDA(cudaMemcpyAsync(tracks[t].XYZ1, d + o_X[t], n * 12, cudaMemcpyDeviceToHost, st));
+        if (tracks[t].status)
+            TR_CUDA(cudaMemcpyAsync(tracks[t].status, d + o_S[t], n * 4, cudaMemcpyDeviceToHost, st));
+    }
+    TR_CUDA(cudaStreamSynchronize(st));
+#undef TR_CUDA
+    return SW_OK;
+}

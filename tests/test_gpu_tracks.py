@@ -1,0 +1,69 @@
+"""sw_sim_tracks (one walk, many instances) against independent per-instance runs: each track's
+outputs must equal sw_sim on that instance alone, bit for bit (same device arithmetic), and the
+oracle within the magnetisation tolerance."""
+import copy
+
+import numpy as np
+import pytest
+
+from spinwalk_gb300 import _lib
+from spinwalk_gb300.problem import Problem
+from tests import oracle_lib
+from tests.helpers import bits_equal, load_golden, m_close
+
+pytestmark = pytest.mark.gpu
+
+
+def _instance(pr, t):
+    """The Problem the reference would run for track t."""
+    q = copy.copy(pr)
+    p = type(pr.params)()
+    C = __import__("ctypes")
+    C.memmove(C.byref(p), C.byref(pr.params), C.sizeof(p))
+    p.n_dummy_scan = t["n_dummy_scan"]
+    p.linear_phase_cycling = t.get("linear_phase_cycling", 0.0)
+    p.quadratic_phase_cycling = t.get("quadratic_phase_cycling", 0.0)
+    q.params = p
+    return q
+
+
+@pytest.mark.parametrize("case", ["bssfp_phase_cycling", "se_multi_te", "lost_spins", "pgse_gradients"])
+def test_tracks_equal_independent_runs(case):
+    pr, _ = load_golden(case)
+    tracks = [dict(linear_phase_cycling=lpc, quadratic_phase_cycling=qpc, n_dummy_scan=nd)
+              for lpc in (0.0, 45.0, 180.0) for qpc in (0.0, 7.5) for nd in (0, 2, 3)]
+    outs = _lib.run_tracks(pr, tracks, fill=np.nan)
+    for t, got in zip(tracks, outs):
+        inst = _instance(pr, t)
+        want = _lib.run(inst, fill=np.nan)
+        assert bits_equal(got["M1"], want["M1"]), (case, t)
+        assert bits_equal(got["T"], want["T"]), (case, t)
+        assert bits_equal(got["XYZ1"], want["XYZ1"]), (case, t)
+        assert np.array_equal(got["status"], want["status"]), (case, t)
+    # one track against the oracle
+    t = tracks[-1]
+    o = oracle_lib.run(_instance(pr, t), fill=np.nan)
+    ok, rel = m_close(outs[-1]["M1"], o["M1"])
+    assert ok, rel
+    assert bits_equal(outs[-1]["XYZ1"], o["XYZ1"])
+
+
+def test_tracks_per_pulse_rf_variants():
+    pr, _ = load_golden("se_multi_te")
+    tracks = [dict(n_dummy_scan=1, RF_FA_deg=[90.0, fa], RF_PH_deg=[0.0, ph])
+              for fa in (120.0, 180.0) for ph in (0.0, 90.0, 33.0)]
+    outs = _lib.run_tracks(pr, tracks, fill=np.nan)
+    for t, got in zip(tracks, outs):
+        inst = _instance(pr, t)
+        seq = dict(inst.seq.arrays)
+        from spinwalk_gb300 import abi
+        inst.seq = abi.Sequence(**{**seq, "RF_FA_deg": t["RF_FA_deg"], "RF_PH_deg": t["RF_PH_deg"]})
+        want = _lib.run(inst, fill=np.nan)
+        assert bits_equal(got["M1"], want["M1"]), t
+        assert bits_equal(got["XYZ1"], want["XYZ1"]), t
+
+
+def test_tracks_reject_duplicates():
+    pr, _ = load_golden("gre")
+    with pytest.raises(_lib.SpinWalkError):
+        _lib.run_tracks(pr, [dict(n_dummy_scan=0), dict(n_dummy_scan=0)])

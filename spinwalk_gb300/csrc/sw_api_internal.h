@@ -59,6 +59,8 @@ struct Layout {
     size_t bytes;
 };
 
+// Kernel timing of the last call on this thread (sw_last_timing).
+extern thread_local sw_timing g_timing;
 // Sets sw_last_error() for the calling thread and returns `code`.
 int fail(int code, const std::string &msg);
 // Parameter checks shared by every entry point.

@@ -8,7 +8,8 @@
 // voxel of its own substrate). So every such instance ("track") can ride on ONE walk.
 //
 // Tracks are grouped by RF configuration (scan-start phase cycling, per-pulse flip angles and
-// phases). Per spin and group only the magnetisation m_g is stored. Within a scan, all groups
+// phases). Per spin and group only the magnetisation m_g is stored; the walk kernel logs the Bloch
+// events of each spin and a second kernel applies them with one thread per (group, spin). Within a scan, all groups
 // share the accumulated phase (`acc`) and its event times, because dephasing, gradients and the
 // RF/echo times are common. A track = (group, recording scan d): before scan d it is m_g; in
 // scan d it records echoes; from its first echo on, its magnetisation (m_rec) and phase
@@ -112,12 +113,40 @@ __global__ void k_groups_init(DevParams P, GroupTables GT, GroupState GS, const 
     }
 }
 
-__device__ __forceinline__ bool walk_groups_spin(const uint32_t spin, uint32_t flags,
+// ---- per-spin Bloch event log ----------------------------------------------------------------
+// The walk kernel records, per spin and round, what the Bloch part has to do (scan starts, RF
+// pulses, echoes, scan ends) together with the shared trigonometry/relaxation factors; the Bloch
+// kernel then applies the log with one thread per (group, spin), so the per-group work is
+// coalesced and never diverges with the spins' individual progress.
+enum : uint32_t { kEvScanStart = 1, kEvRf = 2, kEvTe = 3, kEvScanEnd = 4 };
+constexpr uint32_t kLogCap = 8;           // events per spin per round
+
+struct BlochEvent {
+    uint32_t head;            // type | idx << 8 | ts_old << 24   (idx: ds, pulse or echo index)
+    uint32_t ds;              // scan of the event
+    uint32_t flags;           // bit0 r.relax, bit1 rr.relax, bit2 echo phase already started
+    uint32_t pad;
+    float r[4];               // s, c, e1, e2 of the shared phase
+    float rr[4];              // the same for the recording tracks' phase (after their 1st echo)
+    float xo[4];              // scan end: position
+};
+
+__device__ __forceinline__ void put_relax(float *dst, const RelaxOp &r) {
+    dst[0] = r.s; dst[1] = r.c; dst[2] = r.e1; dst[3] = r.e2;
+}
+__device__ __forceinline__ RelaxOp get_relax(const float *src, bool relax) {
+    RelaxOp r;
+    r.s = src[0]; r.c = src[1]; r.e1 = src[2]; r.e2 = src[3];
+    r.relax = relax;
+    return r;
+}
+
+__device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t flags,
                                                  const DevParams &P, const DevTables &Tb,
                                                  const GroupTables &GT, const GroupState &GS,
                                                  const uint2 *__restrict__ vox,
-                                                 const SpinState &S, const RngState &G) {
-    const size_t n = P.n_spins, plane = (size_t)GT.n_groups * n;
+                                                 const SpinState &S, const RngState &G,
+                                                 uint32_t *log_count, BlochEvent *log) {
     WalkRegs w;
     w.xo[0] = S.x[spin]; w.xo[1] = S.y[spin]; w.xo[2] = S.z[spin];
     w.ind_old = S.ind_old[spin];
@@ -129,6 +158,8 @@ __device__ __forceinline__ bool walk_groups_spin(const uint32_t spin, uint32_t f
     w.nh = G.nhead[spin]; w.nc = G.ncnt[spin]; w.uh = G.uhead[spin]; w.uc = G.ucnt[spin];
     const float *nb = G.nbuf + (size_t)spin * kNormBuf;
     const float *ub = G.ubuf + (size_t)spin * kUnifBuf;
+    BlochEvent *lg = log + (size_t)spin * kLogCap;
+    uint32_t ne = 0;
 
     float acc = S.acc[spin], acc_rec = GS.acc_rec[spin];
     uint32_t tp = S.tp[spin], tp_old = S.tp_old[spin], tp_old_rec = GS.tp_old_rec[spin];
@@ -139,7 +170,6 @@ __device__ __forceinline__ bool walk_groups_spin(const uint32_t spin, uint32_t f
     bool started = (flags & kFlagStarted) != 0;
 
     constexpr uint32_t NONE = 0xffffffffu;
-    const uint32_t span = GT.max_ds + 1;
     bool rec_scan = ds <= GT.max_ds && GT.rec_any[ds] != 0;
     uint32_t t_rf = c_rf < P.n_RF ? (uint32_t)Tb.rf[c_rf].tp : NONE;
     uint32_t t_te = (rec_scan && c_te < P.n_TE) ? (uint32_t)Tb.te_tp[c_te] : NONE;
@@ -148,16 +178,13 @@ __device__ __forceinline__ bool walk_groups_spin(const uint32_t spin, uint32_t f
 
     int status = -1;
     for (;;) {
+        if (ne + 4 > kLogCap) break;                                // log full: pause
         if (!started) {
             if (ds > GT.max_ds) { status = SW_SPIN_OK; break; }
-            for (uint32_t g = 0; g < GT.n_groups; g++) {         // kernels.cu:110-120
-                if (GT.last_ds[g] < ds) continue;
-                float a[3], b[3];
-                const size_t idx = (size_t)g * n + spin;
-                load_m(GS.mg, plane, idx, a);
-                rf_f(GT.scan_rf[(size_t)g * span + ds], a, b);
-                store_m(GS.mg, plane, idx, b);
-            }
+            BlochEvent &e = lg[ne++];                                // kernels.cu:110-120
+            e.head = kEvScanStart | (ds << 8);
+            e.ds = ds;
+            e.flags = 0;
             w.ind_old = P.matrix_length + 1;
             tp = tp_old = 0;
             c_rf = 1; c_te = 0; c_dph = 0; c_grad = 0;
@@ -171,24 +198,17 @@ __device__ __forceinline__ bool walk_groups_spin(const uint32_t spin, uint32_t f
             t_te = (rec_scan && P.n_TE > 0) ? (uint32_t)Tb.te_tp[0] : NONE;
             t_dph = P.n_dephasing > 0 ? (uint32_t)Tb.dph_tp[0] : NONE;
             t_grad = P.n_gradient > 0 ? (uint32_t)Tb.grad_tp[0] : NONE;
+            continue;
         }
         if (tp >= P.n_timepoints) {                                 // kernels.cu:225-231
             const float te = (float)((double)((tp - tp_old) * (uint32_t)P.timestep_us) * 1e-6);
             const RelaxOp r = make_relax(acc, __ldg(Tb.T1f + w.ts_old), __ldg(Tb.T2f + w.ts_old), te);
-            for (uint32_t g = 0; g < GT.n_groups; g++) {
-                if (GT.last_ds[g] < ds) continue;
-                float a[3], b[3];
-                const size_t idx = (size_t)g * n + spin;
-                load_m(GS.mg, plane, idx, a);
-                apply_relax(r, a, b);
-                store_m(GS.mg, plane, idx, b);
-                const int32_t t = GT.rec[(size_t)g * span + ds];
-                if (t >= 0) {                                       // track t ends here
-                    float *x = GT.XYZ1[t] + 3 * (size_t)spin;
-                    x[0] = (float)w.xo[0]; x[1] = (float)w.xo[1]; x[2] = (float)w.xo[2];
-                    if (GT.status[t]) GT.status[t][spin] = SW_SPIN_OK;
-                }
-            }
+            BlochEvent &e = lg[ne++];
+            e.head = kEvScanEnd | (ds << 8);
+            e.ds = ds;
+            e.flags = r.relax ? 1u : 0u;
+            put_relax(e.r, r);
+            e.xo[0] = (float)w.xo[0]; e.xo[1] = (float)w.xo[1]; e.xo[2] = (float)w.xo[2];
             ds++;
             started = false;
             continue;
@@ -224,33 +244,21 @@ __device__ __forceinline__ bool walk_groups_spin(const uint32_t spin, uint32_t f
             const float T1 = __ldg(Tb.T1f + w.ts_old), T2 = __ldg(Tb.T2f + w.ts_old);
             const float te = (float)((double)((tp - tp_old) * (uint32_t)P.timestep_us) * 1e-6);
             const RelaxOp r = make_relax(acc, T1, T2, te);
-            RelaxOp rr = r;
+            BlochEvent &e = lg[ne++];
+            e.head = kEvRf | (c_rf << 8);
+            e.ds = ds;
+            e.flags = (r.relax ? 1u : 0u) | (rec_started ? 4u : 0u);
+            put_relax(e.r, r);
             if (rec_started) {
                 const float ter = (float)((double)((tp - tp_old_rec) * (uint32_t)P.timestep_us) * 1e-6);
-                rr = make_relax(acc_rec, T1, T2, ter);
-            }
-            for (uint32_t g = 0; g < GT.n_groups; g++) {
-                if (GT.last_ds[g] < ds) continue;
-                const RfOp op = GT.rf[(size_t)g * P.n_RF + c_rf];
-                float a[3], b[3];
-                const size_t idx = (size_t)g * n + spin;
-                load_m(GS.mg, plane, idx, a);
-                apply_relax(r, a, b);
-                rf_f(op, b, a);
-                store_m(GS.mg, plane, idx, a);
-                if (rec_started && GT.rec[(size_t)g * span + ds] >= 0) {
-                    load_m(GS.mr, plane, idx, a);
-                    apply_relax(rr, a, b);
-                    rf_f(op, b, a);
-                    store_m(GS.mr, plane, idx, a);
-                }
-            }
-            acc = 0.f;
-            tp_old = tp;
-            if (rec_started) {
+                const RelaxOp rr = make_relax(acc_rec, T1, T2, ter);
+                e.flags |= rr.relax ? 2u : 0u;
+                put_relax(e.rr, rr);
                 acc_rec = 0.f;
                 tp_old_rec = tp;
             }
+            acc = 0.f;
+            tp_old = tp;
             c_rf++;
             t_rf = c_rf < P.n_RF ? (uint32_t)Tb.rf[c_rf].tp : NONE;
         }
@@ -259,18 +267,11 @@ __device__ __forceinline__ bool walk_groups_spin(const uint32_t spin, uint32_t f
             const float te = (float)((double)((tp - (rec_started ? tp_old_rec : tp_old)) *
                                               (uint32_t)P.timestep_us) * 1e-6);
             const RelaxOp r = make_relax(rec_started ? acc_rec : acc, T1, T2, te);
-            for (uint32_t g = 0; g < GT.n_groups; g++) {
-                const int32_t t = GT.rec[(size_t)g * span + ds];
-                if (t < 0) continue;
-                float a[3], b[3];
-                const size_t idx = (size_t)g * n + spin;
-                load_m(rec_started ? GS.mr : GS.mg, plane, idx, a);
-                apply_relax(r, a, b);
-                store_m(GS.mr, plane, idx, b);
-                float *m1 = GT.M1[t] + 3 * ((size_t)spin * P.n_TE + c_te);
-                m1[0] = b[0]; m1[1] = b[1]; m1[2] = b[2];
-                GT.T[t][(size_t)spin * P.n_TE + c_te] = (uint8_t)w.ts_old;
-            }
+            BlochEvent &e = lg[ne++];
+            e.head = kEvTe | (c_te << 8) | (w.ts_old << 24);
+            e.ds = ds;
+            e.flags = (r.relax ? 1u : 0u) | (rec_started ? 4u : 0u);
+            put_relax(e.r, r);
             acc_rec = 0.f;
             tp_old_rec = tp;
             rec_started = true;
@@ -280,6 +281,7 @@ __device__ __forceinline__ bool walk_groups_spin(const uint32_t spin, uint32_t f
         w.xo[0] = xn[0]; w.xo[1] = xn[1]; w.xo[2] = xn[2];
         tp++;
     }
+    log_count[spin] = ne;
     if (status > 0) {            // lost / out of bounds: every track still running ends here
         for (uint32_t t = 0; t < GT.n_tracks; t++) {
             if ((uint32_t)GT.track_nd[t] < ds) continue;
@@ -306,16 +308,81 @@ __device__ __forceinline__ bool walk_groups_spin(const uint32_t spin, uint32_t f
 }
 
 __global__ void __launch_bounds__(256)
-    k_walk_groups(DevParams P, DevTables Tb, GroupTables GT, GroupState GS,
-                  const uint2 *__restrict__ vox, SpinState S, RngState G, uint32_t *active) {
+    k_walk_logged(DevParams P, DevTables Tb, GroupTables GT, GroupState GS,
+                  const uint2 *__restrict__ vox, SpinState S, RngState G, uint32_t *active,
+                  uint32_t *log_count, BlochEvent *log) {
     const uint32_t spin = blockIdx.x * blockDim.x + threadIdx.x;
     bool still = false;
     if (spin < P.n_spins) {
         const uint32_t flags = S.flags[spin];
-        if (!(flags & kFlagDone)) still = walk_groups_spin(spin, flags, P, Tb, GT, GS, vox, S, G);
+        if (!(flags & kFlagDone))
+            still = walk_logged_spin(spin, flags, P, Tb, GT, GS, vox, S, G, log_count, log);
+        else
+            log_count[spin] = 0;
     }
     const unsigned b = __ballot_sync(0xffffffffu, still);
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(active, (uint32_t)__popc(b));
+}
+
+// Applies each spin's logged events to every group (thread per (group, spin), spin fastest).
+__global__ void __launch_bounds__(256)
+    k_bloch_groups(DevParams P, GroupTables GT, GroupState GS,
+                   const uint32_t *__restrict__ log_count, const BlochEvent *__restrict__ log) {
+    const size_t n = P.n_spins, plane = (size_t)GT.n_groups * n;
+    const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (idx >= plane) return;
+    const uint32_t g = (uint32_t)(idx / n);
+    const uint32_t spin = (uint32_t)(idx - (size_t)g * n);
+    const uint32_t cnt = log_count[spin];
+    if (cnt == 0) return;
+    const uint32_t span = GT.max_ds + 1, last = GT.last_ds[g];
+    float m[3], mr[3], t3[3];
+    load_m(GS.mg, plane, idx, m);
+    bool mr_loaded = false, mr_dirty = false;
+    const BlochEvent *lg = log + (size_t)spin * kLogCap;
+    for (uint32_t k = 0; k < cnt; k++) {
+        const BlochEvent e = lg[k];
+        const uint32_t type = e.head & 0xffu, id = (e.head >> 8) & 0xffffu, ds = e.ds;
+        if (ds > last) continue;                                    // group finished earlier
+        const int32_t t = GT.rec[(size_t)g * span + ds];
+        if (type == kEvScanStart) {
+            rf_f(GT.scan_rf[(size_t)g * span + ds], m, t3);
+            m[0] = t3[0]; m[1] = t3[1]; m[2] = t3[2];
+        } else if (type == kEvRf) {
+            const RfOp op = GT.rf[(size_t)g * P.n_RF + id];
+            apply_relax(get_relax(e.r, e.flags & 1u), m, t3);
+            rf_f(op, t3, m);
+            if ((e.flags & 4u) && t >= 0) {
+                if (!mr_loaded) { load_m(GS.mr, plane, idx, mr); mr_loaded = true; }
+                apply_relax(get_relax(e.rr, e.flags & 2u), mr, t3);
+                rf_f(op, t3, mr);
+                mr_dirty = true;
+            }
+        } else if (type == kEvTe) {
+            if (t < 0) continue;
+            const float *src = m;
+            if (e.flags & 4u) {
+                if (!mr_loaded) { load_m(GS.mr, plane, idx, mr); mr_loaded = true; }
+                src = mr;
+            }
+            apply_relax(get_relax(e.r, e.flags & 1u), src, t3);
+            float *o = GT.M1[t] + 3 * ((size_t)spin * P.n_TE + id);
+            o[0] = t3[0]; o[1] = t3[1]; o[2] = t3[2];
+            GT.T[t][(size_t)spin * P.n_TE + id] = (uint8_t)(e.head >> 24);
+            mr[0] = t3[0]; mr[1] = t3[1]; mr[2] = t3[2];
+            mr_loaded = mr_dirty = true;
+        } else {                                                    // scan end
+            apply_relax(get_relax(e.r, e.flags & 1u), m, t3);
+            m[0] = t3[0]; m[1] = t3[1]; m[2] = t3[2];
+            if (t >= 0) {                                           // track t ends here
+                float *x = GT.XYZ1[t] + 3 * (size_t)spin;
+                x[0] = e.xo[0]; x[1] = e.xo[1]; x[2] = e.xo[2];
+                if (GT.status[t]) GT.status[t][spin] = SW_SPIN_OK;
+            }
+        }
+    }
+    store_m(GS.mg, plane, idx, m);
+    if (mr_dirty) store_m(GS.mr, plane, idx, mr);
 }
 
 }  // namespace sw
@@ -437,7 +504,8 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
                  o_tab = slot(im.bytes.size()), o_gtab = slot(gi.bytes.size()),
                  o_ptrs = slot(4 * sizeof(void *) * n_tracks),
                  o_mg = slot(2 * 3 * sizeof(float) * (size_t)ng * n),
-                 o_gs = slot(12 * n);
+                 o_gs = slot(12 * n), o_lcnt = slot(4 * n),
+                 o_log = slot(sizeof(sw::BlochEvent) * sw::kLogCap * n);
     std::vector<size_t> o_M1(n_tracks), o_X(n_tracks), o_T(n_tracks), o_S(n_tracks);
     for (uint32_t t = 0; t < n_tracks; t++) {
         o_M1[t] = slot(n * nte * 12);
@@ -514,10 +582,17 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     GS.tp_old_rec = reinterpret_cast<uint32_t *>(d + o_gs + 4 * n);
     GS.rec_started = reinterpret_cast<uint32_t *>(d + o_gs + 8 * n);
 
+    uint32_t *lcnt = reinterpret_cast<uint32_t *>(d + o_lcnt);
+    sw::BlochEvent *elog = reinterpret_cast<sw::BlochEvent *>(d + o_log);
     const sw::LogfTables LT = sw::api::device_logf_tables();
     if (!LT.bitmap) return fail(SW_ERR_CUDA, "logf tables unavailable");
     sw::Outputs O{nullptr, nullptr, reinterpret_cast<float *>(d + o_scratch_xyz), nullptr,
                   reinterpret_cast<int32_t *>(d + o_scratch_st)};
+    g_timing = sw_timing{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    TR_CUDA(cudaEventCreate(&ev0));
+    TR_CUDA(cudaEventCreate(&ev1));
+    TR_CUDA(cudaEventRecord(ev0, st));
     TR_CUDA(cudaMemsetAsync(L.active, 0, 2 * sizeof(uint32_t), st));
     TR_CUDA(sw::launch_pack(reinterpret_cast<const uint8_t *>(d + o_mask),
                             has_field ? reinterpret_cast<const float *>(d + o_field) : nullptr,
@@ -535,17 +610,29 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     if (h) return fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate");
     const uint64_t steps = (uint64_t)pw.n_timepoints * (uint64_t)(max_ds + 1);
     const uint64_t max_rounds = 64 + steps * (param->max_iterations + 2);
-    for (uint64_t round = 0;; round++) {
+    uint64_t round = 0;
+    for (;; round++) {
         if (round >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
         TR_CUDA(cudaMemsetAsync(L.active, 0, 4, st));
         TR_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
-        sw::k_walk_groups<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P, Tb, GT, GS, L.vox, L.S,
-                                                                       L.G, L.active);
+        sw::k_walk_logged<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+            P, Tb, GT, GS, L.vox, L.S, L.G, L.active, lcnt, elog);
+        TR_CUDA(cudaGetLastError());
+        sw::k_bloch_groups<<<(unsigned)(((size_t)ng * n + 255) / 256), 256, 0, st>>>(
+            P, GT, GS, lcnt, elog);
         TR_CUDA(cudaGetLastError());
         TR_CUDA(cudaMemcpyAsync(&h, L.active, 4, cudaMemcpyDeviceToHost, st));
         TR_CUDA(cudaStreamSynchronize(st));
         if (h == 0) break;
     }
+    TR_CUDA(cudaEventRecord(ev1, st));
+    TR_CUDA(cudaEventSynchronize(ev1));
+    cudaEventElapsedTime(&g_timing.total_ms, ev0, ev1);
+    g_timing.walk_ms = g_timing.total_ms;
+    g_timing.n_chunks = (uint32_t)(round + 1);
+    g_timing.n_launches = (uint32_t)(4 + 3 * (round + 1));
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
     for (uint32_t t = 0; t < n_tracks; t++) {
         if (nte) {
             TR_CUDA(cudaMemcpyAsync(tracks[t].M1, d + o_M1[t], n * nte * 12, cudaMemcpyDeviceToHost, st));

@@ -121,6 +121,14 @@ int sw_phantom_spheres(const uint32_t dims[3], const double fov[3], double rmin,
                        double volume_fraction, uint64_t seed, double dchi, double Y,
                        const double B0_dir[3], double window, uint8_t *mask, float *field);
 
+/*
+ * Parses an INI config exactly as the reference's config_reader::prepare does (PARENT_CONFIG,
+ * indexed keys, float-parsed vectors, checks, microseconds -> time points;
+ * src/sim/config_reader.cpp:25-324) and writes the result as `key value...` text lines.
+ * Returns SW_ERR_CONFIG when the reader rejects the file (the dump then holds "ok 0").
+ */
+int sw_config_dump(const char *ini_path, const char *out_path);
+
 /* Library and device information. */
 int         sw_abi_version(void);
 const char *sw_last_error(void);

@@ -29,7 +29,7 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp", f"-I
              f"-I{CSRC}"]
 
 CU_UNITS = ["sw_kernels.cu", "sw_api.cu", "sw_noalloc.cu", "sw_tracks.cu"]
-CXX_UNITS = ["sw_host.cpp", "sw_phantom.cpp"]
+CXX_UNITS = ["sw_host.cpp", "sw_phantom.cpp", "sw_config.cpp"]
 
 
 def _nvcc():

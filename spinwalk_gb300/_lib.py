@@ -51,6 +51,7 @@ def lib():
         L.sw_sim_device_noalloc.argtypes = sim_args[:10] + [C.c_void_p]
         L.sw_sim_tracks.argtypes = [P(abi.SwParams), P(abi.SwSequence), P(abi.SwTrack), C.c_uint32,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.sw_config_dump.argtypes = [C.c_char_p, C.c_char_p]
         L.sw_sync.argtypes = [C.c_void_p]
         L.sw_last_timing.argtypes = [P(abi.SwTiming)]
         L.sw_debug_logf.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
@@ -114,6 +115,11 @@ def logf_exception_count():
     n, w = C.c_uint64(0), C.c_uint64(0)
     check(lib().sw_logf_exception_count(C.byref(n), C.byref(w)))
     return n.value, w.value
+
+
+def config_dump(ini_path, out_path):
+    """Parsed config as text (the reference's config_reader semantics); returns the rc."""
+    return lib().sw_config_dump(str(ini_path).encode(), str(out_path).encode())
 
 
 def last_timing():

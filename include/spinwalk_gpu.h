@@ -129,6 +129,22 @@ int sw_phantom_spheres(const uint32_t dims[3], const double fov[3], double rmin,
  */
 int sw_config_dump(const char *ini_path, const char *out_path);
 
+/*
+ * sim::monte_carlo::run (src/sim/monte_carlo.cu:199-355) for one INI config on `device`: for
+ * every PHANTOM: read the HDF5 phantom (mask, fieldmap, fov), the optional XYZ0 file, scale the
+ * fieldmap to degrees per time step, run every SCALE, and write the result file
+ * OUTPUT_DIR/SEQ_NAME_<phantom>.h5 with datasets M, XYZ, T, scales, TE as the reference does.
+ */
+int sw_run_config(const char *ini_path, int device);
+
+/* Whole-dataset HDF5 I/O (root group; uint8 = 0, float32 = 1, float64 = 2; little-endian,
+ * contiguous): the subset SpinWalk's phantom and result files use. sw_h5_read with out == NULL
+ * only reports type, rank and dims. */
+int sw_h5_write(const char *path, int n, const char *const *names, const int *types,
+                const int *ranks, const uint64_t *dims, const void *const *data);
+int sw_h5_read(const char *path, const char *name, int *type, int *rank, uint64_t dims[8],
+               void *out, uint64_t out_bytes);
+
 /* Library and device information. */
 int         sw_abi_version(void);
 const char *sw_last_error(void);

@@ -25,11 +25,13 @@ REF_TREE = "/root/reference"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", *ARCH, "-lineinfo", "-fmad=false",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp", f"-I{INC}", f"-I{CSRC}"]
+CUDA_INC = "/usr/local/cuda/include"
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp", f"-I{INC}",
-             f"-I{CSRC}"]
+             f"-I{CSRC}", f"-I{CUDA_INC}"]
+CLI = os.path.join(PKG, "spinwalk")
 
 CU_UNITS = ["sw_kernels.cu", "sw_api.cu", "sw_noalloc.cu", "sw_tracks.cu"]
-CXX_UNITS = ["sw_host.cpp", "sw_phantom.cpp", "sw_config.cpp"]
+CXX_UNITS = ["sw_host.cpp", "sw_phantom.cpp", "sw_config.cpp", "sw_h5.cpp", "sw_driver.cpp"]
 
 
 def _nvcc():
@@ -96,6 +98,11 @@ def build_lib(verbose=False, force=False):
         os.replace(tmp, LIB)
         with open(stamp_file, "w") as f:
             f.write(stamp)
+    cli_src = os.path.join(CSRC, "spinwalk_cli.cpp")
+    if force or not os.path.exists(CLI) or os.path.getmtime(CLI) < max(
+            os.path.getmtime(LIB), os.path.getmtime(cli_src)):
+        _run(["g++", "-O2", "-std=c++17", f"-I{INC}", cli_src, "-o", CLI, f"-L{PKG}",
+              "-lspinwalk_gpu", "-Wl,-rpath,$ORIGIN"], verbose)
     return LIB
 
 

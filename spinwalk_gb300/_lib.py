@@ -52,6 +52,11 @@ def lib():
         L.sw_sim_tracks.argtypes = [P(abi.SwParams), P(abi.SwSequence), P(abi.SwTrack), C.c_uint32,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.sw_config_dump.argtypes = [C.c_char_p, C.c_char_p]
+        L.sw_run_config.argtypes = [C.c_char_p, C.c_int]
+        L.sw_h5_write.argtypes = [C.c_char_p, C.c_int, P(C.c_char_p), P(C.c_int), P(C.c_int),
+                                  P(C.c_uint64), P(C.c_void_p)]
+        L.sw_h5_read.argtypes = [C.c_char_p, C.c_char_p, P(C.c_int), P(C.c_int), P(C.c_uint64),
+                                 C.c_void_p, C.c_uint64]
         L.sw_sync.argtypes = [C.c_void_p]
         L.sw_last_timing.argtypes = [P(abi.SwTiming)]
         L.sw_debug_logf.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
@@ -120,6 +125,38 @@ def logf_exception_count():
 def config_dump(ini_path, out_path):
     """Parsed config as text (the reference's config_reader semantics); returns the rc."""
     return lib().sw_config_dump(str(ini_path).encode(), str(out_path).encode())
+
+
+_H5_TYPES = {np.dtype(np.uint8): 0, np.dtype(np.float32): 1, np.dtype(np.float64): 2}
+_H5_DTYPES = {0: np.uint8, 1: np.float32, 2: np.float64}
+
+
+def h5_write(path, datasets):
+    """Writes {name: numpy array (uint8/float32/float64)} as an HDF5 file (root datasets)."""
+    items = [(k, np.ascontiguousarray(v)) for k, v in datasets.items()]
+    n = len(items)
+    names = (C.c_char_p * n)(*[k.encode() for k, _ in items])
+    types = (C.c_int * n)(*[_H5_TYPES[v.dtype] for _, v in items])
+    ranks = (C.c_int * n)(*[v.ndim for _, v in items])
+    flat = [d for _, v in items for d in v.shape]
+    dims = (C.c_uint64 * max(1, len(flat)))(*flat)
+    data = (C.c_void_p * n)(*[v.ctypes.data for _, v in items])
+    check(lib().sw_h5_write(str(path).encode(), n, names, types, ranks, dims, data))
+
+
+def h5_read(path, name):
+    t, r = C.c_int(0), C.c_int(0)
+    dims = (C.c_uint64 * 8)()
+    check(lib().sw_h5_read(str(path).encode(), name.encode(), C.byref(t), C.byref(r), dims, None, 0))
+    out = np.empty([dims[i] for i in range(r.value)], _H5_DTYPES[t.value])
+    check(lib().sw_h5_read(str(path).encode(), name.encode(), None, None, None,
+                           out.ctypes.data_as(C.c_void_p), out.nbytes))
+    return out
+
+
+def run_config(ini_path, device=0):
+    """sw_run_config: the whole `spinwalk sim -c ini` run (HDF5 in, HDF5 out)."""
+    check(lib().sw_run_config(str(ini_path).encode(), int(device)))
 
 
 def last_timing():

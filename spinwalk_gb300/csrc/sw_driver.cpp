@@ -1,0 +1,260 @@
+// sw_run_config: the reference's sim::monte_carlo::run (src/sim/monte_carlo.cu:199-355) on top
+// of the GPU entry points -- config, phantoms, initial positions, fieldmap scaling, the scale
+// loop and the HDF5 outputs -- plus the HDF5 helpers of the C ABI.
+//
+// Phase-cycling scales (WHAT_TO_SCALE = 2) walk identically, so they run as tracks of one walk
+// (sw_sim_tracks, bit-identical to one run per scale); FoV and gradient scales run one sw_sim
+// per scale as in the reference.
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <filesystem>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "spinwalk_gpu.h"
+#include "sw_config.h"
+#include "sw_h5.h"
+
+namespace {
+
+thread_local std::string g_drv_err;
+
+int drv_fail(int rc, const std::string &m) {
+    g_drv_err = m;
+    std::fprintf(stderr, "spinwalk: %s\n", m.c_str());
+    return rc;
+}
+
+template <typename T>
+bool read_as(const std::string &file, const char *name, std::vector<T> &out,
+             std::vector<uint64_t> *dims, std::string &err) {
+    sw::h5::Dataset d;
+    if (!sw::h5::read(file, name, d, err)) return false;
+    uint64_t n = 1;
+    for (uint64_t x : d.dims) n *= x;
+    out.resize(n);
+    if (d.type == sw::h5::kU8) {
+        for (uint64_t i = 0; i < n; i++) out[i] = (T)(uint8_t)d.data[i];
+    } else if (d.type == sw::h5::kF32) {
+        const float *p = reinterpret_cast<const float *>(d.data.data());
+        for (uint64_t i = 0; i < n; i++) out[i] = (T)p[i];
+    } else {
+        const double *p = reinterpret_cast<const double *>(d.data.data());
+        for (uint64_t i = 0; i < n; i++) out[i] = (T)p[i];
+    }
+    if (dims) *dims = d.dims;
+    return true;
+}
+
+template <typename T>
+sw::h5::Dataset make_ds(const std::vector<uint64_t> &dims, const std::vector<T> &v, sw::h5::Type t) {
+    sw::h5::Dataset d;
+    d.dims = dims;
+    d.type = t;
+    d.data.resize(v.size() * sizeof(T));
+    std::memcpy(d.data.data(), v.data(), d.data.size());
+    return d;
+}
+
+}  // namespace
+
+extern "C" int sw_run_config(const char *ini_path, int device) {
+    using clock = std::chrono::steady_clock;
+    const auto t_run = clock::now();
+    if (!ini_path) return drv_fail(SW_ERR_INVALID, "no config file");
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return drv_fail(SW_ERR_CUDA, "device " + std::to_string(device) + " is not available");
+    }
+    sw::Config c;
+    std::string err;
+    int rc = sw::config_read(ini_path, c, err);
+    if (rc) return drv_fail(rc, err);
+    sw_params p = c.p;
+    std::vector<double> dscale = c.diffusivity;
+    rc = sw_prepare_params(&p, dscale.data(), c.RF_FA_deg.data(), c.T1_ms.data());  // :205
+    if (rc) return drv_fail(rc, "parameters::prepare failed");
+
+    const size_t n = p.n_spins, nte = c.TE_us.size(), ns = c.scales.size();
+    const size_t trj = p.enRecordTrajectory ? (size_t)p.n_timepoints * (p.n_dummy_scan + 1) : 1;
+    // allocate_memory (monte_carlo.cu:61-70): once per run, NOT cleared between phantoms
+    std::vector<float> XYZ0(n * 3), XYZ0s(n * 3), XYZ1(trj * ns * n * 3), M0(n * 3),
+        M1(ns * nte * n * 3);
+    std::vector<uint8_t> T(ns * nte * n);
+    const std::vector<float> gx0 = c.gradientX_mTm, gy0 = c.gradientY_mTm, gz0 = c.gradientZ_mTm;
+    const float lin0 = p.linear_phase_cycling, quad0 = p.quadratic_phase_cycling;
+
+    const auto &phantoms = c.files["PHANTOM"];
+    for (size_t ip = 0; ip < phantoms.size(); ip++) {
+        const std::string &ph = phantoms[ip];
+        std::fprintf(stderr, "spinwalk: simulating phantom %s\n", ph.c_str());
+        // read_phantom (monte_carlo.cu:98-123)
+        std::vector<float> field, fov;
+        std::vector<uint8_t> mask;
+        std::vector<uint64_t> dims;
+        if (!read_as(ph, "fieldmap", field, nullptr, err)) field.clear();
+        if (!read_as(ph, "mask", mask, &dims, err)) return drv_fail(SW_ERR_IO, err);
+        if (!read_as(ph, "fov", fov, nullptr, err)) return drv_fail(SW_ERR_IO, err);
+        if (dims.size() != 3 || fov.size() < 3) return drv_fail(SW_ERR_IO, ph + ": mask must be 3-D, fov 3 values");
+        for (int i = 0; i < 3; i++) p.phantom_size[i] = dims[i];
+        const uint32_t nsub = mask.empty() ? 0 : (uint32_t)*std::max_element(mask.begin(), mask.end()) + 1;
+        if (nsub > p.n_substrate)
+            return drv_fail(SW_ERR_INVALID, "the mask holds more substrate types than the config defines");
+        // initialize_position (monte_carlo.cu:125-153)
+        const std::string &xf = c.files["XYZ0"][ip];
+        if (!xf.empty()) {
+            std::vector<float> x;
+            if (!read_as(xf, "XYZ", x, nullptr, err)) return drv_fail(SW_ERR_IO, err);
+            if (x.size() < XYZ0.size()) return drv_fail(SW_ERR_IO, xf + ": XYZ holds fewer spins than NUMBER_OF_SPINS");
+            std::copy(x.begin(), x.begin() + XYZ0.size(), XYZ0.begin());
+            for (size_t i = 0; i < XYZ0.size(); i++)
+                if (XYZ0[i] < 0 || XYZ0[i] > fov[i % 3])
+                    return drv_fail(SW_ERR_INVALID, "Initial positions are outside the FoV.");
+        } else {
+            sw_initial_positions(fov.data(), p.seed, p.n_spins, XYZ0.data());
+        }
+        // initialize_magnetization (monte_carlo.cu:155-166): the file is read, then every M0 is
+        // set to (0, 0, 1) regardless -- kept as the reference does it
+        const std::string &mf = c.files["M0"][ip];
+        if (!mf.empty()) {
+            std::vector<float> m;
+            if (!read_as(mf, "M", m, nullptr, err)) return drv_fail(SW_ERR_IO, err);
+        }
+        for (size_t i = 0; i < M0.size(); i++) M0[i] = (i % 3 == 2) ? 1.f : 0.f;
+        XYZ0s = XYZ0;
+        p.matrix_length = (int64_t)mask.size();
+        p.fieldmap_exist = field.empty() ? 0 : 1;
+        const float t2d = sw_fieldmap_scale(p.B0, p.timestep_us);          // :241-244
+        for (auto &v : field) v = v * t2d;
+        for (int i = 0; i < 3; i++) p.fov[i] = fov[i];
+
+        sw_sequence q{};
+        q.diffusivity = dscale.data();
+        q.T1_ms = c.T1_ms.data();
+        q.T2_ms = c.T2_ms.data();
+        q.pXY = c.pXY.data();
+        q.RF_FA_deg = c.RF_FA_deg.data();
+        q.RF_PH_deg = c.RF_PH_deg.data();
+        q.RF_us = c.RF_us.data();
+        q.n_RF = (uint32_t)c.RF_us.size();
+        q.TE_us = c.TE_us.data();
+        q.n_TE = (uint32_t)nte;
+        q.dephasing_deg = c.dephasing_deg.data();
+        q.dephasing_us = c.dephasing_us.data();
+        q.n_dephasing = (uint32_t)c.dephasing_us.size();
+        q.gradient_us = c.gradient_us.data();
+        q.n_gradient = (uint32_t)c.gradient_us.size();
+        std::vector<float> gx = gx0, gy = gy0, gz = gz0;
+        q.gradientX_mTm = gx.data();
+        q.gradientY_mTm = gy.data();
+        q.gradientZ_mTm = gz.data();
+
+        const auto t_sim = clock::now();
+        if (c.scale_type == 2 && !p.enRecordTrajectory && ns > 1) {
+            // phase-cycling scales: one walk, one track per scale
+            std::vector<sw_track> tracks(ns);
+            std::vector<std::vector<float>> xyz(ns, std::vector<float>(n * 3));
+            for (size_t k = 0; k < ns; k++) {
+                sw_track &t = tracks[k];
+                t = sw_track{};
+                t.linear_phase_cycling = lin0 * c.scales[k];
+                t.quadratic_phase_cycling = quad0;
+                t.n_dummy_scan = p.n_dummy_scan;
+                t.M1 = M1.data() + 3 * nte * n * k;
+                t.T = T.data() + nte * n * k;
+                t.XYZ1 = xyz[k].data();
+            }
+            rc = sw_sim_tracks(&p, &q, tracks.data(), (uint32_t)ns, field.empty() ? nullptr : field.data(),
+                               mask.data(), M0.data(), XYZ0s.data());
+            if (rc) return drv_fail(rc, sw_last_error());
+            for (size_t k = 0; k < ns; k++)
+                std::copy(xyz[k].begin(), xyz[k].end(), XYZ1.begin() + 3 * n * trj * k);
+        } else {
+            for (size_t k = 0; k < ns; k++) {                          // :273-337
+                const float scale = c.scales[k];
+                if (c.scale_type == 0) {
+                    for (size_t i = 0; i < XYZ0.size(); i++) XYZ0s[i] = XYZ0[i] * scale;
+                    for (int i = 0; i < 3; i++) p.fov[i] = scale * fov[i];
+                } else if (c.scale_type == 1) {
+                    for (size_t i = 0; i < gx.size(); i++) {
+                        gx[i] = gx0[i] * scale;
+                        gy[i] = gy0[i] * scale;
+                        gz[i] = gz0[i] * scale;
+                    }
+                } else {
+                    p.linear_phase_cycling = lin0 * scale;
+                    p.quadratic_phase_cycling = quad0;
+                }
+                rc = sw_sim(&p, &q, field.empty() ? nullptr : field.data(), mask.data(), M0.data(),
+                            XYZ0s.data(), M1.data() + 3 * nte * n * k, XYZ1.data() + 3 * n * trj * k,
+                            T.data() + nte * n * k, nullptr, SW_PREC_FP32, nullptr);
+                if (rc) return drv_fail(rc, sw_last_error());
+            }
+        }
+        const double sim_s = std::chrono::duration<double>(clock::now() - t_sim).count();
+        std::fprintf(stderr, "spinwalk: simulation took %.3f s\n", sim_s);
+
+        // save (monte_carlo.cu:168-197)
+        std::vector<float> te_s;
+        for (size_t i = 0; i < nte; i++) te_s.push_back(c.TE_us[i] * p.timestep_us * 1e-6);
+        std::vector<std::pair<std::string, sw::h5::Dataset>> sets;
+        sets.push_back({"M", make_ds({ns, n, nte, 3}, M1, sw::h5::kF32)});
+        sets.push_back({"XYZ", make_ds({ns, n, trj, 3}, XYZ1, sw::h5::kF32)});
+        sets.push_back({"T", make_ds({ns, n, nte, 1}, T, sw::h5::kU8)});
+        sets.push_back({"scales", make_ds({ns, 1, 1, 1}, c.scales, sw::h5::kF32)});
+        sets.push_back({"TE", make_ds({nte, 1, 1, 1}, te_s, sw::h5::kF32)});
+        const std::string &out = c.outputs[ip];
+        std::error_code ec;
+        std::filesystem::remove(out, ec);
+        if (!sw::h5::write(out, sets, err)) return drv_fail(SW_ERR_IO, err);
+        std::fprintf(stderr, "spinwalk: wrote %s\n", out.c_str());
+    }
+    std::fprintf(stderr, "spinwalk: entire run took %.3f s\n",
+                 std::chrono::duration<double>(clock::now() - t_run).count());
+    return SW_OK;
+}
+
+extern "C" int sw_h5_write(const char *path, int n, const char *const *names, const int *types,
+                           const int *ranks, const uint64_t *dims, const void *const *data) {
+    if (!path || n < 0) return SW_ERR_INVALID;
+    std::vector<std::pair<std::string, sw::h5::Dataset>> sets;
+    size_t dpos = 0;
+    for (int i = 0; i < n; i++) {
+        sw::h5::Dataset d;
+        d.type = (sw::h5::Type)types[i];
+        uint64_t cnt = 1;
+        for (int r = 0; r < ranks[i]; r++) {
+            d.dims.push_back(dims[dpos + r]);
+            cnt *= dims[dpos + r];
+        }
+        dpos += ranks[i];
+        const size_t esz = d.type == sw::h5::kU8 ? 1 : (d.type == sw::h5::kF32 ? 4 : 8);
+        d.data.resize(cnt * esz);
+        if (cnt) std::memcpy(d.data.data(), data[i], cnt * esz);
+        sets.push_back({names[i], std::move(d)});
+    }
+    std::string err;
+    if (!sw::h5::write(path, sets, err)) return drv_fail(SW_ERR_IO, err);
+    return SW_OK;
+}
+
+extern "C" int sw_h5_read(const char *path, const char *name, int *type, int *rank,
+                          uint64_t dims[8], void *out, uint64_t out_bytes) {
+    sw::h5::Dataset d;
+    std::string err;
+    if (!path || !name || !sw::h5::read(path, name, d, err)) return drv_fail(SW_ERR_IO, err);
+    if (d.dims.size() > 8) return drv_fail(SW_ERR_IO, "rank > 8");
+    if (type) *type = (int)d.type;
+    if (rank) *rank = (int)d.dims.size();
+    if (dims)
+        for (size_t i = 0; i < d.dims.size(); i++) dims[i] = d.dims[i];
+    if (out) {
+        if (out_bytes < d.data.size()) return drv_fail(SW_ERR_INVALID, "output buffer too small");
+        std::memcpy(out, d.data.data(), d.data.size());
+    }
+    return SW_OK;
+}

@@ -1,0 +1,124 @@
+"""HDF5 subset (phantom / result files) and the `spinwalk sim -c cfg.ini` drop-in path."""
+import glob
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from spinwalk_gb300 import _lib
+from spinwalk_gb300.problem import Problem, cylinder_phantom
+from tests import oracle_lib
+from tests.helpers import ROOT, bits_equal, m_close
+
+
+def test_h5_roundtrip(tmp_path):
+    rng = np.random.default_rng(0)
+    data = {"mask": rng.integers(0, 3, (5, 6, 7), dtype=np.uint8),
+            "fieldmap": rng.normal(size=(5, 6, 7)).astype(np.float32),
+            "fov": np.array([1e-4, 2e-4, 3e-4], np.float32),
+            "zz_double": rng.normal(size=(4, 2)),
+            "empty": np.zeros((0, 3), np.float32)}
+    f = tmp_path / "p.h5"
+    _lib.h5_write(f, data)
+    assert f.read_bytes()[:8] == b"\x89HDF\r\n\x1a\n"
+    for k, v in data.items():
+        got = _lib.h5_read(f, k)
+        assert got.dtype == v.dtype and got.shape == v.shape
+        assert bits_equal(got, v), k
+    with pytest.raises(_lib.SpinWalkError):
+        _lib.h5_read(f, "missing")
+
+
+def test_h5_reads_a_libhdf5_file():
+    """A file written by libhdf5 itself (a MATLAB v7.3 test file shipped with scipy: HDF5 behind
+    a 512-byte user block, version-1 layout messages)."""
+    scipy = pytest.importorskip("scipy")
+    hits = glob.glob(os.path.join(os.path.dirname(scipy.__file__), "io", "matlab", "tests", "data",
+                                  "testhdf5_7.4_GLNX86.mat"))
+    if not hits:
+        pytest.skip("scipy test data not installed")
+    got = _lib.h5_read(hits[0], "testdouble")
+    assert got.shape == (9, 1)
+    assert np.allclose(got.ravel(), np.arange(9) * np.pi / 4)
+
+
+def _write_case(tmp, scale_type, scales):
+    mask, field = cylinder_phantom(20, 20e-6, 3e-6, 0.1, seed=3)
+    _lib.h5_write(tmp / "phantom.h5", {"mask": mask, "fieldmap": field,
+                                       "fov": np.array([20e-6] * 3, np.float32)})
+    scale_lines = "\n".join(f"SCALE[{i}] = {s}" for i, s in enumerate(scales))
+    (tmp / "cfg.ini").write_text(f"""
+[GENERAL]
+SEQ_NAME = test
+[FILES]
+OUTPUT_DIR = out
+PHANTOM[0] = phantom.h5
+[TISSUE_PARAMETERS]
+DIFFUSIVITY[0] = 1e-9
+DIFFUSIVITY[1] = 1e-9
+P_XY[0] = 1 0.2
+P_XY[1] = 0.3 1
+T1[0] = 2000
+T1[1] = 2000
+T2[0] = 40
+T2[1] = 20
+[SCAN_PARAMETERS]
+TR = 3050
+TE = 1000 3000
+RF_FA = 90 180
+RF_PH = 0 90
+RF_T = 0 1500
+TIME_STEP = 50
+DUMMY_SCAN = 1
+LINEAR_PHASE_CYCLING = 10
+[SIMULATION_PARAMETERS]
+B0 = 9.4
+SEED = 10
+NUMBER_OF_SPINS = 300
+CROSS_FOV = 1
+WHAT_TO_SCALE = {scale_type}
+{scale_lines}
+""")
+    return mask, field
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scale_type,scales", [(0, [1.0, 0.5, 2.0]), (2, [0.0, 1.0, 3.0])])
+def test_run_config_matches_oracle_per_scale(tmp_path, scale_type, scales):
+    mask, field = _write_case(tmp_path, scale_type, scales)
+    r = subprocess.run([os.path.join(ROOT, "spinwalk_gb300", "spinwalk"), "sim", "-c",
+                        str(tmp_path / "cfg.ini")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = tmp_path / "out" / "test_phantom.h5"
+    M, XYZ, T = _lib.h5_read(out, "M"), _lib.h5_read(out, "XYZ"), _lib.h5_read(out, "T")
+    assert M.shape == (len(scales), 300, 2, 3) and T.shape == (len(scales), 300, 2, 1)
+    assert np.allclose(_lib.h5_read(out, "scales").ravel(), scales)
+    assert np.allclose(_lib.h5_read(out, "TE").ravel(), [1e-3, 3e-3])
+    xyz0 = _lib.initial_positions([20e-6] * 3, 10, 300)
+    for k, s in enumerate(scales):
+        s32 = np.float32(s)
+        kw = dict(TR_us=3050, TE_us=(1000, 3000), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
+                  RF_us=(0, 1500), pXY=[[1, 0.2], [0.3, 1]], n_dummy_scan=1, n_spins=300, seed=10,
+                  diffusivity=(float(np.float32(1e-9)),) * 2)      # the INI value is std::stof'd
+        if scale_type == 0:
+            fov = [float(s32 * np.float32(20e-6))] * 3
+            pr = Problem(mask, fov, field, XYZ0=(xyz0 * s32).astype(np.float32),
+                         linear_phase_cycling=10.0, **kw)
+            pr.params.fov[:] = [float(s32 * np.float32(20e-6))] * 3
+        else:
+            pr = Problem(mask, [20e-6] * 3, field, XYZ0=xyz0,
+                         linear_phase_cycling=float(np.float32(10.0) * s32), **kw)
+        o = oracle_lib.run(pr)
+        assert bits_equal(XYZ[k], o["XYZ1"]), k
+        assert bits_equal(T[k][..., 0], o["T"]), k
+        ok, rel = m_close(M[k], o["M1"])
+        assert ok, (k, rel)
+
+
+def test_cli_rejects_cpu_flag_and_bad_config(tmp_path):
+    exe = os.path.join(ROOT, "spinwalk_gb300", "spinwalk")
+    r = subprocess.run([exe, "sim", "-c", "x.ini", "-p"], capture_output=True, text=True)
+    assert r.returncode == 1 and "GPU only" in r.stderr
+    (tmp_path / "bad.ini").write_text("[SCAN_PARAMETERS]\nTE = 5 1\n")
+    assert _lib.config_dump(str(tmp_path / "bad.ini"), tmp_path / "d.txt") != 0

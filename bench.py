@@ -39,6 +39,13 @@ sys.path.insert(0, ROOT)
 
 GATHER_BYTES_PER_SPIN_STEP = 32   # one DRAM sector per random voxel lookup (mask + field record)
 USEFUL_BYTES_PER_SPIN_STEP = 5    # 1 B mask + 4 B field
+SEED_BYTES_PER_SPIN = 2 * 624 * 4 + 6 * 4   # two mt19937 states + 6 ring/index words written
+# DRAM traffic per unit from ncu on the small SE case (profiles/kernels_small_se_300cubed_2e5spins.md),
+# scaled to a full launch by the units it processes (both grow in proportion)
+SEED_DRAM_BYTES_PER_SPIN = 4710.0
+WALK_DRAM_BYTES_PER_SPIN_STEP = 30.8
+SEED_LIMITER = "integer ALU pipe (93.5 % busy, ncu): instruction bound, not HBM"
+WALK_LIMITER = "FP64 pipe (76 % busy, ncu): the voxel gather is not the bound"
 
 
 def workload(name, rank=0):
@@ -283,15 +290,26 @@ def run_ours(args, world, rank, local):
     parts = {"walk": walk_ms, "refill": refill_ms, "seed+init+pack": seed_ms}
     dominant = max(parts, key=parts.get)
     peak, peak_kind = measured_peaks()
-    # walk kernel: algorithmic gather bytes per launch / average launch duration
-    achieved = spin_steps * args.steps * GATHER_BYTES_PER_SPIN_STEP / (walk_ms * 1e-3) / 1e9
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "traffic_per_spin_step.json")
-    if os.path.exists(prof):
-        with open(prof) as f:
-            tb = json.load(f).get("walk_dram_bytes_per_spin_step")
-        if tb:
-            traffic = tb * spin_steps / (n_walk / args.steps)
+    n_chunks = n_walk / args.steps
+    # k_seed (seed+init+pack stage): algorithmic bytes = the generator state it must write
+    seed_launch_s = seed_ms / args.steps * 1e-3
+    seed_roof = {"bound": "hbm", "kernel": "k_seed", "unit_of_work": "spin",
+                 "algorithmic_bytes_per_unit": SEED_BYTES_PER_SPIN,
+                 "achieved": n * SEED_BYTES_PER_SPIN / seed_launch_s / 1e9, "peak": peak,
+                 "unit": "GB/s", "traffic": SEED_DRAM_BYTES_PER_SPIN * n,
+                 "peak_source": peak_kind, "limiter": SEED_LIMITER}
+    # k_walk: one 32 B DRAM sector per spin-step (random voxel gather)
+    walk_launch_s = walk_ms / n_walk * 1e-3
+    walk_units = spin_steps / n_chunks
+    walk_roof = {"bound": "hbm", "kernel": "k_walk", "unit_of_work": "spin-step",
+                 "algorithmic_bytes_per_unit": GATHER_BYTES_PER_SPIN_STEP,
+                 "achieved": walk_units * GATHER_BYTES_PER_SPIN_STEP / walk_launch_s / 1e9,
+                 "peak": peak, "unit": "GB/s",
+                 "traffic": WALK_DRAM_BYTES_PER_SPIN_STEP * walk_units,
+                 "peak_source": peak_kind, "limiter": WALK_LIMITER}
+    for r in (seed_roof, walk_roof):
+        r["frac"] = r["achieved"] / peak
+    roof = {"seed+init+pack": seed_roof, "walk": walk_roof}.get(dominant, walk_roof)
     cpu = None
     if world == 1 or rank == 0:
         if args.cpu_sample > 0:
@@ -307,11 +325,8 @@ def run_ours(args, world, rank, local):
         "config": dict(desc, parallelism=f"spin-range shards x{world}",
                        l2="inputs larger than L2 (packed phantom + generator state)"),
         "kernel_ms_per_step": {k: v / args.steps for k, v in parts.items()},
-        "roofline": {"bound": "hbm", "kernel": "k_walk", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": peak_kind,
-                     "note": f"{GATHER_BYTES_PER_SPIN_STEP} B gather sector per spin-step; "
-                             f"dominant stage: {dominant}"},
+        "roofline": dict(roof, dominant_stage=dominant),
+        "roofline_walk": walk_roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "spin-steps/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},

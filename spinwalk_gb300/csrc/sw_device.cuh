@@ -74,36 +74,60 @@ __device__ __forceinline__ void mt_twist_warp(uint32_t *s, int lane) {
     __syncwarp();
 }
 
-// The same regeneration with the state held in registers: lane l owns words l + 32k in a[k]
-// (k < 20; a[19] only for lanes < 16). x[i+1] and the far word x[i+397] (words < 227) or the
-// already regenerated x[i-227] (words >= 227) arrive by warp shuffles, 41 per regeneration,
-// and no shared memory is touched. Words are regenerated in increasing k, each k reading its
-// operands before any lane overwrites a[k], which reproduces the sequential in-place order.
-__device__ __forceinline__ void mt_twist_regs(uint32_t (&a)[20], int lane) {
+// One word of the regeneration, x[i] <- x[i+397] ^ (y >> 1) ^ (y odd ? 0x9908b0df : 0) with
+// y = upper bit of x[i] | lower 31 bits of x[i+1], written so that the integer ALU pipe (the
+// bound of seeding) carries only three instructions: the bit select and the three-way xor as
+// single lop3 operations and the shift. The odd-bit mask comes from the FMA pipe as
+// (y - 2 (y >> 1)) * 0x9908b0df, which is exact in 32-bit arithmetic.
+__device__ __forceinline__ uint32_t mt_twist1_alu3(uint32_t xi, uint32_t xi1, uint32_t xm) {
+    uint32_t y, bit, mag, r;
+    asm("lop3.b32 %0, %1, %2, 0x80000000, 0xE4;" : "=r"(y) : "r"(xi), "r"(xi1));  // (a&c)|(b&~c)
+    const uint32_t ysh = y >> 1;
+    asm("mad.lo.u32 %0, %1, 0xFFFFFFFE, %2;" : "=r"(bit) : "r"(ysh), "r"(y));
+    asm("mul.lo.u32 %0, %1, 0x9908B0DF;" : "=r"(mag) : "r"(bit));
+    asm("lop3.b32 %0, %1, %2, %3, 0x96;" : "=r"(r) : "r"(xm), "r"(ysh), "r"(mag));  // a^b^c
+    return r;
+}
+
+// The full regeneration with the state held in the registers of a HALF warp (16 lanes): lane
+// hl owns the 13 consecutive words 208k + 13 hl + j in b[k][j] (k < 3, j < 13). A row k is 208
+// consecutive words, fewer than 624 - 397 = 227, so no word of a row reads a word regenerated
+// in the same row, and regenerating rows 0, 1, 2 in turn reproduces the sequential in-place
+// order of mersenne_twister_engine::_M_gen_rand:
+//   x[i+1]   same lane (j < 12), else slot 0 of lane hl+1 in row k, or of lane 0 in row k+1
+//            (lane 15; row 3 is the regenerated row 0, as x[624] is the new x[0]);
+//   x[i+397] 397 = 208 + 14*13 + 7: slot j+7 of lane hl+14 (j < 6) or slot j-6 of lane hl+15
+//            (j >= 6), in row k+1, or k+2 where the lane index wraps; rows k+1 and k+2 modulo
+//            3 are exactly the old (not yet regenerated) or new words the sequential loop reads.
+// Each row costs 14 shuffles for 13 words; every value is shuffled from the row chosen by the
+// PROVIDING lane, which is fixed per lane. With PRED the new words are kept only where `live`.
+template <bool PRED>
+__device__ __forceinline__ void mt_twist13(uint32_t (&b)[3][13], int hl, bool live) {
     constexpr unsigned FULL = 0xffffffffu;
+    const bool q0 = hl == 0, q14 = hl >= 14, q15 = hl == 15;
 #pragma unroll
-    for (int k = 0; k < 20; k++) {
-        uint32_t nxt;
-        if (k < 19) {
-            const uint32_t prov = (lane == 0) ? a[k + 1] : a[k];
-            nxt = __shfl_sync(FULL, prov, (lane + 1) & 31);
-        } else {   // word 623's successor is the regenerated word 0
-            const uint32_t prov = (lane == 0) ? a[0] : a[19];
-            nxt = __shfl_sync(FULL, prov, lane == 15 ? 0 : (lane + 1) & 31);
+    for (int k = 0; k < 3; k++) {
+        const int r1 = (k + 1) % 3, r2 = (k + 2) % 3;
+        const uint32_t n12 = __shfl_sync(FULL, q0 ? b[r1][0] : b[k][0], hl + 1, 16);
+        uint32_t far[13];
+#pragma unroll
+        for (int j = 0; j < 6; j++)
+            far[j] = __shfl_sync(FULL, q14 ? b[r1][j + 7] : b[r2][j + 7], hl + 14, 16);
+#pragma unroll
+        for (int j = 6; j < 13; j++)
+            far[j] = __shfl_sync(FULL, q15 ? b[r1][j - 6] : b[r2][j - 6], hl + 15, 16);
+#pragma unroll
+        for (int j = 0; j < 13; j++) {
+            const uint32_t nw = mt_twist1_alu3(b[k][j], j < 12 ? b[k][j + 1] : n12, far[j]);
+            b[k][j] = PRED ? (live ? nw : b[k][j]) : nw;
         }
-        uint32_t farA = 0u, farB = 0u;
-        if (k <= 7) {
-            const uint32_t prov = (lane >= 13) ? a[k + 12] : ((k + 13 < 20) ? a[k + 13 < 20 ? k + 13 : 0] : 0u);
-            farA = __shfl_sync(FULL, prov, (lane + 13) & 31);
-        }
-        if (k >= 7) {
-            const uint32_t prov = (lane < 29) ? a[k - 7] : ((k >= 8) ? a[k >= 8 ? k - 8 : 0] : 0u);
-            farB = __shfl_sync(FULL, prov, (lane + 29) & 31);
-        }
-        const bool inA = (lane + 32 * k) < 227;
-        const uint32_t nw = mt_twist1(a[k], nxt, inA ? farA : farB);
-        if (k < 19 || lane < 16) a[k] = nw;
     }
+}
+
+// Number of regenerations that mersenne_twister_engine::discard(z) performs right after
+// seeding (position 624): while (z > 624 - p) { z -= 624 - p; regenerate; p = 0; }
+__host__ __device__ __forceinline__ uint32_t mt_discard_twists(uint64_t z) {
+    return z == 0 ? 0u : (uint32_t)(1 + (z - 1) / kMtN);
 }
 
 // generate_canonical<float, 24>(mt19937): float(w) / 2^32, clamped below 1

@@ -5,8 +5,8 @@
 // same per-spin computation is split so that each part runs in the shape the GPU likes:
 //
 //   k_pack    : mask + fieldmap -> one 8-byte record per voxel (one gather per step)
-//   k_seed    : one WARP per spin: mt19937(seed+spin) + discard(seed+spin), the 624-word state
-//               held in the 32 lanes' registers and regenerated with warp shuffles
+//   k_seed    : one HALF warp per spin: mt19937(seed+spin) + discard(seed+spin), the 624-word
+//               state held in 16 lanes' registers (13 words each), regenerated with shuffles
 //   k_init    : one thread per spin: initial voxel, substrate and state (kernels.cu:90-104)
 //   k_refill  : one WARP per spin: tops up the spin's ring buffers of Gaussian deviates
 //               (libstdc++ polar method, 32 candidate pairs per pass, accepted pairs compacted
@@ -44,18 +44,27 @@ __global__ void k_pack(const uint8_t *__restrict__ mask, const float *__restrict
 // ------------------------------------------------------------------------------------------
 // Seeding: std::mt19937 gen(seed + spin); gen.discard(seed + spin)   (kernels.cu:82-88)
 // ------------------------------------------------------------------------------------------
+// One HALF warp per spin (mt_twist13 layout), two spins per warp. The two spins of a warp are
+// neighbours, so their discard counts differ by one and their regeneration counts by at most
+// one: both halves run the common count together, then at most one regeneration whose result
+// only the half that needs it keeps. Seeding (623 dependent multiply-adds) runs on one lane per
+// half into shared memory. The discard work, sum over spins of seed + spin words, is what
+// bounds this kernel (integer pipes), not memory.
 constexpr int kSeedWarps = 4;
 
 __global__ void __launch_bounds__(32 * kSeedWarps)
     k_seed(DevParams P, RngState G, uint32_t spin_lo, uint32_t spin_hi) {
-    __shared__ uint32_t s_mt[kSeedWarps][kMtN];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t *s = s_mt[w];
-    for (uint32_t idx = blockIdx.x * kSeedWarps + w; idx < spin_hi - spin_lo;
-         idx += gridDim.x * kSeedWarps) {
-        const uint32_t spin = spin_hi - 1 - idx;     // most expensive (largest discard) first
+    __shared__ uint32_t s_mt[2 * kSeedWarps][kMtN];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, half = lane >> 4, hl = lane & 15;
+    uint32_t *s = s_mt[2 * w + half];
+    const uint32_t n = spin_hi - spin_lo;
+    for (uint32_t pair = blockIdx.x * kSeedWarps + w; 2ull * pair < n;
+         pair += gridDim.x * kSeedWarps) {
+        const uint32_t idx = 2 * pair + half;
+        const bool valid = idx < n;                  // an odd count leaves one half idle
+        const uint32_t spin = spin_hi - 1 - (valid ? idx : n - 1);  // largest discard first
         const uint64_t sd = P.seed + spin;
-        if (lane == 0) {                             // mersenne_twister_engine::seed
+        if (hl == 0) {                               // mersenne_twister_engine::seed
             uint32_t x = (uint32_t)sd;
             s[0] = x;
             for (uint32_t i = 1; i < kMtN; i++) {
@@ -64,40 +73,37 @@ __global__ void __launch_bounds__(32 * kSeedWarps)
             }
         }
         __syncwarp();
-        uint32_t a[20];                              // lane l holds words l + 32k
+        uint32_t b[3][13];
 #pragma unroll
-        for (int k = 0; k < 20; k++) {
-            const int i = lane + 32 * k;
-            a[k] = i < kMtN ? s[i] : 0u;
-        }
+        for (int k = 0; k < 3; k++)
+#pragma unroll
+            for (int j = 0; j < 13; j++) b[k][j] = s[208 * k + 13 * hl + j];
         __syncwarp();
-        // mersenne_twister_engine::discard: while (z > n - p) { z -= n - p; twist; p = 0; }
-        uint64_t z = sd;
-        uint32_t p = kMtN;
-        while (z > (uint64_t)(kMtN - p)) {
-            z -= kMtN - p;
-            mt_twist_regs(a, lane);
-            p = 0;
-        }
-        p += (uint32_t)z;
-        uint32_t *gr = G.mt_r + (size_t)spin * kMtN, *gu = G.mt_u + (size_t)spin * kMtN;
+        const uint32_t mine = mt_discard_twists(sd);
+        const uint32_t other = __shfl_xor_sync(0xffffffffu, mine, 16);
+        const uint32_t common = min(mine, other);
+        for (uint32_t t = 0; t < common; t++) mt_twist13<false>(b, hl, true);
+        if (max(mine, other) > common) mt_twist13<true>(b, hl, mine > common);
+        // discard leaves the position at z - 624 (regenerations - 1), or 624 when z == 0
+        const uint32_t p = mine == 0 ? (uint32_t)kMtN : (uint32_t)(sd - (uint64_t)kMtN * (mine - 1));
+        if (valid) {
+            uint32_t *gr = G.mt_r + (size_t)spin * kMtN, *gu = G.mt_u + (size_t)spin * kMtN;
 #pragma unroll
-        for (int k = 0; k < 20; k++) {
-            const int i = lane + 32 * k;
-            if (i < kMtN) {
-                gr[i] = a[k];
-                gu[i] = a[k];
+            for (int k = 0; k < 3; k++)
+#pragma unroll
+                for (int j = 0; j < 13; j++) {
+                    gr[208 * k + 13 * hl + j] = b[k][j];
+                    gu[208 * k + 13 * hl + j] = b[k][j];
+                }
+            if (hl == 0) {
+                G.p_r[spin] = p;
+                G.p_u[spin] = p;
+                G.nhead[spin] = 0;
+                G.ncnt[spin] = 0;
+                G.uhead[spin] = 0;
+                G.ucnt[spin] = 0;
             }
         }
-        if (lane == 0) {
-            G.p_r[spin] = p;
-            G.p_u[spin] = p;
-            G.nhead[spin] = 0;
-            G.ncnt[spin] = 0;
-            G.uhead[spin] = 0;
-            G.ucnt[spin] = 0;
-        }
-        __syncwarp();
     }
 }
 
@@ -549,7 +555,8 @@ cudaError_t launch_seed(const DevParams &P, const RngState &G, cudaStream_t st) 
 cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo, uint32_t hi,
                               cudaStream_t st) {
     if (hi <= lo) return cudaSuccess;
-    k_seed<<<grid_for(hi - lo, kSeedWarps, 1 << 30), 32 * kSeedWarps, 0, st>>>(P, G, lo, hi);
+    k_seed<<<grid_for(((int64_t)hi - lo + 1) / 2, kSeedWarps, 1 << 30), 32 * kSeedWarps, 0, st>>>(
+        P, G, lo, hi);
     return cudaGetLastError();
 }
 

@@ -277,6 +277,11 @@ int sw_last_timing(sw_timing *out);
  * device logf on n inputs (device pointers) -- used by the tests. */
 int sw_debug_logf(const float *d_x, float *d_y, uint64_t n, void *stream);
 
+/* Host-visible check of the integer double addition of the walk's position update:
+ * d_y[i] = d_a[i] + d_b[i] (IEEE round to nearest even) on n device doubles -- used by the
+ * tests. */
+int sw_debug_dadd(const double *d_a, const double *d_b, double *d_y, uint64_t n, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -166,9 +166,9 @@ Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl) {
     L.tables = c.take<char>(table_bytes);
     L.active = c.take<uint32_t>(4);
     sw::SpinState &S = L.S;
-    S.x = c.take<double>(n);
-    S.y = c.take<double>(n);
-    S.z = c.take<double>(n);
+    S.x = c.take<uint64_t>(n);
+    S.y = c.take<uint64_t>(n);
+    S.z = c.take<uint64_t>(n);
     S.mx = c.take<float>(n);
     S.my = c.take<float>(n);
     S.mz = c.take<float>(n);
@@ -467,6 +467,12 @@ int sw_sim(const sw_params *param, const sw_sequence *seq, const float *pFieldMa
     SW_TRY(cudaStreamSynchronize(st));
 #undef SW_TRY
     return done(SW_OK);
+}
+
+int sw_debug_dadd(const double *d_a, const double *d_b, double *d_y, uint64_t n, void *stream) {
+    if (!d_a || !d_b || !d_y) return fail(SW_ERR_INVALID, "null device buffer");
+    SW_CUDA(sw::launch_debug_dadd(d_a, d_b, d_y, n, (cudaStream_t)stream));
+    return SW_OK;
 }
 
 int sw_debug_logf(const float *d_x, float *d_y, uint64_t n, void *stream) {

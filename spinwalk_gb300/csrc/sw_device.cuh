@@ -7,6 +7,7 @@
 #pragma once
 #include <stdint.h>
 
+#include "sw_dadd.h"
 #include "sw_logf.h"
 #include "sw_types.h"
 
@@ -166,10 +167,10 @@ __device__ __forceinline__ double f2d_exact(float f) {
 // exponent): the exact 77-bit product of the significands from two 32x32->64 multiplies, rounded
 // to 53 bits to nearest-even by hand. Bit-identical to the IEEE double multiply, without the
 // FP64 pipe.
-__device__ __forceinline__ double mul_fd(float n, uint32_t s_lo, uint32_t s_hi, int es) {
+__device__ __forceinline__ uint64_t mul_fd(float n, uint32_t s_lo, uint32_t s_hi, int es) {
     const uint32_t b = __float_as_uint(n);
     const uint32_t en = (b >> 23) & 0xffu;
-    if (en == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);   // +-0
+    if (en == 0u) return (uint64_t)(b & 0x80000000u) << 32;             // +-0
     const uint32_t mn = (b & 0x7fffffu) | 0x800000u;
     const uint64_t t = (uint64_t)mn * s_lo, u = (uint64_t)mn * s_hi;
     const uint32_t p0 = (uint32_t)t;
@@ -192,37 +193,51 @@ __device__ __forceinline__ double mul_fd(float n, uint32_t s_lo, uint32_t s_hi, 
         e += 1;
     }
     const uint32_t hi = (b & 0x80000000u) | ((uint32_t)(e + 1023) << 20) | (r_hi & 0xfffffu);
-    return __hiloint2double((int)hi, (int)r_lo);
+    return ((uint64_t)hi << 32) | r_lo;
 }
 
 // v < 0 and v >= bound (bound > 0) on the bit patterns (positive doubles order as integers).
-__device__ __forceinline__ bool dneg(double v) {
-    const long long b = __double_as_longlong(v);
-    return b < 0 && (b & 0x7fffffffffffffffLL) != 0;
+__device__ __forceinline__ bool dneg(uint64_t v) {
+    return (int64_t)v < 0 && (v & 0x7fffffffffffffffull) != 0u;
 }
-__device__ __forceinline__ bool dge_pos(double v, double bound) {
-    return __double_as_longlong(v) >= __double_as_longlong(bound);
+__device__ __forceinline__ bool dge_pos(uint64_t v, double bound) {
+    return (int64_t)v >= __double_as_longlong(bound);
 }
 
 // (int64_t)(v * s2g) as the reference computes it (double product, truncation), via an FP32
 // estimate: v is truncated to 24 bits from its bit pattern (relative error < 2^-23), s2g_f is
 // s2g rounded to float (< 2^-24), the float product adds < 2^-24, so |p - v*s2g| < 2^-22 |p|.
 // When p is farther than 2^-21 |p| from an integer (all but ~1e-4 of the calls at 500 voxels)
-// floor(p) is the answer; otherwise, and for v <= 0 or tiny v, the exact double product is used.
-__device__ __forceinline__ int64_t voxel_coord(double v, double s2g, float s2g_f) {
-    const uint32_t hi = (uint32_t)__double2hiint(v), lo = (uint32_t)__double2loint(v);
+// floor(p) is the answer; otherwise, and for v <= 0, tiny v or p >= 2^22, the exact double
+// product is used. floor(p) itself is taken without the conversion units (64-bit conversions
+// and rounding run on the slow FP64 pipe of this GPU): adding 1.5 * 2^23 rounds a p in
+// [0, 2^22) to the nearest integer n exactly, and the sum's bit pattern is 0x4B400000 + n.
+__device__ __forceinline__ int64_t voxel_coord(uint64_t vb, double s2g, float s2g_f) {
+    const uint32_t hi = (uint32_t)(vb >> 32), lo = (uint32_t)vb;
     const uint32_t e = (hi >> 20) & 0x7ffu;
     if ((int32_t)hi > 0 && e > 1023u - 120u) {
         const float vf = __uint_as_float(((e - 1023u + 127u) << 23) | ((hi & 0xfffffu) << 3) |
                                          (lo >> 29));
-        const float p = vf * s2g_f;
-        const float fl = floorf(p);
-        const float fr = p - fl;
-        const float margin = p * 4.76837158203125e-07f;    // 2^-21
-        if (fr > margin && 1.0f - fr > margin) return (int64_t)fl;
+        const float p = __fmul_rn(vf, s2g_f);
+        if (p < 4194304.0f) {                                      // 2^22
+            const float t = __fadd_rn(p, 12582912.0f);             // 1.5 * 2^23
+            float fl = __fsub_rn(t, 12582912.0f);
+            int32_t n = __float_as_int(t) - 0x4B400000;
+            if (fl > p) {
+                fl = __fsub_rn(fl, 1.0f);
+                n -= 1;
+            }
+            const float fr = __fsub_rn(p, fl);
+            const float margin = __fmul_rn(p, 4.76837158203125e-07f);   // 2^-21
+            if (fr > margin && __fsub_rn(1.0f, fr) > margin) return (int64_t)n;
+        }
     }
-    return (int64_t)(v * s2g);
+    return (int64_t)(dfrom(vb) * s2g);
 }
+
+// dscale != 0 for a non-negative double, as an integer test (a double compare is an FP64-pipe
+// instruction)
+__device__ __forceinline__ bool dnonzero(double v) { return __double_as_longlong(v) != 0; }
 
 // ------------------------------------------------------------------------------------------
 // One attempted move of a spin (src/sim/kernels.cu:130-170), shared by the walk kernels
@@ -230,7 +245,7 @@ __device__ __forceinline__ int64_t voxel_coord(double v, double s2g, float s2g_f
 enum MoveResult { kMoveAccepted = 0, kMoveRejected = 1, kMoveLost = 2, kMoveOOB = 3 };
 
 struct WalkRegs {
-    double xo[3];             // last accepted position
+    uint64_t xo[3];           // last accepted position (bit patterns of the doubles)
     int64_t ind_old;
     uint32_t ts_old;          // substrate of the last accepted voxel
     float field;              // its field (deg per step)
@@ -243,24 +258,26 @@ struct WalkRegs {
 // Draws three deviates (when the substrate diffuses), wraps at the FoV, looks the voxel up and
 // applies the permeability test. On acceptance xn holds the new position and the voxel state in
 // w is updated; w.xo is left to the caller (it commits xn after the Bloch events).
-__device__ __forceinline__ int walk_move(WalkRegs &w, double (&xn)[3], const DevParams &P,
+__device__ __forceinline__ int walk_move(WalkRegs &w, uint64_t (&xn)[3], const DevParams &P,
                                          const DevTables &Tb, const uint2 *__restrict__ vox,
                                          const float *nb, const float *ub) {
     xn[0] = w.xo[0];
     xn[1] = w.xo[1];
     xn[2] = w.xo[2];
-    if (w.dscale != 0.) {
+    if (dnonzero(w.dscale)) {
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             const float g = nb[w.nh];
             w.nh = (w.nh + 1 == kNormBuf) ? 0 : w.nh + 1;
-            const double rnd = w.dsp.w ? mul_fd(g, w.dsp.x, w.dsp.y, (int)w.dsp.z)
-                                       : f2d_exact(g) * w.dscale;
-            double v = w.xo[i] + rnd;
+            const uint64_t rnd = w.dsp.w ? mul_fd(g, w.dsp.x, w.dsp.y, (int)w.dsp.z)
+                                         : dbits(f2d_exact(g) * w.dscale);
+            uint64_t v = dadd_fp64(w.xo[i], rnd);   // w.xo[i] + rnd
+            // the wrap in integer arithmetic too: the compiler evaluates a cheap double
+            // expression here on every step whatever the branch, on the slow FP64 unit
             if (dneg(v))
-                v += P.cross_fov ? P.fov[i] : 2 * fabs(rnd);
+                v = dadd_bits(v, P.cross_fov ? dbits(P.fov[i]) : dtwice_abs(rnd));
             else if (dge_pos(v, P.fov[i]))
-                v -= P.cross_fov ? P.fov[i] : 2 * fabs(rnd);
+                v = dadd_bits(v, dflip(P.cross_fov ? dbits(P.fov[i]) : dtwice_abs(rnd)));
             xn[i] = v;
         }
         w.nc -= 3;

@@ -122,9 +122,9 @@ __global__ void k_init(DevParams P, DevTables Tb, const uint2 *__restrict__ vox,
     }
     float *xyz1 = O.XYZ1 + 3 * (size_t)spin * P.traj_len;
     for (int i = 0; i < 3; i++) xyz1[i] = p0[i];                   // kernels.cu:96
-    S.x[spin] = p0[0];
-    S.y[spin] = p0[1];
-    S.z[spin] = p0[2];
+    S.x[spin] = dbits((double)p0[0]);
+    S.y[spin] = dbits((double)p0[1]);
+    S.z[spin] = dbits((double)p0[2]);
     S.mx[spin] = m[0];
     S.my[spin] = m[1];
     S.mz[spin] = m[2];
@@ -293,7 +293,7 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
                                           const SpinState &S, const RngState &G,
                                           const Outputs &O) {
     constexpr bool KAHAN = PREC == SW_PREC_KAHAN;
-    double xo[3] = {S.x[spin], S.y[spin], S.z[spin]};
+    uint64_t xo[3] = {S.x[spin], S.y[spin], S.z[spin]};    // bit patterns of the doubles
     float m0[3] = {S.mx[spin], S.my[spin], S.mz[spin]}, m1[3];
     float acc = S.acc[spin], acc_e = KAHAN ? S.acc_e[spin] : 0.f;
     double accd = 0., d0[3] = {0., 0., 0.}, d1[3];
@@ -359,22 +359,24 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
             started = false;
             continue;
         }
-        if ((dscale != 0. && nc < 3) || uc == 0) break;             // buffers low: pause
+        if ((dnonzero(dscale) && nc < 3) || uc == 0) break;             // buffers low: pause
 
         // ---- random walk + boundary (kernels.cu:130-137) ----
-        double xn[3] = {xo[0], xo[1], xo[2]};
-        if (dscale != 0.) {
+        uint64_t xn[3] = {xo[0], xo[1], xo[2]};
+        if (dnonzero(dscale)) {
 #pragma unroll
             for (int i = 0; i < 3; i++) {
                 const float g = nb[nh];
                 nh = (nh + 1 == kNormBuf) ? 0 : nh + 1;
-                const double rnd = dsp.w ? mul_fd(g, dsp.x, dsp.y, (int)dsp.z)
-                                         : f2d_exact(g) * dscale;
-                double v = xo[i] + rnd;
+                const uint64_t rnd = dsp.w ? mul_fd(g, dsp.x, dsp.y, (int)dsp.z)
+                                           : dbits(f2d_exact(g) * dscale);
+                uint64_t v = dadd_fp64(xo[i], rnd);  // xo[i] + rnd
+                // the wrap in integer arithmetic too: the compiler evaluates a cheap double
+                // expression here on every step whatever the branch, on the slow FP64 unit
                 if (dneg(v))
-                    v += P.cross_fov ? P.fov[i] : 2 * fabs(rnd);
+                    v = dadd_bits(v, P.cross_fov ? dbits(P.fov[i]) : dtwice_abs(rnd));
                 else if (dge_pos(v, P.fov[i]))
-                    v -= P.cross_fov ? P.fov[i] : 2 * fabs(rnd);
+                    v = dadd_bits(v, dflip(P.cross_fov ? dbits(P.fov[i]) : dtwice_abs(rnd)));
                 xn[i] = v;
             }
             nc -= 3;
@@ -418,9 +420,9 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
         }
         // ---- gradient (kernels.cu:181-187) ----
         if (tp == t_grad) {
-            const double g = ((double)__ldg(Tb.gx + c_grad) * xn[0] +
-                              (double)__ldg(Tb.gy + c_grad) * xn[1] +
-                              (double)__ldg(Tb.gz + c_grad) * xn[2]) *
+            const double g = ((double)__ldg(Tb.gx + c_grad) * dfrom(xn[0]) +
+                              (double)__ldg(Tb.gy + c_grad) * dfrom(xn[1]) +
+                              (double)__ldg(Tb.gz + c_grad) * dfrom(xn[2])) *
                              1e-3 * (double)P.timestep_us * 1e-6 * kGamma * kRad2Deg;
             if (KAHAN) {
                 const float ghi = (float)g;
@@ -476,7 +478,7 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
         xo[0] = xn[0]; xo[1] = xn[1]; xo[2] = xn[2];
         if (P.record_traj) {
             float *dst = O.XYZ1 + 3 * ((size_t)spin * P.traj_len + (size_t)ds * P.n_timepoints + tp);
-            dst[0] = (float)xn[0]; dst[1] = (float)xn[1]; dst[2] = (float)xn[2];
+            dst[0] = (float)dfrom(xn[0]); dst[1] = (float)dfrom(xn[1]); dst[2] = (float)dfrom(xn[2]);
         }
         tp++;
     }
@@ -501,7 +503,7 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
         nf |= kFlagDone | ((uint32_t)status << 16);
         if (!P.record_traj) {
             float *dst = O.XYZ1 + 3 * (size_t)spin * P.traj_len;
-            dst[0] = (float)xo[0]; dst[1] = (float)xo[1]; dst[2] = (float)xo[2];
+            dst[0] = (float)dfrom(xo[0]); dst[1] = (float)dfrom(xo[1]); dst[2] = (float)dfrom(xo[2]);
         }
         if (O.status) O.status[spin] = status;
     }
@@ -530,6 +532,12 @@ __global__ void k_debug_logf(const float *x, float *y, uint64_t n, LogfTables L)
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x)
         y[i] = logf_libm(x[i], s_tab, L);
+}
+
+__global__ void k_debug_dadd(const double *a, const double *b, double *y, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        y[i] = dadd_int(a[i], b[i]);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -603,6 +611,12 @@ cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevT
         k_walk<SW_PREC_FP32, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
     else
         k_walk<SW_PREC_FP32, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_dadd(const double *a, const double *b, double *y, uint64_t n,
+                              cudaStream_t st) {
+    k_debug_dadd<<<grid_for((int64_t)n, 256, 152 * 16), 256, 0, st>>>(a, b, y, n);
     return cudaGetLastError();
 }
 

@@ -25,6 +25,8 @@ cudaError_t launch_refill(const DevParams &P, const RngState &G, const uint32_t 
 cudaError_t launch_walk(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
                         const uint2 *vox, const SpinState &S, const RngState &G,
                         const Outputs &O, uint32_t *active, cudaStream_t st);
+cudaError_t launch_debug_dadd(const double *a, const double *b, double *y, uint64_t n,
+                              cudaStream_t st);
 cudaError_t launch_debug_logf(const float *x, float *y, uint64_t n, const LogfTables &L,
                               cudaStream_t st);
 

@@ -208,14 +208,14 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
             e.ds = ds;
             e.flags = r.relax ? 1u : 0u;
             put_relax(e.r, r);
-            e.xo[0] = (float)w.xo[0]; e.xo[1] = (float)w.xo[1]; e.xo[2] = (float)w.xo[2];
+            e.xo[0] = (float)dfrom(w.xo[0]); e.xo[1] = (float)dfrom(w.xo[1]); e.xo[2] = (float)dfrom(w.xo[2]);
             ds++;
             started = false;
             continue;
         }
-        if ((w.dscale != 0. && w.nc < 3) || w.uc == 0) break;       // buffers low: pause
+        if ((dnonzero(w.dscale) && w.nc < 3) || w.uc == 0) break;      // buffers low: pause
 
-        double xn[3];
+        uint64_t xn[3];
         const int mv = walk_move(w, xn, P, Tb, vox, nb, ub);
         if (mv == kMoveRejected) continue;
         if (mv == kMoveLost) { status = SW_SPIN_LOST; break; }
@@ -231,9 +231,9 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
             t_dph = c_dph < P.n_dephasing ? (uint32_t)Tb.dph_tp[c_dph] : NONE;
         }
         if (tp == t_grad) {                                         // kernels.cu:181-187
-            const double g = ((double)__ldg(Tb.gx + c_grad) * xn[0] +
-                              (double)__ldg(Tb.gy + c_grad) * xn[1] +
-                              (double)__ldg(Tb.gz + c_grad) * xn[2]) *
+            const double g = ((double)__ldg(Tb.gx + c_grad) * dfrom(xn[0]) +
+                              (double)__ldg(Tb.gy + c_grad) * dfrom(xn[1]) +
+                              (double)__ldg(Tb.gz + c_grad) * dfrom(xn[2])) *
                              1e-3 * (double)P.timestep_us * 1e-6 * kGamma * kRad2Deg;
             acc = (float)((double)acc + g);
             if (rec_started) acc_rec = (float)((double)acc_rec + g);
@@ -286,7 +286,7 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
         for (uint32_t t = 0; t < GT.n_tracks; t++) {
             if ((uint32_t)GT.track_nd[t] < ds) continue;
             float *x = GT.XYZ1[t] + 3 * (size_t)spin;
-            x[0] = (float)w.xo[0]; x[1] = (float)w.xo[1]; x[2] = (float)w.xo[2];
+            x[0] = (float)dfrom(w.xo[0]); x[1] = (float)dfrom(w.xo[1]); x[2] = (float)dfrom(w.xo[2]);
             if (GT.status[t]) GT.status[t][spin] = status;
         }
     }

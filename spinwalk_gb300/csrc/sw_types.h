@@ -72,7 +72,7 @@ struct LogfTables {
 
 // Per-spin walk state between chunks (structure of arrays, one entry per spin).
 struct SpinState {
-    double *x, *y, *z;        // xyz_old (kernels.cu:93)
+    uint64_t *x, *y, *z;      // xyz_old (kernels.cu:93): bit patterns of the doubles
     float *mx, *my, *mz;      // m0
     float *acc, *acc_e;       // accumulated phase (+ two-sum error in KAHAN mode)
     double *accd;             // FP64 phase (FP64 mode / shadow)

@@ -157,3 +157,31 @@ def test_gpu_rejects_bad_arguments():
     pr.params.matrix_length -= 1
     with pytest.raises(_lib.SpinWalkError):
         _lib.run(pr, precision=7)
+
+
+def test_gpu_integer_double_add_matches_ieee():
+    """Device dadd_int (the walk's position update) == IEEE double addition (numpy) on walk-like
+    operands, cancellations, ties and random bit patterns."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(11)
+    n = 1 << 22
+    x = rng.random(n) * 5e-4
+    g = (rng.random(n) - 0.5) * 8e-7
+    ea = rng.integers(900, 1100, n, dtype=np.uint64)
+    eb = ea + np.uint64(3) - rng.integers(0, 70, n, dtype=np.uint64)
+    fr = np.uint64(0x800fffffffffffff)
+    a = ((rng.integers(0, 2**63, n, dtype=np.uint64) * np.uint64(2)) & fr | (ea << np.uint64(52))).view(np.float64)
+    b = ((rng.integers(0, 2**63, n, dtype=np.uint64) * np.uint64(2) + np.uint64(1)) & fr | (eb << np.uint64(52))).view(np.float64)
+    tie = ((ea - np.uint64(53)) << np.uint64(52)).view(np.float64)
+    rnd = rng.integers(0, 2**63, (2, n), dtype=np.uint64).view(np.float64)
+    A = np.concatenate([x, g, -x, a, a, a, a, rnd[0]])
+    B = np.concatenate([g, x, g, b, -a, -b, tie, rnd[1]])
+    dA, dB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    dY = torch.empty_like(dA)
+    _lib.debug_dadd(dA.data_ptr(), dB.data_ptr(), dY.data_ptr(), A.size)
+    torch.cuda.synchronize()
+    got = dY.cpu().numpy()
+    with np.errstate(all="ignore"):
+        want = A + B
+    same = (got.view(np.uint64) == want.view(np.uint64)) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), f"{(~same).sum()} mismatches, first a={A[~same][0]!r} b={B[~same][0]!r}"

@@ -138,3 +138,22 @@ def test_gpu_entry_points_fail_cleanly_without_gpu():
     pr, _ = load_golden("gre")
     with pytest.raises(_lib.SpinWalkError):
         _lib.run(pr)
+
+
+def test_integer_double_add_matches_ieee_on_host(tmp_path):
+    """The walk's position update (sw_dadd.h, integer arithmetic) built for the host equals the
+    host's IEEE double addition on 8e6 operand pairs."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    exe = tmp_path / "dadd_check"
+    here = os.path.dirname(os.path.abspath(__file__))
+    csrc = os.path.join(os.path.dirname(here), "spinwalk_gb300", "csrc")
+    subprocess.run([gxx, "-O2", "-std=c++17", "-ffp-contract=off", f"-I{csrc}",
+                    os.path.join(here, "dadd_check.cpp"), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe), "1000000"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    n, bad = map(int, r.stdout.split()[-2:])
+    assert n > 8_000_000 and bad == 0

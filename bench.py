@@ -1,6 +1,7 @@
 """Benchmark of the SpinWalk `sim` hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload se|gre] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload se|gre|bssfp|c3]
+                    [--impl ours|reference]
 
 A "step" is one full pass of the hot path over one batch of synthetic input: per-spin generator
 seeding (mt19937(seed+spin) + discard), the walk over all time points and the Bloch update for
@@ -385,6 +386,83 @@ def run_batched(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def c3_instances(rank=0):
+    """Config 3: the config-1 phantom (200^3 random-orientation cylinders, r 5 um, 3 %), 32 FoV
+    scales giving vessel radii 1-100 um (log-spaced; scale = r / 5 um, WHAT_TO_SCALE = 0) x
+    {GRE, SE}; spins per instance log-uniform in [1e4, 1e6] (seed 3); TE = 5, 10, ..., 40 ms,
+    dt 50 us, SE refocusing at 20 ms. One simulation seed for all (as one config's scales)."""
+    from spinwalk_gb300 import _lib
+    from spinwalk_gb300.problem import Problem
+    n, fov = 200, 200e-6
+    mask, field = _lib.phantom_cylinders(n, fov, 5e-6, 0.03, seed=1)
+    rng = np.random.default_rng(3)
+    radii = np.logspace(0, 2, 32)
+    spins = np.round(10 ** rng.uniform(4, 6, 64)).astype(int)
+    te = tuple(range(5000, 40001, 5000))
+    seqs = {"gre": dict(TR_us=40050, TE_us=te, timestep_us=50),
+            "se": dict(TR_us=40050, TE_us=te, RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
+                       RF_us=(0, 20000), timestep_us=50)}
+    seed = 10 + 1_000_003 * rank
+    xyz0 = _lib.initial_positions([fov] * 3, seed, int(spins.max()))
+    probs = []
+    for i, r in enumerate(radii):
+        s32 = np.float32(r / 5.0)
+        f = float(s32 * np.float32(fov))
+        for j, name in enumerate(("gre", "se")):
+            ns = int(spins[2 * i + j])
+            probs.append(Problem(mask, [f] * 3, field, n_spins=ns, seed=seed,
+                                 XYZ0=(xyz0[:ns] * s32).astype(np.float32), **seqs[name]))
+    desc = dict(workload="c3_fov_sweep_32radii_x_gre_se_200cubed",
+                phantom="200^3 cylinders r5um 3% random orientation",
+                instances=len(probs), spins_per_instance="log-uniform [1e4, 1e6], seed 3",
+                sequence="GRE / SE (refocus 20 ms), TE 5..40 ms, dt 50 us, 801 time points",
+                radii_um="1..100 log-spaced (FoV scale r / 5 um)")
+    return probs, desc
+
+
+def run_batch_scales(args, world, rank):
+    """Config 3 batched (sw_sim_batch: phantom packed once, generators seeded once for all 64
+    instances, instances in spin-range chunks on concurrent slots) against the same instances
+    run one sw_sim each. `value` is timed on the host around the whole call (staging copies
+    included; every call uploads the phantom and seeds again)."""
+    import torch  # noqa: F401
+    from spinwalk_gb300 import _lib
+    probs, desc = c3_instances(rank)
+    steps = sum(p.spin_steps() for p in probs)
+    for _ in range(args.warmup):
+        _lib.run_batch(probs)
+    dev_ms, wall = [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            _lib.run_batch(probs)
+            wall.append(time.perf_counter() - t)
+            dev_ms.append(_lib.last_timing()["total_ms"])
+    clocks = clk.summary()
+    plain_ms, plain_wall = 0.0, 0.0
+    for p in probs:
+        t = time.perf_counter()
+        _lib.run(p)
+        plain_wall += time.perf_counter() - t
+        plain_ms += _lib.last_timing()["total_ms"]
+    value = world * steps / (np.mean(dev_ms) * 1e-3)
+    plain = steps / (plain_ms * 1e-3)
+    line = {"metric": "spin-steps/s (batched instances)", "value": value, "unit": "spin-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean(dev_ms)), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(desc, instance_spin_steps=int(steps)),
+            "plain_one_call_per_instance": {"value": plain, "ms": plain_ms,
+                                            "e2e_value": steps / plain_wall},
+            "batched_over_plain": value / plain,
+            "batched_over_plain_e2e": float(np.mean(wall)) and (steps / float(np.mean(wall))) / (steps / plain_wall),
+            "e2e": {"value": world * steps / float(np.mean(wall)), "unit": "spin-steps/s",
+                    "note": "sw_sim_batch with host buffers"},
+            "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -399,6 +477,8 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "bssfp":
         run_batched(args, world, rank)
+    elif args.workload == "c3":
+        run_batch_scales(args, world, rank)
     else:
         run_ours(args, world, rank, local)
 

@@ -273,6 +273,63 @@ typedef struct sw_timing {
 } sw_timing;
 int sw_last_timing(sw_timing *out);
 
+/* One instance of a batch: its parameters, sequence and host buffers, as for sw_sim. */
+typedef struct sw_instance {
+    const sw_params *param;
+    const sw_sequence *seq;
+    const float *M0, *XYZ0;  /* [n_spins][3] */
+    float *M1;               /* [n_spins][n_TE][3] */
+    float *XYZ1;             /* [n_spins][traj][3] */
+    uint8_t *T;              /* [n_spins][n_TE] */
+    int32_t *status;         /* optional [n_spins] */
+} sw_instance;
+
+/* Several instances on one phantom, e.g. the FoV- or gradient-scaled instances of
+ * monte_carlo::run's scale loop (src/sim/monte_carlo.cu:273-337) or instances with different
+ * sequences or spin counts. Every instance gives the same results as its own sw_sim call; the
+ * batch uploads and packs the phantom once and seeds the generators once: the state of spin s
+ * depends only on seed + s (src/sim/kernels.cu:82-88), so the instances (which must share the
+ * seed, phantom size, substrate count and fieldmap) start from prefixes of one seeding of the
+ * largest instance. pFieldMap is in degrees per time step (already scaled, as for sw_sim).
+ * No reference counterpart: the reference re-seeds every spin for every scale. */
+int sw_sim_batch(const sw_instance *items, uint32_t n_items, const float *pFieldMap,
+                 const uint8_t *pMask, int precision);
+
+/* ---- Engine: many jobs on one GPU (scale sweeps, serving) --------------------------------
+ * No reference counterpart: the reference runs one job at a time (monte_carlo::run). An engine
+ * keeps phantoms resident (packed once), seeds each simulation seed's generator states once for
+ * all its jobs (the state of spin s depends only on seed + s, src/sim/kernels.cu:82-88), and runs
+ * jobs in spin-range chunks on `n_slots` concurrent slots of `slot_spins` spins each (about
+ * 6.4 KB of device memory per slot spin, plus a 256 B-per-spin I/O buffer). Every job gives the
+ * results of its own sw_sim call, bit for bit. hbm_budget = 0: 85 % of the free device memory;
+ * phantoms that no queued job uses are evicted when a new one does not fit. One host thread
+ * drives an engine; its host buffers must stay valid until the job is reported done. */
+typedef struct sw_engine sw_engine;
+typedef struct sw_job_result {
+    int64_t job_id;
+    int32_t rc;              /* SW_OK or the job's error                                */
+    int32_t _pad;
+    double latency_s;        /* submit -> results in the caller's buffers               */
+} sw_job_result;
+
+int sw_engine_create(int device, uint32_t n_slots, uint32_t slot_spins, uint64_t hbm_budget,
+                     sw_engine **out);
+int sw_engine_destroy(sw_engine *e);
+/* mask u8 and optional field (degrees per time step, i.e. already scaled as for sw_sim) of
+ * dims[0] x dims[1] x dims[2] voxels, z fastest */
+int sw_engine_add_phantom(sw_engine *e, const uint8_t *mask, const float *field_deg_per_step,
+                          const uint64_t dims[3], uint32_t n_substrate, int32_t *phantom_id);
+/* queues one job (the arguments of sw_sim, on a registered phantom); nothing runs until
+ * sw_engine_poll */
+int sw_engine_submit(sw_engine *e, int32_t phantom, const sw_params *param, const sw_sequence *seq,
+                     int precision, const float *M0, const float *XYZ0, float *M1, float *XYZ1,
+                     uint8_t *T, int32_t *status, int64_t *job_id);
+/* Advances the work and reports finished jobs (at most max_done). wait: 0 = one non-blocking
+ * pass, 1 = until a job finishes or nothing is queued, 2 = until nothing is queued. */
+int sw_engine_poll(sw_engine *e, int wait, sw_job_result *done, uint32_t max_done,
+                   uint32_t *n_done);
+int sw_engine_pending(sw_engine *e, uint32_t *n_pending);
+
 /* Host-visible check of the bit-exact logf used by the Gaussian generator: evaluates the
  * device logf on n inputs (device pointers) -- used by the tests. */
 int sw_debug_logf(const float *d_x, float *d_y, uint64_t n, void *stream);

@@ -51,6 +51,17 @@ def lib():
         L.sw_sim_device_noalloc.argtypes = sim_args[:10] + [C.c_void_p]
         L.sw_sim_tracks.argtypes = [P(abi.SwParams), P(abi.SwSequence), P(abi.SwTrack), C.c_uint32,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.sw_sim_batch.argtypes = [P(abi.SwInstance), C.c_uint32, C.c_void_p, C.c_void_p, C.c_int]
+        L.sw_engine_create.argtypes = [C.c_int, C.c_uint32, C.c_uint32, C.c_uint64, P(C.c_void_p)]
+        L.sw_engine_destroy.argtypes = [C.c_void_p]
+        L.sw_engine_add_phantom.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, P(C.c_uint64),
+                                            C.c_uint32, P(C.c_int32)]
+        L.sw_engine_submit.argtypes = [C.c_void_p, C.c_int32, P(abi.SwParams), P(abi.SwSequence),
+                                       C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, P(C.c_int64)]
+        L.sw_engine_poll.argtypes = [C.c_void_p, C.c_int, P(abi.SwJobResult), C.c_uint32,
+                                     P(C.c_uint32)]
+        L.sw_engine_pending.argtypes = [C.c_void_p, P(C.c_uint32)]
         L.sw_config_dump.argtypes = [C.c_char_p, C.c_char_p]
         L.sw_run_config.argtypes = [C.c_char_p, C.c_int]
         L.sw_h5_write.argtypes = [C.c_char_p, C.c_int, P(C.c_char_p), P(C.c_int), P(C.c_int),
@@ -182,6 +193,84 @@ def run(problem, precision=abi.SW_PREC_FP32, fp64_shadow=False, fill=0.0):
     if M1d is not None:
         out["M1_fp64"] = M1d
     return out
+
+
+def run_batch(problems, precision=abi.SW_PREC_FP32, fill=0.0):
+    """sw_sim_batch over problem.Problem instances that share the phantom and the seed (the
+    phantom arrays of the first are used). Returns one output dict per instance, as run()."""
+    outs = [dict(zip(("M1", "XYZ1", "T", "status"), pr.outputs(fill))) for pr in problems]
+    arr = (abi.SwInstance * len(problems))()
+    for a, pr, o in zip(arr, problems, outs):
+        a.param = C.pointer(pr.params)
+        a.seq = C.pointer(pr.seq.struct)
+        a.M0, a.XYZ0 = _p(pr.M0), _p(pr.XYZ0)
+        a.M1, a.XYZ1, a.T, a.status = _p(o["M1"]), _p(o["XYZ1"]), _p(o["T"]), _p(o["status"])
+    pr0 = problems[0]
+    check(lib().sw_sim_batch(arr, len(problems), _p(pr0.field), _p(pr0.mask), int(precision)))
+    t = last_timing()
+    for o in outs:
+        o["timing"] = t
+    return outs
+
+
+class Engine:
+    """sw_engine: resident phantoms, one seeding per simulation seed, jobs run in spin-range
+    chunks on concurrent slots. Every job equals its own run() bit for bit."""
+
+    def __init__(self, device=0, n_slots=4, slot_spins=1 << 20, hbm_budget=0):
+        self._h = C.c_void_p()
+        check(lib().sw_engine_create(int(device), int(n_slots), int(slot_spins),
+                                     C.c_uint64(int(hbm_budget)), C.byref(self._h)))
+        self._jobs = {}                 # job id -> (problem, outputs): keep buffers alive
+
+    def add_phantom(self, problem):
+        """Registers the phantom (mask, scaled field) of a problem.Problem; returns its id."""
+        pid = C.c_int32()
+        dims = (C.c_uint64 * 3)(*problem.mask.shape)
+        check(lib().sw_engine_add_phantom(self._h, _p(problem.mask), _p(problem.field), dims,
+                                          int(problem.params.n_substrate), C.byref(pid)))
+        return pid.value
+
+    def submit(self, problem, phantom, precision=abi.SW_PREC_FP32, fill=0.0):
+        o = dict(zip(("M1", "XYZ1", "T", "status"), problem.outputs(fill)))
+        jid = C.c_int64()
+        check(lib().sw_engine_submit(self._h, int(phantom), C.byref(problem.params),
+                                     C.byref(problem.seq.struct), int(precision),
+                                     _p(problem.M0), _p(problem.XYZ0), _p(o["M1"]),
+                                     _p(o["XYZ1"]), _p(o["T"]), _p(o["status"]), C.byref(jid)))
+        self._jobs[jid.value] = (problem, o)
+        return jid.value, o
+
+    def poll(self, wait=0, max_done=256):
+        """[(job id, rc, latency s)] of jobs finished since the last poll."""
+        res = (abi.SwJobResult * max_done)()
+        n = C.c_uint32()
+        check(lib().sw_engine_poll(self._h, int(wait), res, max_done, C.byref(n)))
+        out = [(r.job_id, r.rc, r.latency_s) for r in res[:n.value]]
+        for jid, _, _ in out:
+            self._jobs.pop(jid, None)
+        return out
+
+    def run_all(self):
+        done = []
+        while True:
+            d = self.poll(wait=2)
+            done += d
+            n = C.c_uint32()
+            check(lib().sw_engine_pending(self._h, C.byref(n)))
+            if n.value == 0 and not d:
+                return done
+
+    def close(self):
+        if self._h:
+            lib().sw_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def run_device(problem, d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T, d_status=None,

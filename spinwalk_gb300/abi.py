@@ -91,6 +91,24 @@ class SwTrack(C.Structure):
     ]
 
 
+class SwInstance(C.Structure):
+    _fields_ = [
+        ("param", C.POINTER(SwParams)),
+        ("seq", C.POINTER(SwSequence)),
+        ("M0", C.c_void_p),
+        ("XYZ0", C.c_void_p),
+        ("M1", C.c_void_p),
+        ("XYZ1", C.c_void_p),
+        ("T", C.c_void_p),
+        ("status", C.c_void_p),
+    ]
+
+
+class SwJobResult(C.Structure):
+    _fields_ = [("job_id", C.c_int64), ("rc", C.c_int32), ("_pad", C.c_int32),
+                ("latency_s", C.c_double)]
+
+
 class SwTiming(C.Structure):
     _fields_ = [
         ("seed_ms", C.c_float),

@@ -248,6 +248,42 @@ sw::LogfTables logf_tables(const DeviceCtx &c) {
     return sw::LogfTables{c.d_logf_tab, c.d_logf_bitmap};
 }
 
+// Refill + walk rounds until every spin of the layout has finished (the reference's per-spin
+// loop over time points, kernels.cu:107-232, cut into rounds at which the generator rings are
+// topped up). Adds the kernel times and the number of rounds to g_timing.
+int walk_rounds(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
+                const sw::DevParams &P, const sw::DevTables &Tb, const sw::LogfTables &LT,
+                const Layout &L, const sw::Outputs &O, cudaStream_t st, uint32_t &launches) {
+    cudaEvent_t *ev = ctx.ev.data();
+    // Upper bound on rounds: every round advances each unfinished spin by >= 1 attempt.
+    const uint64_t steps = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
+    const uint64_t max_rounds = 64 + steps * (p->max_iterations + 2);
+    uint32_t chunk = 0;
+    for (;; chunk++) {
+        if (chunk >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
+        const bool timed = chunk < kMaxTimedChunks;
+        SW_CUDA(cudaMemsetAsync(L.active, 0, sizeof(uint32_t), st));
+        if (timed) SW_CUDA(cudaEventRecord(ev[4 + 2 * chunk], st));
+        SW_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
+        if (timed) SW_CUDA(cudaEventRecord(ev[5 + 2 * chunk], st));
+        SW_CUDA(sw::launch_walk(precision, dbl, P, Tb, L.vox, L.S, L.G, O, L.active, st));
+        launches += 2;
+        SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        if (timed) SW_CUDA(cudaEventRecord(ev[2], st));
+        SW_CUDA(cudaStreamSynchronize(st));
+        if (timed) {
+            float a = 0.f, b = 0.f;
+            cudaEventElapsedTime(&a, ev[4 + 2 * chunk], ev[5 + 2 * chunk]);
+            cudaEventElapsedTime(&b, ev[5 + 2 * chunk], ev[2]);
+            g_timing.refill_ms += a;
+            g_timing.walk_ms += b;
+        }
+        if (*ctx.h_active == 0) break;
+    }
+    g_timing.n_chunks += chunk + 1;
+    return SW_OK;
+}
+
 int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const float *d_field,
                const uint8_t *d_mask, const float *d_M0, const float *d_XYZ0, float *d_M1,
                float *d_XYZ1, uint8_t *d_T, int32_t *d_status, int precision, double *d_M1d,
@@ -303,36 +339,12 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
     if (*ctx.h_active != 0)
         return fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate");
 
-    // Upper bound on rounds: every round advances each unfinished spin by >= 1 attempt.
-    const uint64_t steps = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
-    const uint64_t max_rounds = 64 + steps * (p->max_iterations + 2);
-    uint32_t chunk = 0;
-    for (;; chunk++) {
-        if (chunk >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
-        const bool timed = chunk < kMaxTimedChunks;
-        SW_CUDA(cudaMemsetAsync(L.active, 0, sizeof(uint32_t), st));
-        if (timed) SW_CUDA(cudaEventRecord(ev[4 + 2 * chunk], st));
-        SW_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
-        if (timed) SW_CUDA(cudaEventRecord(ev[5 + 2 * chunk], st));
-        SW_CUDA(sw::launch_walk(precision, dbl, P, Tb, L.vox, L.S, L.G, O, L.active, st));
-        launches += 2;
-        SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        if (timed) SW_CUDA(cudaEventRecord(ev[2], st));
-        SW_CUDA(cudaStreamSynchronize(st));
-        if (timed) {
-            float a = 0.f, b = 0.f;
-            cudaEventElapsedTime(&a, ev[4 + 2 * chunk], ev[5 + 2 * chunk]);
-            cudaEventElapsedTime(&b, ev[5 + 2 * chunk], ev[2]);
-            g_timing.refill_ms += a;
-            g_timing.walk_ms += b;
-        }
-        if (*ctx.h_active == 0) break;
-    }
+    rc = walk_rounds(ctx, p, precision, dbl, P, Tb, LT, L, O, st, launches);
+    if (rc) return rc;
     SW_CUDA(cudaEventRecord(ev[3], st));
     SW_CUDA(cudaEventSynchronize(ev[3]));
     cudaEventElapsedTime(&g_timing.seed_ms, ev[0], ev[1]);
     cudaEventElapsedTime(&g_timing.total_ms, ev[0], ev[3]);
-    g_timing.n_chunks = chunk + 1;
     g_timing.n_launches = launches;
     return SW_OK;
 }

@@ -3,8 +3,8 @@
 // loop and the HDF5 outputs -- plus the HDF5 helpers of the C ABI.
 //
 // Phase-cycling scales (WHAT_TO_SCALE = 2) walk identically, so they run as tracks of one walk
-// (sw_sim_tracks, bit-identical to one run per scale); FoV and gradient scales run one sw_sim
-// per scale as in the reference.
+// (sw_sim_tracks, bit-identical to one run per scale); FoV and gradient scales run as one
+// sw_sim_batch (one walk per scale, one seeding for all), also bit-identical.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -174,26 +174,47 @@ extern "C" int sw_run_config(const char *ini_path, int device) {
             for (size_t k = 0; k < ns; k++)
                 std::copy(xyz[k].begin(), xyz[k].end(), XYZ1.begin() + 3 * n * trj * k);
         } else {
-            for (size_t k = 0; k < ns; k++) {                          // :273-337
+            // the scale loop (:273-337) as one batch: every scale is its own walk, but the
+            // phantom is packed and the generators seeded once for all scales
+            std::vector<sw_params> ps(ns, p);
+            std::vector<sw_sequence> qs(ns, q);
+            std::vector<std::vector<float>> xyz(ns), gxs(ns), gys(ns), gzs(ns);
+            std::vector<sw_instance> items(ns);
+            for (size_t k = 0; k < ns; k++) {
                 const float scale = c.scales[k];
+                xyz[k] = XYZ0;
                 if (c.scale_type == 0) {
-                    for (size_t i = 0; i < XYZ0.size(); i++) XYZ0s[i] = XYZ0[i] * scale;
-                    for (int i = 0; i < 3; i++) p.fov[i] = scale * fov[i];
+                    for (size_t i = 0; i < XYZ0.size(); i++) xyz[k][i] = XYZ0[i] * scale;
+                    for (int i = 0; i < 3; i++) ps[k].fov[i] = scale * fov[i];
                 } else if (c.scale_type == 1) {
-                    for (size_t i = 0; i < gx.size(); i++) {
-                        gx[i] = gx0[i] * scale;
-                        gy[i] = gy0[i] * scale;
-                        gz[i] = gz0[i] * scale;
+                    gxs[k] = gx0;
+                    gys[k] = gy0;
+                    gzs[k] = gz0;
+                    for (size_t i = 0; i < gx0.size(); i++) {
+                        gxs[k][i] = gx0[i] * scale;
+                        gys[k][i] = gy0[i] * scale;
+                        gzs[k][i] = gz0[i] * scale;
                     }
+                    qs[k].gradientX_mTm = gxs[k].data();
+                    qs[k].gradientY_mTm = gys[k].data();
+                    qs[k].gradientZ_mTm = gzs[k].data();
                 } else {
-                    p.linear_phase_cycling = lin0 * scale;
-                    p.quadratic_phase_cycling = quad0;
+                    ps[k].linear_phase_cycling = lin0 * scale;
+                    ps[k].quadratic_phase_cycling = quad0;
                 }
-                rc = sw_sim(&p, &q, field.empty() ? nullptr : field.data(), mask.data(), M0.data(),
-                            XYZ0s.data(), M1.data() + 3 * nte * n * k, XYZ1.data() + 3 * n * trj * k,
-                            T.data() + nte * n * k, nullptr, SW_PREC_FP32, nullptr);
-                if (rc) return drv_fail(rc, sw_last_error());
+                sw_instance &it = items[k];
+                it.param = &ps[k];
+                it.seq = &qs[k];
+                it.M0 = M0.data();
+                it.XYZ0 = xyz[k].data();
+                it.M1 = M1.data() + 3 * nte * n * k;
+                it.XYZ1 = XYZ1.data() + 3 * n * trj * k;
+                it.T = T.data() + nte * n * k;
+                it.status = nullptr;
             }
+            rc = sw_sim_batch(items.data(), (uint32_t)ns, field.empty() ? nullptr : field.data(),
+                              mask.data(), SW_PREC_FP32);
+            if (rc) return drv_fail(rc, sw_last_error());
         }
         const double sim_s = std::chrono::duration<double>(clock::now() - t_sim).count();
         std::fprintf(stderr, "spinwalk: simulation took %.3f s\n", sim_s);

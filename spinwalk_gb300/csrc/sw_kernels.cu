@@ -112,9 +112,10 @@ __global__ void __launch_bounds__(32 * kSeedWarps)
 // ------------------------------------------------------------------------------------------
 __global__ void k_init(DevParams P, DevTables Tb, const uint2 *__restrict__ vox,
                        const float *__restrict__ M0, const float *__restrict__ XYZ0,
-                       SpinState S, Outputs O, int fp64_state) {
-    const uint32_t spin = blockIdx.x * blockDim.x + threadIdx.x;
-    if (spin >= P.n_spins) return;
+                       SpinState S, Outputs O, int fp64_state, uint32_t spin_lo,
+                       uint32_t spin_hi) {
+    const uint32_t spin = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (spin >= spin_hi) return;
     float p0[3], m[3];
     for (int i = 0; i < 3; i++) {
         p0[i] = XYZ0[3 * (size_t)spin + i];
@@ -571,8 +572,16 @@ cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo
 cudaError_t launch_init(const DevParams &P, const DevTables &Tb, const uint2 *vox,
                         const float *M0, const float *XYZ0, const SpinState &S,
                         const Outputs &O, bool fp64_state, cudaStream_t st) {
-    k_init<<<grid_for(P.n_spins, 256, 1 << 30), 256, 0, st>>>(P, Tb, vox, M0, XYZ0, S, O,
-                                                              fp64_state ? 1 : 0);
+    return launch_init_range(P, Tb, vox, M0, XYZ0, S, O, fp64_state, 0, P.n_spins, st);
+}
+
+cudaError_t launch_init_range(const DevParams &P, const DevTables &Tb, const uint2 *vox,
+                              const float *M0, const float *XYZ0, const SpinState &S,
+                              const Outputs &O, bool fp64_state, uint32_t lo, uint32_t hi,
+                              cudaStream_t st) {
+    if (hi <= lo) return cudaSuccess;
+    k_init<<<grid_for(hi - lo, 256, 1 << 30), 256, 0, st>>>(P, Tb, vox, M0, XYZ0, S, O,
+                                                           fp64_state ? 1 : 0, lo, hi);
     return cudaGetLastError();
 }
 

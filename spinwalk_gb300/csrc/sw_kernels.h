@@ -20,6 +20,10 @@ cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevT
 cudaError_t launch_init(const DevParams &P, const DevTables &Tb, const uint2 *vox,
                         const float *M0, const float *XYZ0, const SpinState &S,
                         const Outputs &O, bool fp64_state, cudaStream_t st);
+cudaError_t launch_init_range(const DevParams &P, const DevTables &Tb, const uint2 *vox,
+                              const float *M0, const float *XYZ0, const SpinState &S,
+                              const Outputs &O, bool fp64_state, uint32_t lo, uint32_t hi,
+                              cudaStream_t st);
 cudaError_t launch_refill(const DevParams &P, const RngState &G, const uint32_t *flags,
                           const LogfTables &L, cudaStream_t st);
 cudaError_t launch_walk(int prec, bool dbl, const DevParams &P, const DevTables &Tb,

@@ -1,6 +1,6 @@
 """Benchmark of the SpinWalk `sim` hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload se|gre|bssfp|c3]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload se|gre|bssfp|c3|serve]
                     [--impl ours|reference]
 
 A "step" is one full pass of the hot path over one batch of synthetic input: per-spin generator
@@ -463,6 +463,110 @@ def run_batch_scales(args, world, rank):
         print(json.dumps(line), flush=True)
 
 
+def serve_requests(n_req, rng_seed=5, rank=0):
+    """Config 5 trace: Poisson arrivals (mean 20 / s), requests on resident phantoms, spins
+    log-uniform in [1e4, 1e7], a mix of GRE, SE and PGSE (b = 1000 s/mm^2, delta 10 ms, Delta
+    20 ms, lobes from 2 ms, G = 91.6 mT/m along x, y or z; TE 34 ms; dt 50 us). One simulation
+    seed for the service (its generator states are computed once, at start-up)."""
+    from spinwalk_gb300 import _lib
+    from spinwalk_gb300.problem import Problem
+    rng = np.random.default_rng(rng_seed)
+    phantoms = []
+    for n, kind, s in ((100, "cyl", 1), (200, "sph", 2), (400, "cyl", 3)):
+        fov = n * 1e-6
+        if kind == "cyl":
+            m, f = _lib.phantom_cylinders(n, fov, 5e-6, 0.03, seed=s)
+        else:
+            m, f = _lib.phantom_spheres(n, fov, 2e-6, 8e-6, 0.05, seed=s)
+        phantoms.append((m, f, fov))
+    seed = 10 + 1_000_003 * rank
+    gre = dict(TR_us=20050, TE_us=(20000,), timestep_us=50)
+    se = dict(TR_us=40050, TE_us=(40000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
+              RF_us=(0, 20000), timestep_us=50)
+    lobe = lambda t0: list(range(t0, t0 + 10000, 50))                       # noqa: E731
+    g_t = lobe(2000) + [12000] + lobe(22000) + [32000]
+    pgse = {}
+    for d, axis in enumerate("xyz"):
+        g = np.zeros((len(g_t), 3), np.float32)
+        for i, t in enumerate(g_t):
+            if t not in (12000, 32000):
+                g[i, d] = 91.6
+        pgse[axis] = dict(TR_us=34050, TE_us=(34000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
+                          RF_us=(0, 17000), timestep_us=50, gradient_us=tuple(g_t),
+                          gradient_xyz=g)
+    spins = np.round(10 ** rng.uniform(4, 7, n_req)).astype(int)
+    which = rng.integers(0, len(phantoms), n_req)
+    kinds = rng.integers(0, 5, n_req)
+    arrivals = np.cumsum(rng.exponential(1 / 20.0, n_req))
+    xyz0 = {}
+    reqs = []
+    for i in range(n_req):
+        m, f, fov = phantoms[which[i]]
+        if fov not in xyz0:
+            xyz0[fov] = _lib.initial_positions([fov] * 3, seed, int(spins.max()))
+        kw = [gre, se, pgse["x"], pgse["y"], pgse["z"]][kinds[i]]
+        reqs.append(Problem(m, [fov] * 3, f, n_spins=int(spins[i]), seed=seed,
+                            XYZ0=xyz0[fov][:spins[i]], **kw))
+    desc = dict(workload="c5_serving_poisson20_%dreq" % n_req,
+                phantoms="100^3 cylinders, 200^3 spheres, 400^3 cylinders (resident)",
+                spins_per_request="log-uniform [1e4, 1e7], seed 5",
+                sequences="GRE 20 ms / SE 40 ms / PGSE b=1000 x,y,z", arrivals="Poisson, 20 / s")
+    return reqs, phantoms, arrivals, desc
+
+
+def run_serve(args, world, rank):
+    """Config 5: the requests are submitted to one engine at their arrival times; latency =
+    submit -> results in the caller's buffers (queueing included)."""
+    import torch  # noqa: F401
+    from spinwalk_gb300 import _lib
+    n_req = args.requests
+    reqs, phantoms, arrivals, desc = serve_requests(n_req, rank=rank)
+    eng = _lib.Engine(n_slots=8, slot_spins=1 << 20)
+    pids = {}
+    t0 = time.perf_counter()
+    for pr in reqs:
+        key = pr.mask.shape
+        if key not in pids:
+            pids[key] = eng.add_phantom(pr)
+    # service start-up: generator states of the largest request, computed once
+    big = max(reqs, key=lambda p: p.params.n_spins)
+    eng.submit(big, pids[big.mask.shape])
+    eng.run_all()
+    startup_s = time.perf_counter() - t0
+    steps = sum(p.spin_steps() for p in reqs)
+    lat = []
+    with ClockSampler(0) as clk:
+        t_start = time.perf_counter()
+        i = 0
+        while i < n_req or len(lat) < n_req:
+            now = time.perf_counter() - t_start
+            while i < n_req and arrivals[i] <= now:
+                eng.submit(reqs[i], pids[reqs[i].mask.shape])
+                i += 1
+            for jid, rc, l in eng.poll(wait=0):
+                assert rc == 0
+                lat.append(l)
+            time.sleep(0.0005)
+        makespan = time.perf_counter() - t_start
+    clocks = clk.summary()
+    lat = np.array(lat)
+    value = world * steps / makespan
+    line = {"metric": "spin-steps/s (served)", "value": value, "unit": "spin-steps/s",
+            "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": makespan * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": dict(desc, requests=n_req, spin_steps=int(steps)),
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "max": float(lat.max())},
+            "offered_spin_steps_per_s": steps / float(arrivals[-1]),
+            "startup_s": startup_s,
+            "e2e": {"value": value, "unit": "spin-steps/s",
+                    "note": "host buffers in and out through the engine, arrivals in real time"},
+            "clocks": clocks}
+    eng.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -471,6 +575,7 @@ def main():
     ap.add_argument("--workload", default="se")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--requests", type=int, default=100, help="serve workload: trace length")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":
@@ -479,6 +584,8 @@ def main():
         run_batched(args, world, rank)
     elif args.workload == "c3":
         run_batch_scales(args, world, rank)
+    elif args.workload == "serve":
+        run_serve(args, world, rank)
     else:
         run_ours(args, world, rank, local)
 

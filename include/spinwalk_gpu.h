@@ -295,6 +295,17 @@ typedef struct sw_instance {
 int sw_sim_batch(const sw_instance *items, uint32_t n_items, const float *pFieldMap,
                  const uint8_t *pMask, int precision);
 
+/* Spins [spin_lo, spin_hi) of one sw_sim call, for sharding a job across GPUs or processes:
+ * M0, XYZ0, M1, XYZ1, T and status hold the rows of those spins only (row 0 = spin_lo); the
+ * results equal those rows of the full call bit for bit (a spin's generators and walk depend
+ * only on its id). Only the range's generator states are seeded. No reference counterpart (the
+ * reference's per-spin function sim::sim(..., spin_no), src/sim/kernels.cuh:21-30, is the
+ * one-spin case). */
+int sw_sim_spins(const sw_params *param, const sw_sequence *seq, const float *pFieldMap,
+                 const uint8_t *pMask, const float *M0, const float *XYZ0, uint32_t spin_lo,
+                 uint32_t spin_hi, float *M1, float *XYZ1, uint8_t *T, int32_t *status,
+                 int precision);
+
 /* ---- Engine: many jobs on one GPU (scale sweeps, serving) --------------------------------
  * No reference counterpart: the reference runs one job at a time (monte_carlo::run). An engine
  * keeps phantoms resident (packed once), seeds each simulation seed's generator states once for

@@ -62,6 +62,9 @@ def lib():
         L.sw_engine_poll.argtypes = [C.c_void_p, C.c_int, P(abi.SwJobResult), C.c_uint32,
                                      P(C.c_uint32)]
         L.sw_engine_pending.argtypes = [C.c_void_p, P(C.c_uint32)]
+        L.sw_sim_spins.argtypes = [P(abi.SwParams), P(abi.SwSequence), C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.sw_config_dump.argtypes = [C.c_char_p, C.c_char_p]
         L.sw_run_config.argtypes = [C.c_char_p, C.c_int]
         L.sw_h5_write.argtypes = [C.c_char_p, C.c_int, P(C.c_char_p), P(C.c_int), P(C.c_int),
@@ -211,6 +214,18 @@ def run_batch(problems, precision=abi.SW_PREC_FP32, fill=0.0):
     for o in outs:
         o["timing"] = t
     return outs
+
+
+def run_spins(problem, lo, hi, precision=abi.SW_PREC_FP32, fill=0.0):
+    """sw_sim_spins: rows [lo, hi) of run(problem) (M1, XYZ1, T, status hold those rows only)."""
+    M1, XYZ1, T, status = problem.outputs(fill)
+    M1, XYZ1, T, status = (np.ascontiguousarray(a[lo:hi]) for a in (M1, XYZ1, T, status))
+    M0 = np.ascontiguousarray(problem.M0[lo:hi])
+    XYZ0 = np.ascontiguousarray(problem.XYZ0[lo:hi])
+    check(lib().sw_sim_spins(C.byref(problem.params), C.byref(problem.seq.struct),
+                             _p(problem.field), _p(problem.mask), _p(M0), _p(XYZ0), int(lo),
+                             int(hi), _p(M1), _p(XYZ1), _p(T), _p(status), int(precision)))
+    return dict(M1=M1, XYZ1=XYZ1, T=T, status=status)
 
 
 class Engine:

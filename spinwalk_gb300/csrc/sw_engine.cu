@@ -88,9 +88,9 @@ struct Phantom {
 };
 
 struct SeedCache {
-    uint32_t *mt = nullptr;         // [cap][624]
+    uint32_t *mt = nullptr;         // [cap][624]: spins base .. base + n - 1
     uint32_t *p = nullptr;          // [cap]
-    uint32_t n = 0, cap = 0;        // spins seeded / allocated
+    uint32_t base = 0, n = 0, cap = 0;
     cudaEvent_t ready = nullptr;    // recorded after the last seeding on the seed stream
 };
 
@@ -112,7 +112,8 @@ struct Job {
     uint8_t *T = nullptr;
     int32_t *status = nullptr;
     size_t nte = 0, trj = 0;
-    uint32_t next_lo = 0, chunk = 0;  // next spin to hand out, spins per chunk
+    uint32_t spin_lo = 0, spin_hi = 0;  // the job's spins; host buffers hold their rows only
+    uint32_t next_lo = 0, chunk = 0;    // next spin to hand out, spins per chunk
     int running = 0;
     int rc = SW_OK;
     double t_submit = 0, t_done = 0;
@@ -158,7 +159,34 @@ struct sw_engine {
 
 namespace {
 
-int ensure_seeded(sw_engine *E, uint64_t seed, uint32_t n, SeedCache *&out) {
+// Seeds k_seed's range [a, b) into cache C (whose first spin is C.base) on the seed stream.
+int seed_into(sw_engine *E, SeedCache &C, uint64_t seed, uint32_t a, uint32_t b) {
+    if (b <= a) return SW_OK;
+    if (E->scratch_cap < b - C.base) {
+        if (E->seed_scratch) {
+            EN_CUDA(cudaStreamSynchronize(E->seed_st));
+            cudaFree(E->seed_scratch);
+            E->seed_scratch = nullptr;
+            E->scratch_cap = 0;
+        }
+        EN_CUDA(cudaMalloc(&E->seed_scratch, (size_t)C.cap * 4));
+        E->scratch_cap = C.cap;
+    }
+    sw::DevParams P{};
+    P.seed = seed;
+    sw::RngState G{};
+    G.mt_r = G.mt_u = shift(C.mt, (uint64_t)C.base * sw::kMtN);
+    G.p_r = G.p_u = shift(C.p, (uint64_t)C.base);
+    G.nhead = G.ncnt = G.uhead = G.ucnt = shift(E->seed_scratch, (uint64_t)C.base);
+    EN_CUDA(sw::launch_seed_range(P, G, a, b, E->seed_st));
+    E->launches++;
+    E->seedings++;
+    return SW_OK;
+}
+
+// Makes the seed cache of `seed` hold spins [lo, hi) (the generator state of spin s after
+// mt19937(seed + s).discard(seed + s), kernels.cu:82-88); grows it when needed.
+int ensure_seeded(sw_engine *E, uint64_t seed, uint32_t lo, uint32_t hi, SeedCache *&out) {
     auto &slot = E->seeds[seed];
     if (!slot) {
         slot.reset(new SeedCache());
@@ -166,18 +194,24 @@ int ensure_seeded(sw_engine *E, uint64_t seed, uint32_t n, SeedCache *&out) {
     }
     SeedCache &C = *slot;
     out = &C;
-    if (C.n >= n) return SW_OK;
-    if (n > C.cap) {                         // grow: copy what is seeded, then extend
-        const uint32_t cap = std::max<uint32_t>(n, std::min<uint64_t>(2ull * C.cap, 0xffffffffu));
-        const size_t bytes = (size_t)cap * sw::kMtN * 4 + (size_t)cap * 4;
+    if (C.n && lo >= C.base && hi <= C.base + C.n) return SW_OK;
+    const uint32_t old_lo = C.base, old_hi = C.base + C.n;
+    const uint32_t new_lo = C.n ? std::min(lo, old_lo) : lo;
+    const uint32_t new_hi = C.n ? std::max(hi, old_hi) : hi;
+    if (new_lo != old_lo || new_hi - new_lo > C.cap) {      // reallocate, keep what is seeded
+        const uint64_t want = (uint64_t)new_hi - new_lo;
+        const uint32_t cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(want, 2ull * C.cap), 0xffffffffu);
+        const uint32_t capped = (uint32_t)std::max<uint64_t>(want, std::min<uint64_t>(cap, want + (want >> 1)));
+        const size_t bytes = (size_t)capped * sw::kMtN * 4 + (size_t)capped * 4;
         if (E->used + bytes > E->budget)
-            return fail(SW_ERR_NOMEM, "seed cache of " + std::to_string(cap) + " spins exceeds the HBM budget");
+            return fail(SW_ERR_NOMEM, "seed cache of " + std::to_string(capped) + " spins exceeds the HBM budget");
         uint32_t *mt = nullptr, *p = nullptr;
-        EN_CUDA(cudaMalloc(&mt, (size_t)cap * sw::kMtN * 4));
-        EN_CUDA(cudaMalloc(&p, (size_t)cap * 4));
+        EN_CUDA(cudaMalloc(&mt, (size_t)capped * sw::kMtN * 4));
+        EN_CUDA(cudaMalloc(&p, (size_t)capped * 4));
         if (C.n) {
-            EN_CUDA(cudaMemcpyAsync(mt, C.mt, (size_t)C.n * sw::kMtN * 4, cudaMemcpyDeviceToDevice, E->seed_st));
-            EN_CUDA(cudaMemcpyAsync(p, C.p, (size_t)C.n * 4, cudaMemcpyDeviceToDevice, E->seed_st));
+            const size_t o = (size_t)old_lo - new_lo;
+            EN_CUDA(cudaMemcpyAsync(mt + o * sw::kMtN, C.mt, (size_t)C.n * sw::kMtN * 4, cudaMemcpyDeviceToDevice, E->seed_st));
+            EN_CUDA(cudaMemcpyAsync(p + o, C.p, (size_t)C.n * 4, cudaMemcpyDeviceToDevice, E->seed_st));
         }
         if (C.mt) {                          // slots may still be copying from the old cache
             EN_CUDA(cudaDeviceSynchronize());
@@ -187,41 +221,32 @@ int ensure_seeded(sw_engine *E, uint64_t seed, uint32_t n, SeedCache *&out) {
         }
         C.mt = mt;
         C.p = p;
-        C.cap = cap;
+        C.cap = capped;
         E->used += bytes;
     }
-    if (E->scratch_cap < n) {
-        if (E->seed_scratch) {
-            EN_CUDA(cudaStreamSynchronize(E->seed_st));
-            cudaFree(E->seed_scratch);
-        }
-        EN_CUDA(cudaMalloc(&E->seed_scratch, (size_t)C.cap * 4));
-        E->scratch_cap = C.cap;
+    C.base = new_lo;
+    int rc = SW_OK;
+    if (C.n == 0) {
+        rc = seed_into(E, C, seed, new_lo, new_hi);
+    } else {
+        if (!rc) rc = seed_into(E, C, seed, new_lo, old_lo);
+        if (!rc) rc = seed_into(E, C, seed, old_hi, new_hi);
     }
-    sw::DevParams P{};
-    P.seed = seed;
-    sw::RngState G{};
-    G.mt_r = G.mt_u = C.mt;
-    G.p_r = G.p_u = C.p;
-    G.nhead = G.ncnt = G.uhead = G.ucnt = E->seed_scratch;
-    EN_CUDA(sw::launch_seed_range(P, G, C.n, n, E->seed_st));
-    E->launches++;
-    E->seedings++;
+    if (rc) return rc;
     EN_CUDA(cudaEventRecord(C.ready, E->seed_st));
-    C.n = n;
+    C.n = new_hi - new_lo;
     return SW_OK;
 }
 
 // Hands the next spin range of a ready job to a free slot and issues the chunk's work.
 int start_chunk(sw_engine *E, Slot &s, Job &j) {
-    const uint32_t n = (uint32_t)j.p.n_spins;
-    const uint32_t lo = j.next_lo, hi = std::min<uint32_t>(n, lo + j.chunk);
+    const uint32_t lo = j.next_lo, hi = std::min<uint32_t>(j.spin_hi, lo + j.chunk);
     j.next_lo = hi;
     j.running++;
     s.job = &j;
     s.lo = lo;
     s.hi = hi;
-    const size_t c = hi - lo, nte = j.nte, trj = j.trj;
+    const size_t c = hi - lo, nte = j.nte, trj = j.trj, r = lo - j.spin_lo;   // r: first host row
     size_t off = 0;
     auto sec = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~size_t(255); return o; };
     s.o_M0 = sec(c * 12);
@@ -234,21 +259,22 @@ int start_chunk(sw_engine *E, Slot &s, Job &j) {
     s.out_bytes = off - s.o_M1;
     // stage: inputs and the caller's current output contents (slots the walk never reaches keep
     // them, as with sw_sim)
-    par_memcpy(s.h_io + s.o_M0, j.M0 + 3 * (size_t)lo, c * 12);
-    par_memcpy(s.h_io + s.o_XYZ0, j.XYZ0 + 3 * (size_t)lo, c * 12);
+    par_memcpy(s.h_io + s.o_M0, j.M0 + 3 * r, c * 12);
+    par_memcpy(s.h_io + s.o_XYZ0, j.XYZ0 + 3 * r, c * 12);
     if (nte) {
-        par_memcpy(s.h_io + s.o_M1, j.M1 + 3 * nte * lo, c * nte * 12);
-        par_memcpy(s.h_io + s.o_T, j.T + nte * lo, c * nte);
+        par_memcpy(s.h_io + s.o_M1, j.M1 + 3 * nte * r, c * nte * 12);
+        par_memcpy(s.h_io + s.o_T, j.T + nte * r, c * nte);
     }
-    par_memcpy(s.h_io + s.o_XYZ1, j.XYZ1 + 3 * trj * lo, c * trj * 12);
+    par_memcpy(s.h_io + s.o_XYZ1, j.XYZ1 + 3 * trj * r, c * trj * 12);
     EN_CUDA(cudaMemcpyAsync(s.d_io, s.h_io, s.in_bytes, cudaMemcpyHostToDevice, s.st));
     EN_CUDA(cudaMemcpyAsync(s.L.tables, j.h_tables, j.im.bytes.size(), cudaMemcpyHostToDevice, s.st));
     // generator states of spins [lo, hi): the job's range of the seed cache, both generators
     EN_CUDA(cudaStreamWaitEvent(s.st, j.seed->ready, 0));
-    EN_CUDA(cudaMemcpyAsync(s.L.G.mt_r, j.seed->mt + (size_t)lo * sw::kMtN, c * sw::kMtN * 4, cudaMemcpyDeviceToDevice, s.st));
-    EN_CUDA(cudaMemcpyAsync(s.L.G.mt_u, j.seed->mt + (size_t)lo * sw::kMtN, c * sw::kMtN * 4, cudaMemcpyDeviceToDevice, s.st));
-    EN_CUDA(cudaMemcpyAsync(s.L.G.p_r, j.seed->p + lo, c * 4, cudaMemcpyDeviceToDevice, s.st));
-    EN_CUDA(cudaMemcpyAsync(s.L.G.p_u, j.seed->p + lo, c * 4, cudaMemcpyDeviceToDevice, s.st));
+    const size_t sc = lo - j.seed->base;                 // the chunk's first spin in the cache
+    EN_CUDA(cudaMemcpyAsync(s.L.G.mt_r, j.seed->mt + sc * sw::kMtN, c * sw::kMtN * 4, cudaMemcpyDeviceToDevice, s.st));
+    EN_CUDA(cudaMemcpyAsync(s.L.G.mt_u, j.seed->mt + sc * sw::kMtN, c * sw::kMtN * 4, cudaMemcpyDeviceToDevice, s.st));
+    EN_CUDA(cudaMemcpyAsync(s.L.G.p_r, j.seed->p + sc, c * 4, cudaMemcpyDeviceToDevice, s.st));
+    EN_CUDA(cudaMemcpyAsync(s.L.G.p_u, j.seed->p + sc, c * 4, cudaMemcpyDeviceToDevice, s.st));
     EN_CUDA(cudaMemsetAsync(s.L.G.nhead, 0, c * 4, s.st));
     EN_CUDA(cudaMemsetAsync(s.L.G.ncnt, 0, c * 4, s.st));
     EN_CUDA(cudaMemsetAsync(s.L.G.uhead, 0, c * 4, s.st));
@@ -322,7 +348,7 @@ int issue_rounds(sw_engine *E, Slot &s, uint64_t k, bool first) {
 }
 
 void job_done_check(sw_engine *E, Job &j) {
-    if (j.running == 0 && (j.next_lo >= j.p.n_spins || j.rc != SW_OK)) {
+    if (j.running == 0 && (j.next_lo >= j.spin_hi || j.rc != SW_OK)) {
         j.t_done = now_s();
         E->phantoms[j.phantom].jobs--;
         if (j.h_tables) {
@@ -374,13 +400,13 @@ int pump(sw_engine *E, int &rc) {
                 s.state = Slot::DRAINING;
             }
         } else {                                         // DRAINING: results are in h_io
-            const size_t c = s.hi - s.lo, nte = j.nte, trj = j.trj;
+            const size_t c = s.hi - s.lo, nte = j.nte, trj = j.trj, r = s.lo - j.spin_lo;
             if (nte) {
-                par_memcpy(j.M1 + 3 * nte * s.lo, s.h_io + s.o_M1, c * nte * 12);
-                par_memcpy(j.T + nte * s.lo, s.h_io + s.o_T, c * nte);
+                par_memcpy(j.M1 + 3 * nte * r, s.h_io + s.o_M1, c * nte * 12);
+                par_memcpy(j.T + nte * r, s.h_io + s.o_T, c * nte);
             }
-            par_memcpy(j.XYZ1 + 3 * trj * s.lo, s.h_io + s.o_XYZ1, c * trj * 12);
-            if (j.status) par_memcpy(j.status + s.lo, s.h_io + s.o_st, c * 4);
+            par_memcpy(j.XYZ1 + 3 * trj * r, s.h_io + s.o_XYZ1, c * trj * 12);
+            if (j.status) par_memcpy(j.status + r, s.h_io + s.o_st, c * 4);
             j.running--;
             s.state = Slot::FREE;
             s.job = nullptr;
@@ -391,7 +417,7 @@ int pump(sw_engine *E, int &rc) {
         if (s.state != Slot::FREE) continue;
         Job *pick = nullptr;
         for (auto &jp : E->queue)
-            if (jp->rc == SW_OK && jp->next_lo < jp->p.n_spins && jp->chunk > 0) {
+            if (jp->rc == SW_OK && jp->next_lo < jp->spin_hi && jp->chunk > 0) {
                 pick = jp.get();
                 break;
             }
@@ -406,7 +432,8 @@ int pump(sw_engine *E, int &rc) {
 
 int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_sequence *q,
                   int precision, const float *M0, const float *XYZ0, float *M1, float *XYZ1,
-                  uint8_t *T, int32_t *status, int64_t *job_id) {
+                  uint8_t *T, int32_t *status, int64_t *job_id, uint64_t spin_lo = 0,
+                  uint64_t spin_hi = ~0ull) {
     int rc = check_args(p, q);
     if (rc) return rc;
     auto pit = E->phantoms.find(phantom);
@@ -419,11 +446,13 @@ int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_se
     if (p->fieldmap_exist && !ph.field) return fail(SW_ERR_INVALID, "fieldmap_exist but the phantom has no fieldmap");
     if (precision != SW_PREC_FP32 && precision != SW_PREC_FP64 && precision != SW_PREC_KAHAN)
         return fail(SW_ERR_INVALID, "precision");
-    const size_t n = p->n_spins, nte = q->n_TE;
+    if (p->n_spins > 0xffffffffull) return fail(SW_ERR_INVALID, "n_spins");
+    if (spin_hi == ~0ull) spin_hi = p->n_spins;
+    if (spin_lo > spin_hi || spin_hi > p->n_spins) return fail(SW_ERR_INVALID, "spin range outside [0, n_spins)");
+    const size_t n = spin_hi - spin_lo, nte = q->n_TE;
     const size_t trj = p->enRecordTrajectory ? (size_t)(p->n_dummy_scan + 1) * p->n_timepoints : 1;
     if (n && (!M0 || !XYZ0 || !XYZ1 || (nte && (!M1 || !T))))
         return fail(SW_ERR_INVALID, "null host buffer");
-    if (n > 0xffffffffull) return fail(SW_ERR_INVALID, "n_spins");
     std::unique_ptr<Job> j(new Job());
     j->id = E->next_job++;
     j->phantom = phantom;
@@ -465,13 +494,15 @@ int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_se
     j->M0 = M0; j->XYZ0 = XYZ0; j->M1 = M1; j->XYZ1 = XYZ1; j->T = T; j->status = status;
     j->nte = nte;
     j->trj = trj;
+    j->spin_lo = j->next_lo = (uint32_t)spin_lo;
+    j->spin_hi = (uint32_t)spin_hi;
     // chunk: a slot's spin capacity, or what its I/O buffer holds for this job
     const size_t per_spin = 24 + nte * 13 + trj * 12 + 4 + 5 * 256;
     const Slot &s0 = E->slots[0];
     j->chunk = (uint32_t)std::min<size_t>(s0.cap, s0.io_bytes / per_spin);
     if (n && j->chunk == 0) return fail(SW_ERR_NOMEM, "one spin's trajectory exceeds a slot's I/O buffer");
     if (n) {
-        rc = ensure_seeded(E, p->seed, (uint32_t)n, j->seed);
+        rc = ensure_seeded(E, p->seed, (uint32_t)spin_lo, (uint32_t)spin_hi, j->seed);
         if (rc) {
             cudaFreeHost(j->h_tables);
             return rc;
@@ -670,6 +701,62 @@ namespace {
 constexpr int kMaxBatchDevices = 64;
 std::mutex g_batch_mu;
 sw_engine *g_batch_engine[kMaxBatchDevices] = {};
+
+// The engine of the one-call entry points (sw_sim_batch, sw_sim_spins) on the current device:
+// its slots (workspaces, staging buffers) are kept from call to call; the caller holds
+// g_batch_mu.
+int acquire_call_engine(uint32_t slots, uint32_t slot_spins, sw_engine *&out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxBatchDevices)
+        return fail(SW_ERR_CUDA, "no current CUDA device");
+    sw_engine *&E = g_batch_engine[dev];
+    if (E && (E->slots.size() < slots || E->slots[0].cap < slot_spins)) {
+        engine_free(E);
+        E = nullptr;
+    }
+    int rc = SW_OK;
+    if (!E && (rc = engine_create(dev, slots, slot_spins, 0, &E))) {
+        E = nullptr;
+        return rc;
+    }
+    E->launches = E->rounds = E->seedings = 0;
+    out = E;
+    return SW_OK;
+}
+
+// Runs the queued jobs to completion and drops the call's phantoms and seed caches (every call
+// does its full work); after a failure the whole engine is dropped.
+int finish_call_engine(sw_engine *E, int rc) {
+    while (!rc && !E->queue.empty()) {
+        const int progress = pump(E, rc);
+        if (!progress && !rc) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+    for (auto &j : E->finished)
+        if (!rc && j->rc) rc = j->rc;
+    const std::string err = rc ? std::string(sw_last_error()) : std::string();
+    g_timing.n_launches = (uint32_t)E->launches;
+    g_timing.n_chunks = (uint32_t)E->rounds;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (rc) {
+        engine_free(E);
+        g_batch_engine[dev] = nullptr;
+        return fail(rc, err);
+    }
+    cudaDeviceSynchronize();
+    for (auto &kv : E->phantoms) cudaFree(kv.second.vox);
+    E->phantoms.clear();
+    for (auto &kv : E->seeds) {
+        cudaFree(kv.second->mt);
+        cudaFree(kv.second->p);
+        cudaEventDestroy(kv.second->ready);
+    }
+    E->seeds.clear();
+    E->finished.clear();
+    E->used = 0;
+    for (const Slot &s : E->slots) E->used += s.L.bytes + s.io_bytes;
+    return SW_OK;
+}
 }  // namespace
 
 extern "C" {
@@ -701,30 +788,18 @@ int sw_sim_batch(const sw_instance *items, uint32_t n_items, const float *pField
     g_timing = sw_timing{};
     const double t0 = now_s();
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxBatchDevices)
-        return fail(SW_ERR_CUDA, "no current CUDA device");
-    // The slots (workspaces, staging buffers) of the last batch on this device are kept for the
-    // next one; phantom and seed cache are per call, so every call does its full work.
     std::lock_guard<std::mutex> lk(g_batch_mu);
-    sw_engine *&E = g_batch_engine[dev];
     const uint32_t slots = std::min<uint32_t>(8, n_items);
     const uint32_t slot_spins = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(n_max, 1u << 20));
-    if (E && (E->slots.size() < slots || E->slots[0].cap < slot_spins)) {
-        engine_free(E);
-        E = nullptr;
-    }
-    int rc = SW_OK;
-    if (!E && (rc = engine_create(dev, slots, slot_spins, 0, &E))) {
-        E = nullptr;
-        return rc;
-    }
-    E->launches = E->rounds = E->seedings = 0;
+    sw_engine *E = nullptr;
+    int rc = acquire_call_engine(slots, slot_spins, E);
+    if (rc) return rc;
     const uint64_t dims[3] = {p0->phantom_size[0], p0->phantom_size[1], p0->phantom_size[2]};
     int32_t ph = 0;
     rc = engine_add_phantom(E, pMask, p0->fieldmap_exist ? pFieldMap : nullptr, dims,
                             p0->n_substrate, &ph);
     SeedCache *sc = nullptr;
-    if (!rc) rc = ensure_seeded(E, p0->seed, (uint32_t)n_max, sc);    // one seeding, largest n
+    if (!rc) rc = ensure_seeded(E, p0->seed, 0, (uint32_t)n_max, sc);   // one seeding, largest n
     std::vector<uint32_t> order(n_items);
     for (uint32_t i = 0; i < n_items; i++) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
@@ -737,35 +812,42 @@ int sw_sim_batch(const sw_instance *items, uint32_t n_items, const float *pField
         rc = engine_submit(E, ph, it.param, it.seq, precision, it.M0, it.XYZ0, it.M1, it.XYZ1,
                            it.T, it.status, &jid);
     }
-    while (!rc && !E->queue.empty()) {
-        const int progress = pump(E, rc);
-        if (!progress && !rc) std::this_thread::sleep_for(std::chrono::microseconds(20));
-    }
-    for (auto &j : E->finished)
-        if (!rc && j->rc) rc = j->rc;
-    const std::string err = rc ? std::string(sw_last_error()) : std::string();
-    g_timing.n_launches = (uint32_t)E->launches;
-    g_timing.n_chunks = (uint32_t)E->rounds;
     const uint64_t seedings = E->seedings;
-    if (rc) {                                    // drop everything after a failure
-        engine_free(E);
-        E = nullptr;
-    } else {                                     // keep the slots only
-        cudaDeviceSynchronize();
-        for (auto &kv : E->phantoms) cudaFree(kv.second.vox);
-        E->phantoms.clear();
-        for (auto &kv : E->seeds) {
-            cudaFree(kv.second->mt);
-            cudaFree(kv.second->p);
-            cudaEventDestroy(kv.second->ready);
-        }
-        E->seeds.clear();
-        E->finished.clear();
-        E->used = 0;
-        for (const Slot &s : E->slots) E->used += s.L.bytes + s.io_bytes;
-    }
+    rc = finish_call_engine(E, rc);
     if (!rc && seedings > 1) rc = fail(SW_ERR_INVALID, "internal error: batch seeded more than once");
-    if (rc) return fail(rc, err);
+    if (rc) return rc;
+    g_timing.total_ms = (float)((now_s() - t0) * 1e3);
+    return SW_OK;
+}
+
+int sw_sim_spins(const sw_params *param, const sw_sequence *seq, const float *pFieldMap,
+                 const uint8_t *pMask, const float *M0, const float *XYZ0, uint32_t spin_lo,
+                 uint32_t spin_hi, float *M1, float *XYZ1, uint8_t *T, int32_t *status,
+                 int precision) {
+    int rc = check_args(param, seq);
+    if (rc) return rc;
+    if (!pMask) return fail(SW_ERR_INVALID, "null mask");
+    if (param->fieldmap_exist && !pFieldMap) return fail(SW_ERR_INVALID, "null fieldmap");
+    if (spin_lo > spin_hi || spin_hi > param->n_spins)
+        return fail(SW_ERR_INVALID, "spin range outside [0, n_spins)");
+    g_timing = sw_timing{};
+    if (spin_hi == spin_lo) return SW_OK;
+    const double t0 = now_s();
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    sw_engine *E = nullptr;
+    const uint32_t n = spin_hi - spin_lo;
+    rc = acquire_call_engine(4, std::max<uint32_t>(1, std::min<uint32_t>((n + 3) / 4, 1u << 20)), E);
+    if (rc) return rc;
+    const uint64_t dims[3] = {param->phantom_size[0], param->phantom_size[1], param->phantom_size[2]};
+    int32_t ph = 0;
+    rc = engine_add_phantom(E, pMask, param->fieldmap_exist ? pFieldMap : nullptr, dims,
+                            param->n_substrate, &ph);
+    int64_t jid = 0;
+    if (!rc)
+        rc = engine_submit(E, ph, param, seq, precision, M0, XYZ0, M1, XYZ1, T, status, &jid,
+                           spin_lo, spin_hi);
+    rc = finish_call_engine(E, rc);
+    if (rc) return rc;
     g_timing.total_ms = (float)((now_s() - t0) * 1e3);
     return SW_OK;
 }

@@ -341,6 +341,28 @@ int sw_engine_poll(sw_engine *e, int wait, sw_job_result *done, uint32_t max_don
                    uint32_t *n_done);
 int sw_engine_pending(sw_engine *e, uint32_t *n_pending);
 
+/* ---- The reference's phantom generators, mask and field on the GPU -----------------------
+ * phantom::cylinder (src/phantom/phantom_cylinder.cpp: parallel cylinders along z, B0 rotated
+ * by `orientation_deg` about y) and phantom::sphere (phantom_sphere.cpp), with the reference's
+ * arguments and units: fov in um, `resolution` voxels per side, dChi, Y (< 0: no field),
+ * radius in um (< 0: random radii up to |radius|), volume fraction in percent, seed. Outputs:
+ * mask u8 and field f32 (T at B0 = 1 T; may be NULL) of resolution^3 voxels, z fastest, and the
+ * actual volume fraction. Shapes are placed on the host as the reference does; mask and field
+ * are bit-identical to the reference's (with random radii: to the reference run on one
+ * thread). The _device variants take device buffers (e.g. for sw_engine_add_phantom). */
+int sw_phantom_cylinder(float fov_um, uint64_t resolution, float dchi, float Y, float radius_um,
+                        float volume_fraction, float orientation_deg, int32_t seed, uint8_t *mask,
+                        float *field, float *bvf_out);
+int sw_phantom_sphere(float fov_um, uint64_t resolution, float dchi, float Y, float radius_um,
+                      float volume_fraction, int32_t seed, uint8_t *mask, float *field,
+                      float *bvf_out);
+int sw_phantom_cylinder_device(float fov_um, uint64_t resolution, float dchi, float Y,
+                               float radius_um, float volume_fraction, float orientation_deg,
+                               int32_t seed, uint8_t *d_mask, float *d_field, float *bvf_out);
+int sw_phantom_sphere_device(float fov_um, uint64_t resolution, float dchi, float Y,
+                             float radius_um, float volume_fraction, int32_t seed,
+                             uint8_t *d_mask, float *d_field, float *bvf_out);
+
 /* Host-visible check of the bit-exact logf used by the Gaussian generator: evaluates the
  * device logf on n inputs (device pointers) -- used by the tests. */
 int sw_debug_logf(const float *d_x, float *d_y, uint64_t n, void *stream);

@@ -65,6 +65,12 @@ def lib():
         L.sw_sim_spins.argtypes = [P(abi.SwParams), P(abi.SwSequence), C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        for f in (L.sw_phantom_cylinder, L.sw_phantom_cylinder_device):
+            f.argtypes = [C.c_float, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_float,
+                          C.c_float, C.c_int32, C.c_void_p, C.c_void_p, P(C.c_float)]
+        for f in (L.sw_phantom_sphere, L.sw_phantom_sphere_device):
+            f.argtypes = [C.c_float, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_float,
+                          C.c_int32, C.c_void_p, C.c_void_p, P(C.c_float)]
         L.sw_config_dump.argtypes = [C.c_char_p, C.c_char_p]
         L.sw_run_config.argtypes = [C.c_char_p, C.c_int]
         L.sw_h5_write.argtypes = [C.c_char_p, C.c_int, P(C.c_char_p), P(C.c_int), P(C.c_int),
@@ -214,6 +220,33 @@ def run_batch(problems, precision=abi.SW_PREC_FP32, fill=0.0):
     for o in outs:
         o["timing"] = t
     return outs
+
+
+def phantom_cylinder(fov_um, resolution, dchi=0.11e-6, Y=0.75, radius_um=8.0,
+                     volume_fraction=4.0, orientation_deg=90.0, seed=10, field=True):
+    """The reference's phantom::cylinder generated on the GPU: (mask u8, field f32 or None,
+    actual volume fraction in percent), arrays of shape (res, res, res)."""
+    n = int(resolution) ** 3
+    mask = np.zeros(n, np.uint8)
+    fld = np.zeros(n, np.float32) if field and Y >= 0 else None
+    bvf = C.c_float()
+    check(lib().sw_phantom_cylinder(fov_um, resolution, dchi, Y, radius_um, volume_fraction,
+                                    orientation_deg, seed, _p(mask), _p(fld), C.byref(bvf)))
+    shape = (resolution,) * 3
+    return mask.reshape(shape), (fld.reshape(shape) if fld is not None else None), bvf.value
+
+
+def phantom_sphere(fov_um, resolution, dchi=0.11e-6, Y=0.75, radius_um=8.0,
+                   volume_fraction=4.0, seed=10, field=True):
+    """The reference's phantom::sphere generated on the GPU (see phantom_cylinder)."""
+    n = int(resolution) ** 3
+    mask = np.zeros(n, np.uint8)
+    fld = np.zeros(n, np.float32) if field and Y >= 0 else None
+    bvf = C.c_float()
+    check(lib().sw_phantom_sphere(fov_um, resolution, dchi, Y, radius_um, volume_fraction, seed,
+                                  _p(mask), _p(fld), C.byref(bvf)))
+    shape = (resolution,) * 3
+    return mask.reshape(shape), (fld.reshape(shape) if fld is not None else None), bvf.value
 
 
 def run_spins(problem, lo, hi, precision=abi.SW_PREC_FP32, fill=0.0):

@@ -1,6 +1,7 @@
 """Benchmark of the SpinWalk `sim` hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload se|gre|bssfp|c3|serve]
+    python bench.py [--gpus N] [--steps K] [--warmup W]
+                    [--workload se|gre|bssfp|c3|serve|phantom]
                     [--impl ours|reference]
 
 A "step" is one full pass of the hot path over one batch of synthetic input: per-spin generator
@@ -472,12 +473,14 @@ def serve_requests(n_req, rng_seed=5, rank=0):
     from spinwalk_gb300.problem import Problem
     rng = np.random.default_rng(rng_seed)
     phantoms = []
-    for n, kind, s in ((100, "cyl", 1), (200, "sph", 2), (400, "cyl", 3)):
+    for n, kind, s in ((100, "cyl", 1), (200, "sph", 2), (800, "ref_cyl", 3)):
         fov = n * 1e-6
         if kind == "cyl":
             m, f = _lib.phantom_cylinders(n, fov, 5e-6, 0.03, seed=s)
-        else:
+        elif kind == "sph":
             m, f = _lib.phantom_spheres(n, fov, 2e-6, 8e-6, 0.05, seed=s)
+        else:      # the reference's cylinder phantom, generated on the GPU
+            m, f, _ = _lib.phantom_cylinder(float(n), n, 0.11e-6 * 0.4, 0.75, 5.0, 3.0, 90.0, s)
         phantoms.append((m, f, fov))
     seed = 10 + 1_000_003 * rank
     gre = dict(TR_us=20050, TE_us=(20000,), timestep_us=50)
@@ -508,7 +511,7 @@ def serve_requests(n_req, rng_seed=5, rank=0):
         reqs.append(Problem(m, [fov] * 3, f, n_spins=int(spins[i]), seed=seed,
                             XYZ0=xyz0[fov][:spins[i]], **kw))
     desc = dict(workload="c5_serving_poisson20_%dreq" % n_req,
-                phantoms="100^3 cylinders, 200^3 spheres, 400^3 cylinders (resident)",
+                phantoms="100^3 cylinders, 200^3 spheres, 800^3 reference cylinders (resident)",
                 spins_per_request="log-uniform [1e4, 1e7], seed 5",
                 sequences="GRE 20 ms / SE 40 ms / PGSE b=1000 x,y,z", arrivals="Poisson, 20 / s")
     return reqs, phantoms, arrivals, desc
@@ -567,6 +570,32 @@ def run_serve(args, world, rank):
         print(json.dumps(line), flush=True)
 
 
+def run_phantom(args, world, rank):
+    """The reference's cylinder phantom (phantom::cylinder: 800 um FoV, 800^3 voxels, r 5 um,
+    3 %, B0 perpendicular, with the dipole field) generated on the GPU; voxels per second."""
+    from spinwalk_gb300 import _lib
+    res = 800
+    for _ in range(args.warmup):
+        _lib.phantom_cylinder(float(res), res, 0.11e-6 * 0.4, 0.75, 5.0, 3.0, 90.0, 1)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        m, f, bvf = _lib.phantom_cylinder(float(res), res, 0.11e-6 * 0.4, 0.75, 5.0, 3.0, 90.0, 1)
+        times.append(time.perf_counter() - t)
+    s = float(np.mean(times))
+    line = {"metric": "phantom voxels/s", "value": res ** 3 / s, "unit": "voxels/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "reference_cylinder_phantom_800cubed",
+                       "generator": "phantom::cylinder (fov 800 um, r 5 um, 3 %, 90 deg, seed 1)",
+                       "actual_volume_fraction": bvf},
+            "e2e": {"value": res ** 3 / s, "unit": "voxels/s",
+                    "note": "host placement + GPU mask/field + copy of 2.5 GB to the host"}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -586,6 +615,8 @@ def main():
         run_batch_scales(args, world, rank)
     elif args.workload == "serve":
         run_serve(args, world, rank)
+    elif args.workload == "phantom":
+        run_phantom(args, world, rank)
     else:
         run_ours(args, world, rank, local)
 

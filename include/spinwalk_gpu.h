@@ -341,6 +341,22 @@ int sw_engine_poll(sw_engine *e, int wait, sw_job_result *done, uint32_t max_don
                    uint32_t *n_done);
 int sw_engine_pending(sw_engine *e, uint32_t *n_pending);
 
+/* ---- Signal mode: the reduction of the results fused into the walk ------------------------
+ * What the reference's analysis computes from M1 and T (the demos average M per tissue and
+ * echo) without writing them: signal[te][substrate][0..2] = the sum over spins of M at echo
+ * te of the spins in that substrate at the echo, count[te][substrate] = how many spins (spins
+ * lost or out of bounds before an echo are not in that echo's sums). Sums in double; the order
+ * of the additions is not fixed, so results agree with a reduction of sw_sim's M1 / T to about
+ * 1e-15 relative. XYZ1 is not produced. No reference counterpart. */
+int sw_sim_signal(const sw_params *param, const sw_sequence *seq, const float *pFieldMap,
+                  const uint8_t *pMask, const float *M0, const float *XYZ0, double *signal,
+                  uint64_t *count, int32_t *status, int precision);
+int sw_engine_submit_signal(sw_engine *e, int32_t phantom, const sw_params *param,
+                            const sw_sequence *seq, int precision, const float *M0,
+                            const float *XYZ0, double *signal, uint64_t *count, int32_t *status,
+                            int64_t *job_id);
+
+
 /* ---- The reference's phantom generators, mask and field on the GPU -----------------------
  * phantom::cylinder (src/phantom/phantom_cylinder.cpp: parallel cylinders along z, B0 rotated
  * by `orientation_deg` about y) and phantom::sphere (phantom_sphere.cpp), with the reference's

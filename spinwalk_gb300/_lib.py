@@ -71,6 +71,12 @@ def lib():
         for f in (L.sw_phantom_sphere, L.sw_phantom_sphere_device):
             f.argtypes = [C.c_float, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_float,
                           C.c_int32, C.c_void_p, C.c_void_p, P(C.c_float)]
+        L.sw_sim_signal.argtypes = [P(abi.SwParams), P(abi.SwSequence), C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_int]
+        L.sw_engine_submit_signal.argtypes = [C.c_void_p, C.c_int32, P(abi.SwParams),
+                                              P(abi.SwSequence), C.c_int, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_void_p, C.c_void_p, P(C.c_int64)]
         L.sw_config_dump.argtypes = [C.c_char_p, C.c_char_p]
         L.sw_run_config.argtypes = [C.c_char_p, C.c_int]
         L.sw_h5_write.argtypes = [C.c_char_p, C.c_int, P(C.c_char_p), P(C.c_int), P(C.c_int),
@@ -249,6 +255,19 @@ def phantom_sphere(fov_um, resolution, dchi=0.11e-6, Y=0.75, radius_um=8.0,
     return mask.reshape(shape), (fld.reshape(shape) if fld is not None else None), bvf.value
 
 
+def run_signal(problem, precision=abi.SW_PREC_FP32):
+    """sw_sim_signal: (signal [nTE, n_substrate, 3] sums of M, count [nTE, n_substrate],
+    status [n]) with the reduction fused into the walk (no per-spin M1 / T / XYZ1)."""
+    ns, nte = problem.params.n_substrate, problem.n_te
+    sig = np.zeros((nte, ns, 3), np.float64)
+    cnt = np.zeros((nte, ns), np.uint64)
+    status = np.full(problem.params.n_spins, -1, np.int32)
+    check(lib().sw_sim_signal(C.byref(problem.params), C.byref(problem.seq.struct),
+                              _p(problem.field), _p(problem.mask), _p(problem.M0),
+                              _p(problem.XYZ0), _p(sig), _p(cnt), _p(status), int(precision)))
+    return sig, cnt, status
+
+
 def run_spins(problem, lo, hi, precision=abi.SW_PREC_FP32, fill=0.0):
     """sw_sim_spins: rows [lo, hi) of run(problem) (M1, XYZ1, T, status hold those rows only)."""
     M1, XYZ1, T, status = problem.outputs(fill)
@@ -286,6 +305,19 @@ class Engine:
                                      C.byref(problem.seq.struct), int(precision),
                                      _p(problem.M0), _p(problem.XYZ0), _p(o["M1"]),
                                      _p(o["XYZ1"]), _p(o["T"]), _p(o["status"]), C.byref(jid)))
+        self._jobs[jid.value] = (problem, o)
+        return jid.value, o
+
+    def submit_signal(self, problem, phantom, precision=abi.SW_PREC_FP32):
+        """Signal mode (see run_signal): returns (job id, dict(signal, count, status))."""
+        ns, nte = problem.params.n_substrate, problem.n_te
+        o = dict(signal=np.zeros((nte, ns, 3), np.float64), count=np.zeros((nte, ns), np.uint64),
+                 status=np.full(problem.params.n_spins, -1, np.int32))
+        jid = C.c_int64()
+        check(lib().sw_engine_submit_signal(self._h, int(phantom), C.byref(problem.params),
+                                            C.byref(problem.seq.struct), int(precision),
+                                            _p(problem.M0), _p(problem.XYZ0), _p(o["signal"]),
+                                            _p(o["count"]), _p(o["status"]), C.byref(jid)))
         self._jobs[jid.value] = (problem, o)
         return jid.value, o
 

@@ -118,6 +118,11 @@ struct Job {
     int rc = SW_OK;
     double t_submit = 0, t_done = 0;
     SeedCache *seed = nullptr;
+    // signal mode: per-(echo, substrate) sums instead of per-spin M1 / T / XYZ1
+    double *h_sig = nullptr, *d_sig = nullptr;
+    uint64_t *h_cnt = nullptr;
+    unsigned long long *d_cnt = nullptr;
+    size_t n_keys = 0;
 };
 
 struct Slot {
@@ -246,7 +251,8 @@ int start_chunk(sw_engine *E, Slot &s, Job &j) {
     s.job = &j;
     s.lo = lo;
     s.hi = hi;
-    const size_t c = hi - lo, nte = j.nte, trj = j.trj, r = lo - j.spin_lo;   // r: first host row
+    const bool sig = j.d_sig != nullptr;
+    const size_t c = hi - lo, nte = sig ? 0 : j.nte, trj = sig ? 0 : j.trj, r = lo - j.spin_lo;
     size_t off = 0;
     auto sec = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~size_t(255); return o; };
     s.o_M0 = sec(c * 12);
@@ -265,7 +271,7 @@ int start_chunk(sw_engine *E, Slot &s, Job &j) {
         par_memcpy(s.h_io + s.o_M1, j.M1 + 3 * nte * r, c * nte * 12);
         par_memcpy(s.h_io + s.o_T, j.T + nte * r, c * nte);
     }
-    par_memcpy(s.h_io + s.o_XYZ1, j.XYZ1 + 3 * trj * r, c * trj * 12);
+    if (trj) par_memcpy(s.h_io + s.o_XYZ1, j.XYZ1 + 3 * trj * r, c * trj * 12);
     EN_CUDA(cudaMemcpyAsync(s.d_io, s.h_io, s.in_bytes, cudaMemcpyHostToDevice, s.st));
     EN_CUDA(cudaMemcpyAsync(s.L.tables, j.h_tables, j.im.bytes.size(), cudaMemcpyHostToDevice, s.st));
     // generator states of spins [lo, hi): the job's range of the seed cache, both generators
@@ -314,11 +320,19 @@ ChunkView view(const Slot &s) {
     G.nbuf = shift(G.nbuf, lo * sw::kNormBuf); G.nhead = shift(G.nhead, lo); G.ncnt = shift(G.ncnt, lo);
     G.ubuf = shift(G.ubuf, lo * sw::kUnifBuf); G.uhead = shift(G.uhead, lo); G.ucnt = shift(G.ucnt, lo);
     char *d = s.d_io;
-    v.O.M1 = shift(reinterpret_cast<float *>(d + s.o_M1), lo * 3 * j.nte);
     v.O.M1d = nullptr;
-    v.O.XYZ1 = shift(reinterpret_cast<float *>(d + s.o_XYZ1), lo * 3 * j.trj);
-    v.O.T = shift(reinterpret_cast<uint8_t *>(d + s.o_T), lo * j.nte);
     v.O.status = shift(reinterpret_cast<int32_t *>(d + s.o_st), lo);
+    if (j.d_sig) {
+        v.O.M1 = nullptr;
+        v.O.XYZ1 = nullptr;
+        v.O.T = nullptr;
+        v.O.sig = j.d_sig;
+        v.O.cnt = j.d_cnt;
+    } else {
+        v.O.M1 = shift(reinterpret_cast<float *>(d + s.o_M1), lo * 3 * j.nte);
+        v.O.XYZ1 = shift(reinterpret_cast<float *>(d + s.o_XYZ1), lo * 3 * j.trj);
+        v.O.T = shift(reinterpret_cast<uint8_t *>(d + s.o_T), lo * j.nte);
+    }
     v.M0 = shift(reinterpret_cast<const float *>(d + s.o_M0), lo * 3);
     v.XYZ0 = shift(reinterpret_cast<const float *>(d + s.o_XYZ0), lo * 3);
     return v;
@@ -349,6 +363,16 @@ int issue_rounds(sw_engine *E, Slot &s, uint64_t k, bool first) {
 
 void job_done_check(sw_engine *E, Job &j) {
     if (j.running == 0 && (j.next_lo >= j.spin_hi || j.rc != SW_OK)) {
+        if (j.d_sig) {                    // every chunk has drained: the sums are final
+            if (j.rc == SW_OK &&
+                (cudaMemcpy(j.h_sig, j.d_sig, j.n_keys * 24, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                 cudaMemcpy(j.h_cnt, j.d_cnt, j.n_keys * 8, cudaMemcpyDeviceToHost) != cudaSuccess))
+                j.rc = fail(SW_ERR_CUDA, "signal read-back");
+            cudaFree(j.d_sig);
+            cudaFree(j.d_cnt);
+            j.d_sig = nullptr;
+            j.d_cnt = nullptr;
+        }
         j.t_done = now_s();
         E->phantoms[j.phantom].jobs--;
         if (j.h_tables) {
@@ -400,12 +424,14 @@ int pump(sw_engine *E, int &rc) {
                 s.state = Slot::DRAINING;
             }
         } else {                                         // DRAINING: results are in h_io
-            const size_t c = s.hi - s.lo, nte = j.nte, trj = j.trj, r = s.lo - j.spin_lo;
+            const bool sig = j.d_sig != nullptr;
+            const size_t c = s.hi - s.lo, nte = sig ? 0 : j.nte, trj = sig ? 0 : j.trj,
+                         r = s.lo - j.spin_lo;
             if (nte) {
                 par_memcpy(j.M1 + 3 * nte * r, s.h_io + s.o_M1, c * nte * 12);
                 par_memcpy(j.T + nte * r, s.h_io + s.o_T, c * nte);
             }
-            par_memcpy(j.XYZ1 + 3 * trj * r, s.h_io + s.o_XYZ1, c * trj * 12);
+            if (trj) par_memcpy(j.XYZ1 + 3 * trj * r, s.h_io + s.o_XYZ1, c * trj * 12);
             if (j.status) par_memcpy(j.status + r, s.h_io + s.o_st, c * 4);
             j.running--;
             s.state = Slot::FREE;
@@ -433,7 +459,7 @@ int pump(sw_engine *E, int &rc) {
 int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_sequence *q,
                   int precision, const float *M0, const float *XYZ0, float *M1, float *XYZ1,
                   uint8_t *T, int32_t *status, int64_t *job_id, uint64_t spin_lo = 0,
-                  uint64_t spin_hi = ~0ull) {
+                  uint64_t spin_hi = ~0ull, double *sig = nullptr, uint64_t *cnt = nullptr) {
     int rc = check_args(p, q);
     if (rc) return rc;
     auto pit = E->phantoms.find(phantom);
@@ -451,7 +477,9 @@ int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_se
     if (spin_lo > spin_hi || spin_hi > p->n_spins) return fail(SW_ERR_INVALID, "spin range outside [0, n_spins)");
     const size_t n = spin_hi - spin_lo, nte = q->n_TE;
     const size_t trj = p->enRecordTrajectory ? (size_t)(p->n_dummy_scan + 1) * p->n_timepoints : 1;
-    if (n && (!M0 || !XYZ0 || !XYZ1 || (nte && (!M1 || !T))))
+    const bool signal = sig != nullptr;
+    if (signal && !cnt) return fail(SW_ERR_INVALID, "signal mode needs the count array");
+    if (n && (!M0 || !XYZ0 || (!signal && (!XYZ1 || (nte && (!M1 || !T))))))
         return fail(SW_ERR_INVALID, "null host buffer");
     std::unique_ptr<Job> j(new Job());
     j->id = E->next_job++;
@@ -496,8 +524,17 @@ int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_se
     j->trj = trj;
     j->spin_lo = j->next_lo = (uint32_t)spin_lo;
     j->spin_hi = (uint32_t)spin_hi;
+    if (signal) {                         // zeroed device sums, shared by the job's chunks
+        j->h_sig = sig;
+        j->h_cnt = cnt;
+        j->n_keys = std::max<size_t>(1, nte * p->n_substrate);
+        EN_CUDA(cudaMalloc(&j->d_sig, j->n_keys * 24));
+        EN_CUDA(cudaMalloc(&j->d_cnt, j->n_keys * 8));
+        EN_CUDA(cudaMemset(j->d_sig, 0, j->n_keys * 24));
+        EN_CUDA(cudaMemset(j->d_cnt, 0, j->n_keys * 8));
+    }
     // chunk: a slot's spin capacity, or what its I/O buffer holds for this job
-    const size_t per_spin = 24 + nte * 13 + trj * 12 + 4 + 5 * 256;
+    const size_t per_spin = signal ? 24 + 4 + 5 * 256 : 24 + nte * 13 + trj * 12 + 4 + 5 * 256;
     const Slot &s0 = E->slots[0];
     j->chunk = (uint32_t)std::min<size_t>(s0.cap, s0.io_bytes / per_spin);
     if (n && j->chunk == 0) return fail(SW_ERR_NOMEM, "one spin's trajectory exceeds a slot's I/O buffer");
@@ -845,6 +882,51 @@ int sw_sim_spins(const sw_params *param, const sw_sequence *seq, const float *pF
     if (!rc)
         rc = engine_submit(E, ph, param, seq, precision, M0, XYZ0, M1, XYZ1, T, status, &jid,
                            spin_lo, spin_hi);
+    rc = finish_call_engine(E, rc);
+    if (rc) return rc;
+    g_timing.total_ms = (float)((now_s() - t0) * 1e3);
+    return SW_OK;
+}
+
+int sw_engine_submit_signal(sw_engine *e, int32_t phantom, const sw_params *param,
+                            const sw_sequence *seq, int precision, const float *M0,
+                            const float *XYZ0, double *signal, uint64_t *count, int32_t *status,
+                            int64_t *job_id) {
+    if (!e || !job_id || !signal || !count) return SW_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(e->mu);
+    if (cudaSetDevice(e->device) != cudaSuccess) return fail(SW_ERR_CUDA, "device");
+    return engine_submit(e, phantom, param, seq, precision, M0, XYZ0, nullptr, nullptr, nullptr,
+                         status, job_id, 0, ~0ull, signal, count);
+}
+
+int sw_sim_signal(const sw_params *param, const sw_sequence *seq, const float *pFieldMap,
+                  const uint8_t *pMask, const float *M0, const float *XYZ0, double *signal,
+                  uint64_t *count, int32_t *status, int precision) {
+    int rc = check_args(param, seq);
+    if (rc) return rc;
+    if (!pMask || !signal || !count) return fail(SW_ERR_INVALID, "null buffer");
+    if (param->fieldmap_exist && !pFieldMap) return fail(SW_ERR_INVALID, "null fieldmap");
+    g_timing = sw_timing{};
+    const size_t keys = (size_t)seq->n_TE * param->n_substrate;
+    if (param->n_spins == 0) {
+        std::memset(signal, 0, keys * 24);
+        std::memset(count, 0, keys * 8);
+        return SW_OK;
+    }
+    const double t0 = now_s();
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    sw_engine *E = nullptr;
+    const uint64_t n = param->n_spins;
+    rc = acquire_call_engine(4, (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n + 3) / 4, 1u << 20)), E);
+    if (rc) return rc;
+    const uint64_t dims[3] = {param->phantom_size[0], param->phantom_size[1], param->phantom_size[2]};
+    int32_t ph = 0;
+    rc = engine_add_phantom(E, pMask, param->fieldmap_exist ? pFieldMap : nullptr, dims,
+                            param->n_substrate, &ph);
+    int64_t jid = 0;
+    if (!rc)
+        rc = engine_submit(E, ph, param, seq, precision, M0, XYZ0, nullptr, nullptr, nullptr,
+                           status, &jid, 0, ~0ull, signal, count);
     rc = finish_call_engine(E, rc);
     if (rc) return rc;
     g_timing.total_ms = (float)((now_s() - t0) * 1e3);

@@ -121,8 +121,10 @@ __global__ void k_init(DevParams P, DevTables Tb, const uint2 *__restrict__ vox,
         p0[i] = XYZ0[3 * (size_t)spin + i];
         m[i] = M0[3 * (size_t)spin + i];
     }
-    float *xyz1 = O.XYZ1 + 3 * (size_t)spin * P.traj_len;
-    for (int i = 0; i < 3; i++) xyz1[i] = p0[i];                   // kernels.cu:96
+    if (O.XYZ1) {
+        float *xyz1 = O.XYZ1 + 3 * (size_t)spin * P.traj_len;
+        for (int i = 0; i < 3; i++) xyz1[i] = p0[i];               // kernels.cu:96
+    }
     S.x[spin] = dbits((double)p0[0]);
     S.y[spin] = dbits((double)p0[1]);
     S.z[spin] = dbits((double)p0[2]);
@@ -282,6 +284,31 @@ __global__ void __launch_bounds__(32 * kRefillWarps)
             }
         }
         __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Signal mode: one echo's M added to its (echo, substrate) sums. The lanes of a warp that reach
+// an echo together with the same key are summed by shuffles first, so that one lane per key
+// does the atomic additions (the lanes of a warp are spins walking in step).
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void signal_add(const Outputs &O, uint32_t key, const double (&v)[3]) {
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, key);
+    const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
+    double s[3] = {v[0], v[1], v[2]};
+    unsigned rest = grp & ~(1u << leader);
+    while (rest) {
+        const int b = __ffs(rest) - 1;
+        rest &= rest - 1;
+        for (int i = 0; i < 3; i++) {
+            const double x = __shfl_sync(grp, v[i], b);
+            if (lane == leader) s[i] += x;
+        }
+    }
+    if (lane == leader) {
+        for (int i = 0; i < 3; i++) atomicAdd(O.sig + 3 * (size_t)key + i, s[i]);
+        atomicAdd(O.cnt + key, (unsigned long long)__popc(grp));
     }
 }
 
@@ -463,13 +490,19 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
                 dephase_relax_d(d0, d1, accd, __ldg(Tb.T1d + ts_old), __ldg(Tb.T2d + ts_old), ted);
                 d0[0] = d1[0]; d0[1] = d1[1]; d0[2] = d1[2];
             }
-            const size_t o = 3 * ((size_t)spin * P.n_TE + c_te);
-            for (int i = 0; i < 3; i++) {
-                m0[i] = m1[i];
-                O.M1[o + i] = (PREC == SW_PREC_FP64) ? (float)d1[i] : m1[i];
-                if (DBL && O.M1d) O.M1d[o + i] = d1[i];
+            for (int i = 0; i < 3; i++) m0[i] = m1[i];
+            if (O.sig) {
+                double v[3];
+                for (int i = 0; i < 3; i++) v[i] = (PREC == SW_PREC_FP64) ? d1[i] : (double)m1[i];
+                signal_add(O, c_te * P.n_substrate + ts_old, v);
+            } else {
+                const size_t o = 3 * ((size_t)spin * P.n_TE + c_te);
+                for (int i = 0; i < 3; i++) {
+                    O.M1[o + i] = (PREC == SW_PREC_FP64) ? (float)d1[i] : m1[i];
+                    if (DBL && O.M1d) O.M1d[o + i] = d1[i];
+                }
+                O.T[(size_t)spin * P.n_TE + c_te] = (uint8_t)ts_old;
             }
-            O.T[(size_t)spin * P.n_TE + c_te] = (uint8_t)ts_old;
             acc = 0.f; acc_e = 0.f; accd = 0.;
             tp_old = tp;
             c_te++;
@@ -477,7 +510,7 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
         }
         // ---- accept the move (kernels.cu:218-223) ----
         xo[0] = xn[0]; xo[1] = xn[1]; xo[2] = xn[2];
-        if (P.record_traj) {
+        if (P.record_traj && O.XYZ1) {
             float *dst = O.XYZ1 + 3 * ((size_t)spin * P.traj_len + (size_t)ds * P.n_timepoints + tp);
             dst[0] = (float)dfrom(xn[0]); dst[1] = (float)dfrom(xn[1]); dst[2] = (float)dfrom(xn[2]);
         }
@@ -502,7 +535,7 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
     uint32_t nf = ts_old | (started ? kFlagStarted : 0u);
     if (status >= 0) {
         nf |= kFlagDone | ((uint32_t)status << 16);
-        if (!P.record_traj) {
+        if (!P.record_traj && O.XYZ1) {
             float *dst = O.XYZ1 + 3 * (size_t)spin * P.traj_len;
             dst[0] = (float)dfrom(xo[0]); dst[1] = (float)dfrom(xo[1]); dst[2] = (float)dfrom(xo[2]);
         }

@@ -99,9 +99,13 @@ struct RngState {
 struct Outputs {
     float *M1;                // [n][n_TE][3]
     double *M1d;              // optional FP64 shadow
-    float *XYZ1;              // [n][traj_len][3]
+    float *XYZ1;              // [n][traj_len][3] (may be null in signal mode)
     uint8_t *T;               // [n][n_TE]
     int32_t *status;          // optional
+    // Signal mode (sig != null): instead of M1 / T, every echo adds the spin's M to
+    // sig[te][substrate][3] and counts it in cnt[te][substrate].
+    double *sig = nullptr;
+    unsigned long long *cnt = nullptr;
 };
 
 }  // namespace sw

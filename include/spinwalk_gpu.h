@@ -53,6 +53,18 @@ extern "C" {
 #define SW_PREC_FP32       0   /* the reference's arithmetic: float phase sum, float Bloch */
 #define SW_PREC_FP64       1   /* same walk, phase sum + rotations + relaxation in double */
 #define SW_PREC_KAHAN      2   /* same walk, compensated (Kahan) float phase sum */
+/* Generator flavour, OR-ed into the `precision` argument of every entry point:
+ *   SW_RNG_MT19937 (0) -- the reference's CPU build: std::mt19937 + libstdc++
+ *                         normal_distribution<float> (polar method) (kernels.cu:82-85);
+ *   SW_RNG_MINSTD      -- the reference's CUDA build: thrust::minstd_rand +
+ *                         thrust::normal_distribution<float> (inverse erfc, one draw per
+ *                         deviate) + thrust::uniform_real_distribution<float>
+ *                         (kernels.cu:76-80), with unfused arithmetic, i.e. as that build's host
+ *                         (--use_cpu) path computes it; its GPU kernel differs from it only where
+ *                         nvcc contracts a*b+c into fused multiply-adds. */
+#define SW_RNG_MT19937     0x000
+#define SW_RNG_MINSTD      0x100
+#define SW_PREC_MASK       0x0ff
 
 /*
  * Scalar simulation parameters. Field-for-field mirror of sim::parameters
@@ -382,6 +394,10 @@ int sw_phantom_sphere_device(float fov_um, uint64_t resolution, float dchi, floa
 /* Host-visible check of the bit-exact logf used by the Gaussian generator: evaluates the
  * device logf on n inputs (device pointers) -- used by the tests. */
 int sw_debug_logf(const float *d_x, float *d_y, uint64_t n, void *stream);
+
+/* Host-visible check of the minstd flavour's Gaussian deviate (thrust normal_distribution_nvcc,
+ * device erfcinvf): d_y[i] = deviate of engine output x_lo + i -- used by the tests. */
+int sw_debug_ms_normal(uint32_t x_lo, uint32_t n, float *d_y, void *stream);
 
 /* Host-visible check of the integer double addition of the walk's position update:
  * d_y[i] = d_a[i] + d_b[i] (IEEE round to nearest even) on n device doubles -- used by the

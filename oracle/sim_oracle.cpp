@@ -8,6 +8,11 @@
 // expression keeps the reference's operand types so float/double rounding matches; the file
 // must be compiled with -ffp-contract=off (oracle/Makefile).
 //
+// The generator flavour of the reference's CUDA build (SW_RNG_MINSTD, kernels.cu:76-80) is
+// restated too: thrust::minstd_rand, thrust::normal_distribution<float> (normal_distribution_nvcc:
+// one draw, inverse erfc) and thrust::uniform_real_distribution<float>, calling CUDA's own
+// host erfcinvf (this file is compiled by nvcc's host pass for that reason).
+//
 // On top of the reference semantics it reports a per-spin status (SW_SPIN_*), and offers the
 // two extra Bloch precisions of the GPU library along the SAME walk:
 //   SW_PREC_FP64  : phase sum, rotations and relaxation in double;
@@ -27,6 +32,56 @@ namespace {
 constexpr double kDeg2Rad = 0.0174532925199433;   // DEG2RAD, simulation_parameters.cuh:24
 constexpr double kRad2Deg = 57.2957795130823;     // RAD2DEG, simulation_parameters.cuh:25
 constexpr double kGamma = 267515315.;             // GAMMA,   definitions.h:20
+
+// ---- generators ----------------------------------------------------------------------------
+struct StdGen {           // the CPU build (kernels.cu:82-88)
+    std::mt19937 gen_r, gen_u;
+    std::normal_distribution<float> nrm{0.f, 1.0f};
+    std::uniform_real_distribution<float> uni{0.f, 1.f};
+    explicit StdGen(uint64_t sd) : gen_r(sd), gen_u(sd) {
+        gen_r.discard(sd);
+        gen_u.discard(sd);
+    }
+    float normal() { return nrm(gen_r); }
+    float uniform() { return uni(gen_u); }
+};
+
+struct MinstdGen {        // the CUDA build: thrust::minstd_rand (kernels.cu:77-80, 87-88)
+    static constexpr uint64_t A = 48271, M = 2147483647;
+    uint32_t xr, xu;
+    static uint32_t seed_discard(uint64_t sd) {
+        uint64_t x = (uint32_t)sd % M;              // linear_congruential_engine::seed
+        if (x == 0) x = 1;
+        uint64_t mul = A, acc = 1;                  // ::discard(z): a^z x mod m
+        for (uint64_t z = sd; z; z >>= 1) {
+            if (z & 1) acc = acc * mul % M;
+            mul = mul * mul % M;
+        }
+        return (uint32_t)(acc * x % M);
+    }
+    explicit MinstdGen(uint64_t sd) : xr(seed_discard(sd)), xu(xr) {}
+    static uint32_t next(uint32_t &x) { return x = (uint32_t)((uint64_t)x * A % M); }
+    static float normal_of(uint32_t x) {            // normal_distribution_nvcc::sample(0, 1)
+        const uint32_t range = (uint32_t)(M - 2);
+        const float S1 = static_cast<float>(1. / static_cast<double>(range));
+        const float S2 = S1 / 2;
+        float S3 = static_cast<float>(-1.4142135623730950488016887242097);
+        uint32_t u = x - 1;
+        if (u > range / 2) {
+            u = range - u;
+            S3 = -S3;
+        }
+        const float p = u * S1 + S2;
+        const float mean = 0.f, stddev = 1.0f;
+        return mean + stddev * S3 * erfcinvf(2 * p);
+    }
+    float normal() { return normal_of(next(xr)); }
+    float uniform() {                               // uniform_real_distribution<float>(0, 1)
+        float r = static_cast<float>(next(xu) - 1);
+        r /= (1.0f + static_cast<float>((uint32_t)(M - 2)));
+        return (r * (1.f - 0.f)) + 0.f;
+    }
+};
 
 // ---- float Bloch primitives with the reference's operand types (kernels.cuh:82-230) ------
 inline void xrot_f(float s, float c, const float *a, float *b) {
@@ -122,17 +177,14 @@ inline int64_t sub2ind(double x, double y, double z, const sw_params *p) {
 }
 
 // One spin, following kernels.cu:72-233 statement by statement.
+template <typename Gen>
 void sim_spin(const sw_params *P, const sw_sequence *Q, const float *fieldmap,
               const uint8_t *mask, const float *M0, const float *XYZ0, float *M1, float *XYZ1,
               uint8_t *T, int32_t *status, uint32_t spin, int precision, double *M1d) {
     const uint64_t trj = P->enRecordTrajectory
                              ? (uint64_t)(P->n_dummy_scan + 1) * P->n_timepoints : 1;
     float *xyz1 = XYZ1 + 3ull * spin * trj;                        // kernels.cu:75
-    std::mt19937 gen_r(P->seed + spin), gen_u(P->seed + spin);     // :82-83
-    std::normal_distribution<float> nrm(0.f, 1.0f);                // :84
-    std::uniform_real_distribution<float> uni(0.f, 1.f);           // :85
-    gen_r.discard(P->seed + spin);                                 // :87-88
-    gen_u.discard(P->seed + spin);
+    Gen gen(P->seed + spin);                                       // :76-88
 
     const bool fp64 = precision == SW_PREC_FP64;
     const bool kahan = precision == SW_PREC_KAHAN;
@@ -180,7 +232,7 @@ void sim_spin(const sw_params *P, const sw_sequence *Q, const float *fieldmap,
         double accd = 0.;
         while (tp < P->n_timepoints) {                               // :128
             for (int i = 0; i < 3 && dscale != 0.; i++) {            // :130-137
-                double rnd = nrm(gen_r) * dscale;
+                double rnd = gen.normal() * dscale;
                 xyz_new[i] = xyz_old[i] + rnd;
                 if (xyz_new[i] < 0)
                     xyz_new[i] += (P->enCrossFOV ? P->fov[i] : 2 * std::abs(rnd));
@@ -195,7 +247,7 @@ void sim_spin(const sw_params *P, const sw_sequence *Q, const float *fieldmap,
             if (ind != ind_old) {                                    // :150-170
                 ts = mask[ind];
                 if (ts != ts_old) {
-                    if (uni(gen_u) >= Q->pXY[ts_old * P->n_substrate + ts]) {
+                    if (gen.uniform() >= Q->pXY[ts_old * P->n_substrate + ts]) {
                         if (itr++ > P->max_iterations) {
                             if (status) status[spin] = SW_SPIN_LOST;
                             return;
@@ -300,10 +352,15 @@ int oracle_sim(const sw_params *P, const sw_sequence *Q, const float *fieldmap,
     const int64_t n = spin_ids ? (int64_t)n_ids : (int64_t)P->n_spins;
     if (n_threads <= 0) n_threads = omp_get_max_threads();
     const float *fm = P->fieldmap_exist ? fieldmap : nullptr;
+    const bool minstd = (precision & ~SW_PREC_MASK) == SW_RNG_MINSTD;
+    precision &= SW_PREC_MASK;
 #pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads)
     for (int64_t i = 0; i < n; i++) {
         uint32_t spin = spin_ids ? spin_ids[i] : (uint32_t)i;
-        sim_spin(P, Q, fm, mask, M0, XYZ0, M1, XYZ1, T, status, spin, precision, M1_fp64);
+        if (minstd)
+            sim_spin<MinstdGen>(P, Q, fm, mask, M0, XYZ0, M1, XYZ1, T, status, spin, precision, M1_fp64);
+        else
+            sim_spin<StdGen>(P, Q, fm, mask, M0, XYZ0, M1, XYZ1, T, status, spin, precision, M1_fp64);
     }
     return 0;
 }
@@ -329,6 +386,13 @@ int oracle_initial_positions(const float fov[3], uint64_t seed, uint32_t n_spins
 void oracle_logf(const float *x, float *y, uint64_t n) {
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < (int64_t)n; i++) y[i] = logf(x[i]);
+}
+
+// The minstd flavour's Gaussian deviate of engine outputs x_lo .. x_lo + n - 1, with CUDA's host
+// erfcinvf: the tests compare it with the device's on every engine output.
+void oracle_ms_normal(uint32_t x_lo, uint32_t n, float *y) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; i++) y[i] = MinstdGen::normal_of(x_lo + (uint32_t)i);
 }
 
 }  // extern "C"

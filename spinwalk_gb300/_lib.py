@@ -86,6 +86,7 @@ def lib():
         L.sw_sync.argtypes = [C.c_void_p]
         L.sw_last_timing.argtypes = [P(abi.SwTiming)]
         L.sw_debug_logf.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
+        L.sw_debug_ms_normal.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
         L.sw_debug_dadd.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
         if L.sw_abi_version() != 1:
             raise SpinWalkError("libspinwalk_gpu ABI version mismatch")
@@ -404,6 +405,10 @@ def run_tracks(problem, tracks, fill=0.0):
 
 def debug_dadd(d_a, d_b, d_y, n, stream=None):
     check(lib().sw_debug_dadd(d_a, d_b, d_y, C.c_uint64(n), stream))
+
+
+def debug_ms_normal(x_lo, n, d_y, stream=None):
+    check(lib().sw_debug_ms_normal(int(x_lo), int(n), d_y, stream))
 
 
 def debug_logf(d_x, d_y, n, stream=None):

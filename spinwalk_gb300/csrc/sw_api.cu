@@ -159,7 +159,7 @@ sw::DevTables dev_tables(const TableImage &im, const char *d) {
 
 
 // Lays out the whole workspace; with base == nullptr it only measures.
-Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl) {
+Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl, bool mt_state) {
     Carve c{base};
     Layout L{};
     L.vox = c.take<uint2>(ml);
@@ -188,8 +188,8 @@ Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl) {
     S.ctr2 = c.take<uint32_t>(n);
     S.flags = c.take<uint32_t>(n);
     sw::RngState &G = L.G;
-    G.mt_r = c.take<uint32_t>(n * sw::kMtN);
-    G.mt_u = c.take<uint32_t>(n * sw::kMtN);
+    G.mt_r = c.take<uint32_t>(mt_state ? n * sw::kMtN : 1);      // minstd: state in p_r / p_u
+    G.mt_u = c.take<uint32_t>(mt_state ? n * sw::kMtN : 1);
     G.p_r = c.take<uint32_t>(n);
     G.p_u = c.take<uint32_t>(n);
     G.nbuf = c.take<float>(n * sw::kNormBuf);
@@ -291,8 +291,11 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
     g_timing = sw_timing{};
     const size_t n = p->n_spins;
     if (n == 0) return SW_OK;
+    const uint32_t rng = (uint32_t)precision & ~(uint32_t)SW_PREC_MASK;
+    precision &= SW_PREC_MASK;
     if (precision != SW_PREC_FP32 && precision != SW_PREC_FP64 && precision != SW_PREC_KAHAN)
         return fail(SW_ERR_INVALID, "precision");
+    if (rng != SW_RNG_MT19937 && rng != SW_RNG_MINSTD) return fail(SW_ERR_INVALID, "generator flavour");
     int rc = ensure_logf(ctx);
     if (rc) return rc;
     const bool dbl = precision == SW_PREC_FP64 || d_M1d != nullptr;
@@ -300,7 +303,7 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
     TableImage im;
     build_tables(p, q, im);
     if (!im.complete()) return fail(SW_ERR_INVALID, "internal error: incomplete parameter tables");
-    Layout L = layout(nullptr, n, p->matrix_length, im.bytes.size(), dbl);
+    Layout L = layout(nullptr, n, p->matrix_length, im.bytes.size(), dbl, rng == SW_RNG_MT19937);
     if (L.bytes > ctx.ws_size) {
         if (ctx.ws) {
             SW_CUDA(cudaStreamSynchronize(st));
@@ -316,12 +319,14 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
         }
         ctx.ws_size = L.bytes;
     }
-    L = layout(ctx.ws, n, p->matrix_length, im.bytes.size(), dbl);
+    L = layout(ctx.ws, n, p->matrix_length, im.bytes.size(), dbl, rng == SW_RNG_MT19937);
     SW_CUDA(cudaMemcpyAsync(L.tables, im.bytes.data(), im.bytes.size(), cudaMemcpyHostToDevice, st));
 
-    const sw::DevParams P = dev_params(p, q);
+    sw::DevParams P = dev_params(p, q);
+    P.rng = rng;
     const sw::DevTables Tb = dev_tables(im, L.tables);
-    const sw::LogfTables LT = logf_tables(ctx);
+    sw::LogfTables LT = logf_tables(ctx);
+    if (rng == SW_RNG_MINSTD && !(LT.ms_delta = minstd_delta_table())) return SW_ERR_CUDA;
     sw::Outputs O{d_M1, d_M1d, d_XYZ1, d_T, d_status};
     cudaEvent_t *ev = ctx.ev.data();
     uint32_t launches = 0;
@@ -484,6 +489,14 @@ int sw_sim(const sw_params *param, const sw_sequence *seq, const float *pFieldMa
 int sw_debug_dadd(const double *d_a, const double *d_b, double *d_y, uint64_t n, void *stream) {
     if (!d_a || !d_b || !d_y) return fail(SW_ERR_INVALID, "null device buffer");
     SW_CUDA(sw::launch_debug_dadd(d_a, d_b, d_y, n, (cudaStream_t)stream));
+    return SW_OK;
+}
+
+int sw_debug_ms_normal(uint32_t x_lo, uint32_t n, float *d_y, void *stream) {
+    if (!d_y) return fail(SW_ERR_INVALID, "null device buffer");
+    const uint32_t *delta = minstd_delta_table();
+    if (!delta) return SW_ERR_CUDA;
+    SW_CUDA(sw::launch_debug_ms_normal(x_lo, n, d_y, delta, (cudaStream_t)stream));
     return SW_OK;
 }
 

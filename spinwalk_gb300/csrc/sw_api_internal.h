@@ -69,10 +69,14 @@ DevParams dev_params(const sw_params *p, const sw_sequence *q);
 void build_tables(const sw_params *p, const sw_sequence *q, TableImage &im);
 DevTables dev_tables(const TableImage &im, const char *d);
 // base == nullptr: only measures (Layout::bytes).
-Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl);
+Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl,
+              bool mt_state = true);
 // The current device's logf tables (built and uploaded on first use); {nullptr, nullptr} and
 // sw_last_error() set on failure.
 LogfTables device_logf_tables();
+// The current device's correction table of the minstd flavour's deviates (sw_minstd.cu), built
+// on first use; nullptr and sw_last_error() set on failure.
+const uint32_t *minstd_delta_table();
 
 }  // namespace api
 }  // namespace sw

@@ -131,6 +131,38 @@ __host__ __device__ __forceinline__ uint32_t mt_discard_twists(uint64_t z) {
     return z == 0 ? 0u : (uint32_t)(1 + (z - 1) / kMtN);
 }
 
+// ------------------------------------------------------------------------------------------
+// thrust::normal_distribution<float> under nvcc (normal_distribution_nvcc, the reference's CUDA
+// build): one minstd output x -> u = x - 1 folded at the middle of the range -> erfcinv.
+// ------------------------------------------------------------------------------------------
+constexpr uint32_t kMsRange = 2147483647u - 2u;        // minstd max - min
+
+// The deviate for a folded u (the branch with S3 = -sqrt 2), every float op separately rounded:
+// mean + stddev * S3 * erfcinv(2 p), p = u S1 + S2 (device erfcinvf).
+__device__ __forceinline__ float ms_normal_folded(uint32_t u) {
+    constexpr float S1 = (float)(1. / (double)kMsRange), S2 = S1 / 2;
+    const float S3 = (float)(-1.4142135623730950488016887242097);
+    const float p = __fadd_rn(__fmul_rn(__uint2float_rn(u), S1), S2);
+    const float e = erfcinvf(__fmul_rn(2.0f, p));
+    return __fadd_rn(0.0f, __fmul_rn(__fmul_rn(1.0f, S3), e));
+}
+
+// The full deviate of engine output x; with `delta` (sw_minstd.cu) the magnitude is corrected to
+// what CUDA's host erfcinvf gives (the reference build's host path).
+__device__ __forceinline__ float ms_normal(uint32_t x, const uint32_t *delta) {
+    uint32_t u = x - 1u;
+    const bool upper = u > kMsRange / 2;
+    if (upper) u = kMsRange - u;
+    uint32_t b = __float_as_uint(ms_normal_folded(u));
+    if (delta) {
+        const uint32_t nib = (__ldg(delta + (u >> 3)) >> ((u & 7u) * 4u)) & 15u;
+        b = (b & 0x80000000u) | ((b & 0x7fffffffu) + (uint32_t)((int32_t)(nib ^ 8u) - 8));
+    }
+    // the upper branch (S3 = +sqrt 2) is the negation, and 0 + (-0) is +0 on both
+    if (upper && (b & 0x7fffffffu)) b ^= 0x80000000u;
+    return __uint_as_float(b);
+}
+
 // generate_canonical<float, 24>(mt19937): float(w) / 2^32, clamped below 1
 // (libstdc++ bits/random.tcc, generate_canonical).
 __device__ __forceinline__ float canon24(uint32_t w) {

@@ -243,55 +243,6 @@ int ensure_seeded(sw_engine *E, uint64_t seed, uint32_t lo, uint32_t hi, SeedCac
     return SW_OK;
 }
 
-// Hands the next spin range of a ready job to a free slot and issues the chunk's work.
-int start_chunk(sw_engine *E, Slot &s, Job &j) {
-    const uint32_t lo = j.next_lo, hi = std::min<uint32_t>(j.spin_hi, lo + j.chunk);
-    j.next_lo = hi;
-    j.running++;
-    s.job = &j;
-    s.lo = lo;
-    s.hi = hi;
-    const bool sig = j.d_sig != nullptr;
-    const size_t c = hi - lo, nte = sig ? 0 : j.nte, trj = sig ? 0 : j.trj, r = lo - j.spin_lo;
-    size_t off = 0;
-    auto sec = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~size_t(255); return o; };
-    s.o_M0 = sec(c * 12);
-    s.o_XYZ0 = sec(c * 12);
-    s.o_M1 = sec(c * nte * 12);
-    s.o_T = sec(c * nte);
-    s.o_XYZ1 = sec(c * trj * 12);
-    s.in_bytes = off;                    // inputs and the outputs' starting contents
-    s.o_st = sec(c * 4);
-    s.out_bytes = off - s.o_M1;
-    // stage: inputs and the caller's current output contents (slots the walk never reaches keep
-    // them, as with sw_sim)
-    par_memcpy(s.h_io + s.o_M0, j.M0 + 3 * r, c * 12);
-    par_memcpy(s.h_io + s.o_XYZ0, j.XYZ0 + 3 * r, c * 12);
-    if (nte) {
-        par_memcpy(s.h_io + s.o_M1, j.M1 + 3 * nte * r, c * nte * 12);
-        par_memcpy(s.h_io + s.o_T, j.T + nte * r, c * nte);
-    }
-    if (trj) par_memcpy(s.h_io + s.o_XYZ1, j.XYZ1 + 3 * trj * r, c * trj * 12);
-    EN_CUDA(cudaMemcpyAsync(s.d_io, s.h_io, s.in_bytes, cudaMemcpyHostToDevice, s.st));
-    EN_CUDA(cudaMemcpyAsync(s.L.tables, j.h_tables, j.im.bytes.size(), cudaMemcpyHostToDevice, s.st));
-    // generator states of spins [lo, hi): the job's range of the seed cache, both generators
-    EN_CUDA(cudaStreamWaitEvent(s.st, j.seed->ready, 0));
-    const size_t sc = lo - j.seed->base;                 // the chunk's first spin in the cache
-    EN_CUDA(cudaMemcpyAsync(s.L.G.mt_r, j.seed->mt + sc * sw::kMtN, c * sw::kMtN * 4, cudaMemcpyDeviceToDevice, s.st));
-    EN_CUDA(cudaMemcpyAsync(s.L.G.mt_u, j.seed->mt + sc * sw::kMtN, c * sw::kMtN * 4, cudaMemcpyDeviceToDevice, s.st));
-    EN_CUDA(cudaMemcpyAsync(s.L.G.p_r, j.seed->p + sc, c * 4, cudaMemcpyDeviceToDevice, s.st));
-    EN_CUDA(cudaMemcpyAsync(s.L.G.p_u, j.seed->p + sc, c * 4, cudaMemcpyDeviceToDevice, s.st));
-    EN_CUDA(cudaMemsetAsync(s.L.G.nhead, 0, c * 4, s.st));
-    EN_CUDA(cudaMemsetAsync(s.L.G.ncnt, 0, c * 4, s.st));
-    EN_CUDA(cudaMemsetAsync(s.L.G.uhead, 0, c * 4, s.st));
-    EN_CUDA(cudaMemsetAsync(s.L.G.ucnt, 0, c * 4, s.st));
-    const uint64_t steps = (uint64_t)j.p.n_timepoints * (uint64_t)(j.p.n_dummy_scan + 1);
-    s.max_rounds = 64 + steps * (j.p.max_iterations + 2);
-    s.rounds = 0;
-    s.state = Slot::RUNNING;
-    return SW_OK;
-}
-
 struct ChunkView {
     sw::SpinState S;
     sw::RngState G;
@@ -336,6 +287,61 @@ ChunkView view(const Slot &s) {
     v.M0 = shift(reinterpret_cast<const float *>(d + s.o_M0), lo * 3);
     v.XYZ0 = shift(reinterpret_cast<const float *>(d + s.o_XYZ0), lo * 3);
     return v;
+}
+
+// Hands the next spin range of a ready job to a free slot and issues the chunk's work.
+int start_chunk(sw_engine *E, Slot &s, Job &j) {
+    const uint32_t lo = j.next_lo, hi = std::min<uint32_t>(j.spin_hi, lo + j.chunk);
+    j.next_lo = hi;
+    j.running++;
+    s.job = &j;
+    s.lo = lo;
+    s.hi = hi;
+    const bool sig = j.d_sig != nullptr;
+    const size_t c = hi - lo, nte = sig ? 0 : j.nte, trj = sig ? 0 : j.trj, r = lo - j.spin_lo;
+    size_t off = 0;
+    auto sec = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~size_t(255); return o; };
+    s.o_M0 = sec(c * 12);
+    s.o_XYZ0 = sec(c * 12);
+    s.o_M1 = sec(c * nte * 12);
+    s.o_T = sec(c * nte);
+    s.o_XYZ1 = sec(c * trj * 12);
+    s.in_bytes = off;                    // inputs and the outputs' starting contents
+    s.o_st = sec(c * 4);
+    s.out_bytes = off - s.o_M1;
+    // stage: inputs and the caller's current output contents (slots the walk never reaches keep
+    // them, as with sw_sim)
+    par_memcpy(s.h_io + s.o_M0, j.M0 + 3 * r, c * 12);
+    par_memcpy(s.h_io + s.o_XYZ0, j.XYZ0 + 3 * r, c * 12);
+    if (nte) {
+        par_memcpy(s.h_io + s.o_M1, j.M1 + 3 * nte * r, c * nte * 12);
+        par_memcpy(s.h_io + s.o_T, j.T + nte * r, c * nte);
+    }
+    if (trj) par_memcpy(s.h_io + s.o_XYZ1, j.XYZ1 + 3 * trj * r, c * trj * 12);
+    EN_CUDA(cudaMemcpyAsync(s.d_io, s.h_io, s.in_bytes, cudaMemcpyHostToDevice, s.st));
+    EN_CUDA(cudaMemcpyAsync(s.L.tables, j.h_tables, j.im.bytes.size(), cudaMemcpyHostToDevice, s.st));
+    const uint64_t steps = (uint64_t)j.p.n_timepoints * (uint64_t)(j.p.n_dummy_scan + 1);
+    s.max_rounds = 64 + steps * (j.p.max_iterations + 2);
+    s.rounds = 0;
+    s.state = Slot::RUNNING;
+    if (j.P.rng == SW_RNG_MINSTD) {      // thrust::minstd_rand: seeding is a modular power
+        const ChunkView v = view(s);
+        EN_CUDA(sw::launch_seed_range(j.P, v.G, lo, hi, s.st));
+        E->launches++;
+        return SW_OK;
+    }
+    // generator states of spins [lo, hi): the job's range of the seed cache, both generators
+    EN_CUDA(cudaStreamWaitEvent(s.st, j.seed->ready, 0));
+    const size_t sc = lo - j.seed->base;                 // the chunk's first spin in the cache
+    EN_CUDA(cudaMemcpyAsync(s.L.G.mt_r, j.seed->mt + sc * sw::kMtN, c * sw::kMtN * 4, cudaMemcpyDeviceToDevice, s.st));
+    EN_CUDA(cudaMemcpyAsync(s.L.G.mt_u, j.seed->mt + sc * sw::kMtN, c * sw::kMtN * 4, cudaMemcpyDeviceToDevice, s.st));
+    EN_CUDA(cudaMemcpyAsync(s.L.G.p_r, j.seed->p + sc, c * 4, cudaMemcpyDeviceToDevice, s.st));
+    EN_CUDA(cudaMemcpyAsync(s.L.G.p_u, j.seed->p + sc, c * 4, cudaMemcpyDeviceToDevice, s.st));
+    EN_CUDA(cudaMemsetAsync(s.L.G.nhead, 0, c * 4, s.st));
+    EN_CUDA(cudaMemsetAsync(s.L.G.ncnt, 0, c * 4, s.st));
+    EN_CUDA(cudaMemsetAsync(s.L.G.uhead, 0, c * 4, s.st));
+    EN_CUDA(cudaMemsetAsync(s.L.G.ucnt, 0, c * 4, s.st));
+    return SW_OK;
 }
 
 // Issues `k` refill/walk rounds (after k_init when first) and the read-back of the active count.
@@ -470,8 +476,11 @@ int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_se
     if (p->n_substrate < ph.n_substrate)
         return fail(SW_ERR_INVALID, "the mask holds more substrate types than the config defines");
     if (p->fieldmap_exist && !ph.field) return fail(SW_ERR_INVALID, "fieldmap_exist but the phantom has no fieldmap");
+    const uint32_t rng = (uint32_t)precision & ~(uint32_t)SW_PREC_MASK;
+    precision &= SW_PREC_MASK;
     if (precision != SW_PREC_FP32 && precision != SW_PREC_FP64 && precision != SW_PREC_KAHAN)
         return fail(SW_ERR_INVALID, "precision");
+    if (rng != SW_RNG_MT19937 && rng != SW_RNG_MINSTD) return fail(SW_ERR_INVALID, "generator flavour");
     if (p->n_spins > 0xffffffffull) return fail(SW_ERR_INVALID, "n_spins");
     if (spin_hi == ~0ull) spin_hi = p->n_spins;
     if (spin_lo > spin_hi || spin_hi > p->n_spins) return fail(SW_ERR_INVALID, "spin range outside [0, n_spins)");
@@ -516,9 +525,12 @@ int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_se
     build_tables(&j->p, &Q, j->im);
     if (!j->im.complete()) return fail(SW_ERR_INVALID, "internal error: incomplete parameter tables");
     if (j->im.bytes.size() > kTableBytes) return fail(SW_ERR_INVALID, "sequence tables larger than 1 MiB");
+    if (rng == SW_RNG_MINSTD && !E->LT.ms_delta && !(E->LT.ms_delta = minstd_delta_table()))
+        return SW_ERR_CUDA;
     EN_CUDA(cudaMallocHost(&j->h_tables, j->im.bytes.size()));
     std::memcpy(j->h_tables, j->im.bytes.data(), j->im.bytes.size());
     j->P = dev_params(&j->p, &Q);
+    j->P.rng = rng;
     j->M0 = M0; j->XYZ0 = XYZ0; j->M1 = M1; j->XYZ1 = XYZ1; j->T = T; j->status = status;
     j->nte = nte;
     j->trj = trj;
@@ -538,7 +550,7 @@ int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_se
     const Slot &s0 = E->slots[0];
     j->chunk = (uint32_t)std::min<size_t>(s0.cap, s0.io_bytes / per_spin);
     if (n && j->chunk == 0) return fail(SW_ERR_NOMEM, "one spin's trajectory exceeds a slot's I/O buffer");
-    if (n) {
+    if (n && rng == SW_RNG_MT19937) {   // the minstd flavour seeds per chunk (O(log) discard)
         rc = ensure_seeded(E, p->seed, (uint32_t)spin_lo, (uint32_t)spin_hi, j->seed);
         if (rc) {
             cudaFreeHost(j->h_tables);

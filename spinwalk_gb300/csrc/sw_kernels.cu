@@ -108,6 +108,116 @@ __global__ void __launch_bounds__(32 * kSeedWarps)
 }
 
 // ------------------------------------------------------------------------------------------
+// Generator flavour of the reference's CUDA build (kernels.cu:76-80): thrust::minstd_rand,
+// x <- 48271 x mod (2^31 - 1), one 31-bit state per generator (kept in p_r / p_u).
+// ------------------------------------------------------------------------------------------
+constexpr uint32_t kMsA = 48271u, kMsM = 2147483647u;
+
+__host__ __device__ constexpr uint32_t ms_mulmod(uint64_t x, uint64_t y) {
+    // exact x*y mod (2^31 - 1) for x, y < 2^31: 2^31 = 1 (mod m), so fold the high bits twice
+    const uint64_t p = x * y;
+    const uint64_t r = (p & kMsM) + (p >> 31);
+    const uint64_t r2 = (r & kMsM) + (r >> 31);
+    return (uint32_t)(r2 >= kMsM ? r2 - kMsM : r2);
+}
+
+struct MsPow {                       // kMsA^(j+1) mod m, j < 32: lane j's jump ahead
+    uint32_t v[32];
+};
+constexpr MsPow ms_pow_table() {
+    MsPow t{};
+    uint32_t a = kMsA;
+    for (int j = 0; j < 32; j++) {
+        t.v[j] = a;
+        a = ms_mulmod(a, kMsA);
+    }
+    return t;
+}
+__constant__ MsPow c_ms_pow = ms_pow_table();
+
+// linear_congruential_engine::seed + discard (thrust/random/detail/linear_congruential_engine
+// .inl, linear_congruential_engine_discard.h): x0 = s mod m (1 if that is 0), then a^z x0.
+__device__ __forceinline__ uint32_t ms_seed_discard(uint32_t s, uint64_t z) {
+    uint32_t x = s % kMsM;
+    if (x == 0u) x = 1u;
+    uint64_t mul = kMsA, acc = 1;
+    while (z) {
+        if (z & 1u) acc = ms_mulmod(acc, mul);
+        mul = ms_mulmod(mul, mul);
+        z >>= 1;
+    }
+    return ms_mulmod(acc, x);
+}
+
+__global__ void k_seed_minstd(DevParams P, RngState G, uint32_t spin_lo, uint32_t spin_hi) {
+    const uint32_t spin = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (spin >= spin_hi) return;
+    const uint64_t sd = P.seed + spin;                 // kernels.cu:77-78, 87-88
+    const uint32_t x = ms_seed_discard((uint32_t)sd, sd);
+    G.p_r[spin] = x;
+    G.p_u[spin] = x;
+    G.nhead[spin] = 0;
+    G.ncnt[spin] = 0;
+    G.uhead[spin] = 0;
+    G.ucnt[spin] = 0;
+}
+
+// thrust::uniform_real_distribution<float>(0, 1): (x - min) / (1 + (max - min)), then * 1 + 0
+__device__ __forceinline__ float ms_uniform(uint32_t x) {
+    const float r = __fdiv_rn(__uint2float_rn(x - 1u), __fadd_rn(1.0f, (float)(kMsM - 2u)));
+    return __fadd_rn(__fmul_rn(r, 1.0f), 0.0f);
+}
+
+// One warp per spin: lane l takes the (l+1)-th next engine output, 32 per pass.
+__global__ void __launch_bounds__(128)
+    k_refill_minstd(DevParams P, RngState G, const uint32_t *__restrict__ flags,
+                    const uint32_t *__restrict__ ms_delta, uint32_t spin_lo, uint32_t spin_hi) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t spin = spin_lo + blockIdx.x * 4 + w; spin < spin_hi; spin += gridDim.x * 4) {
+        const uint32_t fl = flags[spin], nc = G.ncnt[spin], nh = G.nhead[spin],
+                       uc = G.ucnt[spin];
+        if (fl & kFlagDone) continue;
+        if (nc < kNormBuf) {
+            uint32_t x = G.p_r[spin];
+            float *nb = G.nbuf + (size_t)spin * kNormBuf;
+            const uint32_t K = kNormBuf - nc, wpos = nh + nc;
+            for (uint32_t b = 0; b < K; b += 32) {
+                const uint32_t r = min(32u, K - b);
+                if ((uint32_t)lane < r)
+                    nb[(wpos + b + lane) % kNormBuf] =
+                        ms_normal(ms_mulmod(x, c_ms_pow.v[lane]), ms_delta);
+                x = ms_mulmod(x, c_ms_pow.v[r - 1]);
+            }
+            if (lane == 0) {
+                G.p_r[spin] = x;
+                G.ncnt[spin] = kNormBuf;
+            }
+        }
+        if (uc <= kUnifBuf / 2) {
+            uint32_t x = G.p_u[spin];
+            float *ub = G.ubuf + (size_t)spin * kUnifBuf;
+            const uint32_t K = kUnifBuf - uc, wpos = G.uhead[spin] + uc;
+            for (uint32_t b = 0; b < K; b += 32) {
+                const uint32_t r = min(32u, K - b);
+                if ((uint32_t)lane < r)
+                    ub[(wpos + b + lane) % kUnifBuf] = ms_uniform(ms_mulmod(x, c_ms_pow.v[lane]));
+                x = ms_mulmod(x, c_ms_pow.v[r - 1]);
+            }
+            if (lane == 0) {
+                G.p_u[spin] = x;
+                G.ucnt[spin] = kUnifBuf;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void k_debug_ms_normal(uint32_t x_lo, uint32_t n, float *y, const uint32_t *delta) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        y[i] = ms_normal(x_lo + i, delta);
+}
+
+// ------------------------------------------------------------------------------------------
 // Initial state (kernels.cu:90-104)
 // ------------------------------------------------------------------------------------------
 __global__ void k_init(DevParams P, DevTables Tb, const uint2 *__restrict__ vox,
@@ -597,6 +707,10 @@ cudaError_t launch_seed(const DevParams &P, const RngState &G, cudaStream_t st) 
 cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo, uint32_t hi,
                               cudaStream_t st) {
     if (hi <= lo) return cudaSuccess;
+    if (P.rng == SW_RNG_MINSTD) {
+        k_seed_minstd<<<grid_for(hi - lo, 256, 1 << 30), 256, 0, st>>>(P, G, lo, hi);
+        return cudaGetLastError();
+    }
     k_seed<<<grid_for(((int64_t)hi - lo + 1) / 2, kSeedWarps, 1 << 30), 32 * kSeedWarps, 0, st>>>(
         P, G, lo, hi);
     return cudaGetLastError();
@@ -626,6 +740,11 @@ cudaError_t launch_refill(const DevParams &P, const RngState &G, const uint32_t 
 cudaError_t launch_refill_range(const DevParams &P, const RngState &G, const uint32_t *flags,
                                 const LogfTables &L, uint32_t lo, uint32_t hi, cudaStream_t st) {
     if (hi <= lo) return cudaSuccess;
+    if (P.rng == SW_RNG_MINSTD) {
+        k_refill_minstd<<<grid_for(hi - lo, 4, 152 * 64), 128, 0, st>>>(P, G, flags, L.ms_delta,
+                                                                         lo, hi);
+        return cudaGetLastError();
+    }
     k_refill<<<grid_for(hi - lo, kRefillWarps, 152 * 64), 32 * kRefillWarps, 0, st>>>(
         P, G, flags, L, lo, hi);
     return cudaGetLastError();
@@ -659,6 +778,12 @@ cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevT
 cudaError_t launch_debug_dadd(const double *a, const double *b, double *y, uint64_t n,
                               cudaStream_t st) {
     k_debug_dadd<<<grid_for((int64_t)n, 256, 152 * 16), 256, 0, st>>>(a, b, y, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_ms_normal(uint32_t x_lo, uint32_t n, float *y, const uint32_t *delta,
+                                   cudaStream_t st) {
+    k_debug_ms_normal<<<grid_for((int64_t)n, 256, 152 * 16), 256, 0, st>>>(x_lo, n, y, delta);
     return cudaGetLastError();
 }
 

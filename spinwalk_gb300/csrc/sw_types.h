@@ -46,6 +46,7 @@ struct DevParams {
     int32_t timestep_us;
     int32_t cross_fov, record_traj, fieldmap_exist;
     uint64_t traj_len;        // XYZ1 slots per spin
+    uint32_t rng;             // SW_RNG_MT19937 or SW_RNG_MINSTD (generator flavour)
 };
 
 // Small read-only tables (device pointers into one allocation).
@@ -68,6 +69,9 @@ struct DevTables {
 struct LogfTables {
     const float *tab;         // 64 x {invc, Lhi, Llo}
     const uint32_t *bitmap;   // bit (x_bits - 2^-48 bits): host libm differs from the candidate
+    // minstd flavour: 4-bit host-minus-device ulp corrections of its Gaussian deviate
+    // (sw_minstd.cu), indexed by the folded engine output
+    const uint32_t *ms_delta = nullptr;
 };
 
 // Per-spin walk state between chunks (structure of arrays, one entry per spin).

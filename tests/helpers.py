@@ -7,7 +7,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN_DIR = os.path.join(ROOT, "tests", "golden")
 GOLDEN_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN_DIR)
-                      if f.endswith(".npz") and not f.startswith("phantom_"))
+                      if f.endswith(".npz") and not f.startswith(("phantom_", "minstd_")))
 
 
 def load_golden(name):

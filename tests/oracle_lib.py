@@ -37,6 +37,8 @@ def oracle():
         L.oracle_initial_positions.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_void_p]
         L.oracle_logf.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
         L.oracle_logf.restype = None
+        L.oracle_ms_normal.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p]
+        L.oracle_ms_normal.restype = None
         _ora = L
     return _ora
 
@@ -94,6 +96,13 @@ def initial_positions(fov, seed, n):
     f = np.asarray(fov, np.float32)
     oracle().oracle_initial_positions(_p(f), C.c_uint64(int(seed)), C.c_uint32(n), _p(out))
     return out
+
+
+def host_ms_normal(x_lo, n):
+    """The minstd flavour's deviates of engine outputs x_lo .. x_lo+n-1 (CUDA's host erfcinvf)."""
+    y = np.empty(n, np.float32)
+    oracle().oracle_ms_normal(int(x_lo), int(n), _p(y))
+    return y
 
 
 def host_logf(x):

@@ -151,6 +151,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def precision_errors(pr):
+    """Error of the FP32 and compensated-FP32 (Kahan) phase sums against an FP64 run of the same
+    walk (the FP64 shadow the library computes alongside): the largest per-spin |M - M_fp64|
+    (|M| <= 1) and the largest relative error of the echo signal |mean Mxy| over all echoes."""
+    from spinwalk_gb300 import _lib, abi
+    out = {}
+    for name, prec in (("fp32", abi.SW_PREC_FP32), ("kahan", abi.SW_PREC_KAHAN)):
+        r = _lib.run(pr, precision=prec, fp64_shadow=True)
+        m, d = r["M1"].astype(np.float64), r["M1_fp64"]
+        ok = r["status"] == 0
+        sig = np.abs(m[ok, :, 0].mean(0) + 1j * m[ok, :, 1].mean(0))
+        sig64 = np.abs(d[ok, :, 0].mean(0) + 1j * d[ok, :, 1].mean(0))
+        out[name] = {"max_abs_per_spin": float(np.abs(m[ok] - d[ok]).max()),
+                     "signal_rel": float((np.abs(sig - sig64) / np.maximum(sig64, 1e-30)).max())}
+    return out
+
+
 def cpu_sample_ids(n_spins, n_sample):
     """Stratified sample: evenly spaced spin ids over the whole range (the per-spin discard()
     cost grows with the spin id, so a prefix would under-count it)."""
@@ -312,6 +329,7 @@ def run_ours(args, world, rank, local):
     for r in (seed_roof, walk_roof):
         r["frac"] = r["achieved"] / peak
     roof = {"seed+init+pack": seed_roof, "walk": walk_roof}.get(dominant, walk_roof)
+    errors = precision_errors(pr) if args.workload in ("se", "small") else None
     cpu = None
     if world == 1 or rank == 0:
         if args.cpu_sample > 0:
@@ -333,6 +351,7 @@ def run_ours(args, world, rank, local):
         "e2e": {"value": e2e, "unit": "spin-steps/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
+        "error_vs_fp64": errors,
         "clocks": clocks,
         "status_counts": {str(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))},
     }

@@ -86,3 +86,23 @@ def test_engine_rejects_bad_jobs():
                                           C.byref(pid2))
     assert rc != 0 and b"substrate" in _lib.lib().sw_last_error()
     eng.close()
+
+
+def test_engine_results_same_alone_and_in_a_mix_of_arrivals():
+    """Continuous batching: jobs submitted while others run (polled in between) give the same
+    results as each alone."""
+    jobs = _jobs()[:6]
+    alone = [_lib.run(pr) for pr in jobs]
+    eng = _lib.Engine(n_slots=2, slot_spins=300)
+    pids, outs = {}, []
+    for i, pr in enumerate(jobs):
+        key = (pr.mask.shape, float(pr.mask.sum()))
+        if key not in pids:
+            pids[key] = eng.add_phantom(pr)
+        outs.append(eng.submit(pr, pids[key])[1])
+        eng.poll(wait=1 if i % 2 else 0)          # let earlier jobs run before the next arrives
+    eng.run_all()
+    for k, (o, a) in enumerate(zip(outs, alone)):
+        for key in ("M1", "XYZ1", "T", "status"):
+            assert bits_equal(o[key], a[key]), (k, key)
+    eng.close()

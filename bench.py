@@ -44,10 +44,12 @@ USEFUL_BYTES_PER_SPIN_STEP = 5    # 1 B mask + 4 B field
 SEED_BYTES_PER_SPIN = 2 * 624 * 4 + 6 * 4   # two mt19937 states + 6 ring/index words written
 # DRAM traffic per unit from ncu on the small SE case (profiles/kernels_small_se_300cubed_2e5spins.md),
 # scaled to a full launch by the units it processes (both grow in proportion)
-SEED_DRAM_BYTES_PER_SPIN = 4710.0
-WALK_DRAM_BYTES_PER_SPIN_STEP = 30.8
-SEED_LIMITER = "integer ALU pipe (93.5 % busy, ncu): instruction bound, not HBM"
-WALK_LIMITER = "FP64 pipe (76 % busy, ncu): the voxel gather is not the bound"
+SEED_DRAM_BYTES_PER_SPIN = 4713.0
+WALK_DRAM_BYTES_PER_SPIN_STEP = 26.4
+SEED_LIMITER = ("integer instruction issue (ncu: ALU pipe 83 %, issue 74 %, DRAM 2 %): "
+                "7.7 lane instructions per MT word, not HBM")
+WALK_LIMITER = ("latency of the voxel gather (ncu: issue 47 %, long-scoreboard stalls, "
+                "DRAM 10 %, FP64 pipe 40 % for the 3 position additions)")
 
 
 def workload(name, rank=0):

@@ -393,6 +393,9 @@ def run_batched(args, world, rank):
     plain_dev = _lib.last_timing()["total_ms"] * 1e-3
     plain_rate = p.n_spins * p.n_timepoints * (one["n_dummy_scan"] + 1) / plain_dev
     value = inst_steps / (np.mean(dev_ms) * 1e-3)
+    pr.params.linear_phase_cycling = 0.0
+    pr.params.n_dummy_scan = 0
+    rec_err = bssfp_cycle_errors(pr, [t for t in tracks if t["n_dummy_scan"] == 209])
     line = {"metric": "spin-steps/s (batched instances)", "value": value, "unit": "spin-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": float(np.mean(dev_ms)), "higher_is_better": True, "scaling": "weak",
@@ -404,8 +407,35 @@ def run_batched(args, world, rank):
             "batched_over_plain": value / plain_rate,
             "e2e": {"value": inst_steps / float(np.mean(times)), "unit": "spin-steps/s",
                     "note": "includes the per-track host output copies"},
+            "recurrence_error_vs_fp64": rec_err,
             "clocks": clocks}
     print(json.dumps(line), flush=True)
+
+
+def bssfp_cycle_errors(pr, tracks):
+    """Error of the float steady-state recurrence against its FP64 shadow, per phase cycle: the
+    given tracks (one per cycle) run once with plain float and once with compensated (Kahan)
+    phase sums, each beside the FP64 shadow of the same walk (sw_sim_tracks M1_fp64). Per cycle:
+    the relative error of the signal (complex mean of Mx + iMy over spins, first echo) and the
+    largest per-spin |M - M_fp64|."""
+    from spinwalk_gb300 import _lib, abi
+    res = {"cycles": len(tracks), "n_dummy_scan": tracks[0]["n_dummy_scan"],
+           "definition": "signal: |S - S64| / |S64|, S = mean over spins of Mx + iMy at the "
+                         "first echo; spin: max over spins of max |M - M64| (M0 = 1)"}
+    for name, prec in (("fp32", abi.SW_PREC_FP32), ("kahan", abi.SW_PREC_KAHAN)):
+        outs = _lib.run_tracks(pr, tracks, precision=prec, fp64=True)
+        sig, spin = [], []
+        for o in outs:
+            ok = o["status"] == 0
+            m, md = o["M1"][ok, 0].astype(np.float64), o["M1_fp64"][ok, 0]
+            s32 = np.mean(m[:, 0] + 1j * m[:, 1])
+            s64 = np.mean(md[:, 0] + 1j * md[:, 1])
+            sig.append(abs(s32 - s64) / max(abs(s64), 1e-300))
+            spin.append(float(np.max(np.abs(m - md))) if ok.any() else 0.0)
+        res[name] = {"signal_rel_max": float(max(sig)), "signal_rel_median": float(np.median(sig)),
+                     "spin_abs_max": float(max(spin)),
+                     "signal_rel_per_cycle": [float(f"{v:.3g}") for v in sig]}
+    return res
 
 
 def c3_instances(rank=0):

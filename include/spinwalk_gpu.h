@@ -228,7 +228,13 @@ int sw_sync(void *stream);
  * scan), optional per-pulse RF_FA / RF_PH arrays (NULL = the sequence's), and host output
  * buffers. `param` supplies everything else (its n_dummy_scan, phase cycling, c and s are
  * ignored; enRecordTrajectory must be 0). Tracks with identical RF configuration and
- * DUMMY_SCAN are rejected as duplicates. FP32 arithmetic (the reference's).
+ * DUMMY_SCAN are rejected as duplicates.
+ *
+ * precision : SW_PREC_FP32 (the reference's arithmetic), SW_PREC_KAHAN (compensated float phase
+ * sums) or SW_PREC_FP64 (M1 = the FP64 values rounded to float), as for sw_sim. A track's M1_fp64
+ * (optional, host [n_spins][n_TE][3]) receives the FP64 shadow of that track: the steady-state
+ * recurrence over all DUMMY_SCAN scans carried in double, bit-identical to sw_sim's M1_fp64 on
+ * that instance. Generator flavour bits are not accepted (SW_RNG_MT19937 only).
  */
 typedef struct sw_track {
     float linear_phase_cycling;
@@ -241,11 +247,12 @@ typedef struct sw_track {
     float *XYZ1;              /* [n_spins][3] host: final position */
     uint8_t *T;               /* [n_spins][n_TE] host */
     int32_t *status;          /* [n_spins] host, or NULL */
+    double *M1_fp64;          /* [n_spins][n_TE][3] host FP64 shadow, or NULL */
 } sw_track;
 
 int sw_sim_tracks(const sw_params *param, const sw_sequence *seq, const sw_track *tracks,
                   uint32_t n_tracks, const float *pFieldMap, const uint8_t *pMask,
-                  const float *M0, const float *XYZ0);
+                  const float *M0, const float *XYZ0, int precision);
 
 /*
  * sw_sim_device without any device allocation, for callers that are not allowed to allocate

@@ -50,7 +50,7 @@ def lib():
         L.sw_sim_device.argtypes = sim_args + [C.c_void_p]
         L.sw_sim_device_noalloc.argtypes = sim_args[:10] + [C.c_void_p]
         L.sw_sim_tracks.argtypes = [P(abi.SwParams), P(abi.SwSequence), P(abi.SwTrack), C.c_uint32,
-                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.sw_sim_batch.argtypes = [P(abi.SwInstance), C.c_uint32, C.c_void_p, C.c_void_p, C.c_int]
         L.sw_engine_create.argtypes = [C.c_int, C.c_uint32, C.c_uint32, C.c_uint64, P(C.c_void_p)]
         L.sw_engine_destroy.argtypes = [C.c_void_p]
@@ -371,10 +371,11 @@ def run_device_noalloc(problem, d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T
                                       d_status, stream))
 
 
-def run_tracks(problem, tracks, fill=0.0):
+def run_tracks(problem, tracks, fill=0.0, precision=abi.SW_PREC_FP32, fp64=False):
     """sw_sim_tracks: many instances of `problem` sharing one walk. `tracks` is a list of dicts
     with keys linear_phase_cycling, quadratic_phase_cycling, n_dummy_scan and optionally
-    RF_FA_deg / RF_PH_deg arrays. Returns one output dict per track."""
+    RF_FA_deg / RF_PH_deg arrays. Returns one output dict per track; with fp64=True each also
+    holds "M1_fp64", the track's FP64 shadow."""
     n, nte = problem.params.n_spins, problem.n_te
     arr = (abi.SwTrack * len(tracks))()
     outs, keep = [], []
@@ -397,9 +398,14 @@ def run_tracks(problem, tracks, fill=0.0):
         s.XYZ1 = abi.ptr(o["XYZ1"], C.c_float)
         s.T = abi.ptr(o["T"], C.c_uint8)
         s.status = abi.ptr(o["status"], C.c_int32)
+        if fp64:
+            o["M1_fp64"] = np.full((n, nte, 3), fill, np.float64)
+            s.M1_fp64 = abi.ptr(o["M1_fp64"], C.c_double)
+        else:
+            s.M1_fp64 = abi.ptr(None, C.c_double)
     check(lib().sw_sim_tracks(C.byref(problem.params), C.byref(problem.seq.struct), arr,
                               len(tracks), _p(problem.field), _p(problem.mask), _p(problem.M0),
-                              _p(problem.XYZ0)))
+                              _p(problem.XYZ0), int(precision)))
     return outs
 
 

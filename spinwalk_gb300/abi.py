@@ -90,6 +90,7 @@ class SwTrack(C.Structure):
         ("XYZ1", C.POINTER(C.c_float)),
         ("T", C.POINTER(C.c_uint8)),
         ("status", C.POINTER(C.c_int32)),
+        ("M1_fp64", C.POINTER(C.c_double)),
     ]
 
 

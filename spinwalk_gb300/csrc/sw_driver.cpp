@@ -169,7 +169,7 @@ extern "C" int sw_run_config(const char *ini_path, int device) {
                 t.XYZ1 = xyz[k].data();
             }
             rc = sw_sim_tracks(&p, &q, tracks.data(), (uint32_t)ns, field.empty() ? nullptr : field.data(),
-                               mask.data(), M0.data(), XYZ0s.data());
+                               mask.data(), M0.data(), XYZ0s.data(), SW_PREC_FP32);
             if (rc) return drv_fail(rc, sw_last_error());
             for (size_t k = 0; k < ns; k++)
                 std::copy(xyz[k].begin(), xyz[k].end(), XYZ1.begin() + 3 * n * trj * k);

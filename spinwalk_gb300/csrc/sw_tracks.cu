@@ -42,6 +42,7 @@ struct GroupTables {
     const uint32_t *rec_any;  // [max_ds + 1]: some track records in that scan
     const int32_t *track_nd;  // [n_tracks]
     float *const *M1;         // [n_tracks] -> [n][n_TE][3]
+    double *const *M1d;       // [n_tracks] -> [n][n_TE][3] FP64 shadow, entries may be null
     float *const *XYZ1;       // [n_tracks] -> [n][3]
     uint8_t *const *T;        // [n_tracks] -> [n][n_TE]
     int32_t *const *status;   // [n_tracks] -> [n]
@@ -51,8 +52,11 @@ struct GroupState {
     float *mg;                // [3][n_groups][n]
     float *mr;                // [3][n_groups][n]
     float *acc_rec;           // [n]
+    float *acc_rec_e;         // [n] compensation term of acc_rec (Kahan)
     uint32_t *tp_old_rec;     // [n]
     uint32_t *rec_started;    // [n]
+    double *mg64, *mr64;      // FP64 shadow of mg / mr, or null
+    double *accd_rec;         // [n] FP64 shadow of acc_rec
 };
 
 // dephase_relax_f split in two: the trigonometry and exponentials depend only on the shared
@@ -79,12 +83,45 @@ __device__ __forceinline__ void apply_relax(const RelaxOp &r, const float *a, fl
     }
 }
 
+// The same split of dephase_relax_d (the FP64 shadow): operands and operation order as there.
+struct RelaxOpD {
+    double s, c, e1, e2;
+};
+__device__ __forceinline__ RelaxOpD make_relax_d(double phase, double T1, double T2, double dt_s,
+                                                 bool &relax) {
+    RelaxOpD r;
+    sincos(phase * kDeg2Rad, &r.s, &r.c);
+    relax = T1 >= 0 && T2 >= 0;
+    r.e1 = relax ? exp(-dt_s / T1) : 0.;
+    r.e2 = relax ? exp(-dt_s / T2) : 0.;
+    return r;
+}
+__device__ __forceinline__ void apply_relax_d(const double *r, bool relax, const double *a,
+                                              double *b) {
+    zrot_d(r[0], r[1], a, b);
+    if (relax) {
+        b[0] *= r[3];
+        b[1] *= r[3];
+        b[2] = 1. + r[2] * (b[2] - 1.);
+    }
+}
+
 __device__ __forceinline__ void load_m(const float *base, size_t plane, size_t idx, float *m) {
     m[0] = base[idx];
     m[1] = base[plane + idx];
     m[2] = base[2 * plane + idx];
 }
 __device__ __forceinline__ void store_m(float *base, size_t plane, size_t idx, const float *m) {
+    base[idx] = m[0];
+    base[plane + idx] = m[1];
+    base[2 * plane + idx] = m[2];
+}
+__device__ __forceinline__ void load_md(const double *base, size_t plane, size_t idx, double *m) {
+    m[0] = base[idx];
+    m[1] = base[plane + idx];
+    m[2] = base[2 * plane + idx];
+}
+__device__ __forceinline__ void store_md(double *base, size_t plane, size_t idx, const double *m) {
     base[idx] = m[0];
     base[plane + idx] = m[1];
     base[2 * plane + idx] = m[2];
@@ -97,7 +134,13 @@ __global__ void k_groups_init(DevParams P, GroupTables GT, GroupState GS, const 
     const size_t n = P.n_spins, plane = (size_t)GT.n_groups * n;
     const float m[3] = {M0[3 * (size_t)spin], M0[3 * (size_t)spin + 1], M0[3 * (size_t)spin + 2]};
     for (uint32_t g = 0; g < GT.n_groups; g++) store_m(GS.mg, plane, (size_t)g * n + spin, m);
+    if (GS.mg64) {
+        const double md[3] = {m[0], m[1], m[2]};
+        for (uint32_t g = 0; g < GT.n_groups; g++) store_md(GS.mg64, plane, (size_t)g * n + spin, md);
+        GS.accd_rec[spin] = 0.;
+    }
     GS.acc_rec[spin] = 0.f;
+    GS.acc_rec_e[spin] = 0.f;
     GS.tp_old_rec[spin] = 0;
     GS.rec_started[spin] = 0;
     // a start outside the phantom ends every track at once (status set by k_init)
@@ -130,6 +173,11 @@ struct BlochEvent {
     float rr[4];              // the same for the recording tracks' phase (after their 1st echo)
     float xo[4];              // scan end: position
 };
+// FP64 shadow of an event's relaxation operators (parallel array to the event log).
+struct BlochEvent64 {
+    double r[4];
+    double rr[4];
+};
 
 __device__ __forceinline__ void put_relax(float *dst, const RelaxOp &r) {
     dst[0] = r.s; dst[1] = r.c; dst[2] = r.e1; dst[3] = r.e2;
@@ -141,12 +189,17 @@ __device__ __forceinline__ RelaxOp get_relax(const float *src, bool relax) {
     return r;
 }
 
+// KAHAN: compensated float phase sums (acc, acc_rec), as the plain kernel's SW_PREC_KAHAN.
+// SHADOW: FP64 phase sums beside them and FP64 relaxation operators in log64, as the plain
+// kernel's FP64 shadow (DBL) computes them.
+template <bool KAHAN, bool SHADOW>
 __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t flags,
                                                  const DevParams &P, const DevTables &Tb,
                                                  const GroupTables &GT, const GroupState &GS,
                                                  const uint2 *__restrict__ vox,
                                                  const SpinState &S, const RngState &G,
-                                                 uint32_t *log_count, BlochEvent *log) {
+                                                 uint32_t *log_count, BlochEvent *log,
+                                                 BlochEvent64 *log64) {
     WalkRegs w;
     w.xo[0] = S.x[spin]; w.xo[1] = S.y[spin]; w.xo[2] = S.z[spin];
     w.ind_old = S.ind_old[spin];
@@ -159,15 +212,33 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
     const float *nb = G.nbuf + (size_t)spin * kNormBuf;
     const float *ub = G.ubuf + (size_t)spin * kUnifBuf;
     BlochEvent *lg = log + (size_t)spin * kLogCap;
+    BlochEvent64 *lg64 = SHADOW ? log64 + (size_t)spin * kLogCap : nullptr;
     uint32_t ne = 0;
 
     float acc = S.acc[spin], acc_rec = GS.acc_rec[spin];
+    float acc_e = KAHAN ? S.acc_e[spin] : 0.f, acc_rec_e = KAHAN ? GS.acc_rec_e[spin] : 0.f;
+    double accd = SHADOW ? S.accd[spin] : 0., accd_rec = SHADOW ? GS.accd_rec[spin] : 0.;
     uint32_t tp = S.tp[spin], tp_old = S.tp_old[spin], tp_old_rec = GS.tp_old_rec[spin];
     uint32_t ds = S.ds[spin];
     bool rec_started = GS.rec_started[spin] != 0;
     uint32_t ctr = S.ctr[spin], ctr2 = S.ctr2[spin];
     uint32_t c_rf = ctr & 0xffffu, c_te = ctr >> 16, c_dph = ctr2 & 0xffffu, c_grad = ctr2 >> 16;
     bool started = (flags & kFlagStarted) != 0;
+
+    auto fadd = [&](float &s_, float &e_, float x) {
+        if (KAHAN) kahan_add(s_, e_, x); else s_ += x;
+    };
+    // relaxation operator of a phase sum over (tp - t0) time points, float and FP64
+    auto relax_f = [&](float a, float e, uint32_t t0) {
+        const float te = (float)((double)((tp - t0) * (uint32_t)P.timestep_us) * 1e-6);
+        return make_relax(KAHAN ? a + e : a, __ldg(Tb.T1f + w.ts_old), __ldg(Tb.T2f + w.ts_old), te);
+    };
+    auto relax_d = [&](double a, uint32_t t0, double *dst, bool &relax) {
+        const double ted = (double)(tp - t0) * (double)P.timestep_us * 1e-6;
+        const RelaxOpD r = make_relax_d(a, __ldg(Tb.T1d + w.ts_old), __ldg(Tb.T2d + w.ts_old), ted,
+                                        relax);
+        dst[0] = r.s; dst[1] = r.c; dst[2] = r.e1; dst[3] = r.e2;
+    };
 
     constexpr uint32_t NONE = 0xffffffffu;
     bool rec_scan = ds <= GT.max_ds && GT.rec_any[ds] != 0;
@@ -188,8 +259,9 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
             w.ind_old = P.matrix_length + 1;
             tp = tp_old = 0;
             c_rf = 1; c_te = 0; c_dph = 0; c_grad = 0;
-            acc = 0.f;
-            acc_rec = 0.f;
+            acc = 0.f; acc_e = 0.f;
+            acc_rec = 0.f; acc_rec_e = 0.f;
+            accd = 0.; accd_rec = 0.;
             tp_old_rec = 0;
             rec_started = false;
             rec_scan = GT.rec_any[ds] != 0;
@@ -201,14 +273,18 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
             continue;
         }
         if (tp >= P.n_timepoints) {                                 // kernels.cu:225-231
-            const float te = (float)((double)((tp - tp_old) * (uint32_t)P.timestep_us) * 1e-6);
-            const RelaxOp r = make_relax(acc, __ldg(Tb.T1f + w.ts_old), __ldg(Tb.T2f + w.ts_old), te);
-            BlochEvent &e = lg[ne++];
+            const RelaxOp r = relax_f(acc, acc_e, tp_old);
+            BlochEvent &e = lg[ne];
             e.head = kEvScanEnd | (ds << 8);
             e.ds = ds;
             e.flags = r.relax ? 1u : 0u;
             put_relax(e.r, r);
             e.xo[0] = (float)dfrom(w.xo[0]); e.xo[1] = (float)dfrom(w.xo[1]); e.xo[2] = (float)dfrom(w.xo[2]);
+            if (SHADOW) {
+                bool rl;
+                relax_d(accd, tp_old, lg64[ne].r, rl);
+            }
+            ne++;
             ds++;
             started = false;
             continue;
@@ -221,12 +297,22 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
         if (mv == kMoveLost) { status = SW_SPIN_LOST; break; }
         if (mv == kMoveOOB) { status = SW_SPIN_OOB; break; }
 
-        acc += w.field;                                             // kernels.cu:171
-        if (rec_started) acc_rec += w.field;
+        fadd(acc, acc_e, w.field);                                  // kernels.cu:171
+        if (rec_started) fadd(acc_rec, acc_rec_e, w.field);
+        if (SHADOW) {
+            accd += (double)w.field;
+            if (rec_started) accd_rec += (double)w.field;
+        }
         if (tp == t_dph) {                                          // kernels.cu:175-178
-            const float inc = (float)spin * __ldg(Tb.dph_deg + c_dph) / (float)P.n_spins;
-            acc += inc;
-            if (rec_started) acc_rec += inc;
+            const float deg = __ldg(Tb.dph_deg + c_dph);
+            const float inc = (float)spin * deg / (float)P.n_spins;
+            fadd(acc, acc_e, inc);
+            if (rec_started) fadd(acc_rec, acc_rec_e, inc);
+            if (SHADOW) {
+                const double incd = (double)spin * (double)deg / (double)P.n_spins;
+                accd += incd;
+                if (rec_started) accd_rec += incd;
+            }
             c_dph++;
             t_dph = c_dph < P.n_dephasing ? (uint32_t)Tb.dph_tp[c_dph] : NONE;
         }
@@ -235,44 +321,67 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
                               (double)__ldg(Tb.gy + c_grad) * dfrom(xn[1]) +
                               (double)__ldg(Tb.gz + c_grad) * dfrom(xn[2])) *
                              1e-3 * (double)P.timestep_us * 1e-6 * kGamma * kRad2Deg;
-            acc = (float)((double)acc + g);
-            if (rec_started) acc_rec = (float)((double)acc_rec + g);
+            if (KAHAN) {
+                const float ghi = (float)g, glo = (float)(g - (double)ghi);
+                kahan_add(acc, acc_e, ghi);
+                kahan_add(acc, acc_e, glo);
+                if (rec_started) {
+                    kahan_add(acc_rec, acc_rec_e, ghi);
+                    kahan_add(acc_rec, acc_rec_e, glo);
+                }
+            } else {
+                acc = (float)((double)acc + g);
+                if (rec_started) acc_rec = (float)((double)acc_rec + g);
+            }
+            if (SHADOW) {
+                accd += g;
+                if (rec_started) accd_rec += g;
+            }
             c_grad++;
             t_grad = c_grad < P.n_gradient ? (uint32_t)Tb.grad_tp[c_grad] : NONE;
         }
         if (tp == t_rf) {                                           // kernels.cu:190-199
-            const float T1 = __ldg(Tb.T1f + w.ts_old), T2 = __ldg(Tb.T2f + w.ts_old);
-            const float te = (float)((double)((tp - tp_old) * (uint32_t)P.timestep_us) * 1e-6);
-            const RelaxOp r = make_relax(acc, T1, T2, te);
-            BlochEvent &e = lg[ne++];
+            const RelaxOp r = relax_f(acc, acc_e, tp_old);
+            BlochEvent &e = lg[ne];
             e.head = kEvRf | (c_rf << 8);
             e.ds = ds;
             e.flags = (r.relax ? 1u : 0u) | (rec_started ? 4u : 0u);
             put_relax(e.r, r);
+            if (SHADOW) {
+                bool rl;
+                relax_d(accd, tp_old, lg64[ne].r, rl);
+            }
             if (rec_started) {
-                const float ter = (float)((double)((tp - tp_old_rec) * (uint32_t)P.timestep_us) * 1e-6);
-                const RelaxOp rr = make_relax(acc_rec, T1, T2, ter);
+                const RelaxOp rr = relax_f(acc_rec, acc_rec_e, tp_old_rec);
                 e.flags |= rr.relax ? 2u : 0u;
                 put_relax(e.rr, rr);
-                acc_rec = 0.f;
+                if (SHADOW) {
+                    bool rl;
+                    relax_d(accd_rec, tp_old_rec, lg64[ne].rr, rl);
+                }
+                acc_rec = 0.f; acc_rec_e = 0.f; accd_rec = 0.;
                 tp_old_rec = tp;
             }
-            acc = 0.f;
+            ne++;
+            acc = 0.f; acc_e = 0.f; accd = 0.;
             tp_old = tp;
             c_rf++;
             t_rf = c_rf < P.n_RF ? (uint32_t)Tb.rf[c_rf].tp : NONE;
         }
         if (tp == t_te) {                                           // kernels.cu:202-215
-            const float T1 = __ldg(Tb.T1f + w.ts_old), T2 = __ldg(Tb.T2f + w.ts_old);
-            const float te = (float)((double)((tp - (rec_started ? tp_old_rec : tp_old)) *
-                                              (uint32_t)P.timestep_us) * 1e-6);
-            const RelaxOp r = make_relax(rec_started ? acc_rec : acc, T1, T2, te);
-            BlochEvent &e = lg[ne++];
+            const uint32_t t0 = rec_started ? tp_old_rec : tp_old;
+            const RelaxOp r = rec_started ? relax_f(acc_rec, acc_rec_e, t0) : relax_f(acc, acc_e, t0);
+            BlochEvent &e = lg[ne];
             e.head = kEvTe | (c_te << 8) | (w.ts_old << 24);
             e.ds = ds;
             e.flags = (r.relax ? 1u : 0u) | (rec_started ? 4u : 0u);
             put_relax(e.r, r);
-            acc_rec = 0.f;
+            if (SHADOW) {
+                bool rl;
+                relax_d(rec_started ? accd_rec : accd, t0, lg64[ne].r, rl);
+            }
+            ne++;
+            acc_rec = 0.f; acc_rec_e = 0.f; accd_rec = 0.;
             tp_old_rec = tp;
             rec_started = true;
             c_te++;
@@ -293,6 +402,14 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
     S.x[spin] = w.xo[0]; S.y[spin] = w.xo[1]; S.z[spin] = w.xo[2];
     S.acc[spin] = acc;
     GS.acc_rec[spin] = acc_rec;
+    if (KAHAN) {
+        S.acc_e[spin] = acc_e;
+        GS.acc_rec_e[spin] = acc_rec_e;
+    }
+    if (SHADOW) {
+        S.accd[spin] = accd;
+        GS.accd_rec[spin] = accd_rec;
+    }
     GS.tp_old_rec[spin] = tp_old_rec;
     GS.rec_started[spin] = rec_started ? 1u : 0u;
     S.field[spin] = w.field;
@@ -307,16 +424,18 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
     return status < 0;
 }
 
+template <bool KAHAN, bool SHADOW>
 __global__ void __launch_bounds__(256)
     k_walk_logged(DevParams P, DevTables Tb, GroupTables GT, GroupState GS,
                   const uint2 *__restrict__ vox, SpinState S, RngState G, uint32_t *active,
-                  uint32_t *log_count, BlochEvent *log) {
+                  uint32_t *log_count, BlochEvent *log, BlochEvent64 *log64) {
     const uint32_t spin = blockIdx.x * blockDim.x + threadIdx.x;
     bool still = false;
     if (spin < P.n_spins) {
         const uint32_t flags = S.flags[spin];
         if (!(flags & kFlagDone))
-            still = walk_logged_spin(spin, flags, P, Tb, GT, GS, vox, S, G, log_count, log);
+            still = walk_logged_spin<KAHAN, SHADOW>(spin, flags, P, Tb, GT, GS, vox, S, G,
+                                                    log_count, log, log64);
         else
             log_count[spin] = 0;
     }
@@ -325,9 +444,13 @@ __global__ void __launch_bounds__(256)
 }
 
 // Applies each spin's logged events to every group (thread per (group, spin), spin fastest).
+// SHADOW: the same events in FP64 on mg64 / mr64 (the plain kernel's FP64 shadow, per group);
+// OUT64: the float outputs are the FP64 values rounded (the plain kernel's SW_PREC_FP64).
+template <bool SHADOW, bool OUT64>
 __global__ void __launch_bounds__(256)
     k_bloch_groups(DevParams P, GroupTables GT, GroupState GS,
-                   const uint32_t *__restrict__ log_count, const BlochEvent *__restrict__ log) {
+                   const uint32_t *__restrict__ log_count, const BlochEvent *__restrict__ log,
+                   const BlochEvent64 *__restrict__ log64) {
     const size_t n = P.n_spins, plane = (size_t)GT.n_groups * n;
     const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (idx >= plane) return;
@@ -337,43 +460,76 @@ __global__ void __launch_bounds__(256)
     if (cnt == 0) return;
     const uint32_t span = GT.max_ds + 1, last = GT.last_ds[g];
     float m[3], mr[3], t3[3];
+    double md[3], mrd[3], u3[3];
     load_m(GS.mg, plane, idx, m);
+    if (SHADOW) load_md(GS.mg64, plane, idx, md);
     bool mr_loaded = false, mr_dirty = false;
+    auto load_mr = [&]() {
+        if (mr_loaded) return;
+        load_m(GS.mr, plane, idx, mr);
+        if (SHADOW) load_md(GS.mr64, plane, idx, mrd);
+        mr_loaded = true;
+    };
     const BlochEvent *lg = log + (size_t)spin * kLogCap;
+    const BlochEvent64 *lg64 = SHADOW ? log64 + (size_t)spin * kLogCap : nullptr;
     for (uint32_t k = 0; k < cnt; k++) {
         const BlochEvent e = lg[k];
         const uint32_t type = e.head & 0xffu, id = (e.head >> 8) & 0xffffu, ds = e.ds;
         if (ds > last) continue;                                    // group finished earlier
         const int32_t t = GT.rec[(size_t)g * span + ds];
         if (type == kEvScanStart) {
-            rf_f(GT.scan_rf[(size_t)g * span + ds], m, t3);
+            const RfOp op = GT.scan_rf[(size_t)g * span + ds];
+            rf_f(op, m, t3);
             m[0] = t3[0]; m[1] = t3[1]; m[2] = t3[2];
+            if (SHADOW) {
+                rf_d(op, md, u3);
+                md[0] = u3[0]; md[1] = u3[1]; md[2] = u3[2];
+            }
         } else if (type == kEvRf) {
             const RfOp op = GT.rf[(size_t)g * P.n_RF + id];
             apply_relax(get_relax(e.r, e.flags & 1u), m, t3);
             rf_f(op, t3, m);
+            if (SHADOW) {
+                apply_relax_d(lg64[k].r, e.flags & 1u, md, u3);
+                rf_d(op, u3, md);
+            }
             if ((e.flags & 4u) && t >= 0) {
-                if (!mr_loaded) { load_m(GS.mr, plane, idx, mr); mr_loaded = true; }
+                load_mr();
                 apply_relax(get_relax(e.rr, e.flags & 2u), mr, t3);
                 rf_f(op, t3, mr);
+                if (SHADOW) {
+                    apply_relax_d(lg64[k].rr, e.flags & 2u, mrd, u3);
+                    rf_d(op, u3, mrd);
+                }
                 mr_dirty = true;
             }
         } else if (type == kEvTe) {
             if (t < 0) continue;
-            const float *src = m;
-            if (e.flags & 4u) {
-                if (!mr_loaded) { load_m(GS.mr, plane, idx, mr); mr_loaded = true; }
-                src = mr;
-            }
-            apply_relax(get_relax(e.r, e.flags & 1u), src, t3);
+            const bool from_rec = (e.flags & 4u) != 0;
+            if (from_rec) load_mr();
+            apply_relax(get_relax(e.r, e.flags & 1u), from_rec ? mr : m, t3);
+            if (SHADOW) apply_relax_d(lg64[k].r, e.flags & 1u, from_rec ? mrd : md, u3);
             float *o = GT.M1[t] + 3 * ((size_t)spin * P.n_TE + id);
-            o[0] = t3[0]; o[1] = t3[1]; o[2] = t3[2];
+            if (OUT64) {
+                o[0] = (float)u3[0]; o[1] = (float)u3[1]; o[2] = (float)u3[2];
+            } else {
+                o[0] = t3[0]; o[1] = t3[1]; o[2] = t3[2];
+            }
+            if (SHADOW && GT.M1d[t]) {
+                double *od = GT.M1d[t] + 3 * ((size_t)spin * P.n_TE + id);
+                od[0] = u3[0]; od[1] = u3[1]; od[2] = u3[2];
+            }
             GT.T[t][(size_t)spin * P.n_TE + id] = (uint8_t)(e.head >> 24);
             mr[0] = t3[0]; mr[1] = t3[1]; mr[2] = t3[2];
+            if (SHADOW) { mrd[0] = u3[0]; mrd[1] = u3[1]; mrd[2] = u3[2]; }
             mr_loaded = mr_dirty = true;
         } else {                                                    // scan end
             apply_relax(get_relax(e.r, e.flags & 1u), m, t3);
             m[0] = t3[0]; m[1] = t3[1]; m[2] = t3[2];
+            if (SHADOW) {
+                apply_relax_d(lg64[k].r, e.flags & 1u, md, u3);
+                md[0] = u3[0]; md[1] = u3[1]; md[2] = u3[2];
+            }
             if (t >= 0) {                                           // track t ends here
                 float *x = GT.XYZ1[t] + 3 * (size_t)spin;
                 x[0] = e.xo[0]; x[1] = e.xo[1]; x[2] = e.xo[2];
@@ -382,7 +538,11 @@ __global__ void __launch_bounds__(256)
         }
     }
     store_m(GS.mg, plane, idx, m);
-    if (mr_dirty) store_m(GS.mr, plane, idx, mr);
+    if (SHADOW) store_md(GS.mg64, plane, idx, md);
+    if (mr_dirty) {
+        store_m(GS.mr, plane, idx, mr);
+        if (SHADOW) store_md(GS.mr64, plane, idx, mrd);
+    }
 }
 
 }  // namespace sw
@@ -407,9 +567,12 @@ std::vector<float> rf_array(const float *override_, const float *base, uint32_t 
 
 extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
                              const sw_track *tracks, uint32_t n_tracks, const float *pFieldMap,
-                             const uint8_t *pMask, const float *M0, const float *XYZ0) {
+                             const uint8_t *pMask, const float *M0, const float *XYZ0,
+                             int precision) {
     int rc = check_args(param, seq);
     if (rc) return rc;
+    if (precision != SW_PREC_FP32 && precision != SW_PREC_KAHAN && precision != SW_PREC_FP64)
+        return fail(SW_ERR_INVALID, "tracks: precision must be SW_PREC_FP32, _KAHAN or _FP64");
     if (!tracks || n_tracks == 0) return fail(SW_ERR_INVALID, "no tracks");
     if (param->enRecordTrajectory) return fail(SW_ERR_INVALID, "tracks do not record trajectories");
     const size_t n = param->n_spins, nte = seq->n_TE, ml = (size_t)param->matrix_length;
@@ -502,18 +665,25 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     const size_t o_mask = slot(ml), o_field = slot(has_field ? ml * 4 : 0), o_M0 = slot(n * 12),
                  o_XYZ0 = slot(n * 12), o_scratch_xyz = slot(n * 12), o_scratch_st = slot(n * 4),
                  o_tab = slot(im.bytes.size()), o_gtab = slot(gi.bytes.size()),
-                 o_ptrs = slot(4 * sizeof(void *) * n_tracks),
+                 o_ptrs = slot(5 * sizeof(void *) * n_tracks),
                  o_mg = slot(2 * 3 * sizeof(float) * (size_t)ng * n),
-                 o_gs = slot(12 * n), o_lcnt = slot(4 * n),
+                 o_gs = slot(16 * n), o_lcnt = slot(4 * n),
                  o_log = slot(sizeof(sw::BlochEvent) * sw::kLogCap * n);
-    std::vector<size_t> o_M1(n_tracks), o_X(n_tracks), o_T(n_tracks), o_S(n_tracks);
+    bool shadow = precision == SW_PREC_FP64;
+    for (uint32_t t = 0; t < n_tracks; t++) shadow = shadow || (nte && tracks[t].M1_fp64);
+    const size_t o_mg64 = slot(shadow ? 2 * 3 * sizeof(double) * (size_t)ng * n : 0),
+                 o_accd = slot(shadow ? 8 * n : 0),
+                 o_log64 = slot(shadow ? sizeof(sw::BlochEvent64) * sw::kLogCap * n : 0);
+    std::vector<size_t> o_M1(n_tracks), o_X(n_tracks), o_T(n_tracks), o_S(n_tracks),
+        o_M1d(n_tracks);
     for (uint32_t t = 0; t < n_tracks; t++) {
         o_M1[t] = slot(n * nte * 12);
         o_X[t] = slot(n * 12);
         o_T[t] = slot(n * nte);
         o_S[t] = slot(n * 4);
+        o_M1d[t] = slot(tracks[t].M1_fp64 ? n * nte * 24 : 0);
     }
-    const Layout Lm = layout(nullptr, n, param->matrix_length, 0, false);
+    const Layout Lm = layout(nullptr, n, param->matrix_length, 0, shadow);
     const size_t o_ws = slot(Lm.bytes);
     if (off > C.size) {
         if (C.buf) cudaFree(C.buf);
@@ -543,20 +713,25 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     TR_CUDA(cudaMemcpyAsync(d + o_XYZ0, XYZ0, n * 12, cudaMemcpyHostToDevice, st));
     TR_CUDA(cudaMemcpyAsync(d + o_tab, im.bytes.data(), im.bytes.size(), cudaMemcpyHostToDevice, st));
     TR_CUDA(cudaMemcpyAsync(d + o_gtab, gi.bytes.data(), gi.bytes.size(), cudaMemcpyHostToDevice, st));
-    std::vector<void *> ptrs(4 * (size_t)n_tracks);
+    std::vector<void *> ptrs(5 * (size_t)n_tracks);
     for (uint32_t t = 0; t < n_tracks; t++) {
+        const bool t64 = nte && tracks[t].M1_fp64;
         ptrs[t] = d + o_M1[t];
         ptrs[n_tracks + t] = d + o_X[t];
         ptrs[2 * n_tracks + t] = d + o_T[t];
         ptrs[3 * n_tracks + t] = tracks[t].status ? (void *)(d + o_S[t]) : nullptr;
+        ptrs[4 * n_tracks + t] = t64 ? (void *)(d + o_M1d[t]) : nullptr;
         if (nte) {     // unreached echoes keep the caller's contents, as in the reference
             TR_CUDA(cudaMemcpyAsync(d + o_M1[t], tracks[t].M1, n * nte * 12, cudaMemcpyHostToDevice, st));
             TR_CUDA(cudaMemcpyAsync(d + o_T[t], tracks[t].T, n * nte, cudaMemcpyHostToDevice, st));
+            if (t64)
+                TR_CUDA(cudaMemcpyAsync(d + o_M1d[t], tracks[t].M1_fp64, n * nte * 24,
+                                        cudaMemcpyHostToDevice, st));
         }
     }
     TR_CUDA(cudaMemcpyAsync(d + o_ptrs, ptrs.data(), ptrs.size() * sizeof(void *), cudaMemcpyHostToDevice, st));
 
-    const Layout L = layout(d + o_ws, n, param->matrix_length, 0, false);
+    const Layout L = layout(d + o_ws, n, param->matrix_length, 0, shadow);
     const sw::DevParams P = dev_params(&pw, seq);
     const sw::DevTables Tb = dev_tables(im, d + o_tab);
     sw::GroupTables GT;
@@ -575,12 +750,18 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     GT.XYZ1 = reinterpret_cast<float *const *>(dp + n_tracks);
     GT.T = reinterpret_cast<uint8_t *const *>(dp + 2 * (size_t)n_tracks);
     GT.status = reinterpret_cast<int32_t *const *>(dp + 3 * (size_t)n_tracks);
+    GT.M1d = reinterpret_cast<double *const *>(dp + 4 * (size_t)n_tracks);
     sw::GroupState GS;
     GS.mg = reinterpret_cast<float *>(d + o_mg);
     GS.mr = GS.mg + 3 * (size_t)ng * n;
     GS.acc_rec = reinterpret_cast<float *>(d + o_gs);
     GS.tp_old_rec = reinterpret_cast<uint32_t *>(d + o_gs + 4 * n);
     GS.rec_started = reinterpret_cast<uint32_t *>(d + o_gs + 8 * n);
+    GS.acc_rec_e = reinterpret_cast<float *>(d + o_gs + 12 * n);
+    GS.mg64 = shadow ? reinterpret_cast<double *>(d + o_mg64) : nullptr;
+    GS.mr64 = shadow ? GS.mg64 + 3 * (size_t)ng * n : nullptr;
+    GS.accd_rec = shadow ? reinterpret_cast<double *>(d + o_accd) : nullptr;
+    sw::BlochEvent64 *elog64 = shadow ? reinterpret_cast<sw::BlochEvent64 *>(d + o_log64) : nullptr;
 
     uint32_t *lcnt = reinterpret_cast<uint32_t *>(d + o_lcnt);
     sw::BlochEvent *elog = reinterpret_cast<sw::BlochEvent *>(d + o_log);
@@ -599,7 +780,7 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
                             L.vox, param->matrix_length, param->n_substrate, L.active + 1, st));
     TR_CUDA(sw::launch_seed(P, L.G, st));
     TR_CUDA(sw::launch_init(P, Tb, L.vox, reinterpret_cast<const float *>(d + o_M0),
-                            reinterpret_cast<const float *>(d + o_XYZ0), L.S, O, false, st));
+                            reinterpret_cast<const float *>(d + o_XYZ0), L.S, O, shadow, st));
     sw::k_groups_init<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
         P, GT, GS, L.S, reinterpret_cast<const float *>(d + o_M0),
         reinterpret_cast<const float *>(d + o_XYZ0));
@@ -615,11 +796,22 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
         if (round >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
         TR_CUDA(cudaMemsetAsync(L.active, 0, 4, st));
         TR_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
-        sw::k_walk_logged<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-            P, Tb, GT, GS, L.vox, L.S, L.G, L.active, lcnt, elog);
+        const unsigned gw = (unsigned)((n + 255) / 256), gb = (unsigned)(((size_t)ng * n + 255) / 256);
+        if (precision == SW_PREC_KAHAN && shadow)
+            sw::k_walk_logged<true, true><<<gw, 256, 0, st>>>(P, Tb, GT, GS, L.vox, L.S, L.G, L.active, lcnt, elog, elog64);
+        else if (precision == SW_PREC_KAHAN)
+            sw::k_walk_logged<true, false><<<gw, 256, 0, st>>>(P, Tb, GT, GS, L.vox, L.S, L.G, L.active, lcnt, elog, elog64);
+        else if (shadow)
+            sw::k_walk_logged<false, true><<<gw, 256, 0, st>>>(P, Tb, GT, GS, L.vox, L.S, L.G, L.active, lcnt, elog, elog64);
+        else
+            sw::k_walk_logged<false, false><<<gw, 256, 0, st>>>(P, Tb, GT, GS, L.vox, L.S, L.G, L.active, lcnt, elog, elog64);
         TR_CUDA(cudaGetLastError());
-        sw::k_bloch_groups<<<(unsigned)(((size_t)ng * n + 255) / 256), 256, 0, st>>>(
-            P, GT, GS, lcnt, elog);
+        if (precision == SW_PREC_FP64)
+            sw::k_bloch_groups<true, true><<<gb, 256, 0, st>>>(P, GT, GS, lcnt, elog, elog64);
+        else if (shadow)
+            sw::k_bloch_groups<true, false><<<gb, 256, 0, st>>>(P, GT, GS, lcnt, elog, elog64);
+        else
+            sw::k_bloch_groups<false, false><<<gb, 256, 0, st>>>(P, GT, GS, lcnt, elog, elog64);
         TR_CUDA(cudaGetLastError());
         TR_CUDA(cudaMemcpyAsync(&h, L.active, 4, cudaMemcpyDeviceToHost, st));
         TR_CUDA(cudaStreamSynchronize(st));
@@ -637,6 +829,9 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
         if (nte) {
             TR_CUDA(cudaMemcpyAsync(tracks[t].M1, d + o_M1[t], n * nte * 12, cudaMemcpyDeviceToHost, st));
             TR_CUDA(cudaMemcpyAsync(tracks[t].T, d + o_T[t], n * nte, cudaMemcpyDeviceToHost, st));
+            if (tracks[t].M1_fp64)
+                TR_CUDA(cudaMemcpyAsync(tracks[t].M1_fp64, d + o_M1d[t], n * nte * 24,
+                                        cudaMemcpyDeviceToHost, st));
         }
         TR_CUDA(cudaMemcpyAsync(tracks[t].XYZ1, d + o_X[t], n * 12, cudaMemcpyDeviceToHost, st));
         if (tracks[t].status)

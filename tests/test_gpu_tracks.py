@@ -67,3 +67,46 @@ def test_tracks_reject_duplicates():
     pr, _ = load_golden("gre")
     with pytest.raises(_lib.SpinWalkError):
         _lib.run_tracks(pr, [dict(n_dummy_scan=0), dict(n_dummy_scan=0)])
+
+
+@pytest.mark.parametrize("case", ["bssfp_phase_cycling", "se_multi_te", "pgse_gradients",
+                                  "ste_dephasing"])
+@pytest.mark.parametrize("precision", ["kahan", "fp32_shadow", "fp64"])
+def test_tracks_precision_modes_equal_independent_runs(case, precision):
+    """Compensated phase sums, the FP64 shadow and FP64 output of the tracks path are those of
+    sw_sim on each instance alone, bit for bit (the steady-state recurrence carried in double)."""
+    from spinwalk_gb300 import abi
+    prec = {"kahan": abi.SW_PREC_KAHAN, "fp32_shadow": abi.SW_PREC_FP32,
+            "fp64": abi.SW_PREC_FP64}[precision]
+    shadow = precision != "kahan"
+    pr, _ = load_golden(case)
+    tracks = [dict(linear_phase_cycling=lpc, n_dummy_scan=nd)
+              for lpc in (0.0, 90.0, 200.0) for nd in (0, 3)]
+    outs = _lib.run_tracks(pr, tracks, fill=np.nan, precision=prec, fp64=shadow)
+    for t, got in zip(tracks, outs):
+        want = _lib.run(_instance(pr, t), precision=prec, fp64_shadow=shadow, fill=np.nan)
+        assert bits_equal(got["M1"], want["M1"]), (case, precision, t)
+        assert bits_equal(got["T"], want["T"]), (case, precision, t)
+        assert bits_equal(got["XYZ1"], want["XYZ1"]), (case, precision, t)
+        if shadow:
+            assert bits_equal(got["M1_fp64"], want["M1_fp64"]), (case, precision, t)
+
+
+def test_tracks_shadow_leaves_fp32_results_unchanged():
+    pr, _ = load_golden("bssfp_phase_cycling")
+    tracks = [dict(linear_phase_cycling=lpc, n_dummy_scan=nd) for lpc in (0.0, 120.0) for nd in (1, 4)]
+    plain = _lib.run_tracks(pr, tracks, fill=np.nan)
+    shadowed = _lib.run_tracks(pr, tracks, fill=np.nan, fp64=True)
+    for a, b in zip(plain, shadowed):
+        assert bits_equal(a["M1"], b["M1"])
+        assert bits_equal(a["XYZ1"], b["XYZ1"])
+        # FP32 against its FP64 shadow: the stated per-spin error bound of the float path
+        err = np.nanmax(np.abs(b["M1"].astype(np.float64) - b["M1_fp64"]))
+        assert err < 1e-4, err
+
+
+def test_tracks_reject_generator_flavour_bits():
+    from spinwalk_gb300 import abi
+    pr, _ = load_golden("gre")
+    with pytest.raises(_lib.SpinWalkError):
+        _lib.run_tracks(pr, [dict(n_dummy_scan=0)], precision=abi.SW_PREC_FP32 | abi.SW_RNG_MINSTD)

@@ -82,6 +82,16 @@ def workload(name, rank=0):
                     phantom="300^3 cylinders r5um 3%", n_spins=n_spins, time_points=200,
                     sequence="bSSFP FA 30, TR 5 ms, TE 2.5 ms, dt 25 us, 64 phase cycles "
                              "(5.625 deg steps) x DUMMY_SCAN 200..209")
+    elif name in ("dense", "dense_small"):   # many spins per voxel: the Morton re-sort's case
+        n, fov = 100, 100e-6
+        mask, field = _lib.phantom_cylinders(n, fov, 5e-6, 0.03, seed=1)
+        n_spins = 2_000_000 if name == "dense" else 500_000
+        kw = dict(TR_us=40050, TE_us=(40000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
+                  RF_us=(0, 20000), timestep_us=50)
+        desc = dict(workload=f"{name}_se_cylinders_100cubed_{n_spins:.0e}spins_801tp".replace("+0", ""),
+                    phantom="100^3 cylinders r5um 3% (the serving trace's smallest phantom)",
+                    n_spins=n_spins, spins_per_voxel=n_spins / n ** 3, time_points=801,
+                    sequence="SE 90/180, TE 40 ms, dt 50 us", permeability=0.0)
     elif name == "small":      # profiling case: > L2 phantom, few GB on the device
         n, fov = 300, 300e-6
         mask, field = _lib.phantom_spheres(n, fov, 2e-6, 8e-6, 0.05, seed=2)
@@ -242,12 +252,31 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def apply_tuning(args, pr=None):
+    """Walk tuning for the run: --autotune measures every candidate on `pr` (sw_autotune) and
+    installs the fastest; --resort-interval / --walk-block set it directly. Returns what was
+    applied (and the measured table)."""
+    from spinwalk_gb300 import _lib
+    info = {}
+    if args.autotune and pr is not None:
+        t0 = time.perf_counter()
+        best, table = _lib.autotune(pr, apply=True)
+        info = {"autotuned": True, "probe_s": time.perf_counter() - t0, "table": table}
+    elif args.resort_interval is not None or args.walk_block is not None:
+        cur = _lib.get_tuning()
+        _lib.set_tuning(cur["resort_interval"] if args.resort_interval is None else args.resort_interval,
+                        cur["walk_block"] if args.walk_block is None else args.walk_block)
+    info["applied"] = _lib.get_tuning()
+    return info
+
+
 def run_ours(args, world, rank, local):
     import torch
     from spinwalk_gb300 import _lib
 
     torch.cuda.set_device(local)
     pr, desc = workload(args.workload, rank)
+    tuning = apply_tuning(args, pr)
     p = pr.params
     n, nte = p.n_spins, pr.n_te
     dev = torch.device("cuda", local)
@@ -353,6 +382,7 @@ def run_ours(args, world, rank, local):
         "e2e": {"value": e2e, "unit": "spin-steps/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
+        "tuning": tuning,
         "error_vs_fp64": errors,
         "clocks": clocks,
         "status_counts": {str(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))},
@@ -480,6 +510,7 @@ def run_batch_scales(args, world, rank):
     import torch  # noqa: F401
     from spinwalk_gb300 import _lib
     probs, desc = c3_instances(rank)
+    tuning = apply_tuning(args, max(probs, key=lambda q: q.params.n_spins))
     steps = sum(p.spin_steps() for p in probs)
     for _ in range(args.warmup):
         _lib.run_batch(probs)
@@ -510,7 +541,7 @@ def run_batch_scales(args, world, rank):
             "batched_over_plain_e2e": float(np.mean(wall)) and (steps / float(np.mean(wall))) / (steps / plain_wall),
             "e2e": {"value": world * steps / float(np.mean(wall)), "unit": "spin-steps/s",
                     "note": "sw_sim_batch with host buffers"},
-            "clocks": clocks}
+            "tuning": tuning, "clocks": clocks}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -575,6 +606,7 @@ def run_serve(args, world, rank):
     from spinwalk_gb300 import _lib
     n_req = args.requests
     reqs, phantoms, arrivals, desc = serve_requests(n_req, rank=rank)
+    tuning = apply_tuning(args, max(reqs, key=lambda q: q.params.n_spins))
     eng = _lib.Engine(n_slots=8, slot_spins=1 << 20)
     pids = {}
     t0 = time.perf_counter()
@@ -615,7 +647,7 @@ def run_serve(args, world, rank):
             "startup_s": startup_s,
             "e2e": {"value": value, "unit": "spin-steps/s",
                     "note": "host buffers in and out through the engine, arrivals in real time"},
-            "clocks": clocks}
+            "tuning": tuning, "clocks": clocks}
     eng.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -656,6 +688,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--requests", type=int, default=100, help="serve workload: trace length")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick the walk tuning by sw_autotune on the workload before timing")
+    ap.add_argument("--resort-interval", type=int, default=None,
+                    help="walk rounds between Morton re-sorts of the spins (0 = never)")
+    ap.add_argument("--walk-block", type=int, default=None, help="walk kernel block size")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

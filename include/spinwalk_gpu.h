@@ -292,6 +292,46 @@ typedef struct sw_timing {
 } sw_timing;
 int sw_last_timing(sw_timing *out);
 
+/*
+ * Walk tuning, process-wide: read at the start of every later call (sw_sim, sw_sim_device,
+ * sw_sim_batch, sw_sim_spins, sw_sim_signal, engine chunks). Results never depend on it: it only
+ * changes which thread walks which spin and the walk kernel's block size. No counterpart in the
+ * reference (one thread per spin in id order, src/sim/kernels.cu:70-90).
+ *   resort_interval : refill/walk rounds (256 steps each) between Morton re-sorts of the spins
+ *                     by their current voxel; 0 = never (id order)
+ *   walk_block      : threads per block of the walk kernel: 64, 128 or 256
+ */
+typedef struct sw_tuning {
+    uint32_t resort_interval;
+    uint32_t walk_block;
+    uint32_t reserved[6];
+} sw_tuning;
+int sw_set_tuning(const sw_tuning *t);
+int sw_get_tuning(sw_tuning *t);
+
+/* One measured candidate of sw_autotune: device time of the walk per 256-step round, the
+ * re-sorts' share included (model: (sort + sum of the rounds at age 0..I-1 after a sort) / I). */
+typedef struct sw_tune_entry {
+    uint32_t resort_interval;
+    uint32_t walk_block;
+    float ms_per_round;
+    float sort_ms;            /* one re-sort (0 for resort_interval 0) */
+} sw_tune_entry;
+
+/*
+ * Picks the fastest sw_tuning for the walk of this problem by a probe on the current device: the
+ * problem's phantom, spin count, start positions and tissue, walked for up to 20 rounds (time
+ * points extended, no dummy scans, generators of the SW_RNG_MINSTD flavour because their seeding
+ * costs O(log) per spin and the walk is the same), timing every round with CUDA events. Candidates:
+ * resort_interval in {0, 1, 2, 4, 8} x walk_block in {128, 256}. `best` receives the fastest;
+ * `table` (optional, table_len entries) the measured candidates, *n_entries their number;
+ * apply != 0 installs `best` with sw_set_tuning. The probe allocates its own device memory
+ * (about as much as sw_sim on the problem) and frees it before returning.
+ */
+int sw_autotune(const sw_params *param, const sw_sequence *seq, const float *pFieldMap,
+                const uint8_t *pMask, const float *XYZ0, int apply, sw_tuning *best,
+                sw_tune_entry *table, uint32_t table_len, uint32_t *n_entries);
+
 /* One instance of a batch: its parameters, sequence and host buffers, as for sw_sim. */
 typedef struct sw_instance {
     const sw_params *param;

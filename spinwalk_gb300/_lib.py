@@ -85,6 +85,11 @@ def lib():
                                  C.c_void_p, C.c_uint64]
         L.sw_sync.argtypes = [C.c_void_p]
         L.sw_last_timing.argtypes = [P(abi.SwTiming)]
+        L.sw_set_tuning.argtypes = [P(abi.SwTuning)]
+        L.sw_get_tuning.argtypes = [P(abi.SwTuning)]
+        L.sw_autotune.argtypes = [P(abi.SwParams), P(abi.SwSequence), C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_int, P(abi.SwTuning), P(abi.SwTuneEntry),
+                                  C.c_uint32, P(C.c_uint32)]
         L.sw_debug_logf.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
         L.sw_debug_ms_normal.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
         L.sw_debug_dadd.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
@@ -185,6 +190,34 @@ def h5_read(path, name):
 def run_config(ini_path, device=0):
     """sw_run_config: the whole `spinwalk sim -c ini` run (HDF5 in, HDF5 out)."""
     check(lib().sw_run_config(str(ini_path).encode(), int(device)))
+
+
+def set_tuning(resort_interval=0, walk_block=256):
+    """sw_set_tuning: Morton re-sort interval (walk rounds, 0 = never) and walk block size for
+    every later call of this process. Results do not depend on it."""
+    t = abi.SwTuning(resort_interval=int(resort_interval), walk_block=int(walk_block))
+    check(lib().sw_set_tuning(C.byref(t)))
+
+
+def get_tuning():
+    t = abi.SwTuning()
+    check(lib().sw_get_tuning(C.byref(t)))
+    return dict(resort_interval=t.resort_interval, walk_block=t.walk_block)
+
+
+def autotune(problem, apply=False):
+    """sw_autotune on `problem` (a problem.Problem): returns (best, table), best a dict as
+    get_tuning(), table the measured candidates (resort_interval, walk_block, ms_per_round,
+    sort_ms)."""
+    best = abi.SwTuning()
+    tab = (abi.SwTuneEntry * 32)()
+    n = C.c_uint32(0)
+    check(lib().sw_autotune(C.byref(problem.params), C.byref(problem.seq.struct),
+                            _p(problem.field), _p(problem.mask), _p(problem.XYZ0), int(bool(apply)),
+                            C.byref(best), tab, 32, C.byref(n)))
+    table = [dict(resort_interval=e.resort_interval, walk_block=e.walk_block,
+                  ms_per_round=e.ms_per_round, sort_ms=e.sort_ms) for e in tab[:n.value]]
+    return dict(resort_interval=best.resort_interval, walk_block=best.walk_block), table
 
 
 def last_timing():

@@ -112,6 +112,23 @@ class SwJobResult(C.Structure):
                 ("latency_s", C.c_double)]
 
 
+class SwTuning(C.Structure):
+    _fields_ = [
+        ("resort_interval", C.c_uint32),
+        ("walk_block", C.c_uint32),
+        ("reserved", C.c_uint32 * 6),
+    ]
+
+
+class SwTuneEntry(C.Structure):
+    _fields_ = [
+        ("resort_interval", C.c_uint32),
+        ("walk_block", C.c_uint32),
+        ("ms_per_round", C.c_float),
+        ("sort_ms", C.c_float),
+    ]
+
+
 class SwTiming(C.Structure):
     _fields_ = [
         ("seed_ms", C.c_float),

@@ -198,6 +198,9 @@ Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl, bo
     G.ubuf = c.take<float>(n * sw::kUnifBuf);
     G.uhead = c.take<uint32_t>(n);
     G.ucnt = c.take<uint32_t>(n);
+    L.Q.order = c.take<uint32_t>(n);
+    L.Q.key = c.take<uint32_t>(n);
+    L.Q.hist = c.take<uint32_t>(sw::order_hist_words());
     L.bytes = c.off + 256;
     return L;
 }
@@ -258,6 +261,7 @@ int walk_rounds(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
     // Upper bound on rounds: every round advances each unfinished spin by >= 1 attempt.
     const uint64_t steps = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
     const uint64_t max_rounds = 64 + steps * (p->max_iterations + 2);
+    const sw_tuning tu = current_tuning();
     uint32_t chunk = 0;
     for (;; chunk++) {
         if (chunk >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
@@ -266,7 +270,13 @@ int walk_rounds(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
         if (timed) SW_CUDA(cudaEventRecord(ev[4 + 2 * chunk], st));
         SW_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
         if (timed) SW_CUDA(cudaEventRecord(ev[5 + 2 * chunk], st));
-        SW_CUDA(sw::launch_walk(precision, dbl, P, Tb, L.vox, L.S, L.G, O, L.active, st));
+        if (tu.resort_interval && chunk % tu.resort_interval == 0) {
+            SW_CUDA(sw::launch_order(P, L.S, L.Q, 0, P.n_spins, st));
+            launches += 3;
+        }
+        SW_CUDA(sw::launch_walk_range(precision, dbl, P, Tb, L.vox, L.S, L.G, O, L.active, 0,
+                                      P.n_spins, st, tu.resort_interval ? L.Q.order : nullptr,
+                                      (int)tu.walk_block));
         launches += 2;
         SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         if (timed) SW_CUDA(cudaEventRecord(ev[2], st));
@@ -374,7 +384,33 @@ sw::LogfTables sw::api::device_logf_tables() {
     return logf_tables(*ctx);
 }
 
+namespace {
+std::mutex g_tune_mu;
+sw_tuning g_tune{0u, 256u, {0u, 0u, 0u, 0u, 0u, 0u}};
+}  // namespace
+
+sw_tuning sw::api::current_tuning() {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    return g_tune;
+}
+
 extern "C" {
+
+int sw_set_tuning(const sw_tuning *t) {
+    if (!t) return fail(SW_ERR_INVALID, "null tuning");
+    if (t->walk_block != 64 && t->walk_block != 128 && t->walk_block != 256)
+        return fail(SW_ERR_INVALID, "walk_block must be 64, 128 or 256");
+    if (t->resort_interval > 1u << 20) return fail(SW_ERR_INVALID, "resort_interval too large");
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune = *t;
+    return SW_OK;
+}
+
+int sw_get_tuning(sw_tuning *t) {
+    if (!t) return fail(SW_ERR_INVALID, "null tuning");
+    *t = current_tuning();
+    return SW_OK;
+}
 
 int sw_abi_version(void) { return SW_ABI_VERSION; }
 

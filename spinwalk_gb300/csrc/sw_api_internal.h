@@ -56,8 +56,12 @@ struct Layout {
     uint32_t *active;
     SpinState S;
     RngState G;
+    OrderState Q;             // walk order (Morton re-sort)
     size_t bytes;
 };
+
+// Process-wide tuning of the walk (sw_set_tuning / sw_autotune), read at the start of a call.
+sw_tuning current_tuning();
 
 // Kernel timing of the last call on this thread (sw_last_timing).
 extern thread_local sw_timing g_timing;

@@ -118,6 +118,7 @@ struct Job {
     int rc = SW_OK;
     double t_submit = 0, t_done = 0;
     SeedCache *seed = nullptr;
+    sw_tuning tuning{};                 // walk tuning at submission (sw_set_tuning)
     // signal mode: per-(echo, substrate) sums instead of per-spin M1 / T / XYZ1
     double *h_sig = nullptr, *d_sig = nullptr;
     uint64_t *h_cnt = nullptr;
@@ -246,6 +247,7 @@ int ensure_seeded(sw_engine *E, uint64_t seed, uint32_t lo, uint32_t hi, SeedCac
 struct ChunkView {
     sw::SpinState S;
     sw::RngState G;
+    sw::OrderState Q;
     sw::Outputs O;
     const float *M0, *XYZ0;
 };
@@ -270,6 +272,9 @@ ChunkView view(const Slot &s) {
     G.p_r = shift(G.p_r, lo); G.p_u = shift(G.p_u, lo);
     G.nbuf = shift(G.nbuf, lo * sw::kNormBuf); G.nhead = shift(G.nhead, lo); G.ncnt = shift(G.ncnt, lo);
     G.ubuf = shift(G.ubuf, lo * sw::kUnifBuf); G.uhead = shift(G.uhead, lo); G.ucnt = shift(G.ucnt, lo);
+    v.Q = s.L.Q;
+    v.Q.order = shift(v.Q.order, lo);
+    v.Q.key = shift(v.Q.key, lo);
     char *d = s.d_io;
     v.O.M1d = nullptr;
     v.O.status = shift(reinterpret_cast<int32_t *>(d + s.o_st), lo);
@@ -353,11 +358,17 @@ int issue_rounds(sw_engine *E, Slot &s, uint64_t k, bool first) {
     const bool dbl = j.precision == SW_PREC_FP64;
     if (first)
         EN_CUDA(sw::launch_init_range(j.P, Tb, ph.vox, v.M0, v.XYZ0, v.S, v.O, dbl, s.lo, s.hi, s.st));
+    const uint32_t ri = j.tuning.resort_interval;
     for (uint64_t r = 0; r < k; r++) {
         if (r + 1 == k) EN_CUDA(cudaMemsetAsync(s.L.active, 0, sizeof(uint32_t), s.st));
         EN_CUDA(sw::launch_refill_range(j.P, v.G, v.S.flags, E->LT, s.lo, s.hi, s.st));
+        if (ri && (s.rounds + r) % ri == 0) {
+            EN_CUDA(sw::launch_order(j.P, v.S, v.Q, s.lo, s.hi, s.st));
+            E->launches += 3;
+        }
         EN_CUDA(sw::launch_walk_range(j.precision, dbl, j.P, Tb, ph.vox, v.S, v.G, v.O,
-                                      s.L.active, s.lo, s.hi, s.st));
+                                      s.L.active, s.lo, s.hi, s.st, ri ? v.Q.order : nullptr,
+                                      (int)j.tuning.walk_block));
     }
     s.rounds += k;
     E->rounds += k;
@@ -494,6 +505,7 @@ int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_se
     j->id = E->next_job++;
     j->phantom = phantom;
     j->precision = precision;
+    j->tuning = current_tuning();
     j->p = *p;
     j->p.fieldmap_exist = p->fieldmap_exist && ph.field;
     const uint32_t ns = p->n_substrate;

@@ -658,10 +658,12 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
 template <int PREC, bool DBL>
 __global__ void __launch_bounds__(256)
     k_walk(DevParams P, DevTables Tb, const uint2 *__restrict__ vox, SpinState S, RngState G,
-           Outputs O, uint32_t *active, uint32_t spin_lo, uint32_t spin_hi) {
-    const uint32_t spin = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
+           Outputs O, uint32_t *active, uint32_t spin_lo, uint32_t spin_hi,
+           const uint32_t *__restrict__ order) {
+    const uint32_t i = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
     bool still = false;
-    if (spin < spin_hi) {
+    if (i < spin_hi) {
+        const uint32_t spin = order ? __ldg(order + i) : i;
         const uint32_t flags = S.flags[spin];
         if (!(flags & kFlagDone)) still = walk_spin<PREC, DBL>(spin, flags, P, Tb, vox, S, G, O);
     }
@@ -759,19 +761,20 @@ cudaError_t launch_walk(int prec, bool dbl, const DevParams &P, const DevTables 
 cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
                               const uint2 *vox, const SpinState &S, const RngState &G,
                               const Outputs &O, uint32_t *active, uint32_t lo, uint32_t hi,
-                              cudaStream_t st) {
+                              cudaStream_t st, const uint32_t *order, int block) {
     if (hi <= lo) return cudaSuccess;
-    const int g = grid_for(hi - lo, 256, 1 << 30);
+    if (block != 64 && block != 128 && block != 256) return cudaErrorInvalidValue;
+    const int g = grid_for(hi - lo, block, 1 << 30);
     if (prec == SW_PREC_FP64)
-        k_walk<SW_PREC_FP64, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
+        k_walk<SW_PREC_FP64, true><<<g, block, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi, order);
     else if (prec == SW_PREC_KAHAN && dbl)
-        k_walk<SW_PREC_KAHAN, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
+        k_walk<SW_PREC_KAHAN, true><<<g, block, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi, order);
     else if (prec == SW_PREC_KAHAN)
-        k_walk<SW_PREC_KAHAN, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
+        k_walk<SW_PREC_KAHAN, false><<<g, block, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi, order);
     else if (dbl)
-        k_walk<SW_PREC_FP32, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
+        k_walk<SW_PREC_FP32, true><<<g, block, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi, order);
     else
-        k_walk<SW_PREC_FP32, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi);
+        k_walk<SW_PREC_FP32, false><<<g, block, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi, order);
     return cudaGetLastError();
 }
 

@@ -13,10 +13,16 @@ cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo
                               cudaStream_t st);
 cudaError_t launch_refill_range(const DevParams &P, const RngState &G, const uint32_t *flags,
                                 const LogfTables &L, uint32_t lo, uint32_t hi, cudaStream_t st);
+// order: walk order of the spins (null = id order); block: threads per block (64..256).
 cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
                               const uint2 *vox, const SpinState &S, const RngState &G,
                               const Outputs &O, uint32_t *active, uint32_t lo, uint32_t hi,
-                              cudaStream_t st);
+                              cudaStream_t st, const uint32_t *order = nullptr, int block = 256);
+// Morton re-sort of spins [lo, hi) into Q.order (sw_order.cu).
+cudaError_t launch_order(const DevParams &P, const SpinState &S, const OrderState &Q,
+                         uint32_t lo, uint32_t hi, cudaStream_t st);
+OrderShape order_shape(const DevParams &P, uint32_t n_spins);
+size_t order_hist_words();
 cudaError_t launch_init(const DevParams &P, const DevTables &Tb, const uint2 *vox,
                         const float *M0, const float *XYZ0, const SpinState &S,
                         const Outputs &O, bool fp64_state, cudaStream_t st);

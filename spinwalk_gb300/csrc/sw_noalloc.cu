@@ -131,11 +131,16 @@ extern "C" int sw_sim_device_noalloc(const sw_params *p, const sw_sequence *q,
     if (h != 0) return fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate");
     const uint64_t steps = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
     const uint64_t max_rounds = 64 + steps * (p->max_iterations + 2);
+    const sw_tuning tu = current_tuning();
     for (uint64_t round = 0;; round++) {
         if (round >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
         NA_CUDA(cudaMemsetAsync(L.active, 0, sizeof(uint32_t), st));
         NA_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
-        NA_CUDA(sw::launch_walk(SW_PREC_FP32, false, P, Tb, L.vox, L.S, L.G, O, L.active, st));
+        if (tu.resort_interval && round % tu.resort_interval == 0)
+            NA_CUDA(sw::launch_order(P, L.S, L.Q, 0, P.n_spins, st));
+        NA_CUDA(sw::launch_walk_range(SW_PREC_FP32, false, P, Tb, L.vox, L.S, L.G, O, L.active, 0,
+                                      P.n_spins, st, tu.resort_interval ? L.Q.order : nullptr,
+                                      (int)tu.walk_block));
         NA_CUDA(cudaMemcpyAsync(&h, L.active, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         NA_CUDA(cudaStreamSynchronize(st));
         if (h == 0) break;

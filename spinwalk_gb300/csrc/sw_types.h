@@ -112,4 +112,19 @@ struct Outputs {
     unsigned long long *cnt = nullptr;
 };
 
+// Walk order of the spins (Morton re-sort, sw_order.cu). order and key are indexed by global
+// spin id like SpinState; hist has order_hist_words() counters.
+constexpr int kOrderMaxBitsPerAxis = 6;
+struct OrderState {
+    uint32_t *order;          // [n]: thread lo+i walks spin order[lo+i]
+    uint32_t *key;            // [n]
+    uint32_t *hist;           // bucket counters, then offsets
+};
+struct OrderShape {
+    int bits;                 // Morton bits per axis
+    int shift[3];             // voxel coordinate >> shift = cell coordinate
+    int64_t n[3];             // phantom size per axis
+    uint32_t n_buckets;       // 2^(3 bits) cells + 1 bucket of finished spins
+};
+
 }  // namespace sw

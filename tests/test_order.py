@@ -1,0 +1,98 @@
+"""Walk tuning: Morton re-sort of the spins (sw_order.cu), walk block size, sw_autotune. The tuning
+only changes which thread walks which spin, so every result must equal the id-order run bit for
+bit, through every entry point that walks."""
+import numpy as np
+import pytest
+
+from spinwalk_gb300 import _lib
+from spinwalk_gb300.problem import Problem, cylinder_phantom
+from tests.helpers import bits_equal, load_golden
+
+
+@pytest.fixture
+def tuning():
+    """Restores the default tuning after the test (the setting is process-wide)."""
+    yield _lib.set_tuning
+    _lib.set_tuning(0, 256)
+
+
+def test_tuning_roundtrip_and_validation(tuning):
+    tuning(3, 128)
+    assert _lib.get_tuning() == dict(resort_interval=3, walk_block=128)
+    for bad in (dict(resort_interval=1, walk_block=100), dict(resort_interval=1, walk_block=512),
+                dict(resort_interval=1 << 21, walk_block=256)):
+        with pytest.raises(_lib.SpinWalkError):
+            _lib.set_tuning(**bad)
+    assert _lib.get_tuning() == dict(resort_interval=3, walk_block=128)
+
+
+def _dense_problem(n_spins=20000, TE_us=(3000, 9000), **kw):
+    """Many spins per voxel (20000 spins in 16^3 voxels): sorted warps share voxels."""
+    mask, field = cylinder_phantom(16, 32e-6, 3e-6, 0.2, seed=4)
+    return Problem(mask, [32e-6] * 3, field, n_spins=n_spins, seed=7, TR_us=12050, TE_us=TE_us,
+                   timestep_us=20, pXY=[[1, 0.4], [0.3, 1]], **kw)
+
+
+def _same(a, b, keys=("M1", "XYZ1", "T", "status")):
+    for k in keys:
+        assert bits_equal(a[k], b[k]), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["permeable", "se_multi_te", "lost_spins", "pgse_gradients",
+                                  "out_of_bounds_reflect", "trajectory"])
+@pytest.mark.parametrize("interval,block", [(1, 256), (3, 128), (2, 64)])
+def test_sim_results_independent_of_walk_order(tuning, case, interval, block):
+    pr, _ = load_golden(case)
+    want = _lib.run(pr, fill=np.nan)
+    tuning(interval, block)
+    got = _lib.run(pr, fill=np.nan)
+    _same(got, want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_dense_sim_all_precisions_independent_of_walk_order(tuning, precision):
+    pr = _dense_problem()
+    want = _lib.run(pr, precision=precision, fp64_shadow=True, fill=np.nan)
+    tuning(1, 256)
+    got = _lib.run(pr, precision=precision, fp64_shadow=True, fill=np.nan)
+    _same(got, want, ("M1", "XYZ1", "T", "status", "M1_fp64"))
+    assert got["timing"]["n_launches"] > want["timing"]["n_launches"]    # the sorts ran
+
+
+@pytest.mark.gpu
+def test_batch_and_engine_independent_of_walk_order(tuning):
+    probs = [_dense_problem(n) for n in (20000, 5000, 777)]
+    want = [_lib.run(p, fill=np.nan) for p in probs]
+    tuning(1, 128)
+    got = _lib.run_batch(probs, fill=np.nan)
+    for g, w in zip(got, want):
+        _same(g, w)
+
+
+@pytest.mark.gpu
+def test_signal_mode_independent_of_walk_order(tuning):
+    pr = _dense_problem()
+    sig0, cnt0, st0 = _lib.run_signal(pr)
+    tuning(1, 256)
+    sig1, cnt1, st1 = _lib.run_signal(pr)
+    assert np.array_equal(cnt1, cnt0)
+    assert np.array_equal(st1, st0)
+    # double sums of the same float terms in another order
+    np.testing.assert_allclose(sig1, sig0, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_autotune_measures_every_candidate_and_applies(tuning):
+    pr = _dense_problem(n_spins=50000)
+    want = _lib.run(pr, fill=np.nan)
+    best, table = _lib.autotune(pr, apply=True)
+    assert len(table) == 10
+    assert {(e["resort_interval"], e["walk_block"]) for e in table} == {
+        (i, b) for i in (0, 1, 2, 4, 8) for b in (128, 256)}
+    assert all(e["ms_per_round"] > 0 for e in table)
+    fastest = min(table, key=lambda e: e["ms_per_round"])
+    assert best == dict(resort_interval=fastest["resort_interval"], walk_block=fastest["walk_block"])
+    assert _lib.get_tuning() == best
+    _same(_lib.run(pr, fill=np.nan), want)

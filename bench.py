@@ -262,10 +262,12 @@ def apply_tuning(args, pr=None):
         t0 = time.perf_counter()
         best, table = _lib.autotune(pr, apply=True)
         info = {"autotuned": True, "probe_s": time.perf_counter() - t0, "table": table}
-    elif args.resort_interval is not None or args.walk_block is not None:
+    if args.resort_interval is not None or args.walk_block is not None or \
+            args.seed_chunks is not None:
         cur = _lib.get_tuning()
         _lib.set_tuning(cur["resort_interval"] if args.resort_interval is None else args.resort_interval,
-                        cur["walk_block"] if args.walk_block is None else args.walk_block)
+                        cur["walk_block"] if args.walk_block is None else args.walk_block,
+                        cur["seed_chunks"] if args.seed_chunks is None else args.seed_chunks)
     info["applied"] = _lib.get_tuning()
     return info
 
@@ -693,6 +695,8 @@ def main():
     ap.add_argument("--resort-interval", type=int, default=None,
                     help="walk rounds between Morton re-sorts of the spins (0 = never)")
     ap.add_argument("--walk-block", type=int, default=None, help="walk kernel block size")
+    ap.add_argument("--seed-chunks", type=int, default=None,
+                    help="seed/walk pipeline chunks (1 = seed all first, 0 = auto)")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

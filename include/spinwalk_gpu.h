@@ -300,11 +300,17 @@ int sw_last_timing(sw_timing *out);
  *   resort_interval : refill/walk rounds (256 steps each) between Morton re-sorts of the spins
  *                     by their current voxel; 0 = never (id order)
  *   walk_block      : threads per block of the walk kernel: 64, 128 or 256
+ *   seed_chunks     : sw_sim / sw_sim_device seed the spins in this many chunks of equal seeding
+ *                     cost on a low-priority stream and walk each seeded chunk on a
+ *                     high-priority stream meanwhile (0 or 1 = seed everything, then walk;
+ *                     at most 64). Off by default: the co-resident kernels slow each other down
+ *                     by about what the overlap saves.
  */
 typedef struct sw_tuning {
     uint32_t resort_interval;
     uint32_t walk_block;
-    uint32_t reserved[6];
+    uint32_t seed_chunks;
+    uint32_t reserved[5];
 } sw_tuning;
 int sw_set_tuning(const sw_tuning *t);
 int sw_get_tuning(sw_tuning *t);

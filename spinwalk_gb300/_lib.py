@@ -192,17 +192,20 @@ def run_config(ini_path, device=0):
     check(lib().sw_run_config(str(ini_path).encode(), int(device)))
 
 
-def set_tuning(resort_interval=0, walk_block=256):
-    """sw_set_tuning: Morton re-sort interval (walk rounds, 0 = never) and walk block size for
-    every later call of this process. Results do not depend on it."""
-    t = abi.SwTuning(resort_interval=int(resort_interval), walk_block=int(walk_block))
+def set_tuning(resort_interval=0, walk_block=256, seed_chunks=0):
+    """sw_set_tuning: Morton re-sort interval (walk rounds, 0 = never), walk block size and seed
+    chunks of the seed/walk pipeline (0 = auto) for every later call of this process. Results do
+    not depend on it."""
+    t = abi.SwTuning(resort_interval=int(resort_interval), walk_block=int(walk_block),
+                     seed_chunks=int(seed_chunks))
     check(lib().sw_set_tuning(C.byref(t)))
 
 
 def get_tuning():
     t = abi.SwTuning()
     check(lib().sw_get_tuning(C.byref(t)))
-    return dict(resort_interval=t.resort_interval, walk_block=t.walk_block)
+    return dict(resort_interval=t.resort_interval, walk_block=t.walk_block,
+                seed_chunks=t.seed_chunks)
 
 
 def autotune(problem, apply=False):
@@ -217,7 +220,8 @@ def autotune(problem, apply=False):
                             C.byref(best), tab, 32, C.byref(n)))
     table = [dict(resort_interval=e.resort_interval, walk_block=e.walk_block,
                   ms_per_round=e.ms_per_round, sort_ms=e.sort_ms) for e in tab[:n.value]]
-    return dict(resort_interval=best.resort_interval, walk_block=best.walk_block), table
+    return dict(resort_interval=best.resort_interval, walk_block=best.walk_block,
+                seed_chunks=best.seed_chunks), table
 
 
 def last_timing():

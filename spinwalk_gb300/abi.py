@@ -116,7 +116,8 @@ class SwTuning(C.Structure):
     _fields_ = [
         ("resort_interval", C.c_uint32),
         ("walk_block", C.c_uint32),
-        ("reserved", C.c_uint32 * 6),
+        ("seed_chunks", C.c_uint32),
+        ("reserved", C.c_uint32 * 5),
     ]
 
 

@@ -214,6 +214,7 @@ namespace {
 
 constexpr int kMaxDevices = 64;
 constexpr int kMaxTimedChunks = 4096;
+constexpr uint32_t kMaxSeedChunks = 64;
 
 struct DeviceCtx {
     std::mutex mu;
@@ -223,7 +224,10 @@ struct DeviceCtx {
     char *ws = nullptr;
     size_t ws_size = 0;
     uint32_t *h_active = nullptr;          // pinned
-    std::vector<cudaEvent_t> ev;           // timing events
+    std::vector<cudaEvent_t> ev;           // timing events: 4 call-level, then 3 per round
+    cudaStream_t seed_st = nullptr;        // lowest priority: seeding of the chunks
+    cudaStream_t walk_st = nullptr;        // highest priority: pack, init, refill, walk
+    std::vector<cudaEvent_t> pev;          // pipeline: start, done, seed chunk c done / timed
 };
 DeviceCtx g_ctx[kMaxDevices];
 
@@ -241,8 +245,14 @@ int ensure_logf(DeviceCtx &c) {
     SW_CUDA(cudaMemcpy(c.d_logf_bitmap, ex.bitmap.data(), ex.bitmap.size() * sizeof(uint32_t),
                        cudaMemcpyHostToDevice));
     SW_CUDA(cudaMallocHost(&c.h_active, sizeof(uint32_t)));
-    c.ev.resize(2 * kMaxTimedChunks + 4);
+    c.ev.resize(3 * kMaxTimedChunks + 4);
     for (auto &e : c.ev) SW_CUDA(cudaEventCreate(&e));
+    int lo_prio = 0, hi_prio = 0;
+    SW_CUDA(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+    SW_CUDA(cudaStreamCreateWithPriority(&c.seed_st, cudaStreamNonBlocking, lo_prio));
+    SW_CUDA(cudaStreamCreateWithPriority(&c.walk_st, cudaStreamNonBlocking, hi_prio));
+    c.pev.resize(2 + 2 * kMaxSeedChunks);
+    for (auto &e : c.pev) SW_CUDA(cudaEventCreate(&e));
     c.logf_ready = true;
     return SW_OK;
 }
@@ -251,46 +261,105 @@ sw::LogfTables logf_tables(const DeviceCtx &c) {
     return sw::LogfTables{c.d_logf_tab, c.d_logf_bitmap};
 }
 
-// Refill + walk rounds until every spin of the layout has finished (the reference's per-spin
-// loop over time points, kernels.cu:107-232, cut into rounds at which the generator rings are
-// topped up). Adds the kernel times and the number of rounds to g_timing.
-int walk_rounds(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
-                const sw::DevParams &P, const sw::DevTables &Tb, const sw::LogfTables &LT,
-                const Layout &L, const sw::Outputs &O, cudaStream_t st, uint32_t &launches) {
+// Boundaries of `C` spin chunks of equal seeding cost: spin s costs its seeding, discard(seed+s)
+// words plus about one block (624 words) of seeding and first twist.
+std::vector<uint32_t> seed_chunks(const sw::DevParams &P, uint32_t C) {
+    const double n = P.n_spins, a = (double)P.seed + 624.0;
+    auto F = [&](double x) { return x * a + 0.5 * x * (x - 1.0); };   // cost of spins [0, x)
+    std::vector<uint32_t> b(C + 1, 0);
+    b[C] = P.n_spins;
+    const double total = F(n);
+    for (uint32_t c = 1; c < C; c++) {
+        const double t = total * c / C;
+        double lo = 0, hi = n;
+        for (int it = 0; it < 64; it++) {
+            const double mid = 0.5 * (lo + hi);
+            (F(mid) < t ? lo : hi) = mid;
+        }
+        b[c] = std::max(b[c - 1], std::min(P.n_spins, (uint32_t)hi));
+    }
+    return b;
+}
+
+// The walk of one call: the reference's per-spin loop over time points (kernels.cu:107-232) cut
+// into rounds of refill + walk, at which the generator rings are topped up.
+//
+// Pipeline: the spins are seeded in chunks of equal seeding cost on a low-priority stream; on a
+// high-priority stream each chunk, once seeded, is initialised and given the rounds that no spin
+// can finish sooner than (ceil(steps / 256)), so the walk of chunk c runs beside the seeding of
+// chunk c + 1 (the seed is integer-issue bound, the walk latency bound). Then rounds over all
+// spins until none is active. Adds kernel times and rounds to g_timing.
+int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
+                  const sw::DevParams &P, const sw::DevTables &Tb, const sw::LogfTables &LT,
+                  const Layout &L, const sw::Outputs &O, const float *d_M0, const float *d_XYZ0,
+                  uint32_t C, uint32_t &launches) {
     cudaEvent_t *ev = ctx.ev.data();
-    // Upper bound on rounds: every round advances each unfinished spin by >= 1 attempt.
-    const uint64_t steps = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
-    const uint64_t max_rounds = 64 + steps * (p->max_iterations + 2);
+    cudaStream_t ss = ctx.seed_st, ws = ctx.walk_st;
     const sw_tuning tu = current_tuning();
-    uint32_t chunk = 0;
-    for (;; chunk++) {
-        if (chunk >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
-        const bool timed = chunk < kMaxTimedChunks;
-        SW_CUDA(cudaMemsetAsync(L.active, 0, sizeof(uint32_t), st));
-        if (timed) SW_CUDA(cudaEventRecord(ev[4 + 2 * chunk], st));
-        SW_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
-        if (timed) SW_CUDA(cudaEventRecord(ev[5 + 2 * chunk], st));
-        if (tu.resort_interval && chunk % tu.resort_interval == 0) {
-            SW_CUDA(sw::launch_order(P, L.S, L.Q, 0, P.n_spins, st));
+    const std::vector<uint32_t> b = seed_chunks(P, C);
+    const uint64_t steps = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
+    const uint64_t r0 = (steps + sw::kStepsPerRound - 1) / sw::kStepsPerRound;
+    const uint64_t max_rounds = 64 + steps * (p->max_iterations + 2);
+    uint32_t timed = 0;
+    // one refill + (re-sort) + walk round over spins [lo, hi) on the walk stream
+    auto round = [&](uint32_t lo, uint32_t hi, uint64_t r) -> int {
+        const bool t = timed < kMaxTimedChunks;
+        cudaEvent_t *e = ev + 4 + 3 * timed;
+        if (t) SW_CUDA(cudaEventRecord(e[0], ws));
+        SW_CUDA(sw::launch_refill_range(P, L.G, L.S.flags, LT, lo, hi, ws));
+        if (t) SW_CUDA(cudaEventRecord(e[1], ws));
+        if (tu.resort_interval && r % tu.resort_interval == 0) {
+            SW_CUDA(sw::launch_order(P, L.S, L.Q, lo, hi, ws));
             launches += 3;
         }
-        SW_CUDA(sw::launch_walk_range(precision, dbl, P, Tb, L.vox, L.S, L.G, O, L.active, 0,
-                                      P.n_spins, st, tu.resort_interval ? L.Q.order : nullptr,
+        SW_CUDA(sw::launch_walk_range(precision, dbl, P, Tb, L.vox, L.S, L.G, O, L.active, lo, hi,
+                                      ws, tu.resort_interval ? L.Q.order : nullptr,
                                       (int)tu.walk_block));
+        if (t) SW_CUDA(cudaEventRecord(e[2], ws));
+        if (t) timed++;
         launches += 2;
-        SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        if (timed) SW_CUDA(cudaEventRecord(ev[2], st));
-        SW_CUDA(cudaStreamSynchronize(st));
-        if (timed) {
-            float a = 0.f, b = 0.f;
-            cudaEventElapsedTime(&a, ev[4 + 2 * chunk], ev[5 + 2 * chunk]);
-            cudaEventElapsedTime(&b, ev[5 + 2 * chunk], ev[2]);
-            g_timing.refill_ms += a;
-            g_timing.walk_ms += b;
-        }
+        return SW_OK;
+    };
+    // seeding of every chunk, each chunk bracketed by events (start, done)
+    for (uint32_t c = 0; c < C; c++) {
+        SW_CUDA(cudaEventRecord(ctx.pev[2 + 2 * c], ss));
+        SW_CUDA(sw::launch_seed_range(P, L.G, b[c], b[c + 1], ss));
+        SW_CUDA(cudaEventRecord(ctx.pev[3 + 2 * c], ss));
+        launches++;
+    }
+    int rc;
+    uint64_t rounds = 0;
+    for (uint32_t c = 0; c < C; c++) {
+        if (b[c + 1] == b[c]) continue;
+        SW_CUDA(cudaStreamWaitEvent(ws, ctx.pev[3 + 2 * c], 0));
+        SW_CUDA(sw::launch_init_range(P, Tb, L.vox, d_M0, d_XYZ0, L.S, O, dbl, b[c], b[c + 1], ws));
+        launches++;
+        for (uint64_t r = 0; r < r0; r++)
+            if ((rc = round(b[c], b[c + 1], r))) return rc;
+    }
+    rounds = r0;
+    for (;; rounds++) {
+        if (rounds >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
+        SW_CUDA(cudaMemsetAsync(L.active, 0, sizeof(uint32_t), ws));
+        if ((rc = round(0, P.n_spins, rounds))) return rc;
+        SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active, sizeof(uint32_t), cudaMemcpyDeviceToHost, ws));
+        SW_CUDA(cudaStreamSynchronize(ws));
         if (*ctx.h_active == 0) break;
     }
-    g_timing.n_chunks += chunk + 1;
+    for (uint32_t i = 0; i < timed; i++) {
+        float a = 0.f, w = 0.f;
+        cudaEvent_t *e = ev + 4 + 3 * i;
+        cudaEventElapsedTime(&a, e[0], e[1]);
+        cudaEventElapsedTime(&w, e[1], e[2]);
+        g_timing.refill_ms += a;
+        g_timing.walk_ms += w;
+    }
+    for (uint32_t c = 0; c < C; c++) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ctx.pev[2 + 2 * c], ctx.pev[3 + 2 * c]);
+        g_timing.seed_ms += t;
+    }
+    g_timing.n_chunks += (uint32_t)(rounds + 1);
     return SW_OK;
 }
 
@@ -342,23 +411,37 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
     uint32_t launches = 0;
 
     SW_CUDA(cudaEventRecord(ev[0], st));
-    SW_CUDA(cudaMemsetAsync(L.active, 0, 2 * sizeof(uint32_t), st));
+    // the call's work runs on the context's seed / walk streams, ordered after the caller's
+    // stream and joined back into it
+    SW_CUDA(cudaEventRecord(ctx.pev[0], st));
+    SW_CUDA(cudaStreamWaitEvent(ctx.seed_st, ctx.pev[0], 0));
+    SW_CUDA(cudaStreamWaitEvent(ctx.walk_st, ctx.pev[0], 0));
+    cudaStream_t ws = ctx.walk_st;
+    SW_CUDA(cudaMemsetAsync(L.active, 0, 2 * sizeof(uint32_t), ws));
     SW_CUDA(sw::launch_pack(d_mask, p->fieldmap_exist ? d_field : nullptr, L.vox,
-                            p->matrix_length, p->n_substrate, L.active + 1, st));
-    SW_CUDA(sw::launch_seed(P, L.G, st));
-    SW_CUDA(sw::launch_init(P, Tb, L.vox, d_M0, d_XYZ0, L.S, O, dbl, st));
-    launches += 3;
-    SW_CUDA(cudaEventRecord(ev[1], st));
-    SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    SW_CUDA(cudaStreamSynchronize(st));
-    if (*ctx.h_active != 0)
+                            p->matrix_length, p->n_substrate, L.active + 1, ws));
+    launches++;
+    SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, ws));
+    SW_CUDA(cudaStreamSynchronize(ws));
+    if (*ctx.h_active != 0) {
+        SW_CUDA(cudaStreamSynchronize(ctx.seed_st));
         return fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate");
-
-    rc = walk_rounds(ctx, p, precision, dbl, P, Tb, LT, L, O, st, launches);
-    if (rc) return rc;
+    }
+    const sw_tuning tu = current_tuning();
+    // 0 = 1: on GB300 the co-resident seed and walk kernels slow each other down by about what
+    // the overlap saves (SE 1e6 spins: 194 ms per call with 1 chunk, 191 with 4, 198 with 8)
+    uint32_t C = tu.seed_chunks ? tu.seed_chunks : 1u;
+    C = std::min<uint32_t>(std::min<uint32_t>(C, kMaxSeedChunks), (uint32_t)n);
+    rc = walk_pipeline(ctx, p, precision, dbl, P, Tb, LT, L, O, d_M0, d_XYZ0, C, launches);
+    if (rc) {
+        cudaStreamSynchronize(ctx.seed_st);
+        cudaStreamSynchronize(ctx.walk_st);
+        return rc;
+    }
+    SW_CUDA(cudaEventRecord(ctx.pev[1], ws));
+    SW_CUDA(cudaStreamWaitEvent(st, ctx.pev[1], 0));
     SW_CUDA(cudaEventRecord(ev[3], st));
     SW_CUDA(cudaEventSynchronize(ev[3]));
-    cudaEventElapsedTime(&g_timing.seed_ms, ev[0], ev[1]);
     cudaEventElapsedTime(&g_timing.total_ms, ev[0], ev[3]);
     g_timing.n_launches = launches;
     return SW_OK;
@@ -386,7 +469,7 @@ sw::LogfTables sw::api::device_logf_tables() {
 
 namespace {
 std::mutex g_tune_mu;
-sw_tuning g_tune{0u, 256u, {0u, 0u, 0u, 0u, 0u, 0u}};
+sw_tuning g_tune{0u, 256u, 0u, {0u, 0u, 0u, 0u, 0u}};
 }  // namespace
 
 sw_tuning sw::api::current_tuning() {
@@ -401,6 +484,7 @@ int sw_set_tuning(const sw_tuning *t) {
     if (t->walk_block != 64 && t->walk_block != 128 && t->walk_block != 256)
         return fail(SW_ERR_INVALID, "walk_block must be 64, 128 or 256");
     if (t->resort_interval > 1u << 20) return fail(SW_ERR_INVALID, "resort_interval too large");
+    if (t->seed_chunks > kMaxSeedChunks) return fail(SW_ERR_INVALID, "seed_chunks > 64");
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune = *t;
     return SW_OK;

@@ -47,7 +47,7 @@ namespace {
     } while (0)
 
 constexpr size_t kTableBytes = 1 << 20;        // per slot: RF / TE / gradient tables of a job
-constexpr uint32_t kStepsPerRound = sw::kNormBuf / 3;
+using sw::kStepsPerRound;
 
 double now_s() {
     using clk = std::chrono::steady_clock;

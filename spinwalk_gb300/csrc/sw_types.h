@@ -15,6 +15,7 @@ constexpr int kMtM = 397;
 // Ring buffers of generator output per spin (refilled between walk chunks).
 constexpr uint32_t kNormBuf = 768;               // Gaussian deviates: 256 steps x 3 axes
 constexpr uint32_t kUnifBuf = 128;               // uniform deviates for crossing attempts
+constexpr uint32_t kStepsPerRound = kNormBuf / 3;  // longest walk of one refill/walk round
 
 // Spin flags word: bits 0-7 ts_old (substrate of the last accepted voxel), bit 8 "scan
 // started", bit 9 done, bits 16-23 status (SW_SPIN_*).

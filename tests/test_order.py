@@ -13,17 +13,17 @@ from tests.helpers import bits_equal, load_golden
 def tuning():
     """Restores the default tuning after the test (the setting is process-wide)."""
     yield _lib.set_tuning
-    _lib.set_tuning(0, 256)
+    _lib.set_tuning(0, 256, 0)
 
 
 def test_tuning_roundtrip_and_validation(tuning):
-    tuning(3, 128)
-    assert _lib.get_tuning() == dict(resort_interval=3, walk_block=128)
+    tuning(3, 128, 5)
+    assert _lib.get_tuning() == dict(resort_interval=3, walk_block=128, seed_chunks=5)
     for bad in (dict(resort_interval=1, walk_block=100), dict(resort_interval=1, walk_block=512),
-                dict(resort_interval=1 << 21, walk_block=256)):
+                dict(resort_interval=1 << 21, walk_block=256), dict(seed_chunks=65)):
         with pytest.raises(_lib.SpinWalkError):
             _lib.set_tuning(**bad)
-    assert _lib.get_tuning() == dict(resort_interval=3, walk_block=128)
+    assert _lib.get_tuning() == dict(resort_interval=3, walk_block=128, seed_chunks=5)
 
 
 def _dense_problem(n_spins=20000, TE_us=(3000, 9000), **kw):
@@ -93,6 +93,32 @@ def test_autotune_measures_every_candidate_and_applies(tuning):
         (i, b) for i in (0, 1, 2, 4, 8) for b in (128, 256)}
     assert all(e["ms_per_round"] > 0 for e in table)
     fastest = min(table, key=lambda e: e["ms_per_round"])
-    assert best == dict(resort_interval=fastest["resort_interval"], walk_block=fastest["walk_block"])
+    assert (best["resort_interval"], best["walk_block"]) == (fastest["resort_interval"],
+                                                           fastest["walk_block"])
     assert _lib.get_tuning() == best
     _same(_lib.run(pr, fill=np.nan), want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["permeable", "se_multi_te", "lost_spins", "trajectory",
+                                  "out_of_bounds_periodic", "three_substrates"])
+@pytest.mark.parametrize("chunks", [1, 3, 8, 64])
+def test_sim_results_independent_of_seed_chunks(tuning, case, chunks):
+    """The seed/walk pipeline (spins seeded in chunks beside the walk of earlier chunks) gives
+    the results of seeding everything first; more chunks than spins included."""
+    pr, _ = load_golden(case)
+    tuning(0, 256, 1)
+    want = _lib.run(pr, fill=np.nan)
+    tuning(0, 256, chunks)
+    got = _lib.run(pr, fill=np.nan)
+    _same(got, want)
+
+
+@pytest.mark.gpu
+def test_dense_pipeline_with_resort_and_fp64_shadow(tuning):
+    pr = _dense_problem(n_spins=150000)
+    tuning(0, 256, 1)
+    want = _lib.run(pr, precision=2, fp64_shadow=True, fill=np.nan)
+    tuning(2, 128, 7)
+    got = _lib.run(pr, precision=2, fp64_shadow=True, fill=np.nan)
+    _same(got, want, ("M1", "XYZ1", "T", "status", "M1_fp64"))

@@ -180,6 +180,28 @@ def precision_errors(pr):
     return out
 
 
+def bf16_field_errors(pr):
+    """Error of the bfloat16 fieldmap records (SW_FIELD_BF16) on this workload: M of the FP32
+    run with bf16 records against the FP32 run with float records (same walk, same arithmetic)
+    and against the FP64 shadow of the float-record run; largest per-spin |dM| and largest
+    relative error of the echo signal |mean Mxy|."""
+    from spinwalk_gb300 import _lib, abi
+    ref = _lib.run(pr, precision=abi.SW_PREC_FP32, fp64_shadow=True)
+    got = _lib.run(pr, precision=abi.SW_PREC_FP32 | abi.SW_FIELD_BF16)
+    ok = (ref["status"] == 0) & (got["status"] == 0)
+    m = got["M1"].astype(np.float64)[ok]
+
+    def sig(a):
+        return np.abs(a[:, :, 0].mean(0) + 1j * a[:, :, 1].mean(0))
+    out = {}
+    for name, r in (("vs_float_field", ref["M1"].astype(np.float64)[ok]),
+                    ("vs_fp64", ref["M1_fp64"][ok])):
+        out[name] = {"max_abs_per_spin": float(np.abs(m - r).max()),
+                     "signal_rel": float((np.abs(sig(m) - sig(r)) / np.maximum(sig(r), 1e-30)).max())}
+    out["trajectories_equal"] = bool(np.array_equal(got["XYZ1"], ref["XYZ1"]))
+    return out
+
+
 def cpu_sample_ids(n_spins, n_sample):
     """Stratified sample: evenly spaced spin ids over the whole range (the per-spin discard()
     cost grows with the spin id, so a prefix would under-count it)."""
@@ -290,10 +312,14 @@ def run_ours(args, world, rank, local):
              status=torch.zeros(n, dtype=torch.int32, device=dev))
     stream = torch.cuda.current_stream(dev)
 
+    from spinwalk_gb300 import abi
+    prec = abi.SW_PREC_FP32 | (abi.SW_FIELD_BF16 if args.field_bf16 else 0)
+
     def step():
         _lib.run_device(pr, d["field"].data_ptr(), d["mask"].data_ptr(), d["M0"].data_ptr(),
                         d["XYZ0"].data_ptr(), d["M1"].data_ptr(), d["XYZ1"].data_ptr(),
-                        d["T"].data_ptr(), d["status"].data_ptr(), stream=stream.cuda_stream)
+                        d["T"].data_ptr(), d["status"].data_ptr(), precision=prec,
+                        stream=stream.cuda_stream)
 
     for _ in range(args.warmup):
         step()
@@ -322,11 +348,11 @@ def run_ours(args, world, rank, local):
     h2d = pr.mask.nbytes + pr.field.nbytes + pr.M0.nbytes + pr.XYZ0.nbytes + \
         n * nte * 12 + n * nte + n * pr.traj_len * 12
     d2h = n * nte * 12 + n * nte + n * pr.traj_len * 12 + n * 4
-    _lib.run(pr)                                     # warm (host staging)
+    _lib.run(pr, precision=prec)                     # warm (host staging)
     for _ in range(max(1, args.steps)):
         barrier(world)
         t = time.perf_counter()
-        out = _lib.run(pr)
+        out = _lib.run(pr, precision=prec)
         e2e_times.append(time.perf_counter() - t)
     e2e_s = max_over_ranks(world, float(np.mean(e2e_times)))
     e2e = world * spin_steps / e2e_s
@@ -363,6 +389,7 @@ def run_ours(args, world, rank, local):
         r["frac"] = r["achieved"] / peak
     roof = {"seed+init+pack": seed_roof, "walk": walk_roof}.get(dominant, walk_roof)
     errors = precision_errors(pr) if args.workload in ("se", "small") else None
+    bf16_err = bf16_field_errors(pr) if args.field_bf16 else None
     cpu = None
     if world == 1 or rank == 0:
         if args.cpu_sample > 0:
@@ -376,7 +403,9 @@ def run_ours(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded phantom generator, reference-driver initial positions)",
         "config": dict(desc, parallelism=f"spin-range shards x{world}",
-                       l2="inputs larger than L2 (packed phantom + generator state)"),
+                       l2="inputs larger than L2 (packed phantom + generator state)",
+                       field_records="bfloat16, 4 B per voxel" if args.field_bf16
+                       else "float32, 8 B per voxel"),
         "kernel_ms_per_step": {k: v / args.steps for k, v in parts.items()},
         "roofline": dict(roof, dominant_stage=dominant),
         "roofline_walk": walk_roof,
@@ -386,6 +415,7 @@ def run_ours(args, world, rank, local):
         "gpu_launches": int(launches),
         "tuning": tuning,
         "error_vs_fp64": errors,
+        "field_bf16": bf16_err,
         "clocks": clocks,
         "status_counts": {str(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))},
     }
@@ -695,6 +725,8 @@ def main():
     ap.add_argument("--resort-interval", type=int, default=None,
                     help="walk rounds between Morton re-sorts of the spins (0 = never)")
     ap.add_argument("--walk-block", type=int, default=None, help="walk kernel block size")
+    ap.add_argument("--field-bf16", action="store_true",
+                    help="bfloat16 fieldmap records (SW_FIELD_BF16); reports their error")
     ap.add_argument("--seed-chunks", type=int, default=None,
                     help="seed/walk pipeline chunks (1 = seed all first, 0 = auto)")
     args = ap.parse_args()

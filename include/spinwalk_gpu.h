@@ -65,6 +65,14 @@ extern "C" {
 #define SW_RNG_MT19937     0x000
 #define SW_RNG_MINSTD      0x100
 #define SW_PREC_MASK       0x0ff
+/* Fieldmap record, OR-ed into `precision` (sw_sim, sw_sim_device, sw_sim_batch, sw_sim_spins,
+ * sw_sim_signal): SW_FIELD_BF16 packs the phantom as 4-byte voxel records, the field rounded to
+ * bfloat16 (round to nearest even) beside the substrate label, instead of 8-byte records with the
+ * float field -- half the phantom's device memory and gather bytes. Trajectories, substrates and
+ * status are unchanged (the field only enters the phase); M1 is that of the float run on the
+ * field rounded to bfloat16, which differs from the float field's by the stated error of
+ * bench.py --field-bf16 (no counterpart in the reference, whose fieldmap is float). */
+#define SW_FIELD_BF16      0x200
 
 /*
  * Scalar simulation parameters. Field-for-field mirror of sim::parameters
@@ -395,6 +403,11 @@ int sw_engine_destroy(sw_engine *e);
  * dims[0] x dims[1] x dims[2] voxels, z fastest */
 int sw_engine_add_phantom(sw_engine *e, const uint8_t *mask, const float *field_deg_per_step,
                           const uint64_t dims[3], uint32_t n_substrate, int32_t *phantom_id);
+/* as sw_engine_add_phantom; flags = SW_FIELD_BF16 packs 4-byte records (jobs on the phantom then
+ * run with the bfloat16 field; a job that passes SW_FIELD_BF16 needs such a phantom) */
+int sw_engine_add_phantom_ex(sw_engine *e, const uint8_t *mask, const float *field_deg_per_step,
+                             const uint64_t dims[3], uint32_t n_substrate, int flags,
+                             int32_t *phantom_id);
 /* queues one job (the arguments of sw_sim, on a registered phantom); nothing runs until
  * sw_engine_poll */
 int sw_engine_submit(sw_engine *e, int32_t phantom, const sw_params *param, const sw_sequence *seq,

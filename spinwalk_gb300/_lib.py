@@ -56,6 +56,8 @@ def lib():
         L.sw_engine_destroy.argtypes = [C.c_void_p]
         L.sw_engine_add_phantom.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, P(C.c_uint64),
                                             C.c_uint32, P(C.c_int32)]
+        L.sw_engine_add_phantom_ex.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, P(C.c_uint64),
+                                               C.c_uint32, C.c_int, P(C.c_int32)]
         L.sw_engine_submit.argtypes = [C.c_void_p, C.c_int32, P(abi.SwParams), P(abi.SwSequence),
                                        C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, P(C.c_int64)]
@@ -328,12 +330,14 @@ class Engine:
                                      C.c_uint64(int(hbm_budget)), C.byref(self._h)))
         self._jobs = {}                 # job id -> (problem, outputs): keep buffers alive
 
-    def add_phantom(self, problem):
-        """Registers the phantom (mask, scaled field) of a problem.Problem; returns its id."""
+    def add_phantom(self, problem, bf16=False):
+        """Registers the phantom (mask, scaled field) of a problem.Problem; returns its id.
+        bf16: 4-byte voxel records with the field rounded to bfloat16 (SW_FIELD_BF16)."""
         pid = C.c_int32()
         dims = (C.c_uint64 * 3)(*problem.mask.shape)
-        check(lib().sw_engine_add_phantom(self._h, _p(problem.mask), _p(problem.field), dims,
-                                          int(problem.params.n_substrate), C.byref(pid)))
+        check(lib().sw_engine_add_phantom_ex(self._h, _p(problem.mask), _p(problem.field), dims,
+                                             int(problem.params.n_substrate),
+                                             abi.SW_FIELD_BF16 if bf16 else 0, C.byref(pid)))
         return pid.value
 
     def submit(self, problem, phantom, precision=abi.SW_PREC_FP32, fill=0.0):

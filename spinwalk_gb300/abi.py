@@ -25,6 +25,7 @@ SW_SPIN_START_OOB = 3
 SW_PREC_FP32 = 0
 SW_PREC_FP64 = 1
 SW_PREC_KAHAN = 2
+SW_FIELD_BF16 = 0x200
 SW_RNG_MT19937 = 0x000
 SW_RNG_MINSTD = 0x100
 

@@ -370,7 +370,8 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
     g_timing = sw_timing{};
     const size_t n = p->n_spins;
     if (n == 0) return SW_OK;
-    const uint32_t rng = (uint32_t)precision & ~(uint32_t)SW_PREC_MASK;
+    const bool bf16 = (precision & SW_FIELD_BF16) != 0;
+    const uint32_t rng = (uint32_t)precision & ~(uint32_t)(SW_PREC_MASK | SW_FIELD_BF16);
     precision &= SW_PREC_MASK;
     if (precision != SW_PREC_FP32 && precision != SW_PREC_FP64 && precision != SW_PREC_KAHAN)
         return fail(SW_ERR_INVALID, "precision");
@@ -403,6 +404,7 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
 
     sw::DevParams P = dev_params(p, q);
     P.rng = rng;
+    P.field_bf16 = bf16 ? 1 : 0;
     const sw::DevTables Tb = dev_tables(im, L.tables);
     sw::LogfTables LT = logf_tables(ctx);
     if (rng == SW_RNG_MINSTD && !(LT.ms_delta = minstd_delta_table())) return SW_ERR_CUDA;
@@ -419,7 +421,7 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
     cudaStream_t ws = ctx.walk_st;
     SW_CUDA(cudaMemsetAsync(L.active, 0, 2 * sizeof(uint32_t), ws));
     SW_CUDA(sw::launch_pack(d_mask, p->fieldmap_exist ? d_field : nullptr, L.vox,
-                            p->matrix_length, p->n_substrate, L.active + 1, ws));
+                            p->matrix_length, p->n_substrate, L.active + 1, ws, bf16));
     launches++;
     SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, ws));
     SW_CUDA(cudaStreamSynchronize(ws));

@@ -276,6 +276,17 @@ __device__ __forceinline__ bool dnonzero(double v) { return __double_as_longlong
 // ------------------------------------------------------------------------------------------
 enum MoveResult { kMoveAccepted = 0, kMoveRejected = 1, kMoveLost = 2, kMoveOOB = 3 };
 
+// One packed voxel record as {field bits, substrate label}: 8-byte records hold the float field,
+// 4-byte records (SW_FIELD_BF16) the field as bfloat16 in bits 0-15 and the label in bits 16-23.
+__device__ __forceinline__ uint2 voxel_record(const uint2 *__restrict__ vox, int64_t ind,
+                                              int32_t bf16) {
+    if (bf16) {
+        const uint32_t r = __ldg(reinterpret_cast<const uint32_t *>(vox) + ind);
+        return make_uint2(r << 16, r >> 16);
+    }
+    return __ldg(vox + ind);
+}
+
 struct WalkRegs {
     uint64_t xo[3];           // last accepted position (bit patterns of the doubles)
     int64_t ind_old;
@@ -319,7 +330,7 @@ __device__ __forceinline__ int walk_move(WalkRegs &w, uint64_t (&xn)[3], const D
                         voxel_coord(xn[2], P.s2g[2], P.s2g_f[2]);
     if (ind >= P.matrix_length || ind < 0) return kMoveOOB;
     if (ind != w.ind_old) {
-        const uint2 v = __ldg(vox + ind);
+        const uint2 v = voxel_record(vox, ind, P.field_bf16);
         const uint32_t ts = v.y;
         if (ts != w.ts_old) {
             const float u = ub[w.uh];

@@ -84,6 +84,7 @@ struct Phantom {
     uint64_t dims[3] = {0, 0, 0};
     uint32_t n_substrate = 0;
     bool field = false;
+    bool bf16 = false;              // 4-byte records (SW_FIELD_BF16)
     int jobs = 0;                   // jobs still using it
 };
 
@@ -487,7 +488,9 @@ int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_se
     if (p->n_substrate < ph.n_substrate)
         return fail(SW_ERR_INVALID, "the mask holds more substrate types than the config defines");
     if (p->fieldmap_exist && !ph.field) return fail(SW_ERR_INVALID, "fieldmap_exist but the phantom has no fieldmap");
-    const uint32_t rng = (uint32_t)precision & ~(uint32_t)SW_PREC_MASK;
+    if ((precision & SW_FIELD_BF16) && !ph.bf16)
+        return fail(SW_ERR_INVALID, "SW_FIELD_BF16 on a phantom of float records");
+    const uint32_t rng = (uint32_t)precision & ~(uint32_t)(SW_PREC_MASK | SW_FIELD_BF16);
     precision &= SW_PREC_MASK;
     if (precision != SW_PREC_FP32 && precision != SW_PREC_FP64 && precision != SW_PREC_KAHAN)
         return fail(SW_ERR_INVALID, "precision");
@@ -543,6 +546,7 @@ int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_se
     std::memcpy(j->h_tables, j->im.bytes.data(), j->im.bytes.size());
     j->P = dev_params(&j->p, &Q);
     j->P.rng = rng;
+    j->P.field_bf16 = ph.bf16 ? 1 : 0;
     j->M0 = M0; j->XYZ0 = XYZ0; j->M1 = M1; j->XYZ1 = XYZ1; j->T = T; j->status = status;
     j->nte = nte;
     j->trj = trj;
@@ -639,16 +643,18 @@ int engine_create(int device, uint32_t n_slots, uint32_t slot_spins, uint64_t bu
 }
 
 int engine_add_phantom(sw_engine *E, const uint8_t *mask, const float *field, const uint64_t dims[3],
-                       uint32_t n_substrate, int32_t *id) {
+                       uint32_t n_substrate, int32_t *id, int flags = 0) {
     if (!mask || !dims || !id) return fail(SW_ERR_INVALID, "null argument");
+    if (flags & ~SW_FIELD_BF16) return fail(SW_ERR_INVALID, "phantom flags");
+    const bool bf16 = (flags & SW_FIELD_BF16) != 0;
     const int64_t ml = (int64_t)(dims[0] * dims[1] * dims[2]);
     if (ml <= 0 || n_substrate == 0 || n_substrate > 256) return fail(SW_ERR_INVALID, "phantom size / substrates");
-    const size_t bytes = (size_t)ml * 8;
+    const size_t bytes = (size_t)ml * (bf16 ? 4 : 8);
     if (E->used + bytes > E->budget) {        // evict idle phantoms, oldest first
         for (auto it = E->phantoms.begin(); it != E->phantoms.end() && E->used + bytes > E->budget;) {
             if (it->second.jobs == 0) {
                 cudaFree(it->second.vox);
-                E->used -= (size_t)it->second.ml * 8;
+                E->used -= (size_t)it->second.ml * (it->second.bf16 ? 4 : 8);
                 it = E->phantoms.erase(it);
             } else {
                 ++it;
@@ -661,6 +667,7 @@ int engine_add_phantom(sw_engine *E, const uint8_t *mask, const float *field, co
     for (int i = 0; i < 3; i++) ph.dims[i] = dims[i];
     ph.n_substrate = n_substrate;
     ph.field = field != nullptr;
+    ph.bf16 = bf16;
     uint8_t *d_mask = nullptr;
     float *d_field = nullptr;
     uint32_t *d_bad = nullptr, h_bad = 0;
@@ -680,7 +687,7 @@ int engine_add_phantom(sw_engine *E, const uint8_t *mask, const float *field, co
     if (cudaMemcpy(d_mask, mask, ml, cudaMemcpyHostToDevice) != cudaSuccess ||
         (field && cudaMemcpy(d_field, field, ml * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
         cudaMemset(d_bad, 0, 4) != cudaSuccess ||
-        sw::launch_pack(d_mask, d_field, ph.vox, ml, n_substrate, d_bad, E->seed_st) != cudaSuccess ||
+        sw::launch_pack(d_mask, d_field, ph.vox, ml, n_substrate, d_bad, E->seed_st, bf16) != cudaSuccess ||
         cudaMemcpyAsync(&h_bad, d_bad, 4, cudaMemcpyDeviceToHost, E->seed_st) != cudaSuccess ||
         cudaStreamSynchronize(E->seed_st) != cudaSuccess)
         return cleanup(fail(SW_ERR_CUDA, "phantom upload"));
@@ -711,10 +718,16 @@ int sw_engine_destroy(sw_engine *e) {
 
 int sw_engine_add_phantom(sw_engine *e, const uint8_t *mask, const float *field_deg_per_step,
                           const uint64_t dims[3], uint32_t n_substrate, int32_t *phantom_id) {
+    return sw_engine_add_phantom_ex(e, mask, field_deg_per_step, dims, n_substrate, 0, phantom_id);
+}
+
+int sw_engine_add_phantom_ex(sw_engine *e, const uint8_t *mask, const float *field_deg_per_step,
+                             const uint64_t dims[3], uint32_t n_substrate, int flags,
+                             int32_t *phantom_id) {
     if (!e) return SW_ERR_INVALID;
     std::lock_guard<std::mutex> lk(e->mu);
     if (cudaSetDevice(e->device) != cudaSuccess) return fail(SW_ERR_CUDA, "device");
-    return engine_add_phantom(e, mask, field_deg_per_step, dims, n_substrate, phantom_id);
+    return engine_add_phantom(e, mask, field_deg_per_step, dims, n_substrate, phantom_id, flags);
 }
 
 int sw_engine_submit(sw_engine *e, int32_t phantom, const sw_params *param, const sw_sequence *seq,
@@ -857,7 +870,7 @@ int sw_sim_batch(const sw_instance *items, uint32_t n_items, const float *pField
     const uint64_t dims[3] = {p0->phantom_size[0], p0->phantom_size[1], p0->phantom_size[2]};
     int32_t ph = 0;
     rc = engine_add_phantom(E, pMask, p0->fieldmap_exist ? pFieldMap : nullptr, dims,
-                            p0->n_substrate, &ph);
+                            p0->n_substrate, &ph, precision & SW_FIELD_BF16);
     SeedCache *sc = nullptr;
     if (!rc) rc = ensure_seeded(E, p0->seed, 0, (uint32_t)n_max, sc);   // one seeding, largest n
     std::vector<uint32_t> order(n_items);
@@ -901,7 +914,7 @@ int sw_sim_spins(const sw_params *param, const sw_sequence *seq, const float *pF
     const uint64_t dims[3] = {param->phantom_size[0], param->phantom_size[1], param->phantom_size[2]};
     int32_t ph = 0;
     rc = engine_add_phantom(E, pMask, param->fieldmap_exist ? pFieldMap : nullptr, dims,
-                            param->n_substrate, &ph);
+                            param->n_substrate, &ph, precision & SW_FIELD_BF16);
     int64_t jid = 0;
     if (!rc)
         rc = engine_submit(E, ph, param, seq, precision, M0, XYZ0, M1, XYZ1, T, status, &jid,
@@ -946,7 +959,7 @@ int sw_sim_signal(const sw_params *param, const sw_sequence *seq, const float *p
     const uint64_t dims[3] = {param->phantom_size[0], param->phantom_size[1], param->phantom_size[2]};
     int32_t ph = 0;
     rc = engine_add_phantom(E, pMask, param->fieldmap_exist ? pFieldMap : nullptr, dims,
-                            param->n_substrate, &ph);
+                            param->n_substrate, &ph, precision & SW_FIELD_BF16);
     int64_t jid = 0;
     if (!rc)
         rc = engine_submit(E, ph, param, seq, precision, M0, XYZ0, nullptr, nullptr, nullptr,

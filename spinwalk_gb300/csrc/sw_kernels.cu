@@ -16,6 +16,7 @@
 //
 // k_refill and k_walk alternate until every spin has finished. All kernels are compiled with
 // -fmad=false (see sw_device.cuh).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "sw_device.cuh"
@@ -29,14 +30,18 @@ namespace sw {
 // src/sim/monte_carlo.cu:113-118); the host checks the flag before any walk reads the tables.
 __global__ void k_pack(const uint8_t *__restrict__ mask, const float *__restrict__ field,
                        uint2 *__restrict__ out, int64_t n, uint32_t n_substrate,
-                       uint32_t *__restrict__ bad_label) {
+                       uint32_t *__restrict__ bad_label, int bf16) {
     bool bad = false;
+    uint32_t *out4 = reinterpret_cast<uint32_t *>(out);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t f = field ? __float_as_uint(field[i]) : 0u;
+        const float fv = field ? field[i] : 0.f;
         const uint32_t m = mask[i];
         bad |= m >= n_substrate;
-        out[i] = make_uint2(f, m);
+        if (bf16)
+            out4[i] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(fv)) | (m << 16);
+        else
+            out[i] = make_uint2(__float_as_uint(fv), m);
     }
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(bad_label, 1u);
 }
@@ -265,7 +270,7 @@ __global__ void k_init(DevParams P, DevTables Tb, const uint2 *__restrict__ vox,
         if (O.status) O.status[spin] = SW_SPIN_START_OOB;
         return;
     }
-    S.flags[spin] = vox[i0].y & 0xffu;                             // ts_old, not started
+    S.flags[spin] = voxel_record(vox, i0, P.field_bf16).y & 0xffu;  // ts_old, not started
 }
 
 // ------------------------------------------------------------------------------------------
@@ -526,7 +531,7 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
         if (ind >= P.matrix_length || ind < 0) { status = SW_SPIN_OOB; break; }
         // ---- mask, permeability, field (kernels.cu:150-170) ----
         if (ind != ind_old) {
-            const uint2 v = __ldg(vox + ind);
+            const uint2 v = voxel_record(vox, ind, P.field_bf16);
             const uint32_t ts = v.y;
             if (ts != ts_old) {
                 const float u = ub[uh];
@@ -696,9 +701,9 @@ static int grid_for(int64_t work, int block, int max_blocks) {
 }
 
 cudaError_t launch_pack(const uint8_t *mask, const float *field, uint2 *out, int64_t n,
-                        uint32_t n_substrate, uint32_t *bad_label, cudaStream_t st) {
+                        uint32_t n_substrate, uint32_t *bad_label, cudaStream_t st, bool bf16) {
     k_pack<<<grid_for(n, 256, 152 * 32), 256, 0, st>>>(mask, field, out, n, n_substrate,
-                                                        bad_label);
+                                                        bad_label, bf16 ? 1 : 0);
     return cudaGetLastError();
 }
 

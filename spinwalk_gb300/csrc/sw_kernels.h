@@ -6,8 +6,10 @@
 
 namespace sw {
 
+// bf16: 4-byte records (bfloat16 field | label << 16) instead of 8-byte {float field, label}
 cudaError_t launch_pack(const uint8_t *mask, const float *field, uint2 *out, int64_t n,
-                        uint32_t n_substrate, uint32_t *bad_label, cudaStream_t st);
+                        uint32_t n_substrate, uint32_t *bad_label, cudaStream_t st,
+                        bool bf16 = false);
 cudaError_t launch_seed(const DevParams &P, const RngState &G, cudaStream_t st);
 cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo, uint32_t hi,
                               cudaStream_t st);

@@ -48,6 +48,7 @@ struct DevParams {
     int32_t cross_fov, record_traj, fieldmap_exist;
     uint64_t traj_len;        // XYZ1 slots per spin
     uint32_t rng;             // SW_RNG_MT19937 or SW_RNG_MINSTD (generator flavour)
+    int32_t field_bf16;       // packed phantom of 4-byte records (bf16 field | label << 16)
 };
 
 // Small read-only tables (device pointers into one allocation).

@@ -45,6 +45,10 @@ SEED_BYTES_PER_SPIN = 2 * 624 * 4 + 6 * 4   # two mt19937 states + 6 ring/index 
 # DRAM traffic per unit from ncu on the small SE case (profiles/kernels_small_se_300cubed_2e5spins.md),
 # scaled to a full launch by the units it processes (both grow in proportion)
 SEED_DRAM_BYTES_PER_SPIN = 4713.0
+MT_BYTES_PER_SPIN_STEP = 3.82 * 8        # MT words drawn per step x (4 B read + 4 B write)
+WALK_FP64_OPS_PER_SPIN_STEP = 3          # x, y, z position additions (the rest is integer)
+FP64_PEAK_GFLOPS = 152 * 2 * 2070e6 / 1e9  # 2 FP64 lanes per clock per SM at 2070 MHz
+USEFUL_BYTES_PER_SPIN_STEP = 5           # 1 B mask + 4 B field at the visited voxel
 WALK_DRAM_BYTES_PER_SPIN_STEP = 26.4
 SEED_LIMITER = ("integer instruction issue (ncu: ALU pipe 83 %, issue 74 %, DRAM 2 %): "
                 "7.7 lane instructions per MT word, not HBM")
@@ -388,6 +392,19 @@ def run_ours(args, world, rank, local):
     for r in (seed_roof, walk_roof):
         r["frac"] = r["achieved"] / peak
     roof = {"seed+init+pack": seed_roof, "walk": walk_roof}.get(dominant, walk_roof)
+    # walk-only rate (refill + walk kernels, generator seeding excluded) and the secondary
+    # ceilings: MT-state traffic of the refill (3.82 words of 8 B read+write per step) and the
+    # FP64 work of the walk (3 position additions per step, 2 FP64 lanes per clock per SM)
+    walk_refill_s = (walk_ms + refill_ms) / args.steps * 1e-3
+    secondary = {
+        "walk_only_spin_steps_per_s": spin_steps / walk_refill_s,
+        "refill_mt_state_gbs": spin_steps * MT_BYTES_PER_SPIN_STEP / (refill_ms / args.steps * 1e-3) / 1e9,
+        "walk_fp64_gflops": spin_steps * WALK_FP64_OPS_PER_SPIN_STEP / (walk_ms / args.steps * 1e-3) / 1e9,
+        "fp64_peak_gflops": FP64_PEAK_GFLOPS,
+        "useful_gather_gbs": spin_steps * USEFUL_BYTES_PER_SPIN_STEP / (walk_ms / args.steps * 1e-3) / 1e9,
+        "note": "kernel times overlap nothing (one stream); ncu: k_walk L2 hit rate and FP64 pipe "
+                "in profiles/",
+    }
     errors = precision_errors(pr) if args.workload in ("se", "small") else None
     bf16_err = bf16_field_errors(pr) if args.field_bf16 else None
     cpu = None
@@ -409,6 +426,7 @@ def run_ours(args, world, rank, local):
         "kernel_ms_per_step": {k: v / args.steps for k, v in parts.items()},
         "roofline": dict(roof, dominant_stage=dominant),
         "roofline_walk": walk_roof,
+        "secondary_ceilings": secondary,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "spin-steps/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
@@ -436,13 +454,14 @@ def run_batched(args, world, rank):
     walk_steps = p.n_spins * p.n_timepoints * 210
     for _ in range(args.warmup):
         _lib.run_tracks(pr, tracks)
-    times, dev_ms = [], []
+    times, dev_ms, launches = [], [], []
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
             t = time.perf_counter()
             _lib.run_tracks(pr, tracks)
             times.append(time.perf_counter() - t)
             dev_ms.append(_lib.last_timing()["total_ms"])
+            launches.append(_lib.last_timing()["n_launches"])
     clocks = clk.summary()
     # the plain kernel on one instance of the same config, for the batched/plain ratio
     one = dict(tracks[-1])
@@ -470,6 +489,7 @@ def run_batched(args, world, rank):
             "e2e": {"value": inst_steps / float(np.mean(times)), "unit": "spin-steps/s",
                     "note": "includes the per-track host output copies"},
             "recurrence_error_vs_fp64": rec_err,
+            "gpu_launches": int(sum(launches)),
             "clocks": clocks}
     print(json.dumps(line), flush=True)
 
@@ -546,13 +566,14 @@ def run_batch_scales(args, world, rank):
     steps = sum(p.spin_steps() for p in probs)
     for _ in range(args.warmup):
         _lib.run_batch(probs)
-    dev_ms, wall = [], []
+    dev_ms, wall, launches = [], [], []
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
             t = time.perf_counter()
             _lib.run_batch(probs)
             wall.append(time.perf_counter() - t)
             dev_ms.append(_lib.last_timing()["total_ms"])
+            launches.append(_lib.last_timing()["n_launches"])
     clocks = clk.summary()
     plain_ms, plain_wall = 0.0, 0.0
     for p in probs:
@@ -573,6 +594,7 @@ def run_batch_scales(args, world, rank):
             "batched_over_plain_e2e": float(np.mean(wall)) and (steps / float(np.mean(wall))) / (steps / plain_wall),
             "e2e": {"value": world * steps / float(np.mean(wall)), "unit": "spin-steps/s",
                     "note": "sw_sim_batch with host buffers"},
+            "gpu_launches": int(sum(launches)),
             "tuning": tuning, "clocks": clocks}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -645,12 +667,18 @@ def run_serve(args, world, rank):
     for pr in reqs:
         key = pr.mask.shape
         if key not in pids:
-            pids[key] = eng.add_phantom(pr)
+            pids[key] = eng.add_phantom(pr, bf16=args.field_bf16)
+
+    def submit(pr):
+        if args.signal:
+            return eng.submit_signal(pr, pids[pr.mask.shape])
+        return eng.submit(pr, pids[pr.mask.shape])
     # service start-up: generator states of the largest request, computed once
     big = max(reqs, key=lambda p: p.params.n_spins)
-    eng.submit(big, pids[big.mask.shape])
+    submit(big)
     eng.run_all()
     startup_s = time.perf_counter() - t0
+    st0 = eng.stats()
     steps = sum(p.spin_steps() for p in reqs)
     lat = []
     with ClockSampler(0) as clk:
@@ -659,7 +687,7 @@ def run_serve(args, world, rank):
         while i < n_req or len(lat) < n_req:
             now = time.perf_counter() - t_start
             while i < n_req and arrivals[i] <= now:
-                eng.submit(reqs[i], pids[reqs[i].mask.shape])
+                submit(reqs[i])
                 i += 1
             for jid, rc, l in eng.poll(wait=0):
                 assert rc == 0
@@ -667,18 +695,26 @@ def run_serve(args, world, rank):
             time.sleep(0.0005)
         makespan = time.perf_counter() - t_start
     clocks = clk.summary()
+    st1 = eng.stats()
     lat = np.array(lat)
     value = world * steps / makespan
     line = {"metric": "spin-steps/s (served)", "value": value, "unit": "spin-steps/s",
             "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": makespan * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": dict(desc, requests=n_req, spin_steps=int(steps)),
+            "data": "synthetic",
+            "config": dict(desc, requests=n_req, spin_steps=int(steps),
+                           outputs="per-(echo, substrate) signal sums (signal mode)" if args.signal
+                           else "per-spin M1, T, XYZ1, status",
+                           field_records="bfloat16, 4 B per voxel" if args.field_bf16
+                           else "float32, 8 B per voxel"),
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "max": float(lat.max())},
             "offered_spin_steps_per_s": steps / float(arrivals[-1]),
             "startup_s": startup_s,
             "e2e": {"value": value, "unit": "spin-steps/s",
                     "note": "host buffers in and out through the engine, arrivals in real time"},
+            "gpu_launches": int(st1["launches"] - st0["launches"]),
+            "walk_rounds": int(st1["rounds"] - st0["rounds"]),
             "tuning": tuning, "clocks": clocks}
     eng.close()
     if rank == 0:
@@ -725,6 +761,8 @@ def main():
     ap.add_argument("--resort-interval", type=int, default=None,
                     help="walk rounds between Morton re-sorts of the spins (0 = never)")
     ap.add_argument("--walk-block", type=int, default=None, help="walk kernel block size")
+    ap.add_argument("--signal", action="store_true",
+                    help="serve workload: requests in signal mode (no per-spin outputs)")
     ap.add_argument("--field-bf16", action="store_true",
                     help="bfloat16 fieldmap records (SW_FIELD_BF16); reports their error")
     ap.add_argument("--seed-chunks", type=int, default=None,

@@ -418,6 +418,13 @@ int sw_engine_submit(sw_engine *e, int32_t phantom, const sw_params *param, cons
 int sw_engine_poll(sw_engine *e, int wait, sw_job_result *done, uint32_t max_done,
                    uint32_t *n_done);
 int sw_engine_pending(sw_engine *e, uint32_t *n_pending);
+/* Counters since sw_engine_create: kernels launched, refill/walk rounds issued, seedings. */
+typedef struct sw_engine_stats {
+    uint64_t launches;
+    uint64_t rounds;
+    uint64_t seedings;
+} sw_engine_stats;
+int sw_engine_get_stats(sw_engine *e, sw_engine_stats *out);
 
 /* ---- Signal mode: the reduction of the results fused into the walk ------------------------
  * What the reference's analysis computes from M1 and T (the demos average M per tissue and

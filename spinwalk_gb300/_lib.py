@@ -56,6 +56,7 @@ def lib():
         L.sw_engine_destroy.argtypes = [C.c_void_p]
         L.sw_engine_add_phantom.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, P(C.c_uint64),
                                             C.c_uint32, P(C.c_int32)]
+        L.sw_engine_get_stats.argtypes = [C.c_void_p, P(abi.SwEngineStats)]
         L.sw_engine_add_phantom_ex.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, P(C.c_uint64),
                                                C.c_uint32, C.c_int, P(C.c_int32)]
         L.sw_engine_submit.argtypes = [C.c_void_p, C.c_int32, P(abi.SwParams), P(abi.SwSequence),
@@ -372,6 +373,12 @@ class Engine:
         for jid, _, _ in out:
             self._jobs.pop(jid, None)
         return out
+
+    def stats(self):
+        """dict(launches, rounds, seedings) since the engine was created."""
+        s = abi.SwEngineStats()
+        check(lib().sw_engine_get_stats(self._h, C.byref(s)))
+        return dict(launches=s.launches, rounds=s.rounds, seedings=s.seedings)
 
     def run_all(self):
         done = []

@@ -113,6 +113,14 @@ class SwJobResult(C.Structure):
                 ("latency_s", C.c_double)]
 
 
+class SwEngineStats(C.Structure):
+    _fields_ = [
+        ("launches", C.c_uint64),
+        ("rounds", C.c_uint64),
+        ("seedings", C.c_uint64),
+    ]
+
+
 class SwTuning(C.Structure):
     _fields_ = [
         ("resort_interval", C.c_uint32),

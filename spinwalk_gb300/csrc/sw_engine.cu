@@ -977,4 +977,13 @@ int sw_engine_pending(sw_engine *e, uint32_t *n_pending) {
     return SW_OK;
 }
 
+int sw_engine_get_stats(sw_engine *e, sw_engine_stats *out) {
+    if (!e || !out) return SW_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(e->mu);
+    out->launches = e->launches;
+    out->rounds = e->rounds;
+    out->seedings = e->seedings;
+    return SW_OK;
+}
+
 }  // extern "C"

@@ -350,9 +350,11 @@ __global__ void __launch_bounds__(32 * kRefillWarps)
                 if (ok && rank < need) {
                     const float lg = logf_libm(r2, s_tab, L);
                     const float mult = __fsqrt_rn(__fdiv_rn(-2.0f * lg, r2));
-                    const uint32_t pos = (wpos + 2 * (produced + rank)) % kNormBuf;
+                    uint32_t pos = wpos + 2 * (produced + rank);   // < 3 kNormBuf
+                    pos -= pos >= kNormBuf ? kNormBuf : 0u;
+                    pos -= pos >= kNormBuf ? kNormBuf : 0u;
                     nb[pos] = y * mult;                          // returned first
-                    nb[(pos + 1) % kNormBuf] = x * mult;         // saved for the next call
+                    nb[pos + 1 == kNormBuf ? 0 : pos + 1] = x * mult;   // saved for the next call
                 }
                 const uint32_t nacc = __popc(bal);
                 if (nacc <= need) {

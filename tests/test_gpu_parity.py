@@ -185,3 +185,9 @@ def test_gpu_integer_double_add_matches_ieee():
         want = A + B
     same = (got.view(np.uint64) == want.view(np.uint64)) | (np.isnan(got) & np.isnan(want))
     assert same.all(), f"{(~same).sum()} mismatches, first a={A[~same][0]!r} b={B[~same][0]!r}"
+
+
+def test_smoke_entry_point_passes():
+    """The build's smoke check (one small GRE walk against the oracle) passes."""
+    import __graft_entry__
+    __graft_entry__.smoke()

@@ -85,6 +85,32 @@ def test_gpu_large_seed_and_spin_ids():
     assert ok, rel
 
 
+def test_gpu_phantom_beyond_2e31_voxels():
+    """A 1300^3 phantom (2.197e9 voxels > 2^31, the reference's int64 voxel index): spins near
+    the far corner, where the index exceeds 2^31, against the oracle. Mask only (a 17.6 GB packed
+    phantom on the device)."""
+    n = 1300
+    mask = np.zeros((n, n, n), np.uint8)
+    mask[n - 25:n - 10, n - 60:, :] = 1                  # a slab in the high-index corner
+    fov = 1300e-6
+    rng = np.random.default_rng(9)
+    off = rng.uniform(0.005, 0.06, (512, 3))
+    off[:, 0] = rng.uniform(0.004, 0.018, 512)         # x >= 1271: index > 2^31
+    xyz0 = (fov * (1.0 - off)).astype(np.float32)
+    pr = Problem(mask, [fov] * 3, None, n_spins=512, seed=77, TR_us=10050, TE_us=(5000, 10000),
+                 diffusivity=(2e-9, 1e-9), T1_ms=(1500.0, 1200.0), T2_ms=(60.0, 30.0),
+                 pXY=[[1.0, 0.2], [0.1, 1.0]], XYZ0=xyz0)
+    idx = (xyz0.astype(np.float64) * (n / fov)).astype(np.int64)
+    assert (idx[:, 0] * n * n + idx[:, 1] * n + idx[:, 2]).min() > 2 ** 31
+    g = _lib.run(pr, fill=np.nan)
+    o = oracle_lib.run(pr, fill=np.nan)
+    for k in ("XYZ1", "T", "status"):
+        assert bits_equal(g[k], o[k]), k
+    assert (o["T"] == 1).any() and (o["T"] == 0).any()    # both substrates reached
+    ok, rel = m_close(g["M1"], o["M1"])
+    assert ok, rel
+
+
 def test_gpu_deterministic_and_spin_independent():
     pr, _ = load_golden("permeable")
     a = _lib.run(pr)

@@ -754,7 +754,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="se")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--cpu-sample", type=int, default=32768)
     ap.add_argument("--requests", type=int, default=100, help="serve workload: trace length")
     ap.add_argument("--autotune", action="store_true",
                     help="pick the walk tuning by sw_autotune on the workload before timing")

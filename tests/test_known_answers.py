@@ -183,3 +183,36 @@ def test_pgse_attenuation_of_free_diffusion(run):
     want = math.exp(-0.5 * sigma2 * float(np.sum(tail ** 2)))
     assert 0.2 < want < 0.8                          # a measurable attenuation
     assert abs(s - want) < 4.0 / math.sqrt(n), (s, want)
+
+
+@pytest.mark.parametrize("run", IMPLS)
+def test_pgse_b_sweep_recovers_the_diffusivity(run):
+    """The DWI demo's check (demo/spinwalk_dwi.ipynb: simulated D = 1e-9 m^2/s, fitted 9.79e-10):
+    a PGSE b-value sweep on free diffusion, log S linear in b with slope -D. b is the exact
+    value of the discrete waveform (var = 2 b D for the Gaussian walk); the fit must recover D
+    within 3 %."""
+    dt, D, n = 50, 1e-9, 20000
+    lobe1, lobe2 = list(range(2000, 7000, dt)), list(range(12000, 17000, dt))
+    g_us = lobe1 + [7000] + lobe2 + [17000]
+    n_tp, te = 20050 // dt, 400
+    sigma2 = (1e-3 * math.sqrt(2.0 * D * dt)) ** 2
+    bs, logs = [], []
+    for G in (0.0, 60.0, 100.0, 140.0, 180.0):
+        gx = [G if t not in (7000, 17000) else 0.0 for t in g_us]
+        grad = np.zeros((len(g_us), 3), np.float32)
+        grad[:, 0] = gx
+        pr = _problem(n_spins=n, TR_us=20050, TE_us=(20000,), RF_FA=(90.0, 180.0),
+                      RF_PH=(0.0, 90.0), RF_us=(0, 10000), D=D, fov=1e-3, gradient_us=g_us,
+                      gradient_xyz=grad)
+        m = _m(run, pr)[:, 0]
+        logs.append(math.log(abs(np.mean(m[:, 0] + 1j * m[:, 1]))))
+        g = np.zeros(n_tp)
+        for t_us, gv in zip(g_us, gx):
+            g[t_us // dt] = gv * 1e-3 * dt * 1e-6 * GAMMA * (-1.0 if t_us // dt < 200 else 1.0)
+        tail = np.cumsum(g[:te + 1][::-1])[::-1]
+        bs.append(sigma2 * float(np.sum(tail ** 2)) / (2.0 * D))   # s/m^2
+    slope = np.polyfit(np.array(bs), np.array(logs), 1)[0]
+    assert abs(-slope / D - 1.0) < 0.03, -slope
+    # the discrete b agrees with Stejskal-Tanner, gamma^2 G^2 delta^2 (Delta - delta/3)
+    b_st = (GAMMA * 0.18 * 5e-3) ** 2 * (10e-3 - 5e-3 / 3)
+    assert abs(bs[-1] / b_st - 1.0) < 0.02, (bs[-1], b_st)        # ~483 s/mm^2

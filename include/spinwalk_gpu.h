@@ -272,7 +272,7 @@ int sw_sim_tracks(const sw_params *param, const sw_sequence *seq, const sw_track
  * The caller passes device inputs and outputs exactly as for sw_sim_device (FP32 precision, no
  * FP64 shadow). All other device memory comes from one static array of SW_NOALLOC_SCRATCH_BYTES
  * that every GPU loading this part of the library keeps until the process exits. About 48 MiB of
- * it hold the logf correction table; the rest must fit the call: roughly 6 KiB per spin plus
+ * it hold the logf correction table; the rest must fit the call: roughly 8.5 KiB per spin plus
  * 8 bytes per voxel -- larger requests are rejected with SW_ERR_NOMEM and a message, never
  * partially run. No cudaMalloc/cudaFree or other device-allocating routine is called (host-side
  * staging of the small parameter tables uses ordinary host memory).

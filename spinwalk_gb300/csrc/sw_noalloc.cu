@@ -97,7 +97,7 @@ extern "C" int sw_sim_device_noalloc(const sw_params *p, const sw_sequence *q,
     if (need > avail)
         return fail(SW_ERR_NOMEM,
                     "sw_sim_device_noalloc: this problem needs " + std::to_string(need >> 20) +
-                        " MiB of scratch (about 6 KiB per spin + 8 B per voxel) but the static "
+                        " MiB of scratch (about 8.5 KiB per spin + 8 B per voxel) but the static "
                         "array has " + std::to_string(avail >> 20) + " MiB left after the logf "
                         "table; use fewer spins per call or sw_sim_device");
     const Layout L = layout(R.base + R.work_offset, p->n_spins, p->matrix_length,

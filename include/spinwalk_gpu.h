@@ -242,7 +242,7 @@ int sw_sync(void *stream);
  * sums) or SW_PREC_FP64 (M1 = the FP64 values rounded to float), as for sw_sim. A track's M1_fp64
  * (optional, host [n_spins][n_TE][3]) receives the FP64 shadow of that track: the steady-state
  * recurrence over all DUMMY_SCAN scans carried in double, bit-identical to sw_sim's M1_fp64 on
- * that instance. Generator flavour bits are not accepted (SW_RNG_MT19937 only).
+ * that instance. SW_RNG_MINSTD and SW_FIELD_BF16 may be OR-ed in, as for sw_sim.
  */
 typedef struct sw_track {
     float linear_phase_cycling;

@@ -571,8 +571,13 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
                              int precision) {
     int rc = check_args(param, seq);
     if (rc) return rc;
+    const bool bf16 = (precision & SW_FIELD_BF16) != 0;
+    const uint32_t rng = (uint32_t)precision & ~(uint32_t)(SW_PREC_MASK | SW_FIELD_BF16);
+    precision &= SW_PREC_MASK;
     if (precision != SW_PREC_FP32 && precision != SW_PREC_KAHAN && precision != SW_PREC_FP64)
         return fail(SW_ERR_INVALID, "tracks: precision must be SW_PREC_FP32, _KAHAN or _FP64");
+    if (rng != SW_RNG_MT19937 && rng != SW_RNG_MINSTD) return fail(SW_ERR_INVALID, "generator flavour");
+    const bool mt = rng == SW_RNG_MT19937;
     if (!tracks || n_tracks == 0) return fail(SW_ERR_INVALID, "no tracks");
     if (param->enRecordTrajectory) return fail(SW_ERR_INVALID, "tracks do not record trajectories");
     const size_t n = param->n_spins, nte = seq->n_TE, ml = (size_t)param->matrix_length;
@@ -683,7 +688,7 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
         o_S[t] = slot(n * 4);
         o_M1d[t] = slot(tracks[t].M1_fp64 ? n * nte * 24 : 0);
     }
-    const Layout Lm = layout(nullptr, n, param->matrix_length, 0, shadow);
+    const Layout Lm = layout(nullptr, n, param->matrix_length, 0, shadow, mt);
     const size_t o_ws = slot(Lm.bytes);
     if (off > C.size) {
         if (C.buf) cudaFree(C.buf);
@@ -731,8 +736,10 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     }
     TR_CUDA(cudaMemcpyAsync(d + o_ptrs, ptrs.data(), ptrs.size() * sizeof(void *), cudaMemcpyHostToDevice, st));
 
-    const Layout L = layout(d + o_ws, n, param->matrix_length, 0, shadow);
-    const sw::DevParams P = dev_params(&pw, seq);
+    const Layout L = layout(d + o_ws, n, param->matrix_length, 0, shadow, mt);
+    sw::DevParams P = dev_params(&pw, seq);
+    P.rng = rng;
+    P.field_bf16 = bf16 ? 1 : 0;
     const sw::DevTables Tb = dev_tables(im, d + o_tab);
     sw::GroupTables GT;
     GT.n_groups = ng;
@@ -765,8 +772,9 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
 
     uint32_t *lcnt = reinterpret_cast<uint32_t *>(d + o_lcnt);
     sw::BlochEvent *elog = reinterpret_cast<sw::BlochEvent *>(d + o_log);
-    const sw::LogfTables LT = sw::api::device_logf_tables();
+    sw::LogfTables LT = sw::api::device_logf_tables();
     if (!LT.bitmap) return fail(SW_ERR_CUDA, "logf tables unavailable");
+    if (!mt && !(LT.ms_delta = sw::api::minstd_delta_table())) return SW_ERR_CUDA;
     sw::Outputs O{nullptr, nullptr, reinterpret_cast<float *>(d + o_scratch_xyz), nullptr,
                   reinterpret_cast<int32_t *>(d + o_scratch_st)};
     g_timing = sw_timing{};
@@ -777,7 +785,8 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     TR_CUDA(cudaMemsetAsync(L.active, 0, 2 * sizeof(uint32_t), st));
     TR_CUDA(sw::launch_pack(reinterpret_cast<const uint8_t *>(d + o_mask),
                             has_field ? reinterpret_cast<const float *>(d + o_field) : nullptr,
-                            L.vox, param->matrix_length, param->n_substrate, L.active + 1, st));
+                            L.vox, param->matrix_length, param->n_substrate, L.active + 1, st,
+                            bf16));
     TR_CUDA(sw::launch_seed(P, L.G, st));
     TR_CUDA(sw::launch_init(P, Tb, L.vox, reinterpret_cast<const float *>(d + o_M0),
                             reinterpret_cast<const float *>(d + o_XYZ0), L.S, O, shadow, st));

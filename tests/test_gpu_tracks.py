@@ -105,8 +105,24 @@ def test_tracks_shadow_leaves_fp32_results_unchanged():
         assert err < 1e-4, err
 
 
-def test_tracks_reject_generator_flavour_bits():
+@pytest.mark.parametrize("flags", ["minstd", "bf16", "minstd_bf16_kahan"])
+def test_tracks_generator_flavour_and_field_records(flags):
+    """SW_RNG_MINSTD and SW_FIELD_BF16 in the tracks path equal sw_sim with the same flags on
+    each instance, bit for bit."""
     from spinwalk_gb300 import abi
+    prec = {"minstd": abi.SW_RNG_MINSTD, "bf16": abi.SW_FIELD_BF16,
+            "minstd_bf16_kahan": abi.SW_RNG_MINSTD | abi.SW_FIELD_BF16 | abi.SW_PREC_KAHAN}[flags]
+    pr, _ = load_golden("bssfp_phase_cycling")
+    tracks = [dict(linear_phase_cycling=lpc, n_dummy_scan=nd) for lpc in (0.0, 150.0)
+              for nd in (0, 2)]
+    outs = _lib.run_tracks(pr, tracks, fill=np.nan, precision=prec)
+    for t, got in zip(tracks, outs):
+        want = _lib.run(_instance(pr, t), precision=prec, fill=np.nan)
+        for k in ("M1", "XYZ1", "T", "status"):
+            assert bits_equal(got[k], want[k]), (flags, t, k)
+
+
+def test_tracks_reject_unknown_flag_bits():
     pr, _ = load_golden("gre")
     with pytest.raises(_lib.SpinWalkError):
-        _lib.run_tracks(pr, [dict(n_dummy_scan=0)], precision=abi.SW_PREC_FP32 | abi.SW_RNG_MINSTD)
+        _lib.run_tracks(pr, [dict(n_dummy_scan=0)], precision=0x400)

@@ -106,20 +106,7 @@ void build_tables(const sw_params *p, const sw_sequence *q, TableImage &im) {
     std::vector<sw::RfOp> rf, scan;
     sw::build_rf(p, q, rf);
     sw::build_scan_rf(p, q, scan);
-    // the step std-dev split for the integer multiply (positive normal values only)
-    std::vector<uint32_t> dsplit(4 * (size_t)ns, 0u);
-    for (uint32_t i = 0; i < ns; i++) {
-        uint64_t b;
-        std::memcpy(&b, &q->diffusivity[i], 8);
-        const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
-        const bool ok = (b >> 63) == 0 && e != 0 && e != 0x7ff;
-        dsplit[4 * i + 0] = (uint32_t)b;
-        dsplit[4 * i + 1] = (uint32_t)((b >> 32) & 0xfffffu) | 0x100000u;
-        dsplit[4 * i + 2] = (uint32_t)((int32_t)e - 1023);
-        dsplit[4 * i + 3] = ok ? 1u : 0u;
-    }
     im.o_dscale = im.put(q->diffusivity, ns);
-    im.o_dsplit = im.put(dsplit.data(), dsplit.size());
     im.o_T1f = im.put(T1f.data(), ns);
     im.o_T2f = im.put(T2f.data(), ns);
     im.o_T1d = im.put(T1d.data(), ns);
@@ -139,7 +126,6 @@ void build_tables(const sw_params *p, const sw_sequence *q, TableImage &im) {
 sw::DevTables dev_tables(const TableImage &im, const char *d) {
     sw::DevTables t{};
     t.dscale = reinterpret_cast<const double *>(d + im.o_dscale);
-    t.dsplit = reinterpret_cast<const uint32_t *>(d + im.o_dsplit);
     t.T1f = reinterpret_cast<const float *>(d + im.o_T1f);
     t.T2f = reinterpret_cast<const float *>(d + im.o_T2f);
     t.T1d = reinterpret_cast<const double *>(d + im.o_T1d);

@@ -30,12 +30,12 @@ struct Carve {
 struct TableImage {
     std::vector<char> bytes;
     static constexpr size_t kUnset = ~size_t(0);
-    size_t o_dscale = kUnset, o_dsplit = kUnset, o_T1f = kUnset, o_T2f = kUnset, o_T1d = kUnset,
+    size_t o_dscale = kUnset, o_T1f = kUnset, o_T2f = kUnset, o_T1d = kUnset,
            o_T2d = kUnset, o_pXY = kUnset, o_rf = kUnset, o_scan = kUnset, o_te = kUnset,
            o_dtp = kUnset, o_ddeg = kUnset, o_gtp = kUnset, o_gx = kUnset, o_gy = kUnset,
            o_gz = kUnset;
     bool complete() const {
-        for (size_t o : {o_dscale, o_dsplit, o_T1f, o_T2f, o_T1d, o_T2d, o_pXY, o_rf, o_scan,
+        for (size_t o : {o_dscale, o_T1f, o_T2f, o_T1d, o_T2d, o_pXY, o_rf, o_scan,
                          o_te, o_dtp, o_ddeg, o_gtp, o_gx, o_gy, o_gz})
             if (o == kUnset) return false;
         return true;

@@ -194,40 +194,6 @@ __device__ __forceinline__ double f2d_exact(float f) {
     return __hiloint2double((int)hi, (int)(m << 29));
 }
 
-// RN((double)n * s) for a float n (0 or normal) and a positive normal double s given split as
-// s_lo (low 32 significand bits), s_hi (high 21 bits incl. the hidden bit) and es (unbiased
-// exponent): the exact 77-bit product of the significands from two 32x32->64 multiplies, rounded
-// to 53 bits to nearest-even by hand. Bit-identical to the IEEE double multiply, without the
-// FP64 pipe.
-__device__ __forceinline__ uint64_t mul_fd(float n, uint32_t s_lo, uint32_t s_hi, int es) {
-    const uint32_t b = __float_as_uint(n);
-    const uint32_t en = (b >> 23) & 0xffu;
-    if (en == 0u) return (uint64_t)(b & 0x80000000u) << 32;             // +-0
-    const uint32_t mn = (b & 0x7fffffu) | 0x800000u;
-    const uint64_t t = (uint64_t)mn * s_lo, u = (uint64_t)mn * s_hi;
-    const uint32_t p0 = (uint32_t)t;
-    const uint64_t mid = (t >> 32) + (uint32_t)u;
-    const uint32_t p1 = (uint32_t)mid;
-    const uint32_t p2 = (uint32_t)(u >> 32) + (uint32_t)(mid >> 32);   // product < 2^77
-    const uint32_t top = p2 >> 12;                                      // product >= 2^76
-    const uint32_t sh = 23u + top;
-    uint32_t r_lo = __funnelshift_r(p0, p1, sh);
-    uint32_t r_hi = __funnelshift_r(p1, p2, sh);
-    const uint32_t rb = (p0 >> (sh - 1u)) & 1u;
-    const uint32_t st = p0 & ((1u << (sh - 1u)) - 1u);
-    const uint32_t up = rb & ((st != 0u) | (r_lo & 1u));
-    const uint32_t nl = r_lo + up;
-    r_hi += (nl < r_lo);
-    r_lo = nl;
-    int e = (int)en - 127 + es + (int)top;
-    if (r_hi >> 21) {            // rounded up to 2^53
-        r_hi >>= 1;
-        e += 1;
-    }
-    const uint32_t hi = (b & 0x80000000u) | ((uint32_t)(e + 1023) << 20) | (r_hi & 0xfffffu);
-    return ((uint64_t)hi << 32) | r_lo;
-}
-
 // v < 0 and v >= bound (bound > 0) on the bit patterns (positive doubles order as integers).
 __device__ __forceinline__ bool dneg(uint64_t v) {
     return (int64_t)v < 0 && (v & 0x7fffffffffffffffull) != 0u;
@@ -293,7 +259,6 @@ struct WalkRegs {
     uint32_t ts_old;          // substrate of the last accepted voxel
     float field;              // its field (deg per step)
     double dscale;            // its step std-dev
-    uint4 dsp;                // dscale split for mul_fd
     uint32_t itr;             // consecutive rejected moves
     uint32_t nh, nc, uh, uc;  // ring buffer heads / counts
 };
@@ -312,8 +277,7 @@ __device__ __forceinline__ int walk_move(WalkRegs &w, uint64_t (&xn)[3], const D
         for (int i = 0; i < 3; i++) {
             const float g = nb[w.nh];
             w.nh = (w.nh + 1 == kNormBuf) ? 0 : w.nh + 1;
-            const uint64_t rnd = w.dsp.w ? mul_fd(g, w.dsp.x, w.dsp.y, (int)w.dsp.z)
-                                         : dbits(f2d_exact(g) * w.dscale);
+            const uint64_t rnd = dbits(f2d_exact(g) * w.dscale);   // hardware DMUL
             uint64_t v = dadd_fp64(w.xo[i], rnd);   // w.xo[i] + rnd
             // the wrap in integer arithmetic too: the compiler evaluates a cheap double
             // expression here on every step whatever the branch, on the slow FP64 unit
@@ -343,7 +307,6 @@ __device__ __forceinline__ int walk_move(WalkRegs &w, uint64_t (&xn)[3], const D
         w.ind_old = ind;
         w.field = __uint_as_float(v.x);
         w.dscale = __ldg(Tb.dscale + w.ts_old);
-        w.dsp = __ldg(reinterpret_cast<const uint4 *>(Tb.dsplit) + w.ts_old);
     }
     w.itr = 0;
     return kMoveAccepted;

@@ -456,7 +456,6 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
     uint32_t ts_old = flags & 0xffu;
     bool started = (flags & kFlagStarted) != 0;
     double dscale = __ldg(Tb.dscale + ts_old);
-    uint4 dsp = __ldg(reinterpret_cast<const uint4 *>(Tb.dsplit) + ts_old);
 
     uint32_t nh = G.nhead[spin], nc = G.ncnt[spin], uh = G.uhead[spin], uc = G.ucnt[spin];
     const float *nb = G.nbuf + (size_t)spin * kNormBuf;
@@ -527,8 +526,7 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
             for (int i = 0; i < 3; i++) {
                 const float g = nb[nh];
                 nh = (nh + 1 == kNormBuf) ? 0 : nh + 1;
-                const uint64_t rnd = dsp.w ? mul_fd(g, dsp.x, dsp.y, (int)dsp.z)
-                                           : dbits(f2d_exact(g) * dscale);
+                const uint64_t rnd = dbits(f2d_exact(g) * dscale);   // hardware DMUL
                 uint64_t v = dadd_fp64(xo[i], rnd);  // xo[i] + rnd
                 // the wrap in integer arithmetic too: the compiler evaluates a cheap double
                 // expression here on every step whatever the branch, on the slow FP64 unit
@@ -562,7 +560,6 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
             ind_old = ind;
             field = __uint_as_float(v.x);
             dscale = __ldg(Tb.dscale + ts_old);
-            dsp = __ldg(reinterpret_cast<const uint4 *>(Tb.dsplit) + ts_old);
         }
         // ---- phase accumulation (kernels.cu:171-172) ----
         if (KAHAN) kahan_add(acc, acc_e, field); else acc += field;

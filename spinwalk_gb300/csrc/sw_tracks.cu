@@ -206,7 +206,6 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
     w.ts_old = flags & 0xffu;
     w.field = S.field[spin];
     w.dscale = __ldg(Tb.dscale + w.ts_old);
-    w.dsp = __ldg(reinterpret_cast<const uint4 *>(Tb.dsplit) + w.ts_old);
     w.itr = S.itr[spin];
     w.nh = G.nhead[spin]; w.nc = G.ncnt[spin]; w.uh = G.uhead[spin]; w.uc = G.ucnt[spin];
     const float *nb = G.nbuf + (size_t)spin * kNormBuf;

@@ -54,7 +54,6 @@ struct DevParams {
 // Small read-only tables (device pointers into one allocation).
 struct DevTables {
     const double *dscale;     // [ns] step std-dev (m)
-    const uint32_t *dsplit;   // [ns][4] dscale split for mul_fd: s_lo, s_hi, es, usable (1/0)
     const float *T1f, *T2f;   // [ns] float(T1_ms*1e-3) as the reference stores it (kernels.cu:167)
     const double *T1d, *T2d;  // [ns] T1_ms*1e-3 in double (FP64 path)
     const float *pXY;         // [ns*ns]

@@ -477,6 +477,11 @@ int sw_debug_ms_normal(uint32_t x_lo, uint32_t n, float *d_y, void *stream);
  * tests. */
 int sw_debug_dadd(const double *d_a, const double *d_b, double *d_y, uint64_t n, void *stream);
 
+/* Host-visible check of the walk's gradient-phase arithmetic: d_y[i] = (float)d_x[i] (round to
+ * nearest even) by the integer conversion the walk uses, on n device doubles -- used by the
+ * tests. */
+int sw_debug_d2f(const double *d_x, float *d_y, uint64_t n, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -96,6 +96,7 @@ def lib():
         L.sw_debug_logf.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
         L.sw_debug_ms_normal.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
         L.sw_debug_dadd.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
+        L.sw_debug_d2f.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
         if L.sw_abi_version() != 1:
             raise SpinWalkError("libspinwalk_gpu ABI version mismatch")
         _lib = L
@@ -455,6 +456,10 @@ def run_tracks(problem, tracks, fill=0.0, precision=abi.SW_PREC_FP32, fp64=False
                               len(tracks), _p(problem.field), _p(problem.mask), _p(problem.M0),
                               _p(problem.XYZ0), int(precision)))
     return outs
+
+
+def debug_d2f(d_x, d_y, n, stream=None):
+    check(lib().sw_debug_d2f(d_x, d_y, C.c_uint64(n), stream))
 
 
 def debug_dadd(d_a, d_b, d_y, n, stream=None):

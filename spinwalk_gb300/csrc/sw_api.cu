@@ -600,6 +600,12 @@ int sw_debug_dadd(const double *d_a, const double *d_b, double *d_y, uint64_t n,
     return SW_OK;
 }
 
+int sw_debug_d2f(const double *d_x, float *d_y, uint64_t n, void *stream) {
+    if (!d_x || !d_y) return fail(SW_ERR_INVALID, "null device buffer");
+    SW_CUDA(sw::launch_debug_d2f(d_x, d_y, n, (cudaStream_t)stream));
+    return SW_OK;
+}
+
 int sw_debug_ms_normal(uint32_t x_lo, uint32_t n, float *d_y, void *stream) {
     if (!d_y) return fail(SW_ERR_INVALID, "null device buffer");
     const uint32_t *delta = minstd_delta_table();

@@ -194,6 +194,47 @@ __device__ __forceinline__ double f2d_exact(float f) {
     return __hiloint2double((int)hi, (int)(m << 29));
 }
 
+// float(d) for a double given as its bit pattern, rounded to nearest even, with integer
+// operations where the result is a normal float; zero, subnormal, overflowing and non-finite
+// values take the hardware conversion (out of line, so that it is not evaluated on every call).
+#if defined(__CUDA_ARCH__)
+__device__ __noinline__ float d2f_hw(uint64_t b) { return (float)__longlong_as_double((long long)b); }
+#else
+__device__ float d2f_hw(uint64_t b);
+#endif
+__device__ __forceinline__ float d2f_exact(uint64_t b) {
+    const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    if (e - (1023u - 126u) > 253u) return d2f_hw(b);           // float exponent outside 1..254
+    const uint32_t mf = ((hi & 0xfffffu) << 3) | (lo >> 29);    // top 23 significand bits
+    const uint32_t rem = lo & 0x1fffffffu, half = 0x10000000u;
+    const uint32_t up = (rem > half) | ((rem == half) & (mf & 1u));
+    // a carry out of the significand steps the exponent, up to infinity, as rounding does
+    return __uint_as_float((hi & 0x80000000u) + (((e - 1023u + 127u) << 23) | mf) + up);
+}
+
+// The reference's gradient phase in degrees (kernels.cu:181-187),
+//   ((gx x + gy y + gz z) * 1e-3 * dt * 1e-6 * GAMMA * RAD2DEG),
+// every operation rounded as there. A lobe along one axis has two zero coefficients: their
+// products are +-0 and leave a nonzero product unchanged, so only the nonzero one is formed; a
+// zero product, or more than one nonzero coefficient, takes the full sum (sign of zero included).
+__device__ __forceinline__ double grad_phase_deg(float gx, float gy, float gz, const uint64_t (&x)[3],
+                                                 double dt_us) {
+    const bool nx = (__float_as_uint(gx) << 1) != 0u, ny = (__float_as_uint(gy) << 1) != 0u,
+               nz = (__float_as_uint(gz) << 1) != 0u;
+    double s = 0.;
+    bool full = (int)nx + (int)ny + (int)nz != 1;
+    if (!full) {
+        const float g1 = nx ? gx : (ny ? gy : gz);
+        const uint64_t x1 = nx ? x[0] : (ny ? x[1] : x[2]);
+        s = f2d_exact(g1) * dfrom(x1);
+        full = (__double_as_longlong(s) << 1) == 0;
+    }
+    if (full)
+        s = f2d_exact(gx) * dfrom(x[0]) + f2d_exact(gy) * dfrom(x[1]) + f2d_exact(gz) * dfrom(x[2]);
+    return s * 1e-3 * dt_us * 1e-6 * kGamma * kRad2Deg;
+}
+
 // v < 0 and v >= bound (bound > 0) on the bit patterns (positive doubles order as integers).
 __device__ __forceinline__ bool dneg(uint64_t v) {
     return (int64_t)v < 0 && (v & 0x7fffffffffffffffull) != 0u;

@@ -577,16 +577,14 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
         }
         // ---- gradient (kernels.cu:181-187) ----
         if (tp == t_grad) {
-            const double g = ((double)__ldg(Tb.gx + c_grad) * dfrom(xn[0]) +
-                              (double)__ldg(Tb.gy + c_grad) * dfrom(xn[1]) +
-                              (double)__ldg(Tb.gz + c_grad) * dfrom(xn[2])) *
-                             1e-3 * (double)P.timestep_us * 1e-6 * kGamma * kRad2Deg;
+            const double g = grad_phase_deg(__ldg(Tb.gx + c_grad), __ldg(Tb.gy + c_grad),
+                                            __ldg(Tb.gz + c_grad), xn, (double)P.timestep_us);
             if (KAHAN) {
-                const float ghi = (float)g;
+                const float ghi = d2f_exact(dbits(g));
                 kahan_add(acc, acc_e, ghi);
-                kahan_add(acc, acc_e, (float)(g - (double)ghi));
+                kahan_add(acc, acc_e, d2f_exact(dadd_fp64(dbits(g), dflip(dbits(f2d_exact(ghi))))));
             } else {
-                acc = (float)((double)acc + g);
+                acc = d2f_exact(dadd_fp64(dbits(f2d_exact(acc)), dbits(g)));   // (float)((double)acc + g)
             }
             if (DBL) accd += g;
             c_grad++;
@@ -703,6 +701,12 @@ __global__ void k_debug_logf(const float *x, float *y, uint64_t n, LogfTables L)
         y[i] = logf_libm(x[i], s_tab, L);
 }
 
+__global__ void k_debug_d2f(const double *x, float *y, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        y[i] = d2f_exact(dbits(x[i]));
+}
+
 __global__ void k_debug_dadd(const double *a, const double *b, double *y, uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x)
@@ -798,6 +802,11 @@ cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevT
         k_walk<SW_PREC_FP32, true><<<g, block, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi, order);
     else
         k_walk<SW_PREC_FP32, false><<<g, block, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi, order);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_d2f(const double *x, float *y, uint64_t n, cudaStream_t st) {
+    k_debug_d2f<<<grid_for((int64_t)n, 256, 152 * 16), 256, 0, st>>>(x, y, n);
     return cudaGetLastError();
 }
 

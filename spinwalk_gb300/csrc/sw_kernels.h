@@ -39,6 +39,7 @@ cudaError_t launch_walk(int prec, bool dbl, const DevParams &P, const DevTables 
                         const Outputs &O, uint32_t *active, cudaStream_t st);
 cudaError_t launch_debug_dadd(const double *a, const double *b, double *y, uint64_t n,
                               cudaStream_t st);
+cudaError_t launch_debug_d2f(const double *x, float *y, uint64_t n, cudaStream_t st);
 cudaError_t launch_debug_ms_normal(uint32_t x_lo, uint32_t n, float *y, const uint32_t *delta,
                                    cudaStream_t st);
 cudaError_t launch_debug_logf(const float *x, float *y, uint64_t n, const LogfTables &L,

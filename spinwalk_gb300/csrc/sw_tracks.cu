@@ -316,12 +316,11 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
             t_dph = c_dph < P.n_dephasing ? (uint32_t)Tb.dph_tp[c_dph] : NONE;
         }
         if (tp == t_grad) {                                         // kernels.cu:181-187
-            const double g = ((double)__ldg(Tb.gx + c_grad) * dfrom(xn[0]) +
-                              (double)__ldg(Tb.gy + c_grad) * dfrom(xn[1]) +
-                              (double)__ldg(Tb.gz + c_grad) * dfrom(xn[2])) *
-                             1e-3 * (double)P.timestep_us * 1e-6 * kGamma * kRad2Deg;
+            const double g = grad_phase_deg(__ldg(Tb.gx + c_grad), __ldg(Tb.gy + c_grad),
+                                            __ldg(Tb.gz + c_grad), xn, (double)P.timestep_us);
             if (KAHAN) {
-                const float ghi = (float)g, glo = (float)(g - (double)ghi);
+                const float ghi = d2f_exact(dbits(g));
+                const float glo = d2f_exact(dadd_fp64(dbits(g), dflip(dbits(f2d_exact(ghi)))));
                 kahan_add(acc, acc_e, ghi);
                 kahan_add(acc, acc_e, glo);
                 if (rec_started) {
@@ -329,8 +328,8 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
                     kahan_add(acc_rec, acc_rec_e, glo);
                 }
             } else {
-                acc = (float)((double)acc + g);
-                if (rec_started) acc_rec = (float)((double)acc_rec + g);
+                acc = d2f_exact(dadd_fp64(dbits(f2d_exact(acc)), dbits(g)));
+                if (rec_started) acc_rec = d2f_exact(dadd_fp64(dbits(f2d_exact(acc_rec)), dbits(g)));
             }
             if (SHADOW) {
                 accd += g;

@@ -213,6 +213,39 @@ def test_gpu_integer_double_add_matches_ieee():
     assert same.all(), f"{(~same).sum()} mismatches, first a={A[~same][0]!r} b={B[~same][0]!r}"
 
 
+def test_gpu_integer_double_to_float_matches_ieee():
+    """Device d2f_exact (the walk's gradient-phase conversion) == IEEE double -> float rounding to
+    nearest even (numpy) on every exponent, ties, carries into the exponent, the float range's
+    edges (overflow, subnormal results), zeros and non-finite values."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(12)
+    n = 1 << 21
+    e = rng.integers(0, 2047, n, dtype=np.uint64)
+    frac = rng.integers(0, 1 << 52, n, dtype=np.uint64)
+    sign = rng.integers(0, 2, n, dtype=np.uint64) << np.uint64(63)
+    rnd = (sign | (e << np.uint64(52)) | frac).view(np.float64)
+    near = (sign | (rng.integers(880, 1170, n, dtype=np.uint64) << np.uint64(52)) | frac)
+    # ties (low 29 bits exactly half), just above / below, all-ones significands (carry)
+    tie = (near & ~np.uint64(0x1fffffff)) | np.uint64(0x10000000)
+    above, below = tie + np.uint64(1), tie - np.uint64(1)
+    ones = near | np.uint64(0x000fffffffffffff)
+    walk = (rng.standard_normal(n) * 1e3).astype(np.float64)
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 3.4028235677973366e38,
+                        3.4028234663852886e38, 1.1754943508222875e-38, 1.1754942e-38, 1e-45,
+                        7e-46, 1.4e-45, 5e-324, -5e-324], np.float64)
+    X = np.concatenate([rnd, near.view(np.float64), tie.view(np.float64), above.view(np.float64),
+                        below.view(np.float64), ones.view(np.float64), walk, special])
+    dX = torch.from_numpy(X).cuda()
+    dY = torch.empty(X.size, dtype=torch.float32, device="cuda")
+    _lib.debug_d2f(dX.data_ptr(), dY.data_ptr(), X.size)
+    torch.cuda.synchronize()
+    got = dY.cpu().numpy()
+    with np.errstate(all="ignore"):
+        want = X.astype(np.float32)
+    same = (got.view(np.uint32) == want.view(np.uint32)) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), f"{(~same).sum()} mismatches, first x={X[~same][0]!r}"
+
+
 def test_smoke_entry_point_passes():
     """The build's smoke check (one small GRE walk against the oracle) passes."""
     import __graft_entry__

@@ -46,14 +46,15 @@ SEED_BYTES_PER_SPIN = 2 * 624 * 4 + 6 * 4   # two mt19937 states + 6 ring/index 
 # scaled to a full launch by the units it processes (both grow in proportion)
 SEED_DRAM_BYTES_PER_SPIN = 4713.0
 MT_BYTES_PER_SPIN_STEP = 3.82 * 8        # MT words drawn per step x (4 B read + 4 B write)
-WALK_FP64_OPS_PER_SPIN_STEP = 3          # x, y, z position additions (the rest is integer)
+WALK_FP64_OPS_PER_SPIN_STEP = 6          # x, y, z step multiplies and position additions
 FP64_PEAK_GFLOPS = 152 * 2 * 2070e6 / 1e9  # 2 FP64 lanes per clock per SM at 2070 MHz
 USEFUL_BYTES_PER_SPIN_STEP = 5           # 1 B mask + 4 B field at the visited voxel
-WALK_DRAM_BYTES_PER_SPIN_STEP = 26.4
+WALK_DRAM_BYTES_PER_SPIN_STEP = 26.0
 SEED_LIMITER = ("integer instruction issue (ncu: ALU pipe 83 %, issue 74 %, DRAM 2 %): "
                 "7.7 lane instructions per MT word, not HBM")
-WALK_LIMITER = ("latency of the voxel gather (ncu: issue 47 %, long-scoreboard stalls, "
-                "DRAM 10 %, FP64 pipe 40 % for the 3 position additions)")
+WALK_LIMITER = ("FP64 pipe (ncu: 64 %, 3 position additions + 3 step multiplies per step at 2 "
+                "lanes/clock/SM) and the latency of the voxel gather (issue 38 %, long-scoreboard "
+                "stalls, DRAM 10 %)")
 
 
 def workload(name, rank=0):

@@ -213,9 +213,13 @@ def cpu_sample_ids(n_spins, n_sample):
     return np.unique(np.linspace(0, n_spins - 1, n_sample).round().astype(np.uint32))
 
 
-def time_cpu(pr, n_sample, threads=0):
+def time_cpu(pr, n_sample, threads=0, lowest=False):
+    """The oracle port on `threads` host threads over n_sample spin ids: stratified over the
+    whole range (end to end, the per-spin discard included), or the lowest ids (lowest=True:
+    discard(seed + spin) of a few thousand words, i.e. the walk-only rate)."""
     from tests import oracle_lib
-    ids = cpu_sample_ids(pr.params.n_spins, n_sample)
+    ids = (np.arange(min(n_sample, pr.params.n_spins), dtype=np.uint32) if lowest
+           else cpu_sample_ids(pr.params.n_spins, n_sample))
     outs = pr.outputs()
     t = time.perf_counter()
     oracle_lib.run(pr, spin_ids=ids, n_threads=threads, outputs=outs)
@@ -412,9 +416,14 @@ def run_ours(args, world, rank, local):
     if world == 1 or rank == 0:
         if args.cpu_sample > 0:
             rate, ns, dt = time_cpu(pr, args.cpu_sample, os.cpu_count())
+            wrate, wns, wdt = time_cpu(pr, max(1, args.cpu_sample // 4), os.cpu_count(),
+                                       lowest=True)
             cpu = {"value": rate, "unit": "spin-steps/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"{ns} stratified spin ids of {n} ({pr.params.n_timepoints} time "
-                             f"points each, {dt:.1f} s wall on {os.cpu_count()} threads)"}
+                             f"points each, {dt:.1f} s wall on {os.cpu_count()} threads)",
+                   "walk_only": {"value": wrate, "unit": "spin-steps/s",
+                                 "sample": f"spin ids 0..{wns - 1} (discard of at most "
+                                           f"{int(pr.params.seed) + wns} words), {wdt:.1f} s wall"}}
     line = {
         "metric": "spin-steps/s", "value": value, "unit": "spin-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,

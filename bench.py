@@ -294,11 +294,12 @@ def apply_tuning(args, pr=None):
         best, table = _lib.autotune(pr, apply=True)
         info = {"autotuned": True, "probe_s": time.perf_counter() - t0, "table": table}
     if args.resort_interval is not None or args.walk_block is not None or \
-            args.seed_chunks is not None:
+            args.seed_chunks is not None or args.round_streams is not None:
         cur = _lib.get_tuning()
         _lib.set_tuning(cur["resort_interval"] if args.resort_interval is None else args.resort_interval,
                         cur["walk_block"] if args.walk_block is None else args.walk_block,
-                        cur["seed_chunks"] if args.seed_chunks is None else args.seed_chunks)
+                        cur["seed_chunks"] if args.seed_chunks is None else args.seed_chunks,
+                        cur["round_streams"] if args.round_streams is None else args.round_streams)
     info["applied"] = _lib.get_tuning()
     return info
 
@@ -400,14 +401,17 @@ def run_ours(args, world, rank, local):
     # walk-only rate (refill + walk kernels, generator seeding excluded) and the secondary
     # ceilings: MT-state traffic of the refill (3.82 words of 8 B read+write per step) and the
     # FP64 work of the walk (3 position additions per step, 2 FP64 lanes per clock per SM)
-    walk_refill_s = (walk_ms + refill_ms) / args.steps * 1e-3
+    # wall time of the rounds: the call minus its seeding stage (the kernel times of the two
+    # halves of the rounds overlap, so their sum would overstate it)
+    walk_refill_s = ms / args.steps * 1e-3 - seed_ms / args.steps * 1e-3
     secondary = {
         "walk_only_spin_steps_per_s": spin_steps / walk_refill_s,
         "refill_mt_state_gbs": spin_steps * MT_BYTES_PER_SPIN_STEP / (refill_ms / args.steps * 1e-3) / 1e9,
         "walk_fp64_gflops": spin_steps * WALK_FP64_OPS_PER_SPIN_STEP / (walk_ms / args.steps * 1e-3) / 1e9,
         "fp64_peak_gflops": FP64_PEAK_GFLOPS,
         "useful_gather_gbs": spin_steps * USEFUL_BYTES_PER_SPIN_STEP / (walk_ms / args.steps * 1e-3) / 1e9,
-        "note": "kernel times overlap nothing (one stream); ncu: k_walk L2 hit rate and FP64 pipe "
+        "note": "walk-only = call time minus the seeding stage; the refill and walk kernel times "
+                "of the two halves of the rounds overlap; ncu: k_walk L2 hit rate and FP64 pipe "
                 "in profiles/",
     }
     errors = precision_errors(pr) if args.workload in ("se", "small") else None
@@ -434,6 +438,9 @@ def run_ours(args, world, rank, local):
                        field_records="bfloat16, 4 B per voxel" if args.field_bf16
                        else "float32, 8 B per voxel"),
         "kernel_ms_per_step": {k: v / args.steps for k, v in parts.items()},
+        "kernel_ms_note": "sums of launch durations; the refill/walk rounds run as two halves on "
+                          "two streams whose kernels overlap, so walk + refill exceed their wall "
+                          "time",
         "roofline": dict(roof, dominant_stage=dominant),
         "roofline_walk": walk_roof,
         "secondary_ceilings": secondary,
@@ -775,6 +782,8 @@ def main():
                     help="serve workload: requests in signal mode (no per-spin outputs)")
     ap.add_argument("--field-bf16", action="store_true",
                     help="bfloat16 fieldmap records (SW_FIELD_BF16); reports their error")
+    ap.add_argument("--round-streams", type=int, default=None,
+                    help="refill/walk rounds as this many independent halves on own streams (1, 2)")
     ap.add_argument("--seed-chunks", type=int, default=None,
                     help="seed/walk pipeline chunks (1 = seed all first, 0 = auto)")
     args = ap.parse_args()

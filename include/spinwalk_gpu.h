@@ -313,12 +313,17 @@ int sw_last_timing(sw_timing *out);
  *                     high-priority stream meanwhile (0 or 1 = seed everything, then walk;
  *                     at most 64). Off by default: the co-resident kernels slow each other down
  *                     by about what the overlap saves.
+ *   round_streams   : sw_sim / sw_sim_device run the refill/walk rounds of the spins as this
+ *                     many independent halves on their own streams (1 = one, 2 = two, 0 = auto:
+ *                     two from 2^17 spins on), so that one half's walk overlaps the other
+ *                     half's refill
  */
 typedef struct sw_tuning {
     uint32_t resort_interval;
     uint32_t walk_block;
     uint32_t seed_chunks;
-    uint32_t reserved[5];
+    uint32_t round_streams;
+    uint32_t reserved[4];
 } sw_tuning;
 int sw_set_tuning(const sw_tuning *t);
 int sw_get_tuning(sw_tuning *t);

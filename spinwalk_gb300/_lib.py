@@ -196,12 +196,12 @@ def run_config(ini_path, device=0):
     check(lib().sw_run_config(str(ini_path).encode(), int(device)))
 
 
-def set_tuning(resort_interval=0, walk_block=256, seed_chunks=0):
+def set_tuning(resort_interval=0, walk_block=256, seed_chunks=0, round_streams=0):
     """sw_set_tuning: Morton re-sort interval (walk rounds, 0 = never), walk block size and seed
     chunks of the seed/walk pipeline (0 = auto) for every later call of this process. Results do
     not depend on it."""
     t = abi.SwTuning(resort_interval=int(resort_interval), walk_block=int(walk_block),
-                     seed_chunks=int(seed_chunks))
+                     seed_chunks=int(seed_chunks), round_streams=int(round_streams))
     check(lib().sw_set_tuning(C.byref(t)))
 
 
@@ -209,7 +209,7 @@ def get_tuning():
     t = abi.SwTuning()
     check(lib().sw_get_tuning(C.byref(t)))
     return dict(resort_interval=t.resort_interval, walk_block=t.walk_block,
-                seed_chunks=t.seed_chunks)
+                seed_chunks=t.seed_chunks, round_streams=t.round_streams)
 
 
 def autotune(problem, apply=False):
@@ -225,7 +225,7 @@ def autotune(problem, apply=False):
     table = [dict(resort_interval=e.resort_interval, walk_block=e.walk_block,
                   ms_per_round=e.ms_per_round, sort_ms=e.sort_ms) for e in tab[:n.value]]
     return dict(resort_interval=best.resort_interval, walk_block=best.walk_block,
-                seed_chunks=best.seed_chunks), table
+                seed_chunks=best.seed_chunks, round_streams=best.round_streams), table
 
 
 def last_timing():

@@ -126,7 +126,8 @@ class SwTuning(C.Structure):
         ("resort_interval", C.c_uint32),
         ("walk_block", C.c_uint32),
         ("seed_chunks", C.c_uint32),
-        ("reserved", C.c_uint32 * 5),
+        ("round_streams", C.c_uint32),
+        ("reserved", C.c_uint32 * 4),
     ]
 
 

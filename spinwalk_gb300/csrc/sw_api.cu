@@ -186,7 +186,7 @@ Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl, bo
     G.ucnt = c.take<uint32_t>(n);
     L.Q.order = c.take<uint32_t>(n);
     L.Q.key = c.take<uint32_t>(n);
-    L.Q.hist = c.take<uint32_t>(sw::order_hist_words());
+    L.Q.hist = c.take<uint32_t>(2 * sw::order_hist_words());   // one histogram per half of the rounds
     L.bytes = c.off + 256;
     return L;
 }
@@ -213,6 +213,7 @@ struct DeviceCtx {
     std::vector<cudaEvent_t> ev;           // timing events: 4 call-level, then 3 per round
     cudaStream_t seed_st = nullptr;        // lowest priority: seeding of the chunks
     cudaStream_t walk_st = nullptr;        // highest priority: pack, init, refill, walk
+    cudaStream_t walk_st2 = nullptr;       // highest priority: the second half's rounds
     std::vector<cudaEvent_t> pev;          // pipeline: start, done, seed chunk c done / timed
 };
 DeviceCtx g_ctx[kMaxDevices];
@@ -230,14 +231,15 @@ int ensure_logf(DeviceCtx &c) {
                        cudaMemcpyHostToDevice));
     SW_CUDA(cudaMemcpy(c.d_logf_bitmap, ex.bitmap.data(), ex.bitmap.size() * sizeof(uint32_t),
                        cudaMemcpyHostToDevice));
-    SW_CUDA(cudaMallocHost(&c.h_active, sizeof(uint32_t)));
+    SW_CUDA(cudaMallocHost(&c.h_active, 2 * sizeof(uint32_t)));
     c.ev.resize(3 * kMaxTimedChunks + 4);
     for (auto &e : c.ev) SW_CUDA(cudaEventCreate(&e));
     int lo_prio = 0, hi_prio = 0;
     SW_CUDA(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
     SW_CUDA(cudaStreamCreateWithPriority(&c.seed_st, cudaStreamNonBlocking, lo_prio));
     SW_CUDA(cudaStreamCreateWithPriority(&c.walk_st, cudaStreamNonBlocking, hi_prio));
-    c.pev.resize(2 + 2 * kMaxSeedChunks);
+    SW_CUDA(cudaStreamCreateWithPriority(&c.walk_st2, cudaStreamNonBlocking, hi_prio));
+    c.pev.resize(4 + 2 * kMaxSeedChunks);
     for (auto &e : c.pev) SW_CUDA(cudaEventCreate(&e));
     c.logf_ready = true;
     return SW_OK;
@@ -280,57 +282,85 @@ int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
                   const Layout &L, const sw::Outputs &O, const float *d_M0, const float *d_XYZ0,
                   uint32_t C, uint32_t &launches) {
     cudaEvent_t *ev = ctx.ev.data();
-    cudaStream_t ss = ctx.seed_st, ws = ctx.walk_st;
+    cudaStream_t ss = ctx.seed_st;
     const sw_tuning tu = current_tuning();
     const std::vector<uint32_t> b = seed_chunks(P, C);
     const uint64_t steps = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
     const uint64_t r0 = (steps + sw::kStepsPerRound - 1) / sw::kStepsPerRound;
     const uint64_t max_rounds = 64 + steps * (p->max_iterations + 2);
+    // the rounds run as H independent halves of the spins, half h on stream ws[h] with its own
+    // active counter (L.active[0] / [2])
+    // 0 = auto: two halves from 2^17 spins on (SE 1e6 spins: 192.1 -> 189.0 ms per call, the
+    // refill of one half overlapping the walk of the other)
+    const uint32_t want = tu.round_streams ? tu.round_streams : (P.n_spins >= (1u << 17) ? 2u : 1u);
+    const uint32_t H = (want == 2 && P.n_spins >= 2) ? 2u : 1u;
+    const cudaStream_t ws[2] = {ctx.walk_st, ctx.walk_st2};
+    const uint32_t hb[3] = {0u, H == 2 ? P.n_spins / 2 : P.n_spins, P.n_spins};
     uint32_t timed = 0;
-    // one refill + (re-sort) + walk round over spins [lo, hi) on the walk stream
-    auto round = [&](uint32_t lo, uint32_t hi, uint64_t r) -> int {
+    // one refill + (re-sort) + walk round over spins [lo, hi) of half h
+    auto round = [&](uint32_t h, uint32_t lo, uint32_t hi, uint64_t r) -> int {
+        cudaStream_t st = ws[h];
         const bool t = timed < kMaxTimedChunks;
         cudaEvent_t *e = ev + 4 + 3 * timed;
-        if (t) SW_CUDA(cudaEventRecord(e[0], ws));
-        SW_CUDA(sw::launch_refill_range(P, L.G, L.S.flags, LT, lo, hi, ws));
-        if (t) SW_CUDA(cudaEventRecord(e[1], ws));
+        if (t) SW_CUDA(cudaEventRecord(e[0], st));
+        SW_CUDA(sw::launch_refill_range(P, L.G, L.S.flags, LT, lo, hi, st));
+        if (t) SW_CUDA(cudaEventRecord(e[1], st));
         if (tu.resort_interval && r % tu.resort_interval == 0) {
-            SW_CUDA(sw::launch_order(P, L.S, L.Q, lo, hi, ws));
+            sw::OrderState Qh = L.Q;                    // each half sorts with its own histogram
+            Qh.hist = L.Q.hist + h * sw::order_hist_words();
+            SW_CUDA(sw::launch_order(P, L.S, Qh, lo, hi, st));
             launches += 3;
         }
-        SW_CUDA(sw::launch_walk_range(precision, dbl, P, Tb, L.vox, L.S, L.G, O, L.active, lo, hi,
-                                      ws, tu.resort_interval ? L.Q.order : nullptr,
+        SW_CUDA(sw::launch_walk_range(precision, dbl, P, Tb, L.vox, L.S, L.G, O, L.active + 2 * h,
+                                      lo, hi, st, tu.resort_interval ? L.Q.order : nullptr,
                                       (int)tu.walk_block));
-        if (t) SW_CUDA(cudaEventRecord(e[2], ws));
+        if (t) SW_CUDA(cudaEventRecord(e[2], st));
         if (t) timed++;
         launches += 2;
         return SW_OK;
     };
     // seeding of every chunk, each chunk bracketed by events (start, done)
     for (uint32_t c = 0; c < C; c++) {
-        SW_CUDA(cudaEventRecord(ctx.pev[2 + 2 * c], ss));
+        SW_CUDA(cudaEventRecord(ctx.pev[4 + 2 * c], ss));
         SW_CUDA(sw::launch_seed_range(P, L.G, b[c], b[c + 1], ss));
-        SW_CUDA(cudaEventRecord(ctx.pev[3 + 2 * c], ss));
+        SW_CUDA(cudaEventRecord(ctx.pev[5 + 2 * c], ss));
         launches++;
+    }
+    if (H == 2) {                          // the second stream starts after the call's pack
+        SW_CUDA(cudaEventRecord(ctx.pev[2], ws[0]));
+        SW_CUDA(cudaStreamWaitEvent(ws[1], ctx.pev[2], 0));
     }
     int rc;
-    uint64_t rounds = 0;
-    for (uint32_t c = 0; c < C; c++) {
-        if (b[c + 1] == b[c]) continue;
-        SW_CUDA(cudaStreamWaitEvent(ws, ctx.pev[3 + 2 * c], 0));
-        SW_CUDA(sw::launch_init_range(P, Tb, L.vox, d_M0, d_XYZ0, L.S, O, dbl, b[c], b[c + 1], ws));
-        launches++;
-        for (uint64_t r = 0; r < r0; r++)
-            if ((rc = round(b[c], b[c + 1], r))) return rc;
-    }
-    rounds = r0;
+    // the first r0 rounds (no spin can finish sooner) of each seeded piece, without waiting
+    for (uint32_t h = 0; h < H; h++)
+        for (uint32_t c = 0; c < C; c++) {
+            const uint32_t lo = std::max(b[c], hb[h]), hi = std::min(b[c + 1], hb[h + 1]);
+            if (hi <= lo) continue;
+            SW_CUDA(cudaStreamWaitEvent(ws[h], ctx.pev[5 + 2 * c], 0));
+            SW_CUDA(sw::launch_init_range(P, Tb, L.vox, d_M0, d_XYZ0, L.S, O, dbl, lo, hi, ws[h]));
+            launches++;
+            for (uint64_t r = 0; r < r0; r++)
+                if ((rc = round(h, lo, hi, r))) return rc;
+        }
+    uint64_t rounds = r0;
     for (;; rounds++) {
         if (rounds >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
-        SW_CUDA(cudaMemsetAsync(L.active, 0, sizeof(uint32_t), ws));
-        if ((rc = round(0, P.n_spins, rounds))) return rc;
-        SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active, sizeof(uint32_t), cudaMemcpyDeviceToHost, ws));
-        SW_CUDA(cudaStreamSynchronize(ws));
-        if (*ctx.h_active == 0) break;
+        for (uint32_t h = 0; h < H; h++) {
+            SW_CUDA(cudaMemsetAsync(L.active + 2 * h, 0, sizeof(uint32_t), ws[h]));
+            if ((rc = round(h, hb[h], hb[h + 1], rounds))) return rc;
+            SW_CUDA(cudaMemcpyAsync(ctx.h_active + h, L.active + 2 * h, sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost, ws[h]));
+        }
+        uint32_t act = 0;
+        for (uint32_t h = 0; h < H; h++) {
+            SW_CUDA(cudaStreamSynchronize(ws[h]));
+            act += ctx.h_active[h];
+        }
+        if (act == 0) break;
+    }
+    if (H == 2) {                          // join: the call continues on the first stream
+        SW_CUDA(cudaEventRecord(ctx.pev[3], ws[1]));
+        SW_CUDA(cudaStreamWaitEvent(ws[0], ctx.pev[3], 0));
     }
     for (uint32_t i = 0; i < timed; i++) {
         float a = 0.f, w = 0.f;
@@ -342,7 +372,7 @@ int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
     }
     for (uint32_t c = 0; c < C; c++) {
         float t = 0.f;
-        cudaEventElapsedTime(&t, ctx.pev[2 + 2 * c], ctx.pev[3 + 2 * c]);
+        cudaEventElapsedTime(&t, ctx.pev[4 + 2 * c], ctx.pev[5 + 2 * c]);
         g_timing.seed_ms += t;
     }
     g_timing.n_chunks += (uint32_t)(rounds + 1);
@@ -424,6 +454,7 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
     if (rc) {
         cudaStreamSynchronize(ctx.seed_st);
         cudaStreamSynchronize(ctx.walk_st);
+        cudaStreamSynchronize(ctx.walk_st2);
         return rc;
     }
     SW_CUDA(cudaEventRecord(ctx.pev[1], ws));
@@ -457,7 +488,7 @@ sw::LogfTables sw::api::device_logf_tables() {
 
 namespace {
 std::mutex g_tune_mu;
-sw_tuning g_tune{0u, 256u, 0u, {0u, 0u, 0u, 0u, 0u}};
+sw_tuning g_tune{0u, 256u, 0u, 0u, {0u, 0u, 0u, 0u}};
 }  // namespace
 
 sw_tuning sw::api::current_tuning() {
@@ -473,6 +504,7 @@ int sw_set_tuning(const sw_tuning *t) {
         return fail(SW_ERR_INVALID, "walk_block must be 64, 128 or 256");
     if (t->resort_interval > 1u << 20) return fail(SW_ERR_INVALID, "resort_interval too large");
     if (t->seed_chunks > kMaxSeedChunks) return fail(SW_ERR_INVALID, "seed_chunks > 64");
+    if (t->round_streams > 2) return fail(SW_ERR_INVALID, "round_streams must be 0, 1 or 2");
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune = *t;
     return SW_OK;

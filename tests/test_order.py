@@ -13,17 +13,19 @@ from tests.helpers import bits_equal, load_golden
 def tuning():
     """Restores the default tuning after the test (the setting is process-wide)."""
     yield _lib.set_tuning
-    _lib.set_tuning(0, 256, 0)
+    _lib.set_tuning(0, 256, 0, 0)
 
 
 def test_tuning_roundtrip_and_validation(tuning):
-    tuning(3, 128, 5)
-    assert _lib.get_tuning() == dict(resort_interval=3, walk_block=128, seed_chunks=5)
+    tuning(3, 128, 5, 2)
+    want = dict(resort_interval=3, walk_block=128, seed_chunks=5, round_streams=2)
+    assert _lib.get_tuning() == want
     for bad in (dict(resort_interval=1, walk_block=100), dict(resort_interval=1, walk_block=512),
-                dict(resort_interval=1 << 21, walk_block=256), dict(seed_chunks=65)):
+                dict(resort_interval=1 << 21, walk_block=256), dict(seed_chunks=65),
+                dict(round_streams=3)):
         with pytest.raises(_lib.SpinWalkError):
             _lib.set_tuning(**bad)
-    assert _lib.get_tuning() == dict(resort_interval=3, walk_block=128, seed_chunks=5)
+    assert _lib.get_tuning() == want
 
 
 def _dense_problem(n_spins=20000, TE_us=(3000, 9000), **kw):
@@ -122,3 +124,17 @@ def test_dense_pipeline_with_resort_and_fp64_shadow(tuning):
     tuning(2, 128, 7)
     got = _lib.run(pr, precision=2, fp64_shadow=True, fill=np.nan)
     _same(got, want, ("M1", "XYZ1", "T", "status", "M1_fp64"))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["permeable", "se_multi_te", "lost_spins", "trajectory",
+                                  "bssfp_phase_cycling"])
+@pytest.mark.parametrize("chunks", [1, 3])
+def test_sim_results_independent_of_round_streams(tuning, case, chunks):
+    """The rounds as two independent halves on two streams give the one-stream results."""
+    pr, _ = load_golden(case)
+    tuning(0, 256, 1, 1)
+    want = _lib.run(pr, fill=np.nan)
+    tuning(0, 256, chunks, 2)
+    got = _lib.run(pr, fill=np.nan)
+    _same(got, want)

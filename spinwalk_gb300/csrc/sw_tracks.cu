@@ -426,10 +426,11 @@ template <bool KAHAN, bool SHADOW>
 __global__ void __launch_bounds__(256)
     k_walk_logged(DevParams P, DevTables Tb, GroupTables GT, GroupState GS,
                   const uint2 *__restrict__ vox, SpinState S, RngState G, uint32_t *active,
-                  uint32_t *log_count, BlochEvent *log, BlochEvent64 *log64) {
-    const uint32_t spin = blockIdx.x * blockDim.x + threadIdx.x;
+                  uint32_t *log_count, BlochEvent *log, BlochEvent64 *log64, uint32_t spin_lo,
+                  uint32_t spin_hi) {
+    const uint32_t spin = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
     bool still = false;
-    if (spin < P.n_spins) {
+    if (spin < spin_hi) {
         const uint32_t flags = S.flags[spin];
         if (!(flags & kFlagDone))
             still = walk_logged_spin<KAHAN, SHADOW>(spin, flags, P, Tb, GT, GS, vox, S, G,
@@ -448,12 +449,13 @@ template <bool SHADOW, bool OUT64>
 __global__ void __launch_bounds__(256)
     k_bloch_groups(DevParams P, GroupTables GT, GroupState GS,
                    const uint32_t *__restrict__ log_count, const BlochEvent *__restrict__ log,
-                   const BlochEvent64 *__restrict__ log64) {
-    const size_t n = P.n_spins, plane = (size_t)GT.n_groups * n;
-    const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (idx >= plane) return;
-    const uint32_t g = (uint32_t)(idx / n);
-    const uint32_t spin = (uint32_t)(idx - (size_t)g * n);
+                   const BlochEvent64 *__restrict__ log64, uint32_t spin_lo, uint32_t spin_hi) {
+    const size_t n = P.n_spins, plane = (size_t)GT.n_groups * n, n_half = spin_hi - spin_lo;
+    const size_t th = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (th >= (size_t)GT.n_groups * n_half) return;
+    const uint32_t g = (uint32_t)(th / n_half);
+    const uint32_t spin = spin_lo + (uint32_t)(th - (size_t)g * n_half);
+    const size_t idx = (size_t)g * n + spin;                 // index in a [n_groups][n] plane
     const uint32_t cnt = log_count[spin];
     if (cnt == 0) return;
     const uint32_t span = GT.max_ds + 1, last = GT.last_ds[g];
@@ -553,6 +555,8 @@ struct TracksCtx {
     std::mutex mu;
     char *buf = nullptr;
     size_t size = 0;
+    cudaStream_t st[2] = {nullptr, nullptr};  // the two halves of the rounds
+    uint32_t *h_active = nullptr;             // pinned, one counter per half
 };
 TracksCtx g_tctx[64];
 
@@ -701,7 +705,18 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
         C.size = off;
     }
     char *d = C.buf;
-    cudaStream_t st = nullptr;
+    if (!C.st[0]) {
+        for (int i = 0; i < 2; i++)
+            if (cudaStreamCreateWithFlags(&C.st[i], cudaStreamNonBlocking) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(SW_ERR_CUDA, "tracks streams");
+            }
+        if (cudaMallocHost(&C.h_active, 2 * sizeof(uint32_t)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SW_ERR_CUDA, "tracks pinned counters");
+        }
+    }
+    cudaStream_t st = C.st[0];
 #define TR_CUDA(call)                                                                      \
     do {                                                                                   \
         cudaError_t e_ = (call);                                                           \
@@ -798,38 +813,73 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     if (h) return fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate");
     const uint64_t steps = (uint64_t)pw.n_timepoints * (uint64_t)(max_ds + 1);
     const uint64_t max_rounds = 64 + steps * (param->max_iterations + 2);
-    uint64_t round = 0;
-    for (;; round++) {
-        if (round >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
-        TR_CUDA(cudaMemsetAsync(L.active, 0, 4, st));
-        TR_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
-        const unsigned gw = (unsigned)((n + 255) / 256), gb = (unsigned)(((size_t)ng * n + 255) / 256);
+    // the rounds as two independent halves of the spins on two streams (from 2^16 spins on):
+    // one half's refill and Bloch update overlap the other half's walk
+    const uint32_t H = n >= (1u << 16) ? 2u : 1u;
+    const uint32_t hb[3] = {0u, H == 2 ? (uint32_t)(n / 2) : (uint32_t)n, (uint32_t)n};
+    cudaEvent_t evh = nullptr;
+    TR_CUDA(cudaEventCreateWithFlags(&evh, cudaEventDisableTiming));
+    if (H == 2) {                                  // the second half starts after the set-up
+        TR_CUDA(cudaEventRecord(evh, C.st[0]));
+        TR_CUDA(cudaStreamWaitEvent(C.st[1], evh, 0));
+    }
+    auto issue_round = [&](uint32_t hh) -> int {
+        const uint32_t lo = hb[hh], hi = hb[hh + 1];
+        cudaStream_t s = C.st[hh];
+        uint32_t *act = L.active + 2 * hh;
+        TR_CUDA(sw::launch_refill_range(P, L.G, L.S.flags, LT, lo, hi, s));
+        const unsigned gw = (hi - lo + 255) / 256, gb = (unsigned)(((size_t)ng * (hi - lo) + 255) / 256);
         if (precision == SW_PREC_KAHAN && shadow)
-            sw::k_walk_logged<true, true><<<gw, 256, 0, st>>>(P, Tb, GT, GS, L.vox, L.S, L.G, L.active, lcnt, elog, elog64);
+            sw::k_walk_logged<true, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elog64, lo, hi);
         else if (precision == SW_PREC_KAHAN)
-            sw::k_walk_logged<true, false><<<gw, 256, 0, st>>>(P, Tb, GT, GS, L.vox, L.S, L.G, L.active, lcnt, elog, elog64);
+            sw::k_walk_logged<true, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elog64, lo, hi);
         else if (shadow)
-            sw::k_walk_logged<false, true><<<gw, 256, 0, st>>>(P, Tb, GT, GS, L.vox, L.S, L.G, L.active, lcnt, elog, elog64);
+            sw::k_walk_logged<false, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elog64, lo, hi);
         else
-            sw::k_walk_logged<false, false><<<gw, 256, 0, st>>>(P, Tb, GT, GS, L.vox, L.S, L.G, L.active, lcnt, elog, elog64);
+            sw::k_walk_logged<false, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elog64, lo, hi);
         TR_CUDA(cudaGetLastError());
         if (precision == SW_PREC_FP64)
-            sw::k_bloch_groups<true, true><<<gb, 256, 0, st>>>(P, GT, GS, lcnt, elog, elog64);
+            sw::k_bloch_groups<true, true><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, lo, hi);
         else if (shadow)
-            sw::k_bloch_groups<true, false><<<gb, 256, 0, st>>>(P, GT, GS, lcnt, elog, elog64);
+            sw::k_bloch_groups<true, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, lo, hi);
         else
-            sw::k_bloch_groups<false, false><<<gb, 256, 0, st>>>(P, GT, GS, lcnt, elog, elog64);
+            sw::k_bloch_groups<false, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, lo, hi);
         TR_CUDA(cudaGetLastError());
-        TR_CUDA(cudaMemcpyAsync(&h, L.active, 4, cudaMemcpyDeviceToHost, st));
-        TR_CUDA(cudaStreamSynchronize(st));
-        if (h == 0) break;
+        return SW_OK;
+    };
+    // rounds that no spin can finish sooner (each advances a spin by at most kStepsPerRound
+    // time points), issued without waiting; then rounds until no spin is active
+    const uint64_t r0 = (steps + sw::kStepsPerRound - 1) / sw::kStepsPerRound;
+    uint64_t round = 0;
+    for (; round < r0; round++)
+        for (uint32_t hh = 0; hh < H; hh++)
+            if ((rc = issue_round(hh))) return rc;
+    for (;; round++) {
+        if (round >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
+        for (uint32_t hh = 0; hh < H; hh++) {
+            TR_CUDA(cudaMemsetAsync(L.active + 2 * hh, 0, 4, C.st[hh]));
+            if ((rc = issue_round(hh))) return rc;
+            TR_CUDA(cudaMemcpyAsync(C.h_active + hh, L.active + 2 * hh, 4, cudaMemcpyDeviceToHost,
+                                    C.st[hh]));
+        }
+        uint32_t live = 0;
+        for (uint32_t hh = 0; hh < H; hh++) {
+            TR_CUDA(cudaStreamSynchronize(C.st[hh]));
+            live += C.h_active[hh];
+        }
+        if (live == 0) break;
     }
+    if (H == 2) {                                  // join the halves on the first stream
+        TR_CUDA(cudaEventRecord(evh, C.st[1]));
+        TR_CUDA(cudaStreamWaitEvent(C.st[0], evh, 0));
+    }
+    cudaEventDestroy(evh);
     TR_CUDA(cudaEventRecord(ev1, st));
     TR_CUDA(cudaEventSynchronize(ev1));
     cudaEventElapsedTime(&g_timing.total_ms, ev0, ev1);
     g_timing.walk_ms = g_timing.total_ms;
     g_timing.n_chunks = (uint32_t)(round + 1);
-    g_timing.n_launches = (uint32_t)(4 + 3 * (round + 1));
+    g_timing.n_launches = (uint32_t)(4 + 3 * H * (round + 1));
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
     for (uint32_t t = 0; t < n_tracks; t++) {

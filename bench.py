@@ -168,14 +168,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def precision_errors(pr):
+def precision_errors(pr, rng=0):
     """Error of the FP32 and compensated-FP32 (Kahan) phase sums against an FP64 run of the same
     walk (the FP64 shadow the library computes alongside): the largest per-spin |M - M_fp64|
     (|M| <= 1) and the largest relative error of the echo signal |mean Mxy| over all echoes."""
     from spinwalk_gb300 import _lib, abi
     out = {}
     for name, prec in (("fp32", abi.SW_PREC_FP32), ("kahan", abi.SW_PREC_KAHAN)):
-        r = _lib.run(pr, precision=prec, fp64_shadow=True)
+        r = _lib.run(pr, precision=prec | rng, fp64_shadow=True)
         m, d = r["M1"].astype(np.float64), r["M1_fp64"]
         ok = r["status"] == 0
         sig = np.abs(m[ok, :, 0].mean(0) + 1j * m[ok, :, 1].mean(0))
@@ -213,7 +213,7 @@ def cpu_sample_ids(n_spins, n_sample):
     return np.unique(np.linspace(0, n_spins - 1, n_sample).round().astype(np.uint32))
 
 
-def time_cpu(pr, n_sample, threads=0, lowest=False):
+def time_cpu(pr, n_sample, threads=0, lowest=False, rng=0):
     """The oracle port on `threads` host threads over n_sample spin ids: stratified over the
     whole range (end to end, the per-spin discard included), or the lowest ids (lowest=True:
     discard(seed + spin) of a few thousand words, i.e. the walk-only rate)."""
@@ -222,7 +222,7 @@ def time_cpu(pr, n_sample, threads=0, lowest=False):
            else cpu_sample_ids(pr.params.n_spins, n_sample))
     outs = pr.outputs()
     t = time.perf_counter()
-    oracle_lib.run(pr, spin_ids=ids, n_threads=threads, outputs=outs)
+    oracle_lib.run(pr, precision=rng, spin_ids=ids, n_threads=threads, outputs=outs)
     dt = time.perf_counter() - t
     steps = len(ids) * pr.params.n_timepoints * (pr.params.n_dummy_scan + 1)
     return steps / dt, len(ids), dt
@@ -323,7 +323,8 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.current_stream(dev)
 
     from spinwalk_gb300 import abi
-    prec = abi.SW_PREC_FP32 | (abi.SW_FIELD_BF16 if args.field_bf16 else 0)
+    rng = abi.SW_RNG_MINSTD if args.rng == "minstd" else abi.SW_RNG_MT19937
+    prec = abi.SW_PREC_FP32 | (abi.SW_FIELD_BF16 if args.field_bf16 else 0) | rng
 
     def step():
         _lib.run_device(pr, d["field"].data_ptr(), d["mask"].data_ptr(), d["M0"].data_ptr(),
@@ -414,14 +415,14 @@ def run_ours(args, world, rank, local):
                 "of the two halves of the rounds overlap; ncu: k_walk L2 hit rate and FP64 pipe "
                 "in profiles/",
     }
-    errors = precision_errors(pr) if args.workload in ("se", "small") else None
+    errors = precision_errors(pr, rng) if args.workload in ("se", "small") else None
     bf16_err = bf16_field_errors(pr) if args.field_bf16 else None
     cpu = None
     if world == 1 or rank == 0:
         if args.cpu_sample > 0:
-            rate, ns, dt = time_cpu(pr, args.cpu_sample, os.cpu_count())
+            rate, ns, dt = time_cpu(pr, args.cpu_sample, os.cpu_count(), rng=rng)
             wrate, wns, wdt = time_cpu(pr, max(1, args.cpu_sample // 4), os.cpu_count(),
-                                       lowest=True)
+                                       lowest=True, rng=rng)
             cpu = {"value": rate, "unit": "spin-steps/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"{ns} stratified spin ids of {n} ({pr.params.n_timepoints} time "
                              f"points each, {dt:.1f} s wall on {os.cpu_count()} threads)",
@@ -436,7 +437,10 @@ def run_ours(args, world, rank, local):
         "config": dict(desc, parallelism=f"spin-range shards x{world}",
                        l2="inputs larger than L2 (packed phantom + generator state)",
                        field_records="bfloat16, 4 B per voxel" if args.field_bf16
-                       else "float32, 8 B per voxel"),
+                       else "float32, 8 B per voxel",
+                       generators="thrust minstd_rand + erfcinv normal (the reference's CUDA "
+                                  "build)" if args.rng == "minstd" else
+                                  "std::mt19937 + polar normal (the reference's CPU build)"),
         "kernel_ms_per_step": {k: v / args.steps for k, v in parts.items()},
         "kernel_ms_note": "sums of launch durations; the refill/walk rounds run as two halves on "
                           "two streams whose kernels overlap, so walk + refill exceed their wall "
@@ -782,6 +786,8 @@ def main():
                     help="serve workload: requests in signal mode (no per-spin outputs)")
     ap.add_argument("--field-bf16", action="store_true",
                     help="bfloat16 fieldmap records (SW_FIELD_BF16); reports their error")
+    ap.add_argument("--rng", default="mt19937", choices=["mt19937", "minstd"],
+                    help="generator flavour: the reference's CPU build (default) or CUDA build")
     ap.add_argument("--round-streams", type=int, default=None,
                     help="refill/walk rounds as this many independent halves on own streams (1, 2)")
     ap.add_argument("--seed-chunks", type=int, default=None,

@@ -541,6 +541,64 @@ def bssfp_cycle_errors(pr, tracks):
     return res
 
 
+def run_dwi(args, world, rank):
+    """DWI b-value sweep (the reference's gradient scale loop, WHAT_TO_SCALE = 1): PGSE along x
+    (b = 1000 s/mm^2 at scale 1, delta 10 ms, Delta 20 ms) on the 200^3 cylinder phantom of
+    config 1, 1e6 spins, 8 gradient scales 0 .. 1.4 (b 0 .. 1960 s/mm^2). One walk with a phase
+    per scale (sw_sim_tracks) against one walk per scale with one seeding (sw_sim_batch); the
+    work is counted per instance."""
+    import torch  # noqa: F401
+    from spinwalk_gb300 import _lib
+    from spinwalk_gb300.problem import Problem
+    n, fov = 200, 200e-6
+    mask, field = _lib.phantom_cylinders(n, fov, 5e-6, 0.03, seed=1)
+    lobe = lambda t0: list(range(t0, t0 + 10000, 50))                       # noqa: E731
+    g_t = lobe(2000) + [12000] + lobe(22000) + [32000]
+    g = np.zeros((len(g_t), 3), np.float32)
+    for i, t in enumerate(g_t):
+        if t not in (12000, 32000):
+            g[i, 0] = 91.6
+    kw = dict(TR_us=34050, TE_us=(34000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
+              RF_us=(0, 17000), timestep_us=50, gradient_us=tuple(g_t), gradient_xyz=g)
+    n_spins = 1_000_000
+    pr = Problem(mask, [fov] * 3, field, n_spins=n_spins, seed=10 + 1_000_003 * rank, **kw)
+    scales = [0.2 * i for i in range(8)]
+    tracks = [dict(gradient_scale=sc, n_dummy_scan=0) for sc in scales]
+
+    def scaled(sc):
+        q = Problem(mask, [fov] * 3, field, n_spins=n_spins, seed=10 + 1_000_003 * rank,
+                    **dict(kw, gradient_xyz=g * np.float32(sc)))
+        return q
+    insts = [scaled(sc) for sc in scales]
+    steps = len(scales) * pr.spin_steps()
+    for _ in range(args.warmup):
+        _lib.run_tracks(pr, tracks)
+    t_ms, b_ms = [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            _lib.run_tracks(pr, tracks)
+            t_ms.append(_lib.last_timing()["total_ms"])
+    clocks = clk.summary()
+    _lib.run_batch(insts)
+    for _ in range(max(1, args.steps // 2)):
+        _lib.run_batch(insts)
+        b_ms.append(_lib.last_timing()["total_ms"])
+    value = world * steps / (np.mean(t_ms) * 1e-3)
+    batch = steps / (np.mean(b_ms) * 1e-3)
+    line = {"metric": "spin-steps/s (gradient-scale sweep, per instance)", "value": value,
+            "unit": "spin-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean(t_ms)), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "dwi_pgse_8_gradient_scales_200cubed_1e6spins",
+                       "phantom": "200^3 cylinders r5um 3% (config 1)", "n_spins": n_spins,
+                       "sequence": "PGSE x, delta 10 ms, Delta 20 ms, TE 34 ms, dt 50 us",
+                       "gradient_scales": scales},
+            "one_walk_per_scale": {"value": batch, "ms": float(np.mean(b_ms))},
+            "shared_over_separate": value / batch, "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def c3_instances(rank=0):
     """Config 3: the config-1 phantom (200^3 random-orientation cylinders, r 5 um, 3 %), 32 FoV
     scales giving vessel radii 1-100 um (log-spaced; scale = r / 5 um, WHAT_TO_SCALE = 0) x
@@ -798,6 +856,8 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "bssfp":
         run_batched(args, world, rank)
+    elif args.workload == "dwi":
+        run_dwi(args, world, rank)
     elif args.workload == "c3":
         run_batch_scales(args, world, rank)
     elif args.workload == "serve":

@@ -256,7 +256,14 @@ typedef struct sw_track {
     uint8_t *T;               /* [n_spins][n_TE] host */
     int32_t *status;          /* [n_spins] host, or NULL */
     double *M1_fp64;          /* [n_spins][n_TE][3] host FP64 shadow, or NULL */
+    float gradient_scale;     /* with SW_TRACK_GRADIENT_SCALE: the gradients times this scale */
+    uint32_t options;         /* SW_TRACK_* bits */
 } sw_track;
+/* The track's gradient waveform is the sequence's scaled by gradient_scale (float multiply, as
+ * the reference's gradient scale loop does, src/sim/monte_carlo.cu:287-290). Tracks with
+ * different gradient scales share the walk but not the phase: each distinct scale keeps its own
+ * phase sums (at most 8 distinct scales per call, SW_PREC_FP32 only, no FP64 shadow). */
+#define SW_TRACK_GRADIENT_SCALE 0x1u
 
 int sw_sim_tracks(const sw_params *param, const sw_sequence *seq, const sw_track *tracks,
                   uint32_t n_tracks, const float *pFieldMap, const uint8_t *pMask,

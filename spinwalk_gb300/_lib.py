@@ -423,8 +423,8 @@ def run_device_noalloc(problem, d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T
 def run_tracks(problem, tracks, fill=0.0, precision=abi.SW_PREC_FP32, fp64=False):
     """sw_sim_tracks: many instances of `problem` sharing one walk. `tracks` is a list of dicts
     with keys linear_phase_cycling, quadratic_phase_cycling, n_dummy_scan and optionally
-    RF_FA_deg / RF_PH_deg arrays. Returns one output dict per track; with fp64=True each also
-    holds "M1_fp64", the track's FP64 shadow."""
+    RF_FA_deg / RF_PH_deg arrays and gradient_scale. Returns one output dict per track; with
+    fp64=True each also holds "M1_fp64", the track's FP64 shadow."""
     n, nte = problem.params.n_spins, problem.n_te
     arr = (abi.SwTrack * len(tracks))()
     outs, keep = [], []
@@ -447,6 +447,9 @@ def run_tracks(problem, tracks, fill=0.0, precision=abi.SW_PREC_FP32, fp64=False
         s.XYZ1 = abi.ptr(o["XYZ1"], C.c_float)
         s.T = abi.ptr(o["T"], C.c_uint8)
         s.status = abi.ptr(o["status"], C.c_int32)
+        if t.get("gradient_scale") is not None:
+            s.gradient_scale = float(t["gradient_scale"])
+            s.options |= abi.SW_TRACK_GRADIENT_SCALE
         if fp64:
             o["M1_fp64"] = np.full((n, nte, 3), fill, np.float64)
             s.M1_fp64 = abi.ptr(o["M1_fp64"], C.c_double)

@@ -26,6 +26,7 @@ SW_PREC_FP32 = 0
 SW_PREC_FP64 = 1
 SW_PREC_KAHAN = 2
 SW_FIELD_BF16 = 0x200
+SW_TRACK_GRADIENT_SCALE = 0x1
 SW_RNG_MT19937 = 0x000
 SW_RNG_MINSTD = 0x100
 
@@ -92,6 +93,8 @@ class SwTrack(C.Structure):
         ("T", C.POINTER(C.c_uint8)),
         ("status", C.POINTER(C.c_int32)),
         ("M1_fp64", C.POINTER(C.c_double)),
+        ("gradient_scale", C.c_float),
+        ("options", C.c_uint32),
     ]
 
 

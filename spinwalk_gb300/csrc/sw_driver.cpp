@@ -2,9 +2,10 @@
 // of the GPU entry points -- config, phantoms, initial positions, fieldmap scaling, the scale
 // loop and the HDF5 outputs -- plus the HDF5 helpers of the C ABI.
 //
-// Phase-cycling scales (WHAT_TO_SCALE = 2) walk identically, so they run as tracks of one walk
-// (sw_sim_tracks, bit-identical to one run per scale); FoV and gradient scales run as one
-// sw_sim_batch (one walk per scale, one seeding for all), also bit-identical.
+// Phase-cycling scales (WHAT_TO_SCALE = 2) and gradient scales (up to 8 distinct ones) walk
+// identically, so they run as tracks of one walk (sw_sim_tracks, bit-identical to one run per
+// scale; gradient scales keep one phase per scale); FoV scales, and repeated or more gradient
+// scales, run as one sw_sim_batch (one walk per scale, one seeding for all), also bit-identical.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -154,15 +155,26 @@ extern "C" int sw_run_config(const char *ini_path, int device) {
         q.gradientZ_mTm = gz.data();
 
         const auto t_sim = clock::now();
-        if (c.scale_type == 2 && !p.enRecordTrajectory && ns > 1) {
-            // phase-cycling scales: one walk, one track per scale
+        // phase-cycling scales, and up to 8 distinct gradient scales, share one walk (tracks);
+        // repeated scales would be duplicate tracks, so they take the batch below
+        std::vector<float> sorted_scales(c.scales.begin(), c.scales.end());
+        std::sort(sorted_scales.begin(), sorted_scales.end());
+        const bool distinct = std::adjacent_find(sorted_scales.begin(), sorted_scales.end()) ==
+                              sorted_scales.end();
+        const bool share = (c.scale_type == 2 || (c.scale_type == 1 && ns <= 8)) && distinct;
+        if (share && !p.enRecordTrajectory && ns > 1) {
+            // one walk, one track per scale
             std::vector<sw_track> tracks(ns);
             std::vector<std::vector<float>> xyz(ns, std::vector<float>(n * 3));
             for (size_t k = 0; k < ns; k++) {
                 sw_track &t = tracks[k];
                 t = sw_track{};
-                t.linear_phase_cycling = lin0 * c.scales[k];
+                t.linear_phase_cycling = c.scale_type == 2 ? lin0 * c.scales[k] : lin0;
                 t.quadratic_phase_cycling = quad0;
+                if (c.scale_type == 1) {
+                    t.gradient_scale = c.scales[k];
+                    t.options = SW_TRACK_GRADIENT_SCALE;
+                }
                 t.n_dummy_scan = p.n_dummy_scan;
                 t.M1 = M1.data() + 3 * nte * n * k;
                 t.T = T.data() + nte * n * k;

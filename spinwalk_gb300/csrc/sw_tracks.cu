@@ -43,6 +43,10 @@ struct GroupTables {
     const int32_t *track_nd;  // [n_tracks]
     float *const *M1;         // [n_tracks] -> [n][n_TE][3]
     double *const *M1d;       // [n_tracks] -> [n][n_TE][3] FP64 shadow, entries may be null
+    // gradient classes (tracks with distinct gradient scales): each keeps its own phase sums
+    uint32_t n_cls;           // 1: one shared phase (the kernels without classes)
+    const uint32_t *cls;      // [n_groups]: the group's class
+    const float *gscale;      // [n_cls]: the class's gradient scale
     float *const *XYZ1;       // [n_tracks] -> [n][3]
     uint8_t *const *T;        // [n_tracks] -> [n][n_TE]
     int32_t *const *status;   // [n_tracks] -> [n]
@@ -57,6 +61,7 @@ struct GroupState {
     uint32_t *rec_started;    // [n]
     double *mg64, *mr64;      // FP64 shadow of mg / mr, or null
     double *accd_rec;         // [n] FP64 shadow of acc_rec
+    float *acc_c, *acc_rec_c; // [n_cls][n]: acc and acc_rec per gradient class
 };
 
 // dephase_relax_f split in two: the trigonometry and exponentials depend only on the shared
@@ -177,6 +182,12 @@ struct BlochEvent {
 struct BlochEvent64 {
     double r[4];
     double rr[4];
+};
+// An event's relaxation operators for one gradient class ([n][kLogCap][n_cls], parallel to the
+// event log).
+struct BlochEventC {
+    float r[4];
+    float rr[4];
 };
 
 __device__ __forceinline__ void put_relax(float *dst, const RelaxOp &r) {
@@ -442,14 +453,244 @@ __global__ void __launch_bounds__(256)
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(active, (uint32_t)__popc(b));
 }
 
+// The logged walk with NC gradient classes (FP32 arithmetic): the trajectory and events are
+// shared, the phase sums acc / acc_rec are kept per class, the gradient term of class c uses the
+// sequence's gradients times gscale[c] (float multiply, as the reference's gradient scale loop,
+// monte_carlo.cu:287-290), and each event logs one pair of relaxation operators per class.
+// Every other operation is the one walk_logged_spin performs.
+template <int NC>
+__device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flags,
+                                              const DevParams &P, const DevTables &Tb,
+                                              const GroupTables &GT, const GroupState &GS,
+                                              const uint2 *__restrict__ vox, const SpinState &S,
+                                              const RngState &G, uint32_t *log_count,
+                                              BlochEvent *log, BlochEventC *logc) {
+    WalkRegs w;
+    w.xo[0] = S.x[spin]; w.xo[1] = S.y[spin]; w.xo[2] = S.z[spin];
+    w.ind_old = S.ind_old[spin];
+    w.ts_old = flags & 0xffu;
+    w.field = S.field[spin];
+    w.dscale = __ldg(Tb.dscale + w.ts_old);
+    w.itr = S.itr[spin];
+    w.nh = G.nhead[spin]; w.nc = G.ncnt[spin]; w.uh = G.uhead[spin]; w.uc = G.ucnt[spin];
+    const float *nb = G.nbuf + (size_t)spin * kNormBuf;
+    const float *ub = G.ubuf + (size_t)spin * kUnifBuf;
+    BlochEvent *lg = log + (size_t)spin * kLogCap;
+    BlochEventC *lc = logc + (size_t)spin * kLogCap * NC;
+    uint32_t ne = 0;
+    const size_t n = P.n_spins;
+
+    float acc[NC], acc_rec[NC], gs[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        acc[c] = GS.acc_c[(size_t)c * n + spin];
+        acc_rec[c] = GS.acc_rec_c[(size_t)c * n + spin];
+        gs[c] = __ldg(GT.gscale + c);
+    }
+    uint32_t tp = S.tp[spin], tp_old = S.tp_old[spin], tp_old_rec = GS.tp_old_rec[spin];
+    uint32_t ds = S.ds[spin];
+    bool rec_started = GS.rec_started[spin] != 0;
+    uint32_t ctr = S.ctr[spin], ctr2 = S.ctr2[spin];
+    uint32_t c_rf = ctr & 0xffffu, c_te = ctr >> 16, c_dph = ctr2 & 0xffffu, c_grad = ctr2 >> 16;
+    bool started = (flags & kFlagStarted) != 0;
+
+    auto relax_f = [&](float a, uint32_t t0) {
+        const float te = (float)((double)((tp - t0) * (uint32_t)P.timestep_us) * 1e-6);
+        return make_relax(a, __ldg(Tb.T1f + w.ts_old), __ldg(Tb.T2f + w.ts_old), te);
+    };
+
+    constexpr uint32_t NONE = 0xffffffffu;
+    bool rec_scan = ds <= GT.max_ds && GT.rec_any[ds] != 0;
+    uint32_t t_rf = c_rf < P.n_RF ? (uint32_t)Tb.rf[c_rf].tp : NONE;
+    uint32_t t_te = (rec_scan && c_te < P.n_TE) ? (uint32_t)Tb.te_tp[c_te] : NONE;
+    uint32_t t_dph = c_dph < P.n_dephasing ? (uint32_t)Tb.dph_tp[c_dph] : NONE;
+    uint32_t t_grad = c_grad < P.n_gradient ? (uint32_t)Tb.grad_tp[c_grad] : NONE;
+
+    int status = -1;
+    for (;;) {
+        if (ne + 4 > kLogCap) break;                                // log full: pause
+        if (!started) {
+            if (ds > GT.max_ds) { status = SW_SPIN_OK; break; }
+            BlochEvent &e = lg[ne++];                                // kernels.cu:110-120
+            e.head = kEvScanStart | (ds << 8);
+            e.ds = ds;
+            e.flags = 0;
+            w.ind_old = P.matrix_length + 1;
+            tp = tp_old = 0;
+            c_rf = 1; c_te = 0; c_dph = 0; c_grad = 0;
+#pragma unroll
+            for (int c = 0; c < NC; c++) { acc[c] = 0.f; acc_rec[c] = 0.f; }
+            tp_old_rec = 0;
+            rec_started = false;
+            rec_scan = GT.rec_any[ds] != 0;
+            started = true;
+            t_rf = 1 < P.n_RF ? (uint32_t)Tb.rf[1].tp : NONE;
+            t_te = (rec_scan && P.n_TE > 0) ? (uint32_t)Tb.te_tp[0] : NONE;
+            t_dph = P.n_dephasing > 0 ? (uint32_t)Tb.dph_tp[0] : NONE;
+            t_grad = P.n_gradient > 0 ? (uint32_t)Tb.grad_tp[0] : NONE;
+            continue;
+        }
+        if (tp >= P.n_timepoints) {                                 // kernels.cu:225-231
+            BlochEvent &e = lg[ne];
+            bool rl = false;
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                const RelaxOp r = relax_f(acc[c], tp_old);
+                put_relax(lc[ne * NC + c].r, r);
+                rl = r.relax;
+            }
+            e.head = kEvScanEnd | (ds << 8);
+            e.ds = ds;
+            e.flags = rl ? 1u : 0u;
+            e.xo[0] = (float)dfrom(w.xo[0]); e.xo[1] = (float)dfrom(w.xo[1]); e.xo[2] = (float)dfrom(w.xo[2]);
+            ne++;
+            ds++;
+            started = false;
+            continue;
+        }
+        if ((dnonzero(w.dscale) && w.nc < 3) || w.uc == 0) break;      // buffers low: pause
+
+        uint64_t xn[3];
+        const int mv = walk_move(w, xn, P, Tb, vox, nb, ub);
+        if (mv == kMoveRejected) continue;
+        if (mv == kMoveLost) { status = SW_SPIN_LOST; break; }
+        if (mv == kMoveOOB) { status = SW_SPIN_OOB; break; }
+
+#pragma unroll
+        for (int c = 0; c < NC; c++) {                              // kernels.cu:171
+            acc[c] += w.field;
+            if (rec_started) acc_rec[c] += w.field;
+        }
+        if (tp == t_dph) {                                          // kernels.cu:175-178
+            const float inc = (float)spin * __ldg(Tb.dph_deg + c_dph) / (float)P.n_spins;
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                acc[c] += inc;
+                if (rec_started) acc_rec[c] += inc;
+            }
+            c_dph++;
+            t_dph = c_dph < P.n_dephasing ? (uint32_t)Tb.dph_tp[c_dph] : NONE;
+        }
+        if (tp == t_grad) {                                         // kernels.cu:181-187
+            const float gx = __ldg(Tb.gx + c_grad), gy = __ldg(Tb.gy + c_grad),
+                        gz = __ldg(Tb.gz + c_grad);
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                const double g = grad_phase_deg(gx * gs[c], gy * gs[c], gz * gs[c], xn,
+                                                (double)P.timestep_us);
+                acc[c] = d2f_exact(dadd_fp64(dbits(f2d_exact(acc[c])), dbits(g)));
+                if (rec_started)
+                    acc_rec[c] = d2f_exact(dadd_fp64(dbits(f2d_exact(acc_rec[c])), dbits(g)));
+            }
+            c_grad++;
+            t_grad = c_grad < P.n_gradient ? (uint32_t)Tb.grad_tp[c_grad] : NONE;
+        }
+        if (tp == t_rf) {                                           // kernels.cu:190-199
+            BlochEvent &e = lg[ne];
+            bool rl = false, rrl = false;
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                const RelaxOp r = relax_f(acc[c], tp_old);
+                put_relax(lc[ne * NC + c].r, r);
+                rl = r.relax;
+                if (rec_started) {
+                    const RelaxOp rr = relax_f(acc_rec[c], tp_old_rec);
+                    put_relax(lc[ne * NC + c].rr, rr);
+                    rrl = rr.relax;
+                    acc_rec[c] = 0.f;
+                }
+                acc[c] = 0.f;
+            }
+            e.head = kEvRf | (c_rf << 8);
+            e.ds = ds;
+            e.flags = (rl ? 1u : 0u) | (rrl ? 2u : 0u) | (rec_started ? 4u : 0u);
+            if (rec_started) tp_old_rec = tp;
+            ne++;
+            tp_old = tp;
+            c_rf++;
+            t_rf = c_rf < P.n_RF ? (uint32_t)Tb.rf[c_rf].tp : NONE;
+        }
+        if (tp == t_te) {                                           // kernels.cu:202-215
+            const uint32_t t0 = rec_started ? tp_old_rec : tp_old;
+            BlochEvent &e = lg[ne];
+            bool rl = false;
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                const RelaxOp r = relax_f(rec_started ? acc_rec[c] : acc[c], t0);
+                put_relax(lc[ne * NC + c].r, r);
+                rl = r.relax;
+                acc_rec[c] = 0.f;
+            }
+            e.head = kEvTe | (c_te << 8) | (w.ts_old << 24);
+            e.ds = ds;
+            e.flags = (rl ? 1u : 0u) | (rec_started ? 4u : 0u);
+            ne++;
+            tp_old_rec = tp;
+            rec_started = true;
+            c_te++;
+            t_te = c_te < P.n_TE ? (uint32_t)Tb.te_tp[c_te] : NONE;
+        }
+        w.xo[0] = xn[0]; w.xo[1] = xn[1]; w.xo[2] = xn[2];
+        tp++;
+    }
+    log_count[spin] = ne;
+    if (status > 0) {            // lost / out of bounds: every track still running ends here
+        for (uint32_t t = 0; t < GT.n_tracks; t++) {
+            if ((uint32_t)GT.track_nd[t] < ds) continue;
+            float *x = GT.XYZ1[t] + 3 * (size_t)spin;
+            x[0] = (float)dfrom(w.xo[0]); x[1] = (float)dfrom(w.xo[1]); x[2] = (float)dfrom(w.xo[2]);
+            if (GT.status[t]) GT.status[t][spin] = status;
+        }
+    }
+    S.x[spin] = w.xo[0]; S.y[spin] = w.xo[1]; S.z[spin] = w.xo[2];
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        GS.acc_c[(size_t)c * n + spin] = acc[c];
+        GS.acc_rec_c[(size_t)c * n + spin] = acc_rec[c];
+    }
+    GS.tp_old_rec[spin] = tp_old_rec;
+    GS.rec_started[spin] = rec_started ? 1u : 0u;
+    S.field[spin] = w.field;
+    S.ind_old[spin] = w.ind_old;
+    S.tp[spin] = tp; S.tp_old[spin] = tp_old; S.ds[spin] = ds; S.itr[spin] = w.itr;
+    S.ctr[spin] = c_rf | (c_te << 16);
+    S.ctr2[spin] = c_dph | (c_grad << 16);
+    G.nhead[spin] = w.nh; G.ncnt[spin] = w.nc; G.uhead[spin] = w.uh; G.ucnt[spin] = w.uc;
+    uint32_t nf = w.ts_old | (started ? kFlagStarted : 0u);
+    if (status >= 0) nf |= kFlagDone | ((uint32_t)status << 16);
+    S.flags[spin] = nf;
+    return status < 0;
+}
+
+template <int NC>
+__global__ void __launch_bounds__(256)
+    k_walk_cls(DevParams P, DevTables Tb, GroupTables GT, GroupState GS,
+               const uint2 *__restrict__ vox, SpinState S, RngState G, uint32_t *active,
+               uint32_t *log_count, BlochEvent *log, BlochEventC *logc, uint32_t spin_lo,
+               uint32_t spin_hi) {
+    const uint32_t spin = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    bool still = false;
+    if (spin < spin_hi) {
+        const uint32_t flags = S.flags[spin];
+        if (!(flags & kFlagDone))
+            still = walk_cls_spin<NC>(spin, flags, P, Tb, GT, GS, vox, S, G, log_count, log, logc);
+        else
+            log_count[spin] = 0;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, still);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(active, (uint32_t)__popc(b));
+}
+
 // Applies each spin's logged events to every group (thread per (group, spin), spin fastest).
 // SHADOW: the same events in FP64 on mg64 / mr64 (the plain kernel's FP64 shadow, per group);
 // OUT64: the float outputs are the FP64 values rounded (the plain kernel's SW_PREC_FP64).
-template <bool SHADOW, bool OUT64>
+// CLS: the relaxation operators come from the group's gradient class (logc).
+template <bool SHADOW, bool OUT64, bool CLS>
 __global__ void __launch_bounds__(256)
     k_bloch_groups(DevParams P, GroupTables GT, GroupState GS,
                    const uint32_t *__restrict__ log_count, const BlochEvent *__restrict__ log,
-                   const BlochEvent64 *__restrict__ log64, uint32_t spin_lo, uint32_t spin_hi) {
+                   const BlochEvent64 *__restrict__ log64, const BlochEventC *__restrict__ logc,
+                   uint32_t spin_lo, uint32_t spin_hi) {
     const size_t n = P.n_spins, plane = (size_t)GT.n_groups * n, n_half = spin_hi - spin_lo;
     const size_t th = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (th >= (size_t)GT.n_groups * n_half) return;
@@ -472,6 +713,11 @@ __global__ void __launch_bounds__(256)
     };
     const BlochEvent *lg = log + (size_t)spin * kLogCap;
     const BlochEvent64 *lg64 = SHADOW ? log64 + (size_t)spin * kLogCap : nullptr;
+    const uint32_t ncls = CLS ? GT.n_cls : 1u, cl = CLS ? GT.cls[g] : 0u;
+    const BlochEventC *lgc = CLS ? logc + (size_t)spin * kLogCap * ncls : nullptr;
+    // the event's operators: shared, or the group's class's
+    auto op_r = [&](const BlochEvent &e, uint32_t k) { return CLS ? lgc[k * ncls + cl].r : e.r; };
+    auto op_rr = [&](const BlochEvent &e, uint32_t k) { return CLS ? lgc[k * ncls + cl].rr : e.rr; };
     for (uint32_t k = 0; k < cnt; k++) {
         const BlochEvent e = lg[k];
         const uint32_t type = e.head & 0xffu, id = (e.head >> 8) & 0xffffu, ds = e.ds;
@@ -487,7 +733,7 @@ __global__ void __launch_bounds__(256)
             }
         } else if (type == kEvRf) {
             const RfOp op = GT.rf[(size_t)g * P.n_RF + id];
-            apply_relax(get_relax(e.r, e.flags & 1u), m, t3);
+            apply_relax(get_relax(op_r(e, k), e.flags & 1u), m, t3);
             rf_f(op, t3, m);
             if (SHADOW) {
                 apply_relax_d(lg64[k].r, e.flags & 1u, md, u3);
@@ -495,7 +741,7 @@ __global__ void __launch_bounds__(256)
             }
             if ((e.flags & 4u) && t >= 0) {
                 load_mr();
-                apply_relax(get_relax(e.rr, e.flags & 2u), mr, t3);
+                apply_relax(get_relax(op_rr(e, k), e.flags & 2u), mr, t3);
                 rf_f(op, t3, mr);
                 if (SHADOW) {
                     apply_relax_d(lg64[k].rr, e.flags & 2u, mrd, u3);
@@ -507,7 +753,7 @@ __global__ void __launch_bounds__(256)
             if (t < 0) continue;
             const bool from_rec = (e.flags & 4u) != 0;
             if (from_rec) load_mr();
-            apply_relax(get_relax(e.r, e.flags & 1u), from_rec ? mr : m, t3);
+            apply_relax(get_relax(op_r(e, k), e.flags & 1u), from_rec ? mr : m, t3);
             if (SHADOW) apply_relax_d(lg64[k].r, e.flags & 1u, from_rec ? mrd : md, u3);
             float *o = GT.M1[t] + 3 * ((size_t)spin * P.n_TE + id);
             if (OUT64) {
@@ -524,7 +770,7 @@ __global__ void __launch_bounds__(256)
             if (SHADOW) { mrd[0] = u3[0]; mrd[1] = u3[1]; mrd[2] = u3[2]; }
             mr_loaded = mr_dirty = true;
         } else {                                                    // scan end
-            apply_relax(get_relax(e.r, e.flags & 1u), m, t3);
+            apply_relax(get_relax(op_r(e, k), e.flags & 1u), m, t3);
             m[0] = t3[0]; m[1] = t3[1]; m[2] = t3[2];
             if (SHADOW) {
                 apply_relax_d(lg64[k].r, e.flags & 1u, md, u3);
@@ -590,16 +836,20 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
         if (!tracks[t].XYZ1 || (nte && (!tracks[t].M1 || !tracks[t].T)))
             return fail(SW_ERR_INVALID, "track output buffer missing");
     }
-    // ---- group tracks by RF configuration ----
-    using Key = std::tuple<float, float, std::vector<float>, std::vector<float>>;
+    bool shadow = precision == SW_PREC_FP64;
+    for (uint32_t t = 0; t < n_tracks; t++) shadow = shadow || (nte && tracks[t].M1_fp64);
+    // ---- group tracks by RF configuration and gradient scale ----
+    using Key = std::tuple<float, float, std::vector<float>, std::vector<float>, float>;
     std::map<Key, uint32_t> gid;
     std::vector<Key> groups;
     std::vector<uint32_t> tgroup(n_tracks);
     uint32_t max_ds = 0;
     for (uint32_t t = 0; t < n_tracks; t++) {
+        if (tracks[t].options & ~SW_TRACK_GRADIENT_SCALE) return fail(SW_ERR_INVALID, "track options");
+        const float gsc = (tracks[t].options & SW_TRACK_GRADIENT_SCALE) ? tracks[t].gradient_scale : 1.0f;
         Key k{tracks[t].linear_phase_cycling, tracks[t].quadratic_phase_cycling,
               rf_array(tracks[t].RF_FA_deg, seq->RF_FA_deg, seq->n_RF),
-              rf_array(tracks[t].RF_PH_deg, seq->RF_PH_deg, seq->n_RF)};
+              rf_array(tracks[t].RF_PH_deg, seq->RF_PH_deg, seq->n_RF), gsc};
         auto it = gid.find(k);
         if (it == gid.end()) {
             it = gid.emplace(k, (uint32_t)groups.size()).first;
@@ -614,7 +864,8 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     for (uint32_t t = 0; t < n_tracks; t++) {
         const uint32_t d = (uint32_t)tracks[t].n_dummy_scan, g = tgroup[t];
         if (rec[(size_t)g * span + d] >= 0)
-            return fail(SW_ERR_INVALID, "two tracks with the same RF configuration and DUMMY_SCAN");
+            return fail(SW_ERR_INVALID,
+                        "two tracks with the same RF configuration, gradient scale and DUMMY_SCAN");
         rec[(size_t)g * span + d] = (int32_t)t;
         last_ds[g] = std::max(last_ds[g], d);
         rec_any[d] = 1;
@@ -623,7 +874,8 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     // per-group RF operations: parameters::prepare's c/s and the scan-start phases of each group
     std::vector<sw::RfOp> scan_rf((size_t)ng * span), rfops((size_t)ng * seq->n_RF);
     for (uint32_t g = 0; g < ng; g++) {
-        const auto &[lin, quad, fa, ph] = groups[g];
+        const auto &[lin, quad, fa, ph, gsc] = groups[g];
+        (void)gsc;
         sw_params pg = *param;
         pg.linear_phase_cycling = lin;
         pg.quadratic_phase_cycling = quad;
@@ -642,8 +894,40 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     sw_params pw = *param;            // the walk: the longest track
     pw.n_dummy_scan = (int32_t)max_ds;
 
+    // gradient classes: the distinct gradient scales. One scale scales the walk's gradient table
+    // (the same float multiply); several keep a phase per class in the walk (k_walk_cls).
+    std::vector<float> cls_scale;
+    std::vector<uint32_t> gcls(ng);
+    for (uint32_t g = 0; g < ng; g++) {
+        const float gsc = std::get<4>(groups[g]);
+        uint32_t c = 0;
+        while (c < cls_scale.size() && std::memcmp(&cls_scale[c], &gsc, 4) != 0) c++;
+        if (c == cls_scale.size()) cls_scale.push_back(gsc);
+        gcls[g] = c;
+    }
+    const uint32_t n_cls = (uint32_t)cls_scale.size();
+    if (n_cls > 8) return fail(SW_ERR_INVALID, "tracks: at most 8 distinct gradient scales per call");
+    if (n_cls > 1 && (precision != SW_PREC_FP32 || shadow))
+        return fail(SW_ERR_INVALID, "tracks: several gradient scales need SW_PREC_FP32 without the FP64 shadow");
+    const uint32_t NC = n_cls <= 1 ? 1u : (n_cls <= 2 ? 2u : (n_cls <= 4 ? 4u : 8u));
+    std::vector<float> gsx, gsy, gsz;   // the one scale applied to the sequence's gradients
+    sw_sequence qw = *seq;
+    if (n_cls == 1 && cls_scale[0] != 1.0f) {
+        const float sc = cls_scale[0];
+        for (uint32_t k = 0; k < seq->n_gradient; k++) {
+            gsx.push_back(seq->gradientX_mTm[k] * sc);
+            gsy.push_back(seq->gradientY_mTm[k] * sc);
+            gsz.push_back(seq->gradientZ_mTm[k] * sc);
+        }
+        qw.gradientX_mTm = gsx.data();
+        qw.gradientY_mTm = gsy.data();
+        qw.gradientZ_mTm = gsz.data();
+    }
+    std::vector<float> gscale_pad(NC);
+    for (uint32_t c = 0; c < NC; c++) gscale_pad[c] = cls_scale[std::min(c, n_cls - 1)];
+
     TableImage im;
-    build_tables(&pw, seq, im);
+    build_tables(&pw, &qw, im);
     if (!im.complete()) return fail(SW_ERR_INVALID, "internal error: incomplete parameter tables");
     TableImage gi;                    // group tables
     const size_t o_scan = gi.put(scan_rf.data(), scan_rf.size());
@@ -652,6 +936,8 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     const size_t o_last = gi.put(last_ds.data(), last_ds.size());
     const size_t o_any = gi.put(rec_any.data(), rec_any.size());
     const size_t o_nd = gi.put(track_nd.data(), track_nd.size());
+    const size_t o_gcls = gi.put(gcls.data(), gcls.size());
+    const size_t o_gsc = gi.put(gscale_pad.data(), gscale_pad.size());
 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
@@ -676,8 +962,8 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
                  o_mg = slot(2 * 3 * sizeof(float) * (size_t)ng * n),
                  o_gs = slot(16 * n), o_lcnt = slot(4 * n),
                  o_log = slot(sizeof(sw::BlochEvent) * sw::kLogCap * n);
-    bool shadow = precision == SW_PREC_FP64;
-    for (uint32_t t = 0; t < n_tracks; t++) shadow = shadow || (nte && tracks[t].M1_fp64);
+    const size_t o_accc = slot(NC > 1 ? 2 * sizeof(float) * NC * n : 0),
+                 o_logc = slot(NC > 1 ? sizeof(sw::BlochEventC) * sw::kLogCap * NC * n : 0);
     const size_t o_mg64 = slot(shadow ? 2 * 3 * sizeof(double) * (size_t)ng * n : 0),
                  o_accd = slot(shadow ? 8 * n : 0),
                  o_log64 = slot(shadow ? sizeof(sw::BlochEvent64) * sw::kLogCap * n : 0);
@@ -771,6 +1057,9 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     GT.T = reinterpret_cast<uint8_t *const *>(dp + 2 * (size_t)n_tracks);
     GT.status = reinterpret_cast<int32_t *const *>(dp + 3 * (size_t)n_tracks);
     GT.M1d = reinterpret_cast<double *const *>(dp + 4 * (size_t)n_tracks);
+    GT.n_cls = NC;
+    GT.cls = reinterpret_cast<const uint32_t *>(d + o_gtab + o_gcls);
+    GT.gscale = reinterpret_cast<const float *>(d + o_gtab + o_gsc);
     sw::GroupState GS;
     GS.mg = reinterpret_cast<float *>(d + o_mg);
     GS.mr = GS.mg + 3 * (size_t)ng * n;
@@ -782,6 +1071,10 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     GS.mr64 = shadow ? GS.mg64 + 3 * (size_t)ng * n : nullptr;
     GS.accd_rec = shadow ? reinterpret_cast<double *>(d + o_accd) : nullptr;
     sw::BlochEvent64 *elog64 = shadow ? reinterpret_cast<sw::BlochEvent64 *>(d + o_log64) : nullptr;
+    GS.acc_c = NC > 1 ? reinterpret_cast<float *>(d + o_accc) : nullptr;
+    GS.acc_rec_c = NC > 1 ? GS.acc_c + (size_t)NC * n : nullptr;
+    sw::BlochEventC *elogc = NC > 1 ? reinterpret_cast<sw::BlochEventC *>(d + o_logc) : nullptr;
+    if (NC > 1) TR_CUDA(cudaMemsetAsync(GS.acc_c, 0, 2 * sizeof(float) * NC * n, st));
 
     uint32_t *lcnt = reinterpret_cast<uint32_t *>(d + o_lcnt);
     sw::BlochEvent *elog = reinterpret_cast<sw::BlochEvent *>(d + o_log);
@@ -829,6 +1122,18 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
         uint32_t *act = L.active + 2 * hh;
         TR_CUDA(sw::launch_refill_range(P, L.G, L.S.flags, LT, lo, hi, s));
         const unsigned gw = (hi - lo + 255) / 256, gb = (unsigned)(((size_t)ng * (hi - lo) + 255) / 256);
+        if (NC > 1) {                              // gradient classes (FP32, no shadow)
+            if (NC == 2)
+                sw::k_walk_cls<2><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+            else if (NC == 4)
+                sw::k_walk_cls<4><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+            else
+                sw::k_walk_cls<8><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+            TR_CUDA(cudaGetLastError());
+            sw::k_bloch_groups<false, false, true><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, elogc, lo, hi);
+            TR_CUDA(cudaGetLastError());
+            return SW_OK;
+        }
         if (precision == SW_PREC_KAHAN && shadow)
             sw::k_walk_logged<true, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elog64, lo, hi);
         else if (precision == SW_PREC_KAHAN)
@@ -839,11 +1144,11 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
             sw::k_walk_logged<false, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elog64, lo, hi);
         TR_CUDA(cudaGetLastError());
         if (precision == SW_PREC_FP64)
-            sw::k_bloch_groups<true, true><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, lo, hi);
+            sw::k_bloch_groups<true, true, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, nullptr, lo, hi);
         else if (shadow)
-            sw::k_bloch_groups<true, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, lo, hi);
+            sw::k_bloch_groups<true, false, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, nullptr, lo, hi);
         else
-            sw::k_bloch_groups<false, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, lo, hi);
+            sw::k_bloch_groups<false, false, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, nullptr, lo, hi);
         TR_CUDA(cudaGetLastError());
         return SW_OK;
     };

@@ -126,3 +126,51 @@ def test_tracks_reject_unknown_flag_bits():
     pr, _ = load_golden("gre")
     with pytest.raises(_lib.SpinWalkError):
         _lib.run_tracks(pr, [dict(n_dummy_scan=0)], precision=0x400)
+
+
+def _scaled(pr, t):
+    """The instance the reference's gradient scale loop runs: the sequence's gradients times the
+    scale, a float multiply (src/sim/monte_carlo.cu:287-290)."""
+    from spinwalk_gb300 import abi
+    inst = _instance(pr, t)
+    if t.get("gradient_scale") is not None:
+        sc = np.float32(t["gradient_scale"])
+        seq = dict(inst.seq.arrays)
+        for k in ("gradientX_mTm", "gradientY_mTm", "gradientZ_mTm"):
+            seq[k] = (np.asarray(seq[k], np.float32) * sc).astype(np.float32)
+        inst.seq = abi.Sequence(**seq)
+    return inst
+
+
+@pytest.mark.parametrize("scales", [(0.0, 0.5, 1.0, 2.0), (0.25,), (1.0, 3.0), (0.1, 0.2, 0.3, 0.4, 0.6, 0.7, 0.8)])
+def test_tracks_gradient_scales_equal_independent_runs(scales):
+    """Gradient-scale sweeps (the DWI b-value series) on one walk: each scale keeps its own phase
+    sums and equals sw_sim with the scaled gradients, bit for bit."""
+    pr, _ = load_golden("pgse_gradients")
+    tracks = [dict(gradient_scale=s, n_dummy_scan=0) for s in scales]
+    outs = _lib.run_tracks(pr, tracks, fill=np.nan)
+    for t, got in zip(tracks, outs):
+        want = _lib.run(_scaled(pr, t), fill=np.nan)
+        for k in ("M1", "XYZ1", "T", "status"):
+            assert bits_equal(got[k], want[k]), (t, k)
+
+
+def test_tracks_gradient_scales_with_phase_cycling_and_dummy_scans():
+    pr, _ = load_golden("pgse_gradients")
+    tracks = [dict(gradient_scale=s, linear_phase_cycling=lpc, n_dummy_scan=nd)
+              for s in (1.0, 3.0) for lpc in (0.0, 90.0) for nd in (0, 1)]
+    outs = _lib.run_tracks(pr, tracks, fill=np.nan)
+    for t, got in zip(tracks, outs):
+        want = _lib.run(_scaled(pr, t), fill=np.nan)
+        for k in ("M1", "XYZ1", "T", "status"):
+            assert bits_equal(got[k], want[k]), (t, k)
+
+
+def test_tracks_gradient_scale_limits():
+    from spinwalk_gb300 import abi
+    pr, _ = load_golden("pgse_gradients")
+    with pytest.raises(_lib.SpinWalkError):          # more than 8 distinct scales
+        _lib.run_tracks(pr, [dict(gradient_scale=0.1 * i, n_dummy_scan=0) for i in range(9)])
+    with pytest.raises(_lib.SpinWalkError):          # several scales need FP32 without shadow
+        _lib.run_tracks(pr, [dict(gradient_scale=s, n_dummy_scan=0) for s in (1.0, 2.0)],
+                        precision=abi.SW_PREC_KAHAN)

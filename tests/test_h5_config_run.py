@@ -43,6 +43,10 @@ def test_h5_reads_a_libhdf5_file():
     assert np.allclose(got.ravel(), np.arange(9) * np.pi / 4)
 
 
+GRAD_T = (200, 400, 600, 800, 1600, 1800, 2000, 2200)
+GRAD_X = (30.0, 30.0, 30.0, 0.0, 30.0, 30.0, 30.0, 0.0)
+
+
 def _write_case(tmp, scale_type, scales):
     mask, field = cylinder_phantom(20, 20e-6, 3e-6, 0.1, seed=3)
     _lib.h5_write(tmp / "phantom.h5", {"mask": mask, "fieldmap": field,
@@ -72,6 +76,10 @@ RF_T = 0 1500
 TIME_STEP = 50
 DUMMY_SCAN = 1
 LINEAR_PHASE_CYCLING = 10
+GRADIENT_T = {" ".join(str(t) for t in GRAD_T)}
+GRADIENT_X = {" ".join(str(g) for g in GRAD_X)}
+GRADIENT_Y = {" ".join("0" for _ in GRAD_T)}
+GRADIENT_Z = {" ".join("0" for _ in GRAD_T)}
 [SIMULATION_PARAMETERS]
 B0 = 9.4
 SEED = 10
@@ -84,7 +92,8 @@ WHAT_TO_SCALE = {scale_type}
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("scale_type,scales", [(0, [1.0, 0.5, 2.0]), (2, [0.0, 1.0, 3.0])])
+@pytest.mark.parametrize("scale_type,scales", [(0, [1.0, 0.5, 2.0]), (2, [0.0, 1.0, 3.0]),
+                                              (1, [0.0, 0.5, 2.0, 3.0]), (1, [1.0, 1.0])])
 def test_run_config_matches_oracle_per_scale(tmp_path, scale_type, scales):
     mask, field = _write_case(tmp_path, scale_type, scales)
     r = subprocess.run([os.path.join(ROOT, "spinwalk_gb300", "spinwalk"), "sim", "-c",
@@ -98,14 +107,19 @@ def test_run_config_matches_oracle_per_scale(tmp_path, scale_type, scales):
     xyz0 = _lib.initial_positions([20e-6] * 3, 10, 300)
     for k, s in enumerate(scales):
         s32 = np.float32(s)
+        g = np.zeros((len(GRAD_T), 3), np.float32)
+        g[:, 0] = np.asarray(GRAD_X, np.float32) * (s32 if scale_type == 1 else np.float32(1))
         kw = dict(TR_us=3050, TE_us=(1000, 3000), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
                   RF_us=(0, 1500), pXY=[[1, 0.2], [0.3, 1]], n_dummy_scan=1, n_spins=300, seed=10,
-                  diffusivity=(float(np.float32(1e-9)),) * 2)      # the INI value is std::stof'd
+                  diffusivity=(float(np.float32(1e-9)),) * 2,      # the INI value is std::stof'd
+                  gradient_us=GRAD_T, gradient_xyz=g)
         if scale_type == 0:
             fov = [float(s32 * np.float32(20e-6))] * 3
             pr = Problem(mask, fov, field, XYZ0=(xyz0 * s32).astype(np.float32),
                          linear_phase_cycling=10.0, **kw)
             pr.params.fov[:] = [float(s32 * np.float32(20e-6))] * 3
+        elif scale_type == 1:
+            pr = Problem(mask, [20e-6] * 3, field, XYZ0=xyz0, linear_phase_cycling=10.0, **kw)
         else:
             pr = Problem(mask, [20e-6] * 3, field, XYZ0=xyz0,
                          linear_phase_cycling=float(np.float32(10.0) * s32), **kw)

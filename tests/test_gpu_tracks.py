@@ -174,3 +174,34 @@ def test_tracks_gradient_scale_limits():
     with pytest.raises(_lib.SpinWalkError):          # several scales need FP32 without shadow
         _lib.run_tracks(pr, [dict(gradient_scale=s, n_dummy_scan=0) for s in (1.0, 2.0)],
                         precision=abi.SW_PREC_KAHAN)
+
+
+def _large(case, n_spins=70000):
+    """A golden case's phantom and sequence with n_spins >= 2^16: the tracks path then runs its
+    rounds as two halves of the spins on two streams."""
+    import json
+    import os
+    from spinwalk_gb300.problem import Problem
+    from tests.helpers import GOLDEN_DIR
+    z = np.load(os.path.join(GOLDEN_DIR, case + ".npz"))
+    kw = json.loads(str(z["kwargs"]))
+    kw = {k: (tuple(v) if isinstance(v, list) and k not in ("pXY", "gradient_xyz") else v)
+          for k, v in kw.items()}
+    kw["n_spins"] = n_spins
+    field = z["field_T"] if z["field_T"].size else None
+    return Problem(z["mask"], [float(z["fov"])] * 3, field, **kw)
+
+
+@pytest.mark.parametrize("case,tracks,precision,fp64", [
+    ("bssfp_phase_cycling", [dict(linear_phase_cycling=l, n_dummy_scan=d)
+                             for l in (0.0, 120.0) for d in (0, 2)], 0, False),
+    ("bssfp_phase_cycling", [dict(linear_phase_cycling=l, n_dummy_scan=1) for l in (0.0, 45.0)], 2, True),
+    ("pgse_gradients", [dict(gradient_scale=s, n_dummy_scan=0) for s in (0.0, 0.5, 1.0, 2.0)], 0, False),
+])
+def test_tracks_two_halves_equal_independent_runs(case, tracks, precision, fp64):
+    pr = _large(case)
+    outs = _lib.run_tracks(pr, tracks, fill=np.nan, precision=precision, fp64=fp64)
+    for t, got in zip(tracks, outs):
+        want = _lib.run(_scaled(pr, t), precision=precision, fp64_shadow=fp64, fill=np.nan)
+        for k in ("M1", "XYZ1", "T", "status") + (("M1_fp64",) if fp64 else ()):
+            assert bits_equal(got[k], want[k]), (case, t, k)

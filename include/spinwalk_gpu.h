@@ -262,7 +262,7 @@ typedef struct sw_track {
 /* The track's gradient waveform is the sequence's scaled by gradient_scale (float multiply, as
  * the reference's gradient scale loop does, src/sim/monte_carlo.cu:287-290). Tracks with
  * different gradient scales share the walk but not the phase: each distinct scale keeps its own
- * phase sums (at most 8 distinct scales per call, SW_PREC_FP32 only, no FP64 shadow). */
+ * phase sums (at most 8 distinct scales per call; SW_PREC_FP32 or _KAHAN, no FP64 shadow). */
 #define SW_TRACK_GRADIENT_SCALE 0x1u
 
 int sw_sim_tracks(const sw_params *param, const sw_sequence *seq, const sw_track *tracks,

@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(256)
 // sequence's gradients times gscale[c] (float multiply, as the reference's gradient scale loop,
 // monte_carlo.cu:287-290), and each event logs one pair of relaxation operators per class.
 // Every other operation is the one walk_logged_spin performs.
-template <int NC>
+template <int NC, bool KAHAN>
 __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flags,
                                               const DevParams &P, const DevTables &Tb,
                                               const GroupTables &GT, const GroupState &GS,
@@ -480,13 +480,19 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
     uint32_t ne = 0;
     const size_t n = P.n_spins;
 
-    float acc[NC], acc_rec[NC], gs[NC];
+    // per class: phase sums, their compensation terms (KAHAN), gradient scale
+    float acc[NC], acc_rec[NC], acc_e[NC], acc_rec_e[NC], gs[NC];
 #pragma unroll
     for (int c = 0; c < NC; c++) {
         acc[c] = GS.acc_c[(size_t)c * n + spin];
         acc_rec[c] = GS.acc_rec_c[(size_t)c * n + spin];
+        acc_e[c] = KAHAN ? GS.acc_c[(size_t)(2 * NC + c) * n + spin] : 0.f;
+        acc_rec_e[c] = KAHAN ? GS.acc_c[(size_t)(3 * NC + c) * n + spin] : 0.f;
         gs[c] = __ldg(GT.gscale + c);
     }
+    auto fadd = [&](float &s_, float &e_, float x) {
+        if (KAHAN) kahan_add(s_, e_, x); else s_ += x;
+    };
     uint32_t tp = S.tp[spin], tp_old = S.tp_old[spin], tp_old_rec = GS.tp_old_rec[spin];
     uint32_t ds = S.ds[spin];
     bool rec_started = GS.rec_started[spin] != 0;
@@ -494,9 +500,9 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
     uint32_t c_rf = ctr & 0xffffu, c_te = ctr >> 16, c_dph = ctr2 & 0xffffu, c_grad = ctr2 >> 16;
     bool started = (flags & kFlagStarted) != 0;
 
-    auto relax_f = [&](float a, uint32_t t0) {
+    auto relax_f = [&](float a, float e, uint32_t t0) {
         const float te = (float)((double)((tp - t0) * (uint32_t)P.timestep_us) * 1e-6);
-        return make_relax(a, __ldg(Tb.T1f + w.ts_old), __ldg(Tb.T2f + w.ts_old), te);
+        return make_relax(KAHAN ? a + e : a, __ldg(Tb.T1f + w.ts_old), __ldg(Tb.T2f + w.ts_old), te);
     };
 
     constexpr uint32_t NONE = 0xffffffffu;
@@ -519,7 +525,7 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
             tp = tp_old = 0;
             c_rf = 1; c_te = 0; c_dph = 0; c_grad = 0;
 #pragma unroll
-            for (int c = 0; c < NC; c++) { acc[c] = 0.f; acc_rec[c] = 0.f; }
+            for (int c = 0; c < NC; c++) { acc[c] = acc_e[c] = acc_rec[c] = acc_rec_e[c] = 0.f; }
             tp_old_rec = 0;
             rec_started = false;
             rec_scan = GT.rec_any[ds] != 0;
@@ -535,7 +541,7 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
             bool rl = false;
 #pragma unroll
             for (int c = 0; c < NC; c++) {
-                const RelaxOp r = relax_f(acc[c], tp_old);
+                const RelaxOp r = relax_f(acc[c], acc_e[c], tp_old);
                 put_relax(lc[ne * NC + c].r, r);
                 rl = r.relax;
             }
@@ -558,15 +564,15 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
 
 #pragma unroll
         for (int c = 0; c < NC; c++) {                              // kernels.cu:171
-            acc[c] += w.field;
-            if (rec_started) acc_rec[c] += w.field;
+            fadd(acc[c], acc_e[c], w.field);
+            if (rec_started) fadd(acc_rec[c], acc_rec_e[c], w.field);
         }
         if (tp == t_dph) {                                          // kernels.cu:175-178
             const float inc = (float)spin * __ldg(Tb.dph_deg + c_dph) / (float)P.n_spins;
 #pragma unroll
             for (int c = 0; c < NC; c++) {
-                acc[c] += inc;
-                if (rec_started) acc_rec[c] += inc;
+                fadd(acc[c], acc_e[c], inc);
+                if (rec_started) fadd(acc_rec[c], acc_rec_e[c], inc);
             }
             c_dph++;
             t_dph = c_dph < P.n_dephasing ? (uint32_t)Tb.dph_tp[c_dph] : NONE;
@@ -578,9 +584,20 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
             for (int c = 0; c < NC; c++) {
                 const double g = grad_phase_deg(gx * gs[c], gy * gs[c], gz * gs[c], xn,
                                                 (double)P.timestep_us);
-                acc[c] = d2f_exact(dadd_fp64(dbits(f2d_exact(acc[c])), dbits(g)));
-                if (rec_started)
-                    acc_rec[c] = d2f_exact(dadd_fp64(dbits(f2d_exact(acc_rec[c])), dbits(g)));
+                if (KAHAN) {
+                    const float ghi = d2f_exact(dbits(g));
+                    const float glo = d2f_exact(dadd_fp64(dbits(g), dflip(dbits(f2d_exact(ghi)))));
+                    kahan_add(acc[c], acc_e[c], ghi);
+                    kahan_add(acc[c], acc_e[c], glo);
+                    if (rec_started) {
+                        kahan_add(acc_rec[c], acc_rec_e[c], ghi);
+                        kahan_add(acc_rec[c], acc_rec_e[c], glo);
+                    }
+                } else {
+                    acc[c] = d2f_exact(dadd_fp64(dbits(f2d_exact(acc[c])), dbits(g)));
+                    if (rec_started)
+                        acc_rec[c] = d2f_exact(dadd_fp64(dbits(f2d_exact(acc_rec[c])), dbits(g)));
+                }
             }
             c_grad++;
             t_grad = c_grad < P.n_gradient ? (uint32_t)Tb.grad_tp[c_grad] : NONE;
@@ -590,16 +607,16 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
             bool rl = false, rrl = false;
 #pragma unroll
             for (int c = 0; c < NC; c++) {
-                const RelaxOp r = relax_f(acc[c], tp_old);
+                const RelaxOp r = relax_f(acc[c], acc_e[c], tp_old);
                 put_relax(lc[ne * NC + c].r, r);
                 rl = r.relax;
                 if (rec_started) {
-                    const RelaxOp rr = relax_f(acc_rec[c], tp_old_rec);
+                    const RelaxOp rr = relax_f(acc_rec[c], acc_rec_e[c], tp_old_rec);
                     put_relax(lc[ne * NC + c].rr, rr);
                     rrl = rr.relax;
-                    acc_rec[c] = 0.f;
+                    acc_rec[c] = acc_rec_e[c] = 0.f;
                 }
-                acc[c] = 0.f;
+                acc[c] = acc_e[c] = 0.f;
             }
             e.head = kEvRf | (c_rf << 8);
             e.ds = ds;
@@ -616,10 +633,11 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
             bool rl = false;
 #pragma unroll
             for (int c = 0; c < NC; c++) {
-                const RelaxOp r = relax_f(rec_started ? acc_rec[c] : acc[c], t0);
+                const RelaxOp r = rec_started ? relax_f(acc_rec[c], acc_rec_e[c], t0)
+                                              : relax_f(acc[c], acc_e[c], t0);
                 put_relax(lc[ne * NC + c].r, r);
                 rl = r.relax;
-                acc_rec[c] = 0.f;
+                acc_rec[c] = acc_rec_e[c] = 0.f;
             }
             e.head = kEvTe | (c_te << 8) | (w.ts_old << 24);
             e.ds = ds;
@@ -647,6 +665,10 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
     for (int c = 0; c < NC; c++) {
         GS.acc_c[(size_t)c * n + spin] = acc[c];
         GS.acc_rec_c[(size_t)c * n + spin] = acc_rec[c];
+        if (KAHAN) {
+            GS.acc_c[(size_t)(2 * NC + c) * n + spin] = acc_e[c];
+            GS.acc_c[(size_t)(3 * NC + c) * n + spin] = acc_rec_e[c];
+        }
     }
     GS.tp_old_rec[spin] = tp_old_rec;
     GS.rec_started[spin] = rec_started ? 1u : 0u;
@@ -662,7 +684,7 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
     return status < 0;
 }
 
-template <int NC>
+template <int NC, bool KAHAN>
 __global__ void __launch_bounds__(256)
     k_walk_cls(DevParams P, DevTables Tb, GroupTables GT, GroupState GS,
                const uint2 *__restrict__ vox, SpinState S, RngState G, uint32_t *active,
@@ -673,7 +695,8 @@ __global__ void __launch_bounds__(256)
     if (spin < spin_hi) {
         const uint32_t flags = S.flags[spin];
         if (!(flags & kFlagDone))
-            still = walk_cls_spin<NC>(spin, flags, P, Tb, GT, GS, vox, S, G, log_count, log, logc);
+            still = walk_cls_spin<NC, KAHAN>(spin, flags, P, Tb, GT, GS, vox, S, G, log_count, log,
+                                             logc);
         else
             log_count[spin] = 0;
     }
@@ -907,8 +930,9 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     }
     const uint32_t n_cls = (uint32_t)cls_scale.size();
     if (n_cls > 8) return fail(SW_ERR_INVALID, "tracks: at most 8 distinct gradient scales per call");
-    if (n_cls > 1 && (precision != SW_PREC_FP32 || shadow))
-        return fail(SW_ERR_INVALID, "tracks: several gradient scales need SW_PREC_FP32 without the FP64 shadow");
+    if (n_cls > 1 && (precision == SW_PREC_FP64 || shadow))
+        return fail(SW_ERR_INVALID, "tracks: several gradient scales need SW_PREC_FP32 or _KAHAN "
+                                    "without the FP64 shadow");
     const uint32_t NC = n_cls <= 1 ? 1u : (n_cls <= 2 ? 2u : (n_cls <= 4 ? 4u : 8u));
     std::vector<float> gsx, gsy, gsz;   // the one scale applied to the sequence's gradients
     sw_sequence qw = *seq;
@@ -962,7 +986,7 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
                  o_mg = slot(2 * 3 * sizeof(float) * (size_t)ng * n),
                  o_gs = slot(16 * n), o_lcnt = slot(4 * n),
                  o_log = slot(sizeof(sw::BlochEvent) * sw::kLogCap * n);
-    const size_t o_accc = slot(NC > 1 ? 2 * sizeof(float) * NC * n : 0),
+    const size_t o_accc = slot(NC > 1 ? 4 * sizeof(float) * NC * n : 0),   // acc, acc_rec (+ compensations)
                  o_logc = slot(NC > 1 ? sizeof(sw::BlochEventC) * sw::kLogCap * NC * n : 0);
     const size_t o_mg64 = slot(shadow ? 2 * 3 * sizeof(double) * (size_t)ng * n : 0),
                  o_accd = slot(shadow ? 8 * n : 0),
@@ -1074,7 +1098,7 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     GS.acc_c = NC > 1 ? reinterpret_cast<float *>(d + o_accc) : nullptr;
     GS.acc_rec_c = NC > 1 ? GS.acc_c + (size_t)NC * n : nullptr;
     sw::BlochEventC *elogc = NC > 1 ? reinterpret_cast<sw::BlochEventC *>(d + o_logc) : nullptr;
-    if (NC > 1) TR_CUDA(cudaMemsetAsync(GS.acc_c, 0, 2 * sizeof(float) * NC * n, st));
+    if (NC > 1) TR_CUDA(cudaMemsetAsync(GS.acc_c, 0, 4 * sizeof(float) * NC * n, st));
 
     uint32_t *lcnt = reinterpret_cast<uint32_t *>(d + o_lcnt);
     sw::BlochEvent *elog = reinterpret_cast<sw::BlochEvent *>(d + o_log);
@@ -1123,12 +1147,19 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
         TR_CUDA(sw::launch_refill_range(P, L.G, L.S.flags, LT, lo, hi, s));
         const unsigned gw = (hi - lo + 255) / 256, gb = (unsigned)(((size_t)ng * (hi - lo) + 255) / 256);
         if (NC > 1) {                              // gradient classes (FP32, no shadow)
-            if (NC == 2)
-                sw::k_walk_cls<2><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+            const bool kh = precision == SW_PREC_KAHAN;
+            if (NC == 2 && kh)
+                sw::k_walk_cls<2, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+            else if (NC == 2)
+                sw::k_walk_cls<2, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+            else if (NC == 4 && kh)
+                sw::k_walk_cls<4, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
             else if (NC == 4)
-                sw::k_walk_cls<4><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+                sw::k_walk_cls<4, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+            else if (kh)
+                sw::k_walk_cls<8, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
             else
-                sw::k_walk_cls<8><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+                sw::k_walk_cls<8, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
             TR_CUDA(cudaGetLastError());
             sw::k_bloch_groups<false, false, true><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, elogc, lo, hi);
             TR_CUDA(cudaGetLastError());

@@ -171,9 +171,23 @@ def test_tracks_gradient_scale_limits():
     pr, _ = load_golden("pgse_gradients")
     with pytest.raises(_lib.SpinWalkError):          # more than 8 distinct scales
         _lib.run_tracks(pr, [dict(gradient_scale=0.1 * i, n_dummy_scan=0) for i in range(9)])
-    with pytest.raises(_lib.SpinWalkError):          # several scales need FP32 without shadow
+    with pytest.raises(_lib.SpinWalkError):          # several scales: no FP64 arithmetic / shadow
         _lib.run_tracks(pr, [dict(gradient_scale=s, n_dummy_scan=0) for s in (1.0, 2.0)],
-                        precision=abi.SW_PREC_KAHAN)
+                        precision=abi.SW_PREC_FP64)
+    with pytest.raises(_lib.SpinWalkError):
+        _lib.run_tracks(pr, [dict(gradient_scale=s, n_dummy_scan=0) for s in (1.0, 2.0)], fp64=True)
+
+
+@pytest.mark.parametrize("scales", [(0.0, 1.0), (0.5, 1.0, 1.5, 2.0, 2.5)])
+def test_tracks_gradient_scales_kahan(scales):
+    from spinwalk_gb300 import abi
+    pr, _ = load_golden("pgse_gradients")
+    tracks = [dict(gradient_scale=s, n_dummy_scan=nd) for s in scales for nd in (0, 1)]
+    outs = _lib.run_tracks(pr, tracks, fill=np.nan, precision=abi.SW_PREC_KAHAN)
+    for t, got in zip(tracks, outs):
+        want = _lib.run(_scaled(pr, t), precision=abi.SW_PREC_KAHAN, fill=np.nan)
+        for k in ("M1", "XYZ1", "T", "status"):
+            assert bits_equal(got[k], want[k]), (t, k)
 
 
 def _large(case, n_spins=70000):

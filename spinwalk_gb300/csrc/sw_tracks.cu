@@ -16,6 +16,12 @@
 // (acc_rec, reset at each echo) diverge from the group's -- one extra state per group in a
 // recording scan. A track ends with its recording scan. Every float operation is the one the
 // plain kernel performs for that instance, so each track is bit-identical to sw_sim on it.
+//
+// Gradient scales (the reference's gradient scale loop) change the phase, not the trajectory:
+// tracks with distinct scales fall into gradient classes, and k_walk_cls keeps the phase sums
+// per class (each event logs one pair of relaxation operators per class). The rounds run as two
+// halves of the spins on two streams, so one half's refill and Bloch update overlap the other
+// half's walk.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -175,35 +175,47 @@ __global__ void k_groups_init(DevParams P, GroupTables GT, GroupState GS, const 
 enum : uint32_t { kEvScanStart = 1, kEvRf = 2, kEvTe = 3, kEvScanEnd = 4 };
 constexpr uint32_t kLogCap = 8;           // events per spin per round
 
-struct BlochEvent {
-    uint32_t head;            // type | idx << 8 | ts_old << 24   (idx: ds, pulse or echo index)
-    uint32_t ds;              // scan of the event
-    uint32_t flags;           // bit0 r.relax, bit1 rr.relax, bit2 echo phase already started
-    uint32_t pad;
-    float r[4];               // s, c, e1, e2 of the shared phase
-    float rr[4];              // the same for the recording tracks' phase (after their 1st echo)
-    float xo[4];              // scan end: position
-};
-// FP64 shadow of an event's relaxation operators (parallel array to the event log).
-struct BlochEvent64 {
-    double r[4];
-    double rr[4];
-};
-// An event's relaxation operators for one gradient class ([n][kLogCap][n_cls], parallel to the
-// event log).
-struct BlochEventC {
-    float r[4];
-    float rr[4];
+// The log is kept slot-major: every field is an array [slot][spin] (spin fastest; [slot][2][spin]
+// for the FP64 pairs, [slot][class][spin] for the class operators), so the walk's writes of
+// slot k and the Bloch kernel's reads of slot k by 32 consecutive spins are 512-byte coalesced
+// accesses, and a field an event does not use is never read.
+struct EventLog {
+    uint4 *head;              // x: type | idx << 8 | ts_old << 24 (idx: ds, pulse or echo index),
+                              // y: scan, z: flags (bit0 r.relax, bit1 rr.relax, bit2 echo phase
+                              // already started)
+    float4 *r;                // s, c, e1, e2 of the shared phase
+    float4 *rr;               // the same for the recording tracks' phase (after their 1st echo)
+    float4 *xo;               // scan end: position
+    double2 *r64, *rr64;      // FP64 shadow of r / rr: (s, c), (e1, e2)
+    float4 *rc, *rrc;         // r / rr per gradient class
+    size_t n;                 // spins (the stride of a slot)
+
+    __device__ __forceinline__ size_t at(uint32_t k, uint32_t spin) const {
+        return (size_t)k * n + spin;
+    }
+    __device__ __forceinline__ void put_head(uint32_t k, uint32_t spin, uint32_t h, uint32_t ds,
+                                             uint32_t flags) const {
+        head[at(k, spin)] = make_uint4(h, ds, flags, 0u);
+    }
 };
 
-__device__ __forceinline__ void put_relax(float *dst, const RelaxOp &r) {
-    dst[0] = r.s; dst[1] = r.c; dst[2] = r.e1; dst[3] = r.e2;
-}
-__device__ __forceinline__ RelaxOp get_relax(const float *src, bool relax) {
+__device__ __forceinline__ float4 relax4(const RelaxOp &r) { return make_float4(r.s, r.c, r.e1, r.e2); }
+__device__ __forceinline__ RelaxOp get_relax(const float4 v, bool relax) {
     RelaxOp r;
-    r.s = src[0]; r.c = src[1]; r.e1 = src[2]; r.e2 = src[3];
+    r.s = v.x; r.c = v.y; r.e1 = v.z; r.e2 = v.w;
     r.relax = relax;
     return r;
+}
+// FP64 operator pair of slot k: a[(2k) n + spin] = (s, c), a[(2k+1) n + spin] = (e1, e2)
+__device__ __forceinline__ void put_relax64(double2 *a, const EventLog &L, uint32_t k,
+                                            uint32_t spin, const double *o) {
+    a[(size_t)(2 * k) * L.n + spin] = make_double2(o[0], o[1]);
+    a[(size_t)(2 * k + 1) * L.n + spin] = make_double2(o[2], o[3]);
+}
+__device__ __forceinline__ void get_relax64(const double2 *a, const EventLog &L, uint32_t k,
+                                            uint32_t spin, double *o) {
+    const double2 p = a[(size_t)(2 * k) * L.n + spin], q = a[(size_t)(2 * k + 1) * L.n + spin];
+    o[0] = p.x; o[1] = p.y; o[2] = q.x; o[3] = q.y;
 }
 
 // KAHAN: compensated float phase sums (acc, acc_rec), as the plain kernel's SW_PREC_KAHAN.
@@ -215,8 +227,7 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
                                                  const GroupTables &GT, const GroupState &GS,
                                                  const uint2 *__restrict__ vox,
                                                  const SpinState &S, const RngState &G,
-                                                 uint32_t *log_count, BlochEvent *log,
-                                                 BlochEvent64 *log64) {
+                                                 uint32_t *log_count, const EventLog &L) {
     WalkRegs w;
     w.xo[0] = S.x[spin]; w.xo[1] = S.y[spin]; w.xo[2] = S.z[spin];
     w.ind_old = S.ind_old[spin];
@@ -227,8 +238,6 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
     w.nh = G.nhead[spin]; w.nc = G.ncnt[spin]; w.uh = G.uhead[spin]; w.uc = G.ucnt[spin];
     const float *nb = G.nbuf + (size_t)spin * kNormBuf;
     const float *ub = G.ubuf + (size_t)spin * kUnifBuf;
-    BlochEvent *lg = log + (size_t)spin * kLogCap;
-    BlochEvent64 *lg64 = SHADOW ? log64 + (size_t)spin * kLogCap : nullptr;
     uint32_t ne = 0;
 
     float acc = S.acc[spin], acc_rec = GS.acc_rec[spin];
@@ -268,10 +277,7 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
         if (ne + 4 > kLogCap) break;                                // log full: pause
         if (!started) {
             if (ds > GT.max_ds) { status = SW_SPIN_OK; break; }
-            BlochEvent &e = lg[ne++];                                // kernels.cu:110-120
-            e.head = kEvScanStart | (ds << 8);
-            e.ds = ds;
-            e.flags = 0;
+            L.put_head(ne++, spin, kEvScanStart | (ds << 8), ds, 0u);  // kernels.cu:110-120
             w.ind_old = P.matrix_length + 1;
             tp = tp_old = 0;
             c_rf = 1; c_te = 0; c_dph = 0; c_grad = 0;
@@ -290,15 +296,15 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
         }
         if (tp >= P.n_timepoints) {                                 // kernels.cu:225-231
             const RelaxOp r = relax_f(acc, acc_e, tp_old);
-            BlochEvent &e = lg[ne];
-            e.head = kEvScanEnd | (ds << 8);
-            e.ds = ds;
-            e.flags = r.relax ? 1u : 0u;
-            put_relax(e.r, r);
-            e.xo[0] = (float)dfrom(w.xo[0]); e.xo[1] = (float)dfrom(w.xo[1]); e.xo[2] = (float)dfrom(w.xo[2]);
+            L.put_head(ne, spin, kEvScanEnd | (ds << 8), ds, r.relax ? 1u : 0u);
+            L.r[L.at(ne, spin)] = relax4(r);
+            L.xo[L.at(ne, spin)] = make_float4((float)dfrom(w.xo[0]), (float)dfrom(w.xo[1]),
+                                               (float)dfrom(w.xo[2]), 0.f);
             if (SHADOW) {
                 bool rl;
-                relax_d(accd, tp_old, lg64[ne].r, rl);
+                double o[4];
+                relax_d(accd, tp_old, o, rl);
+                put_relax64(L.r64, L, ne, spin, o);
             }
             ne++;
             ds++;
@@ -357,26 +363,28 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
         }
         if (tp == t_rf) {                                           // kernels.cu:190-199
             const RelaxOp r = relax_f(acc, acc_e, tp_old);
-            BlochEvent &e = lg[ne];
-            e.head = kEvRf | (c_rf << 8);
-            e.ds = ds;
-            e.flags = (r.relax ? 1u : 0u) | (rec_started ? 4u : 0u);
-            put_relax(e.r, r);
+            uint32_t fl = (r.relax ? 1u : 0u) | (rec_started ? 4u : 0u);
+            L.r[L.at(ne, spin)] = relax4(r);
             if (SHADOW) {
                 bool rl;
-                relax_d(accd, tp_old, lg64[ne].r, rl);
+                double o[4];
+                relax_d(accd, tp_old, o, rl);
+                put_relax64(L.r64, L, ne, spin, o);
             }
             if (rec_started) {
                 const RelaxOp rr = relax_f(acc_rec, acc_rec_e, tp_old_rec);
-                e.flags |= rr.relax ? 2u : 0u;
-                put_relax(e.rr, rr);
+                fl |= rr.relax ? 2u : 0u;
+                L.rr[L.at(ne, spin)] = relax4(rr);
                 if (SHADOW) {
                     bool rl;
-                    relax_d(accd_rec, tp_old_rec, lg64[ne].rr, rl);
+                    double o[4];
+                    relax_d(accd_rec, tp_old_rec, o, rl);
+                    put_relax64(L.rr64, L, ne, spin, o);
                 }
                 acc_rec = 0.f; acc_rec_e = 0.f; accd_rec = 0.;
                 tp_old_rec = tp;
             }
+            L.put_head(ne, spin, kEvRf | (c_rf << 8), ds, fl);
             ne++;
             acc = 0.f; acc_e = 0.f; accd = 0.;
             tp_old = tp;
@@ -386,14 +394,14 @@ __device__ __forceinline__ bool walk_logged_spin(const uint32_t spin, uint32_t f
         if (tp == t_te) {                                           // kernels.cu:202-215
             const uint32_t t0 = rec_started ? tp_old_rec : tp_old;
             const RelaxOp r = rec_started ? relax_f(acc_rec, acc_rec_e, t0) : relax_f(acc, acc_e, t0);
-            BlochEvent &e = lg[ne];
-            e.head = kEvTe | (c_te << 8) | (w.ts_old << 24);
-            e.ds = ds;
-            e.flags = (r.relax ? 1u : 0u) | (rec_started ? 4u : 0u);
-            put_relax(e.r, r);
+            L.put_head(ne, spin, kEvTe | (c_te << 8) | (w.ts_old << 24), ds,
+                       (r.relax ? 1u : 0u) | (rec_started ? 4u : 0u));
+            L.r[L.at(ne, spin)] = relax4(r);
             if (SHADOW) {
                 bool rl;
-                relax_d(rec_started ? accd_rec : accd, t0, lg64[ne].r, rl);
+                double o[4];
+                relax_d(rec_started ? accd_rec : accd, t0, o, rl);
+                put_relax64(L.r64, L, ne, spin, o);
             }
             ne++;
             acc_rec = 0.f; acc_rec_e = 0.f; accd_rec = 0.;
@@ -443,15 +451,14 @@ template <bool KAHAN, bool SHADOW>
 __global__ void __launch_bounds__(256)
     k_walk_logged(DevParams P, DevTables Tb, GroupTables GT, GroupState GS,
                   const uint2 *__restrict__ vox, SpinState S, RngState G, uint32_t *active,
-                  uint32_t *log_count, BlochEvent *log, BlochEvent64 *log64, uint32_t spin_lo,
-                  uint32_t spin_hi) {
+                  uint32_t *log_count, EventLog L, uint32_t spin_lo, uint32_t spin_hi) {
     const uint32_t spin = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
     bool still = false;
     if (spin < spin_hi) {
         const uint32_t flags = S.flags[spin];
         if (!(flags & kFlagDone))
             still = walk_logged_spin<KAHAN, SHADOW>(spin, flags, P, Tb, GT, GS, vox, S, G,
-                                                    log_count, log, log64);
+                                                    log_count, L);
         else
             log_count[spin] = 0;
     }
@@ -470,7 +477,7 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
                                               const GroupTables &GT, const GroupState &GS,
                                               const uint2 *__restrict__ vox, const SpinState &S,
                                               const RngState &G, uint32_t *log_count,
-                                              BlochEvent *log, BlochEventC *logc) {
+                                              const EventLog &L) {
     WalkRegs w;
     w.xo[0] = S.x[spin]; w.xo[1] = S.y[spin]; w.xo[2] = S.z[spin];
     w.ind_old = S.ind_old[spin];
@@ -481,10 +488,9 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
     w.nh = G.nhead[spin]; w.nc = G.ncnt[spin]; w.uh = G.uhead[spin]; w.uc = G.ucnt[spin];
     const float *nb = G.nbuf + (size_t)spin * kNormBuf;
     const float *ub = G.ubuf + (size_t)spin * kUnifBuf;
-    BlochEvent *lg = log + (size_t)spin * kLogCap;
-    BlochEventC *lc = logc + (size_t)spin * kLogCap * NC;
     uint32_t ne = 0;
     const size_t n = P.n_spins;
+    auto cls_at = [&](uint32_t k, int c) { return ((size_t)k * NC + c) * n + spin; };
 
     // per class: phase sums, their compensation terms (KAHAN), gradient scale
     float acc[NC], acc_rec[NC], acc_e[NC], acc_rec_e[NC], gs[NC];
@@ -523,10 +529,7 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
         if (ne + 4 > kLogCap) break;                                // log full: pause
         if (!started) {
             if (ds > GT.max_ds) { status = SW_SPIN_OK; break; }
-            BlochEvent &e = lg[ne++];                                // kernels.cu:110-120
-            e.head = kEvScanStart | (ds << 8);
-            e.ds = ds;
-            e.flags = 0;
+            L.put_head(ne++, spin, kEvScanStart | (ds << 8), ds, 0u);  // kernels.cu:110-120
             w.ind_old = P.matrix_length + 1;
             tp = tp_old = 0;
             c_rf = 1; c_te = 0; c_dph = 0; c_grad = 0;
@@ -543,18 +546,16 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
             continue;
         }
         if (tp >= P.n_timepoints) {                                 // kernels.cu:225-231
-            BlochEvent &e = lg[ne];
             bool rl = false;
 #pragma unroll
             for (int c = 0; c < NC; c++) {
                 const RelaxOp r = relax_f(acc[c], acc_e[c], tp_old);
-                put_relax(lc[ne * NC + c].r, r);
+                L.rc[cls_at(ne, c)] = relax4(r);
                 rl = r.relax;
             }
-            e.head = kEvScanEnd | (ds << 8);
-            e.ds = ds;
-            e.flags = rl ? 1u : 0u;
-            e.xo[0] = (float)dfrom(w.xo[0]); e.xo[1] = (float)dfrom(w.xo[1]); e.xo[2] = (float)dfrom(w.xo[2]);
+            L.put_head(ne, spin, kEvScanEnd | (ds << 8), ds, rl ? 1u : 0u);
+            L.xo[L.at(ne, spin)] = make_float4((float)dfrom(w.xo[0]), (float)dfrom(w.xo[1]),
+                                               (float)dfrom(w.xo[2]), 0.f);
             ne++;
             ds++;
             started = false;
@@ -609,24 +610,22 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
             t_grad = c_grad < P.n_gradient ? (uint32_t)Tb.grad_tp[c_grad] : NONE;
         }
         if (tp == t_rf) {                                           // kernels.cu:190-199
-            BlochEvent &e = lg[ne];
             bool rl = false, rrl = false;
 #pragma unroll
             for (int c = 0; c < NC; c++) {
                 const RelaxOp r = relax_f(acc[c], acc_e[c], tp_old);
-                put_relax(lc[ne * NC + c].r, r);
+                L.rc[cls_at(ne, c)] = relax4(r);
                 rl = r.relax;
                 if (rec_started) {
                     const RelaxOp rr = relax_f(acc_rec[c], acc_rec_e[c], tp_old_rec);
-                    put_relax(lc[ne * NC + c].rr, rr);
+                    L.rrc[cls_at(ne, c)] = relax4(rr);
                     rrl = rr.relax;
                     acc_rec[c] = acc_rec_e[c] = 0.f;
                 }
                 acc[c] = acc_e[c] = 0.f;
             }
-            e.head = kEvRf | (c_rf << 8);
-            e.ds = ds;
-            e.flags = (rl ? 1u : 0u) | (rrl ? 2u : 0u) | (rec_started ? 4u : 0u);
+            L.put_head(ne, spin, kEvRf | (c_rf << 8), ds,
+                       (rl ? 1u : 0u) | (rrl ? 2u : 0u) | (rec_started ? 4u : 0u));
             if (rec_started) tp_old_rec = tp;
             ne++;
             tp_old = tp;
@@ -635,19 +634,17 @@ __device__ __forceinline__ bool walk_cls_spin(const uint32_t spin, uint32_t flag
         }
         if (tp == t_te) {                                           // kernels.cu:202-215
             const uint32_t t0 = rec_started ? tp_old_rec : tp_old;
-            BlochEvent &e = lg[ne];
             bool rl = false;
 #pragma unroll
             for (int c = 0; c < NC; c++) {
                 const RelaxOp r = rec_started ? relax_f(acc_rec[c], acc_rec_e[c], t0)
                                               : relax_f(acc[c], acc_e[c], t0);
-                put_relax(lc[ne * NC + c].r, r);
+                L.rc[cls_at(ne, c)] = relax4(r);
                 rl = r.relax;
                 acc_rec[c] = acc_rec_e[c] = 0.f;
             }
-            e.head = kEvTe | (c_te << 8) | (w.ts_old << 24);
-            e.ds = ds;
-            e.flags = (rl ? 1u : 0u) | (rec_started ? 4u : 0u);
+            L.put_head(ne, spin, kEvTe | (c_te << 8) | (w.ts_old << 24), ds,
+                       (rl ? 1u : 0u) | (rec_started ? 4u : 0u));
             ne++;
             tp_old_rec = tp;
             rec_started = true;
@@ -694,15 +691,13 @@ template <int NC, bool KAHAN>
 __global__ void __launch_bounds__(256)
     k_walk_cls(DevParams P, DevTables Tb, GroupTables GT, GroupState GS,
                const uint2 *__restrict__ vox, SpinState S, RngState G, uint32_t *active,
-               uint32_t *log_count, BlochEvent *log, BlochEventC *logc, uint32_t spin_lo,
-               uint32_t spin_hi) {
+               uint32_t *log_count, EventLog L, uint32_t spin_lo, uint32_t spin_hi) {
     const uint32_t spin = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
     bool still = false;
     if (spin < spin_hi) {
         const uint32_t flags = S.flags[spin];
         if (!(flags & kFlagDone))
-            still = walk_cls_spin<NC, KAHAN>(spin, flags, P, Tb, GT, GS, vox, S, G, log_count, log,
-                                             logc);
+            still = walk_cls_spin<NC, KAHAN>(spin, flags, P, Tb, GT, GS, vox, S, G, log_count, L);
         else
             log_count[spin] = 0;
     }
@@ -717,9 +712,8 @@ __global__ void __launch_bounds__(256)
 template <bool SHADOW, bool OUT64, bool CLS>
 __global__ void __launch_bounds__(256)
     k_bloch_groups(DevParams P, GroupTables GT, GroupState GS,
-                   const uint32_t *__restrict__ log_count, const BlochEvent *__restrict__ log,
-                   const BlochEvent64 *__restrict__ log64, const BlochEventC *__restrict__ logc,
-                   uint32_t spin_lo, uint32_t spin_hi) {
+                   const uint32_t *__restrict__ log_count, const EventLog L, uint32_t spin_lo,
+                   uint32_t spin_hi) {
     const size_t n = P.n_spins, plane = (size_t)GT.n_groups * n, n_half = spin_hi - spin_lo;
     const size_t th = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (th >= (size_t)GT.n_groups * n_half) return;
@@ -740,16 +734,18 @@ __global__ void __launch_bounds__(256)
         if (SHADOW) load_md(GS.mr64, plane, idx, mrd);
         mr_loaded = true;
     };
-    const BlochEvent *lg = log + (size_t)spin * kLogCap;
-    const BlochEvent64 *lg64 = SHADOW ? log64 + (size_t)spin * kLogCap : nullptr;
     const uint32_t ncls = CLS ? GT.n_cls : 1u, cl = CLS ? GT.cls[g] : 0u;
-    const BlochEventC *lgc = CLS ? logc + (size_t)spin * kLogCap * ncls : nullptr;
     // the event's operators: shared, or the group's class's
-    auto op_r = [&](const BlochEvent &e, uint32_t k) { return CLS ? lgc[k * ncls + cl].r : e.r; };
-    auto op_rr = [&](const BlochEvent &e, uint32_t k) { return CLS ? lgc[k * ncls + cl].rr : e.rr; };
+    auto op_r = [&](uint32_t k) {
+        return __ldg(CLS ? L.rc + ((size_t)k * ncls + cl) * n + spin : L.r + L.at(k, spin));
+    };
+    auto op_rr = [&](uint32_t k) {
+        return __ldg(CLS ? L.rrc + ((size_t)k * ncls + cl) * n + spin : L.rr + L.at(k, spin));
+    };
+    double o64[4];
     for (uint32_t k = 0; k < cnt; k++) {
-        const BlochEvent e = lg[k];
-        const uint32_t type = e.head & 0xffu, id = (e.head >> 8) & 0xffffu, ds = e.ds;
+        const uint4 hd = __ldg(L.head + L.at(k, spin));
+        const uint32_t type = hd.x & 0xffu, id = (hd.x >> 8) & 0xffffu, ds = hd.y, flags = hd.z;
         if (ds > last) continue;                                    // group finished earlier
         const int32_t t = GT.rec[(size_t)g * span + ds];
         if (type == kEvScanStart) {
@@ -762,28 +758,33 @@ __global__ void __launch_bounds__(256)
             }
         } else if (type == kEvRf) {
             const RfOp op = GT.rf[(size_t)g * P.n_RF + id];
-            apply_relax(get_relax(op_r(e, k), e.flags & 1u), m, t3);
+            apply_relax(get_relax(op_r(k), flags & 1u), m, t3);
             rf_f(op, t3, m);
             if (SHADOW) {
-                apply_relax_d(lg64[k].r, e.flags & 1u, md, u3);
+                get_relax64(L.r64, L, k, spin, o64);
+                apply_relax_d(o64, flags & 1u, md, u3);
                 rf_d(op, u3, md);
             }
-            if ((e.flags & 4u) && t >= 0) {
+            if ((flags & 4u) && t >= 0) {
                 load_mr();
-                apply_relax(get_relax(op_rr(e, k), e.flags & 2u), mr, t3);
+                apply_relax(get_relax(op_rr(k), flags & 2u), mr, t3);
                 rf_f(op, t3, mr);
                 if (SHADOW) {
-                    apply_relax_d(lg64[k].rr, e.flags & 2u, mrd, u3);
+                    get_relax64(L.rr64, L, k, spin, o64);
+                    apply_relax_d(o64, flags & 2u, mrd, u3);
                     rf_d(op, u3, mrd);
                 }
                 mr_dirty = true;
             }
         } else if (type == kEvTe) {
             if (t < 0) continue;
-            const bool from_rec = (e.flags & 4u) != 0;
+            const bool from_rec = (flags & 4u) != 0;
             if (from_rec) load_mr();
-            apply_relax(get_relax(op_r(e, k), e.flags & 1u), from_rec ? mr : m, t3);
-            if (SHADOW) apply_relax_d(lg64[k].r, e.flags & 1u, from_rec ? mrd : md, u3);
+            apply_relax(get_relax(op_r(k), flags & 1u), from_rec ? mr : m, t3);
+            if (SHADOW) {
+                get_relax64(L.r64, L, k, spin, o64);
+                apply_relax_d(o64, flags & 1u, from_rec ? mrd : md, u3);
+            }
             float *o = GT.M1[t] + 3 * ((size_t)spin * P.n_TE + id);
             if (OUT64) {
                 o[0] = (float)u3[0]; o[1] = (float)u3[1]; o[2] = (float)u3[2];
@@ -794,20 +795,22 @@ __global__ void __launch_bounds__(256)
                 double *od = GT.M1d[t] + 3 * ((size_t)spin * P.n_TE + id);
                 od[0] = u3[0]; od[1] = u3[1]; od[2] = u3[2];
             }
-            GT.T[t][(size_t)spin * P.n_TE + id] = (uint8_t)(e.head >> 24);
+            GT.T[t][(size_t)spin * P.n_TE + id] = (uint8_t)(hd.x >> 24);
             mr[0] = t3[0]; mr[1] = t3[1]; mr[2] = t3[2];
             if (SHADOW) { mrd[0] = u3[0]; mrd[1] = u3[1]; mrd[2] = u3[2]; }
             mr_loaded = mr_dirty = true;
         } else {                                                    // scan end
-            apply_relax(get_relax(op_r(e, k), e.flags & 1u), m, t3);
+            apply_relax(get_relax(op_r(k), flags & 1u), m, t3);
             m[0] = t3[0]; m[1] = t3[1]; m[2] = t3[2];
             if (SHADOW) {
-                apply_relax_d(lg64[k].r, e.flags & 1u, md, u3);
+                get_relax64(L.r64, L, k, spin, o64);
+                apply_relax_d(o64, flags & 1u, md, u3);
                 md[0] = u3[0]; md[1] = u3[1]; md[2] = u3[2];
             }
             if (t >= 0) {                                           // track t ends here
                 float *x = GT.XYZ1[t] + 3 * (size_t)spin;
-                x[0] = e.xo[0]; x[1] = e.xo[1]; x[2] = e.xo[2];
+                const float4 xo = __ldg(L.xo + L.at(k, spin));
+                x[0] = xo.x; x[1] = xo.y; x[2] = xo.z;
                 if (GT.status[t]) GT.status[t][spin] = SW_SPIN_OK;
             }
         }
@@ -991,12 +994,12 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
                  o_ptrs = slot(5 * sizeof(void *) * n_tracks),
                  o_mg = slot(2 * 3 * sizeof(float) * (size_t)ng * n),
                  o_gs = slot(16 * n), o_lcnt = slot(4 * n),
-                 o_log = slot(sizeof(sw::BlochEvent) * sw::kLogCap * n);
+                 o_log = slot(4 * 16 * sw::kLogCap * n);       // head, r, rr, xo
     const size_t o_accc = slot(NC > 1 ? 4 * sizeof(float) * NC * n : 0),   // acc, acc_rec (+ compensations)
-                 o_logc = slot(NC > 1 ? sizeof(sw::BlochEventC) * sw::kLogCap * NC * n : 0);
+                 o_logc = slot(NC > 1 ? 2 * 16 * sw::kLogCap * NC * n : 0);   // rc, rrc
     const size_t o_mg64 = slot(shadow ? 2 * 3 * sizeof(double) * (size_t)ng * n : 0),
                  o_accd = slot(shadow ? 8 * n : 0),
-                 o_log64 = slot(shadow ? sizeof(sw::BlochEvent64) * sw::kLogCap * n : 0);
+                 o_log64 = slot(shadow ? 2 * 32 * sw::kLogCap * n : 0);   // r64, rr64
     std::vector<size_t> o_M1(n_tracks), o_X(n_tracks), o_T(n_tracks), o_S(n_tracks),
         o_M1d(n_tracks);
     for (uint32_t t = 0; t < n_tracks; t++) {
@@ -1100,14 +1103,27 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
     GS.mg64 = shadow ? reinterpret_cast<double *>(d + o_mg64) : nullptr;
     GS.mr64 = shadow ? GS.mg64 + 3 * (size_t)ng * n : nullptr;
     GS.accd_rec = shadow ? reinterpret_cast<double *>(d + o_accd) : nullptr;
-    sw::BlochEvent64 *elog64 = shadow ? reinterpret_cast<sw::BlochEvent64 *>(d + o_log64) : nullptr;
     GS.acc_c = NC > 1 ? reinterpret_cast<float *>(d + o_accc) : nullptr;
     GS.acc_rec_c = NC > 1 ? GS.acc_c + (size_t)NC * n : nullptr;
-    sw::BlochEventC *elogc = NC > 1 ? reinterpret_cast<sw::BlochEventC *>(d + o_logc) : nullptr;
     if (NC > 1) TR_CUDA(cudaMemsetAsync(GS.acc_c, 0, 4 * sizeof(float) * NC * n, st));
 
     uint32_t *lcnt = reinterpret_cast<uint32_t *>(d + o_lcnt);
-    sw::BlochEvent *elog = reinterpret_cast<sw::BlochEvent *>(d + o_log);
+    // the event log, slot-major ([slot][spin] per field)
+    sw::EventLog elog{};
+    elog.n = n;
+    const size_t slot_n = (size_t)sw::kLogCap * n;
+    elog.head = reinterpret_cast<uint4 *>(d + o_log);
+    elog.r = reinterpret_cast<float4 *>(d + o_log + 16 * slot_n);
+    elog.rr = reinterpret_cast<float4 *>(d + o_log + 32 * slot_n);
+    elog.xo = reinterpret_cast<float4 *>(d + o_log + 48 * slot_n);
+    if (shadow) {
+        elog.r64 = reinterpret_cast<double2 *>(d + o_log64);
+        elog.rr64 = reinterpret_cast<double2 *>(d + o_log64 + 32 * slot_n);
+    }
+    if (NC > 1) {
+        elog.rc = reinterpret_cast<float4 *>(d + o_logc);
+        elog.rrc = reinterpret_cast<float4 *>(d + o_logc + 16 * slot_n * NC);
+    }
     sw::LogfTables LT = sw::api::device_logf_tables();
     if (!LT.bitmap) return fail(SW_ERR_CUDA, "logf tables unavailable");
     if (!mt && !(LT.ms_delta = sw::api::minstd_delta_table())) return SW_ERR_CUDA;
@@ -1155,37 +1171,37 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
         if (NC > 1) {                              // gradient classes (FP32, no shadow)
             const bool kh = precision == SW_PREC_KAHAN;
             if (NC == 2 && kh)
-                sw::k_walk_cls<2, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+                sw::k_walk_cls<2, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, lo, hi);
             else if (NC == 2)
-                sw::k_walk_cls<2, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+                sw::k_walk_cls<2, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, lo, hi);
             else if (NC == 4 && kh)
-                sw::k_walk_cls<4, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+                sw::k_walk_cls<4, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, lo, hi);
             else if (NC == 4)
-                sw::k_walk_cls<4, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+                sw::k_walk_cls<4, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, lo, hi);
             else if (kh)
-                sw::k_walk_cls<8, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+                sw::k_walk_cls<8, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, lo, hi);
             else
-                sw::k_walk_cls<8, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elogc, lo, hi);
+                sw::k_walk_cls<8, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, lo, hi);
             TR_CUDA(cudaGetLastError());
-            sw::k_bloch_groups<false, false, true><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, elogc, lo, hi);
+            sw::k_bloch_groups<false, false, true><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, lo, hi);
             TR_CUDA(cudaGetLastError());
             return SW_OK;
         }
         if (precision == SW_PREC_KAHAN && shadow)
-            sw::k_walk_logged<true, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elog64, lo, hi);
+            sw::k_walk_logged<true, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, lo, hi);
         else if (precision == SW_PREC_KAHAN)
-            sw::k_walk_logged<true, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elog64, lo, hi);
+            sw::k_walk_logged<true, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, lo, hi);
         else if (shadow)
-            sw::k_walk_logged<false, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elog64, lo, hi);
+            sw::k_walk_logged<false, true><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, lo, hi);
         else
-            sw::k_walk_logged<false, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, elog64, lo, hi);
+            sw::k_walk_logged<false, false><<<gw, 256, 0, s>>>(P, Tb, GT, GS, L.vox, L.S, L.G, act, lcnt, elog, lo, hi);
         TR_CUDA(cudaGetLastError());
         if (precision == SW_PREC_FP64)
-            sw::k_bloch_groups<true, true, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, nullptr, lo, hi);
+            sw::k_bloch_groups<true, true, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, lo, hi);
         else if (shadow)
-            sw::k_bloch_groups<true, false, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, nullptr, lo, hi);
+            sw::k_bloch_groups<true, false, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, lo, hi);
         else
-            sw::k_bloch_groups<false, false, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, elog64, nullptr, lo, hi);
+            sw::k_bloch_groups<false, false, false><<<gb, 256, 0, s>>>(P, GT, GS, lcnt, elog, lo, hi);
         TR_CUDA(cudaGetLastError());
         return SW_OK;
     };

@@ -18,7 +18,8 @@ Workloads: gradient echo, 200^3 cylinders, 1e5 spins, 401 time points; spin echo
 1e6 spins, 2001 time points, permeability 0.01; the 64-instance FoV sweep (32 radii x GRE/SE,
 1e4-1e6 spins each) through sw_sim_batch; bSSFP on 300^3 cylinders with 2e5 spins and 210 TRs
 of 200 time points, through sw_sim_tracks (a subset of the 640 phase-cycle x dummy-scan
-instances).
+instances); requests of the serving trace on its resident 100^3, 200^3 and 800^3 phantoms
+through one engine (each the same alone and in the mix).
 """
 import numpy as np
 import pytest
@@ -152,3 +153,30 @@ def test_full_size_bssfp_tracks():
         _check_rows(outs[j], _oracle_rows(pr, ids), ids, f"track {j}")
     for o in outs:
         assert _norm_bound(o["M1"], o["status"]) <= 1.0 + 1e-6
+
+
+def test_full_size_serving_trace():
+    """Requests of the serving trace (GRE / SE / PGSE along x, y, z on the resident 100^3,
+    200^3 and 800^3 phantoms, 1e4-2e6 spins) submitted to one engine in arrival order while the
+    earlier ones run, with the serving benchmark's slots (8 x 2^20 spins, so the larger jobs run
+    in chunks): each result equals the request run alone bit for bit, and sampled spins equal
+    the oracle."""
+    reqs, phantoms, arrivals, desc = bench.serve_requests(40)
+    picked = [pr for pr in reqs if pr.params.n_spins <= 2_000_000][:12]
+    assert len({pr.mask.shape for pr in picked}) > 1
+    eng = _lib.Engine(n_slots=8, slot_spins=1 << 20)
+    pids, outs, done = {}, [], []
+    for pr in picked:
+        if pr.mask.shape not in pids:
+            pids[pr.mask.shape] = eng.add_phantom(pr)
+        outs.append(eng.submit(pr, pids[pr.mask.shape], fill=np.nan)[1])
+        done += eng.poll(wait=0)
+    done += eng.run_all()
+    eng.close()
+    assert len(done) == len(picked) and all(rc == 0 for _, rc, _ in done)
+    for k, (pr, o) in enumerate(zip(picked, outs)):
+        alone = _lib.run(pr, fill=np.nan)
+        for key in ("M1", "XYZ1", "T", "status"):
+            assert bits_equal(o[key], alone[key]), f"request {k}: {key} differs in the mix"
+        ids = _sample_ids(pr.params.n_spins, 64)
+        _check_rows(alone, _oracle_rows(pr, ids), ids, f"request {k}")

@@ -20,14 +20,18 @@
 #include "sw_config.h"
 #include "sw_h5.h"
 
+namespace sw {
+namespace api {
+int fail(int code, const std::string &msg);   // sets sw_last_error() (sw_api.cu)
+}  // namespace api
+}  // namespace sw
+
 namespace {
 
-thread_local std::string g_drv_err;
-
+// Reports on stderr, as the reference's driver logs, and sets sw_last_error().
 int drv_fail(int rc, const std::string &m) {
-    g_drv_err = m;
     std::fprintf(stderr, "spinwalk: %s\n", m.c_str());
-    return rc;
+    return sw::api::fail(rc, m);
 }
 
 template <typename T>

@@ -96,9 +96,11 @@ WHAT_TO_SCALE = {scale_type}
                                               (1, [0.0, 0.5, 2.0, 3.0]), (1, [1.0, 1.0])])
 def test_run_config_matches_oracle_per_scale(tmp_path, scale_type, scales):
     mask, field = _write_case(tmp_path, scale_type, scales)
-    r = subprocess.run([os.path.join(ROOT, "spinwalk_gb300", "spinwalk"), "sim", "-c",
-                        str(tmp_path / "cfg.ini")], capture_output=True, text=True)
+    r = subprocess.run([os.path.join(ROOT, "spinwalk_gb300", "spinwalk"), "-l",
+                        str(tmp_path / "run.log"), "sim", "-c", str(tmp_path / "cfg.ini")],
+                       capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+    assert "Finished " + str(tmp_path / "cfg.ini") in (tmp_path / "run.log").read_text()
     out = tmp_path / "out" / "test_phantom.h5"
     M, XYZ, T = _lib.h5_read(out, "M"), _lib.h5_read(out, "XYZ"), _lib.h5_read(out, "T")
     assert M.shape == (len(scales), 300, 2, 3) and T.shape == (len(scales), 300, 2, 1)
@@ -136,3 +138,35 @@ def test_cli_rejects_cpu_flag_and_bad_config(tmp_path):
     assert r.returncode == 1 and "GPU only" in r.stderr
     (tmp_path / "bad.ini").write_text("[SCAN_PARAMETERS]\nTE = 5 1\n")
     assert _lib.config_dump(str(tmp_path / "bad.ini"), tmp_path / "d.txt") != 0
+
+
+def test_cli_log_file_and_option_forms(tmp_path):
+    """The reference's global -l/--log option (default log_spinwalk.txt in the working
+    directory, appended): the CLI accepts it in both forms, and a failed config is logged."""
+    exe = os.path.join(ROOT, "spinwalk_gb300", "spinwalk")
+    missing = str(tmp_path / "missing.ini")
+    for args, log in ((["-l", str(tmp_path / "a.log"), "sim", "-c", missing], tmp_path / "a.log"),
+                      ([f"--log={tmp_path / 'b.log'}", "sim", f"--configs={missing}", "--device=0"],
+                       tmp_path / "b.log"),
+                      (["sim", "-c", missing, "-d", "0"], tmp_path / "log_spinwalk.txt")):
+        r = subprocess.run([exe, *args], capture_output=True, text=True, cwd=tmp_path)
+        assert r.returncode == 1, r.stdout + r.stderr
+        assert "Aborting" in r.stdout
+        lines = log.read_text().splitlines()
+        assert any("[info]: Simulating " + missing in ln for ln in lines)
+        err = [ln for ln in lines if "[error]: " + missing + ": " in ln]
+        assert err and all(ln.split(missing + ": ", 1)[1].strip() for ln in err), lines
+    r = subprocess.run([exe, "--log"], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 1 and "usage" in r.stderr
+
+
+def test_driver_errors_set_last_error(tmp_path):
+    """Errors of the HDF5 helpers and of the driver come back as a code plus a message in
+    sw_last_error(), like every other entry point."""
+    with pytest.raises(_lib.SpinWalkError, match=r"spinwalk error -?\d+: \S"):
+        _lib.h5_read(tmp_path / "none.h5", "M")
+    _lib.h5_write(tmp_path / "ok.h5", {"M": np.zeros((2, 3), np.float32)})
+    with pytest.raises(_lib.SpinWalkError, match=r"spinwalk error -?\d+: \S"):
+        _lib.h5_read(tmp_path / "ok.h5", "no_such_dataset")
+    with pytest.raises(_lib.SpinWalkError, match=r"spinwalk error -?\d+: \S"):
+        _lib.run_config(tmp_path / "missing.ini")

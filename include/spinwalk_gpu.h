@@ -157,9 +157,12 @@ int sw_config_dump(const char *ini_path, const char *out_path);
  */
 int sw_run_config(const char *ini_path, int device);
 
-/* Whole-dataset HDF5 I/O (root group; uint8 = 0, float32 = 1, float64 = 2; little-endian,
- * contiguous): the subset SpinWalk's phantom and result files use. sw_h5_read with out == NULL
- * only reports type, rank and dims. */
+/* Whole-dataset HDF5 I/O (root group; little-endian, contiguous or compact): the subset
+ * SpinWalk's phantom and result files use. Type codes: uint8 = 0, float32 = 1, float64 = 2,
+ * int8 = 3, uint16 = 4, int16 = 5, uint32 = 6, int32 = 7, uint64 = 8, int64 = 9. sw_h5_read
+ * returns the stored type and bytes (with out == NULL only type, rank and dims); sw_run_config
+ * converts what it reads to the types the reference reads (mask uint8, the rest float) as
+ * libhdf5 does: integers saturate, floats truncate toward zero (NaN -> 0). */
 int sw_h5_write(const char *path, int n, const char *const *names, const int *types,
                 const int *ranks, const uint64_t *dims, const void *const *data);
 int sw_h5_read(const char *path, const char *name, int *type, int *rank, uint64_t dims[8],

@@ -164,8 +164,9 @@ def config_dump(ini_path, out_path):
     return lib().sw_config_dump(str(ini_path).encode(), str(out_path).encode())
 
 
-_H5_TYPES = {np.dtype(np.uint8): 0, np.dtype(np.float32): 1, np.dtype(np.float64): 2}
-_H5_DTYPES = {0: np.uint8, 1: np.float32, 2: np.float64}
+_H5_DTYPES = {0: np.uint8, 1: np.float32, 2: np.float64, 3: np.int8, 4: np.uint16, 5: np.int16,
+              6: np.uint32, 7: np.int32, 8: np.uint64, 9: np.int64}
+_H5_TYPES = {np.dtype(t): c for c, t in _H5_DTYPES.items()}
 
 
 def h5_write(path, datasets):

@@ -11,7 +11,9 @@
 #include <cstdio>
 #include <cstring>
 #include <filesystem>
+#include <limits>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -34,26 +36,7 @@ int drv_fail(int rc, const std::string &m) {
     return sw::api::fail(rc, m);
 }
 
-template <typename T>
-bool read_as(const std::string &file, const char *name, std::vector<T> &out,
-             std::vector<uint64_t> *dims, std::string &err) {
-    sw::h5::Dataset d;
-    if (!sw::h5::read(file, name, d, err)) return false;
-    uint64_t n = 1;
-    for (uint64_t x : d.dims) n *= x;
-    out.resize(n);
-    if (d.type == sw::h5::kU8) {
-        for (uint64_t i = 0; i < n; i++) out[i] = (T)(uint8_t)d.data[i];
-    } else if (d.type == sw::h5::kF32) {
-        const float *p = reinterpret_cast<const float *>(d.data.data());
-        for (uint64_t i = 0; i < n; i++) out[i] = (T)p[i];
-    } else {
-        const double *p = reinterpret_cast<const double *>(d.data.data());
-        for (uint64_t i = 0; i < n; i++) out[i] = (T)p[i];
-    }
-    if (dims) *dims = d.dims;
-    return true;
-}
+
 
 template <typename T>
 sw::h5::Dataset make_ds(const std::vector<uint64_t> &dims, const std::vector<T> &v, sw::h5::Type t) {
@@ -101,9 +84,9 @@ extern "C" int sw_run_config(const char *ini_path, int device) {
         std::vector<float> field, fov;
         std::vector<uint8_t> mask;
         std::vector<uint64_t> dims;
-        if (!read_as(ph, "fieldmap", field, nullptr, err)) field.clear();
-        if (!read_as(ph, "mask", mask, &dims, err)) return drv_fail(SW_ERR_IO, err);
-        if (!read_as(ph, "fov", fov, nullptr, err)) return drv_fail(SW_ERR_IO, err);
+        if (!sw::h5::read_as(ph, "fieldmap", field, nullptr, err)) field.clear();
+        if (!sw::h5::read_as(ph, "mask", mask, &dims, err)) return drv_fail(SW_ERR_IO, err);
+        if (!sw::h5::read_as(ph, "fov", fov, nullptr, err)) return drv_fail(SW_ERR_IO, err);
         if (dims.size() != 3 || fov.size() < 3) return drv_fail(SW_ERR_IO, ph + ": mask must be 3-D, fov 3 values");
         for (int i = 0; i < 3; i++) p.phantom_size[i] = dims[i];
         const uint32_t nsub = mask.empty() ? 0 : (uint32_t)*std::max_element(mask.begin(), mask.end()) + 1;
@@ -113,7 +96,7 @@ extern "C" int sw_run_config(const char *ini_path, int device) {
         const std::string &xf = c.files["XYZ0"][ip];
         if (!xf.empty()) {
             std::vector<float> x;
-            if (!read_as(xf, "XYZ", x, nullptr, err)) return drv_fail(SW_ERR_IO, err);
+            if (!sw::h5::read_as(xf, "XYZ", x, nullptr, err)) return drv_fail(SW_ERR_IO, err);
             if (x.size() < XYZ0.size()) return drv_fail(SW_ERR_IO, xf + ": XYZ holds fewer spins than NUMBER_OF_SPINS");
             std::copy(x.begin(), x.begin() + XYZ0.size(), XYZ0.begin());
             for (size_t i = 0; i < XYZ0.size(); i++)
@@ -127,7 +110,7 @@ extern "C" int sw_run_config(const char *ini_path, int device) {
         const std::string &mf = c.files["M0"][ip];
         if (!mf.empty()) {
             std::vector<float> m;
-            if (!read_as(mf, "M", m, nullptr, err)) return drv_fail(SW_ERR_IO, err);
+            if (!sw::h5::read_as(mf, "M", m, nullptr, err)) return drv_fail(SW_ERR_IO, err);
         }
         for (size_t i = 0; i < M0.size(); i++) M0[i] = (i % 3 == 2) ? 1.f : 0.f;
         XYZ0s = XYZ0;
@@ -262,6 +245,8 @@ extern "C" int sw_h5_write(const char *path, int n, const char *const *names, co
     size_t dpos = 0;
     for (int i = 0; i < n; i++) {
         sw::h5::Dataset d;
+        if (!sw::h5::valid_type(types[i]))
+            return drv_fail(SW_ERR_INVALID, std::string("dataset ") + names[i] + ": unknown type code");
         d.type = (sw::h5::Type)types[i];
         uint64_t cnt = 1;
         for (int r = 0; r < ranks[i]; r++) {
@@ -269,7 +254,7 @@ extern "C" int sw_h5_write(const char *path, int n, const char *const *names, co
             cnt *= dims[dpos + r];
         }
         dpos += ranks[i];
-        const size_t esz = d.type == sw::h5::kU8 ? 1 : (d.type == sw::h5::kF32 ? 4 : 8);
+        const size_t esz = sw::h5::type_size(d.type);
         d.data.resize(cnt * esz);
         if (cnt) std::memcpy(d.data.data(), data[i], cnt * esz);
         sets.push_back({names[i], std::move(d)});

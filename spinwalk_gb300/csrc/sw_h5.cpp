@@ -195,7 +195,10 @@ bool read(const std::string &file, const std::string &name, Dataset &out, std::s
     if (!little) { err = "big-endian data are not supported"; return false; }
     uint64_t count = 1;
     for (uint64_t d : out.dims) count *= d;
-    if (dtype_class == 0 && dtype_size == 1 && !is_signed) out.type = kU8;
+    if (dtype_class == 0 && dtype_size == 1) out.type = is_signed ? kI8 : kU8;
+    else if (dtype_class == 0 && dtype_size == 2) out.type = is_signed ? kI16 : kU16;
+    else if (dtype_class == 0 && dtype_size == 4) out.type = is_signed ? kI32 : kU32;
+    else if (dtype_class == 0 && dtype_size == 8) out.type = is_signed ? kI64 : kU64;
     else if (dtype_class == 1 && dtype_size == 4) out.type = kF32;
     else if (dtype_class == 1 && dtype_size == 8) out.type = kF64;
     else { err = "dataset " + name + ": unsupported datatype"; return false; }
@@ -324,7 +327,8 @@ bool write(const std::string &file, const std::vector<std::pair<std::string, Dat
     std::vector<uint64_t> ohdr(sorted.size());
     for (size_t i = 0; i < sorted.size(); i++) {
         const Dataset &d = *sorted[i].second;
-        const uint64_t esz = d.type == kU8 ? 1 : (d.type == kF32 ? 4 : 8);
+        if (!valid_type(d.type)) { err = "dataset " + sorted[i].first + ": unknown type"; return false; }
+        const uint64_t esz = type_size(d.type);
         uint64_t count = 1;
         for (uint64_t x : d.dims) count *= x;
         if (d.data.size() != count * esz) { err = "dataset " + sorted[i].first + ": size mismatch"; return false; }
@@ -335,11 +339,11 @@ bool write(const std::string &file, const std::vector<std::pair<std::string, Dat
         std::vector<char> sp{1, (char)d.dims.size(), 0, 0, 0, 0, 0, 0};
         for (uint64_t x : d.dims) app(sp, le(x, 8));
         std::vector<char> dt;
-        if (d.type == kU8) {
-            dt = {0x10, 0, 0, 0};                          // version 1, fixed-point, LE unsigned
-            app(dt, le(1, 4));
-            app(dt, le(0, 2));
-            app(dt, le(8, 2));
+        if (!is_float(d.type)) {                           // version 1, fixed-point, LE
+            dt = {0x10, (char)(is_signed_int(d.type) ? 0x08 : 0), 0, 0};
+            app(dt, le(esz, 4));
+            app(dt, le(0, 2));                             // bit offset
+            app(dt, le(8 * esz, 2));                       // bit precision
         } else {
             const bool f32 = d.type == kF32;
             dt = {0x11, 0x20, (char)(f32 ? 31 : 63), 0};   // version 1, IEEE float, LE

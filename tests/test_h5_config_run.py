@@ -1,6 +1,7 @@
 """HDF5 subset (phantom / result files) and the `spinwalk sim -c cfg.ini` drop-in path."""
 import glob
 import os
+import shutil
 import subprocess
 
 import numpy as np
@@ -28,6 +29,35 @@ def test_h5_roundtrip(tmp_path):
         assert bits_equal(got, v), k
     with pytest.raises(_lib.SpinWalkError):
         _lib.h5_read(f, "missing")
+
+
+def test_h5_integer_types_roundtrip(tmp_path):
+    """Integer datasets of every width and signedness (MATLAB writes masks as int8, h5py may
+    write int64): stored and read back with their own type."""
+    rng = np.random.default_rng(1)
+    data = {f"d_{np.dtype(t).name}": rng.integers(np.iinfo(t).min, np.iinfo(t).max, (3, 4, 5),
+                                                  dtype=t, endpoint=True)
+            for t in (np.int8, np.uint16, np.int16, np.uint32, np.int32, np.uint64, np.int64)}
+    f = tmp_path / "ints.h5"
+    _lib.h5_write(f, data)
+    for k, v in data.items():
+        got = _lib.h5_read(f, k)
+        assert got.dtype == v.dtype and bits_equal(got, v), k
+
+
+def test_h5_type_conversion_rules(tmp_path):
+    """The conversion sw_run_config applies to datasets stored in other types than the
+    reference reads (mask uint8, the rest float), with libhdf5's rules (tests/h5_convert_check.cpp)."""
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    exe = tmp_path / "h5_convert_check"
+    csrc = os.path.join(ROOT, "spinwalk_gb300", "csrc")
+    subprocess.run([gxx, "-O2", "-std=c++17", f"-I{csrc}",
+                    os.path.join(ROOT, "tests", "h5_convert_check.cpp"), "-o", str(exe)],
+                   check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout
 
 
 def test_h5_reads_a_libhdf5_file():
@@ -170,3 +200,25 @@ def test_driver_errors_set_last_error(tmp_path):
         _lib.h5_read(tmp_path / "ok.h5", "no_such_dataset")
     with pytest.raises(_lib.SpinWalkError, match=r"spinwalk error -?\d+: \S"):
         _lib.run_config(tmp_path / "missing.ini")
+
+
+@pytest.mark.gpu
+def test_run_config_reads_matlab_style_phantom(tmp_path):
+    """The reference README's MATLAB recipe stores the mask as int8 (MATLAB has no uint8 HDF5
+    writer) and h5py users often keep float64 arrays: the same config run on such a phantom
+    (int8 mask, float64 fieldmap and fov, float32 values widened) writes the result file of the
+    uint8 / float32 phantom, bit for bit."""
+    mask, field = _write_case(tmp_path, 0, [1.0, 2.0])
+    _lib.h5_write(tmp_path / "phantom_m.h5", {"mask": mask.astype(np.int8),
+                                              "fieldmap": field.astype(np.float64),
+                                              "fov": np.array([20e-6] * 3, np.float32).astype(np.float64)})
+    cfg = (tmp_path / "cfg.ini").read_text()
+    (tmp_path / "cfg_m.ini").write_text(cfg.replace("PHANTOM[0] = phantom.h5", "PHANTOM[0] = phantom_m.h5"))
+    exe = os.path.join(ROOT, "spinwalk_gb300", "spinwalk")
+    for ini in ("cfg.ini", "cfg_m.ini"):
+        r = subprocess.run([exe, "-l", str(tmp_path / "run.log"), "sim", "-c", str(tmp_path / ini)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+    a, b = tmp_path / "out" / "test_phantom.h5", tmp_path / "out" / "test_phantom_m.h5"
+    for k in ("M", "XYZ", "T", "scales", "TE"):
+        assert bits_equal(_lib.h5_read(a, k), _lib.h5_read(b, k)), k

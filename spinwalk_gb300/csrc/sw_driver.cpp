@@ -54,10 +54,7 @@ extern "C" int sw_run_config(const char *ini_path, int device) {
     using clock = std::chrono::steady_clock;
     const auto t_run = clock::now();
     if (!ini_path) return drv_fail(SW_ERR_INVALID, "no config file");
-    if (cudaSetDevice(device) != cudaSuccess) {
-        cudaGetLastError();
-        return drv_fail(SW_ERR_CUDA, "device " + std::to_string(device) + " is not available");
-    }
+    bool device_set = false;        // selected before the first simulation, after the inputs
     sw::Config c;
     std::string err;
     int rc = sw::config_read(ini_path, c, err);
@@ -84,10 +81,21 @@ extern "C" int sw_run_config(const char *ini_path, int device) {
         std::vector<float> field, fov;
         std::vector<uint8_t> mask;
         std::vector<uint64_t> dims;
-        if (!sw::h5::read_as(ph, "fieldmap", field, nullptr, err)) field.clear();
+        // the fieldmap is optional: absent means none, present but unreadable is an error
+        if (!sw::h5::exists(ph, "fieldmap")) field.clear();
+        else if (!sw::h5::read_as(ph, "fieldmap", field, nullptr, err)) return drv_fail(SW_ERR_IO, err);
         if (!sw::h5::read_as(ph, "mask", mask, &dims, err)) return drv_fail(SW_ERR_IO, err);
         if (!sw::h5::read_as(ph, "fov", fov, nullptr, err)) return drv_fail(SW_ERR_IO, err);
-        if (dims.size() != 3 || fov.size() < 3) return drv_fail(SW_ERR_IO, ph + ": mask must be 3-D, fov 3 values");
+        // h5_helper::read without resizing (h5_helper.h:59-66): fov holds exactly 3 values
+        if (fov.size() != 3)
+            return drv_fail(SW_ERR_IO, ph + ": dataset \"fov\" has different size " +
+                                           std::to_string(fov.size()) + " vs 3");
+        if (dims.size() != 3) return drv_fail(SW_ERR_IO, ph + ": mask must be 3-D");
+        // the reference indexes the fieldmap with the mask's voxel index and never checks
+        // their sizes; a shorter fieldmap would be read past its end, so it is refused
+        if (!field.empty() && field.size() != mask.size())
+            return drv_fail(SW_ERR_INVALID, ph + ": fieldmap has " + std::to_string(field.size()) +
+                                                " voxels, mask " + std::to_string(mask.size()));
         for (int i = 0; i < 3; i++) p.phantom_size[i] = dims[i];
         const uint32_t nsub = mask.empty() ? 0 : (uint32_t)*std::max_element(mask.begin(), mask.end()) + 1;
         if (nsub > p.n_substrate)
@@ -97,8 +105,11 @@ extern "C" int sw_run_config(const char *ini_path, int device) {
         if (!xf.empty()) {
             std::vector<float> x;
             if (!sw::h5::read_as(xf, "XYZ", x, nullptr, err)) return drv_fail(SW_ERR_IO, err);
-            if (x.size() < XYZ0.size()) return drv_fail(SW_ERR_IO, xf + ": XYZ holds fewer spins than NUMBER_OF_SPINS");
-            std::copy(x.begin(), x.begin() + XYZ0.size(), XYZ0.begin());
+            if (x.size() != XYZ0.size())           // h5_helper::read without resizing
+                return drv_fail(SW_ERR_IO, xf + ": dataset \"XYZ\" has different size " +
+                                               std::to_string(x.size()) + " vs " +
+                                               std::to_string(XYZ0.size()));
+            std::copy(x.begin(), x.end(), XYZ0.begin());
             for (size_t i = 0; i < XYZ0.size(); i++)
                 if (XYZ0[i] < 0 || XYZ0[i] > fov[i % 3])
                     return drv_fail(SW_ERR_INVALID, "Initial positions are outside the FoV.");
@@ -111,8 +122,19 @@ extern "C" int sw_run_config(const char *ini_path, int device) {
         if (!mf.empty()) {
             std::vector<float> m;
             if (!sw::h5::read_as(mf, "M", m, nullptr, err)) return drv_fail(SW_ERR_IO, err);
+            if (m.size() != M0.size())              // h5_helper::read without resizing
+                return drv_fail(SW_ERR_IO, mf + ": dataset \"M\" has different size " +
+                                               std::to_string(m.size()) + " vs " +
+                                               std::to_string(M0.size()));
         }
         for (size_t i = 0; i < M0.size(); i++) M0[i] = (i % 3 == 2) ? 1.f : 0.f;
+        if (!device_set) {
+            if (cudaSetDevice(device) != cudaSuccess) {
+                cudaGetLastError();
+                return drv_fail(SW_ERR_CUDA, "device " + std::to_string(device) + " is not available");
+            }
+            device_set = true;
+        }
         XYZ0s = XYZ0;
         p.matrix_length = (int64_t)mask.size();
         p.fieldmap_exist = field.empty() ? 0 : 1;

@@ -222,3 +222,50 @@ def test_run_config_reads_matlab_style_phantom(tmp_path):
     a, b = tmp_path / "out" / "test_phantom.h5", tmp_path / "out" / "test_phantom_m.h5"
     for k in ("M", "XYZ", "T", "scales", "TE"):
         assert bits_equal(_lib.h5_read(a, k), _lib.h5_read(b, k)), k
+
+
+def _expect_run_error(ini, *fragments):
+    with pytest.raises(_lib.SpinWalkError) as e:
+        _lib.run_config(ini)
+    for f in fragments:
+        assert f in str(e.value), str(e.value)
+
+
+def test_run_config_input_checks(tmp_path):
+    """Phantom and start-file checks of sw_run_config, made before any GPU is selected: fov,
+    XYZ and M must have exactly the size the reference reads them with (h5_helper::read without
+    resizing fails on any other size); a fieldmap must have as many voxels as the mask (the
+    reference would read past a shorter one)."""
+    mask, field = _write_case(tmp_path, 0, [1.0])
+    cfg = (tmp_path / "cfg.ini").read_text()
+    fov = np.array([20e-6] * 3, np.float32)
+
+    def case(name, phantom=None, xyz=None, m=None):
+        d = tmp_path / name
+        d.mkdir()
+        _lib.h5_write(d / "phantom.h5", phantom or {"mask": mask, "fieldmap": field, "fov": fov})
+        extra = ""
+        if xyz is not None:
+            _lib.h5_write(d / "xyz.h5", {"XYZ": xyz})
+            extra += "XYZ0[0] = xyz.h5\n"
+        if m is not None:
+            _lib.h5_write(d / "m.h5", {"M": m})
+            extra += "M0[0] = m.h5\n"
+        (d / "cfg.ini").write_text(cfg.replace("PHANTOM[0] = phantom.h5",
+                                               "PHANTOM[0] = phantom.h5\n" + extra))
+        return d / "cfg.ini"
+
+    _expect_run_error(case("fov4", {"mask": mask, "fov": np.append(fov, 1e-6).astype(np.float32)}),
+                      '"fov" has different size 4 vs 3')
+    _expect_run_error(case("short_field", {"mask": mask, "fieldmap": field.ravel()[:-1].copy(),
+                                           "fov": fov}), "fieldmap has", "voxels")
+    xyz = np.full((301, 3), 10e-6, np.float32)
+    _expect_run_error(case("xyz_long", xyz=xyz), '"XYZ" has different size 903 vs 900')
+    _expect_run_error(case("xyz_out", xyz=np.full((300, 3), 30e-6, np.float32)),
+                      "outside the FoV")
+    _expect_run_error(case("m_short", xyz=xyz[:300].copy(), m=np.zeros((299, 3), np.float32)),
+                      '"M" has different size 897 vs 900')
+    # valid inputs get as far as selecting the device (none on a CPU-only machine)
+    if _lib.device_count() == 0:
+        _expect_run_error(case("valid", xyz=xyz[:300].copy(), m=np.zeros((300, 3), np.float32)),
+                          "device 0 is not available")

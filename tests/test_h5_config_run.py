@@ -269,3 +269,19 @@ def test_run_config_input_checks(tmp_path):
     if _lib.device_count() == 0:
         _expect_run_error(case("valid", xyz=xyz[:300].copy(), m=np.zeros((300, 3), np.float32)),
                           "device 0 is not available")
+
+
+def test_h5_refuses_chunked_layout(tmp_path):
+    """Chunked (and so compressed) datasets are outside the subset: refused with an error that
+    names the dataset (here a contiguous file whose layout message is patched to class 2)."""
+    import struct
+    f = tmp_path / "c.h5"
+    _lib.h5_write(f, {"mask": np.zeros((2, 2, 2), np.uint8)})
+    b = bytearray(f.read_bytes())
+    hdr = struct.pack("<HHB3x", 0x0008, 24, 0) + b"\x03\x01"
+    at = b.find(hdr)
+    assert at > 0
+    b[at + 9] = 2
+    f.write_bytes(bytes(b))
+    with pytest.raises(_lib.SpinWalkError, match="mask: only contiguous/compact layouts"):
+        _lib.h5_read(f, "mask")

@@ -54,6 +54,25 @@ def test_oracle_matches_reference_live(seed):
         assert bits_equal(a[k], b[k]), k
 
 
+@pytest.mark.skipif(not oracle_lib.ref_available(), reason="reference source tree not present")
+@pytest.mark.parametrize("seed,trials", [(7, 20), (8, 20), (2024, 60)])
+def test_oracle_matches_reference_on_random_configs(seed, trials):
+    """The randomised configurations of the GPU parity test (tests/fuzz_configs.py, same seeds):
+    several RF pulses and echoes, dephasing and gradient events, dummy scans with phase cycling,
+    two or three substrates, both boundaries, trajectories, seeds up to 2^31 (and 60 more of the
+    longer campaign's seed). The oracle's FP32
+    run equals the reference's own sim::sim built from its sources, bit for bit, so the oracle
+    the GPU is checked against is pinned on exactly these inputs."""
+    from tests import fuzz_configs
+    rng = np.random.default_rng(seed)
+    for trial in range(trials):
+        pr = fuzz_configs.random_case(rng)[0]
+        a = oracle_lib.run(pr, fill=np.nan)
+        b = oracle_lib.run_ref(pr, fill=np.nan)
+        for k in ("M1", "XYZ1", "T"):
+            assert bits_equal(a[k], b[k]), (trial, k)
+
+
 def test_oracle_spin_subset_is_independent():
     """Spins are independent: a subset run writes the same values at the same slots."""
     pr, _ = load_golden("permeable")

@@ -16,9 +16,11 @@ from spinwalk_gb300 import abi
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_PATH = os.path.join(ROOT, "oracle", "liboracle.so")
 REF_PATH = os.path.join(ROOT, "oracle", "_ref", "libref_sim.so")
+REF_NVCC_PATH = os.path.join(ROOT, "oracle", "_ref", "libref_sim_nvcc.so")
 
 _ora = None
 _ref = None
+_ref_nvcc = None
 
 
 def _p(a):
@@ -79,6 +81,26 @@ def run(problem, precision=abi.SW_PREC_FP32, fp64_shadow=False, spin_ids=None, n
     if M1d is not None:
         out["M1_fp64"] = M1d
     return out
+
+
+def ref_nvcc_available():
+    return os.path.exists(REF_NVCC_PATH)
+
+
+def run_ref_nvcc(problem, fill=0.0):
+    """The reference's own sim::sim as its nvcc host (--use_cpu) path builds it: the generator
+    flavour of its CUDA build (oracle/_ref/libref_sim_nvcc.so)."""
+    global _ref_nvcc
+    if _ref_nvcc is None:
+        L = C.CDLL(REF_NVCC_PATH)
+        L.ref_sim.argtypes = [C.POINTER(abi.SwParams), C.POINTER(abi.SwSequence)] + \
+            [C.c_void_p] * 7 + [C.c_void_p, C.c_uint32, C.c_int]
+        _ref_nvcc = L
+    M1, XYZ1, T, _ = problem.outputs(fill)
+    _ref_nvcc.ref_sim(C.byref(problem.params), C.byref(problem.seq.struct), _p(problem.field),
+                      _p(problem.mask), _p(problem.M0), _p(problem.XYZ0), _p(M1), _p(XYZ1), _p(T),
+                      None, 0, 0)
+    return dict(M1=M1, XYZ1=XYZ1, T=T)
 
 
 def run_ref(problem, spin_ids=None, n_threads=0, fill=0.0):

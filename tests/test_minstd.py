@@ -29,6 +29,22 @@ def test_oracle_minstd_matches_reference_fixture(case):
         assert bits_equal(o[k], ref[k]), k
 
 
+@pytest.mark.skipif(not oracle_lib.ref_nvcc_available(),
+                    reason="reference source tree not present (its nvcc host build)")
+@pytest.mark.parametrize("seed", [7, 8])
+def test_oracle_minstd_matches_reference_on_random_configs(seed):
+    """The randomised configurations of the GPU parity test (tests/fuzz_configs.py, same seeds)
+    in this flavour: the oracle equals the reference's nvcc host build bit for bit."""
+    from tests import fuzz_configs
+    rng = np.random.default_rng(seed)
+    for trial in range(20):
+        pr = fuzz_configs.random_case(rng)[0]
+        a = oracle_lib.run(pr, precision=MINSTD, fill=np.nan)
+        b = oracle_lib.run_ref_nvcc(pr, fill=np.nan)
+        for k in ("M1", "XYZ1", "T"):
+            assert bits_equal(a[k], b[k]), (trial, k)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", GOLDEN_CASES)
 def test_gpu_minstd_matches_reference_fixture(case):

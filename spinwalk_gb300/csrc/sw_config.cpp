@@ -376,8 +376,14 @@ int config_dump(const Config &c, const std::string &out) {
 
 }  // namespace sw
 
+namespace sw {
+namespace api {
+int fail(int code, const std::string &msg);   // sets sw_last_error() (sw_api.cu)
+}  // namespace api
+}  // namespace sw
+
 extern "C" int sw_config_dump(const char *ini_path, const char *out_path) {
-    if (!ini_path || !out_path) return SW_ERR_INVALID;
+    if (!ini_path || !out_path) return sw::api::fail(SW_ERR_INVALID, "sw_config_dump: null path");
     sw::Config c;
     std::string err;
     const int rc = sw::config_read(ini_path, c, err);
@@ -387,7 +393,8 @@ extern "C" int sw_config_dump(const char *ini_path, const char *out_path) {
             std::fprintf(f, "ok 0\n");
             std::fclose(f);
         }
-        return rc;
+        return sw::api::fail(rc, err);
     }
-    return sw::config_dump(c, out_path);
+    const int wrc = sw::config_dump(c, out_path);
+    return wrc ? sw::api::fail(wrc, std::string("cannot write ") + out_path) : SW_OK;
 }

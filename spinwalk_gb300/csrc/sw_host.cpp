@@ -9,6 +9,7 @@
 #include <cstring>
 #include <mutex>
 #include <random>
+#include <string>
 #include <vector>
 
 #include <omp.h>
@@ -107,6 +108,12 @@ void build_rf(const sw_params *, const sw_sequence *q, std::vector<RfOp> &out) {
 
 }  // namespace sw
 
+namespace sw {
+namespace api {
+int fail(int code, const std::string &msg);   // sets sw_last_error() (sw_api.cu)
+}  // namespace api
+}  // namespace sw
+
 extern "C" {
 
 float sw_fieldmap_scale(float B0, int32_t timestep_us) {
@@ -116,8 +123,10 @@ float sw_fieldmap_scale(float B0, int32_t timestep_us) {
 
 int sw_prepare_params(sw_params *p, double *diffusivity, const float *RF_FA_deg,
                       const float *T1_ms) {
-    if (!p || !RF_FA_deg || !T1_ms || !diffusivity) return SW_ERR_INVALID;
-    if (p->timestep_us <= 0) return SW_ERR_INVALID;
+    if (!p || !RF_FA_deg || !T1_ms || !diffusivity)
+        return sw::api::fail(SW_ERR_INVALID, "sw_prepare_params: null argument");
+    if (p->timestep_us <= 0)
+        return sw::api::fail(SW_ERR_INVALID, "sw_prepare_params: TIME_STEP must be positive");
     p->c = cosf(RF_FA_deg[0] * sw::kDeg2Rad);              // simulation_parameters.cuh:229-230
     p->s = sinf(RF_FA_deg[0] * sw::kDeg2Rad);
     p->n_timepoints = p->TR_us / p->timestep_us;           // :231
@@ -131,7 +140,7 @@ int sw_prepare_params(sw_params *p, double *diffusivity, const float *RF_FA_deg,
 
 // monte_carlo::initialize_position without a file (src/sim/monte_carlo.cu:141-151).
 int sw_initial_positions(const float fov[3], uint64_t seed, uint32_t n_spins, float *XYZ0) {
-    if (!fov || !XYZ0) return SW_ERR_INVALID;
+    if (!fov || !XYZ0) return sw::api::fail(SW_ERR_INVALID, "sw_initial_positions: null argument");
     std::mt19937 gen(seed);
     std::uniform_real_distribution<float> dx(0.01 * fov[0], 0.99 * fov[0]);
     std::uniform_real_distribution<float> dy(0.01 * fov[1], 0.99 * fov[1]);

@@ -16,6 +16,7 @@
 #include <cstdint>
 #include <cstring>
 #include <random>
+#include <string>
 #include <vector>
 
 #include <omp.h>
@@ -31,18 +32,26 @@ struct Cyl {
 
 }  // namespace
 
+namespace sw {
+namespace api {
+int fail(int code, const std::string &msg);   // sets sw_last_error() (sw_api.cu)
+}  // namespace api
+}  // namespace sw
+
 extern "C" {
 
 int sw_phantom_cylinders(const uint32_t dims[3], const double fov[3], double radius,
                          double volume_fraction, uint64_t seed, int random_orientation,
                          double dchi, double Y, const double B0_dir[3], uint8_t *mask,
                          float *field) {
-    if (!dims || !fov || !mask || radius <= 0 || volume_fraction < 0) return SW_ERR_INVALID;
+    if (!dims || !fov || !mask || radius <= 0 || volume_fraction < 0)
+        return sw::api::fail(SW_ERR_INVALID, "sw_phantom_cylinders: null buffer, radius <= 0 or "
+                                             "negative volume fraction");
     const uint64_t nx = dims[0], ny = dims[1], nz = dims[2];
     double b0[3] = {0, 0, 1};
     if (B0_dir) {
         double n = std::sqrt(B0_dir[0] * B0_dir[0] + B0_dir[1] * B0_dir[1] + B0_dir[2] * B0_dir[2]);
-        if (n <= 0) return SW_ERR_INVALID;
+        if (n <= 0) return sw::api::fail(SW_ERR_INVALID, "B0 direction has zero length");
         for (int i = 0; i < 3; i++) b0[i] = B0_dir[i] / n;
     }
     std::mt19937_64 rng(seed);
@@ -116,12 +125,14 @@ int sw_phantom_cylinders(const uint32_t dims[3], const double fov[3], double rad
 int sw_phantom_spheres(const uint32_t dims[3], const double fov[3], double rmin, double rmax,
                        double volume_fraction, uint64_t seed, double dchi, double Y,
                        const double B0_dir[3], double window, uint8_t *mask, float *field) {
-    if (!dims || !fov || !mask || rmin <= 0 || rmax < rmin || window < 1) return SW_ERR_INVALID;
+    if (!dims || !fov || !mask || rmin <= 0 || rmax < rmin || window < 1)
+        return sw::api::fail(SW_ERR_INVALID, "sw_phantom_spheres: null buffer, radii not "
+                                             "0 < rmin <= rmax, or window < 1");
     const int64_t nx = dims[0], ny = dims[1], nz = dims[2];
     double b0[3] = {0, 0, 1};
     if (B0_dir) {
         double n = std::sqrt(B0_dir[0] * B0_dir[0] + B0_dir[1] * B0_dir[1] + B0_dir[2] * B0_dir[2]);
-        if (n <= 0) return SW_ERR_INVALID;
+        if (n <= 0) return sw::api::fail(SW_ERR_INVALID, "B0 direction has zero length");
         for (int i = 0; i < 3; i++) b0[i] = B0_dir[i] / n;
     }
     std::mt19937_64 rng(seed);

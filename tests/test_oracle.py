@@ -176,3 +176,24 @@ def test_integer_double_add_matches_ieee_on_host(tmp_path):
     assert r.returncode == 0, r.stdout
     n, bad = map(int, r.stdout.split()[-2:])
     assert n > 8_000_000 and bad == 0
+
+
+def test_host_entry_points_report_errors():
+    """The host-only entry points return an error code and say why in sw_last_error()."""
+    L = _lib.lib()
+    p = abi.SwParams()
+    assert L.sw_prepare_params(C.byref(p), None, None, None) == abi.SW_ERR_INVALID
+    assert b"null argument" in L.sw_last_error()
+    d = (C.c_double * 2)(1e-9, 1e-9)
+    fa, t1 = (C.c_float * 1)(90.0), (C.c_float * 1)(1000.0)
+    p.timestep_us = 0
+    assert L.sw_prepare_params(C.byref(p), d, fa, t1) == abi.SW_ERR_INVALID
+    assert b"TIME_STEP" in L.sw_last_error()
+    assert L.sw_initial_positions(None, 1, 4, None) == abi.SW_ERR_INVALID
+    assert b"sw_initial_positions" in L.sw_last_error()
+    with pytest.raises(_lib.SpinWalkError, match="radius"):
+        _lib.phantom_cylinders(8, 8e-6, -1e-6, 0.1, seed=1)
+    with pytest.raises(_lib.SpinWalkError, match="zero length"):
+        _lib.phantom_spheres(8, 8e-6, 1e-6, 2e-6, 0.1, seed=1, B0_dir=(0.0, 0.0, 0.0))
+    assert _lib.config_dump("/nonexistent/x.ini", os.devnull) != 0
+    assert L.sw_last_error()

@@ -10,8 +10,10 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <filesystem>
 #include <limits>
+#include <new>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -50,7 +52,7 @@ sw::h5::Dataset make_ds(const std::vector<uint64_t> &dims, const std::vector<T> 
 
 }  // namespace
 
-extern "C" int sw_run_config(const char *ini_path, int device) {
+static int run_config_impl(const char *ini_path, int device) {
     using clock = std::chrono::steady_clock;
     const auto t_run = clock::now();
     if (!ini_path) return drv_fail(SW_ERR_INVALID, "no config file");
@@ -260,9 +262,9 @@ extern "C" int sw_run_config(const char *ini_path, int device) {
     return SW_OK;
 }
 
-extern "C" int sw_h5_write(const char *path, int n, const char *const *names, const int *types,
+static int h5_write_impl(const char *path, int n, const char *const *names, const int *types,
                            const int *ranks, const uint64_t *dims, const void *const *data) {
-    if (!path || n < 0) return SW_ERR_INVALID;
+    if (!path || n < 0) return drv_fail(SW_ERR_INVALID, "sw_h5_write: null path or negative count");
     std::vector<std::pair<std::string, sw::h5::Dataset>> sets;
     size_t dpos = 0;
     for (int i = 0; i < n; i++) {
@@ -286,7 +288,7 @@ extern "C" int sw_h5_write(const char *path, int n, const char *const *names, co
     return SW_OK;
 }
 
-extern "C" int sw_h5_read(const char *path, const char *name, int *type, int *rank,
+static int h5_read_impl(const char *path, const char *name, int *type, int *rank,
                           uint64_t dims[8], void *out, uint64_t out_bytes) {
     sw::h5::Dataset d;
     std::string err;
@@ -301,4 +303,31 @@ extern "C" int sw_h5_read(const char *path, const char *name, int *type, int *ra
         std::memcpy(out, d.data.data(), d.data.size());
     }
     return SW_OK;
+}
+
+// The C ABI never lets an exception out (an allocation that fails for a huge NUMBER_OF_SPINS,
+// for instance): it becomes an error code and a message.
+template <typename F>
+static int guarded(const char *what, F &&f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc &) {
+        return drv_fail(SW_ERR_NOMEM, std::string(what) + ": out of host memory");
+    } catch (const std::exception &e) {
+        return drv_fail(SW_ERR_IO, std::string(what) + ": " + e.what());
+    }
+}
+
+extern "C" int sw_run_config(const char *ini_path, int device) {
+    return guarded("sw_run_config", [&] { return run_config_impl(ini_path, device); });
+}
+
+extern "C" int sw_h5_write(const char *path, int n, const char *const *names, const int *types,
+                           const int *ranks, const uint64_t *dims, const void *const *data) {
+    return guarded("sw_h5_write", [&] { return h5_write_impl(path, n, names, types, ranks, dims, data); });
+}
+
+extern "C" int sw_h5_read(const char *path, const char *name, int *type, int *rank,
+                          uint64_t dims[8], void *out, uint64_t out_bytes) {
+    return guarded("sw_h5_read", [&] { return h5_read_impl(path, name, type, rank, dims, out, out_bytes); });
 }

@@ -7,11 +7,15 @@
 // scales, TE. libhdf5 with default settings stores such files with a version-0 superblock, an
 // "old-style" root group (symbol-table message -> version-1 B-tree of group nodes -> symbol table
 // nodes, names in a local heap), version-1 object headers and contiguous data. That subset is
-// what this file reads (plus continuation blocks and 64-bit floats) and writes.
+// what this file reads (plus continuation blocks and 64-bit floats) and writes. The reader also
+// takes chunked datasets (version-1 B-tree chunk index) with the deflate, shuffle and fletcher32
+// filters, as h5py's compression="gzip" and MATLAB's compressed files store them; unwritten
+// chunks read as zeros (the default fill value).
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <fstream>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -22,6 +26,8 @@ namespace h5 {
 namespace {
 
 constexpr uint64_t kUndef = ~uint64_t(0);
+// Largest dataset read (far above any phantom: 800^3 float32 is 2 GiB).
+constexpr uint64_t kMaxDatasetBytes = 1ull << 40;
 const unsigned char kSig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
 
 struct Buf {
@@ -38,6 +44,16 @@ struct Msg {
     uint16_t type;
     uint64_t off, size;
 };
+
+// Whether bytes [rel, rel + n) lie inside message m.
+bool fits(const Msg &m, uint64_t rel, uint64_t n) { return rel <= m.size && n <= m.size - rel; }
+
+// r = a * b; false on overflow
+bool mul_ok(uint64_t a, uint64_t b, uint64_t &r) {
+    if (a != 0 && b > ~uint64_t(0) / a) return false;
+    r = a * b;
+    return true;
+}
 
 // Messages of a version-1 object header, following continuation blocks.
 bool header_messages(const Buf &B, uint64_t addr, std::vector<Msg> &out, std::string &err) {
@@ -68,18 +84,20 @@ bool read_string(const Buf &B, uint64_t off, std::string &s) {
 
 // Walks a version-1 B-tree of group nodes and collects (name, object header address).
 bool group_entries(const Buf &B, uint64_t btree, uint64_t heap_data,
-                   std::vector<std::pair<std::string, uint64_t>> &out, std::string &err, int depth = 0) {
-    if (depth > 32 || !B.ok(btree, 24) || std::memcmp(&B.b[btree], "TREE", 4) != 0) {
+                   std::vector<std::pair<std::string, uint64_t>> &out, std::string &err,
+                   uint64_t &budget, int depth = 0) {
+    if (depth > 32 || budget == 0 || !B.ok(btree, 24) || std::memcmp(&B.b[btree], "TREE", 4) != 0) {
         err = "bad group B-tree";
         return false;
     }
+    budget--;
     const unsigned level = (unsigned)B.u(btree + 5, 1), used = (unsigned)B.u(btree + 6, 2);
     uint64_t p = btree + 24 + 8;                 // past the first key
     for (unsigned i = 0; i < used; i++, p += 16) {
         if (!B.ok(p, 8)) { err = "truncated B-tree"; return false; }
         const uint64_t child = B.u(p, 8);
         if (level > 0) {
-            if (!group_entries(B, child, heap_data, out, err, depth + 1)) return false;
+            if (!group_entries(B, child, heap_data, out, err, budget, depth + 1)) return false;
             continue;
         }
         if (!B.ok(child, 8) || std::memcmp(&B.b[child], "SNOD", 4) != 0) {
@@ -87,6 +105,8 @@ bool group_entries(const Buf &B, uint64_t btree, uint64_t heap_data,
             return false;
         }
         const unsigned ns = (unsigned)B.u(child + 6, 2);
+        if (budget < ns) { err = "bad group B-tree"; return false; }
+        budget -= ns;
         for (unsigned k = 0; k < ns; k++) {
             const uint64_t e = child + 8 + 40ull * k;
             if (!B.ok(e, 40)) { err = "truncated symbol table node"; return false; }
@@ -116,10 +136,385 @@ bool root_entries(const Buf &B, std::vector<std::pair<std::string, uint64_t>> &o
             err = "bad local heap";
             return false;
         }
-        return group_entries(B, btree, B.u(heap + 24, 8), out, err);
+        uint64_t budget = B.b.size() / 24 + 1;            // nodes and entries a valid tree can hold
+        return group_entries(B, btree, B.u(heap + 24, 8), out, err, budget);
     }
     err = "root group has no symbol table (new-style groups are not supported)";
     return false;
+}
+
+// ---- chunked storage: the version-1 B-tree chunk index, filters and a deflate decoder ---------
+
+// Bits of a deflate stream, least significant bit first (RFC 1951 section 3.1.1).
+struct BitReader {
+    const uint8_t *p;
+    size_t n, pos = 0;
+    uint64_t buf = 0;
+    int cnt = 0;
+    bool get(int k, uint32_t &v) {                     // k <= 24
+        while (cnt < k) {
+            if (pos >= n) return false;
+            buf |= (uint64_t)p[pos++] << cnt;
+            cnt += 8;
+        }
+        v = (uint32_t)(buf & ((1ull << k) - 1));
+        buf >>= k;
+        cnt -= k;
+        return true;
+    }
+    void to_byte() {                                   // drop the bits of a partial byte
+        buf >>= (cnt & 7);
+        cnt -= cnt & 7;
+    }
+};
+
+// A canonical Huffman code: the number of codes of each length and the symbols in code order.
+struct Huffman {
+    uint16_t count[16];
+    uint16_t symbol[320];
+};
+
+// Returns false for an over-subscribed set of lengths; an incomplete set is accepted (its
+// unused codes fail to decode).
+bool huffman_build(Huffman &h, const uint8_t *len, int n) {
+    std::memset(h.count, 0, sizeof h.count);
+    for (int s = 0; s < n; s++) h.count[len[s]]++;
+    int left = 1;
+    for (int l = 1; l < 16; l++) {
+        left = 2 * left - h.count[l];
+        if (left < 0) return false;
+    }
+    uint16_t next[16];
+    next[1] = 0;
+    for (int l = 1; l < 15; l++) next[l + 1] = (uint16_t)(next[l] + h.count[l]);
+    for (int s = 0; s < n; s++)
+        if (len[s]) h.symbol[next[len[s]]++] = (uint16_t)s;
+    return true;
+}
+
+// One symbol: codes are read most significant bit first; -1 when the stream ends or the code
+// is not in the set.
+int huffman_decode(BitReader &br, const Huffman &h) {
+    int code = 0, first = 0, index = 0;
+    for (int l = 1; l < 16; l++) {
+        uint32_t bit;
+        if (!br.get(1, bit)) return -1;
+        code |= (int)bit;
+        const int count = h.count[l];
+        if (code - first < count) return h.symbol[index + code - first];
+        index += count;
+        first = (first + count) << 1;
+        code <<= 1;
+    }
+    return -1;
+}
+
+// Literal/length and distance symbols of one compressed block (RFC 1951 section 3.2.5).
+bool inflate_codes(BitReader &br, const Huffman &lit, const Huffman &dist, size_t limit,
+                   std::vector<uint8_t> &out) {
+    static const uint16_t kLenBase[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
+                                          31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+    static const uint8_t kLenExtra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
+                                          2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+    static const uint16_t kDistBase[30] = {1,    2,    3,    4,    5,    7,     9,     13,    17,  25,
+                                           33,   49,   65,   97,   129,  193,   257,   385,   513, 769,
+                                           1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
+    static const uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2,  3,  3,  4,  4,  5,  5,  6,
+                                           6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+    for (;;) {
+        int sym = huffman_decode(br, lit);
+        if (sym < 0) return false;
+        if (sym < 256) {
+            if (out.size() >= limit) return false;
+            out.push_back((uint8_t)sym);
+            continue;
+        }
+        if (sym == 256) return true;
+        sym -= 257;
+        if (sym >= 29) return false;
+        uint32_t e;
+        if (!br.get(kLenExtra[sym], e)) return false;
+        const size_t len = kLenBase[sym] + e;
+        const int d = huffman_decode(br, dist);
+        if (d < 0 || d >= 30 || !br.get(kDistExtra[d], e)) return false;
+        const size_t back = kDistBase[d] + e;
+        if (back > out.size() || out.size() + len > limit) return false;
+        for (size_t i = 0; i < len; i++) {
+            const uint8_t c = out[out.size() - back];
+            out.push_back(c);
+        }
+    }
+}
+
+uint32_t adler32(const std::vector<uint8_t> &v) {
+    uint32_t a = 1, b = 0;
+    for (uint8_t c : v) {
+        a = (a + c) % 65521u;
+        b = (b + a) % 65521u;
+    }
+    return (b << 16) | a;
+}
+
+// A zlib stream (RFC 1950: header, deflate blocks, Adler-32 of the output), as HDF5's deflate
+// filter writes it; at most `limit` output bytes.
+bool zlib_inflate(const uint8_t *p, size_t n, size_t limit, std::vector<uint8_t> &out,
+                  std::string &err) {
+    out.clear();
+    if (n < 6 || (p[0] & 15) != 8 || (p[0] >> 4) > 7 || ((p[0] << 8) | p[1]) % 31 != 0 ||
+        (p[1] & 0x20)) {
+        err = "deflate filter: not a zlib stream";
+        return false;
+    }
+    BitReader br{p + 2, n - 2};
+    uint32_t last = 0, type = 0;
+    do {
+        if (!br.get(1, last) || !br.get(2, type)) break;
+        if (type == 0) {                                   // stored
+            br.to_byte();
+            uint32_t len, nlen;
+            if (!br.get(16, len) || !br.get(16, nlen) || len != (~nlen & 0xffffu)) break;
+            if (out.size() + len > limit) break;
+            uint32_t c = 0;
+            for (uint32_t i = 0; i < len && br.get(8, c); i++) out.push_back((uint8_t)c);
+        } else if (type == 1) {                            // fixed codes
+            static Huffman fl, fd;
+            static const bool built = [] {
+                uint8_t l[288];
+                for (int i = 0; i < 288; i++) l[i] = i < 144 ? 8 : i < 256 ? 9 : i < 280 ? 7 : 8;
+                huffman_build(fl, l, 288);
+                for (int i = 0; i < 30; i++) l[i] = 5;
+                huffman_build(fd, l, 30);
+                return true;
+            }();
+            (void)built;
+            if (!inflate_codes(br, fl, fd, limit, out)) break;
+        } else if (type == 2) {                            // dynamic codes
+            uint32_t hlit, hdist, hclen;
+            if (!br.get(5, hlit) || !br.get(5, hdist) || !br.get(4, hclen)) break;
+            hlit += 257;
+            hdist += 1;
+            hclen += 4;
+            if (hlit > 286 || hdist > 30) break;
+            static const uint8_t kOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5,
+                                               11, 4, 12, 3, 13, 2, 14, 1, 15};
+            uint8_t lens[320] = {0};
+            bool ok = true;
+            for (uint32_t i = 0; i < hclen && ok; i++) {
+                uint32_t v = 0;
+                ok = br.get(3, v);
+                lens[kOrder[i]] = (uint8_t)v;
+            }
+            Huffman lc;
+            if (!ok || !huffman_build(lc, lens, 19)) break;
+            std::memset(lens, 0, sizeof lens);
+            uint32_t idx = 0;
+            while (ok && idx < hlit + hdist) {
+                const int sym = huffman_decode(br, lc);
+                uint32_t rep = 0, v = 0;
+                uint8_t val = 0;
+                if (sym < 0) { ok = false; break; }
+                if (sym < 16) { lens[idx++] = (uint8_t)sym; continue; }
+                if (sym == 16) {
+                    if (idx == 0 || !br.get(2, v)) { ok = false; break; }
+                    val = lens[idx - 1];
+                    rep = 3 + v;
+                } else if (sym == 17) {
+                    if (!br.get(3, v)) { ok = false; break; }
+                    rep = 3 + v;
+                } else {
+                    if (!br.get(7, v)) { ok = false; break; }
+                    rep = 11 + v;
+                }
+                if (idx + rep > hlit + hdist) { ok = false; break; }
+                while (rep--) lens[idx++] = val;
+            }
+            Huffman lit, dist;
+            if (!ok || lens[256] == 0 || !huffman_build(lit, lens, (int)hlit) ||
+                !huffman_build(dist, lens + hlit, (int)hdist) ||
+                !inflate_codes(br, lit, dist, limit, out))
+                break;
+        } else {
+            break;
+        }
+        if (last) {
+            br.to_byte();
+            uint32_t a[4];
+            for (int i = 0; i < 4; i++)
+                if (!br.get(8, a[i])) { err = "deflate filter: truncated stream"; return false; }
+            const uint32_t want = (a[0] << 24) | (a[1] << 16) | (a[2] << 8) | a[3];
+            if (want != adler32(out)) { err = "deflate filter: Adler-32 mismatch"; return false; }
+            return true;
+        }
+    } while (true);
+    err = "deflate filter: corrupt or oversized stream";
+    return false;
+}
+
+struct Filter {
+    uint16_t id;
+    std::vector<uint32_t> cd;       // client data
+};
+
+// The filter pipeline message (0x000B), versions 1 and 2.
+bool filter_pipeline(const Buf &B, const Msg &m, std::vector<Filter> &out, std::string &err) {
+    const unsigned ver = (unsigned)B.u(m.off, 1), nf = (unsigned)B.u(m.off + 1, 1);
+    uint64_t p = m.off + (ver == 1 ? 8 : 2);
+    const uint64_t end = m.off + m.size;
+    if (ver != 1 && ver != 2) { err = "unsupported filter pipeline version"; return false; }
+    for (unsigned i = 0; i < nf; i++) {
+        if (p + 8 > end) { err = "truncated filter pipeline"; return false; }
+        Filter f;
+        f.id = (uint16_t)B.u(p, 2);
+        p += 2;
+        uint64_t name_len = 0;
+        if (ver == 1 || f.id >= 256) {
+            name_len = B.u(p, 2);
+            p += 2;
+        }
+        p += 2;                                            // flags
+        const unsigned ncd = (unsigned)B.u(p, 2);
+        p += 2;
+        if (ver == 1) name_len = (name_len + 7) & ~uint64_t(7);
+        p += name_len;
+        for (unsigned k = 0; k < ncd; k++, p += 4) {
+            if (p + 4 > end) { err = "truncated filter pipeline"; return false; }
+            f.cd.push_back((uint32_t)B.u(p, 4));
+        }
+        if (ver == 1 && (ncd & 1)) p += 4;
+        out.push_back(f);
+    }
+    return true;
+}
+
+// One chunk through the pipeline in reverse (the filters a chunk's mask marks as skipped are
+// not applied to it): deflate (1), shuffle (2), fletcher32 (3).
+bool unfilter(const std::vector<Filter> &fs, uint32_t mask, std::vector<uint8_t> &data,
+              size_t expect, std::string &err) {
+    for (size_t i = fs.size(); i-- > 0;) {
+        if ((mask >> i) & 1u) continue;
+        const Filter &f = fs[i];
+        if (f.id == 1) {
+            std::vector<uint8_t> out;
+            if (!zlib_inflate(data.data(), data.size(), expect, out, err)) return false;
+            data.swap(out);
+        } else if (f.id == 2) {
+            const size_t es = f.cd.empty() ? 1 : f.cd[0];
+            if (es > 1) {
+                const size_t n = data.size() / es;
+                std::vector<uint8_t> out(data.size());
+                for (size_t b = 0; b < es; b++)
+                    for (size_t k = 0; k < n; k++) out[k * es + b] = data[b * n + k];
+                std::copy(data.begin() + n * es, data.end(), out.begin() + n * es);
+                data.swap(out);
+            }
+        } else if (f.id == 3) {
+            if (data.size() < 4) { err = "fletcher32 filter: chunk shorter than its checksum"; return false; }
+            data.resize(data.size() - 4);
+        } else {
+            err = "unsupported HDF5 filter " + std::to_string(f.id) +
+                  " (deflate, shuffle and fletcher32 are supported)";
+            return false;
+        }
+    }
+    return true;
+}
+
+struct ChunkRef {
+    uint64_t addr, size;
+    uint32_t mask;
+    std::vector<uint64_t> off;
+};
+
+// Walks the version-1 B-tree of raw data chunks (node type 1); `nd` is the dataset rank + 1.
+// `budget` bounds the nodes visited and chunks listed (a damaged tree may point back at itself).
+bool chunk_index(const Buf &B, uint64_t node, unsigned nd, std::vector<ChunkRef> &out,
+                 std::string &err, uint64_t &budget, int depth = 0) {
+    if (depth > 32 || budget == 0 || !B.ok(node, 24) || std::memcmp(&B.b[node], "TREE", 4) != 0 ||
+        B.u(node + 4, 1) != 1) {
+        err = "bad chunk B-tree";
+        return false;
+    }
+    budget--;
+    const unsigned level = (unsigned)B.u(node + 5, 1), used = (unsigned)B.u(node + 6, 2);
+    const uint64_t key = 8 + 8ull * nd;
+    uint64_t p = node + 24;
+    for (unsigned i = 0; i < used; i++, p += key + 8) {
+        if (!B.ok(p, key + 8)) { err = "truncated chunk B-tree"; return false; }
+        const uint64_t child = B.u(p + key, 8);
+        if (level > 0) {
+            if (!chunk_index(B, child, nd, out, err, budget, depth + 1)) return false;
+            continue;
+        }
+        if (budget == 0) { err = "bad chunk B-tree"; return false; }
+        budget--;
+        ChunkRef c{child, B.u(p, 4), (uint32_t)B.u(p + 4, 4), {}};
+        for (unsigned k = 0; k < nd; k++) c.off.push_back(B.u(p + 8 + 8ull * k, 8));
+        out.push_back(std::move(c));
+    }
+    return true;
+}
+
+// The whole dataset from its chunks; chunks that were never written read as zeros.
+bool read_chunked(const Buf &B, const std::vector<uint64_t> &dims, uint64_t esz, uint64_t btree,
+                  const std::vector<uint64_t> &cdim, const std::vector<Filter> &filters,
+                  std::vector<char> &data, std::string &err) {
+    const size_t rank = dims.size();
+    if (rank == 0 || cdim.size() != rank + 1 || cdim[rank] != esz) {
+        err = "chunk dimensions do not match the dataset";
+        return false;
+    }
+    uint64_t count = 1, celems = 1, grid = 1;
+    for (size_t k = 0; k < rank; k++) {
+        if (cdim[k] == 0) { err = "zero chunk dimension"; return false; }
+        count *= dims[k];                                  // the caller checked the total
+        if (!mul_ok(celems, cdim[k], celems) || !mul_ok(grid, (dims[k] + cdim[k] - 1) / cdim[k], grid)) {
+            err = "bad chunk dimensions";
+            return false;
+        }
+    }
+    if (celems > kMaxDatasetBytes / esz) { err = "bad chunk dimensions"; return false; }
+    data.assign(count * esz, 0);
+    if (btree == kUndef) return true;
+    std::vector<ChunkRef> chunks;
+    uint64_t budget = grid + B.b.size() / 24 + 1;          // chunks + nodes a valid tree can hold
+    if (!chunk_index(B, btree, (unsigned)rank + 1, chunks, err, budget)) return false;
+    const size_t cbytes = celems * esz;
+    std::vector<uint8_t> buf;
+    for (const ChunkRef &c : chunks) {
+        if (c.off[rank] != 0) { err = "bad chunk offset"; return false; }
+        for (size_t k = 0; k < rank; k++)
+            if (c.off[k] % cdim[k] != 0 || c.off[k] >= dims[k]) { err = "bad chunk offset"; return false; }
+        if (!B.ok(c.addr, c.size)) { err = "chunk outside the file"; return false; }
+        buf.assign((const uint8_t *)B.b.data() + c.addr, (const uint8_t *)B.b.data() + c.addr + c.size);
+        if (!unfilter(filters, c.mask, buf, cbytes, err)) return false;
+        if (buf.size() != cbytes) {
+            err = "chunk decodes to " + std::to_string(buf.size()) + " bytes, expected " +
+                  std::to_string(cbytes);
+            return false;
+        }
+        // copy the rows along the last dimension that lie inside the dataset
+        const uint64_t run = std::min(cdim[rank - 1], dims[rank - 1] - c.off[rank - 1]);
+        std::vector<uint64_t> loc(rank, 0);
+        for (;;) {
+            bool inside = true;
+            uint64_t g = 0, l = 0;
+            for (size_t k = 0; k < rank; k++) {
+                const uint64_t x = c.off[k] + loc[k];
+                if (x >= dims[k]) inside = false;
+                g = g * dims[k] + x;
+                l = l * cdim[k] + loc[k];
+            }
+            if (inside) std::memcpy(data.data() + g * esz, buf.data() + l * esz, run * esz);
+            size_t k = rank - 1;                           // next row: odometer over dims 0..rank-2
+            while (k > 0) {
+                if (++loc[k - 1] < cdim[k - 1]) break;
+                loc[k - 1] = 0;
+                k--;
+            }
+            if (k == 0) break;
+        }
+    }
+    return true;
 }
 
 // Loads the file and drops a user block: the superblock may start at 0, 512, 1024, ...; file
@@ -140,7 +535,9 @@ bool load(const std::string &file, std::vector<char> &b, std::string &err) {
 
 }  // namespace
 
-bool read(const std::string &file, const std::string &name, Dataset &out, std::string &err) {
+namespace {
+
+bool read_impl(const std::string &file, const std::string &name, Dataset &out, std::string &err) {
     std::vector<char> bytes;
     if (!load(file, bytes, err)) return false;
     Buf B{bytes};
@@ -155,46 +552,92 @@ bool read(const std::string &file, const std::string &name, Dataset &out, std::s
     out = Dataset{};
     int dtype_class = -1;
     uint64_t dtype_size = 0, data_addr = kUndef, data_size = 0;
-    bool little = true, is_signed = false;
+    bool little = true, is_signed = false, chunked = false;
+    std::vector<uint64_t> cdim;
+    std::vector<Filter> filters;
+    for (const Msg &m : msgs) {
+        if (m.type == 0x000B && !filter_pipeline(B, m, filters, err)) return false;
+    }
     for (const Msg &m : msgs) {
         if (m.type == 0x0001) {                                    // dataspace
+            if (!fits(m, 0, 2)) { err = "dataset " + name + ": bad dataspace"; return false; }
             const unsigned ver = (unsigned)B.u(m.off, 1), rank = (unsigned)B.u(m.off + 1, 1);
-            const uint64_t p = m.off + (ver == 1 ? 8 : 4);
-            for (unsigned i = 0; i < rank; i++) out.dims.push_back(B.u(p + 8ull * i, 8));
+            const uint64_t rel = ver == 1 ? 8 : 4;
+            if (rank > 32 || !fits(m, rel, 8ull * rank)) {
+                err = "dataset " + name + ": bad dataspace";
+                return false;
+            }
+            for (unsigned i = 0; i < rank; i++) out.dims.push_back(B.u(m.off + rel + 8ull * i, 8));
         } else if (m.type == 0x0003) {                             // datatype
+            if (!fits(m, 0, 8)) { err = "dataset " + name + ": bad datatype"; return false; }
             dtype_class = (int)(B.u(m.off, 1) & 0x0f);
             const unsigned bits0 = (unsigned)B.u(m.off + 1, 1);
             little = (bits0 & 1u) == 0;
             is_signed = dtype_class == 0 && (bits0 & 8u);
             dtype_size = B.u(m.off + 4, 4);
         } else if (m.type == 0x0008) {                             // data layout
+            const std::string bad = "dataset " + name + ": bad layout message";
+            if (!fits(m, 0, 3)) { err = bad; return false; }
             const unsigned ver = (unsigned)B.u(m.off, 1);
             if (ver == 3 && B.u(m.off + 1, 1) == 1) {
+                if (!fits(m, 2, 16)) { err = bad; return false; }
                 data_addr = B.u(m.off + 2, 8);
                 data_size = B.u(m.off + 10, 8);
             } else if (ver == 3 && B.u(m.off + 1, 1) == 0) {      // compact
+                if (!fits(m, 2, 2)) { err = bad; return false; }
                 data_size = B.u(m.off + 2, 2);
                 data_addr = m.off + 4;
+                if (!fits(m, 4, data_size)) { err = bad; return false; }
+            } else if (ver == 3 && B.u(m.off + 1, 1) == 2) {      // chunked: B-tree, chunk dims
+                const unsigned nd = (unsigned)B.u(m.off + 2, 1);
+                if (nd > 33 || !fits(m, 3, 8 + 4ull * nd)) { err = bad; return false; }
+                data_addr = B.u(m.off + 3, 8);
+                for (unsigned i = 0; i < nd; i++) cdim.push_back(B.u(m.off + 11 + 4ull * i, 4));
+                chunked = true;
+            } else if ((ver == 1 || ver == 2) && B.u(m.off + 2, 1) == 2) {
+                const unsigned nd = (unsigned)B.u(m.off + 1, 1);
+                if (nd > 33 || !fits(m, 8, 8 + 4ull * nd)) { err = bad; return false; }
+                data_addr = B.u(m.off + 8, 8);
+                for (unsigned i = 0; i < nd; i++) cdim.push_back(B.u(m.off + 16 + 4ull * i, 4));
+                chunked = true;
             } else if ((ver == 1 || ver == 2) && B.u(m.off + 2, 1) == 1) {
                 // version 1/2: rank+1 4-byte dimensions (last = element size) after the address
                 const unsigned r = (unsigned)B.u(m.off + 1, 1);
+                if (r > 33 || !fits(m, 8, 8 + 4ull * r)) { err = bad; return false; }
                 data_addr = B.u(m.off + 8, 8);
                 data_size = 1;
-                for (unsigned i = 0; i < r; i++) data_size *= B.u(m.off + 16 + 4ull * i, 4);
+                for (unsigned i = 0; i < r; i++)
+                    if (!mul_ok(data_size, B.u(m.off + 16 + 4ull * i, 4), data_size)) {
+                        err = bad;
+                        return false;
+                    }
             } else if ((ver == 1 || ver == 2) && B.u(m.off + 2, 1) == 0) {
                 const unsigned r = (unsigned)B.u(m.off + 1, 1);
-                const uint64_t p = m.off + 8 + 4ull * r;
-                data_size = B.u(p, 4);
-                data_addr = p + 4;
+                const uint64_t rel = 8 + 4ull * r;
+                if (r > 33 || !fits(m, rel, 4)) { err = bad; return false; }
+                data_size = B.u(m.off + rel, 4);
+                data_addr = m.off + rel + 4;
+                if (!fits(m, rel + 4, data_size)) { err = bad; return false; }
             } else {
-                err = "dataset " + name + ": only contiguous/compact layouts are supported";
+                err = "dataset " + name + ": unsupported storage layout";
                 return false;
             }
         }
     }
     if (!little) { err = "big-endian data are not supported"; return false; }
-    uint64_t count = 1;
-    for (uint64_t d : out.dims) count *= d;
+    uint64_t count = 1, nbytes = 0;
+    for (uint64_t d : out.dims)
+        if (!mul_ok(count, d, count)) { err = "dataset " + name + ": bad dimensions"; return false; }
+    // a file cannot hold more than deflate's ~1032:1 expansion of its own size (unwritten
+    // datasets and chunks aside, which get 1 GiB): a damaged size field fails here instead of
+    // allocating
+    const uint64_t limit = std::min<uint64_t>(kMaxDatasetBytes,
+                                              std::max<uint64_t>(1ull << 30, 1100ull * bytes.size()));
+    if (!mul_ok(count, dtype_size, nbytes) || nbytes > limit) {
+        err = "dataset " + name + ": size " + std::to_string(nbytes) +
+              " bytes is impossible for a file of " + std::to_string(bytes.size()) + " bytes";
+        return false;
+    }
     if (dtype_class == 0 && dtype_size == 1) out.type = is_signed ? kI8 : kU8;
     else if (dtype_class == 0 && dtype_size == 2) out.type = is_signed ? kI16 : kU16;
     else if (dtype_class == 0 && dtype_size == 4) out.type = is_signed ? kI32 : kU32;
@@ -202,6 +645,14 @@ bool read(const std::string &file, const std::string &name, Dataset &out, std::s
     else if (dtype_class == 1 && dtype_size == 4) out.type = kF32;
     else if (dtype_class == 1 && dtype_size == 8) out.type = kF64;
     else { err = "dataset " + name + ": unsupported datatype"; return false; }
+    if (chunked) {
+        if (!read_chunked(B, out.dims, dtype_size, data_addr, cdim, filters, out.data, err)) {
+            err = "dataset " + name + ": " + err;
+            return false;
+        }
+        return true;
+    }
+    if (!filters.empty()) { err = "dataset " + name + ": filters on a contiguous dataset"; return false; }
     if (data_addr == kUndef) {                                     // never written: zeros
         out.data.assign(count * dtype_size, 0);
         return true;
@@ -212,6 +663,20 @@ bool read(const std::string &file, const std::string &name, Dataset &out, std::s
     }
     out.data.assign(bytes.begin() + data_addr, bytes.begin() + data_addr + count * dtype_size);
     return true;
+}
+
+}  // namespace
+
+// Any allocation failure (a damaged file can claim a huge dataset) becomes an error, never an
+// exception across the C ABI.
+bool read(const std::string &file, const std::string &name, Dataset &out, std::string &err) {
+    try {
+        return read_impl(file, name, out, err);
+    } catch (const std::exception &e) {
+        out = Dataset{};
+        err = "dataset " + name + " in " + file + ": " + e.what();
+        return false;
+    }
 }
 
 bool list(const std::string &file, std::vector<std::string> &names, std::string &err) {

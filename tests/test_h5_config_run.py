@@ -271,17 +271,145 @@ def test_run_config_input_checks(tmp_path):
                           "device 0 is not available")
 
 
-def test_h5_refuses_chunked_layout(tmp_path):
-    """Chunked (and so compressed) datasets are outside the subset: refused with an error that
-    names the dataset (here a contiguous file whose layout message is patched to class 2)."""
-    import struct
+@pytest.mark.parametrize("dtype", [np.uint8, np.int8, np.int16, np.float32, np.float64])
+@pytest.mark.parametrize("filters,level,version", [
+    (("shuffle", "deflate"), 6, 1), (("deflate",), 9, 2), (("deflate",), 1, 1),
+    (("deflate",), 0, 2), (("shuffle",), 6, 1), ((), 6, 1), (("shuffle", "deflate", "fletcher32"), 4, 2)])
+def test_h5_chunked_datasets(tmp_path, dtype, filters, level, version):
+    """Chunked datasets (h5py's compression="gzip", MATLAB's compressed files): partial edge
+    chunks, deflate streams from zlib at several levels (stored, fixed and dynamic Huffman
+    blocks), shuffle and fletcher32, filter pipeline messages of versions 1 and 2."""
+    from tests.h5_chunked import write_chunked
+    rng = np.random.default_rng(int(level) + len(filters))
+    shape = (13, 17, 9)
+    if np.dtype(dtype).kind == "f":
+        a = rng.normal(size=shape).astype(dtype)
+        a[:4] = np.round(a[:4])                    # some compressible rows
+    else:
+        info = np.iinfo(dtype)
+        a = rng.integers(info.min, info.max, shape, dtype=dtype, endpoint=True)
+        a[5:] //= 16                               # long runs of small values
     f = tmp_path / "c.h5"
-    _lib.h5_write(f, {"mask": np.zeros((2, 2, 2), np.uint8)})
+    write_chunked(f, "fieldmap", a, (4, 5, 3), filters=filters, level=level,
+                  pipeline_version=version)
+    got = _lib.h5_read(f, "fieldmap")
+    assert got.dtype == a.dtype and got.shape == a.shape
+    assert bits_equal(got, a)
+
+
+def test_h5_chunked_index_shapes(tmp_path):
+    """Two-level chunk B-trees, unwritten chunks (zeros), chunks stored with every filter
+    skipped, ranks 1 and 4, a compressible phantom-like mask."""
+    from tests.h5_chunked import write_chunked
+    rng = np.random.default_rng(5)
+    mask = (rng.random((40, 40, 40)) < 0.05).astype(np.uint8)
+    write_chunked(tmp_path / "m.h5", "mask", mask, (8, 8, 8), leaf_entries=7)
+    assert bits_equal(_lib.h5_read(tmp_path / "m.h5", "mask"), mask)
+    a = rng.normal(size=(6, 7, 8)).astype(np.float32)
+    write_chunked(tmp_path / "s.h5", "x", a, (2, 4, 8), skip_chunks={(0, 1, 0), (2, 0, 0)},
+                  raw_chunks={(1, 1, 0)}, leaf_entries=2)
+    want = a.copy()
+    want[0:2, 4:7, :] = 0
+    want[4:6, 0:4, :] = 0
+    assert bits_equal(_lib.h5_read(tmp_path / "s.h5", "x"), want)
+    v = rng.normal(size=(1000,))
+    write_chunked(tmp_path / "v.h5", "v", v, (64,))
+    assert bits_equal(_lib.h5_read(tmp_path / "v.h5", "v"), v)
+    w = rng.integers(0, 100, (3, 4, 5, 6), dtype=np.int32)
+    write_chunked(tmp_path / "w.h5", "w", w, (2, 3, 2, 4), leaf_entries=5)
+    assert bits_equal(_lib.h5_read(tmp_path / "w.h5", "w"), w)
+    z = np.zeros((5, 5, 5), np.float32)
+    write_chunked(tmp_path / "z.h5", "z", np.ones((5, 5, 5), np.float32), (5, 5, 5),
+                  skip_chunks={(0, 0, 0)})
+    assert bits_equal(_lib.h5_read(tmp_path / "z.h5", "z"), z)
+
+
+def test_h5_chunked_errors(tmp_path):
+    """A corrupted deflate stream and an unsupported filter are errors naming the dataset,
+    never data."""
+    import struct
+    from tests.h5_chunked import write_chunked
+    a = np.arange(4000, dtype=np.float32).reshape(10, 20, 20)
+    f = tmp_path / "c.h5"
+    write_chunked(f, "fieldmap", a, (5, 20, 20), filters=("deflate",))
     b = bytearray(f.read_bytes())
-    hdr = struct.pack("<HHB3x", 0x0008, 24, 0) + b"\x03\x01"
-    at = b.find(hdr)
+    at = b.find(bytes([0x78, 0x9C]))               # first zlib stream (level 6 header)
     assert at > 0
-    b[at + 9] = 2
+    b[at + 40] ^= 0xFF
     f.write_bytes(bytes(b))
-    with pytest.raises(_lib.SpinWalkError, match="mask: only contiguous/compact layouts"):
-        _lib.h5_read(f, "mask")
+    with pytest.raises(_lib.SpinWalkError, match="fieldmap: .*deflate"):
+        _lib.h5_read(f, "fieldmap")
+    write_chunked(f, "fieldmap", a, (5, 20, 20), filters=("deflate",))
+    b = bytearray(f.read_bytes())
+    at = b.find(b"deflate\0")                     # the filter's name in a version-1 pipeline
+    assert at > 8 and struct.unpack_from("<H", b, at - 8)[0] == 1
+    struct.pack_into("<H", b, at - 8, 32000)       # its id -> LZF
+    f.write_bytes(bytes(b))
+    with pytest.raises(_lib.SpinWalkError, match="fieldmap: unsupported HDF5 filter 32000"):
+        _lib.h5_read(f, "fieldmap")
+
+
+def test_h5_deflate_streams_of_every_zlib_strategy(tmp_path):
+    """The deflate decoder on streams of every zlib strategy (default, filtered, Huffman only,
+    run-length, fixed codes), levels 0-9 and windows 2^9-2^15, over random, sparse, run-length,
+    periodic and smooth data in chunks of 1 byte up to the whole array."""
+    import zlib
+    from tests.h5_chunked import write_chunked
+    rng = np.random.default_rng(11)
+    strategies = [zlib.Z_DEFAULT_STRATEGY, zlib.Z_FILTERED, zlib.Z_HUFFMAN_ONLY, zlib.Z_RLE,
+                  zlib.Z_FIXED]
+    for trial in range(80):
+        size = int(rng.integers(1, 40000))
+        kind = trial % 5
+        if kind == 0:
+            a = rng.integers(0, 256, size, dtype=np.uint8)
+        elif kind == 1:
+            a = (rng.random(size) < 0.02).astype(np.uint8)
+        elif kind == 2:
+            a = np.repeat(rng.integers(0, 4, size // 37 + 1, dtype=np.uint8), 37)[:size]
+        elif kind == 3:
+            a = (np.arange(size) % int(rng.integers(1, 300))).astype(np.uint8)
+        else:
+            s = np.sin(np.arange(size // 4 + 1) * 1e-3).astype(np.float32)
+            a = np.frombuffer(s.tobytes(), np.uint8)[:size].copy()
+        f = tmp_path / "x.h5"
+        write_chunked(f, "x", a, (int(rng.integers(1, size + 1)),), filters=("deflate",),
+                      level=int(rng.integers(0, 10)), strategy=strategies[trial % 5],
+                      wbits=int(rng.integers(9, 16)), leaf_entries=16)
+        assert bits_equal(_lib.h5_read(f, "x"), a), trial
+
+
+def test_h5_damaged_files_are_errors(tmp_path):
+    """Damaged phantom files (random bytes, bit flips, truncations, huge 8-byte size fields) in
+    contiguous and chunked layouts either read or fail with an error: no crash, no huge
+    allocation (a size the file cannot hold is refused)."""
+    from tests.h5_chunked import write_chunked
+    rng = np.random.default_rng(17)
+    _lib.h5_write(tmp_path / "a.h5", {"x": rng.normal(size=(7, 8, 9)).astype(np.float32),
+                                      "mask": np.zeros((4, 4, 4), np.uint8)})
+    write_chunked(tmp_path / "b.h5", "x", rng.normal(size=(20, 20, 20)), (5, 7, 20),
+                  filters=("shuffle", "deflate", "fletcher32"), leaf_entries=3)
+    outcomes = {"read": 0, "error": 0}
+    for src in ("a.h5", "b.h5"):
+        raw = (tmp_path / src).read_bytes()
+        for k in range(150):
+            c = bytearray(raw)
+            mode = k % 4
+            if mode == 0:
+                for _ in range(int(rng.integers(1, 4))):
+                    c[int(rng.integers(0, len(c)))] = int(rng.integers(0, 256))
+            elif mode == 1:
+                c = c[:int(rng.integers(0, len(c)))]
+            elif mode == 2:
+                i = int(rng.integers(0, len(c) - 8))
+                c[i:i + 8] = int(rng.integers(0, 2 ** 63)).to_bytes(8, "little")
+            else:
+                c[int(rng.integers(0, len(c)))] ^= 1 << int(rng.integers(0, 8))
+            f = tmp_path / "d.h5"
+            f.write_bytes(bytes(c))
+            try:
+                _lib.h5_read(f, "x")
+                outcomes["read"] += 1
+            except _lib.SpinWalkError:
+                outcomes["error"] += 1
+    assert outcomes["error"] > 100 and sum(outcomes.values()) == 300

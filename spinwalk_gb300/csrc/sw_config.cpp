@@ -128,12 +128,28 @@ struct Reader {
     Config &c;
     std::string top;          // the top-level file (output dir is resolved against it)
     std::string err;
+    std::vector<std::string> chain;   // the files being read, outermost first
 
     bool read(const std::string &path) {
         if (!fs::exists(path)) {
             err = "config file does not exist: " + path;
             return false;
         }
+        // a file that is its own ancestor would recurse forever (the reference's reader does);
+        // here it is an error
+        std::error_code ec;
+        const std::string canon = fs::weakly_canonical(fs::absolute(path), ec).string();
+        if (std::find(chain.begin(), chain.end(), canon) != chain.end()) {
+            err = "PARENT_CONFIG cycle through " + path;
+            return false;
+        }
+        chain.push_back(canon);
+        const bool ok = read_one(path);
+        chain.pop_back();
+        return ok;
+    }
+
+    bool read_one(const std::string &path) {
         Ini ini;
         if (!parse_ini(path, ini)) {
             err = "failed to read config file: " + path;

@@ -223,3 +223,16 @@ def test_config_reader_matches_reference_on_its_shipped_configs(tmp_path):
             assert ours.read_text() == ref.read_text(), f
             parsed.append(f)
     assert len(parsed) >= 6, parsed
+
+
+def test_config_parent_cycle_is_an_error(tmp_path):
+    """A config that is its own ancestor through PARENT_CONFIG (directly or via another file)
+    is refused with a message; the reference's reader would recurse until the stack overflows."""
+    from spinwalk_gb300 import _lib as L
+    (tmp_path / "self.ini").write_text("[GENERAL]\nPARENT_CONFIG = self.ini\nSEQ_NAME = s\n")
+    (tmp_path / "a.ini").write_text("[GENERAL]\nPARENT_CONFIG = sub/../b.ini\n")
+    (tmp_path / "sub").mkdir()
+    (tmp_path / "b.ini").write_text("[GENERAL]\nPARENT_CONFIG = a.ini\n")
+    for name in ("self.ini", "a.ini"):
+        assert L.config_dump(str(tmp_path / name), tmp_path / "out.txt") != 0
+        assert b"PARENT_CONFIG cycle" in L.lib().sw_last_error()

@@ -38,6 +38,9 @@ int fail(int code, const std::string &msg);   // sets sw_last_error() (sw_api.cu
 }  // namespace api
 }  // namespace sw
 
+// Upper bound on the shapes one synthetic phantom may hold (the voxel loop visits every shape).
+constexpr double kMaxShapes = 1e6;
+
 extern "C" {
 
 int sw_phantom_cylinders(const uint32_t dims[3], const double fov[3], double radius,
@@ -60,6 +63,10 @@ int sw_phantom_cylinders(const uint32_t dims[3], const double fov[3], double rad
     std::vector<Cyl> cyl;
     const double target = volume_fraction * fov[0] * fov[1] * fov[2];
     const double L = std::cbrt(fov[0] * fov[1] * fov[2]);
+    if (target / (M_PI * radius * radius * L) > kMaxShapes)
+        return sw::api::fail(SW_ERR_INVALID, "sw_phantom_cylinders: the volume fraction needs more "
+                                             "than " + std::to_string((long)kMaxShapes) +
+                                             " cylinders of this radius");
     double vol = 0;
     while (vol < target) {
         Cyl c{};
@@ -140,6 +147,10 @@ int sw_phantom_spheres(const uint32_t dims[3], const double fov[3], double rmin,
     struct Sph { double c[3], r; };
     std::vector<Sph> sph;
     const double target = volume_fraction * fov[0] * fov[1] * fov[2];
+    if (target / (4.0 / 3.0 * M_PI * rmin * rmin * rmin) > kMaxShapes)
+        return sw::api::fail(SW_ERR_INVALID, "sw_phantom_spheres: the volume fraction may need more "
+                                             "than " + std::to_string((long)kMaxShapes) +
+                                             " spheres of these radii");
     double vol = 0;
     while (vol < target) {
         Sph s;

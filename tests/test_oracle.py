@@ -195,5 +195,9 @@ def test_host_entry_points_report_errors():
         _lib.phantom_cylinders(8, 8e-6, -1e-6, 0.1, seed=1)
     with pytest.raises(_lib.SpinWalkError, match="zero length"):
         _lib.phantom_spheres(8, 8e-6, 1e-6, 2e-6, 0.1, seed=1, B0_dir=(0.0, 0.0, 0.0))
+    with pytest.raises(_lib.SpinWalkError, match="more than 1000000 cylinders"):
+        _lib.phantom_cylinders(8, 8e-6, 1e-12, 0.5, seed=1)
+    with pytest.raises(_lib.SpinWalkError, match="more than 1000000 spheres"):
+        _lib.phantom_spheres(8, 8e-6, 1e-12, 2e-6, 0.5, seed=1)
     assert _lib.config_dump("/nonexistent/x.ini", os.devnull) != 0
     assert L.sw_last_error()

@@ -164,8 +164,10 @@ def test_run_config_matches_oracle_per_scale(tmp_path, scale_type, scales):
 
 def test_cli_rejects_cpu_flag_and_bad_config(tmp_path):
     exe = os.path.join(ROOT, "spinwalk_gb300", "spinwalk")
-    r = subprocess.run([exe, "sim", "-c", "x.ini", "-p"], capture_output=True, text=True)
+    r = subprocess.run([exe, "sim", "-c", "x.ini", "-p"], capture_output=True, text=True,
+                       cwd=tmp_path)
     assert r.returncode == 1 and "GPU only" in r.stderr
+    assert "GPU only" in (tmp_path / "log_spinwalk.txt").read_text()
     (tmp_path / "bad.ini").write_text("[SCAN_PARAMETERS]\nTE = 5 1\n")
     assert _lib.config_dump(str(tmp_path / "bad.ini"), tmp_path / "d.txt") != 0
 

@@ -172,6 +172,11 @@ int sw_h5_read(const char *path, const char *name, int *type, int *rank, uint64_
 int         sw_abi_version(void);
 const char *sw_last_error(void);
 int         sw_device_count(int *count);
+/* sim::print_device_info (src/sim/device_helper.cu:47-76), the CLI's -g/--gpu_info, as text in
+ * `buf` (NUL-terminated, at most `len` bytes): the CUDA versions of driver and runtime, the
+ * number of devices, and for `device` its name, compute capability and free / total memory.
+ * Without a device the text says so and SW_ERR_CUDA is returned. */
+int         sw_device_info(int device, char *buf, uint64_t len);
 
 /*
  * parameters::prepare (src/sim/simulation_parameters.cuh:227-245) on plain arrays:

@@ -31,6 +31,7 @@ def lib():
         L.sw_abi_version.restype = C.c_int
         L.sw_last_error.restype = C.c_char_p
         L.sw_device_count.argtypes = [P(C.c_int)]
+        L.sw_device_info.argtypes = [C.c_int, C.c_char_p, C.c_uint64]
         L.sw_prepare_params.argtypes = [P(abi.SwParams), P(C.c_double), P(C.c_float),
                                         P(C.c_float)]
         L.sw_fieldmap_scale.restype = C.c_float
@@ -106,6 +107,14 @@ def lib():
 def check(rc):
     if rc != abi.SW_OK:
         raise SpinWalkError(f"spinwalk error {rc}: {lib().sw_last_error().decode()}")
+
+
+def device_info(device=0):
+    """(rc, text) of sw_device_info: CUDA versions, device count, the device's name, compute
+    capability and memory (the reference CLI's -g/--gpu_info)."""
+    buf = C.create_string_buffer(1024)
+    rc = lib().sw_device_info(int(device), buf, len(buf))
+    return rc, buf.value.decode()
 
 
 def device_count():

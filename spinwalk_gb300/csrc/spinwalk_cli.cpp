@@ -68,11 +68,11 @@ int main(int argc, char **argv) {
             std::printf("spinwalk (GB300 sim path) ABI %d\n", sw_abi_version());
             return 0;
         }
-        if (a == "-g" || a == "--gpu_info") {
-            int n = 0;
-            sw_device_count(&n);
-            std::printf("GPUs: %d\n", n);
-            return n > 0 ? 0 : 1;
+        if (a == "-g" || a == "--gpu_info") {         // sim::print_device_info
+            char info[1024];
+            const int rc = sw_device_info(0, info, sizeof info);
+            std::printf("%s", info);
+            return rc == SW_OK ? 0 : 1;
         }
         if ((a == "-l" || a == "--log") && i + 1 < argc) {
             log_file = argv[++i];

@@ -331,3 +331,35 @@ extern "C" int sw_h5_read(const char *path, const char *name, int *type, int *ra
                           uint64_t dims[8], void *out, uint64_t out_bytes) {
     return guarded("sw_h5_read", [&] { return h5_read_impl(path, name, type, rank, dims, out, out_bytes); });
 }
+
+extern "C" int sw_device_info(int device, char *buf, uint64_t len) {
+    if (!buf || len == 0) return drv_fail(SW_ERR_INVALID, "sw_device_info: no buffer");
+    auto ver = [](int v) { return std::to_string(v / 1000) + "." + std::to_string((v % 1000) / 10); };
+    int rt = 0, drv = 0, n = 0;
+    cudaRuntimeGetVersion(&rt);
+    cudaDriverGetVersion(&drv);
+    std::string t = "The latest version of CUDA supported by the driver: " + ver(drv) +
+                    ", current CUDA version: " + ver(rt) + "\n";
+    int rc = SW_OK;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
+    cudaGetLastError();
+    t += "Number of devices: " + std::to_string(n) + "\n";
+    cudaDeviceProp prop;
+    size_t free_b = 0, total_b = 0;
+    if (device < 0 || device >= n) {
+        rc = SW_ERR_CUDA;
+        t += "device " + std::to_string(device) + " is not available\n";
+    } else if (cudaGetDeviceProperties(&prop, device) != cudaSuccess || cudaSetDevice(device) != cudaSuccess ||
+               cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        rc = SW_ERR_CUDA;
+        t += "device " + std::to_string(device) + ": properties not available\n";
+    } else {
+        t += std::string(prop.name) + "\n-Compute Capability: " + std::to_string(prop.major) + "." +
+             std::to_string(prop.minor) + "\n-Free GPU Memory: " + std::to_string(free_b >> 20) +
+             " MB (out of " + std::to_string(total_b >> 20) + " MB)\n";
+    }
+    std::snprintf(buf, (size_t)len, "%s", t.c_str());
+    if (rc) return sw::api::fail(rc, "device " + std::to_string(device) + " is not available");
+    return SW_OK;
+}

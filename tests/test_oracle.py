@@ -201,3 +201,14 @@ def test_host_entry_points_report_errors():
         _lib.phantom_spheres(8, 8e-6, 1e-12, 2e-6, 0.5, seed=1)
     assert _lib.config_dump("/nonexistent/x.ini", os.devnull) != 0
     assert L.sw_last_error()
+
+
+def test_device_info_text():
+    """sw_device_info (the CLI's -g/--gpu_info): on a machine without a GPU it says so and
+    returns an error; with one it names the device and its compute capability."""
+    rc, text = _lib.device_info(0)
+    assert "current CUDA version" in text and "Number of devices" in text
+    if _lib.device_count() == 0:
+        assert rc == abi.SW_ERR_CUDA and "not available" in text
+    else:
+        assert rc == abi.SW_OK and "Compute Capability:" in text

@@ -292,7 +292,8 @@ static int h5_read_impl(const char *path, const char *name, int *type, int *rank
                           uint64_t dims[8], void *out, uint64_t out_bytes) {
     sw::h5::Dataset d;
     std::string err;
-    if (!path || !name || !sw::h5::read(path, name, d, err)) return drv_fail(SW_ERR_IO, err);
+    if (!path || !name) return drv_fail(SW_ERR_INVALID, "sw_h5_read: null path or name");
+    if (!sw::h5::read(path, name, d, err, out != nullptr)) return drv_fail(SW_ERR_IO, err);
     if (d.dims.size() > 8) return drv_fail(SW_ERR_IO, "rank > 8");
     if (type) *type = (int)d.type;
     if (rank) *rank = (int)d.dims.size();

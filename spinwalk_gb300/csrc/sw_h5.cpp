@@ -11,6 +11,11 @@
 // takes chunked datasets (version-1 B-tree chunk index) with the deflate, shuffle and fletcher32
 // filters, as h5py's compression="gzip" and MATLAB's compressed files store them; unwritten
 // chunks read as zeros (the default fill value).
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
@@ -30,8 +35,59 @@ constexpr uint64_t kUndef = ~uint64_t(0);
 constexpr uint64_t kMaxDatasetBytes = 1ull << 40;
 const unsigned char kSig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
 
+// The file's bytes from its superblock on (a read-only memory map: only the pages a read
+// touches are loaded).
+struct View {
+    const char *p = nullptr;
+    uint64_t n = 0;
+    const char &operator[](uint64_t i) const { return p[i]; }
+    uint64_t size() const { return n; }
+    const char *data() const { return p; }
+};
+
+class MappedFile {
+  public:
+    MappedFile() = default;
+    MappedFile(const MappedFile &) = delete;
+    MappedFile &operator=(const MappedFile &) = delete;
+    ~MappedFile() {
+        if (map_) munmap(map_, len_);
+    }
+    // Maps the file and drops a user block: the superblock may start at 0, 512, 1024, ...; file
+    // addresses are relative to it (base address 0 in that frame).
+    bool open(const std::string &file, std::string &err) {
+        const int fd = ::open(file.c_str(), O_RDONLY);
+        if (fd < 0) { err = "cannot open " + file; return false; }
+        struct stat st;
+        if (fstat(fd, &st) != 0 || st.st_size < 8) {
+            ::close(fd);
+            err = file + " is not an HDF5 file";
+            return false;
+        }
+        len_ = (size_t)st.st_size;
+        void *m = mmap(nullptr, len_, PROT_READ, MAP_PRIVATE, fd, 0);
+        ::close(fd);
+        if (m == MAP_FAILED) { err = "cannot map " + file; return false; }
+        map_ = m;
+        const char *base = static_cast<const char *>(m);
+        for (uint64_t at = 0; at + 8 <= len_; at = at ? 2 * at : 512) {
+            if (std::memcmp(base + at, kSig, 8) == 0) {
+                view = View{base + at, len_ - at};
+                return true;
+            }
+        }
+        err = file + " is not an HDF5 file";
+        return false;
+    }
+    View view;
+
+  private:
+    void *map_ = nullptr;
+    size_t len_ = 0;
+};
+
 struct Buf {
-    const std::vector<char> &b;
+    const View &b;
     bool ok(uint64_t off, uint64_t n) const { return off <= b.size() && n <= b.size() - off; }
     uint64_t u(uint64_t off, int n) const {
         uint64_t v = 0;
@@ -517,30 +573,16 @@ bool read_chunked(const Buf &B, const std::vector<uint64_t> &dims, uint64_t esz,
     return true;
 }
 
-// Loads the file and drops a user block: the superblock may start at 0, 512, 1024, ...; file
-// addresses are relative to it (base address 0 in that frame).
-bool load(const std::string &file, std::vector<char> &b, std::string &err) {
-    std::ifstream f(file, std::ios::binary);
-    if (!f) { err = "cannot open " + file; return false; }
-    b.assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
-    for (uint64_t at = 0; at + 8 <= b.size(); at = at ? 2 * at : 512) {
-        if (std::memcmp(b.data() + at, kSig, 8) == 0) {
-            if (at) b.erase(b.begin(), b.begin() + (std::ptrdiff_t)at);
-            return true;
-        }
-    }
-    err = file + " is not an HDF5 file";
-    return false;
-}
-
 }  // namespace
 
 namespace {
 
-bool read_impl(const std::string &file, const std::string &name, Dataset &out, std::string &err) {
-    std::vector<char> bytes;
-    if (!load(file, bytes, err)) return false;
-    Buf B{bytes};
+bool read_impl(const std::string &file, const std::string &name, Dataset &out, std::string &err,
+               bool with_data) {
+    MappedFile mf;
+    if (!mf.open(file, err)) return false;
+    Buf B{mf.view};
+    const View &bytes = mf.view;
     std::vector<std::pair<std::string, uint64_t>> ents;
     if (!root_entries(B, ents, err)) return false;
     uint64_t addr = kUndef;
@@ -645,6 +687,7 @@ bool read_impl(const std::string &file, const std::string &name, Dataset &out, s
     else if (dtype_class == 1 && dtype_size == 4) out.type = kF32;
     else if (dtype_class == 1 && dtype_size == 8) out.type = kF64;
     else { err = "dataset " + name + ": unsupported datatype"; return false; }
+    if (!with_data) return true;
     if (chunked) {
         if (!read_chunked(B, out.dims, dtype_size, data_addr, cdim, filters, out.data, err)) {
             err = "dataset " + name + ": " + err;
@@ -661,7 +704,7 @@ bool read_impl(const std::string &file, const std::string &name, Dataset &out, s
         err = "dataset " + name + ": data outside the file";
         return false;
     }
-    out.data.assign(bytes.begin() + data_addr, bytes.begin() + data_addr + count * dtype_size);
+    out.data.assign(bytes.data() + data_addr, bytes.data() + data_addr + count * dtype_size);
     return true;
 }
 
@@ -669,9 +712,10 @@ bool read_impl(const std::string &file, const std::string &name, Dataset &out, s
 
 // Any allocation failure (a damaged file can claim a huge dataset) becomes an error, never an
 // exception across the C ABI.
-bool read(const std::string &file, const std::string &name, Dataset &out, std::string &err) {
+bool read(const std::string &file, const std::string &name, Dataset &out, std::string &err,
+          bool with_data) {
     try {
-        return read_impl(file, name, out, err);
+        return read_impl(file, name, out, err, with_data);
     } catch (const std::exception &e) {
         out = Dataset{};
         err = "dataset " + name + " in " + file + ": " + e.what();
@@ -680,9 +724,9 @@ bool read(const std::string &file, const std::string &name, Dataset &out, std::s
 }
 
 bool list(const std::string &file, std::vector<std::string> &names, std::string &err) {
-    std::vector<char> bytes;
-    if (!load(file, bytes, err)) return false;
-    Buf B{bytes};
+    MappedFile mf;
+    if (!mf.open(file, err)) return false;
+    Buf B{mf.view};
     std::vector<std::pair<std::string, uint64_t>> ents;
     if (!root_entries(B, ents, err)) return false;
     names.clear();
@@ -691,10 +735,10 @@ bool list(const std::string &file, std::vector<std::string> &names, std::string 
 }
 
 bool exists(const std::string &file, const std::string &name) {
-    std::vector<char> bytes;
     std::string err;
-    if (!load(file, bytes, err)) return false;
-    Buf B{bytes};
+    MappedFile mf;
+    if (!mf.open(file, err)) return false;
+    Buf B{mf.view};
     std::vector<std::pair<std::string, uint64_t>> ents;
     if (!root_entries(B, ents, err)) return false;
     for (auto &e : ents)

@@ -35,7 +35,9 @@ struct Dataset {
     std::vector<char> data;     // little-endian, row-major
 };
 
-bool read(const std::string &file, const std::string &name, Dataset &out, std::string &err);
+// The dataset `name` of the root group; with_data = false fills only dims and type.
+bool read(const std::string &file, const std::string &name, Dataset &out, std::string &err,
+          bool with_data = true);
 bool exists(const std::string &file, const std::string &name);
 bool list(const std::string &file, std::vector<std::string> &names, std::string &err);
 bool write(const std::string &file, const std::vector<std::pair<std::string, Dataset>> &sets,

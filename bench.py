@@ -1,27 +1,34 @@
 """Benchmark of the SpinWalk `sim` hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W]
-                    [--workload se|gre|bssfp|c3|serve|phantom]
-                    [--impl ours|reference]
+                    [--workload se|gre|c3|bssfp|serve|dwi|phantom|dense|small]
+                    [--impl ours|reference] [--no-legs]
 
 A "step" is one full pass of the hot path over one batch of synthetic input: per-spin generator
 seeding (mt19937(seed+spin) + discard), the walk over all time points and the Bloch update for
 every spin -- exactly the work of the reference's per-scale loop (src/sim/monte_carlo.cu:310-335).
 
-Workloads (synthetic, seeded; the reference publishes no dataset):
-  se  (default) spin echo, 500^3 phantom of random spheres (r 2-8 um, 5 %), 1e6 spins, 2001 time
-      points (TE 40 ms, dt 20 us, TR = TE + dt), permeability 0.01 both ways.
-  gre gradient echo, 200^3 phantom of random-orientation cylinders (r 5 um, 3 %), 1e5 spins,
-      401 time points (TE 20 ms, dt 50 us).
+The default run (`--workload se`) prints ONE line whose headline `value` is the plain kernel on
+the spin-echo workload (500^3 spheres, 1e6 spins, 2001 time points), and whose `legs` hold the
+other measurements of the metric, each with its own error against FP64:
+  gre      plain gradient echo, 200^3 cylinders, 1e5 spins, 401 time points
+  batched  64-instance FoV sweep (32 radii x GRE/SE, 1e4..1e6 spins each) in one sw_sim_batch
+  tracks   bSSFP, 64 phase cycles x DUMMY_SCAN 200..209 on one walk (sw_sim_tracks)
+  served   Poisson trace of 100 requests (GRE/SE/PGSE, 1e4..1e7 spins, three resident phantoms)
+           through the serving engine: warm (generator states cached), cold (first pass,
+           seeding inside the trace) and the service start-up
+The batched and served rates are also given as ratios to the plain headline value.
 
-Metric: spin-steps/s (spins x time points x scans per second of the whole pass). `value` is
-timed with CUDA events with every input already in HBM; `e2e` goes through the public host-buffer
-entry point sw_sim (host->device copies of the inputs and device->host copies of the results
-inside the timed region). Inputs (packed phantom, generator state) are larger than L2, so no
-explicit flush is needed between steps.
+Metric unit: spin-steps/s (spins x time points x scans per second; for batches, summed over the
+instances). `value` is timed with CUDA events with every input already in HBM; `e2e` goes through
+the public host-buffer entry point sw_sim (host->device copies of the inputs and device->host
+copies of the results inside the timed region). Inputs (packed phantom, generator state) are
+larger than L2, so no explicit flush is needed between steps.
 
 --impl reference times the reference algorithm's CPU path (the oracle port of sim::sim, with
 std::mt19937) on all host cores on a bounded, stratified sample of the same workload's spin ids.
+It builds its inputs with oracle/libsynth.so (the synthetic phantom generator compiled alone)
+and the oracle's initial positions, and never loads the CUDA library.
 Multi-GPU: spins are independent, so each rank walks its own spin range (weak scaling, no
 collective on the data path).
 """
@@ -39,8 +46,11 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = "spin-steps/s/GPU (batched+served vs plain) at ≤1e-5 err vs FP64; p50/p99 latency"
+UNIT = "spin-steps/s"
+
 GATHER_BYTES_PER_SPIN_STEP = 32   # one DRAM sector per random voxel lookup (mask + field record)
-USEFUL_BYTES_PER_SPIN_STEP = 5    # 1 B mask + 4 B field
+USEFUL_BYTES_PER_SPIN_STEP = 5    # 1 B mask + 4 B field at the visited voxel
 SEED_BYTES_PER_SPIN = 2 * 624 * 4 + 6 * 4   # two mt19937 states + 6 ring/index words written
 # DRAM traffic per unit from ncu on the small SE case (profiles/kernels_small_se_300cubed_2e5spins.md),
 # scaled to a full launch by the units it processes (both grow in proportion)
@@ -48,7 +58,6 @@ SEED_DRAM_BYTES_PER_SPIN = 4713.0
 MT_BYTES_PER_SPIN_STEP = 3.82 * 8        # MT words drawn per step x (4 B read + 4 B write)
 WALK_FP64_OPS_PER_SPIN_STEP = 6          # x, y, z step multiplies and position additions
 FP64_PEAK_GFLOPS = 152 * 2 * 2070e6 / 1e9  # 2 FP64 lanes per clock per SM at 2070 MHz
-USEFUL_BYTES_PER_SPIN_STEP = 5           # 1 B mask + 4 B field at the visited voxel
 WALK_DRAM_BYTES_PER_SPIN_STEP = 26.0
 SEED_LIMITER = ("integer instruction issue (ncu: ALU pipe 83 %, issue 74 %, DRAM 2 %): "
                 "7.7 lane instructions per MT word, not HBM")
@@ -57,12 +66,46 @@ WALK_LIMITER = ("FP64 pipe (ncu: 64 %, 3 position additions + 3 step multiplies 
                 "stalls, DRAM 10 %)")
 
 
-def workload(name, rank=0):
-    from spinwalk_gb300 import _lib
+# ------------------------------------------------------------------------------------------
+# Inputs
+# ------------------------------------------------------------------------------------------
+class Inputs:
+    """Where the synthetic inputs come from. The GPU arm uses the library (sw_phantom_*,
+    sw_initial_positions); the CPU reference arm the same generator source built alone
+    (oracle/libsynth.so) and the oracle's restatement of the reference driver's initial
+    positions, so that it never loads the CUDA library. Both give identical arrays."""
+
+    def __init__(self, oracle_side=False):
+        self.oracle_side = oracle_side
+
+    def _L(self):
+        if not self.oracle_side:
+            return None
+        from tests import oracle_lib
+        return oracle_lib.synth()
+
+    def spheres(self, n, fov, rmin, rmax, vf, seed):
+        from spinwalk_gb300 import _lib
+        return _lib.phantom_spheres(n, fov, rmin, rmax, vf, seed=seed, L=self._L())
+
+    def cylinders(self, n, fov, r, vf, seed):
+        from spinwalk_gb300 import _lib
+        return _lib.phantom_cylinders(n, fov, r, vf, seed=seed, L=self._L())
+
+    def positions(self, fov, seed, n):
+        if self.oracle_side:
+            from tests import oracle_lib
+            return oracle_lib.initial_positions(fov, seed, n)
+        from spinwalk_gb300 import _lib
+        return _lib.initial_positions(fov, seed, n)
+
+
+def workload(name, rank=0, inputs=None):
     from spinwalk_gb300.problem import Problem
+    inputs = inputs or Inputs()
     if name == "se":
         n, fov = 500, 500e-6
-        mask, field = _lib.phantom_spheres(n, fov, 2e-6, 8e-6, 0.05, seed=2)
+        mask, field = inputs.spheres(n, fov, 2e-6, 8e-6, 0.05, seed=2)
         n_spins = 1_000_000
         kw = dict(TR_us=40020, TE_us=(40000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
                   RF_us=(0, 20000), timestep_us=20, pXY=[[1.0, 0.01], [0.01, 1.0]],
@@ -72,15 +115,15 @@ def workload(name, rank=0):
                     permeability=0.01)
     elif name == "gre":
         n, fov = 200, 200e-6
-        mask, field = _lib.phantom_cylinders(n, fov, 5e-6, 0.03, seed=1)
+        mask, field = inputs.cylinders(n, fov, 5e-6, 0.03, seed=1)
         n_spins = 100_000
         kw = dict(TR_us=20050, TE_us=(20000,), timestep_us=50)
         desc = dict(workload="gre_cylinders_200cubed_1e5spins_401tp",
                     phantom="200^3 cylinders r5um 3% random orientation", n_spins=n_spins,
                     time_points=401, sequence="GRE 90, TE 20 ms, dt 50 us", permeability=0.0)
-    elif name == "bssfp":      # config 4 phantom/sequence; batched by run_tracks()
+    elif name == "bssfp":      # config 4 phantom/sequence; batched by leg_tracks()
         n, fov = 300, 300e-6
-        mask, field = _lib.phantom_cylinders(n, fov, 5e-6, 0.03, seed=4)
+        mask, field = inputs.cylinders(n, fov, 5e-6, 0.03, seed=4)
         n_spins = 200_000
         kw = dict(TR_us=5000, TE_us=(2500,), RF_FA=(30.0,), timestep_us=25, n_dummy_scan=209)
         desc = dict(workload="bssfp_cylinders_300cubed_2e5spins_64pc_x_10tr",
@@ -89,7 +132,7 @@ def workload(name, rank=0):
                              "(5.625 deg steps) x DUMMY_SCAN 200..209")
     elif name in ("dense", "dense_small"):   # many spins per voxel: the Morton re-sort's case
         n, fov = 100, 100e-6
-        mask, field = _lib.phantom_cylinders(n, fov, 5e-6, 0.03, seed=1)
+        mask, field = inputs.cylinders(n, fov, 5e-6, 0.03, seed=1)
         n_spins = 2_000_000 if name == "dense" else 500_000
         kw = dict(TR_us=40050, TE_us=(40000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
                   RF_us=(0, 20000), timestep_us=50)
@@ -99,7 +142,7 @@ def workload(name, rank=0):
                     sequence="SE 90/180, TE 40 ms, dt 50 us", permeability=0.0)
     elif name == "small":      # profiling case: > L2 phantom, few GB on the device
         n, fov = 300, 300e-6
-        mask, field = _lib.phantom_spheres(n, fov, 2e-6, 8e-6, 0.05, seed=2)
+        mask, field = inputs.spheres(n, fov, 2e-6, 8e-6, 0.05, seed=2)
         n_spins = 200_000
         kw = dict(TR_us=4020, TE_us=(4000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
                   RF_us=(0, 2000), timestep_us=20, pXY=[[1.0, 0.01], [0.01, 1.0]])
@@ -107,8 +150,20 @@ def workload(name, rank=0):
     else:
         raise SystemExit(f"unknown workload {name}")
     seed = 10 + 1_000_003 * rank          # each rank: its own disjoint spin population
-    pr = Problem(mask, [fov] * 3, field, n_spins=n_spins, seed=seed, **kw)
+    xyz0 = inputs.positions([fov] * 3, seed, n_spins)
+    pr = Problem(mask, [fov] * 3, field, n_spins=n_spins, seed=seed, XYZ0=xyz0, **kw)
     return pr, desc
+
+
+def bench_config(args, desc):
+    """The `config` object of both arms' lines: the workload and nothing that differs between
+    them (how the GPU arm shards is in its own `parallelism` key)."""
+    return dict(desc, l2="inputs larger than L2 (packed phantom + generator state)",
+                field_records="bfloat16, 4 B per voxel" if args.field_bf16
+                else "float32 fieldmap",
+                generators="thrust minstd_rand + erfcinv normal (the reference's CUDA build)"
+                if args.rng == "minstd" else
+                "std::mt19937 + polar normal (the reference's CPU build)")
 
 
 def measured_peaks():
@@ -168,21 +223,42 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# ------------------------------------------------------------------------------------------
+# Error against FP64
+# ------------------------------------------------------------------------------------------
+def _signal(m, ok):
+    """|mean over spins of Mx + iMy| per echo."""
+    return np.abs(m[ok, :, 0].mean(0) + 1j * m[ok, :, 1].mean(0))
+
+
+def fp64_error(pr, prec, rng=0):
+    """Error of one run in precision `prec` against the FP64 shadow of the same walk (computed by
+    the library alongside): the largest per-spin |M - M_fp64| (|M| <= 1) and the largest
+    relative error of the echo signal |mean Mxy| over all echoes."""
+    from spinwalk_gb300 import _lib
+    r = _lib.run(pr, precision=prec | rng, fp64_shadow=True)
+    m, d = r["M1"].astype(np.float64), r["M1_fp64"]
+    ok = r["status"] == 0
+    if not ok.any():
+        return {"max_abs_per_spin": 0.0, "signal_rel": 0.0}
+    s32, s64 = _signal(m, ok), _signal(d, ok)
+    return {"max_abs_per_spin": float(np.abs(m[ok] - d[ok]).max()),
+            "signal_rel": float((np.abs(s32 - s64) / np.maximum(s64, 1e-30)).max())}
+
+
 def precision_errors(pr, rng=0):
-    """Error of the FP32 and compensated-FP32 (Kahan) phase sums against an FP64 run of the same
-    walk (the FP64 shadow the library computes alongside): the largest per-spin |M - M_fp64|
-    (|M| <= 1) and the largest relative error of the echo signal |mean Mxy| over all echoes."""
-    from spinwalk_gb300 import _lib, abi
-    out = {}
-    for name, prec in (("fp32", abi.SW_PREC_FP32), ("kahan", abi.SW_PREC_KAHAN)):
-        r = _lib.run(pr, precision=prec | rng, fp64_shadow=True)
-        m, d = r["M1"].astype(np.float64), r["M1_fp64"]
-        ok = r["status"] == 0
-        sig = np.abs(m[ok, :, 0].mean(0) + 1j * m[ok, :, 1].mean(0))
-        sig64 = np.abs(d[ok, :, 0].mean(0) + 1j * d[ok, :, 1].mean(0))
-        out[name] = {"max_abs_per_spin": float(np.abs(m[ok] - d[ok]).max()),
-                     "signal_rel": float((np.abs(sig - sig64) / np.maximum(sig64, 1e-30)).max())}
-    return out
+    """fp32 and compensated-FP32 (Kahan) phase sums against FP64, on one problem."""
+    from spinwalk_gb300 import abi
+    return {name: fp64_error(pr, prec, rng)
+            for name, prec in (("fp32", abi.SW_PREC_FP32), ("kahan", abi.SW_PREC_KAHAN))}
+
+
+def max_errors(problems, rng=0):
+    """FP32 error against FP64 over several problems (the worst of each figure)."""
+    from spinwalk_gb300 import abi
+    errs = [fp64_error(p, abi.SW_PREC_FP32, rng) for p in problems]
+    return {"max_abs_per_spin": max(e["max_abs_per_spin"] for e in errs),
+            "signal_rel": max(e["signal_rel"] for e in errs)}
 
 
 def bf16_field_errors(pr):
@@ -207,6 +283,9 @@ def bf16_field_errors(pr):
     return out
 
 
+# ------------------------------------------------------------------------------------------
+# CPU baseline (the oracle port of the reference's CPU path)
+# ------------------------------------------------------------------------------------------
 def cpu_sample_ids(n_spins, n_sample):
     """Stratified sample: evenly spaced spin ids over the whole range (the per-spin discard()
     cost grows with the spin id, so a prefix would under-count it)."""
@@ -254,32 +333,38 @@ def max_over_ranks(world, x):
     return float(t.item())
 
 
+def rng_flag(args):
+    from spinwalk_gb300 import abi
+    return abi.SW_RNG_MINSTD if args.rng == "minstd" else abi.SW_RNG_MT19937
+
+
 def run_reference(args, world, rank):
-    """CPU reference arm: the oracle port on all host cores, rank 0 only."""
+    """CPU reference arm: the oracle port on all host cores, rank 0 only. Its inputs come from
+    oracle/libsynth.so and the oracle (the CUDA library is never loaded)."""
     if rank != 0:
         return
-    pr, desc = workload(args.workload)
+    pr, desc = workload(args.workload, inputs=Inputs(oracle_side=True))
+    rng = rng_flag(args)
     cores = os.cpu_count()
-    n_sample = args.cpu_sample
+    n_sample = args.ref_sample
     for _ in range(args.warmup):
-        time_cpu(pr, max(16, n_sample // 8), cores)
+        time_cpu(pr, max(16, n_sample // 8), cores, rng=rng)
     rates, secs = [], []
     for _ in range(args.steps):
-        r, n, dt = time_cpu(pr, n_sample, cores)
+        r, n, dt = time_cpu(pr, n_sample, cores, rng=rng)
         rates.append(r)
         secs.append(dt)
     v = float(np.mean(rates))
     sample = (f"{n} stratified spin ids of {pr.params.n_spins} per step, "
               f"{pr.params.n_timepoints} time points each, extrapolated as spin-steps/s")
-    line = {"impl": "reference", "metric": "spin-steps/s", "value": v, "unit": "spin-steps/s",
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * float(np.mean(secs)), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(desc, l2="inputs larger than L2"),
-            "cpu_baseline": {"value": v, "unit": "spin-steps/s", "cores": cores, "kind": "port",
+            "config": bench_config(args, desc),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
-            "e2e": {"value": v, "unit": "spin-steps/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -304,27 +389,30 @@ def apply_tuning(args, pr=None):
     return info
 
 
-def run_ours(args, world, rank, local):
+# ------------------------------------------------------------------------------------------
+# Plain kernel (the headline) and the plain GRE leg
+# ------------------------------------------------------------------------------------------
+def device_buffers(pr, dev):
     import torch
-    from spinwalk_gb300 import _lib
-
-    torch.cuda.set_device(local)
-    pr, desc = workload(args.workload, rank)
-    tuning = apply_tuning(args, pr)
     p = pr.params
     n, nte = p.n_spins, pr.n_te
-    dev = torch.device("cuda", local)
-    d = dict(field=torch.from_numpy(pr.field).to(dev), mask=torch.from_numpy(pr.mask).to(dev),
-             M0=torch.from_numpy(pr.M0).to(dev), XYZ0=torch.from_numpy(pr.XYZ0).to(dev),
-             M1=torch.zeros((n, nte, 3), dtype=torch.float32, device=dev),
-             XYZ1=torch.zeros((n, pr.traj_len, 3), dtype=torch.float32, device=dev),
-             T=torch.zeros((n, nte), dtype=torch.uint8, device=dev),
-             status=torch.zeros(n, dtype=torch.int32, device=dev))
-    stream = torch.cuda.current_stream(dev)
+    return dict(field=torch.from_numpy(pr.field).to(dev), mask=torch.from_numpy(pr.mask).to(dev),
+                M0=torch.from_numpy(pr.M0).to(dev), XYZ0=torch.from_numpy(pr.XYZ0).to(dev),
+                M1=torch.zeros((n, nte, 3), dtype=torch.float32, device=dev),
+                XYZ1=torch.zeros((n, pr.traj_len, 3), dtype=torch.float32, device=dev),
+                T=torch.zeros((n, nte), dtype=torch.uint8, device=dev),
+                status=torch.zeros(n, dtype=torch.int32, device=dev))
 
-    from spinwalk_gb300 import abi
-    rng = abi.SW_RNG_MINSTD if args.rng == "minstd" else abi.SW_RNG_MT19937
-    prec = abi.SW_PREC_FP32 | (abi.SW_FIELD_BF16 if args.field_bf16 else 0) | rng
+
+def time_plain(pr, prec, steps, warmup, world, local, clocks=True):
+    """The plain kernel on device buffers: `steps` passes timed with CUDA events on the
+    launching stream (barrier + synchronize on both sides), then the same pass end to end
+    through sw_sim with host buffers. Returns a dict of the figures."""
+    import torch
+    from spinwalk_gb300 import _lib
+    dev = torch.device("cuda", local)
+    d = device_buffers(pr, dev)
+    stream = torch.cuda.current_stream(dev)
 
     def step():
         _lib.run_device(pr, d["field"].data_ptr(), d["mask"].data_ptr(), d["M0"].data_ptr(),
@@ -332,273 +420,65 @@ def run_ours(args, world, rank, local):
                         d["T"].data_ptr(), d["status"].data_ptr(), precision=prec,
                         stream=stream.cuda_stream)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
-    spin_steps = pr.spin_steps()
     timings = []
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        barrier(world)
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        for _ in range(args.steps):
-            step()
-            timings.append(_lib.last_timing())
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        barrier(world)
-    clocks = clk.summary()
-    ms = ev0.elapsed_time(ev1)
-    ms = max_over_ranks(world, ms)
-    value = world * spin_steps * args.steps / (ms * 1e-3)
+    sampler = ClockSampler(local) if clocks else None
+    if sampler:
+        sampler.__enter__()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(steps):
+        step()
+        timings.append(_lib.last_timing())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    if sampler:
+        sampler.__exit__()
+    ms = max_over_ranks(world, ev0.elapsed_time(ev1))
     st = d["status"].cpu().numpy()
+    del d
 
-    # ---- end to end through the host-buffer entry point ----
-    e2e_times = []
-    h2d = pr.mask.nbytes + pr.field.nbytes + pr.M0.nbytes + pr.XYZ0.nbytes + \
-        n * nte * 12 + n * nte + n * pr.traj_len * 12
+    # end to end through the host-buffer entry point
+    n, nte = pr.params.n_spins, pr.n_te
+    h2d = pr.mask.nbytes + pr.field.nbytes + pr.M0.nbytes + pr.XYZ0.nbytes
     d2h = n * nte * 12 + n * nte + n * pr.traj_len * 12 + n * 4
     _lib.run(pr, precision=prec)                     # warm (host staging)
-    for _ in range(max(1, args.steps)):
+    e2e_times = []
+    for _ in range(max(1, steps)):
         barrier(world)
         t = time.perf_counter()
         out = _lib.run(pr, precision=prec)
         e2e_times.append(time.perf_counter() - t)
     e2e_s = max_over_ranks(world, float(np.mean(e2e_times)))
-    e2e = world * spin_steps / e2e_s
     assert np.array_equal(out["status"], st)
-
-    if rank != 0:
-        return
-    walk_ms = sum(t["walk_ms"] for t in timings)
-    refill_ms = sum(t["refill_ms"] for t in timings)
-    seed_ms = sum(t["seed_ms"] for t in timings)
-    n_walk = sum(t["n_chunks"] for t in timings)
-    launches = sum(t["n_launches"] for t in timings)
-    parts = {"walk": walk_ms, "refill": refill_ms, "seed+init+pack": seed_ms}
-    dominant = max(parts, key=parts.get)
-    peak, peak_kind = measured_peaks()
-    n_chunks = n_walk / args.steps
-    # k_seed (seed+init+pack stage): algorithmic bytes = the generator state it must write
-    seed_launch_s = seed_ms / args.steps * 1e-3
-    seed_roof = {"bound": "hbm", "kernel": "k_seed", "unit_of_work": "spin",
-                 "algorithmic_bytes_per_unit": SEED_BYTES_PER_SPIN,
-                 "achieved": n * SEED_BYTES_PER_SPIN / seed_launch_s / 1e9, "peak": peak,
-                 "unit": "GB/s", "traffic": SEED_DRAM_BYTES_PER_SPIN * n,
-                 "peak_source": peak_kind, "limiter": SEED_LIMITER}
-    # k_walk: one 32 B DRAM sector per spin-step (random voxel gather)
-    walk_launch_s = walk_ms / n_walk * 1e-3
-    walk_units = spin_steps / n_chunks
-    walk_roof = {"bound": "hbm", "kernel": "k_walk", "unit_of_work": "spin-step",
-                 "algorithmic_bytes_per_unit": GATHER_BYTES_PER_SPIN_STEP,
-                 "achieved": walk_units * GATHER_BYTES_PER_SPIN_STEP / walk_launch_s / 1e9,
-                 "peak": peak, "unit": "GB/s",
-                 "traffic": WALK_DRAM_BYTES_PER_SPIN_STEP * walk_units,
-                 "peak_source": peak_kind, "limiter": WALK_LIMITER}
-    for r in (seed_roof, walk_roof):
-        r["frac"] = r["achieved"] / peak
-    roof = {"seed+init+pack": seed_roof, "walk": walk_roof}.get(dominant, walk_roof)
-    # walk-only rate (refill + walk kernels, generator seeding excluded) and the secondary
-    # ceilings: MT-state traffic of the refill (3.82 words of 8 B read+write per step) and the
-    # FP64 work of the walk (3 position additions per step, 2 FP64 lanes per clock per SM)
-    # wall time of the rounds: the call minus its seeding stage (the kernel times of the two
-    # halves of the rounds overlap, so their sum would overstate it)
-    walk_refill_s = ms / args.steps * 1e-3 - seed_ms / args.steps * 1e-3
-    secondary = {
-        "walk_only_spin_steps_per_s": spin_steps / walk_refill_s,
-        "refill_mt_state_gbs": spin_steps * MT_BYTES_PER_SPIN_STEP / (refill_ms / args.steps * 1e-3) / 1e9,
-        "walk_fp64_gflops": spin_steps * WALK_FP64_OPS_PER_SPIN_STEP / (walk_ms / args.steps * 1e-3) / 1e9,
-        "fp64_peak_gflops": FP64_PEAK_GFLOPS,
-        "useful_gather_gbs": spin_steps * USEFUL_BYTES_PER_SPIN_STEP / (walk_ms / args.steps * 1e-3) / 1e9,
-        "note": "walk-only = call time minus the seeding stage; the refill and walk kernel times "
-                "of the two halves of the rounds overlap; ncu: k_walk L2 hit rate and FP64 pipe "
-                "in profiles/",
-    }
-    errors = precision_errors(pr, rng) if args.workload in ("se", "small") else None
-    bf16_err = bf16_field_errors(pr) if args.field_bf16 else None
-    cpu = None
-    if world == 1 or rank == 0:
-        if args.cpu_sample > 0:
-            rate, ns, dt = time_cpu(pr, args.cpu_sample, os.cpu_count(), rng=rng)
-            wrate, wns, wdt = time_cpu(pr, max(1, args.cpu_sample // 4), os.cpu_count(),
-                                       lowest=True, rng=rng)
-            cpu = {"value": rate, "unit": "spin-steps/s", "cores": os.cpu_count(), "kind": "port",
-                   "sample": f"{ns} stratified spin ids of {n} ({pr.params.n_timepoints} time "
-                             f"points each, {dt:.1f} s wall on {os.cpu_count()} threads)",
-                   "walk_only": {"value": wrate, "unit": "spin-steps/s",
-                                 "sample": f"spin ids 0..{wns - 1} (discard of at most "
-                                           f"{int(pr.params.seed) + wns} words), {wdt:.1f} s wall"}}
-    line = {
-        "metric": "spin-steps/s", "value": value, "unit": "spin-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded phantom generator, reference-driver initial positions)",
-        "config": dict(desc, parallelism=f"spin-range shards x{world}",
-                       l2="inputs larger than L2 (packed phantom + generator state)",
-                       field_records="bfloat16, 4 B per voxel" if args.field_bf16
-                       else "float32, 8 B per voxel",
-                       generators="thrust minstd_rand + erfcinv normal (the reference's CUDA "
-                                  "build)" if args.rng == "minstd" else
-                                  "std::mt19937 + polar normal (the reference's CPU build)"),
-        "kernel_ms_per_step": {k: v / args.steps for k, v in parts.items()},
-        "kernel_ms_note": "sums of launch durations; the refill/walk rounds run as two halves on "
-                          "two streams whose kernels overlap, so walk + refill exceed their wall "
-                          "time",
-        "roofline": dict(roof, dominant_stage=dominant),
-        "roofline_walk": walk_roof,
-        "secondary_ceilings": secondary,
-        "cpu_baseline": cpu,
-        "e2e": {"value": e2e, "unit": "spin-steps/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": int(launches),
-        "tuning": tuning,
-        "error_vs_fp64": errors,
-        "field_bf16": bf16_err,
-        "clocks": clocks,
-        "status_counts": {str(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))},
-    }
-    print(json.dumps(line), flush=True)
+    return dict(ms=ms, timings=timings, status=st, e2e_s=e2e_s, h2d=h2d, d2h=d2h,
+                clocks=sampler.summary() if sampler else None)
 
 
-def run_batched(args, world, rank):
-    """Config 4 batched: 64 phase-cycling scales x 10 sampled TRs (DUMMY_SCAN 200..209) = 640
-    reference instances on ONE walk (sw_sim_tracks). Work is counted per instance, as the
-    reference executes it: sum over instances of spins x time points x (DUMMY_SCAN + 1)."""
-    import torch  # noqa: F401  (device selection only)
-    from spinwalk_gb300 import _lib
-    pr, desc = workload("bssfp", rank)
-    p = pr.params
-    tracks = [dict(linear_phase_cycling=5.625 * i, n_dummy_scan=d)
-              for i in range(64) for d in range(200, 210)]
-    inst_steps = sum(p.n_spins * p.n_timepoints * (t["n_dummy_scan"] + 1) for t in tracks)
-    walk_steps = p.n_spins * p.n_timepoints * 210
-    for _ in range(args.warmup):
-        _lib.run_tracks(pr, tracks)
-    times, dev_ms, launches = [], [], []
-    with ClockSampler(0) as clk:
-        for _ in range(args.steps):
-            t = time.perf_counter()
-            _lib.run_tracks(pr, tracks)
-            times.append(time.perf_counter() - t)
-            dev_ms.append(_lib.last_timing()["total_ms"])
-            launches.append(_lib.last_timing()["n_launches"])
-    clocks = clk.summary()
-    # the plain kernel on one instance of the same config, for the batched/plain ratio
-    one = dict(tracks[-1])
-    pr.params.linear_phase_cycling = one["linear_phase_cycling"]
-    pr.params.n_dummy_scan = one["n_dummy_scan"]
-    _lib.run(pr)
-    t = time.perf_counter()
-    _lib.run(pr)
-    plain_s = time.perf_counter() - t
-    plain_dev = _lib.last_timing()["total_ms"] * 1e-3
-    plain_rate = p.n_spins * p.n_timepoints * (one["n_dummy_scan"] + 1) / plain_dev
-    value = inst_steps / (np.mean(dev_ms) * 1e-3)
-    pr.params.linear_phase_cycling = 0.0
-    pr.params.n_dummy_scan = 0
-    rec_err = bssfp_cycle_errors(pr, [t for t in tracks if t["n_dummy_scan"] == 209])
-    line = {"metric": "spin-steps/s (batched instances)", "value": value, "unit": "spin-steps/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": float(np.mean(dev_ms)), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(desc, instances=len(tracks), instance_spin_steps=int(inst_steps),
-                           distinct_walk_spin_steps=int(walk_steps)),
-            "distinct_walk_steps_per_s": walk_steps / (np.mean(dev_ms) * 1e-3),
-            "plain_kernel_one_instance": {"value": plain_rate, "e2e_s": plain_s},
-            "batched_over_plain": value / plain_rate,
-            "e2e": {"value": inst_steps / float(np.mean(times)), "unit": "spin-steps/s",
-                    "note": "includes the per-track host output copies"},
-            "recurrence_error_vs_fp64": rec_err,
-            "gpu_launches": int(sum(launches)),
-            "clocks": clocks}
-    print(json.dumps(line), flush=True)
+def leg_gre(args, local=0):
+    """Config 1, plain: GRE on 200^3 cylinders, 1e5 spins, 401 time points."""
+    from spinwalk_gb300 import abi
+    pr, desc = workload("gre")
+    steps = max(3, min(args.steps, 10))
+    r = time_plain(pr, abi.SW_PREC_FP32 | rng_flag(args), steps, max(3, args.warmup), 1, local,
+                   clocks=False)
+    ss = pr.spin_steps()
+    return {"workload": desc["workload"], "value": ss * steps / (r["ms"] * 1e-3), "unit": UNIT,
+            "ms_per_step": r["ms"] / steps, "steps": steps,
+            "e2e": {"value": ss / r["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": int(r["h2d"]),
+                    "d2h_bytes_per_step": int(r["d2h"])},
+            "gpu_launches": int(sum(t["n_launches"] for t in r["timings"])),
+            "error_vs_fp64": precision_errors(pr, rng_flag(args))}
 
 
-def bssfp_cycle_errors(pr, tracks):
-    """Error of the float steady-state recurrence against its FP64 shadow, per phase cycle: the
-    given tracks (one per cycle) run once with plain float and once with compensated (Kahan)
-    phase sums, each beside the FP64 shadow of the same walk (sw_sim_tracks M1_fp64). Per cycle:
-    the relative error of the signal (complex mean of Mx + iMy over spins, first echo) and the
-    largest per-spin |M - M_fp64|."""
-    from spinwalk_gb300 import _lib, abi
-    res = {"cycles": len(tracks), "n_dummy_scan": tracks[0]["n_dummy_scan"],
-           "definition": "signal: |S - S64| / |S64|, S = mean over spins of Mx + iMy at the "
-                         "first echo; spin: max over spins of max |M - M64| (M0 = 1)"}
-    for name, prec in (("fp32", abi.SW_PREC_FP32), ("kahan", abi.SW_PREC_KAHAN)):
-        outs = _lib.run_tracks(pr, tracks, precision=prec, fp64=True)
-        sig, spin = [], []
-        for o in outs:
-            ok = o["status"] == 0
-            m, md = o["M1"][ok, 0].astype(np.float64), o["M1_fp64"][ok, 0]
-            s32 = np.mean(m[:, 0] + 1j * m[:, 1])
-            s64 = np.mean(md[:, 0] + 1j * md[:, 1])
-            sig.append(abs(s32 - s64) / max(abs(s64), 1e-300))
-            spin.append(float(np.max(np.abs(m - md))) if ok.any() else 0.0)
-        res[name] = {"signal_rel_max": float(max(sig)), "signal_rel_median": float(np.median(sig)),
-                     "spin_abs_max": float(max(spin)),
-                     "signal_rel_per_cycle": [float(f"{v:.3g}") for v in sig]}
-    return res
-
-
-def run_dwi(args, world, rank):
-    """DWI b-value sweep (the reference's gradient scale loop, WHAT_TO_SCALE = 1): PGSE along x
-    (b = 1000 s/mm^2 at scale 1, delta 10 ms, Delta 20 ms) on the 200^3 cylinder phantom of
-    config 1, 1e6 spins, 8 gradient scales 0 .. 1.4 (b 0 .. 1960 s/mm^2). One walk with a phase
-    per scale (sw_sim_tracks) against one walk per scale with one seeding (sw_sim_batch); the
-    work is counted per instance."""
-    import torch  # noqa: F401
-    from spinwalk_gb300 import _lib
-    from spinwalk_gb300.problem import Problem
-    n, fov = 200, 200e-6
-    mask, field = _lib.phantom_cylinders(n, fov, 5e-6, 0.03, seed=1)
-    lobe = lambda t0: list(range(t0, t0 + 10000, 50))                       # noqa: E731
-    g_t = lobe(2000) + [12000] + lobe(22000) + [32000]
-    g = np.zeros((len(g_t), 3), np.float32)
-    for i, t in enumerate(g_t):
-        if t not in (12000, 32000):
-            g[i, 0] = 91.6
-    kw = dict(TR_us=34050, TE_us=(34000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
-              RF_us=(0, 17000), timestep_us=50, gradient_us=tuple(g_t), gradient_xyz=g)
-    n_spins = 1_000_000
-    pr = Problem(mask, [fov] * 3, field, n_spins=n_spins, seed=10 + 1_000_003 * rank, **kw)
-    scales = [0.2 * i for i in range(8)]
-    tracks = [dict(gradient_scale=sc, n_dummy_scan=0) for sc in scales]
-
-    def scaled(sc):
-        q = Problem(mask, [fov] * 3, field, n_spins=n_spins, seed=10 + 1_000_003 * rank,
-                    **dict(kw, gradient_xyz=g * np.float32(sc)))
-        return q
-    insts = [scaled(sc) for sc in scales]
-    steps = len(scales) * pr.spin_steps()
-    for _ in range(args.warmup):
-        _lib.run_tracks(pr, tracks)
-    t_ms, b_ms = [], []
-    with ClockSampler(0) as clk:
-        for _ in range(args.steps):
-            _lib.run_tracks(pr, tracks)
-            t_ms.append(_lib.last_timing()["total_ms"])
-    clocks = clk.summary()
-    _lib.run_batch(insts)
-    for _ in range(max(1, args.steps // 2)):
-        _lib.run_batch(insts)
-        b_ms.append(_lib.last_timing()["total_ms"])
-    value = world * steps / (np.mean(t_ms) * 1e-3)
-    batch = steps / (np.mean(b_ms) * 1e-3)
-    line = {"metric": "spin-steps/s (gradient-scale sweep, per instance)", "value": value,
-            "unit": "spin-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": float(np.mean(t_ms)), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "dwi_pgse_8_gradient_scales_200cubed_1e6spins",
-                       "phantom": "200^3 cylinders r5um 3% (config 1)", "n_spins": n_spins,
-                       "sequence": "PGSE x, delta 10 ms, Delta 20 ms, TE 34 ms, dt 50 us",
-                       "gradient_scales": scales},
-            "one_walk_per_scale": {"value": batch, "ms": float(np.mean(b_ms))},
-            "shared_over_separate": value / batch, "clocks": clocks}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-
-
+# ------------------------------------------------------------------------------------------
+# Batched: the config-3 FoV sweep in one sw_sim_batch
+# ------------------------------------------------------------------------------------------
 def c3_instances(rank=0):
     """Config 3: the config-1 phantom (200^3 random-orientation cylinders, r 5 um, 3 %), 32 FoV
     scales giving vessel radii 1-100 um (log-spaced; scale = r / 5 um, WHAT_TO_SCALE = 0) x
@@ -633,27 +513,26 @@ def c3_instances(rank=0):
     return probs, desc
 
 
-def run_batch_scales(args, world, rank):
+def leg_batched(args, rank=0, world=1):
     """Config 3 batched (sw_sim_batch: phantom packed once, generators seeded once for all 64
     instances, instances in spin-range chunks on concurrent slots) against the same instances
-    run one sw_sim each. `value` is timed on the host around the whole call (staging copies
-    included; every call uploads the phantom and seeds again)."""
-    import torch  # noqa: F401
+    run one sw_sim each. `value` is the device time of the whole call (CUDA events); `e2e` the
+    host time around it (staging copies included; every call uploads the phantom and seeds
+    again)."""
     from spinwalk_gb300 import _lib
     probs, desc = c3_instances(rank)
     tuning = apply_tuning(args, max(probs, key=lambda q: q.params.n_spins))
     steps = sum(p.spin_steps() for p in probs)
-    for _ in range(args.warmup):
+    reps = max(3, min(args.steps, 5))
+    for _ in range(max(3, min(args.warmup, 3))):
         _lib.run_batch(probs)
     dev_ms, wall, launches = [], [], []
-    with ClockSampler(0) as clk:
-        for _ in range(args.steps):
-            t = time.perf_counter()
-            _lib.run_batch(probs)
-            wall.append(time.perf_counter() - t)
-            dev_ms.append(_lib.last_timing()["total_ms"])
-            launches.append(_lib.last_timing()["n_launches"])
-    clocks = clk.summary()
+    for _ in range(reps):
+        t = time.perf_counter()
+        _lib.run_batch(probs)
+        wall.append(time.perf_counter() - t)
+        dev_ms.append(_lib.last_timing()["total_ms"])
+        launches.append(_lib.last_timing()["n_launches"])
     plain_ms, plain_wall = 0.0, 0.0
     for p in probs:
         t = time.perf_counter()
@@ -662,28 +541,108 @@ def run_batch_scales(args, world, rank):
         plain_ms += _lib.last_timing()["total_ms"]
     value = world * steps / (np.mean(dev_ms) * 1e-3)
     plain = steps / (plain_ms * 1e-3)
-    line = {"metric": "spin-steps/s (batched instances)", "value": value, "unit": "spin-steps/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": float(np.mean(dev_ms)), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+    # FP32 error against FP64 on the smallest, two middle and the largest radius, GRE and SE
+    # (a batch instance is bit-identical to its own sw_sim run)
+    err_idx = sorted({0, 1, 30, 31, 62, 63} | {int(np.argmax([p.params.n_spins for p in probs]))})
+    return {"workload": desc["workload"], "value": value, "unit": UNIT,
+            "ms_per_step": float(np.mean(dev_ms)), "steps": reps,
             "config": dict(desc, instance_spin_steps=int(steps)),
             "plain_one_call_per_instance": {"value": plain, "ms": plain_ms,
                                             "e2e_value": steps / plain_wall},
-            "batched_over_plain": value / plain,
-            "batched_over_plain_e2e": float(np.mean(wall)) and (steps / float(np.mean(wall))) / (steps / plain_wall),
-            "e2e": {"value": world * steps / float(np.mean(wall)), "unit": "spin-steps/s",
+            "batched_over_one_call_per_instance": value / plain,
+            "e2e": {"value": world * steps / float(np.mean(wall)), "unit": UNIT,
                     "note": "sw_sim_batch with host buffers"},
             "gpu_launches": int(sum(launches)),
-            "tuning": tuning, "clocks": clocks}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+            "error_vs_fp64": dict(max_errors([probs[i] for i in err_idx], rng_flag(args)),
+                                  precision="fp32", instances=err_idx),
+            "tuning": tuning}
 
 
+# ------------------------------------------------------------------------------------------
+# Tracks: config 4 (bSSFP phase cycles x dummy scans on one walk)
+# ------------------------------------------------------------------------------------------
+def bssfp_cycle_errors(pr, tracks):
+    """Error of the float steady-state recurrence against its FP64 shadow, per phase cycle: the
+    given tracks (one per cycle) run once with plain float and once with compensated (Kahan)
+    phase sums, each beside the FP64 shadow of the same walk (sw_sim_tracks M1_fp64). Per cycle:
+    the relative error of the signal (complex mean of Mx + iMy over spins, first echo) and the
+    largest per-spin |M - M_fp64|."""
+    from spinwalk_gb300 import _lib, abi
+    res = {"cycles": len(tracks), "n_dummy_scan": tracks[0]["n_dummy_scan"],
+           "definition": "signal: |S - S64| / |S64|, S = mean over spins of Mx + iMy at the "
+                         "first echo; spin: max over spins of max |M - M64| (M0 = 1)"}
+    for name, prec in (("fp32", abi.SW_PREC_FP32), ("kahan", abi.SW_PREC_KAHAN)):
+        outs = _lib.run_tracks(pr, tracks, precision=prec, fp64=True)
+        sig, spin = [], []
+        for o in outs:
+            ok = o["status"] == 0
+            m, md = o["M1"][ok, 0].astype(np.float64), o["M1_fp64"][ok, 0]
+            s32 = np.mean(m[:, 0] + 1j * m[:, 1])
+            s64 = np.mean(md[:, 0] + 1j * md[:, 1])
+            sig.append(abs(s32 - s64) / max(abs(s64), 1e-300))
+            spin.append(float(np.max(np.abs(m - md))) if ok.any() else 0.0)
+        res[name] = {"signal_rel_max": float(max(sig)), "signal_rel_median": float(np.median(sig)),
+                     "spin_abs_max": float(max(spin)),
+                     "signal_rel_per_cycle": [float(f"{v:.3g}") for v in sig]}
+    return res
+
+
+def leg_tracks(args, rank=0, world=1):
+    """Config 4 batched: 64 phase-cycling scales x 10 sampled TRs (DUMMY_SCAN 200..209) = 640
+    reference instances on ONE walk (sw_sim_tracks). Work is counted per instance, as the
+    reference executes it: sum over instances of spins x time points x (DUMMY_SCAN + 1)."""
+    from spinwalk_gb300 import _lib
+    pr, desc = workload("bssfp", rank)
+    p = pr.params
+    tracks = [dict(linear_phase_cycling=5.625 * i, n_dummy_scan=d)
+              for i in range(64) for d in range(200, 210)]
+    inst_steps = sum(p.n_spins * p.n_timepoints * (t["n_dummy_scan"] + 1) for t in tracks)
+    walk_steps = p.n_spins * p.n_timepoints * 210
+    reps = max(2, min(args.steps, 3))
+    for _ in range(max(3, min(args.warmup, 3))):
+        _lib.run_tracks(pr, tracks)
+    times, dev_ms, launches = [], [], []
+    for _ in range(reps):
+        t = time.perf_counter()
+        _lib.run_tracks(pr, tracks)
+        times.append(time.perf_counter() - t)
+        dev_ms.append(_lib.last_timing()["total_ms"])
+        launches.append(_lib.last_timing()["n_launches"])
+    # the plain kernel on one instance of the same config, for the batched/plain ratio
+    one = dict(tracks[-1])
+    pr.params.linear_phase_cycling = one["linear_phase_cycling"]
+    pr.params.n_dummy_scan = one["n_dummy_scan"]
+    _lib.run(pr)
+    t = time.perf_counter()
+    _lib.run(pr)
+    plain_s = time.perf_counter() - t
+    plain_dev = _lib.last_timing()["total_ms"] * 1e-3
+    plain_rate = p.n_spins * p.n_timepoints * (one["n_dummy_scan"] + 1) / plain_dev
+    value = world * inst_steps / (np.mean(dev_ms) * 1e-3)
+    pr.params.linear_phase_cycling = 0.0
+    pr.params.n_dummy_scan = 0
+    rec_err = bssfp_cycle_errors(pr, [t for t in tracks if t["n_dummy_scan"] == 209])
+    return {"workload": desc["workload"], "value": value, "unit": UNIT,
+            "ms_per_step": float(np.mean(dev_ms)), "steps": reps,
+            "config": dict(desc, instances=len(tracks), instance_spin_steps=int(inst_steps),
+                           distinct_walk_spin_steps=int(walk_steps)),
+            "distinct_walk_steps_per_s": walk_steps / (np.mean(dev_ms) * 1e-3),
+            "plain_kernel_one_instance": {"value": plain_rate, "e2e_s": plain_s},
+            "tracks_over_one_instance": value / plain_rate,
+            "e2e": {"value": inst_steps / float(np.mean(times)), "unit": UNIT,
+                    "note": "includes the per-track host output copies"},
+            "gpu_launches": int(sum(launches)),
+            "error_vs_fp64": {"recurrence": rec_err}}
+
+
+# ------------------------------------------------------------------------------------------
+# Served: the config-5 trace through the serving engine
+# ------------------------------------------------------------------------------------------
 def serve_requests(n_req, rng_seed=5, rank=0):
     """Config 5 trace: Poisson arrivals (mean 20 / s), requests on resident phantoms, spins
     log-uniform in [1e4, 1e7], a mix of GRE, SE and PGSE (b = 1000 s/mm^2, delta 10 ms, Delta
     20 ms, lobes from 2 ms, G = 91.6 mT/m along x, y or z; TE 34 ms; dt 50 us). One simulation
-    seed for the service (its generator states are computed once, at start-up)."""
+    seed for the service."""
     from spinwalk_gb300 import _lib
     from spinwalk_gb300.problem import Problem
     rng = np.random.default_rng(rng_seed)
@@ -729,16 +688,44 @@ def serve_requests(n_req, rng_seed=5, rank=0):
                 phantoms="100^3 cylinders, 200^3 spheres, 800^3 reference cylinders (resident)",
                 spins_per_request="log-uniform [1e4, 1e7], seed 5",
                 sequences="GRE 20 ms / SE 40 ms / PGSE b=1000 x,y,z", arrivals="Poisson, 20 / s")
-    return reqs, phantoms, arrivals, desc
+    return reqs, phantoms, arrivals, kinds, desc
 
 
-def run_serve(args, world, rank):
+def play_trace(eng, reqs, arrivals, submit):
+    """Submits the requests at their arrival times (real time) and polls until every result is
+    in the caller's buffers. Returns (makespan s, latencies s, engine stats delta)."""
+    n_req = len(reqs)
+    st0 = eng.stats()
+    lat = []
+    t_start = time.perf_counter()
+    i = 0
+    while i < n_req or len(lat) < n_req:
+        now = time.perf_counter() - t_start
+        while i < n_req and arrivals[i] <= now:
+            submit(reqs[i])
+            i += 1
+        for jid, rc, lt in eng.poll(wait=0):
+            assert rc == 0
+            lat.append(lt)
+        time.sleep(0.0005)
+    makespan = time.perf_counter() - t_start
+    st1 = eng.stats()
+    return makespan, np.array(lat), {k: int(st1[k] - st0[k]) for k in st1}
+
+
+def _lat(lat):
+    return {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+            "max": float(lat.max())}
+
+
+def leg_served(args, rank=0, world=1):
     """Config 5: the requests are submitted to one engine at their arrival times; latency =
-    submit -> results in the caller's buffers (queueing included)."""
-    import torch  # noqa: F401
+    submit -> results in the caller's buffers (queueing included). Two passes of the same trace
+    on one engine: `cold` is the first (generator states computed as requests need them, inside
+    the trace), `value` the second (warm: every request's states come from the cache)."""
     from spinwalk_gb300 import _lib
     n_req = args.requests
-    reqs, phantoms, arrivals, desc = serve_requests(n_req, rank=rank)
+    reqs, phantoms, arrivals, kinds, desc = serve_requests(n_req, rank=rank)
     tuning = apply_tuning(args, max(reqs, key=lambda q: q.params.n_spins))
     eng = _lib.Engine(n_slots=8, slot_spins=1 << 20)
     pids = {}
@@ -747,57 +734,237 @@ def run_serve(args, world, rank):
         key = pr.mask.shape
         if key not in pids:
             pids[key] = eng.add_phantom(pr, bf16=args.field_bf16)
+    phantom_s = time.perf_counter() - t0
 
     def submit(pr):
         if args.signal:
             return eng.submit_signal(pr, pids[pr.mask.shape])
         return eng.submit(pr, pids[pr.mask.shape])
-    # service start-up: generator states of the largest request, computed once
-    big = max(reqs, key=lambda p: p.params.n_spins)
-    submit(big)
-    eng.run_all()
-    startup_s = time.perf_counter() - t0
-    st0 = eng.stats()
     steps = sum(p.spin_steps() for p in reqs)
-    lat = []
+    cold_s, cold_lat, cold_st = play_trace(eng, reqs, arrivals, submit)
     with ClockSampler(0) as clk:
-        t_start = time.perf_counter()
-        i = 0
-        while i < n_req or len(lat) < n_req:
-            now = time.perf_counter() - t_start
-            while i < n_req and arrivals[i] <= now:
-                submit(reqs[i])
-                i += 1
-            for jid, rc, l in eng.poll(wait=0):
-                assert rc == 0
-                lat.append(l)
-            time.sleep(0.0005)
-        makespan = time.perf_counter() - t_start
+        warm_s, warm_lat, warm_st = play_trace(eng, reqs, arrivals, submit)
     clocks = clk.summary()
-    st1 = eng.stats()
-    lat = np.array(lat)
-    value = world * steps / makespan
-    line = {"metric": "spin-steps/s (served)", "value": value, "unit": "spin-steps/s",
-            "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": makespan * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
+    eng.close()
+    # FP32 error against FP64 on the smallest request of each kind (a served request is
+    # bit-identical to its own sw_sim run)
+    sample = []
+    for k in range(5):
+        idx = [i for i in range(n_req) if kinds[i] == k]
+        if idx:
+            sample.append(min(idx, key=lambda i: reqs[i].params.n_spins))
+    value = world * steps / warm_s
+    return {"workload": desc["workload"], "value": value, "unit": UNIT,
+            "ms_per_step": warm_s * 1e3, "steps": 1,
             "config": dict(desc, requests=n_req, spin_steps=int(steps),
                            outputs="per-(echo, substrate) signal sums (signal mode)" if args.signal
                            else "per-spin M1, T, XYZ1, status",
                            field_records="bfloat16, 4 B per voxel" if args.field_bf16
                            else "float32, 8 B per voxel"),
-            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                          "max": float(lat.max())},
+            "latency_s": _lat(warm_lat),
+            "cold": {"value": world * steps / cold_s, "makespan_s": cold_s,
+                     "latency_s": _lat(cold_lat), "seedings": cold_st["seedings"],
+                     "note": "first pass of the trace on a new engine: every generator state "
+                             "is computed inside the trace, when a request first needs it"},
+            "startup": {"phantom_upload_s": phantom_s,
+                        "note": "phantoms packed and made resident before the first request"},
             "offered_spin_steps_per_s": steps / float(arrivals[-1]),
-            "startup_s": startup_s,
-            "e2e": {"value": value, "unit": "spin-steps/s",
+            "e2e": {"value": value, "unit": UNIT,
                     "note": "host buffers in and out through the engine, arrivals in real time"},
-            "gpu_launches": int(st1["launches"] - st0["launches"]),
-            "walk_rounds": int(st1["rounds"] - st0["rounds"]),
+            "gpu_launches": int(warm_st["launches"]), "walk_rounds": int(warm_st["rounds"]),
+            "seedings_warm": int(warm_st["seedings"]),
+            "error_vs_fp64": dict(max_errors([reqs[i] for i in sample], rng_flag(args)),
+                                  precision="fp32", requests=sample),
             "tuning": tuning, "clocks": clocks}
-    eng.close()
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------------
+# The default line
+# ------------------------------------------------------------------------------------------
+def run_ours(args, world, rank, local):
+    import torch
+    from spinwalk_gb300 import _lib, abi
+
+    torch.cuda.set_device(local)
+    pr, desc = workload(args.workload, rank)
+    tuning = apply_tuning(args, pr)
+    p = pr.params
+    n = p.n_spins
+    rng = rng_flag(args)
+    prec = abi.SW_PREC_FP32 | (abi.SW_FIELD_BF16 if args.field_bf16 else 0) | rng
+    spin_steps = pr.spin_steps()
+    r = time_plain(pr, prec, args.steps, args.warmup, world, local)
+    ms, timings, st, clocks = r["ms"], r["timings"], r["status"], r["clocks"]
+    value = world * spin_steps * args.steps / (ms * 1e-3)
+    e2e = world * spin_steps / r["e2e_s"]
+
+    if rank != 0:
+        return
+    walk_ms = sum(t["walk_ms"] for t in timings)
+    refill_ms = sum(t["refill_ms"] for t in timings)
+    seed_ms = sum(t["seed_ms"] for t in timings)
+    n_walk = sum(t["n_chunks"] for t in timings)
+    launches = sum(t["n_launches"] for t in timings)
+    parts = {"walk": walk_ms, "refill": refill_ms, "seed+init+pack": seed_ms}
+    dominant = max(parts, key=parts.get)
+    peak, peak_kind = measured_peaks()
+    n_chunks = n_walk / args.steps
+    # k_seed (seed+init+pack stage): algorithmic bytes = the generator state it must write
+    seed_launch_s = seed_ms / args.steps * 1e-3
+    seed_roof = {"bound": "hbm", "kernel": "k_seed", "unit_of_work": "spin",
+                 "algorithmic_bytes_per_unit": SEED_BYTES_PER_SPIN,
+                 "achieved": n * SEED_BYTES_PER_SPIN / seed_launch_s / 1e9, "peak": peak,
+                 "unit": "GB/s", "traffic": SEED_DRAM_BYTES_PER_SPIN * n,
+                 "peak_source": peak_kind, "limiter": SEED_LIMITER}
+    # k_walk: one 32 B DRAM sector per spin-step (random voxel gather)
+    walk_launch_s = walk_ms / n_walk * 1e-3
+    walk_units = spin_steps / n_chunks
+    walk_roof = {"bound": "hbm", "kernel": "k_walk", "unit_of_work": "spin-step",
+                 "algorithmic_bytes_per_unit": GATHER_BYTES_PER_SPIN_STEP,
+                 "achieved": walk_units * GATHER_BYTES_PER_SPIN_STEP / walk_launch_s / 1e9,
+                 "peak": peak, "unit": "GB/s",
+                 "traffic": WALK_DRAM_BYTES_PER_SPIN_STEP * walk_units,
+                 "peak_source": peak_kind, "limiter": WALK_LIMITER}
+    for rf in (seed_roof, walk_roof):
+        rf["frac"] = rf["achieved"] / peak
+    roof = {"seed+init+pack": seed_roof, "walk": walk_roof}.get(dominant, walk_roof)
+    # walk-only rate: the call's wall time minus its seeding stage (the kernel times of the two
+    # halves of the rounds overlap, so their sum would overstate it)
+    walk_refill_s = ms / args.steps * 1e-3 - seed_ms / args.steps * 1e-3
+    secondary = {
+        "walk_only_spin_steps_per_s": spin_steps / walk_refill_s,
+        "refill_mt_state_gbs": spin_steps * MT_BYTES_PER_SPIN_STEP / (refill_ms / args.steps * 1e-3) / 1e9,
+        "walk_fp64_gflops": spin_steps * WALK_FP64_OPS_PER_SPIN_STEP / (walk_ms / args.steps * 1e-3) / 1e9,
+        "fp64_peak_gflops": FP64_PEAK_GFLOPS,
+        "useful_gather_gbs": spin_steps * USEFUL_BYTES_PER_SPIN_STEP / (walk_ms / args.steps * 1e-3) / 1e9,
+        "note": "walk-only = call time minus the seeding stage; the refill and walk kernel times "
+                "of the two halves of the rounds overlap; ncu: k_walk L2 hit rate and FP64 pipe "
+                "in profiles/",
+    }
+    errors = precision_errors(pr, rng) if args.workload in ("se", "small") else None
+    bf16_err = bf16_field_errors(pr) if args.field_bf16 else None
+    cpu = None
+    if args.cpu_sample > 0:
+        rate, ns, dt = time_cpu(pr, args.cpu_sample, os.cpu_count(), rng=rng)
+        wrate, wns, wdt = time_cpu(pr, max(1, args.cpu_sample // 16), os.cpu_count(),
+                                   lowest=True, rng=rng)
+        cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{ns} stratified spin ids of {n} ({pr.params.n_timepoints} time "
+                         f"points each, {dt:.1f} s wall on {os.cpu_count()} threads)",
+               "walk_only": {"value": wrate, "unit": UNIT,
+                             "sample": f"spin ids 0..{wns - 1} (discard of at most "
+                                       f"{int(pr.params.seed) + wns} words), {wdt:.1f} s wall"}}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded phantom generator, reference-driver initial positions)",
+        "config": bench_config(args, desc),
+        "value_is": "the plain kernel (one sw_sim_device pass: seeding, walk and Bloch update of "
+                    "every spin) on the spin-echo workload; legs.batched and legs.served are "
+                    "the batched and served rates",
+        "parallelism": f"spin-range shards x{world}",
+        "kernel_ms_per_step": {k: v / args.steps for k, v in parts.items()},
+        "kernel_ms_note": "sums of launch durations; the refill/walk rounds run as two halves on "
+                          "two streams whose kernels overlap, so walk + refill exceed their wall "
+                          "time",
+        "roofline": dict(roof, dominant_stage=dominant),
+        "roofline_walk": walk_roof,
+        "secondary_ceilings": secondary,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(r["h2d"]),
+                "d2h_bytes_per_step": int(r["d2h"])},
+        "gpu_launches": int(launches),
+        "tuning": tuning,
+        "error_vs_fp64": errors,
+        "field_bf16": bf16_err,
+        "clocks": clocks,
+        "status_counts": {str(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))},
+    }
+    if args.workload == "se" and not args.no_legs and world == 1:
+        legs = {}
+        for name, fn in (("gre", leg_gre), ("batched", leg_batched), ("tracks", leg_tracks),
+                         ("served", leg_served)):
+            t = time.perf_counter()
+            legs[name] = fn(args) if name != "gre" else fn(args, local)
+            legs[name]["leg_wall_s"] = time.perf_counter() - t
+        line["legs"] = legs
+        line["batched_over_plain"] = legs["batched"]["value"] / value
+        line["served_over_plain"] = legs["served"]["value"] / value
+        line["served_cold_over_plain"] = legs["served"]["cold"]["value"] / value
+        line["tracks_over_plain"] = legs["tracks"]["value"] / value
+        line["ratios_note"] = ("leg value / headline value (plain kernel on the spin-echo "
+                               "workload); each leg also carries its ratio to the plain kernel "
+                               "on its own instances")
+    print(json.dumps(line), flush=True)
+
+
+def print_leg(args, world, rank, leg):
+    """One line for a leg run on its own (--workload c3 / bssfp / serve)."""
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": leg["value"], "unit": UNIT, "n_gpus": world,
+            "steps": leg.get("steps", args.steps), "warmup": args.warmup,
+            "ms_per_step": leg.get("ms_per_step"), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic"}
+    line.update({k: v for k, v in leg.items() if k not in line})
+    print(json.dumps(line), flush=True)
+
+
+def run_dwi(args, world, rank):
+    """DWI b-value sweep (the reference's gradient scale loop, WHAT_TO_SCALE = 1): PGSE along x
+    (b = 1000 s/mm^2 at scale 1, delta 10 ms, Delta 20 ms) on the 200^3 cylinder phantom of
+    config 1, 1e6 spins, 8 gradient scales 0 .. 1.4 (b 0 .. 1960 s/mm^2). One walk with a phase
+    per scale (sw_sim_tracks) against one walk per scale with one seeding (sw_sim_batch); the
+    work is counted per instance."""
+    import torch  # noqa: F401
+    from spinwalk_gb300 import _lib
+    from spinwalk_gb300.problem import Problem
+    n, fov = 200, 200e-6
+    mask, field = _lib.phantom_cylinders(n, fov, 5e-6, 0.03, seed=1)
+    lobe = lambda t0: list(range(t0, t0 + 10000, 50))                       # noqa: E731
+    g_t = lobe(2000) + [12000] + lobe(22000) + [32000]
+    g = np.zeros((len(g_t), 3), np.float32)
+    for i, t in enumerate(g_t):
+        if t not in (12000, 32000):
+            g[i, 0] = 91.6
+    kw = dict(TR_us=34050, TE_us=(34000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
+              RF_us=(0, 17000), timestep_us=50, gradient_us=tuple(g_t), gradient_xyz=g)
+    n_spins = 1_000_000
+    pr = Problem(mask, [fov] * 3, field, n_spins=n_spins, seed=10 + 1_000_003 * rank, **kw)
+    scales = [0.2 * i for i in range(8)]
+    tracks = [dict(gradient_scale=sc, n_dummy_scan=0) for sc in scales]
+
+    def scaled(sc):
+        return Problem(mask, [fov] * 3, field, n_spins=n_spins, seed=10 + 1_000_003 * rank,
+                       **dict(kw, gradient_xyz=g * np.float32(sc)))
+    insts = [scaled(sc) for sc in scales]
+    steps = len(scales) * pr.spin_steps()
+    for _ in range(args.warmup):
+        _lib.run_tracks(pr, tracks)
+    t_ms, b_ms = [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            _lib.run_tracks(pr, tracks)
+            t_ms.append(_lib.last_timing()["total_ms"])
+    clocks = clk.summary()
+    _lib.run_batch(insts)
+    for _ in range(max(1, args.steps // 2)):
+        _lib.run_batch(insts)
+        b_ms.append(_lib.last_timing()["total_ms"])
+    value = world * steps / (np.mean(t_ms) * 1e-3)
+    batch = steps / (np.mean(b_ms) * 1e-3)
+    leg = {"value": value, "ms_per_step": float(np.mean(t_ms)), "steps": args.steps,
+           "config": {"workload": "dwi_pgse_8_gradient_scales_200cubed_1e6spins",
+                      "phantom": "200^3 cylinders r5um 3% (config 1)", "n_spins": n_spins,
+                      "sequence": "PGSE x, delta 10 ms, Delta 20 ms, TE 34 ms, dt 50 us",
+                      "gradient_scales": scales},
+           "one_walk_per_scale": {"value": batch, "ms": float(np.mean(b_ms))},
+           "shared_over_separate": value / batch,
+           "error_vs_fp64": dict(max_errors([insts[0], insts[-1]], rng_flag(args)),
+                                 precision="fp32", scales=[scales[0], scales[-1]]),
+           "clocks": clocks}
+    print_leg(args, world, rank, leg)
 
 
 def run_phantom(args, world, rank):
@@ -833,15 +1000,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="se")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample", type=int, default=32768)
-    ap.add_argument("--requests", type=int, default=100, help="serve workload: trace length")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="se workload: skip the GRE / batched / tracks / served legs")
+    ap.add_argument("--cpu-sample", type=int, default=262144,
+                    help="spin ids of the GPU arm's CPU baseline (stratified over the range)")
+    ap.add_argument("--ref-sample", type=int, default=32768,
+                    help="spin ids per step of the CPU reference arm (stratified)")
+    ap.add_argument("--requests", type=int, default=100, help="served leg: trace length")
     ap.add_argument("--autotune", action="store_true",
                     help="pick the walk tuning by sw_autotune on the workload before timing")
     ap.add_argument("--resort-interval", type=int, default=None,
                     help="walk rounds between Morton re-sorts of the spins (0 = never)")
     ap.add_argument("--walk-block", type=int, default=None, help="walk kernel block size")
     ap.add_argument("--signal", action="store_true",
-                    help="serve workload: requests in signal mode (no per-spin outputs)")
+                    help="served leg: requests in signal mode (no per-spin outputs)")
     ap.add_argument("--field-bf16", action="store_true",
                     help="bfloat16 fieldmap records (SW_FIELD_BF16); reports their error")
     ap.add_argument("--rng", default="mt19937", choices=["mt19937", "minstd"],
@@ -854,14 +1026,14 @@ def main():
     world, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, world, rank)
-    elif args.workload == "bssfp":
-        run_batched(args, world, rank)
+        return
+    if args.workload in ("bssfp", "c3", "serve"):
+        import torch
+        torch.cuda.set_device(local)
+        fn = {"bssfp": leg_tracks, "c3": leg_batched, "serve": leg_served}[args.workload]
+        print_leg(args, world, rank, fn(args, rank, world))
     elif args.workload == "dwi":
         run_dwi(args, world, rank)
-    elif args.workload == "c3":
-        run_batch_scales(args, world, rank)
-    elif args.workload == "serve":
-        run_serve(args, world, rank)
     elif args.workload == "phantom":
         run_phantom(args, world, rank)
     else:

@@ -3,7 +3,10 @@
   spinwalk_gb300/libspinwalk_gpu.so   nvcc, sm_103a only, -fmad=false (bit-exact float order)
   spinwalk_gb300/spinwalk             the `spinwalk sim -c cfg.ini` command-line host (C++)
   oracle/liboracle.so                 the test oracle (g++), built here for tests and bench
-  oracle/_ref/libref_sim.so           the reference's own sim(), only where its source exists
+  oracle/libsynth.so                  the synthetic phantom generator alone (the CPU reference
+                                      arm of the benchmark makes its inputs with it)
+  oracle/_ref/libref_sim.so           the reference's own sim(), only where its source tree is
+                                      given by the SPINWALK_REF_SRC environment variable
 
 Translation units compile in parallel; a unit is rebuilt when any source or header changed.
 """
@@ -20,7 +23,7 @@ CSRC = os.path.join(PKG, "csrc")
 INC = os.path.join(ROOT, "include")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libspinwalk_gpu.so")
-REF_TREE = "/root/reference"
+REF_TREE = os.environ.get("SPINWALK_REF_SRC", "")   # the SpinWalk source tree, if any
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", *ARCH, "-lineinfo", "-fmad=false",
@@ -108,8 +111,8 @@ def build_lib(verbose=False, force=False):
 
 def build_oracle(verbose=False):
     od = os.path.join(ROOT, "oracle")
-    _run(["make", "-s", "-C", od, "liboracle.so"], verbose)
-    if os.path.isdir(os.path.join(REF_TREE, "src", "sim")):
+    _run(["make", "-s", "-C", od, "liboracle.so", "libsynth.so"], verbose)
+    if REF_TREE and os.path.isdir(os.path.join(REF_TREE, "src", "sim")):
         _run(["make", "-s", "-C", od, "ref", f"REF={REF_TREE}"], verbose)
 
 

@@ -38,12 +38,7 @@ def lib():
         L.sw_fieldmap_scale.argtypes = [C.c_float, C.c_int32]
         L.sw_initial_positions.argtypes = [P(C.c_float), C.c_uint64, C.c_uint32, P(C.c_float)]
         L.sw_logf_exception_count.argtypes = [P(C.c_uint64), P(C.c_uint64)]
-        L.sw_phantom_cylinders.argtypes = [P(C.c_uint32), P(C.c_double), C.c_double, C.c_double,
-                                           C.c_uint64, C.c_int, C.c_double, C.c_double,
-                                           P(C.c_double), C.c_void_p, C.c_void_p]
-        L.sw_phantom_spheres.argtypes = [P(C.c_uint32), P(C.c_double), C.c_double, C.c_double,
-                                         C.c_double, C.c_uint64, C.c_double, C.c_double,
-                                         P(C.c_double), C.c_double, C.c_void_p, C.c_void_p]
+        set_phantom_argtypes(L)
         sim_args = [P(abi.SwParams), P(abi.SwSequence), C.c_void_p, C.c_void_p, C.c_void_p,
                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                     C.c_void_p]
@@ -135,30 +130,53 @@ def initial_positions(fov, seed, n_spins):
     return out
 
 
+def set_phantom_argtypes(L):
+    """Argument types of sw_phantom_cylinders / sw_phantom_spheres on library handle L."""
+    P = C.POINTER
+    L.sw_phantom_cylinders.argtypes = [P(C.c_uint32), P(C.c_double), C.c_double, C.c_double,
+                                       C.c_uint64, C.c_int, C.c_double, C.c_double,
+                                       P(C.c_double), C.c_void_p, C.c_void_p]
+    L.sw_phantom_spheres.argtypes = [P(C.c_uint32), P(C.c_double), C.c_double, C.c_double,
+                                     C.c_double, C.c_uint64, C.c_double, C.c_double,
+                                     P(C.c_double), C.c_double, C.c_void_p, C.c_void_p]
+
+
+def _phantom_rc(rc, L, what):
+    if rc == abi.SW_OK:
+        return
+    if L is None:
+        check(rc)
+    raise SpinWalkError(f"{what} failed with code {rc}")
+
+
 def phantom_cylinders(n, fov_m, radius_m, volume_fraction, seed, random_orientation=True,
-                      dchi=0.11e-6 * 0.4, Y=0.75, B0_dir=(0.0, 0.0, 1.0)):
-    """Seeded infinite cylinders: (mask uint8 [n,n,n], field float32 Tesla at 1 T)."""
+                      dchi=0.11e-6 * 0.4, Y=0.75, B0_dir=(0.0, 0.0, 1.0), L=None):
+    """Seeded infinite cylinders: (mask uint8 [n,n,n], field float32 Tesla at 1 T). L: another
+    library handle exporting sw_phantom_cylinders (default: this library)."""
     dims = (C.c_uint32 * 3)(n, n, n)
     fov = (C.c_double * 3)(fov_m, fov_m, fov_m)
     b0 = (C.c_double * 3)(*B0_dir)
     mask = np.empty((n, n, n), np.uint8)
     field = np.empty((n, n, n), np.float32)
-    check(lib().sw_phantom_cylinders(dims, fov, radius_m, volume_fraction, int(seed),
-                                     1 if random_orientation else 0, dchi, Y, b0, _p(mask),
-                                     _p(field)))
+    rc = (L or lib()).sw_phantom_cylinders(dims, fov, radius_m, volume_fraction, int(seed),
+                                           1 if random_orientation else 0, dchi, Y, b0, _p(mask),
+                                           _p(field))
+    _phantom_rc(rc, L, "sw_phantom_cylinders")
     return mask, field
 
 
 def phantom_spheres(n, fov_m, rmin_m, rmax_m, volume_fraction, seed, dchi=0.11e-6 * 0.4,
-                    Y=0.75, B0_dir=(0.0, 0.0, 1.0), window=5.0):
-    """Seeded spheres with superposed dipole fields: (mask uint8, field float32 Tesla at 1 T)."""
+                    Y=0.75, B0_dir=(0.0, 0.0, 1.0), window=5.0, L=None):
+    """Seeded spheres with superposed dipole fields: (mask uint8, field float32 Tesla at 1 T).
+    L: another library handle exporting sw_phantom_spheres (default: this library)."""
     dims = (C.c_uint32 * 3)(n, n, n)
     fov = (C.c_double * 3)(fov_m, fov_m, fov_m)
     b0 = (C.c_double * 3)(*B0_dir)
     mask = np.empty((n, n, n), np.uint8)
     field = np.empty((n, n, n), np.float32)
-    check(lib().sw_phantom_spheres(dims, fov, rmin_m, rmax_m, volume_fraction, int(seed), dchi,
-                                   Y, b0, window, _p(mask), _p(field)))
+    rc = (L or lib()).sw_phantom_spheres(dims, fov, rmin_m, rmax_m, volume_fraction, int(seed),
+                                         dchi, Y, b0, window, _p(mask), _p(field))
+    _phantom_rc(rc, L, "sw_phantom_spheres")
     return mask, field
 
 

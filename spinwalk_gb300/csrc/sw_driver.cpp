@@ -347,6 +347,9 @@ extern "C" int sw_device_info(int device, char *buf, uint64_t len) {
     t += "Number of devices: " + std::to_string(n) + "\n";
     cudaDeviceProp prop;
     size_t free_b = 0, total_b = 0;
+    int prev = -1;                           // the caller's current device, restored below
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    cudaGetLastError();
     if (device < 0 || device >= n) {
         rc = SW_ERR_CUDA;
         t += "device " + std::to_string(device) + " is not available\n";
@@ -359,6 +362,10 @@ extern "C" int sw_device_info(int device, char *buf, uint64_t len) {
         t += std::string(prop.name) + "\n-Compute Capability: " + std::to_string(prop.major) + "." +
              std::to_string(prop.minor) + "\n-Free GPU Memory: " + std::to_string(free_b >> 20) +
              " MB (out of " + std::to_string(total_b >> 20) + " MB)\n";
+    }
+    if (prev >= 0 && prev != device) {
+        cudaSetDevice(prev);
+        cudaGetLastError();
     }
     std::snprintf(buf, (size_t)len, "%s", t.c_str());
     if (rc) return sw::api::fail(rc, "device " + std::to_string(device) + " is not available");

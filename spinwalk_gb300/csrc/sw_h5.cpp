@@ -20,6 +20,7 @@
 #include <cstdint>
 #include <cstring>
 #include <fstream>
+#include <new>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -54,7 +55,9 @@ class MappedFile {
         if (map_) munmap(map_, len_);
     }
     // Maps the file and drops a user block: the superblock may start at 0, 512, 1024, ...; file
-    // addresses are relative to it (base address 0 in that frame).
+    // addresses are relative to it (base address 0 in that frame). Where the file system cannot
+    // map the file, the whole file is read into memory instead. A mapped file must not be
+    // truncated while it is read (the process would get SIGBUS on the lost pages).
     bool open(const std::string &file, std::string &err) {
         const int fd = ::open(file.c_str(), O_RDONLY);
         if (fd < 0) { err = "cannot open " + file; return false; }
@@ -66,10 +69,32 @@ class MappedFile {
         }
         len_ = (size_t)st.st_size;
         void *m = mmap(nullptr, len_, PROT_READ, MAP_PRIVATE, fd, 0);
+        const char *base = nullptr;
+        if (m != MAP_FAILED) {
+            map_ = m;
+            base = static_cast<const char *>(m);
+        } else {                                   // buffered read of the whole file
+            try {
+                copy_.resize(len_);
+            } catch (const std::bad_alloc &) {
+                ::close(fd);
+                err = "cannot map or read " + file + " (out of memory)";
+                return false;
+            }
+            size_t got = 0;
+            while (got < len_) {
+                const ssize_t r = ::pread(fd, copy_.data() + got, len_ - got, (off_t)got);
+                if (r <= 0) break;
+                got += (size_t)r;
+            }
+            if (got != len_) {
+                ::close(fd);
+                err = "cannot read " + file;
+                return false;
+            }
+            base = copy_.data();
+        }
         ::close(fd);
-        if (m == MAP_FAILED) { err = "cannot map " + file; return false; }
-        map_ = m;
-        const char *base = static_cast<const char *>(m);
         for (uint64_t at = 0; at + 8 <= len_; at = at ? 2 * at : 512) {
             if (std::memcmp(base + at, kSig, 8) == 0) {
                 view = View{base + at, len_ - at};
@@ -83,6 +108,7 @@ class MappedFile {
 
   private:
     void *map_ = nullptr;
+    std::vector<char> copy_;    // the file's bytes where it could not be mapped
     size_t len_ = 0;
 };
 

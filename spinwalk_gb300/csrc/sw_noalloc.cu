@@ -103,10 +103,14 @@ extern "C" int sw_sim_device_noalloc(const sw_params *p, const sw_sequence *q,
     const Layout L = layout(R.base + R.work_offset, p->n_spins, p->matrix_length,
                             im.bytes.size(), false);
     cudaStream_t st = (cudaStream_t)stream;
+    // On an error the call first waits for what it already queued on `stream`, so that no
+    // kernel of a failed call still writes the shared array when the next call takes it over.
 #define NA_CUDA(call)                                                                      \
     do {                                                                                   \
         cudaError_t e_ = (call);                                                           \
         if (e_ != cudaSuccess) {                                                           \
+            cudaGetLastError();                                                            \
+            cudaStreamSynchronize(st);                                                     \
             cudaGetLastError();                                                            \
             return fail(SW_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));  \
         }                                                                                  \
@@ -133,7 +137,9 @@ extern "C" int sw_sim_device_noalloc(const sw_params *p, const sw_sequence *q,
     const uint64_t max_rounds = 64 + steps * (p->max_iterations + 2);
     const sw_tuning tu = current_tuning();
     for (uint64_t round = 0;; round++) {
-        if (round >= max_rounds) return fail(SW_ERR_TIMEOUT, "walk did not finish");
+        if (round >= max_rounds) {          // every round was waited for: nothing in flight
+            return fail(SW_ERR_TIMEOUT, "walk did not finish");
+        }
         NA_CUDA(cudaMemsetAsync(L.active, 0, sizeof(uint32_t), st));
         NA_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
         if (tu.resort_interval && round % tu.resort_interval == 0)

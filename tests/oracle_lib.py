@@ -15,10 +15,12 @@ from spinwalk_gb300 import abi
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_PATH = os.path.join(ROOT, "oracle", "liboracle.so")
+SYNTH_PATH = os.path.join(ROOT, "oracle", "libsynth.so")
 REF_PATH = os.path.join(ROOT, "oracle", "_ref", "libref_sim.so")
 REF_NVCC_PATH = os.path.join(ROOT, "oracle", "_ref", "libref_sim_nvcc.so")
 
 _ora = None
+_synth = None
 _ref = None
 _ref_nvcc = None
 
@@ -43,6 +45,21 @@ def oracle():
         L.oracle_ms_normal.restype = None
         _ora = L
     return _ora
+
+
+def synth():
+    """oracle/libsynth.so: the synthetic phantom generator built alone (no CUDA library), so that
+    the benchmark's CPU reference arm makes the same phantoms without loading the GPU library."""
+    global _synth
+    if _synth is None:
+        if not os.path.exists(SYNTH_PATH):
+            from spinwalk_gb300 import _build
+            _build.build_oracle()
+        from spinwalk_gb300 import _lib
+        L = C.CDLL(SYNTH_PATH)
+        _lib.set_phantom_argtypes(L)
+        _synth = L
+    return _synth
 
 
 def ref_available():

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from spinwalk_gb300 import _lib
-from tests.helpers import bits_equal, load_golden, m_close
+from tests.helpers import bits_equal, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -58,8 +58,8 @@ def test_noalloc_matches_device_entry_point_twice(case):
         assert bits_equal(got["XYZ1"], want["XYZ1"]), (case, call)
         assert bits_equal(got["T"], want["T"]), (case, call)
         assert np.array_equal(got["status"], want["status"]), (case, call)
-        ok, rel = m_close(got["M1"], want["M1"])
-        assert ok, (case, call, rel)
+        # same kernels, same inputs: the magnetisation is bit-identical too
+        assert bits_equal(got["M1"], want["M1"]), (case, call)
         if call == 1:     # after set-up, a call allocates no device memory at all
             assert free_after == free_before, (free_before, free_after)
 

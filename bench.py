@@ -254,11 +254,15 @@ def precision_errors(pr, rng=0):
 
 
 def max_errors(problems, rng=0):
-    """FP32 error against FP64 over several problems (the worst of each figure)."""
+    """FP32 and compensated-FP32 (Kahan) errors against FP64 over several problems (the worst of
+    each figure)."""
     from spinwalk_gb300 import abi
-    errs = [fp64_error(p, abi.SW_PREC_FP32, rng) for p in problems]
-    return {"max_abs_per_spin": max(e["max_abs_per_spin"] for e in errs),
-            "signal_rel": max(e["signal_rel"] for e in errs)}
+    out = {}
+    for name, prec in (("fp32", abi.SW_PREC_FP32), ("kahan", abi.SW_PREC_KAHAN)):
+        errs = [fp64_error(p, prec, rng) for p in problems]
+        out[name] = {"max_abs_per_spin": max(e["max_abs_per_spin"] for e in errs),
+                     "signal_rel": max(e["signal_rel"] for e in errs)}
+    return out
 
 
 def bf16_field_errors(pr):
@@ -379,12 +383,14 @@ def apply_tuning(args, pr=None):
         best, table = _lib.autotune(pr, apply=True)
         info = {"autotuned": True, "probe_s": time.perf_counter() - t0, "table": table}
     if args.resort_interval is not None or args.walk_block is not None or \
-            args.seed_chunks is not None or args.round_streams is not None:
+            args.seed_chunks is not None or args.round_streams is not None or \
+            args.jump_min_kwords is not None:
         cur = _lib.get_tuning()
         _lib.set_tuning(cur["resort_interval"] if args.resort_interval is None else args.resort_interval,
                         cur["walk_block"] if args.walk_block is None else args.walk_block,
                         cur["seed_chunks"] if args.seed_chunks is None else args.seed_chunks,
-                        cur["round_streams"] if args.round_streams is None else args.round_streams)
+                        cur["round_streams"] if args.round_streams is None else args.round_streams,
+                        cur["jump_min_kwords"] if args.jump_min_kwords is None else args.jump_min_kwords)
     info["applied"] = _lib.get_tuning()
     return info
 
@@ -541,8 +547,8 @@ def leg_batched(args, rank=0, world=1):
         plain_ms += _lib.last_timing()["total_ms"]
     value = world * steps / (np.mean(dev_ms) * 1e-3)
     plain = steps / (plain_ms * 1e-3)
-    # FP32 error against FP64 on the smallest, two middle and the largest radius, GRE and SE
-    # (a batch instance is bit-identical to its own sw_sim run)
+    # error against FP64 on the smallest, a middle and the largest radius, GRE and SE, and the
+    # largest instance (a batch instance is bit-identical to its own sw_sim run)
     err_idx = sorted({0, 1, 30, 31, 62, 63} | {int(np.argmax([p.params.n_spins for p in probs]))})
     return {"workload": desc["workload"], "value": value, "unit": UNIT,
             "ms_per_step": float(np.mean(dev_ms)), "steps": reps,
@@ -554,7 +560,7 @@ def leg_batched(args, rank=0, world=1):
                     "note": "sw_sim_batch with host buffers"},
             "gpu_launches": int(sum(launches)),
             "error_vs_fp64": dict(max_errors([probs[i] for i in err_idx], rng_flag(args)),
-                                  precision="fp32", instances=err_idx),
+                                  instances=err_idx, timed_precision="fp32"),
             "tuning": tuning}
 
 
@@ -746,7 +752,7 @@ def leg_served(args, rank=0, world=1):
         warm_s, warm_lat, warm_st = play_trace(eng, reqs, arrivals, submit)
     clocks = clk.summary()
     eng.close()
-    # FP32 error against FP64 on the smallest request of each kind (a served request is
+    # error against FP64 on the smallest request of each kind (a served request is
     # bit-identical to its own sw_sim run)
     sample = []
     for k in range(5):
@@ -774,7 +780,7 @@ def leg_served(args, rank=0, world=1):
             "gpu_launches": int(warm_st["launches"]), "walk_rounds": int(warm_st["rounds"]),
             "seedings_warm": int(warm_st["seedings"]),
             "error_vs_fp64": dict(max_errors([reqs[i] for i in sample], rng_flag(args)),
-                                  precision="fp32", requests=sample),
+                                  requests=sample, timed_precision="fp32"),
             "tuning": tuning, "clocks": clocks}
 
 
@@ -962,7 +968,7 @@ def run_dwi(args, world, rank):
            "one_walk_per_scale": {"value": batch, "ms": float(np.mean(b_ms))},
            "shared_over_separate": value / batch,
            "error_vs_fp64": dict(max_errors([insts[0], insts[-1]], rng_flag(args)),
-                                 precision="fp32", scales=[scales[0], scales[-1]]),
+                                 scales=[scales[0], scales[-1]], timed_precision="fp32"),
            "clocks": clocks}
     print_leg(args, world, rank, leg)
 
@@ -1022,6 +1028,8 @@ def main():
                     help="refill/walk rounds as this many independent halves on own streams (1, 2)")
     ap.add_argument("--seed-chunks", type=int, default=None,
                     help="seed/walk pipeline chunks (1 = seed all first, 0 = auto)")
+    ap.add_argument("--jump-min-kwords", type=int, default=None,
+                    help="seeding jumps ahead from this discard count (x 1024 words; 0 = default)")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

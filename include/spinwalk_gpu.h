@@ -332,13 +332,19 @@ int sw_last_timing(sw_timing *out);
  *                     many independent halves on their own streams (1 = one, 2 = two, 0 = auto:
  *                     two from 2^17 spins on), so that one half's walk overlaps the other
  *                     half's refill
+ *   jump_min_kwords : seeding: spins whose discard count seed + spin reaches this many times
+ *                     1024 words compute their state by jump-ahead (a polynomial over GF(2),
+ *                     work independent of the count) instead of generating seed + spin words;
+ *                     0 = default (1024, i.e. 2^20 words). No reference counterpart (the
+ *                     reference discards word by word, src/sim/kernels.cu:87-88).
  */
 typedef struct sw_tuning {
     uint32_t resort_interval;
     uint32_t walk_block;
     uint32_t seed_chunks;
     uint32_t round_streams;
-    uint32_t reserved[4];
+    uint32_t jump_min_kwords;
+    uint32_t reserved[3];
 } sw_tuning;
 int sw_set_tuning(const sw_tuning *t);
 int sw_get_tuning(sw_tuning *t);
@@ -501,6 +507,12 @@ int sw_debug_dadd(const double *d_a, const double *d_b, double *d_y, uint64_t n,
  * nearest even) by the integer conversion the walk uses, on n device doubles -- used by the
  * tests. */
 int sw_debug_d2f(const double *d_x, float *d_y, uint64_t n, void *stream);
+
+/* Host-side check of the jump-ahead seeding (no GPU needed): the state of std::mt19937(z) after
+ * discard(z) -- its 624-word buffer and next position -- computed through the jump polynomial
+ * that the seeding kernel uses for discard counts of at least 2^20. No reference counterpart (the
+ * reference discards word by word, src/sim/kernels.cu:87-88) -- used by the tests. */
+int sw_debug_mt_jump(uint64_t z, uint32_t *block, uint32_t *pos);
 
 #ifdef __cplusplus
 }

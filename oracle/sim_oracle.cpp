@@ -23,6 +23,7 @@
 #include <cstdint>
 #include <cstring>
 #include <random>
+#include <sstream>
 #include <omp.h>
 
 #include "spinwalk_gpu.h"
@@ -379,6 +380,18 @@ int oracle_initial_positions(const float fov[3], uint64_t seed, uint32_t n_spins
         XYZ0[3 * i + 2] = dz(gen);
     }
     return 0;
+}
+
+// The state of std::mt19937(z) after discard(z), as kernels.cu:82-88 leaves each generator: the
+// engine's 624-word buffer and position, read back through its stream output (libstdc++ writes
+// the buffer then the position). Tests check the library's jump-ahead against it.
+void oracle_mt_discard(uint64_t z, uint32_t *block, uint32_t *pos) {
+    std::mt19937 gen((uint32_t)z);
+    gen.discard(z);
+    std::stringstream ss;
+    ss << gen;
+    for (int i = 0; i < 624; i++) ss >> block[i];
+    ss >> *pos;
 }
 
 // glibc logf over a float array (the host libm the reference links): used by tests to check

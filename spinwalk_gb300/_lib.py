@@ -93,6 +93,7 @@ def lib():
         L.sw_debug_ms_normal.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
         L.sw_debug_dadd.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
         L.sw_debug_d2f.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
+        L.sw_debug_mt_jump.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p]
         if L.sw_abi_version() != 1:
             raise SpinWalkError("libspinwalk_gpu ABI version mismatch")
         _lib = L
@@ -224,12 +225,15 @@ def run_config(ini_path, device=0):
     check(lib().sw_run_config(str(ini_path).encode(), int(device)))
 
 
-def set_tuning(resort_interval=0, walk_block=256, seed_chunks=0, round_streams=0):
-    """sw_set_tuning: Morton re-sort interval (walk rounds, 0 = never), walk block size and seed
-    chunks of the seed/walk pipeline (0 = auto) for every later call of this process. Results do
-    not depend on it."""
+def set_tuning(resort_interval=0, walk_block=256, seed_chunks=0, round_streams=0,
+               jump_min_kwords=0):
+    """sw_set_tuning: Morton re-sort interval (walk rounds, 0 = never), walk block size, seed
+    chunks of the seed/walk pipeline (0 = auto), round halves (0 = auto) and the discard count
+    from which seeding jumps ahead (in 1024 words, 0 = default 2^20 words) for every later call
+    of this process. Results do not depend on it."""
     t = abi.SwTuning(resort_interval=int(resort_interval), walk_block=int(walk_block),
-                     seed_chunks=int(seed_chunks), round_streams=int(round_streams))
+                     seed_chunks=int(seed_chunks), round_streams=int(round_streams),
+                     jump_min_kwords=int(jump_min_kwords))
     check(lib().sw_set_tuning(C.byref(t)))
 
 
@@ -237,7 +241,8 @@ def get_tuning():
     t = abi.SwTuning()
     check(lib().sw_get_tuning(C.byref(t)))
     return dict(resort_interval=t.resort_interval, walk_block=t.walk_block,
-                seed_chunks=t.seed_chunks, round_streams=t.round_streams)
+                seed_chunks=t.seed_chunks, round_streams=t.round_streams,
+                jump_min_kwords=t.jump_min_kwords)
 
 
 def autotune(problem, apply=False):
@@ -253,7 +258,8 @@ def autotune(problem, apply=False):
     table = [dict(resort_interval=e.resort_interval, walk_block=e.walk_block,
                   ms_per_round=e.ms_per_round, sort_ms=e.sort_ms) for e in tab[:n.value]]
     return dict(resort_interval=best.resort_interval, walk_block=best.walk_block,
-                seed_chunks=best.seed_chunks, round_streams=best.round_streams), table
+                seed_chunks=best.seed_chunks, round_streams=best.round_streams,
+                jump_min_kwords=best.jump_min_kwords), table
 
 
 def last_timing():
@@ -503,3 +509,12 @@ def debug_ms_normal(x_lo, n, d_y, stream=None):
 
 def debug_logf(d_x, d_y, n, stream=None):
     check(lib().sw_debug_logf(d_x, d_y, C.c_uint64(n), stream))
+
+
+def debug_mt_jump(z):
+    """sw_debug_mt_jump: (624-word buffer, position) of mt19937(z) after discard(z), computed on
+    the host through the jump polynomial."""
+    block = np.zeros(624, np.uint32)
+    pos = np.zeros(1, np.uint32)
+    check(lib().sw_debug_mt_jump(C.c_uint64(int(z)), _p(block), _p(pos)))
+    return block, int(pos[0])

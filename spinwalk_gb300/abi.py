@@ -130,7 +130,8 @@ class SwTuning(C.Structure):
         ("walk_block", C.c_uint32),
         ("seed_chunks", C.c_uint32),
         ("round_streams", C.c_uint32),
-        ("reserved", C.c_uint32 * 4),
+        ("jump_min_kwords", C.c_uint32),
+        ("reserved", C.c_uint32 * 3),
     ]
 
 

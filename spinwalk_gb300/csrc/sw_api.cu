@@ -17,6 +17,7 @@
 #include "spinwalk_gpu.h"
 #include "sw_host.h"
 #include "sw_kernels.h"
+#include "sw_mtjump.h"
 #include "sw_api_internal.h"
 
 namespace sw {
@@ -215,6 +216,8 @@ struct DeviceCtx {
     cudaStream_t walk_st = nullptr;        // highest priority: pack, init, refill, walk
     cudaStream_t walk_st2 = nullptr;       // highest priority: the second half's rounds
     std::vector<cudaEvent_t> pev;          // pipeline: start, done, seed chunk c done / timed
+    uint32_t *d_jump = nullptr;            // jump polynomials of the call's high spin ids
+    size_t jump_words = 0;
 };
 DeviceCtx g_ctx[kMaxDevices];
 
@@ -319,10 +322,18 @@ int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
         launches += 2;
         return SW_OK;
     };
+    // high spin ids jump ahead instead of discarding (the previous call has finished with the
+    // table: every call waits for its work before it returns)
+    sw::JumpTable jt;
+    if (P.rng == SW_RNG_MT19937) {
+        const int rj = jump_table(P.seed, 0, P.n_spins, jump_min_z(tu), ctx.d_jump,
+                                  ctx.jump_words, jt);
+        if (rj) return rj;
+    }
     // seeding of every chunk, each chunk bracketed by events (start, done)
     for (uint32_t c = 0; c < C; c++) {
         SW_CUDA(cudaEventRecord(ctx.pev[4 + 2 * c], ss));
-        SW_CUDA(sw::launch_seed_range(P, L.G, b[c], b[c + 1], ss));
+        SW_CUDA(sw::launch_seed_range(P, L.G, b[c], b[c + 1], ss, &jt));
         SW_CUDA(cudaEventRecord(ctx.pev[5 + 2 * c], ss));
         launches++;
     }
@@ -488,8 +499,44 @@ sw::LogfTables sw::api::device_logf_tables() {
 
 namespace {
 std::mutex g_tune_mu;
-sw_tuning g_tune{0u, 256u, 0u, 0u, {0u, 0u, 0u, 0u}};
+sw_tuning g_tune{0u, 256u, 0u, 0u, 0u, {0u, 0u, 0u}};
 }  // namespace
+
+int sw::api::jump_table(uint64_t seed, uint32_t lo, uint32_t hi, uint64_t z_min, uint32_t *&buf,
+                        size_t &buf_words, sw::JumpTable &jt) {
+    jt = sw::JumpTable{};
+    const uint64_t c = std::max<uint64_t>(lo, seed >= z_min ? 0 : z_min - seed);
+    if (c >= hi) return SW_OK;                      // every spin discards
+    const uint64_t R_lo = sw::mt_regenerations(seed + c), R_hi = sw::mt_regenerations(seed + hi - 1) + 1;
+    const size_t words = (size_t)(R_hi - R_lo) * sw::kJumpPolyWords;
+    std::vector<uint32_t> host(words);
+    try {
+        sw::mt_jump_polys(R_lo, (uint32_t)(R_hi - R_lo), host.data());
+    } catch (const std::exception &e) {
+        return fail(SW_ERR_INVALID, std::string("jump polynomials: ") + e.what());
+    }
+    if (words > buf_words) {
+        if (buf) cudaFree(buf);
+        buf = nullptr;
+        buf_words = 0;
+        cudaError_t e = cudaMalloc(&buf, words * 4);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SW_ERR_NOMEM, std::string("jump polynomials: ") + cudaGetErrorString(e));
+        }
+        buf_words = words;
+    }
+    cudaError_t e = cudaMemcpy(buf, host.data(), words * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SW_ERR_CUDA, std::string("jump polynomials: ") + cudaGetErrorString(e));
+    }
+    jt.polys = buf;
+    jt.R_lo = R_lo;
+    jt.R_hi = R_hi;
+    jt.z_min = z_min;
+    return SW_OK;
+}
 
 sw_tuning sw::api::current_tuning() {
     std::lock_guard<std::mutex> lk(g_tune_mu);

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "spinwalk_gpu.h"
+#include "sw_kernels.h"
 #include "sw_types.h"
 
 namespace sw {
@@ -62,6 +63,16 @@ struct Layout {
 
 // Process-wide tuning of the walk (sw_set_tuning / sw_autotune), read at the start of a call.
 sw_tuning current_tuning();
+// The discard count from which seeding jumps ahead under tuning t (at least 624).
+inline uint64_t jump_min_z(const sw_tuning &t) {
+    const uint64_t z = t.jump_min_kwords ? 1024ull * t.jump_min_kwords : kJumpMinZ;
+    return z < 624 ? 624 : z;
+}
+// Device jump polynomials (sw_mtjump.h) for the spins [lo, hi) of `seed` whose discard count
+// seed + spin reaches z_min, computed on the host and copied into buf (grown on demand; the
+// caller makes sure no kernel still reads it). jt.polys stays null when no spin jumps.
+int jump_table(uint64_t seed, uint32_t lo, uint32_t hi, uint64_t z_min, uint32_t *&buf,
+               size_t &buf_words, JumpTable &jt);
 
 // Kernel timing of the last call on this thread (sw_last_timing).
 extern thread_local sw_timing g_timing;

@@ -152,6 +152,8 @@ struct sw_engine {
     uint64_t budget = 0, used = 0;
     cudaStream_t seed_st = nullptr;
     uint32_t *seed_scratch = nullptr;        // ring counters written by k_seed, not needed here
+    uint32_t *d_jump = nullptr;              // jump polynomials of the last seeding's high spin ids
+    size_t jump_words = 0;
     uint32_t scratch_cap = 0;
     std::vector<Slot> slots;
     std::map<int32_t, Phantom> phantoms;
@@ -185,7 +187,14 @@ int seed_into(sw_engine *E, SeedCache &C, uint64_t seed, uint32_t a, uint32_t b)
     G.mt_r = G.mt_u = shift(C.mt, (uint64_t)C.base * sw::kMtN);
     G.p_r = G.p_u = shift(C.p, (uint64_t)C.base);
     G.nhead = G.ncnt = G.uhead = G.ucnt = shift(E->seed_scratch, (uint64_t)C.base);
-    EN_CUDA(sw::launch_seed_range(P, G, a, b, E->seed_st));
+    sw::JumpTable jt;                    // high spin ids jump ahead instead of discarding
+    const uint64_t zmin = jump_min_z(current_tuning());
+    if (P.rng == SW_RNG_MT19937 && (uint64_t)seed + b > zmin) {
+        EN_CUDA(cudaStreamSynchronize(E->seed_st));     // the last seeding may still read it
+        const int rj = jump_table(seed, a, b, zmin, E->d_jump, E->jump_words, jt);
+        if (rj) return rj;
+    }
+    EN_CUDA(sw::launch_seed_range(P, G, a, b, E->seed_st, &jt));
     E->launches++;
     E->seedings++;
     return SW_OK;
@@ -600,6 +609,7 @@ void engine_free(sw_engine *E) {
     for (auto &j : E->queue)
         if (j->h_tables) cudaFreeHost(j->h_tables);
     if (E->seed_scratch) cudaFree(E->seed_scratch);
+    if (E->d_jump) cudaFree(E->d_jump);
     if (E->seed_st) cudaStreamDestroy(E->seed_st);
     delete E;
 }

@@ -17,6 +17,8 @@
 // k_refill and k_walk alternate until every spin has finished. All kernels are compiled with
 // -fmad=false (see sw_device.cuh).
 #include <cuda_bf16.h>
+
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include "sw_device.cuh"
@@ -113,6 +115,121 @@ __global__ void __launch_bounds__(32 * kSeedWarps)
 }
 
 // ------------------------------------------------------------------------------------------
+// Seeding by jump-ahead (sw_mtjump.h): the same state as k_seed for spins whose discard count
+// z = seed + spin is large, in work independent of z. With J = 624 R - 1 (R regenerations of
+// discard(z)) and g = x^J mod phi (host-computed, one per R), the state after J words is
+// h_j = XOR over k with g_k = 1 of x[k + j], j < 624, over the spin's own output sequence x.
+// One warp per spin: lane l accumulates h_j for the 21 words j = 21 l + i in registers; x lives
+// in a 1024-word ring in shared memory, generated 32 words at a time ahead of use. Each lane
+// slides a window of 42 registers (the current and the next block of 21 sequence words) along
+// x, so a step k reads one new word per lane instead of 21; the XOR of a window is a uniform
+// branch on g_k. The block of regeneration R is then h_1 .. h_623 plus one more word.
+// ------------------------------------------------------------------------------------------
+constexpr int kJumpWarps = 4;
+constexpr uint32_t kJumpRing = 1024;      // sequence words per warp in shared memory
+constexpr int kJumpPer = 21;              // state words per lane: 32 x 21 = 672 >= 624
+constexpr uint32_t kJumpAhead = kJumpPer + kJumpPer * 31 + kJumpPer;   // sequence needed past k0
+
+// Bits k0 .. k0 + 20 of the jump polynomial (624 words; bits past 19936 are zero).
+__device__ __forceinline__ uint32_t jump_bits(const uint32_t *__restrict__ g, uint32_t k0) {
+    const uint32_t q = k0 >> 5, r = k0 & 31u;
+    uint64_t v = __ldg(g + q);
+    if (q + 1 < (uint32_t)kMtN) v |= (uint64_t)__ldg(g + q + 1) << 32;
+    return (uint32_t)(v >> r) & ((1u << kJumpPer) - 1u);
+}
+
+// Steps k0 .. k0 + 20: cur holds x[k0 + 21 lane + m], nxt is loaded with the next block
+// x[k0 + 21 + 21 lane + m]; window element i of step t is cur[t + i] or nxt[t + i - 21].
+__device__ __forceinline__ void jump_block(uint32_t (&h)[kJumpPer], const uint32_t (&cur)[kJumpPer],
+                                           uint32_t (&nxt)[kJumpPer], const uint32_t *xs,
+                                           uint32_t k0, int lane, uint32_t gb) {
+#pragma unroll
+    for (int m = 0; m < kJumpPer; m++)
+        nxt[m] = xs[(k0 + kJumpPer + kJumpPer * lane + m) & (kJumpRing - 1u)];
+#pragma unroll
+    for (int t = 0; t < kJumpPer; t++) {
+        if ((gb >> t) & 1u) {
+#pragma unroll
+            for (int i = 0; i < kJumpPer; i++)
+                h[i] ^= (t + i < kJumpPer) ? cur[t + i] : nxt[t + i - kJumpPer];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(32 * kJumpWarps, 6)
+    k_seed_jump(DevParams P, RngState G, const uint32_t *__restrict__ polys, uint64_t R_lo,
+                uint32_t spin_lo, uint32_t spin_hi) {
+    __shared__ uint32_t s_x[kJumpWarps][kJumpRing];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t *xs = s_x[w];
+    constexpr uint32_t M = kJumpRing - 1u;
+    for (uint32_t spin = spin_lo + blockIdx.x * kJumpWarps + w; spin < spin_hi;
+         spin += gridDim.x * kJumpWarps) {
+        const uint64_t sd = P.seed + spin;
+        const uint32_t R = mt_discard_twists(sd);
+        const uint32_t *g = polys + (size_t)(R - R_lo) * kMtN;
+        if (lane == 0) {                             // mersenne_twister_engine::seed
+            uint32_t x = (uint32_t)sd;
+            xs[0] = x;
+            for (uint32_t i = 1; i < kMtN; i++) {
+                x = 1812433253u * (x ^ (x >> 30)) + i;
+                xs[i] = x;
+            }
+        }
+        __syncwarp();
+        uint32_t gen = kMtN;                         // x[0 .. gen) are in the ring
+        auto generate_to = [&](uint32_t upto) {
+            while (gen < upto) {
+                const uint32_t n = gen + lane;
+                const uint32_t v = mt_twist1(xs[(n - 624u) & M], xs[(n - 623u) & M], xs[(n - 227u) & M]);
+                __syncwarp();
+                xs[n & M] = v;
+                __syncwarp();
+                gen += 32;
+            }
+        };
+        uint32_t h[kJumpPer], A[kJumpPer], B[kJumpPer];
+        generate_to(kJumpPer * 32);
+#pragma unroll
+        for (int i = 0; i < kJumpPer; i++) {
+            h[i] = 0;
+            A[i] = xs[(kJumpPer * lane + i) & M];
+        }
+        for (uint32_t k0 = 0; k0 < (uint32_t)kMtDegreeDev; k0 += 2 * kJumpPer) {
+            generate_to(k0 + kJumpAhead);
+            jump_block(h, A, B, xs, k0, lane, jump_bits(g, k0));
+            generate_to(k0 + kJumpPer + kJumpAhead);
+            jump_block(h, B, A, xs, k0 + kJumpPer, lane, jump_bits(g, k0 + kJumpPer));
+        }
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < kJumpPer; i++)
+            if (kJumpPer * lane + i < kMtN) xs[kJumpPer * lane + i] = h[i];
+        __syncwarp();
+        // block of regeneration R: x[624 R + q] = h_(q+1), q < 623, and one more twist word
+        uint32_t *gr = G.mt_r + (size_t)spin * kMtN, *gu = G.mt_u + (size_t)spin * kMtN;
+        for (int q = lane; q < kMtN - 1; q += 32) {
+            const uint32_t v = xs[q + 1];
+            gr[q] = v;
+            gu[q] = v;
+        }
+        if (lane == 0) {
+            const uint32_t v = mt_twist1(xs[0], xs[1], xs[397]);
+            gr[kMtN - 1] = v;
+            gu[kMtN - 1] = v;
+            const uint32_t p = (uint32_t)(sd - (uint64_t)kMtN * (R - 1));
+            G.p_r[spin] = p;
+            G.p_u[spin] = p;
+            G.nhead[spin] = 0;
+            G.ncnt[spin] = 0;
+            G.uhead[spin] = 0;
+            G.ucnt[spin] = 0;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------------------------
 // Generator flavour of the reference's CUDA build (kernels.cu:76-80): thrust::minstd_rand,
 // x <- 48271 x mod (2^31 - 1), one 31-bit state per generator (kept in p_r / p_u).
 // ------------------------------------------------------------------------------------------
@@ -173,46 +290,52 @@ __device__ __forceinline__ float ms_uniform(uint32_t x) {
     return __fadd_rn(__fmul_rn(r, 1.0f), 0.0f);
 }
 
-// One warp per spin: lane l takes the (l+1)-th next engine output, 32 per pass.
+// One warp per spin: lane l takes the (l+1)-th next engine output, 32 per pass. Tops up the
+// spin's Gaussian ring (and its uniform ring when at most half full).
+__device__ __forceinline__ void refill_spin_minstd(uint32_t spin, const RngState &G,
+                                                   const uint32_t *__restrict__ ms_delta,
+                                                   int lane) {
+    const uint32_t nc = G.ncnt[spin], nh = G.nhead[spin], uc = G.ucnt[spin];
+    if (nc < kNormBuf) {
+        uint32_t x = G.p_r[spin];
+        float *nb = G.nbuf + (size_t)spin * kNormBuf;
+        const uint32_t K = kNormBuf - nc, wpos = nh + nc;
+        for (uint32_t b = 0; b < K; b += 32) {
+            const uint32_t r = min(32u, K - b);
+            if ((uint32_t)lane < r)
+                nb[(wpos + b + lane) % kNormBuf] =
+                    ms_normal(ms_mulmod(x, c_ms_pow.v[lane]), ms_delta);
+            x = ms_mulmod(x, c_ms_pow.v[r - 1]);
+        }
+        if (lane == 0) {
+            G.p_r[spin] = x;
+            G.ncnt[spin] = kNormBuf;
+        }
+    }
+    if (uc <= kUnifBuf / 2) {
+        uint32_t x = G.p_u[spin];
+        float *ub = G.ubuf + (size_t)spin * kUnifBuf;
+        const uint32_t K = kUnifBuf - uc, wpos = G.uhead[spin] + uc;
+        for (uint32_t b = 0; b < K; b += 32) {
+            const uint32_t r = min(32u, K - b);
+            if ((uint32_t)lane < r)
+                ub[(wpos + b + lane) % kUnifBuf] = ms_uniform(ms_mulmod(x, c_ms_pow.v[lane]));
+            x = ms_mulmod(x, c_ms_pow.v[r - 1]);
+        }
+        if (lane == 0) {
+            G.p_u[spin] = x;
+            G.ucnt[spin] = kUnifBuf;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128)
     k_refill_minstd(DevParams P, RngState G, const uint32_t *__restrict__ flags,
                     const uint32_t *__restrict__ ms_delta, uint32_t spin_lo, uint32_t spin_hi) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (uint32_t spin = spin_lo + blockIdx.x * 4 + w; spin < spin_hi; spin += gridDim.x * 4) {
-        const uint32_t fl = flags[spin], nc = G.ncnt[spin], nh = G.nhead[spin],
-                       uc = G.ucnt[spin];
-        if (fl & kFlagDone) continue;
-        if (nc < kNormBuf) {
-            uint32_t x = G.p_r[spin];
-            float *nb = G.nbuf + (size_t)spin * kNormBuf;
-            const uint32_t K = kNormBuf - nc, wpos = nh + nc;
-            for (uint32_t b = 0; b < K; b += 32) {
-                const uint32_t r = min(32u, K - b);
-                if ((uint32_t)lane < r)
-                    nb[(wpos + b + lane) % kNormBuf] =
-                        ms_normal(ms_mulmod(x, c_ms_pow.v[lane]), ms_delta);
-                x = ms_mulmod(x, c_ms_pow.v[r - 1]);
-            }
-            if (lane == 0) {
-                G.p_r[spin] = x;
-                G.ncnt[spin] = kNormBuf;
-            }
-        }
-        if (uc <= kUnifBuf / 2) {
-            uint32_t x = G.p_u[spin];
-            float *ub = G.ubuf + (size_t)spin * kUnifBuf;
-            const uint32_t K = kUnifBuf - uc, wpos = G.uhead[spin] + uc;
-            for (uint32_t b = 0; b < K; b += 32) {
-                const uint32_t r = min(32u, K - b);
-                if ((uint32_t)lane < r)
-                    ub[(wpos + b + lane) % kUnifBuf] = ms_uniform(ms_mulmod(x, c_ms_pow.v[lane]));
-                x = ms_mulmod(x, c_ms_pow.v[r - 1]);
-            }
-            if (lane == 0) {
-                G.p_u[spin] = x;
-                G.ucnt[spin] = kUnifBuf;
-            }
-        }
+        if (flags[spin] & kFlagDone) continue;
+        refill_spin_minstd(spin, G, ms_delta, lane);
         __syncwarp();
     }
 }
@@ -295,6 +418,107 @@ __device__ __forceinline__ uint32_t block_word(const uint32_t *gst, const uint32
     return in_smem ? s[i] : gst[i];
 }
 
+// One warp tops up the rings of one spin from its mt19937 states: Gaussian deviates from gen_r
+// (normal_distribution<float>, polar method, 32 candidate pairs per pass) and, when at most half
+// full, crossing uniforms from gen_u. `s` is the warp's 624-word shared block.
+__device__ __forceinline__ void refill_spin_mt(uint32_t spin, const RngState &G,
+                                               const LogfTables &L, const float *s_tab,
+                                               uint32_t *s, int lane) {
+    const unsigned lt_mask = (1u << lane) - 1u;
+    // ---- Gaussian deviates from gen_r (normal_distribution<float>, polar method) ----
+    const uint32_t nc = G.ncnt[spin];
+    const uint32_t K = (kNormBuf - nc) / 2;                 // pairs to add
+    if (K > 0) {
+        uint32_t *gst = G.mt_r + (size_t)spin * kMtN;
+        float *nb = G.nbuf + (size_t)spin * kNormBuf;
+        const uint32_t wpos = G.nhead[spin] + nc;
+        uint32_t p = G.p_r[spin];
+        uint32_t produced = 0;
+        bool in_smem = false;
+        while (produced < K) {
+            if (p >= (uint32_t)kMtN) {
+                twist_block(gst, s, in_smem, lane);
+                p = 0;
+            }
+            uint32_t w0 = 0, w1 = 0;
+            uint32_t npairs;
+            bool straddle = false;
+            if (kMtN - p == 1) {            // pair = last word of this block + first of next
+                w0 = block_word(gst, s, in_smem, kMtN - 1);
+                twist_block(gst, s, in_smem, lane);
+                w1 = s[0];
+                npairs = 1;
+                straddle = true;
+            } else {
+                npairs = min(32u, (kMtN - p) / 2);
+                if ((uint32_t)lane < npairs) {
+                    w0 = block_word(gst, s, in_smem, p + 2 * lane);
+                    w1 = block_word(gst, s, in_smem, p + 2 * lane + 1);
+                }
+            }
+            const bool valid = (uint32_t)lane < npairs;
+            const float u1 = canon24(mt_temper(w0)), u2 = canon24(mt_temper(w1));
+            const float x = 2.0f * u1 - 1.0f, y = 2.0f * u2 - 1.0f;
+            const float r2 = x * x + y * y;
+            const bool ok = valid && !(r2 > 1.0f || r2 == 0.0f);
+            const unsigned bal = __ballot_sync(0xffffffffu, ok);
+            const uint32_t rank = __popc(bal & lt_mask);
+            const uint32_t need = K - produced;
+            if (ok && rank < need) {
+                const float lg = logf_libm(r2, s_tab, L);
+                const float mult = __fsqrt_rn(__fdiv_rn(-2.0f * lg, r2));
+                uint32_t pos = wpos + 2 * (produced + rank);   // < 3 kNormBuf
+                pos -= pos >= kNormBuf ? kNormBuf : 0u;
+                pos -= pos >= kNormBuf ? kNormBuf : 0u;
+                nb[pos] = y * mult;                          // returned first
+                nb[pos + 1 == kNormBuf ? 0 : pos + 1] = x * mult;   // saved for the next call
+            }
+            const uint32_t nacc = __popc(bal);
+            if (nacc <= need) {
+                produced += nacc;
+                p = straddle ? 1 : p + 2 * npairs;
+            } else {
+                const unsigned m2 = __ballot_sync(0xffffffffu, ok && rank == need - 1);
+                const uint32_t last = __ffs(m2) - 1;
+                produced = K;
+                p = p + 2 * (last + 1);
+            }
+        }
+        if (lane == 0) {
+            G.p_r[spin] = p;
+            G.ncnt[spin] = nc + 2 * K;
+        }
+    }
+    // ---- crossing uniforms from gen_u (uniform_real_distribution<float>(0,1)) ----
+    const uint32_t uc = G.ucnt[spin];
+    if (uc <= kUnifBuf / 2) {
+        uint32_t *gst = G.mt_u + (size_t)spin * kMtN;
+        float *ub = G.ubuf + (size_t)spin * kUnifBuf;
+        const uint32_t wpos = G.uhead[spin] + uc;
+        const uint32_t need = kUnifBuf - uc;
+        uint32_t p = G.p_u[spin];
+        uint32_t produced = 0;
+        bool in_smem = false;
+        while (produced < need) {
+            if (p >= (uint32_t)kMtN) {
+                twist_block(gst, s, in_smem, lane);
+                p = 0;
+            }
+            const uint32_t n = min(min(32u, (uint32_t)kMtN - p), need - produced);
+            if ((uint32_t)lane < n) {
+                const uint32_t wv = block_word(gst, s, in_smem, p + lane);
+                ub[(wpos + produced + lane) % kUnifBuf] = canon24(mt_temper(wv));
+            }
+            p += n;
+            produced += n;
+        }
+        if (lane == 0) {
+            G.p_u[spin] = p;
+            G.ucnt[spin] = uc + need;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(32 * kRefillWarps)
     k_refill(DevParams P, RngState G, const uint32_t *__restrict__ flags, LogfTables L,
              uint32_t spin_lo, uint32_t spin_hi) {
@@ -303,103 +527,10 @@ __global__ void __launch_bounds__(32 * kRefillWarps)
     for (int i = threadIdx.x; i < 192; i += blockDim.x) s_tab[i] = L.tab[i];
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned lt_mask = (1u << lane) - 1u;
-    uint32_t *s = s_mt[w];
     for (uint32_t spin = spin_lo + blockIdx.x * kRefillWarps + w; spin < spin_hi;
          spin += gridDim.x * kRefillWarps) {
         if (flags[spin] & kFlagDone) continue;
-        // ---- Gaussian deviates from gen_r (normal_distribution<float>, polar method) ----
-        const uint32_t nc = G.ncnt[spin];
-        const uint32_t K = (kNormBuf - nc) / 2;                 // pairs to add
-        if (K > 0) {
-            uint32_t *gst = G.mt_r + (size_t)spin * kMtN;
-            float *nb = G.nbuf + (size_t)spin * kNormBuf;
-            const uint32_t wpos = G.nhead[spin] + nc;
-            uint32_t p = G.p_r[spin];
-            uint32_t produced = 0;
-            bool in_smem = false;
-            while (produced < K) {
-                if (p >= (uint32_t)kMtN) {
-                    twist_block(gst, s, in_smem, lane);
-                    p = 0;
-                }
-                uint32_t w0 = 0, w1 = 0;
-                uint32_t npairs;
-                bool straddle = false;
-                if (kMtN - p == 1) {            // pair = last word of this block + first of next
-                    w0 = block_word(gst, s, in_smem, kMtN - 1);
-                    twist_block(gst, s, in_smem, lane);
-                    w1 = s[0];
-                    npairs = 1;
-                    straddle = true;
-                } else {
-                    npairs = min(32u, (kMtN - p) / 2);
-                    if ((uint32_t)lane < npairs) {
-                        w0 = block_word(gst, s, in_smem, p + 2 * lane);
-                        w1 = block_word(gst, s, in_smem, p + 2 * lane + 1);
-                    }
-                }
-                const bool valid = (uint32_t)lane < npairs;
-                const float u1 = canon24(mt_temper(w0)), u2 = canon24(mt_temper(w1));
-                const float x = 2.0f * u1 - 1.0f, y = 2.0f * u2 - 1.0f;
-                const float r2 = x * x + y * y;
-                const bool ok = valid && !(r2 > 1.0f || r2 == 0.0f);
-                const unsigned bal = __ballot_sync(0xffffffffu, ok);
-                const uint32_t rank = __popc(bal & lt_mask);
-                const uint32_t need = K - produced;
-                if (ok && rank < need) {
-                    const float lg = logf_libm(r2, s_tab, L);
-                    const float mult = __fsqrt_rn(__fdiv_rn(-2.0f * lg, r2));
-                    uint32_t pos = wpos + 2 * (produced + rank);   // < 3 kNormBuf
-                    pos -= pos >= kNormBuf ? kNormBuf : 0u;
-                    pos -= pos >= kNormBuf ? kNormBuf : 0u;
-                    nb[pos] = y * mult;                          // returned first
-                    nb[pos + 1 == kNormBuf ? 0 : pos + 1] = x * mult;   // saved for the next call
-                }
-                const uint32_t nacc = __popc(bal);
-                if (nacc <= need) {
-                    produced += nacc;
-                    p = straddle ? 1 : p + 2 * npairs;
-                } else {
-                    const unsigned m2 = __ballot_sync(0xffffffffu, ok && rank == need - 1);
-                    const uint32_t last = __ffs(m2) - 1;
-                    produced = K;
-                    p = p + 2 * (last + 1);
-                }
-            }
-            if (lane == 0) {
-                G.p_r[spin] = p;
-                G.ncnt[spin] = nc + 2 * K;
-            }
-        }
-        // ---- crossing uniforms from gen_u (uniform_real_distribution<float>(0,1)) ----
-        const uint32_t uc = G.ucnt[spin];
-        if (uc <= kUnifBuf / 2) {
-            uint32_t *gst = G.mt_u + (size_t)spin * kMtN;
-            float *ub = G.ubuf + (size_t)spin * kUnifBuf;
-            const uint32_t wpos = G.uhead[spin] + uc;
-            const uint32_t need = kUnifBuf - uc;
-            uint32_t p = G.p_u[spin];
-            uint32_t produced = 0;
-            bool in_smem = false;
-            while (produced < need) {
-                if (p >= (uint32_t)kMtN) {
-                    twist_block(gst, s, in_smem, lane);
-                    p = 0;
-                }
-                const uint32_t n = min(min(32u, (uint32_t)kMtN - p), need - produced);
-                if ((uint32_t)lane < n) {
-                    const uint32_t wv = block_word(gst, s, in_smem, p + lane);
-                    ub[(wpos + produced + lane) % kUnifBuf] = canon24(mt_temper(wv));
-                }
-                p += n;
-                produced += n;
-            }
-            if (lane == 0) {
-                G.p_u[spin] = p;
-                G.ucnt[spin] = uc + need;
-            }
-        }
+        refill_spin_mt(spin, G, L, s_tab, s_mt[w], lane);
         __syncwarp();
     }
 }
@@ -734,14 +865,27 @@ cudaError_t launch_seed(const DevParams &P, const RngState &G, cudaStream_t st) 
 }
 
 cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo, uint32_t hi,
-                              cudaStream_t st) {
+                              cudaStream_t st, const JumpTable *jt) {
     if (hi <= lo) return cudaSuccess;
     if (P.rng == SW_RNG_MINSTD) {
         k_seed_minstd<<<grid_for(hi - lo, 256, 1 << 30), 256, 0, st>>>(P, G, lo, hi);
         return cudaGetLastError();
     }
-    k_seed<<<grid_for(((int64_t)hi - lo + 1) / 2, kSeedWarps, 1 << 30), 32 * kSeedWarps, 0, st>>>(
-        P, G, lo, hi);
+    // spins from c on jump (z = seed + spin >= z_min), the rest discard
+    uint32_t c = hi;
+    if (jt && jt->polys) {
+        if (jt->z_min < (uint64_t)kMtN) return cudaErrorInvalidValue;
+        c = (uint32_t)std::min<uint64_t>(hi, std::max<uint64_t>(lo, P.seed >= jt->z_min ? 0 : jt->z_min - P.seed));
+        if (c < hi && (mt_discard_twists(P.seed + c) < jt->R_lo ||
+                       mt_discard_twists(P.seed + hi - 1) >= jt->R_hi))
+            return cudaErrorInvalidValue;            // the table does not cover these spins
+    }
+    if (c > lo)
+        k_seed<<<grid_for(((int64_t)c - lo + 1) / 2, kSeedWarps, 1 << 30), 32 * kSeedWarps, 0, st>>>(
+            P, G, lo, c);
+    if (hi > c)
+        k_seed_jump<<<grid_for(hi - c, kJumpWarps, 152 * 6), 32 * kJumpWarps, 0, st>>>(
+            P, G, jt->polys, jt->R_lo, c, hi);
     return cudaGetLastError();
 }
 

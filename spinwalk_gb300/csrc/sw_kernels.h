@@ -11,8 +11,17 @@ cudaError_t launch_pack(const uint8_t *mask, const float *field, uint2 *out, int
                         uint32_t n_substrate, uint32_t *bad_label, cudaStream_t st,
                         bool bf16 = false);
 cudaError_t launch_seed(const DevParams &P, const RngState &G, cudaStream_t st);
+// Jump polynomials on the device (sw_mtjump.h): 624 words per regeneration count R in
+// [R_lo, R_hi), for the spins whose discard count seed + spin is at least z_min (>= 624).
+struct JumpTable {
+    const uint32_t *polys = nullptr;
+    uint64_t R_lo = 0, R_hi = 0;
+    uint64_t z_min = ~0ull;
+};
+// Spins with seed + spin >= jt->z_min are seeded by jump-ahead when jt is given (it must cover
+// their regeneration counts), the others by the plain discard.
 cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo, uint32_t hi,
-                              cudaStream_t st);
+                              cudaStream_t st, const JumpTable *jt = nullptr);
 cudaError_t launch_refill_range(const DevParams &P, const RngState &G, const uint32_t *flags,
                                 const LogfTables &L, uint32_t lo, uint32_t hi, cudaStream_t st);
 // order: walk order of the spins (null = id order); block: threads per block (64..256).

@@ -16,6 +16,11 @@ constexpr int kMtM = 397;
 constexpr uint32_t kNormBuf = 768;               // Gaussian deviates: 256 steps x 3 axes
 constexpr uint32_t kUnifBuf = 128;               // uniform deviates for crossing attempts
 constexpr uint32_t kStepsPerRound = kNormBuf / 3;  // longest walk of one refill/walk round
+// Seeding: by default, spins whose discard count seed + spin reaches this jump ahead
+// (k_seed_jump) instead of regenerating seed + spin words (k_seed); sw_tuning.jump_min_kwords
+// overrides it.
+constexpr uint64_t kJumpMinZ = 1ull << 20;
+constexpr int kMtDegreeDev = 19937;               // degree of mt19937's characteristic polynomial
 
 // Spin flags word: bits 0-7 ts_old (substrate of the last accepted voxel), bit 8 "scan
 // started", bit 9 done, bits 16-23 status (SW_SPIN_*).

@@ -43,6 +43,8 @@ def oracle():
         L.oracle_logf.restype = None
         L.oracle_ms_normal.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p]
         L.oracle_ms_normal.restype = None
+        L.oracle_mt_discard.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p]
+        L.oracle_mt_discard.restype = None
         _ora = L
     return _ora
 
@@ -149,3 +151,11 @@ def host_logf(x):
     y = np.empty_like(x)
     oracle().oracle_logf(_p(x), _p(y), x.size)
     return y
+
+
+def mt_discard(z):
+    """(624-word buffer, position) of std::mt19937(z) after discard(z) (libstdc++)."""
+    block = np.zeros(624, np.uint32)
+    pos = np.zeros(1, np.uint32)
+    oracle().oracle_mt_discard(C.c_uint64(int(z)), _p(block), _p(pos))
+    return block, int(pos[0])

@@ -161,7 +161,7 @@ def test_full_size_serving_trace():
     earlier ones run, with the serving benchmark's slots (8 x 2^20 spins, so the larger jobs run
     in chunks): each result equals the request run alone bit for bit, and sampled spins equal
     the oracle."""
-    reqs, phantoms, arrivals, desc = bench.serve_requests(40)
+    reqs, phantoms, arrivals, kinds, desc = bench.serve_requests(40)
     picked = [pr for pr in reqs if pr.params.n_spins <= 2_000_000][:12]
     assert len({pr.mask.shape for pr in picked}) > 1
     eng = _lib.Engine(n_slots=8, slot_spins=1 << 20)

@@ -17,8 +17,9 @@ def tuning():
 
 
 def test_tuning_roundtrip_and_validation(tuning):
-    tuning(3, 128, 5, 2)
-    want = dict(resort_interval=3, walk_block=128, seed_chunks=5, round_streams=2)
+    tuning(3, 128, 5, 2, 7)
+    want = dict(resort_interval=3, walk_block=128, seed_chunks=5, round_streams=2,
+                jump_min_kwords=7)
     assert _lib.get_tuning() == want
     for bad in (dict(resort_interval=1, walk_block=100), dict(resort_interval=1, walk_block=512),
                 dict(resort_interval=1 << 21, walk_block=256), dict(seed_chunks=65),
@@ -138,3 +139,4 @@ def test_sim_results_independent_of_round_streams(tuning, case, chunks):
     tuning(0, 256, chunks, 2)
     got = _lib.run(pr, fill=np.nan)
     _same(got, want)
+

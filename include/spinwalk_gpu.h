@@ -335,8 +335,9 @@ int sw_last_timing(sw_timing *out);
  *   jump_min_kwords : seeding: spins whose discard count seed + spin reaches this many times
  *                     1024 words compute their state by jump-ahead (a polynomial over GF(2),
  *                     work independent of the count) instead of generating seed + spin words;
- *                     0 = default (1024, i.e. 2^20 words). No reference counterpart (the
- *                     reference discards word by word, src/sim/kernels.cu:87-88).
+ *                     0 = default (2304, i.e. 2.36e6 words, where the two cost the same on
+ *                     GB300). No reference counterpart (the reference discards word by word,
+ *                     src/sim/kernels.cu:87-88).
  */
 typedef struct sw_tuning {
     uint32_t resort_interval;
@@ -510,7 +511,7 @@ int sw_debug_d2f(const double *d_x, float *d_y, uint64_t n, void *stream);
 
 /* Host-side check of the jump-ahead seeding (no GPU needed): the state of std::mt19937(z) after
  * discard(z) -- its 624-word buffer and next position -- computed through the jump polynomial
- * that the seeding kernel uses for discard counts of at least 2^20. No reference counterpart (the
+ * that the seeding kernel uses for large discard counts. No reference counterpart (the
  * reference discards word by word, src/sim/kernels.cu:87-88) -- used by the tests. */
 int sw_debug_mt_jump(uint64_t z, uint32_t *block, uint32_t *pos);
 

@@ -33,7 +33,8 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp", f"-I
              f"-I{CSRC}", f"-I{CUDA_INC}"]
 CLI = os.path.join(PKG, "spinwalk")
 
-CU_UNITS = ["sw_kernels.cu", "sw_api.cu", "sw_noalloc.cu", "sw_tracks.cu", "sw_engine.cu", "sw_phantom_gpu.cu", "sw_minstd.cu", "sw_order.cu", "sw_tune.cu"]
+CU_UNITS = ["sw_kernels.cu", "sw_api.cu", "sw_noalloc.cu", "sw_tracks.cu", "sw_engine.cu",
+            "sw_phantom_gpu.cu", "sw_minstd.cu", "sw_order.cu", "sw_tune.cu", "sw_pool.cu"]
 CXX_UNITS = ["sw_host.cpp", "sw_phantom.cpp", "sw_config.cpp", "sw_h5.cpp", "sw_driver.cpp",
              "sw_mtjump.cpp"]
 

@@ -74,6 +74,12 @@ inline uint64_t jump_min_z(const sw_tuning &t) {
 int jump_table(uint64_t seed, uint32_t lo, uint32_t hi, uint64_t z_min, uint32_t *&buf,
                size_t &buf_words, JumpTable &jt);
 
+// sw_sim_batch with pooled generators (sw_pool.cu): runs the batch and sets `taken`, or leaves
+// `taken` false for the engine path (another generator flavour, or a pool larger than half the
+// free device memory).
+int run_batch_pooled(const sw_instance *items, uint32_t n_items, const float *pFieldMap,
+                     const uint8_t *pMask, int precision, bool &taken);
+
 // Kernel timing of the last call on this thread (sw_last_timing).
 extern thread_local sw_timing g_timing;
 // Sets sw_last_error() for the calling thread and returns `code`.

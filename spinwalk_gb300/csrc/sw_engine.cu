@@ -871,6 +871,14 @@ int sw_sim_batch(const sw_instance *items, uint32_t n_items, const float *pField
     if (p0->fieldmap_exist && !pFieldMap) return fail(SW_ERR_INVALID, "null fieldmap");
     g_timing = sw_timing{};
     const double t0 = now_s();
+    {   // one generator pair per spin id for all instances (sw_pool.cu), where it applies
+        bool taken = false;
+        const int rp = run_batch_pooled(items, n_items, pFieldMap, pMask, precision, taken);
+        if (taken || rp) {
+            if (!rp) g_timing.total_ms = (float)((now_s() - t0) * 1e3);
+            return rp;
+        }
+    }
     std::lock_guard<std::mutex> lk(g_batch_mu);
     const uint32_t slots = std::min<uint32_t>(8, n_items);
     const uint32_t slot_spins = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(n_max, 1u << 20));

@@ -418,100 +418,126 @@ __device__ __forceinline__ uint32_t block_word(const uint32_t *gst, const uint32
     return in_smem ? s[i] : gst[i];
 }
 
+// Appends K polar pairs (normal_distribution<float>: y*m first, x*m saved for the next call) from
+// the mt19937 state gst at position p to the ring nb of RLEN deviates, from slot wpos (< 2 RLEN
+// before reduction) on; 32 candidate pairs per pass, accepted pairs compacted with a ballot.
+// `s` is the warp's 624-word shared block.
+template <uint32_t RLEN>
+__device__ __forceinline__ uint32_t ring_slot(uint32_t x) {
+    if constexpr ((RLEN & (RLEN - 1)) == 0) {
+        return x & (RLEN - 1);
+    } else {                                          // x < 3 RLEN
+        x -= x >= RLEN ? RLEN : 0u;
+        x -= x >= RLEN ? RLEN : 0u;
+        return x;
+    }
+}
+
+template <uint32_t RLEN>
+__device__ __forceinline__ void refill_normals_mt(uint32_t *gst, uint32_t &p, float *nb,
+                                                  uint32_t wpos, uint32_t K, uint32_t *s,
+                                                  const float *s_tab, const LogfTables &L,
+                                                  int lane) {
+    const unsigned lt_mask = (1u << lane) - 1u;
+    uint32_t produced = 0;
+    bool in_smem = false;
+    while (produced < K) {
+        if (p >= (uint32_t)kMtN) {
+            twist_block(gst, s, in_smem, lane);
+            p = 0;
+        }
+        uint32_t w0 = 0, w1 = 0;
+        uint32_t npairs;
+        bool straddle = false;
+        if (kMtN - p == 1) {            // pair = last word of this block + first of next
+            w0 = block_word(gst, s, in_smem, kMtN - 1);
+            twist_block(gst, s, in_smem, lane);
+            w1 = s[0];
+            npairs = 1;
+            straddle = true;
+        } else {
+            npairs = min(32u, (kMtN - p) / 2);
+            if ((uint32_t)lane < npairs) {
+                w0 = block_word(gst, s, in_smem, p + 2 * lane);
+                w1 = block_word(gst, s, in_smem, p + 2 * lane + 1);
+            }
+        }
+        const bool valid = (uint32_t)lane < npairs;
+        const float u1 = canon24(mt_temper(w0)), u2 = canon24(mt_temper(w1));
+        const float x = 2.0f * u1 - 1.0f, y = 2.0f * u2 - 1.0f;
+        const float r2 = x * x + y * y;
+        const bool ok = valid && !(r2 > 1.0f || r2 == 0.0f);
+        const unsigned bal = __ballot_sync(0xffffffffu, ok);
+        const uint32_t rank = __popc(bal & lt_mask);
+        const uint32_t need = K - produced;
+        if (ok && rank < need) {
+            const float lg = logf_libm(r2, s_tab, L);
+            const float mult = __fsqrt_rn(__fdiv_rn(-2.0f * lg, r2));
+            const uint32_t pos = ring_slot<RLEN>(wpos + 2 * (produced + rank));
+            nb[pos] = y * mult;                                  // returned first
+            nb[pos + 1 == RLEN ? 0 : pos + 1] = x * mult;        // saved for the next call
+        }
+        const uint32_t nacc = __popc(bal);
+        if (nacc <= need) {
+            produced += nacc;
+            p = straddle ? 1 : p + 2 * npairs;
+        } else {
+            const unsigned m2 = __ballot_sync(0xffffffffu, ok && rank == need - 1);
+            const uint32_t last = __ffs(m2) - 1;
+            produced = K;
+            p = p + 2 * (last + 1);
+        }
+    }
+}
+
+// Appends `need` crossing uniforms (uniform_real_distribution<float>(0,1)) from the state gst at
+// position p to the ring ub of RLEN entries (a power of two), from count wpos on.
+template <uint32_t RLEN>
+__device__ __forceinline__ void refill_uniforms_mt(uint32_t *gst, uint32_t &p, float *ub,
+                                                   uint32_t wpos, uint32_t need, uint32_t *s,
+                                                   int lane) {
+    uint32_t produced = 0;
+    bool in_smem = false;
+    while (produced < need) {
+        if (p >= (uint32_t)kMtN) {
+            twist_block(gst, s, in_smem, lane);
+            p = 0;
+        }
+        const uint32_t n = min(min(32u, (uint32_t)kMtN - p), need - produced);
+        if ((uint32_t)lane < n) {
+            const uint32_t wv = block_word(gst, s, in_smem, p + lane);
+            ub[(wpos + produced + lane) % RLEN] = canon24(mt_temper(wv));
+        }
+        p += n;
+        produced += n;
+    }
+}
+
 // One warp tops up the rings of one spin from its mt19937 states: Gaussian deviates from gen_r
-// (normal_distribution<float>, polar method, 32 candidate pairs per pass) and, when at most half
-// full, crossing uniforms from gen_u. `s` is the warp's 624-word shared block.
+// (normal_distribution<float>, polar method) and, when at most half full, crossing uniforms from
+// gen_u. `s` is the warp's 624-word shared block.
 __device__ __forceinline__ void refill_spin_mt(uint32_t spin, const RngState &G,
                                                const LogfTables &L, const float *s_tab,
                                                uint32_t *s, int lane) {
-    const unsigned lt_mask = (1u << lane) - 1u;
-    // ---- Gaussian deviates from gen_r (normal_distribution<float>, polar method) ----
     const uint32_t nc = G.ncnt[spin];
     const uint32_t K = (kNormBuf - nc) / 2;                 // pairs to add
     if (K > 0) {
-        uint32_t *gst = G.mt_r + (size_t)spin * kMtN;
-        float *nb = G.nbuf + (size_t)spin * kNormBuf;
-        const uint32_t wpos = G.nhead[spin] + nc;
         uint32_t p = G.p_r[spin];
-        uint32_t produced = 0;
-        bool in_smem = false;
-        while (produced < K) {
-            if (p >= (uint32_t)kMtN) {
-                twist_block(gst, s, in_smem, lane);
-                p = 0;
-            }
-            uint32_t w0 = 0, w1 = 0;
-            uint32_t npairs;
-            bool straddle = false;
-            if (kMtN - p == 1) {            // pair = last word of this block + first of next
-                w0 = block_word(gst, s, in_smem, kMtN - 1);
-                twist_block(gst, s, in_smem, lane);
-                w1 = s[0];
-                npairs = 1;
-                straddle = true;
-            } else {
-                npairs = min(32u, (kMtN - p) / 2);
-                if ((uint32_t)lane < npairs) {
-                    w0 = block_word(gst, s, in_smem, p + 2 * lane);
-                    w1 = block_word(gst, s, in_smem, p + 2 * lane + 1);
-                }
-            }
-            const bool valid = (uint32_t)lane < npairs;
-            const float u1 = canon24(mt_temper(w0)), u2 = canon24(mt_temper(w1));
-            const float x = 2.0f * u1 - 1.0f, y = 2.0f * u2 - 1.0f;
-            const float r2 = x * x + y * y;
-            const bool ok = valid && !(r2 > 1.0f || r2 == 0.0f);
-            const unsigned bal = __ballot_sync(0xffffffffu, ok);
-            const uint32_t rank = __popc(bal & lt_mask);
-            const uint32_t need = K - produced;
-            if (ok && rank < need) {
-                const float lg = logf_libm(r2, s_tab, L);
-                const float mult = __fsqrt_rn(__fdiv_rn(-2.0f * lg, r2));
-                uint32_t pos = wpos + 2 * (produced + rank);   // < 3 kNormBuf
-                pos -= pos >= kNormBuf ? kNormBuf : 0u;
-                pos -= pos >= kNormBuf ? kNormBuf : 0u;
-                nb[pos] = y * mult;                          // returned first
-                nb[pos + 1 == kNormBuf ? 0 : pos + 1] = x * mult;   // saved for the next call
-            }
-            const uint32_t nacc = __popc(bal);
-            if (nacc <= need) {
-                produced += nacc;
-                p = straddle ? 1 : p + 2 * npairs;
-            } else {
-                const unsigned m2 = __ballot_sync(0xffffffffu, ok && rank == need - 1);
-                const uint32_t last = __ffs(m2) - 1;
-                produced = K;
-                p = p + 2 * (last + 1);
-            }
-        }
+        refill_normals_mt<kNormBuf>(G.mt_r + (size_t)spin * kMtN, p,
+                                    G.nbuf + (size_t)spin * kNormBuf, G.nhead[spin] + nc, K, s,
+                                    s_tab, L, lane);
         if (lane == 0) {
             G.p_r[spin] = p;
             G.ncnt[spin] = nc + 2 * K;
         }
     }
-    // ---- crossing uniforms from gen_u (uniform_real_distribution<float>(0,1)) ----
     const uint32_t uc = G.ucnt[spin];
     if (uc <= kUnifBuf / 2) {
-        uint32_t *gst = G.mt_u + (size_t)spin * kMtN;
-        float *ub = G.ubuf + (size_t)spin * kUnifBuf;
-        const uint32_t wpos = G.uhead[spin] + uc;
         const uint32_t need = kUnifBuf - uc;
         uint32_t p = G.p_u[spin];
-        uint32_t produced = 0;
-        bool in_smem = false;
-        while (produced < need) {
-            if (p >= (uint32_t)kMtN) {
-                twist_block(gst, s, in_smem, lane);
-                p = 0;
-            }
-            const uint32_t n = min(min(32u, (uint32_t)kMtN - p), need - produced);
-            if ((uint32_t)lane < n) {
-                const uint32_t wv = block_word(gst, s, in_smem, p + lane);
-                ub[(wpos + produced + lane) % kUnifBuf] = canon24(mt_temper(wv));
-            }
-            p += n;
-            produced += n;
-        }
+        refill_uniforms_mt<kUnifBuf>(G.mt_u + (size_t)spin * kMtN, p,
+                                     G.ubuf + (size_t)spin * kUnifBuf, G.uhead[spin] + uc, need,
+                                     s, lane);
         if (lane == 0) {
             G.p_u[spin] = p;
             G.ucnt[spin] = uc + need;
@@ -531,6 +557,55 @@ __global__ void __launch_bounds__(32 * kRefillWarps)
          spin += gridDim.x * kRefillWarps) {
         if (flags[spin] & kFlagDone) continue;
         refill_spin_mt(spin, G, L, s_tab, s_mt[w], lane);
+        __syncwarp();
+    }
+}
+
+// Pooled generators (PoolState): one warp per stream tops its Gaussian ring up to the lowest
+// read position of the pairs that paused in the last walk plus kPoolNorm (whole pairs), and its
+// uniform ring likewise; streams no walking pair reported are skipped. The deviates of stream s
+// are those spin s draws in every instance of the batch.
+__global__ void __launch_bounds__(32 * kRefillWarps)
+    k_refill_pool(PoolState Q, LogfTables L, uint32_t n_streams) {
+    __shared__ float s_tab[192];
+    __shared__ uint32_t s_mt[kRefillWarps][kMtN];
+    for (int i = threadIdx.x; i < 192; i += blockDim.x) s_tab[i] = L.tab[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t st = blockIdx.x * kRefillWarps + w; st < n_streams;
+         st += gridDim.x * kRefillWarps) {
+        const uint32_t nm = Q.nmin[st], um = Q.umin[st];
+        if (nm == kPoolNone && um == kPoolNone) continue;
+        if (nm != kPoolNone) {
+            const uint32_t target = (nm + kPoolNorm) & ~1u, w0 = Q.nw[st];
+            if (target > w0) {
+                uint32_t p = Q.p_r[st];
+                refill_normals_mt<kPoolNorm>(Q.mt_r + (size_t)st * kMtN, p,
+                                             Q.nbuf + (size_t)st * kPoolNorm, w0 & (kPoolNorm - 1),
+                                             (target - w0) / 2, s_mt[w], s_tab, L, lane);
+                if (lane == 0) {
+                    Q.p_r[st] = p;
+                    Q.nw[st] = target;
+                }
+            }
+        }
+        if (um != kPoolNone) {
+            const uint32_t target = um + kPoolUnif, w0 = Q.uw[st];
+            if (target > w0) {
+                uint32_t p = Q.p_u[st];
+                refill_uniforms_mt<kPoolUnif>(Q.mt_u + (size_t)st * kMtN, p,
+                                              Q.ubuf + (size_t)st * kPoolUnif, w0, target - w0,
+                                              s_mt[w], lane);
+                if (lane == 0) {
+                    Q.p_u[st] = p;
+                    Q.uw[st] = target;
+                }
+            }
+        }
+        if (lane == 0) {              // the next walk reports afresh
+            Q.nmin[st] = kPoolNone;
+            Q.umin[st] = kPoolNone;
+        }
         __syncwarp();
     }
 }
@@ -563,11 +638,13 @@ __device__ __forceinline__ void signal_add(const Outputs &O, uint32_t key, const
 // ------------------------------------------------------------------------------------------
 // The walk (kernels.cu:107-232)
 // ------------------------------------------------------------------------------------------
-template <int PREC, bool DBL>
+// POOL: the spin draws from the pooled stream of its id (PoolState Q) instead of its own rings;
+// G.nhead / G.uhead hold its read positions in that stream (absolute counts).
+template <int PREC, bool DBL, bool POOL = false>
 __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, const DevParams &P,
                                           const DevTables &Tb, const uint2 *__restrict__ vox,
                                           const SpinState &S, const RngState &G,
-                                          const Outputs &O) {
+                                          const Outputs &O, const PoolState &Q = PoolState{}) {
     constexpr bool KAHAN = PREC == SW_PREC_KAHAN;
     uint64_t xo[3] = {S.x[spin], S.y[spin], S.z[spin]};    // bit patterns of the doubles
     float m0[3] = {S.mx[spin], S.my[spin], S.mz[spin]}, m1[3];
@@ -588,9 +665,25 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
     bool started = (flags & kFlagStarted) != 0;
     double dscale = __ldg(Tb.dscale + ts_old);
 
-    uint32_t nh = G.nhead[spin], nc = G.ncnt[spin], uh = G.uhead[spin], uc = G.ucnt[spin];
-    const float *nb = G.nbuf + (size_t)spin * kNormBuf;
-    const float *ub = G.ubuf + (size_t)spin * kUnifBuf;
+    constexpr uint32_t NLEN = POOL ? kPoolNorm : kNormBuf, ULEN = POOL ? kPoolUnif : kUnifBuf;
+    uint32_t nh, nc, uh, uc;
+    const float *nb, *ub;
+    if (POOL) {
+        const uint32_t nr = G.nhead[spin], ur = G.uhead[spin];
+        nc = Q.nw[spin] - nr;
+        uc = Q.uw[spin] - ur;
+        nh = nr & (kPoolNorm - 1);
+        uh = ur & (kPoolUnif - 1);
+        nb = Q.nbuf + (size_t)spin * kPoolNorm;
+        ub = Q.ubuf + (size_t)spin * kPoolUnif;
+    } else {
+        nh = G.nhead[spin];
+        nc = G.ncnt[spin];
+        uh = G.uhead[spin];
+        uc = G.ucnt[spin];
+        nb = G.nbuf + (size_t)spin * kNormBuf;
+        ub = G.ubuf + (size_t)spin * kUnifBuf;
+    }
 
     constexpr uint32_t NONE = 0xffffffffu;
     const bool last_scan0 = ds == P.n_dummy_scan;
@@ -656,7 +749,7 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
 #pragma unroll
             for (int i = 0; i < 3; i++) {
                 const float g = nb[nh];
-                nh = (nh + 1 == kNormBuf) ? 0 : nh + 1;
+                nh = (nh + 1 == NLEN) ? 0 : nh + 1;
                 const uint64_t rnd = dbits(f2d_exact(g) * dscale);   // hardware DMUL
                 uint64_t v = dadd_fp64(xo[i], rnd);  // xo[i] + rnd
                 // the wrap in integer arithmetic too: the compiler evaluates a cheap double
@@ -680,7 +773,7 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
             const uint32_t ts = v.y;
             if (ts != ts_old) {
                 const float u = ub[uh];
-                uh = (uh + 1 == kUnifBuf) ? 0 : uh + 1;
+                uh = (uh + 1 == ULEN) ? 0 : uh + 1;
                 uc--;
                 if (u >= __ldg(Tb.pXY + ts_old * P.n_substrate + ts)) {
                     if ((uint64_t)(itr++) > P.max_iterations) { status = SW_SPIN_LOST; break; }
@@ -791,7 +884,17 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
     S.tp[spin] = tp; S.tp_old[spin] = tp_old; S.ds[spin] = ds; S.itr[spin] = itr;
     S.ctr[spin] = c_rf | (c_te << 16);
     S.ctr2[spin] = c_dph | (c_grad << 16);
-    G.nhead[spin] = nh; G.ncnt[spin] = nc; G.uhead[spin] = uh; G.ucnt[spin] = uc;
+    if (POOL) {               // read positions: written counts minus what is left
+        const uint32_t nr = Q.nw[spin] - nc, ur = Q.uw[spin] - uc;
+        G.nhead[spin] = nr;
+        G.uhead[spin] = ur;
+        if (status < 0) {         // paused: the stream's next refill keeps what this pair needs
+            atomicMin(Q.nmin + spin, nr);
+            atomicMin(Q.umin + spin, ur);
+        }
+    } else {
+        G.nhead[spin] = nh; G.ncnt[spin] = nc; G.uhead[spin] = uh; G.ucnt[spin] = uc;
+    }
     uint32_t nf = ts_old | (started ? kFlagStarted : 0u);
     if (status >= 0) {
         nf |= kFlagDone | ((uint32_t)status << 16);
@@ -818,6 +921,22 @@ __global__ void __launch_bounds__(256, 4)
         const uint32_t spin = order ? __ldg(order + i) : i;
         const uint32_t flags = S.flags[spin];
         if (!(flags & kFlagDone)) still = walk_spin<PREC, DBL>(spin, flags, P, Tb, vox, S, G, O);
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, still);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(active, (uint32_t)__popc(b));
+}
+
+// The walk of one instance of a pooled batch: spins [spin_lo, spin_hi), generators from Q.
+template <int PREC, bool DBL>
+__global__ void __launch_bounds__(256, 4)
+    k_walk_pool(DevParams P, DevTables Tb, const uint2 *__restrict__ vox, SpinState S, RngState G,
+                Outputs O, PoolState Q, uint32_t *active, uint32_t spin_lo, uint32_t spin_hi) {
+    const uint32_t spin = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    bool still = false;
+    if (spin < spin_hi) {
+        const uint32_t flags = S.flags[spin];
+        if (!(flags & kFlagDone))
+            still = walk_spin<PREC, DBL, true>(spin, flags, P, Tb, vox, S, G, O, Q);
     }
     const unsigned b = __ballot_sync(0xffffffffu, still);
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(active, (uint32_t)__popc(b));
@@ -946,6 +1065,33 @@ cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevT
         k_walk<SW_PREC_FP32, true><<<g, block, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi, order);
     else
         k_walk<SW_PREC_FP32, false><<<g, block, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi, order);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refill_pool(const PoolState &Q, const LogfTables &L, uint32_t n_streams,
+                               cudaStream_t st) {
+    if (n_streams == 0) return cudaSuccess;
+    k_refill_pool<<<grid_for(n_streams, kRefillWarps, 152 * 64), 32 * kRefillWarps, 0, st>>>(
+        Q, L, n_streams);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_walk_pool_range(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
+                                   const uint2 *vox, const SpinState &S, const RngState &G,
+                                   const Outputs &O, const PoolState &Q, uint32_t *active,
+                                   uint32_t lo, uint32_t hi, cudaStream_t st) {
+    if (hi <= lo) return cudaSuccess;
+    const int g = grid_for(hi - lo, 256, 1 << 30);
+    if (prec == SW_PREC_FP64)
+        k_walk_pool<SW_PREC_FP64, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, Q, active, lo, hi);
+    else if (prec == SW_PREC_KAHAN && dbl)
+        k_walk_pool<SW_PREC_KAHAN, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, Q, active, lo, hi);
+    else if (prec == SW_PREC_KAHAN)
+        k_walk_pool<SW_PREC_KAHAN, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, Q, active, lo, hi);
+    else if (dbl)
+        k_walk_pool<SW_PREC_FP32, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, Q, active, lo, hi);
+    else
+        k_walk_pool<SW_PREC_FP32, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, Q, active, lo, hi);
     return cudaGetLastError();
 }
 

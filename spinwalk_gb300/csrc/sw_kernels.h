@@ -29,6 +29,14 @@ cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevT
                               const uint2 *vox, const SpinState &S, const RngState &G,
                               const Outputs &O, uint32_t *active, uint32_t lo, uint32_t hi,
                               cudaStream_t st, const uint32_t *order = nullptr, int block = 256);
+// Pooled generators of a batch (PoolState): refill of streams [0, n_streams), and the walk of one
+// instance's spins [lo, hi) drawing from them (G.nhead / G.uhead: the instance's read positions).
+cudaError_t launch_refill_pool(const PoolState &Q, const LogfTables &L, uint32_t n_streams,
+                               cudaStream_t st);
+cudaError_t launch_walk_pool_range(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
+                                   const uint2 *vox, const SpinState &S, const RngState &G,
+                                   const Outputs &O, const PoolState &Q, uint32_t *active,
+                                   uint32_t lo, uint32_t hi, cudaStream_t st);
 // Morton re-sort of spins [lo, hi) into Q.order (sw_order.cu).
 cudaError_t launch_order(const DevParams &P, const SpinState &S, const OrderState &Q,
                          uint32_t lo, uint32_t hi, cudaStream_t st);

@@ -1,0 +1,405 @@
+// Batches with pooled generators: sw_sim_batch when every instance shares the seed (which the
+// batch requires) and draws from std::mt19937.
+//
+// The reference's scale loop runs one simulation per instance (src/sim/monte_carlo.cu:273-337)
+// and seeds every spin's generators anew each time: mt19937(seed + spin), discard(seed + spin)
+// (src/sim/kernels.cu:82-88). So spin s of every instance draws the SAME sequence of Gaussian
+// steps and crossing uniforms; instances differ only in how fast they consume it (rejected
+// crossings redraw, and the sequences differ). Here each spin id s is one "stream": one
+// generator pair and one ring of each kind (PoolState), seeded once and refilled once per round
+// for all instances together; every instance keeps only its own read positions. The refill work
+// of a batch is then that of its largest instance instead of the sum over instances.
+//
+// A round: k_refill_pool over the streams, then the walk of every instance (one launch each, on
+// kWalkStreams streams); a stream's ring is topped up to the lowest read position of the pairs
+// that paused in the previous walk plus the ring length, so nothing unread is overwritten.
+// Results equal one sw_sim call per instance bit for bit (tests/test_batch.py).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <omp.h>
+
+#include "spinwalk_gpu.h"
+#include "sw_api_internal.h"
+#include "sw_kernels.h"
+
+namespace {
+
+using namespace sw::api;
+
+constexpr int kMaxDevices = 64;
+constexpr int kWalkStreams = 8;
+
+struct PoolCtx {
+    std::mutex mu;
+    char *d = nullptr;                   // device workspace
+    size_t d_bytes = 0;
+    char *h = nullptr;                   // pinned staging of the instances' inputs and outputs
+    size_t h_bytes = 0;
+    uint32_t *d_jump = nullptr;          // jump polynomials of the high spin ids
+    size_t jump_words = 0;
+    cudaStream_t main = nullptr;         // pack, seeding, refills, copies
+    cudaStream_t walk[kWalkStreams] = {};
+    cudaEvent_t refilled = nullptr, walked[kWalkStreams] = {};
+    uint32_t *h_active = nullptr;        // pinned
+    bool ready = false;
+};
+PoolCtx g_pool[kMaxDevices];
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+#define PL_CUDA(call)                                                                      \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            cudaGetLastError();                                                            \
+            return fail(SW_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));  \
+        }                                                                                  \
+    } while (0)
+
+int ensure_ctx(PoolCtx &c) {
+    if (c.ready) return SW_OK;
+    int lo = 0, hi = 0;
+    PL_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    PL_CUDA(cudaStreamCreateWithPriority(&c.main, cudaStreamNonBlocking, hi));
+    for (auto &s : c.walk) PL_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, hi));
+    PL_CUDA(cudaEventCreateWithFlags(&c.refilled, cudaEventDisableTiming));
+    for (auto &e : c.walked) PL_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PL_CUDA(cudaMallocHost(&c.h_active, sizeof(uint32_t)));
+    c.ready = true;
+    return SW_OK;
+}
+
+// Large host copies split across threads (one core copies about 10 GB/s).
+void par_copy(void *dst, const void *src, size_t bytes) {
+    constexpr size_t kPiece = 4 << 20;
+    if (bytes < 2 * kPiece) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    const int64_t pieces = (int64_t)((bytes + kPiece - 1) / kPiece);
+#pragma omp parallel for num_threads(8) schedule(static)
+    for (int64_t i = 0; i < pieces; i++) {
+        const size_t o = (size_t)i * kPiece, n = std::min(kPiece, bytes - o);
+        std::memcpy(static_cast<char *>(dst) + o, static_cast<const char *>(src) + o, n);
+    }
+}
+
+struct Inst {
+    const sw_instance *it;
+    size_t n, nte, trj;
+    bool dbl;
+    TableImage im;
+    sw::DevParams P;
+    sw::SpinState S;
+    sw::RngState G;                      // nhead / uhead: read positions in the streams
+    char *tables;
+    // device I/O (offsets into the I/O region, same offsets in the pinned staging): the inputs
+    // of all instances first, then their outputs
+    size_t o_M0, o_XYZ0, o_M1, o_T, o_XYZ1, o_st;
+};
+
+}  // namespace
+
+int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const float *pFieldMap,
+                              const uint8_t *pMask, int precision, bool &taken) {
+    taken = false;
+    const bool bf16 = (precision & SW_FIELD_BF16) != 0;
+    const uint32_t rng = (uint32_t)precision & ~(uint32_t)(SW_PREC_MASK | SW_FIELD_BF16);
+    const int prec = precision & SW_PREC_MASK;
+    if (rng != SW_RNG_MT19937) return SW_OK;                 // minstd: the engine path
+    if (prec != SW_PREC_FP32 && prec != SW_PREC_FP64 && prec != SW_PREC_KAHAN)
+        return fail(SW_ERR_INVALID, "precision");
+    const sw_params *p0 = items[0].param;
+    const size_t ml = (size_t)p0->matrix_length;
+    uint64_t n_max = 0;
+    for (uint32_t i = 0; i < n_items; i++) n_max = std::max<uint64_t>(n_max, items[i].param->n_spins);
+    if (n_max == 0) {
+        taken = true;
+        return SW_OK;
+    }
+
+    // ---- layout: phantom, pool, per-instance state, then the I/O region ----
+    std::vector<Inst> in(n_items);
+    Carve c{nullptr};
+    auto plan = [&](char *base) {
+        c = Carve{base};
+        uint2 *vox = c.take<uint2>(bf16 ? (ml + 1) / 2 : ml);
+        (void)vox;
+        c.take<uint32_t>(4);                                  // active counter, bad-label flag
+        c.take<uint32_t>(n_max * sw::kMtN);                  // mt_r
+        c.take<uint32_t>(n_max * sw::kMtN);                  // mt_u
+        for (int k = 0; k < 6; k++) c.take<uint32_t>(n_max);  // p_r p_u nw uw nmin umin
+        c.take<float>(n_max * sw::kPoolNorm);
+        c.take<float>(n_max * sw::kPoolUnif);
+        for (Inst &I : in) {
+            const size_t n = I.n;
+            I.tables = c.take<char>(I.im.bytes.size());
+            sw::SpinState &S = I.S;
+            S.x = c.take<uint64_t>(n);
+            S.y = c.take<uint64_t>(n);
+            S.z = c.take<uint64_t>(n);
+            S.mx = c.take<float>(n);
+            S.my = c.take<float>(n);
+            S.mz = c.take<float>(n);
+            S.acc = c.take<float>(n);
+            S.acc_e = c.take<float>(n);
+            S.accd = c.take<double>(I.dbl ? n : 1);
+            S.dmx = c.take<double>(I.dbl ? n : 1);
+            S.dmy = c.take<double>(I.dbl ? n : 1);
+            S.dmz = c.take<double>(I.dbl ? n : 1);
+            S.field = c.take<float>(n);
+            S.ind_old = c.take<int64_t>(n);
+            S.tp = c.take<uint32_t>(n);
+            S.tp_old = c.take<uint32_t>(n);
+            S.ds = c.take<uint32_t>(n);
+            S.itr = c.take<uint32_t>(n);
+            S.ctr = c.take<uint32_t>(n);
+            S.ctr2 = c.take<uint32_t>(n);
+            S.flags = c.take<uint32_t>(n);
+            I.G = sw::RngState{};
+            I.G.nhead = c.take<uint32_t>(n);
+            I.G.uhead = c.take<uint32_t>(n);
+        }
+    };
+    size_t io = 0;
+    for (uint32_t i = 0; i < n_items; i++) {
+        Inst &I = in[i];
+        I.it = &items[i];
+        const sw_params *p = I.it->param;
+        I.n = p->n_spins;
+        I.nte = I.it->seq->n_TE;
+        I.trj = p->enRecordTrajectory ? (size_t)(p->n_dummy_scan + 1) * p->n_timepoints : 1;
+        I.dbl = prec == SW_PREC_FP64;
+        build_tables(p, I.it->seq, I.im);
+        if (!I.im.complete()) return fail(SW_ERR_INVALID, "internal error: incomplete parameter tables");
+        I.P = dev_params(p, I.it->seq);
+        I.P.rng = SW_RNG_MT19937;
+        I.P.field_bf16 = bf16 ? 1 : 0;
+    }
+    auto sec = [&](size_t bytes) { size_t o = io; io = (io + bytes + 255) & ~size_t(255); return o; };
+    for (Inst &I : in) {
+        I.o_M0 = sec(I.n * 12);
+        I.o_XYZ0 = sec(I.n * 12);
+    }
+    const size_t out_begin = io;          // outputs: uploaded with their contents, read back
+    for (Inst &I : in) {
+        I.o_M1 = sec(I.n * I.nte * 12);
+        I.o_T = sec(I.n * I.nte);
+        I.o_XYZ1 = sec(I.n * I.trj * 12);
+        I.o_st = sec(I.n * 4);
+    }
+    plan(nullptr);
+    const size_t state_bytes = (c.off + 255) & ~size_t(255);
+    const size_t need = state_bytes + io + 256;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return SW_OK;                                        // let the engine path report it
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return fail(SW_ERR_CUDA, "no current CUDA device");
+    }
+    PoolCtx &X = g_pool[dev];
+    std::lock_guard<std::mutex> lk(X.mu);
+    // the pool holds every instance at once: above half the free memory, run instances as
+    // engine jobs instead (bounded slots)
+    if (need > X.d_bytes && need - X.d_bytes > free_b / 2) return SW_OK;
+    taken = true;
+    int rc = ensure_ctx(X);
+    if (rc) return rc;
+    const LogfTables LT = device_logf_tables();
+    if (!LT.tab) return SW_ERR_CUDA;
+    if (need > X.d_bytes) {
+        if (X.d) cudaFree(X.d);
+        X.d = nullptr;
+        X.d_bytes = 0;
+        cudaError_t e = cudaMalloc(&X.d, need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SW_ERR_NOMEM, "batch workspace of " + std::to_string(need >> 20) +
+                                          " MiB: " + cudaGetErrorString(e));
+        }
+        X.d_bytes = need;
+    }
+    if (io > X.h_bytes) {
+        if (X.h) cudaFreeHost(X.h);
+        X.h = nullptr;
+        X.h_bytes = 0;
+        cudaError_t e = cudaMallocHost(&X.h, io);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SW_ERR_NOMEM, "batch staging of " + std::to_string(io >> 20) +
+                                          " MiB: " + cudaGetErrorString(e));
+        }
+        X.h_bytes = io;
+    }
+    plan(X.d);
+    Carve c2{X.d};
+    uint2 *vox = c2.take<uint2>(bf16 ? (ml + 1) / 2 : ml);
+    uint32_t *cnt = c2.take<uint32_t>(4);
+    sw::PoolState Q;
+    Q.mt_r = c2.take<uint32_t>(n_max * sw::kMtN);
+    Q.mt_u = c2.take<uint32_t>(n_max * sw::kMtN);
+    Q.p_r = c2.take<uint32_t>(n_max);
+    Q.p_u = c2.take<uint32_t>(n_max);
+    Q.nw = c2.take<uint32_t>(n_max);
+    Q.uw = c2.take<uint32_t>(n_max);
+    Q.nmin = c2.take<uint32_t>(n_max);
+    Q.umin = c2.take<uint32_t>(n_max);
+    Q.nbuf = c2.take<float>(n_max * sw::kPoolNorm);
+    Q.ubuf = c2.take<float>(n_max * sw::kPoolUnif);
+    char *d_io = X.d + state_bytes;
+    cudaStream_t ms = X.main;
+    uint32_t launches = 0;
+
+    // ---- phantom (mask + field -> records), generator streams ----
+    {
+        uint8_t *d_mask = nullptr;
+        float *d_field = nullptr;
+        // the I/O region is free until the instances' inputs are staged: use it for the phantom
+        // upload when it is large enough, else a temporary allocation
+        const size_t ph_bytes = ml + (p0->fieldmap_exist ? ml * 4 : 0) + 512;
+        char *tmp = nullptr;
+        char *up = d_io;
+        if (ph_bytes > io) {
+            PL_CUDA(cudaMalloc(&tmp, ph_bytes));
+            up = tmp;
+        }
+        d_mask = reinterpret_cast<uint8_t *>(up);
+        if (p0->fieldmap_exist) d_field = reinterpret_cast<float *>(up + ((ml + 255) & ~size_t(255)));
+        PL_CUDA(cudaMemcpyAsync(d_mask, pMask, ml, cudaMemcpyHostToDevice, ms));
+        if (d_field) PL_CUDA(cudaMemcpyAsync(d_field, pFieldMap, ml * 4, cudaMemcpyHostToDevice, ms));
+        PL_CUDA(cudaMemsetAsync(cnt, 0, 4 * sizeof(uint32_t), ms));
+        PL_CUDA(sw::launch_pack(d_mask, d_field, vox, (int64_t)ml, p0->n_substrate, cnt + 1, ms, bf16));
+        launches++;
+        uint32_t bad = 0;
+        PL_CUDA(cudaMemcpyAsync(&bad, cnt + 1, 4, cudaMemcpyDeviceToHost, ms));
+        PL_CUDA(cudaStreamSynchronize(ms));
+        if (tmp) cudaFree(tmp);
+        if (bad) return fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate");
+    }
+    sw::JumpTable jt;
+    rc = jump_table(p0->seed, 0, (uint32_t)n_max, jump_min_z(current_tuning()), X.d_jump,
+                    X.jump_words, jt);
+    if (rc) return rc;
+    {
+        sw::DevParams Ps{};
+        Ps.seed = p0->seed;
+        Ps.rng = SW_RNG_MT19937;
+        sw::RngState Gs{};
+        Gs.mt_r = Q.mt_r;
+        Gs.mt_u = Q.mt_u;
+        Gs.p_r = Q.p_r;
+        Gs.p_u = Q.p_u;
+        // k_seed zeroes the ring counters of each spin: here the streams' written counts and
+        // their lowest read positions, which is where every stream starts
+        Gs.nhead = Q.nw;
+        Gs.ncnt = Q.uw;
+        Gs.uhead = Q.nmin;
+        Gs.ucnt = Q.umin;
+        PL_CUDA(sw::launch_seed_range(Ps, Gs, 0, (uint32_t)n_max, ms, &jt));
+        launches++;
+    }
+
+    // ---- instances: inputs (and the outputs' current contents) staged, uploaded, k_init ----
+    for (Inst &I : in) {
+        const sw_instance &it = *I.it;
+        par_copy(X.h + I.o_M0, it.M0, I.n * 12);
+        par_copy(X.h + I.o_XYZ0, it.XYZ0, I.n * 12);
+        if (I.nte) {
+            par_copy(X.h + I.o_M1, it.M1, I.n * I.nte * 12);
+            par_copy(X.h + I.o_T, it.T, I.n * I.nte);
+        }
+        par_copy(X.h + I.o_XYZ1, it.XYZ1, I.n * I.trj * 12);
+    }
+    cudaStream_t w0 = X.walk[0];
+    PL_CUDA(cudaMemcpyAsync(d_io, X.h, io, cudaMemcpyHostToDevice, w0));
+    std::vector<sw::DevTables> Tb(n_items);
+    std::vector<sw::Outputs> O(n_items);
+    for (uint32_t i = 0; i < n_items; i++) {
+        Inst &I = in[i];
+        PL_CUDA(cudaMemcpyAsync(I.tables, I.im.bytes.data(), I.im.bytes.size(), cudaMemcpyHostToDevice, w0));
+        Tb[i] = dev_tables(I.im, I.tables);
+        O[i] = sw::Outputs{I.nte ? reinterpret_cast<float *>(d_io + I.o_M1) : nullptr, nullptr,
+                           reinterpret_cast<float *>(d_io + I.o_XYZ1),
+                           I.nte ? reinterpret_cast<uint8_t *>(d_io + I.o_T) : nullptr,
+                           reinterpret_cast<int32_t *>(d_io + I.o_st)};
+        if (!I.n) continue;
+        PL_CUDA(cudaMemsetAsync(I.G.nhead, 0, I.n * 4, w0));
+        PL_CUDA(cudaMemsetAsync(I.G.uhead, 0, I.n * 4, w0));
+        PL_CUDA(sw::launch_init_range(I.P, Tb[i], vox, reinterpret_cast<const float *>(d_io + I.o_M0),
+                                      reinterpret_cast<const float *>(d_io + I.o_XYZ0), I.S, O[i],
+                                      I.dbl, 0, (uint32_t)I.n, w0));
+        launches++;
+    }
+    PL_CUDA(cudaEventRecord(X.walked[0], w0));
+    PL_CUDA(cudaStreamWaitEvent(ms, X.walked[0], 0));
+
+    // ---- rounds ----
+    uint64_t steps_max = 0, max_rounds = 64;
+    for (const Inst &I : in) {
+        const sw_params *p = I.it->param;
+        const uint64_t st = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
+        steps_max = std::max(steps_max, st);
+        max_rounds = std::max<uint64_t>(max_rounds, 64 + st * (p->max_iterations + 2));
+    }
+    // every pair needs 3 deviates per step and a round gives at most kPoolNorm: no pair can
+    // finish sooner than r0 rounds, which are issued without waiting
+    const uint64_t r0 = std::max<uint64_t>(1, (3 * steps_max + sw::kPoolNorm - 1) / sw::kPoolNorm);
+    uint64_t rounds = 0;
+    for (;; rounds++) {
+        if (rounds >= max_rounds) {
+            for (auto s : X.walk) cudaStreamSynchronize(s);
+            cudaStreamSynchronize(ms);
+            return fail(SW_ERR_TIMEOUT, "walk did not finish");
+        }
+        PL_CUDA(cudaMemsetAsync(cnt, 0, sizeof(uint32_t), ms));
+        PL_CUDA(sw::launch_refill_pool(Q, LT, (uint32_t)n_max, ms));
+        PL_CUDA(cudaEventRecord(X.refilled, ms));
+        launches++;
+        for (int k = 0; k < kWalkStreams; k++) PL_CUDA(cudaStreamWaitEvent(X.walk[k], X.refilled, 0));
+        for (uint32_t i = 0; i < n_items; i++) {
+            const Inst &I = in[i];
+            if (!I.n) continue;
+            PL_CUDA(sw::launch_walk_pool_range(prec, I.dbl, I.P, Tb[i], vox, I.S, I.G, O[i], Q, cnt,
+                                               0, (uint32_t)I.n, X.walk[i % kWalkStreams]));
+            launches++;
+        }
+        for (int k = 0; k < kWalkStreams; k++) {
+            PL_CUDA(cudaEventRecord(X.walked[k], X.walk[k]));
+            PL_CUDA(cudaStreamWaitEvent(ms, X.walked[k], 0));
+        }
+        if (rounds + 1 < r0) continue;
+        PL_CUDA(cudaMemcpyAsync(X.h_active, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, ms));
+        PL_CUDA(cudaStreamSynchronize(ms));
+        if (*X.h_active == 0) break;
+    }
+
+    // ---- outputs ----
+    PL_CUDA(cudaMemcpyAsync(X.h + out_begin, d_io + out_begin, io - out_begin,
+                            cudaMemcpyDeviceToHost, ms));
+    PL_CUDA(cudaStreamSynchronize(ms));
+    for (Inst &I : in) {
+        const sw_instance &it = *I.it;
+        if (I.nte) {
+            par_copy(it.M1, X.h + I.o_M1, I.n * I.nte * 12);
+            par_copy(it.T, X.h + I.o_T, I.n * I.nte);
+        }
+        par_copy(it.XYZ1, X.h + I.o_XYZ1, I.n * I.trj * 12);
+        if (it.status) par_copy(it.status, X.h + I.o_st, I.n * 4);
+    }
+    g_timing.n_chunks = (uint32_t)(rounds + 1);          // refill/walk rounds
+    g_timing.n_launches = launches;
+    return SW_OK;
+}

@@ -18,9 +18,24 @@ constexpr uint32_t kUnifBuf = 128;               // uniform deviates for crossin
 constexpr uint32_t kStepsPerRound = kNormBuf / 3;  // longest walk of one refill/walk round
 // Seeding: by default, spins whose discard count seed + spin reaches this jump ahead
 // (k_seed_jump) instead of regenerating seed + spin words (k_seed); sw_tuning.jump_min_kwords
-// overrides it.
-constexpr uint64_t kJumpMinZ = 1ull << 20;
+// overrides it. Measured on GB300: the jump costs 0.55 us of the whole GPU per spin whatever the
+// count, the discard 1 / 4.2e12 s per word, so they break even near 2.3e6 words.
+constexpr uint64_t kJumpMinZ = 2304ull * 1024;
 constexpr int kMtDegreeDev = 19937;               // degree of mt19937's characteristic polynomial
+
+// Pooled generators of a batch whose instances share the seed: one generator pair and one ring
+// of each kind per spin id s (a "stream"), read by every instance's spin s at its own position.
+// Counts are absolute since seeding; ring slot = count % ring length.
+constexpr uint32_t kPoolNorm = 1024;             // Gaussian deviates per stream
+constexpr uint32_t kPoolUnif = 256;              // crossing uniforms per stream
+constexpr uint32_t kPoolNone = 0xffffffffu;      // no walking pair reported a read position
+struct PoolState {
+    uint32_t *mt_r, *mt_u;    // [n_streams][624]
+    uint32_t *p_r, *p_u;      // next output index in the current block
+    float *nbuf, *ubuf;       // [n_streams][kPoolNorm], [n_streams][kPoolUnif]
+    uint32_t *nw, *uw;        // deviates written so far
+    uint32_t *nmin, *umin;    // lowest read position of the pairs that paused in the last walk
+};
 
 // Spin flags word: bits 0-7 ts_old (substrate of the last accepted voxel), bit 8 "scan
 // started", bit 9 done, bits 16-23 status (SW_SPIN_*).

@@ -51,14 +51,14 @@ def test_batch_equals_one_run_per_instance():
 
 @pytest.mark.gpu
 def test_batch_counts_its_work():
-    """One pack + one seeding, then per instance k_init and its refill / walk rounds (two
-    launches each); every instance needs at least one round."""
+    """One pack + one seeding of the pooled generator streams, k_init per instance, then rounds
+    of one refill of the streams and one walk launch per instance; at least one round."""
     probs = _instances()
     _lib.run_batch(probs)
     t = _lib.last_timing()
     busy = sum(1 for pr in probs if pr.params.n_spins)
-    assert t["n_chunks"] >= busy
-    assert t["n_launches"] >= 2 + 2 * t["n_chunks"] + busy
+    assert t["n_chunks"] >= 1
+    assert t["n_launches"] == 2 + busy + t["n_chunks"] * (1 + busy)
 
 
 def test_batch_rejects_mixed_seeds_and_phantoms():
@@ -71,3 +71,60 @@ def test_batch_rejects_mixed_seeds_and_phantoms():
     probs[1].params.matrix_length = 23 * 24 * 24
     with pytest.raises(_lib.SpinWalkError, match="phantom"):
         _lib.run_batch(probs)
+
+
+def _rejecting_instances(n_inst=12, n=900, seed=31):
+    """Instances that draw at different paces from the same generator streams: a three-substrate
+    random mask (a crossing attempt on most steps) with partial permeabilities, reflecting and
+    periodic boundaries, different FoV scales and sequences."""
+    rng = np.random.default_rng(2)
+    mask = rng.integers(0, 3, (16, 16, 16)).astype(np.uint8)
+    field = rng.normal(0, 1e-7, (16, 16, 16)).astype(np.float32)
+    fov = 16e-6
+    xyz0 = _lib.initial_positions([fov] * 3, seed, n)
+    out = []
+    for i in range(n_inst):
+        s32 = np.float32(0.6 + 0.1 * i)
+        f = float(s32 * np.float32(fov))
+        kw = dict(TR_us=8050, TE_us=(3000, 8000), timestep_us=50,
+                  diffusivity=(1e-9, 2e-9, 0.5e-9), T1_ms=(1000.0, 1500.0, 2000.0),
+                  T2_ms=(40.0, 30.0, 20.0),
+                  pXY=[[1, .5 - .03 * i, .1], [.4, 1, .2], [.3, .6, 1]], cross_fov=i % 3 != 0)
+        if i % 2:
+            kw.update(RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0), RF_us=(0, 4000))
+        out.append(Problem(mask, [f] * 3, field, n_spins=n - 37 * i, seed=seed,
+                           XYZ0=(xyz0[:n - 37 * i] * s32).astype(np.float32), **kw))
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_pooled_streams_with_uneven_consumption_equal_one_run_per_instance(precision):
+    """The pooled generator streams serve instances that reject crossings at different rates
+    (so their read positions drift apart within a round) and finish at different times."""
+    probs = _rejecting_instances()
+    batch = _lib.run_batch(probs, precision=precision, fill=np.nan)
+    assert batch[0]["timing"]["n_chunks"] >= 2
+    for k, (pr, b) in enumerate(zip(probs, batch)):
+        one = _lib.run(pr, precision=precision, fill=np.nan)
+        for key in ("M1", "XYZ1", "T", "status"):
+            assert bits_equal(b[key], one[key]), (k, key)
+
+
+@pytest.mark.gpu
+def test_pooled_batch_with_jump_ahead_seeds_and_the_minstd_flavour():
+    """A large seed (the streams seeded by jump-ahead) and, through the engine path, the
+    generator flavour of the reference's CUDA build."""
+    probs = _rejecting_instances(n_inst=4, n=400, seed=2 ** 29 + 11)
+    batch = _lib.run_batch(probs, fill=np.nan)
+    for k, (pr, b) in enumerate(zip(probs, batch)):
+        one = _lib.run(pr, fill=np.nan)
+        for key in ("M1", "XYZ1", "T", "status"):
+            assert bits_equal(b[key], one[key]), (k, key)
+    probs = _instances()
+    batch = _lib.run_batch(probs, precision=0x100)
+    for k, (pr, b) in enumerate(zip(probs, batch)):
+        if pr.params.n_spins:
+            one = _lib.run(pr, precision=0x100)
+            for key in ("M1", "XYZ1", "T", "status"):
+                assert bits_equal(b[key], one[key]), (k, key)

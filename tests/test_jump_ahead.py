@@ -1,10 +1,10 @@
 """Jump-ahead seeding: the state of mt19937(seed + spin) after discard(seed + spin)
 (src/sim/kernels.cu:82-88) computed through x^J mod phi instead of seed + spin generated words,
-for discard counts of at least 2^20 (sw_mtjump.h, k_seed_jump).
+for large discard counts (sw_mtjump.h, k_seed_jump; by default from 2304 x 1024 words).
 
 CPU: the host polynomials against libstdc++'s own discard, at the edges of a regeneration and
 far out (a random 32-bit seed, the reference's SEED = 0 case). GPU: walks of high spin ids, of
-large seeds and of ranges across the 2^20 boundary, against the oracle (which discards word by
+large seeds and of ranges across the threshold, against the oracle (which discards word by
 word), and through the serving engine with a distinct seed per request."""
 import numpy as np
 import pytest
@@ -14,7 +14,7 @@ from spinwalk_gb300.problem import Problem, cylinder_phantom
 from tests import oracle_lib
 from tests.helpers import bits_equal, m_close
 
-JUMP_MIN_Z = 1 << 20
+JUMP_MIN_Z = 2304 * 1024
 NEVER = 0xffffffff              # jump_min_kwords beyond any discard count: every spin discards
 
 
@@ -68,7 +68,7 @@ def test_gpu_high_spin_ids_jump(lo):
 
 @pytest.mark.gpu
 def test_gpu_range_across_the_jump_boundary():
-    """Spins on both sides of seed + spin = 2^20 in one call: the lower ones discard, the
+    """Spins on both sides of the default threshold in one call: the lower ones discard, the
     upper ones jump, and both match."""
     seed = 10
     lo, hi = JUMP_MIN_Z - seed - 150, JUMP_MIN_Z - seed + 170

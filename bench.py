@@ -384,13 +384,14 @@ def apply_tuning(args, pr=None):
         info = {"autotuned": True, "probe_s": time.perf_counter() - t0, "table": table}
     if args.resort_interval is not None or args.walk_block is not None or \
             args.seed_chunks is not None or args.round_streams is not None or \
-            args.jump_min_kwords is not None:
+            args.jump_min_kwords is not None or args.ring_steps is not None:
         cur = _lib.get_tuning()
         _lib.set_tuning(cur["resort_interval"] if args.resort_interval is None else args.resort_interval,
                         cur["walk_block"] if args.walk_block is None else args.walk_block,
                         cur["seed_chunks"] if args.seed_chunks is None else args.seed_chunks,
                         cur["round_streams"] if args.round_streams is None else args.round_streams,
-                        cur["jump_min_kwords"] if args.jump_min_kwords is None else args.jump_min_kwords)
+                        cur["jump_min_kwords"] if args.jump_min_kwords is None else args.jump_min_kwords,
+                        cur["ring_steps"] if args.ring_steps is None else args.ring_steps)
     info["applied"] = _lib.get_tuning()
     return info
 
@@ -697,6 +698,24 @@ def serve_requests(n_req, rng_seed=5, rank=0):
     return reqs, phantoms, arrivals, kinds, desc
 
 
+def distinct_seed_requests(reqs, rng_seed=6):
+    """Copies of `reqs` with a random 32-bit seed each (seeded draw) and the start positions the
+    reference driver derives from that seed (monte_carlo.cu:141-151)."""
+    import copy
+
+    from spinwalk_gb300 import _lib, abi
+    rng = np.random.default_rng(rng_seed)
+    out = []
+    for pr in reqs:
+        q = copy.copy(pr)
+        q.params = abi.SwParams.from_buffer_copy(pr.params)
+        q.params.seed = int(rng.integers(1, 2 ** 32))
+        q.XYZ0 = _lib.initial_positions([q.params.fov[i] for i in range(3)], q.params.seed,
+                                        q.params.n_spins)
+        out.append(q)
+    return out
+
+
 def play_trace(eng, reqs, arrivals, submit):
     """Submits the requests at their arrival times (real time) and polls until every result is
     in the caller's buffers. Returns (makespan s, latencies s, engine stats delta)."""
@@ -751,6 +770,12 @@ def leg_served(args, rank=0, world=1):
     with ClockSampler(0) as clk:
         warm_s, warm_lat, warm_st = play_trace(eng, reqs, arrivals, submit)
     clocks = clk.summary()
+    # distinct seeds: the first requests of the trace, each with its own random 32-bit seed (what
+    # SEED = 0 draws, simulation_parameters.cuh:233-234) and its own start positions, so no
+    # request can use another's generator states
+    dreqs = distinct_seed_requests(reqs[:args.distinct_requests])
+    dsteps = sum(p.spin_steps() for p in dreqs)
+    dist_s, dist_lat, dist_st = play_trace(eng, dreqs, arrivals[:len(dreqs)], submit)
     eng.close()
     # error against FP64 on the smallest request of each kind (a served request is
     # bit-identical to its own sw_sim run)
@@ -772,6 +797,14 @@ def leg_served(args, rank=0, world=1):
                      "latency_s": _lat(cold_lat), "seedings": cold_st["seedings"],
                      "note": "first pass of the trace on a new engine: every generator state "
                              "is computed inside the trace, when a request first needs it"},
+            "distinct_seeds": {"value": world * dsteps / dist_s, "makespan_s": dist_s,
+                               "requests": len(dreqs), "spin_steps": int(dsteps),
+                               "spins": int(sum(p.params.n_spins for p in dreqs)),
+                               "latency_s": _lat(dist_lat), "seedings": dist_st["seedings"],
+                               "note": "the first requests of the trace at their arrival times, "
+                                       "each with its own random 32-bit seed and start "
+                                       "positions: every spin is seeded inside the trace (by "
+                                       "jump-ahead, the discard counts being ~1e9)"},
             "startup": {"phantom_upload_s": phantom_s,
                         "note": "phantoms packed and made resident before the first request"},
             "offered_spin_steps_per_s": steps / float(arrivals[-1]),
@@ -1013,6 +1046,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=32768,
                     help="spin ids per step of the CPU reference arm (stratified)")
     ap.add_argument("--requests", type=int, default=100, help="served leg: trace length")
+    ap.add_argument("--distinct-requests", type=int, default=20,
+                    help="served leg: requests of the distinct-seed pass")
     ap.add_argument("--autotune", action="store_true",
                     help="pick the walk tuning by sw_autotune on the workload before timing")
     ap.add_argument("--resort-interval", type=int, default=None,
@@ -1028,6 +1063,8 @@ def main():
                     help="refill/walk rounds as this many independent halves on own streams (1, 2)")
     ap.add_argument("--seed-chunks", type=int, default=None,
                     help="seed/walk pipeline chunks (1 = seed all first, 0 = auto)")
+    ap.add_argument("--ring-steps", type=int, default=None,
+                    help="walk steps per refill/walk round (0 = default 256)")
     ap.add_argument("--jump-min-kwords", type=int, default=None,
                     help="seeding jumps ahead from this discard count (x 1024 words; 0 = default)")
     args = ap.parse_args()

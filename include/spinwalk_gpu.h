@@ -338,6 +338,11 @@ int sw_last_timing(sw_timing *out);
  *                     0 = default (2304, i.e. 2.36e6 words, where the two cost the same on
  *                     GB300). No reference counterpart (the reference discards word by word,
  *                     src/sim/kernels.cu:87-88).
+ *   ring_steps      : sw_sim / sw_sim_device / sw_sim_spins / sw_sim_signal: walk steps one
+ *                     refill of a spin's Gaussian ring lasts (3 deviates each), i.e. the steps
+ *                     of one refill/walk round and of one walk launch; 0 = default (256),
+ *                     else 32 .. 4096. Longer rings mean fewer rounds and launches but more
+ *                     ring memory (12 B per step per spin) between refill and walk.
  */
 typedef struct sw_tuning {
     uint32_t resort_interval;
@@ -345,18 +350,21 @@ typedef struct sw_tuning {
     uint32_t seed_chunks;
     uint32_t round_streams;
     uint32_t jump_min_kwords;
-    uint32_t reserved[3];
+    uint32_t ring_steps;
+    uint32_t reserved[2];
 } sw_tuning;
 int sw_set_tuning(const sw_tuning *t);
 int sw_get_tuning(sw_tuning *t);
 
-/* One measured candidate of sw_autotune: device time of the walk per 256-step round, the
- * re-sorts' share included (model: (sort + sum of the rounds at age 0..I-1 after a sort) / I). */
+/* One measured candidate of sw_autotune: device time of the refill and walk per 256 walk steps,
+ * the re-sorts' share included (model: (sort + sum of the rounds at age 0..I-1 after a sort) / I),
+ * rounds of ring_steps steps scaled to 256. */
 typedef struct sw_tune_entry {
     uint32_t resort_interval;
     uint32_t walk_block;
     float ms_per_round;
     float sort_ms;            /* one re-sort (0 for resort_interval 0) */
+    uint32_t ring_steps;      /* steps of one refill/walk round */
 } sw_tune_entry;
 
 /*
@@ -364,7 +372,8 @@ typedef struct sw_tune_entry {
  * problem's phantom, spin count, start positions and tissue, walked for up to 20 rounds (time
  * points extended, no dummy scans, generators of the SW_RNG_MINSTD flavour because their seeding
  * costs O(log) per spin and the walk is the same), timing every round with CUDA events. Candidates:
- * resort_interval in {0, 1, 2, 4, 8} x walk_block in {128, 256}. `best` receives the fastest;
+ * resort_interval in {0, 1, 2, 4, 8} x walk_block in {128, 256} with rounds of 256 steps, and
+ * rounds of 128 or 512 steps (ring_steps) in id order at block 256. `best` receives the fastest;
  * `table` (optional, table_len entries) the measured candidates, *n_entries their number;
  * apply != 0 installs `best` with sw_set_tuning. The probe allocates its own device memory
  * (about as much as sw_sim on the problem) and frees it before returning.
@@ -445,11 +454,17 @@ int sw_engine_submit(sw_engine *e, int32_t phantom, const sw_params *param, cons
 int sw_engine_poll(sw_engine *e, int wait, sw_job_result *done, uint32_t max_done,
                    uint32_t *n_done);
 int sw_engine_pending(sw_engine *e, uint32_t *n_pending);
-/* Counters since sw_engine_create: kernels launched, refill/walk rounds issued, seedings. */
+/* Counters since sw_engine_create: kernels launched, refill/walk rounds issued, seedings; and
+ * the device memory the engine holds against its HBM budget (slots, resident phantoms, seed
+ * caches), with the number of seed caches held. Seed caches that no queued job uses are freed,
+ * least recently used first, when a new one would exceed the budget. */
 typedef struct sw_engine_stats {
     uint64_t launches;
     uint64_t rounds;
     uint64_t seedings;
+    uint64_t hbm_used;
+    uint64_t hbm_budget;
+    uint64_t seed_caches;
 } sw_engine_stats;
 int sw_engine_get_stats(sw_engine *e, sw_engine_stats *out);
 

@@ -226,23 +226,28 @@ def run_config(ini_path, device=0):
 
 
 def set_tuning(resort_interval=0, walk_block=256, seed_chunks=0, round_streams=0,
-               jump_min_kwords=0):
+               jump_min_kwords=0, ring_steps=0):
     """sw_set_tuning: Morton re-sort interval (walk rounds, 0 = never), walk block size, seed
-    chunks of the seed/walk pipeline (0 = auto), round halves (0 = auto) and the discard count
-    from which seeding jumps ahead (in 1024 words, 0 = default 2304) for every later call of
-    this process. Results do not depend on it."""
+    chunks of the seed/walk pipeline (0 = auto), round halves (0 = auto), the discard count
+    from which seeding jumps ahead (in 1024 words, 0 = default 2304) and the steps of one
+    refill/walk round (0 = default 256) for every later call of this process. Results do not
+    depend on it."""
     t = abi.SwTuning(resort_interval=int(resort_interval), walk_block=int(walk_block),
                      seed_chunks=int(seed_chunks), round_streams=int(round_streams),
-                     jump_min_kwords=int(jump_min_kwords))
+                     jump_min_kwords=int(jump_min_kwords), ring_steps=int(ring_steps))
     check(lib().sw_set_tuning(C.byref(t)))
+
+
+def _tuning_dict(t):
+    return dict(resort_interval=t.resort_interval, walk_block=t.walk_block,
+                seed_chunks=t.seed_chunks, round_streams=t.round_streams,
+                jump_min_kwords=t.jump_min_kwords, ring_steps=t.ring_steps)
 
 
 def get_tuning():
     t = abi.SwTuning()
     check(lib().sw_get_tuning(C.byref(t)))
-    return dict(resort_interval=t.resort_interval, walk_block=t.walk_block,
-                seed_chunks=t.seed_chunks, round_streams=t.round_streams,
-                jump_min_kwords=t.jump_min_kwords)
+    return _tuning_dict(t)
 
 
 def autotune(problem, apply=False):
@@ -256,10 +261,9 @@ def autotune(problem, apply=False):
                             _p(problem.field), _p(problem.mask), _p(problem.XYZ0), int(bool(apply)),
                             C.byref(best), tab, 32, C.byref(n)))
     table = [dict(resort_interval=e.resort_interval, walk_block=e.walk_block,
-                  ms_per_round=e.ms_per_round, sort_ms=e.sort_ms) for e in tab[:n.value]]
-    return dict(resort_interval=best.resort_interval, walk_block=best.walk_block,
-                seed_chunks=best.seed_chunks, round_streams=best.round_streams,
-                jump_min_kwords=best.jump_min_kwords), table
+                  ms_per_round=e.ms_per_round, sort_ms=e.sort_ms, ring_steps=e.ring_steps)
+             for e in tab[:n.value]]
+    return _tuning_dict(best), table
 
 
 def last_timing():
@@ -410,10 +414,12 @@ class Engine:
         return out
 
     def stats(self):
-        """dict(launches, rounds, seedings) since the engine was created."""
+        """dict(launches, rounds, seedings) since the engine was created, and the HBM it holds
+        (hbm_used of hbm_budget bytes, seed_caches held)."""
         s = abi.SwEngineStats()
         check(lib().sw_engine_get_stats(self._h, C.byref(s)))
-        return dict(launches=s.launches, rounds=s.rounds, seedings=s.seedings)
+        return dict(launches=s.launches, rounds=s.rounds, seedings=s.seedings,
+                    hbm_used=s.hbm_used, hbm_budget=s.hbm_budget, seed_caches=s.seed_caches)
 
     def run_all(self):
         done = []

@@ -121,6 +121,9 @@ class SwEngineStats(C.Structure):
         ("launches", C.c_uint64),
         ("rounds", C.c_uint64),
         ("seedings", C.c_uint64),
+        ("hbm_used", C.c_uint64),
+        ("hbm_budget", C.c_uint64),
+        ("seed_caches", C.c_uint64),
     ]
 
 
@@ -131,7 +134,8 @@ class SwTuning(C.Structure):
         ("seed_chunks", C.c_uint32),
         ("round_streams", C.c_uint32),
         ("jump_min_kwords", C.c_uint32),
-        ("reserved", C.c_uint32 * 3),
+        ("ring_steps", C.c_uint32),
+        ("reserved", C.c_uint32 * 2),
     ]
 
 
@@ -141,6 +145,7 @@ class SwTuneEntry(C.Structure):
         ("walk_block", C.c_uint32),
         ("ms_per_round", C.c_float),
         ("sort_ms", C.c_float),
+        ("ring_steps", C.c_uint32),
     ]
 
 

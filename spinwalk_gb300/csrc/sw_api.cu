@@ -146,7 +146,8 @@ sw::DevTables dev_tables(const TableImage &im, const char *d) {
 
 
 // Lays out the whole workspace; with base == nullptr it only measures.
-Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl, bool mt_state) {
+Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl, bool mt_state,
+              uint32_t nlen) {
     Carve c{base};
     Layout L{};
     L.vox = c.take<uint2>(ml);
@@ -179,7 +180,8 @@ Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl, bo
     G.mt_u = c.take<uint32_t>(mt_state ? n * sw::kMtN : 1);
     G.p_r = c.take<uint32_t>(n);
     G.p_u = c.take<uint32_t>(n);
-    G.nbuf = c.take<float>(n * sw::kNormBuf);
+    G.nlen = nlen;
+    G.nbuf = c.take<float>(n * nlen);
     G.nhead = c.take<uint32_t>(n);
     G.ncnt = c.take<uint32_t>(n);
     G.ubuf = c.take<float>(n * sw::kUnifBuf);
@@ -289,7 +291,8 @@ int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
     const sw_tuning tu = current_tuning();
     const std::vector<uint32_t> b = seed_chunks(P, C);
     const uint64_t steps = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
-    const uint64_t r0 = (steps + sw::kStepsPerRound - 1) / sw::kStepsPerRound;
+    const uint64_t per_round = L.G.nlen / 3;      // steps a full ring lasts
+    const uint64_t r0 = (steps + per_round - 1) / per_round;
     const uint64_t max_rounds = 64 + steps * (p->max_iterations + 2);
     // the rounds run as H independent halves of the spins, half h on stream ws[h] with its own
     // active counter (L.active[0] / [2])
@@ -410,7 +413,9 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
     TableImage im;
     build_tables(p, q, im);
     if (!im.complete()) return fail(SW_ERR_INVALID, "internal error: incomplete parameter tables");
-    Layout L = layout(nullptr, n, p->matrix_length, im.bytes.size(), dbl, rng == SW_RNG_MT19937);
+    const uint32_t nlen = ring_len(current_tuning());
+    Layout L = layout(nullptr, n, p->matrix_length, im.bytes.size(), dbl, rng == SW_RNG_MT19937,
+                      nlen);
     if (L.bytes > ctx.ws_size) {
         if (ctx.ws) {
             SW_CUDA(cudaStreamSynchronize(st));
@@ -426,7 +431,7 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
         }
         ctx.ws_size = L.bytes;
     }
-    L = layout(ctx.ws, n, p->matrix_length, im.bytes.size(), dbl, rng == SW_RNG_MT19937);
+    L = layout(ctx.ws, n, p->matrix_length, im.bytes.size(), dbl, rng == SW_RNG_MT19937, nlen);
     SW_CUDA(cudaMemcpyAsync(L.tables, im.bytes.data(), im.bytes.size(), cudaMemcpyHostToDevice, st));
 
     sw::DevParams P = dev_params(p, q);
@@ -499,7 +504,7 @@ sw::LogfTables sw::api::device_logf_tables() {
 
 namespace {
 std::mutex g_tune_mu;
-sw_tuning g_tune{0u, 256u, 0u, 0u, 0u, {0u, 0u, 0u}};
+sw_tuning g_tune{0u, 256u, 0u, 0u, 0u, 0u, {0u, 0u}};
 }  // namespace
 
 int sw::api::jump_table(uint64_t seed, uint32_t lo, uint32_t hi, uint64_t z_min, uint32_t *&buf,
@@ -552,6 +557,8 @@ int sw_set_tuning(const sw_tuning *t) {
     if (t->resort_interval > 1u << 20) return fail(SW_ERR_INVALID, "resort_interval too large");
     if (t->seed_chunks > kMaxSeedChunks) return fail(SW_ERR_INVALID, "seed_chunks > 64");
     if (t->round_streams > 2) return fail(SW_ERR_INVALID, "round_streams must be 0, 1 or 2");
+    if (t->ring_steps != 0 && (t->ring_steps < 32 || t->ring_steps > 4096))
+        return fail(SW_ERR_INVALID, "ring_steps must be 0 (default) or 32 .. 4096");
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune = *t;
     return SW_OK;

@@ -63,6 +63,8 @@ struct Layout {
 
 // Process-wide tuning of the walk (sw_set_tuning / sw_autotune), read at the start of a call.
 sw_tuning current_tuning();
+// Gaussian deviates per ring (3 per step of a round) under tuning t.
+inline uint32_t ring_len(const sw_tuning &t) { return 3u * (t.ring_steps ? t.ring_steps : kNormBuf / 3); }
 // The discard count from which seeding jumps ahead under tuning t (at least 624).
 inline uint64_t jump_min_z(const sw_tuning &t) {
     const uint64_t z = t.jump_min_kwords ? 1024ull * t.jump_min_kwords : kJumpMinZ;
@@ -89,9 +91,9 @@ int check_args(const sw_params *p, const sw_sequence *q);
 DevParams dev_params(const sw_params *p, const sw_sequence *q);
 void build_tables(const sw_params *p, const sw_sequence *q, TableImage &im);
 DevTables dev_tables(const TableImage &im, const char *d);
-// base == nullptr: only measures (Layout::bytes).
+// base == nullptr: only measures (Layout::bytes). nlen: Gaussian deviates per ring.
 Layout layout(char *base, size_t n, int64_t ml, size_t table_bytes, bool dbl,
-              bool mt_state = true);
+              bool mt_state = true, uint32_t nlen = kNormBuf);
 // The current device's logf tables (built and uploaded on first use); {nullptr, nullptr} and
 // sw_last_error() set on failure.
 LogfTables device_logf_tables();

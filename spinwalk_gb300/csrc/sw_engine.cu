@@ -93,6 +93,8 @@ struct SeedCache {
     uint32_t *p = nullptr;          // [cap]
     uint32_t base = 0, n = 0, cap = 0;
     cudaEvent_t ready = nullptr;    // recorded after the last seeding on the seed stream
+    uint32_t jobs = 0;              // queued or running jobs that copy from it
+    uint64_t last_use = 0;          // engine tick of the last job that used it
 };
 
 struct Job {
@@ -164,6 +166,7 @@ struct sw_engine {
     int64_t next_job = 1;
     sw::LogfTables LT{nullptr, nullptr};
     uint64_t launches = 0, rounds = 0, seedings = 0;   // kernels, refill/walk rounds, k_seed calls
+    uint64_t tick = 0;                                  // seed cache use counter (LRU)
 };
 
 namespace {
@@ -219,6 +222,23 @@ int ensure_seeded(sw_engine *E, uint64_t seed, uint32_t lo, uint32_t hi, SeedCac
         const uint32_t cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(want, 2ull * C.cap), 0xffffffffu);
         const uint32_t capped = (uint32_t)std::max<uint64_t>(want, std::min<uint64_t>(cap, want + (want >> 1)));
         const size_t bytes = (size_t)capped * sw::kMtN * 4 + (size_t)capped * 4;
+        if (E->used + bytes > E->budget) {   // evict caches no job uses, least recently used first
+            EN_CUDA(cudaStreamSynchronize(E->seed_st));
+            while (E->used + bytes > E->budget) {
+                auto victim = E->seeds.end();
+                for (auto it = E->seeds.begin(); it != E->seeds.end(); ++it)
+                    if (it->first != seed && it->second->jobs == 0 && it->second->mt &&
+                        (victim == E->seeds.end() || it->second->last_use < victim->second->last_use))
+                        victim = it;
+                if (victim == E->seeds.end()) break;
+                SeedCache &V = *victim->second;
+                cudaFree(V.mt);
+                cudaFree(V.p);
+                cudaEventDestroy(V.ready);
+                E->used -= (size_t)V.cap * sw::kMtN * 4 + (size_t)V.cap * 4;
+                E->seeds.erase(victim);
+            }
+        }
         if (E->used + bytes > E->budget)
             return fail(SW_ERR_NOMEM, "seed cache of " + std::to_string(capped) + " spins exceeds the HBM budget");
         uint32_t *mt = nullptr, *p = nullptr;
@@ -402,6 +422,10 @@ void job_done_check(sw_engine *E, Job &j) {
         }
         j.t_done = now_s();
         E->phantoms[j.phantom].jobs--;
+        if (j.seed) {                      // its chunks no longer copy from the cache
+            j.seed->jobs--;
+            j.seed = nullptr;
+        }
         if (j.h_tables) {
             cudaFreeHost(j.h_tables);
             j.h_tables = nullptr;
@@ -581,6 +605,8 @@ int engine_submit(sw_engine *E, int32_t phantom, const sw_params *p, const sw_se
             cudaFreeHost(j->h_tables);
             return rc;
         }
+        j->seed->jobs++;
+        j->seed->last_use = ++E->tick;
     }
     j->t_submit = now_s();
     E->phantoms[phantom].jobs++;
@@ -1001,6 +1027,9 @@ int sw_engine_get_stats(sw_engine *e, sw_engine_stats *out) {
     out->launches = e->launches;
     out->rounds = e->rounds;
     out->seedings = e->seedings;
+    out->hbm_used = e->used;
+    out->hbm_budget = e->budget;
+    out->seed_caches = e->seeds.size();
     return SW_OK;
 }
 

@@ -138,22 +138,74 @@ __device__ __forceinline__ uint32_t jump_bits(const uint32_t *__restrict__ g, ui
     return (uint32_t)(v >> r) & ((1u << kJumpPer) - 1u);
 }
 
+__device__ __forceinline__ uint32_t xor3(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t r;
+    asm("lop3.b32 %0, %1, %2, %3, 0x96;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+    return r;
+}
+
 // Steps k0 .. k0 + 20: cur holds x[k0 + 21 lane + m], nxt is loaded with the next block
-// x[k0 + 21 + 21 lane + m]; window element i of step t is cur[t + i] or nxt[t + i - 21].
+// x[k0 + 21 + 21 lane + m]; window element i of step t is cur[t + i] or nxt[t + i - 21]. The
+// steps go three at a time on their three polynomial bits: two windows are added with one
+// three-input xor, so a triple costs one operation per word on average instead of 1.5.
+template <int T>
+__device__ __forceinline__ uint32_t jw(const uint32_t (&cur)[kJumpPer], const uint32_t (&nxt)[kJumpPer],
+                                       int i) {
+    return (T + i < kJumpPer) ? cur[T + i] : nxt[T + i - kJumpPer];
+}
+
+template <int T>
+__device__ __forceinline__ void jump_triple(uint32_t (&h)[kJumpPer], const uint32_t (&cur)[kJumpPer],
+                                            const uint32_t (&nxt)[kJumpPer], uint32_t bits) {
+    switch (bits & 7u) {
+    case 1:
+#pragma unroll
+        for (int i = 0; i < kJumpPer; i++) h[i] ^= jw<T>(cur, nxt, i);
+        break;
+    case 2:
+#pragma unroll
+        for (int i = 0; i < kJumpPer; i++) h[i] ^= jw<T + 1>(cur, nxt, i);
+        break;
+    case 4:
+#pragma unroll
+        for (int i = 0; i < kJumpPer; i++) h[i] ^= jw<T + 2>(cur, nxt, i);
+        break;
+    case 3:
+#pragma unroll
+        for (int i = 0; i < kJumpPer; i++) h[i] = xor3(h[i], jw<T>(cur, nxt, i), jw<T + 1>(cur, nxt, i));
+        break;
+    case 5:
+#pragma unroll
+        for (int i = 0; i < kJumpPer; i++) h[i] = xor3(h[i], jw<T>(cur, nxt, i), jw<T + 2>(cur, nxt, i));
+        break;
+    case 6:
+#pragma unroll
+        for (int i = 0; i < kJumpPer; i++)
+            h[i] = xor3(h[i], jw<T + 1>(cur, nxt, i), jw<T + 2>(cur, nxt, i));
+        break;
+    case 7:
+#pragma unroll
+        for (int i = 0; i < kJumpPer; i++)
+            h[i] ^= xor3(jw<T>(cur, nxt, i), jw<T + 1>(cur, nxt, i), jw<T + 2>(cur, nxt, i));
+        break;
+    default:
+        break;
+    }
+}
+
 __device__ __forceinline__ void jump_block(uint32_t (&h)[kJumpPer], const uint32_t (&cur)[kJumpPer],
                                            uint32_t (&nxt)[kJumpPer], const uint32_t *xs,
                                            uint32_t k0, int lane, uint32_t gb) {
 #pragma unroll
     for (int m = 0; m < kJumpPer; m++)
         nxt[m] = xs[(k0 + kJumpPer + kJumpPer * lane + m) & (kJumpRing - 1u)];
-#pragma unroll
-    for (int t = 0; t < kJumpPer; t++) {
-        if ((gb >> t) & 1u) {
-#pragma unroll
-            for (int i = 0; i < kJumpPer; i++)
-                h[i] ^= (t + i < kJumpPer) ? cur[t + i] : nxt[t + i - kJumpPer];
-        }
-    }
+    jump_triple<0>(h, cur, nxt, gb);
+    jump_triple<3>(h, cur, nxt, gb >> 3);
+    jump_triple<6>(h, cur, nxt, gb >> 6);
+    jump_triple<9>(h, cur, nxt, gb >> 9);
+    jump_triple<12>(h, cur, nxt, gb >> 12);
+    jump_triple<15>(h, cur, nxt, gb >> 15);
+    jump_triple<18>(h, cur, nxt, gb >> 18);
 }
 
 __global__ void __launch_bounds__(32 * kJumpWarps, 6)
@@ -295,21 +347,21 @@ __device__ __forceinline__ float ms_uniform(uint32_t x) {
 __device__ __forceinline__ void refill_spin_minstd(uint32_t spin, const RngState &G,
                                                    const uint32_t *__restrict__ ms_delta,
                                                    int lane) {
-    const uint32_t nc = G.ncnt[spin], nh = G.nhead[spin], uc = G.ucnt[spin];
-    if (nc < kNormBuf) {
+    const uint32_t nc = G.ncnt[spin], nh = G.nhead[spin], uc = G.ucnt[spin], nlen = G.nlen;
+    if (nc < nlen) {
         uint32_t x = G.p_r[spin];
-        float *nb = G.nbuf + (size_t)spin * kNormBuf;
-        const uint32_t K = kNormBuf - nc, wpos = nh + nc;
+        float *nb = G.nbuf + (size_t)spin * nlen;
+        const uint32_t K = nlen - nc, wpos = nh + nc;
         for (uint32_t b = 0; b < K; b += 32) {
             const uint32_t r = min(32u, K - b);
             if ((uint32_t)lane < r)
-                nb[(wpos + b + lane) % kNormBuf] =
+                nb[(wpos + b + lane) % nlen] =
                     ms_normal(ms_mulmod(x, c_ms_pow.v[lane]), ms_delta);
             x = ms_mulmod(x, c_ms_pow.v[r - 1]);
         }
         if (lane == 0) {
             G.p_r[spin] = x;
-            G.ncnt[spin] = kNormBuf;
+            G.ncnt[spin] = nlen;
         }
     }
     if (uc <= kUnifBuf / 2) {
@@ -419,25 +471,19 @@ __device__ __forceinline__ uint32_t block_word(const uint32_t *gst, const uint32
 }
 
 // Appends K polar pairs (normal_distribution<float>: y*m first, x*m saved for the next call) from
-// the mt19937 state gst at position p to the ring nb of RLEN deviates, from slot wpos (< 2 RLEN
-// before reduction) on; 32 candidate pairs per pass, accepted pairs compacted with a ballot.
-// `s` is the warp's 624-word shared block.
-template <uint32_t RLEN>
-__device__ __forceinline__ uint32_t ring_slot(uint32_t x) {
-    if constexpr ((RLEN & (RLEN - 1)) == 0) {
-        return x & (RLEN - 1);
-    } else {                                          // x < 3 RLEN
-        x -= x >= RLEN ? RLEN : 0u;
-        x -= x >= RLEN ? RLEN : 0u;
-        return x;
-    }
+// the mt19937 state gst at position p to the ring nb of rlen deviates, from slot wpos on (wpos +
+// 2 K < 3 rlen); 32 candidate pairs per pass, accepted pairs compacted with a ballot. `s` is the
+// warp's 624-word shared block.
+__device__ __forceinline__ uint32_t ring_slot(uint32_t x, uint32_t rlen) {   // x < 3 rlen
+    x -= x >= rlen ? rlen : 0u;
+    x -= x >= rlen ? rlen : 0u;
+    return x;
 }
 
-template <uint32_t RLEN>
 __device__ __forceinline__ void refill_normals_mt(uint32_t *gst, uint32_t &p, float *nb,
-                                                  uint32_t wpos, uint32_t K, uint32_t *s,
-                                                  const float *s_tab, const LogfTables &L,
-                                                  int lane) {
+                                                  uint32_t rlen, uint32_t wpos, uint32_t K,
+                                                  uint32_t *s, const float *s_tab,
+                                                  const LogfTables &L, int lane) {
     const unsigned lt_mask = (1u << lane) - 1u;
     uint32_t produced = 0;
     bool in_smem = false;
@@ -473,9 +519,9 @@ __device__ __forceinline__ void refill_normals_mt(uint32_t *gst, uint32_t &p, fl
         if (ok && rank < need) {
             const float lg = logf_libm(r2, s_tab, L);
             const float mult = __fsqrt_rn(__fdiv_rn(-2.0f * lg, r2));
-            const uint32_t pos = ring_slot<RLEN>(wpos + 2 * (produced + rank));
+            const uint32_t pos = ring_slot(wpos + 2 * (produced + rank), rlen);
             nb[pos] = y * mult;                                  // returned first
-            nb[pos + 1 == RLEN ? 0 : pos + 1] = x * mult;        // saved for the next call
+            nb[pos + 1 == rlen ? 0 : pos + 1] = x * mult;        // saved for the next call
         }
         const uint32_t nacc = __popc(bal);
         if (nacc <= need) {
@@ -520,12 +566,11 @@ __device__ __forceinline__ void refill_spin_mt(uint32_t spin, const RngState &G,
                                                const LogfTables &L, const float *s_tab,
                                                uint32_t *s, int lane) {
     const uint32_t nc = G.ncnt[spin];
-    const uint32_t K = (kNormBuf - nc) / 2;                 // pairs to add
+    const uint32_t K = (G.nlen - nc) / 2;                   // pairs to add
     if (K > 0) {
         uint32_t p = G.p_r[spin];
-        refill_normals_mt<kNormBuf>(G.mt_r + (size_t)spin * kMtN, p,
-                                    G.nbuf + (size_t)spin * kNormBuf, G.nhead[spin] + nc, K, s,
-                                    s_tab, L, lane);
+        refill_normals_mt(G.mt_r + (size_t)spin * kMtN, p, G.nbuf + (size_t)spin * G.nlen, G.nlen,
+                          G.nhead[spin] + nc, K, s, s_tab, L, lane);
         if (lane == 0) {
             G.p_r[spin] = p;
             G.ncnt[spin] = nc + 2 * K;
@@ -562,9 +607,10 @@ __global__ void __launch_bounds__(32 * kRefillWarps)
 }
 
 // Pooled generators (PoolState): one warp per stream tops its Gaussian ring up to the lowest
-// read position of the pairs that paused in the last walk plus kPoolNorm (whole pairs), and its
-// uniform ring likewise; streams no walking pair reported are skipped. The deviates of stream s
-// are those spin s draws in every instance of the batch.
+// read position of the pairs that paused in the last walk plus kPoolNorm (whole pairs); streams
+// no walking pair reported are skipped. The deviates of stream s are those spin s draws in every
+// instance of the batch. The pair with the lowest read position then has a full ring, so the
+// batch always makes progress.
 __global__ void __launch_bounds__(32 * kRefillWarps)
     k_refill_pool(PoolState Q, LogfTables L, uint32_t n_streams) {
     __shared__ float s_tab[192];
@@ -574,37 +620,44 @@ __global__ void __launch_bounds__(32 * kRefillWarps)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (uint32_t st = blockIdx.x * kRefillWarps + w; st < n_streams;
          st += gridDim.x * kRefillWarps) {
-        const uint32_t nm = Q.nmin[st], um = Q.umin[st];
-        if (nm == kPoolNone && um == kPoolNone) continue;
-        if (nm != kPoolNone) {
-            const uint32_t target = (nm + kPoolNorm) & ~1u, w0 = Q.nw[st];
-            if (target > w0) {
-                uint32_t p = Q.p_r[st];
-                refill_normals_mt<kPoolNorm>(Q.mt_r + (size_t)st * kMtN, p,
-                                             Q.nbuf + (size_t)st * kPoolNorm, w0 & (kPoolNorm - 1),
-                                             (target - w0) / 2, s_mt[w], s_tab, L, lane);
-                if (lane == 0) {
-                    Q.p_r[st] = p;
-                    Q.nw[st] = target;
-                }
+        const uint32_t nm = Q.nmin[st];
+        if (nm == kPoolNone) continue;
+        const uint32_t target = (nm + kPoolNorm) & ~1u, w0 = Q.nw[st];
+        if (target > w0) {
+            uint32_t p = Q.p_r[st];
+            refill_normals_mt(Q.mt_r + (size_t)st * kMtN, p, Q.nbuf + (size_t)st * kPoolNorm,
+                              kPoolNorm, w0 & (kPoolNorm - 1), (target - w0) / 2, s_mt[w], s_tab,
+                              L, lane);
+            if (lane == 0) {
+                Q.p_r[st] = p;
+                Q.nw[st] = target;
             }
         }
-        if (um != kPoolNone) {
-            const uint32_t target = um + kPoolUnif, w0 = Q.uw[st];
-            if (target > w0) {
-                uint32_t p = Q.p_u[st];
-                refill_uniforms_mt<kPoolUnif>(Q.mt_u + (size_t)st * kMtN, p,
-                                              Q.ubuf + (size_t)st * kPoolUnif, w0, target - w0,
-                                              s_mt[w], lane);
-                if (lane == 0) {
-                    Q.p_u[st] = p;
-                    Q.uw[st] = target;
-                }
-            }
-        }
-        if (lane == 0) {              // the next walk reports afresh
-            Q.nmin[st] = kPoolNone;
-            Q.umin[st] = kPoolNone;
+        if (lane == 0) Q.nmin[st] = kPoolNone;      // the next walk reports afresh
+        __syncwarp();
+    }
+}
+
+// The crossing uniforms of one instance of a pooled batch: each walking spin's own gen_u ring,
+// topped up when at most half full (as k_refill does for them).
+__global__ void __launch_bounds__(32 * kRefillWarps)
+    k_refill_uniforms(RngState G, const uint32_t *__restrict__ flags, uint32_t spin_lo,
+                      uint32_t spin_hi) {
+    __shared__ uint32_t s_mt[kRefillWarps][kMtN];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t spin = spin_lo + blockIdx.x * kRefillWarps + w; spin < spin_hi;
+         spin += gridDim.x * kRefillWarps) {
+        if (flags[spin] & kFlagDone) continue;
+        const uint32_t uc = G.ucnt[spin];
+        if (uc > kUnifBuf / 2) continue;
+        const uint32_t need = kUnifBuf - uc;
+        uint32_t p = G.p_u[spin];
+        refill_uniforms_mt<kUnifBuf>(G.mt_u + (size_t)spin * kMtN, p,
+                                     G.ubuf + (size_t)spin * kUnifBuf, G.uhead[spin] + uc, need,
+                                     s_mt[w], lane);
+        if (lane == 0) {
+            G.p_u[spin] = p;
+            G.ucnt[spin] = uc + need;
         }
         __syncwarp();
     }
@@ -638,8 +691,9 @@ __device__ __forceinline__ void signal_add(const Outputs &O, uint32_t key, const
 // ------------------------------------------------------------------------------------------
 // The walk (kernels.cu:107-232)
 // ------------------------------------------------------------------------------------------
-// POOL: the spin draws from the pooled stream of its id (PoolState Q) instead of its own rings;
-// G.nhead / G.uhead hold its read positions in that stream (absolute counts).
+// POOL: the spin draws its Gaussian steps from the pooled stream of its id (PoolState Q) instead
+// of its own ring, G.nhead holding its read position there (an absolute count); its crossing
+// uniforms come from its own ring as usual.
 template <int PREC, bool DBL, bool POOL = false>
 __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, const DevParams &P,
                                           const DevTables &Tb, const uint2 *__restrict__ vox,
@@ -665,25 +719,22 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
     bool started = (flags & kFlagStarted) != 0;
     double dscale = __ldg(Tb.dscale + ts_old);
 
-    constexpr uint32_t NLEN = POOL ? kPoolNorm : kNormBuf, ULEN = POOL ? kPoolUnif : kUnifBuf;
-    uint32_t nh, nc, uh, uc;
-    const float *nb, *ub;
+    const uint32_t NLEN = POOL ? kPoolNorm : G.nlen;
+    constexpr uint32_t ULEN = kUnifBuf;
+    uint32_t nh, nc;
+    const float *nb;
     if (POOL) {
-        const uint32_t nr = G.nhead[spin], ur = G.uhead[spin];
+        const uint32_t nr = G.nhead[spin];
         nc = Q.nw[spin] - nr;
-        uc = Q.uw[spin] - ur;
         nh = nr & (kPoolNorm - 1);
-        uh = ur & (kPoolUnif - 1);
         nb = Q.nbuf + (size_t)spin * kPoolNorm;
-        ub = Q.ubuf + (size_t)spin * kPoolUnif;
     } else {
         nh = G.nhead[spin];
         nc = G.ncnt[spin];
-        uh = G.uhead[spin];
-        uc = G.ucnt[spin];
-        nb = G.nbuf + (size_t)spin * kNormBuf;
-        ub = G.ubuf + (size_t)spin * kUnifBuf;
+        nb = G.nbuf + (size_t)spin * NLEN;
     }
+    uint32_t uh = G.uhead[spin], uc = G.ucnt[spin];
+    const float *ub = G.ubuf + (size_t)spin * kUnifBuf;
 
     constexpr uint32_t NONE = 0xffffffffu;
     const bool last_scan0 = ds == P.n_dummy_scan;
@@ -884,17 +935,14 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
     S.tp[spin] = tp; S.tp_old[spin] = tp_old; S.ds[spin] = ds; S.itr[spin] = itr;
     S.ctr[spin] = c_rf | (c_te << 16);
     S.ctr2[spin] = c_dph | (c_grad << 16);
-    if (POOL) {               // read positions: written counts minus what is left
-        const uint32_t nr = Q.nw[spin] - nc, ur = Q.uw[spin] - uc;
+    if (POOL) {               // read position: written count minus what is left
+        const uint32_t nr = Q.nw[spin] - nc;
         G.nhead[spin] = nr;
-        G.uhead[spin] = ur;
-        if (status < 0) {         // paused: the stream's next refill keeps what this pair needs
-            atomicMin(Q.nmin + spin, nr);
-            atomicMin(Q.umin + spin, ur);
-        }
+        if (status < 0) atomicMin(Q.nmin + spin, nr);   // the next refill keeps what it needs
     } else {
-        G.nhead[spin] = nh; G.ncnt[spin] = nc; G.uhead[spin] = uh; G.ucnt[spin] = uc;
+        G.nhead[spin] = nh; G.ncnt[spin] = nc;
     }
+    G.uhead[spin] = uh; G.ucnt[spin] = uc;
     uint32_t nf = ts_old | (started ? kFlagStarted : 0u);
     if (status >= 0) {
         nf |= kFlagDone | ((uint32_t)status << 16);
@@ -1073,6 +1121,14 @@ cudaError_t launch_refill_pool(const PoolState &Q, const LogfTables &L, uint32_t
     if (n_streams == 0) return cudaSuccess;
     k_refill_pool<<<grid_for(n_streams, kRefillWarps, 152 * 64), 32 * kRefillWarps, 0, st>>>(
         Q, L, n_streams);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refill_uniforms(const RngState &G, const uint32_t *flags, uint32_t lo,
+                                   uint32_t hi, cudaStream_t st) {
+    if (hi <= lo) return cudaSuccess;
+    k_refill_uniforms<<<grid_for(hi - lo, kRefillWarps, 152 * 64), 32 * kRefillWarps, 0, st>>>(
+        G, flags, lo, hi);
     return cudaGetLastError();
 }
 

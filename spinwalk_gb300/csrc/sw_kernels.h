@@ -29,10 +29,13 @@ cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevT
                               const uint2 *vox, const SpinState &S, const RngState &G,
                               const Outputs &O, uint32_t *active, uint32_t lo, uint32_t hi,
                               cudaStream_t st, const uint32_t *order = nullptr, int block = 256);
-// Pooled generators of a batch (PoolState): refill of streams [0, n_streams), and the walk of one
-// instance's spins [lo, hi) drawing from them (G.nhead / G.uhead: the instance's read positions).
+// Pooled Gaussian generators of a batch (PoolState): refill of streams [0, n_streams), the
+// refill of one instance's own crossing uniforms, and its walk over spins [lo, hi) drawing from
+// the streams (G.nhead: the instance's read positions in them).
 cudaError_t launch_refill_pool(const PoolState &Q, const LogfTables &L, uint32_t n_streams,
                                cudaStream_t st);
+cudaError_t launch_refill_uniforms(const RngState &G, const uint32_t *flags, uint32_t lo,
+                                   uint32_t hi, cudaStream_t st);
 cudaError_t launch_walk_pool_range(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
                                    const uint2 *vox, const SpinState &S, const RngState &G,
                                    const Outputs &O, const PoolState &Q, uint32_t *active,

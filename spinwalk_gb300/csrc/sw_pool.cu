@@ -1,19 +1,23 @@
-// Batches with pooled generators: sw_sim_batch when every instance shares the seed (which the
-// batch requires) and draws from std::mt19937.
+// Batches with pooled Gaussian generators: sw_sim_batch when every instance shares the seed
+// (which the batch requires) and draws from std::mt19937.
 //
 // The reference's scale loop runs one simulation per instance (src/sim/monte_carlo.cu:273-337)
 // and seeds every spin's generators anew each time: mt19937(seed + spin), discard(seed + spin)
 // (src/sim/kernels.cu:82-88). So spin s of every instance draws the SAME sequence of Gaussian
-// steps and crossing uniforms; instances differ only in how fast they consume it (rejected
-// crossings redraw, and the sequences differ). Here each spin id s is one "stream": one
-// generator pair and one ring of each kind (PoolState), seeded once and refilled once per round
-// for all instances together; every instance keeps only its own read positions. The refill work
-// of a batch is then that of its largest instance instead of the sum over instances.
+// steps; instances differ only in how fast they consume it (rejected crossings redraw, and the
+// sequences differ). Here each spin id s is one "stream": one gen_r and one ring of deviates
+// (PoolState), seeded once and refilled once per round for all instances together; every
+// instance keeps only its read positions. The Gaussian work of a batch -- three deviates per
+// step, most of a round's refill -- is then that of its largest instance instead of the sum over
+// instances. Each instance's spins keep their own gen_u (crossing uniforms, drawn only at
+// substrate changes), copied from the stream's seeded state: pooling both kinds could deadlock
+// (one spin waiting for uniforms a slower spin holds back, that one waiting for Gaussians the
+// first holds back), while with one pooled kind the slowest reader always gets a full ring.
 //
-// A round: k_refill_pool over the streams, then the walk of every instance (one launch each, on
-// kWalkStreams streams); a stream's ring is topped up to the lowest read position of the pairs
-// that paused in the previous walk plus the ring length, so nothing unread is overwritten.
-// Results equal one sw_sim call per instance bit for bit (tests/test_batch.py).
+// A round: k_refill_pool over the streams, then per instance its uniforms and its walk (one
+// launch each, on kWalkStreams streams); a stream's ring is topped up to the lowest read position
+// of the pairs that paused in the previous walk plus the ring length, so nothing unread is
+// overwritten. Results equal one sw_sim call per instance bit for bit (tests/test_batch.py).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -100,7 +104,7 @@ struct Inst {
     TableImage im;
     sw::DevParams P;
     sw::SpinState S;
-    sw::RngState G;                      // nhead / uhead: read positions in the streams
+    sw::RngState G;                      // nhead: read positions in the streams; own gen_u
     char *tables;
     // device I/O (offsets into the I/O region, same offsets in the pinned staging): the inputs
     // of all instances first, then their outputs
@@ -136,10 +140,8 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
         (void)vox;
         c.take<uint32_t>(4);                                  // active counter, bad-label flag
         c.take<uint32_t>(n_max * sw::kMtN);                  // mt_r
-        c.take<uint32_t>(n_max * sw::kMtN);                  // mt_u
-        for (int k = 0; k < 6; k++) c.take<uint32_t>(n_max);  // p_r p_u nw uw nmin umin
+        for (int k = 0; k < 3; k++) c.take<uint32_t>(n_max);  // p_r nw nmin
         c.take<float>(n_max * sw::kPoolNorm);
-        c.take<float>(n_max * sw::kPoolUnif);
         for (Inst &I : in) {
             const size_t n = I.n;
             I.tables = c.take<char>(I.im.bytes.size());
@@ -167,7 +169,11 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
             S.flags = c.take<uint32_t>(n);
             I.G = sw::RngState{};
             I.G.nhead = c.take<uint32_t>(n);
+            I.G.mt_u = c.take<uint32_t>(n * sw::kMtN);
+            I.G.p_u = c.take<uint32_t>(n);
+            I.G.ubuf = c.take<float>(n * sw::kUnifBuf);
             I.G.uhead = c.take<uint32_t>(n);
+            I.G.ucnt = c.take<uint32_t>(n);
         }
     };
     size_t io = 0;
@@ -250,15 +256,10 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
     uint32_t *cnt = c2.take<uint32_t>(4);
     sw::PoolState Q;
     Q.mt_r = c2.take<uint32_t>(n_max * sw::kMtN);
-    Q.mt_u = c2.take<uint32_t>(n_max * sw::kMtN);
     Q.p_r = c2.take<uint32_t>(n_max);
-    Q.p_u = c2.take<uint32_t>(n_max);
     Q.nw = c2.take<uint32_t>(n_max);
-    Q.uw = c2.take<uint32_t>(n_max);
     Q.nmin = c2.take<uint32_t>(n_max);
-    Q.umin = c2.take<uint32_t>(n_max);
     Q.nbuf = c2.take<float>(n_max * sw::kPoolNorm);
-    Q.ubuf = c2.take<float>(n_max * sw::kPoolUnif);
     char *d_io = X.d + state_bytes;
     cudaStream_t ms = X.main;
     uint32_t launches = 0;
@@ -297,19 +298,25 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
         sw::DevParams Ps{};
         Ps.seed = p0->seed;
         Ps.rng = SW_RNG_MT19937;
+        // k_seed writes the state twice (gen_r and gen_u start alike) and zeroes four ring
+        // counters per spin: here the stream's state, its written count and its lowest read
+        // position, which is where every stream starts
         sw::RngState Gs{};
-        Gs.mt_r = Q.mt_r;
-        Gs.mt_u = Q.mt_u;
-        Gs.p_r = Q.p_r;
-        Gs.p_u = Q.p_u;
-        // k_seed zeroes the ring counters of each spin: here the streams' written counts and
-        // their lowest read positions, which is where every stream starts
-        Gs.nhead = Q.nw;
-        Gs.ncnt = Q.uw;
-        Gs.uhead = Q.nmin;
-        Gs.ucnt = Q.umin;
+        Gs.mt_r = Gs.mt_u = Q.mt_r;
+        Gs.p_r = Gs.p_u = Q.p_r;
+        Gs.nhead = Gs.uhead = Q.nw;
+        Gs.ncnt = Gs.ucnt = Q.nmin;
         PL_CUDA(sw::launch_seed_range(Ps, Gs, 0, (uint32_t)n_max, ms, &jt));
         launches++;
+        // each instance's gen_u starts from the same seeded state, before any refill moves it
+        for (Inst &I : in) {
+            if (!I.n) continue;
+            PL_CUDA(cudaMemcpyAsync(I.G.mt_u, Q.mt_r, I.n * sw::kMtN * 4, cudaMemcpyDeviceToDevice, ms));
+            PL_CUDA(cudaMemcpyAsync(I.G.p_u, Q.p_r, I.n * 4, cudaMemcpyDeviceToDevice, ms));
+            PL_CUDA(cudaMemsetAsync(I.G.nhead, 0, I.n * 4, ms));
+            PL_CUDA(cudaMemsetAsync(I.G.uhead, 0, I.n * 4, ms));
+            PL_CUDA(cudaMemsetAsync(I.G.ucnt, 0, I.n * 4, ms));
+        }
     }
 
     // ---- instances: inputs (and the outputs' current contents) staged, uploaded, k_init ----
@@ -336,8 +343,6 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
                            I.nte ? reinterpret_cast<uint8_t *>(d_io + I.o_T) : nullptr,
                            reinterpret_cast<int32_t *>(d_io + I.o_st)};
         if (!I.n) continue;
-        PL_CUDA(cudaMemsetAsync(I.G.nhead, 0, I.n * 4, w0));
-        PL_CUDA(cudaMemsetAsync(I.G.uhead, 0, I.n * 4, w0));
         PL_CUDA(sw::launch_init_range(I.P, Tb[i], vox, reinterpret_cast<const float *>(d_io + I.o_M0),
                                       reinterpret_cast<const float *>(d_io + I.o_XYZ0), I.S, O[i],
                                       I.dbl, 0, (uint32_t)I.n, w0));
@@ -372,9 +377,11 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
         for (uint32_t i = 0; i < n_items; i++) {
             const Inst &I = in[i];
             if (!I.n) continue;
+            cudaStream_t ws = X.walk[i % kWalkStreams];
+            PL_CUDA(sw::launch_refill_uniforms(I.G, I.S.flags, 0, (uint32_t)I.n, ws));
             PL_CUDA(sw::launch_walk_pool_range(prec, I.dbl, I.P, Tb[i], vox, I.S, I.G, O[i], Q, cnt,
-                                               0, (uint32_t)I.n, X.walk[i % kWalkStreams]));
-            launches++;
+                                               0, (uint32_t)I.n, ws));
+            launches += 2;
         }
         for (int k = 0; k < kWalkStreams; k++) {
             PL_CUDA(cudaEventRecord(X.walked[k], X.walk[k]));

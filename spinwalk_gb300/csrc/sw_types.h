@@ -13,7 +13,7 @@ constexpr int kMtN = 624;                        // mt19937 state size (words)
 constexpr int kMtM = 397;
 
 // Ring buffers of generator output per spin (refilled between walk chunks).
-constexpr uint32_t kNormBuf = 768;               // Gaussian deviates: 256 steps x 3 axes
+constexpr uint32_t kNormBuf = 768;               // Gaussian deviates: 256 steps x 3 axes (default)
 constexpr uint32_t kUnifBuf = 128;               // uniform deviates for crossing attempts
 constexpr uint32_t kStepsPerRound = kNormBuf / 3;  // longest walk of one refill/walk round
 // Seeding: by default, spins whose discard count seed + spin reaches this jump ahead
@@ -23,18 +23,19 @@ constexpr uint32_t kStepsPerRound = kNormBuf / 3;  // longest walk of one refill
 constexpr uint64_t kJumpMinZ = 2304ull * 1024;
 constexpr int kMtDegreeDev = 19937;               // degree of mt19937's characteristic polynomial
 
-// Pooled generators of a batch whose instances share the seed: one generator pair and one ring
-// of each kind per spin id s (a "stream"), read by every instance's spin s at its own position.
-// Counts are absolute since seeding; ring slot = count % ring length.
+// Pooled Gaussian generators of a batch whose instances share the seed: one gen_r and one ring
+// of deviates per spin id s (a "stream"), read by every instance's spin s at its own position.
+// Counts are absolute since seeding; ring slot = count % kPoolNorm. (The crossing uniforms of
+// gen_u stay with each instance's spin: with two pooled rings, a spin waiting for uniforms held
+// back by a slower one could hold back that spin's Gaussians in turn.)
 constexpr uint32_t kPoolNorm = 1024;             // Gaussian deviates per stream
-constexpr uint32_t kPoolUnif = 256;              // crossing uniforms per stream
 constexpr uint32_t kPoolNone = 0xffffffffu;      // no walking pair reported a read position
 struct PoolState {
-    uint32_t *mt_r, *mt_u;    // [n_streams][624]
-    uint32_t *p_r, *p_u;      // next output index in the current block
-    float *nbuf, *ubuf;       // [n_streams][kPoolNorm], [n_streams][kPoolUnif]
-    uint32_t *nw, *uw;        // deviates written so far
-    uint32_t *nmin, *umin;    // lowest read position of the pairs that paused in the last walk
+    uint32_t *mt_r;           // [n_streams][624]
+    uint32_t *p_r;            // next output index in the current block
+    float *nbuf;              // [n_streams][kPoolNorm]
+    uint32_t *nw;             // deviates written so far
+    uint32_t *nmin;           // lowest read position of the pairs that paused in the last walk
 };
 
 // Spin flags word: bits 0-7 ts_old (substrate of the last accepted voxel), bit 8 "scan
@@ -115,10 +116,11 @@ struct SpinState {
 struct RngState {
     uint32_t *mt_r, *mt_u;    // [n][624]
     uint32_t *p_r, *p_u;      // next output index in the current 624-word block
-    float *nbuf;              // [n][kNormBuf]
+    float *nbuf;              // [n][nlen]
     uint32_t *nhead, *ncnt;
     float *ubuf;              // [n][kUnifBuf]
     uint32_t *uhead, *ucnt;
+    uint32_t nlen = kNormBuf; // Gaussian deviates per ring: 3 x the steps of one round
 };
 
 struct Outputs {

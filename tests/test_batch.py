@@ -52,13 +52,14 @@ def test_batch_equals_one_run_per_instance():
 @pytest.mark.gpu
 def test_batch_counts_its_work():
     """One pack + one seeding of the pooled generator streams, k_init per instance, then rounds
-    of one refill of the streams and one walk launch per instance; at least one round."""
+    of one refill of the streams and, per instance, a refill of its crossing uniforms and its
+    walk; at least one round."""
     probs = _instances()
     _lib.run_batch(probs)
     t = _lib.last_timing()
     busy = sum(1 for pr in probs if pr.params.n_spins)
     assert t["n_chunks"] >= 1
-    assert t["n_launches"] == 2 + busy + t["n_chunks"] * (1 + busy)
+    assert t["n_launches"] == 2 + busy + t["n_chunks"] * (1 + 2 * busy)
 
 
 def test_batch_rejects_mixed_seeds_and_phantoms():
@@ -101,7 +102,8 @@ def _rejecting_instances(n_inst=12, n=900, seed=31):
 @pytest.mark.parametrize("precision", [0, 1, 2])
 def test_pooled_streams_with_uneven_consumption_equal_one_run_per_instance(precision):
     """The pooled generator streams serve instances that reject crossings at different rates
-    (so their read positions drift apart within a round) and finish at different times."""
+    (so their read positions drift apart within a round, further than a ring holds) and finish
+    at different times."""
     probs = _rejecting_instances()
     batch = _lib.run_batch(probs, precision=precision, fill=np.nan)
     assert batch[0]["timing"]["n_chunks"] >= 2

@@ -106,3 +106,32 @@ def test_engine_results_same_alone_and_in_a_mix_of_arrivals():
         for key in ("M1", "XYZ1", "T", "status"):
             assert bits_equal(o[key], a[key]), (k, key)
     eng.close()
+
+
+def test_engine_evicts_idle_seed_caches_under_its_budget():
+    """Requests with distinct seeds each need their own generator-state cache (2.5 KB per spin);
+    under a small HBM budget the engine frees the caches no queued job uses, least recently used
+    first, instead of refusing the next request. Every result still equals its run alone."""
+    mask, field = cylinder_phantom(24, FOV, 4e-6, 0.12, seed=5)
+    gre = dict(TR_us=3050, TE_us=(3000,), timestep_us=50)
+    reqs = [Problem(mask, [FOV] * 3, field, n_spins=4000, seed=1000 + 17 * i, **gre)
+            for i in range(6)]
+    alone = [_lib.run(pr) for pr in reqs]
+    probe = _lib.Engine(n_slots=2, slot_spins=2048)
+    probe.add_phantom(reqs[0])
+    base = probe.stats()["hbm_used"]            # slots and the resident phantom
+    probe.close()
+    cache = 4000 * (624 * 4 + 4)                 # one seed cache of 4000 spins
+    eng = _lib.Engine(n_slots=2, slot_spins=2048, hbm_budget=base + int(2.5 * cache))
+    try:
+        pid = eng.add_phantom(reqs[0])
+        for pr, want in zip(reqs, alone):
+            _, out = eng.submit(pr, pid)
+            assert all(rc == 0 for _, rc, _ in eng.run_all())
+            for k in ("M1", "XYZ1", "T", "status"):
+                assert bits_equal(out[k], want[k]), k
+            st = eng.stats()
+            assert st["hbm_used"] <= st["hbm_budget"] and st["seed_caches"] <= 2
+        assert eng.stats()["seedings"] >= len(reqs)
+    finally:
+        eng.close()

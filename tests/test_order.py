@@ -17,13 +17,13 @@ def tuning():
 
 
 def test_tuning_roundtrip_and_validation(tuning):
-    tuning(3, 128, 5, 2, 7)
+    tuning(3, 128, 5, 2, 7, 300)
     want = dict(resort_interval=3, walk_block=128, seed_chunks=5, round_streams=2,
-                jump_min_kwords=7)
+                jump_min_kwords=7, ring_steps=300)
     assert _lib.get_tuning() == want
     for bad in (dict(resort_interval=1, walk_block=100), dict(resort_interval=1, walk_block=512),
                 dict(resort_interval=1 << 21, walk_block=256), dict(seed_chunks=65),
-                dict(round_streams=3)):
+                dict(round_streams=3), dict(ring_steps=31), dict(ring_steps=4097)):
         with pytest.raises(_lib.SpinWalkError):
             _lib.set_tuning(**bad)
     assert _lib.get_tuning() == want
@@ -91,15 +91,41 @@ def test_autotune_measures_every_candidate_and_applies(tuning):
     pr = _dense_problem(n_spins=50000)
     want = _lib.run(pr, fill=np.nan)
     best, table = _lib.autotune(pr, apply=True)
-    assert len(table) == 10
-    assert {(e["resort_interval"], e["walk_block"]) for e in table} == {
-        (i, b) for i in (0, 1, 2, 4, 8) for b in (128, 256)}
+    assert len(table) == 12
+    assert {(e["resort_interval"], e["walk_block"], e["ring_steps"]) for e in table} == {
+        (i, b, 256) for i in (0, 1, 2, 4, 8) for b in (128, 256)} | {(0, 256, 128), (0, 256, 512)}
     assert all(e["ms_per_round"] > 0 for e in table)
     fastest = min(table, key=lambda e: e["ms_per_round"])
     assert (best["resort_interval"], best["walk_block"]) == (fastest["resort_interval"],
                                                            fastest["walk_block"])
+    assert best["ring_steps"] == (0 if fastest["ring_steps"] == 256 else fastest["ring_steps"])
     assert _lib.get_tuning() == best
     _same(_lib.run(pr, fill=np.nan), want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["permeable", "se_multi_te", "lost_spins", "pgse_gradients",
+                                  "trajectory", "three_substrates", "bssfp_phase_cycling"])
+@pytest.mark.parametrize("ring_steps", [32, 100, 512, 4096])
+def test_sim_results_independent_of_ring_steps(tuning, case, ring_steps):
+    """Rounds of any length (the steps one refill of a spin's Gaussian ring lasts, an autotuner
+    candidate) give the results of the default 256-step rounds, in both generator flavours."""
+    pr, _ = load_golden(case)
+    for flavour in (0, 0x100):
+        want = _lib.run(pr, precision=flavour, fill=np.nan)
+        tuning(0, 256, 0, 0, 0, ring_steps)
+        got = _lib.run(pr, precision=flavour, fill=np.nan)
+        tuning()
+        _same(got, want)
+
+
+@pytest.mark.gpu
+def test_dense_ring_steps_with_halves_resort_and_shadow(tuning):
+    pr = _dense_problem(n_spins=150000)
+    want = _lib.run(pr, precision=2, fp64_shadow=True, fill=np.nan)
+    tuning(2, 128, 3, 2, 0, 77)
+    got = _lib.run(pr, precision=2, fp64_shadow=True, fill=np.nan)
+    _same(got, want, ("M1", "XYZ1", "T", "status", "M1_fp64"))
 
 
 @pytest.mark.gpu

@@ -59,6 +59,7 @@ MT_BYTES_PER_SPIN_STEP = 3.82 * 8        # MT words drawn per step x (4 B read +
 WALK_FP64_OPS_PER_SPIN_STEP = 6          # x, y, z step multiplies and position additions
 FP64_PEAK_GFLOPS = 152 * 2 * 2070e6 / 1e9  # 2 FP64 lanes per clock per SM at 2070 MHz
 WALK_DRAM_BYTES_PER_SPIN_STEP = 26.0
+SEED_LANE_INST_PER_WORD = 7.7            # ncu, k_seed: lane instructions per regenerated MT word
 SEED_LIMITER = ("integer instruction issue (ncu: ALU pipe 83 %, issue 74 %, DRAM 2 %): "
                 "7.7 lane instructions per MT word, not HBM")
 WALK_LIMITER = ("FP64 pipe (ncu: 64 %, 3 position additions + 3 step multiplies per step at 2 "
@@ -100,7 +101,7 @@ class Inputs:
         return _lib.initial_positions(fov, seed, n)
 
 
-def workload(name, rank=0, inputs=None):
+def workload(name, rank=0, inputs=None, seed=None):
     from spinwalk_gb300.problem import Problem
     inputs = inputs or Inputs()
     if name == "se":
@@ -149,7 +150,8 @@ def workload(name, rank=0, inputs=None):
         desc = dict(workload="small_se_300cubed_2e5spins_201tp", n_spins=n_spins, time_points=201)
     else:
         raise SystemExit(f"unknown workload {name}")
-    seed = 10 + 1_000_003 * rank          # each rank: its own disjoint spin population
+    if seed is None:
+        seed = 10 + 1_000_003 * rank      # each rank: its own disjoint spin population
     xyz0 = inputs.positions([fov] * 3, seed, n_spins)
     pr = Problem(mask, [fov] * 3, field, n_spins=n_spins, seed=seed, XYZ0=xyz0, **kw)
     return pr, desc
@@ -347,7 +349,7 @@ def run_reference(args, world, rank):
     oracle/libsynth.so and the oracle (the CUDA library is never loaded)."""
     if rank != 0:
         return
-    pr, desc = workload(args.workload, inputs=Inputs(oracle_side=True))
+    pr, desc = workload(args.workload, inputs=Inputs(oracle_side=True), seed=args.seed)
     rng = rng_flag(args)
     cores = os.cpu_count()
     n_sample = args.ref_sample
@@ -486,7 +488,7 @@ def leg_gre(args, local=0):
 # ------------------------------------------------------------------------------------------
 # Batched: the config-3 FoV sweep in one sw_sim_batch
 # ------------------------------------------------------------------------------------------
-def c3_instances(rank=0):
+def c3_instances(rank=0, max_spins=None):
     """Config 3: the config-1 phantom (200^3 random-orientation cylinders, r 5 um, 3 %), 32 FoV
     scales giving vessel radii 1-100 um (log-spaced; scale = r / 5 um, WHAT_TO_SCALE = 0) x
     {GRE, SE}; spins per instance log-uniform in [1e4, 1e6] (seed 3); TE = 5, 10, ..., 40 ms,
@@ -498,6 +500,8 @@ def c3_instances(rank=0):
     rng = np.random.default_rng(3)
     radii = np.logspace(0, 2, 32)
     spins = np.round(10 ** rng.uniform(4, 6, 64)).astype(int)
+    if max_spins:                      # a smaller case of the same sweep (profiling)
+        spins = np.minimum(spins, max_spins)
     te = tuple(range(5000, 40001, 5000))
     seqs = {"gre": dict(TR_us=40050, TE_us=te, timestep_us=50),
             "se": dict(TR_us=40050, TE_us=te, RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
@@ -527,7 +531,7 @@ def leg_batched(args, rank=0, world=1):
     host time around it (staging copies included; every call uploads the phantom and seeds
     again)."""
     from spinwalk_gb300 import _lib
-    probs, desc = c3_instances(rank)
+    probs, desc = c3_instances(rank, args.max_spins)
     tuning = apply_tuning(args, max(probs, key=lambda q: q.params.n_spins))
     steps = sum(p.spin_steps() for p in probs)
     reps = max(3, min(args.steps, 5))
@@ -825,7 +829,7 @@ def run_ours(args, world, rank, local):
     from spinwalk_gb300 import _lib, abi
 
     torch.cuda.set_device(local)
-    pr, desc = workload(args.workload, rank)
+    pr, desc = workload(args.workload, rank, seed=args.seed)
     tuning = apply_tuning(args, pr)
     p = pr.params
     n = p.n_spins
@@ -866,6 +870,19 @@ def run_ours(args, world, rank, local):
                  "peak_source": peak_kind, "limiter": WALK_LIMITER}
     for rf in (seed_roof, walk_roof):
         rf["frac"] = rf["achieved"] / peak
+    # the seeding's own ceiling is instruction issue: the words its discards regenerate (624 per
+    # regeneration, mt_discard_twists), at the measured instructions per word, against 4 warp
+    # instructions per SM clock
+    z = int(p.seed) + np.arange(n, dtype=np.int64)
+    regen_words = float(624 * np.where(z > 0, 1 + (z - 1) // 624, 0).sum())
+    sm_hz = (clocks.get("sm_mhz") or 2070.0) * 1e6 if clocks else 2070e6
+    issue_peak = 152 * 4 * sm_hz
+    issued = regen_words * SEED_LANE_INST_PER_WORD / 32 / seed_launch_s
+    seed_roof["issue_roofline"] = {"achieved_warp_inst_per_s": issued, "peak": issue_peak,
+                                   "frac": issued / issue_peak, "regenerated_words": regen_words,
+                                   "note": "words x 7.7 lane instructions (ncu) / 32 per warp "
+                                           "instruction, against 4 warp instructions per SM "
+                                           "clock at the sampled SM clock"}
     roof = {"seed+init+pack": seed_roof, "walk": walk_roof}.get(dominant, walk_roof)
     # walk-only rate: the call's wall time minus its seeding stage (the kernel times of the two
     # halves of the rounds overlap, so their sum would overstate it)
@@ -1045,6 +1062,11 @@ def main():
                     help="spin ids of the GPU arm's CPU baseline (stratified over the range)")
     ap.add_argument("--ref-sample", type=int, default=32768,
                     help="spin ids per step of the CPU reference arm (stratified)")
+    ap.add_argument("--seed", type=int, default=None,
+                    help="plain workloads: simulation seed (default 10; a large one makes the "
+                         "seeding jump ahead)")
+    ap.add_argument("--max-spins", type=int, default=None,
+                    help="c3 workload: cap on the spins of every instance (a smaller case)")
     ap.add_argument("--requests", type=int, default=100, help="served leg: trace length")
     ap.add_argument("--distinct-requests", type=int, default=20,
                     help="served leg: requests of the distinct-seed pass")

@@ -386,14 +386,17 @@ def apply_tuning(args, pr=None):
         info = {"autotuned": True, "probe_s": time.perf_counter() - t0, "table": table}
     if args.resort_interval is not None or args.walk_block is not None or \
             args.seed_chunks is not None or args.round_streams is not None or \
-            args.jump_min_kwords is not None or args.ring_steps is not None:
+            args.jump_min_kwords is not None or args.ring_steps is not None or \
+            args.walk_blocks_per_sm is not None:
         cur = _lib.get_tuning()
         _lib.set_tuning(cur["resort_interval"] if args.resort_interval is None else args.resort_interval,
                         cur["walk_block"] if args.walk_block is None else args.walk_block,
                         cur["seed_chunks"] if args.seed_chunks is None else args.seed_chunks,
                         cur["round_streams"] if args.round_streams is None else args.round_streams,
                         cur["jump_min_kwords"] if args.jump_min_kwords is None else args.jump_min_kwords,
-                        cur["ring_steps"] if args.ring_steps is None else args.ring_steps)
+                        cur["ring_steps"] if args.ring_steps is None else args.ring_steps,
+                        cur["walk_blocks_per_sm"] if args.walk_blocks_per_sm is None
+                        else args.walk_blocks_per_sm)
     info["applied"] = _lib.get_tuning()
     return info
 
@@ -1085,6 +1088,8 @@ def main():
                     help="refill/walk rounds as this many independent halves on own streams (1, 2)")
     ap.add_argument("--seed-chunks", type=int, default=None,
                     help="seed/walk pipeline chunks (1 = seed all first, 0 = auto)")
+    ap.add_argument("--walk-blocks-per-sm", type=int, default=None,
+                    help="cap on the walk kernel's blocks per SM (0 = none)")
     ap.add_argument("--ring-steps", type=int, default=None,
                     help="walk steps per refill/walk round (0 = default 256)")
     ap.add_argument("--jump-min-kwords", type=int, default=None,

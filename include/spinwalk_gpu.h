@@ -343,6 +343,9 @@ int sw_last_timing(sw_timing *out);
  *                     of one refill/walk round and of one walk launch; 0 = default (256),
  *                     else 32 .. 4096. Longer rings mean fewer rounds and launches but more
  *                     ring memory (12 B per step per spin) between refill and walk.
+ *   walk_blocks_per_sm : sw_sim / sw_sim_device: caps the walk launch at this many blocks per
+ *                     SM, the blocks striding over the spins, so that the other half's refill
+ *                     can run beside it on every SM; 0 = default (no cap, one thread per spin).
  */
 typedef struct sw_tuning {
     uint32_t resort_interval;
@@ -351,7 +354,8 @@ typedef struct sw_tuning {
     uint32_t round_streams;
     uint32_t jump_min_kwords;
     uint32_t ring_steps;
-    uint32_t reserved[2];
+    uint32_t walk_blocks_per_sm;
+    uint32_t reserved[1];
 } sw_tuning;
 int sw_set_tuning(const sw_tuning *t);
 int sw_get_tuning(sw_tuning *t);

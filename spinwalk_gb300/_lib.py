@@ -226,22 +226,24 @@ def run_config(ini_path, device=0):
 
 
 def set_tuning(resort_interval=0, walk_block=256, seed_chunks=0, round_streams=0,
-               jump_min_kwords=0, ring_steps=0):
+               jump_min_kwords=0, ring_steps=0, walk_blocks_per_sm=0):
     """sw_set_tuning: Morton re-sort interval (walk rounds, 0 = never), walk block size, seed
     chunks of the seed/walk pipeline (0 = auto), round halves (0 = auto), the discard count
     from which seeding jumps ahead (in 1024 words, 0 = default 2304) and the steps of one
-    refill/walk round (0 = default 256) for every later call of this process. Results do not
-    depend on it."""
+    refill/walk round (0 = default 256) and a cap on the walk's blocks per SM (0 = none) for
+    every later call of this process. Results do not depend on it."""
     t = abi.SwTuning(resort_interval=int(resort_interval), walk_block=int(walk_block),
                      seed_chunks=int(seed_chunks), round_streams=int(round_streams),
-                     jump_min_kwords=int(jump_min_kwords), ring_steps=int(ring_steps))
+                     jump_min_kwords=int(jump_min_kwords), ring_steps=int(ring_steps),
+                     walk_blocks_per_sm=int(walk_blocks_per_sm))
     check(lib().sw_set_tuning(C.byref(t)))
 
 
 def _tuning_dict(t):
     return dict(resort_interval=t.resort_interval, walk_block=t.walk_block,
                 seed_chunks=t.seed_chunks, round_streams=t.round_streams,
-                jump_min_kwords=t.jump_min_kwords, ring_steps=t.ring_steps)
+                jump_min_kwords=t.jump_min_kwords, ring_steps=t.ring_steps,
+                walk_blocks_per_sm=t.walk_blocks_per_sm)
 
 
 def get_tuning():

@@ -135,7 +135,8 @@ class SwTuning(C.Structure):
         ("round_streams", C.c_uint32),
         ("jump_min_kwords", C.c_uint32),
         ("ring_steps", C.c_uint32),
-        ("reserved", C.c_uint32 * 2),
+        ("walk_blocks_per_sm", C.c_uint32),
+        ("reserved", C.c_uint32 * 1),
     ]
 
 

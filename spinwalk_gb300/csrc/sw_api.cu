@@ -319,7 +319,7 @@ int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
         }
         SW_CUDA(sw::launch_walk_range(precision, dbl, P, Tb, L.vox, L.S, L.G, O, L.active + 2 * h,
                                       lo, hi, st, tu.resort_interval ? L.Q.order : nullptr,
-                                      (int)tu.walk_block));
+                                      (int)tu.walk_block, walk_grid_cap(tu)));
         if (t) SW_CUDA(cudaEventRecord(e[2], st));
         if (t) timed++;
         launches += 2;
@@ -504,8 +504,22 @@ sw::LogfTables sw::api::device_logf_tables() {
 
 namespace {
 std::mutex g_tune_mu;
-sw_tuning g_tune{0u, 256u, 0u, 0u, 0u, 0u, {0u, 0u}};
+sw_tuning g_tune{0u, 256u, 0u, 0u, 0u, 0u, 0u, {0u}};
 }  // namespace
+
+int sw::api::walk_grid_cap(const sw_tuning &t) {
+    if (!t.walk_blocks_per_sm) return 0;
+    static int sms = [] {
+        int dev = 0, n = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            return 152;
+        }
+        return n;
+    }();
+    return (int)t.walk_blocks_per_sm * sms;
+}
 
 int sw::api::jump_table(uint64_t seed, uint32_t lo, uint32_t hi, uint64_t z_min, uint32_t *&buf,
                         size_t &buf_words, sw::JumpTable &jt) {
@@ -557,6 +571,7 @@ int sw_set_tuning(const sw_tuning *t) {
     if (t->resort_interval > 1u << 20) return fail(SW_ERR_INVALID, "resort_interval too large");
     if (t->seed_chunks > kMaxSeedChunks) return fail(SW_ERR_INVALID, "seed_chunks > 64");
     if (t->round_streams > 2) return fail(SW_ERR_INVALID, "round_streams must be 0, 1 or 2");
+    if (t->walk_blocks_per_sm > 16) return fail(SW_ERR_INVALID, "walk_blocks_per_sm must be 0 .. 16");
     if (t->ring_steps != 0 && (t->ring_steps < 32 || t->ring_steps > 4096))
         return fail(SW_ERR_INVALID, "ring_steps must be 0 (default) or 32 .. 4096");
     std::lock_guard<std::mutex> lk(g_tune_mu);

@@ -63,6 +63,8 @@ struct Layout {
 
 // Process-wide tuning of the walk (sw_set_tuning / sw_autotune), read at the start of a call.
 sw_tuning current_tuning();
+// Grid cap of the walk kernel under tuning t (0: one thread per spin, no cap).
+int walk_grid_cap(const sw_tuning &t);
 // Gaussian deviates per ring (3 per step of a round) under tuning t.
 inline uint32_t ring_len(const sw_tuning &t) { return 3u * (t.ring_steps ? t.ring_steps : kNormBuf / 3); }
 // The discard count from which seeding jumps ahead under tuning t (at least 624).

@@ -963,15 +963,22 @@ __global__ void __launch_bounds__(256, 4)
     k_walk(DevParams P, DevTables Tb, const uint2 *__restrict__ vox, SpinState S, RngState G,
            Outputs O, uint32_t *active, uint32_t spin_lo, uint32_t spin_hi,
            const uint32_t *__restrict__ order) {
-    const uint32_t i = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
-    bool still = false;
-    if (i < spin_hi) {
-        const uint32_t spin = order ? __ldg(order + i) : i;
-        const uint32_t flags = S.flags[spin];
-        if (!(flags & kFlagDone)) still = walk_spin<PREC, DBL>(spin, flags, P, Tb, vox, S, G, O);
+    // grid-stride by whole warps: a grid smaller than the spins (a cap on blocks per SM) leaves
+    // room on each SM for the other half's refill
+    const uint32_t stride = gridDim.x * blockDim.x, lane = threadIdx.x & 31u;
+    uint32_t paused = 0;
+    for (uint32_t base = spin_lo + blockIdx.x * blockDim.x + (threadIdx.x - lane);
+         base < spin_hi; base += stride) {
+        const uint32_t i = base + lane;
+        bool still = false;
+        if (i < spin_hi) {
+            const uint32_t spin = order ? __ldg(order + i) : i;
+            const uint32_t flags = S.flags[spin];
+            if (!(flags & kFlagDone)) still = walk_spin<PREC, DBL>(spin, flags, P, Tb, vox, S, G, O);
+        }
+        paused += __popc(__ballot_sync(0xffffffffu, still));
     }
-    const unsigned b = __ballot_sync(0xffffffffu, still);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(active, (uint32_t)__popc(b));
+    if (lane == 0 && paused) atomicAdd(active, paused);
 }
 
 // The walk of one instance of a pooled batch: spins [spin_lo, spin_hi), generators from Q.
@@ -1099,10 +1106,10 @@ cudaError_t launch_walk(int prec, bool dbl, const DevParams &P, const DevTables 
 cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
                               const uint2 *vox, const SpinState &S, const RngState &G,
                               const Outputs &O, uint32_t *active, uint32_t lo, uint32_t hi,
-                              cudaStream_t st, const uint32_t *order, int block) {
+                              cudaStream_t st, const uint32_t *order, int block, int max_blocks) {
     if (hi <= lo) return cudaSuccess;
     if (block != 64 && block != 128 && block != 256) return cudaErrorInvalidValue;
-    const int g = grid_for(hi - lo, block, 1 << 30);
+    const int g = grid_for(hi - lo, block, max_blocks > 0 ? max_blocks : 1 << 30);
     if (prec == SW_PREC_FP64)
         k_walk<SW_PREC_FP64, true><<<g, block, 0, st>>>(P, Tb, vox, S, G, O, active, lo, hi, order);
     else if (prec == SW_PREC_KAHAN && dbl)

@@ -24,11 +24,13 @@ cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo
                               cudaStream_t st, const JumpTable *jt = nullptr);
 cudaError_t launch_refill_range(const DevParams &P, const RngState &G, const uint32_t *flags,
                                 const LogfTables &L, uint32_t lo, uint32_t hi, cudaStream_t st);
-// order: walk order of the spins (null = id order); block: threads per block (64..256).
+// order: walk order of the spins (null = id order); block: threads per block (64..256);
+// max_blocks > 0 caps the grid (the blocks then stride over the spins).
 cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
                               const uint2 *vox, const SpinState &S, const RngState &G,
                               const Outputs &O, uint32_t *active, uint32_t lo, uint32_t hi,
-                              cudaStream_t st, const uint32_t *order = nullptr, int block = 256);
+                              cudaStream_t st, const uint32_t *order = nullptr, int block = 256,
+                              int max_blocks = 0);
 // Pooled Gaussian generators of a batch (PoolState): refill of streams [0, n_streams), the
 // refill of one instance's own crossing uniforms, and its walk over spins [lo, hi) drawing from
 // the streams (G.nhead: the instance's read positions in them).

@@ -17,13 +17,14 @@ def tuning():
 
 
 def test_tuning_roundtrip_and_validation(tuning):
-    tuning(3, 128, 5, 2, 7, 300)
+    tuning(3, 128, 5, 2, 7, 300, 3)
     want = dict(resort_interval=3, walk_block=128, seed_chunks=5, round_streams=2,
-                jump_min_kwords=7, ring_steps=300)
+                jump_min_kwords=7, ring_steps=300, walk_blocks_per_sm=3)
     assert _lib.get_tuning() == want
     for bad in (dict(resort_interval=1, walk_block=100), dict(resort_interval=1, walk_block=512),
                 dict(resort_interval=1 << 21, walk_block=256), dict(seed_chunks=65),
-                dict(round_streams=3), dict(ring_steps=31), dict(ring_steps=4097)):
+                dict(round_streams=3), dict(ring_steps=31), dict(ring_steps=4097),
+                dict(walk_blocks_per_sm=17)):
         with pytest.raises(_lib.SpinWalkError):
             _lib.set_tuning(**bad)
     assert _lib.get_tuning() == want
@@ -166,3 +167,14 @@ def test_sim_results_independent_of_round_streams(tuning, case, chunks):
     got = _lib.run(pr, fill=np.nan)
     _same(got, want)
 
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cap", [1, 2, 3])
+def test_dense_walk_grid_cap(tuning, cap):
+    """A capped walk grid (blocks striding over the spins) walks every spin as the full grid."""
+    pr = _dense_problem(n_spins=150000)
+    want = _lib.run(pr, precision=2, fp64_shadow=True, fill=np.nan)
+    tuning(0, 256, 1, 2, 0, 0, cap)
+    got = _lib.run(pr, precision=2, fp64_shadow=True, fill=np.nan)
+    _same(got, want, ("M1", "XYZ1", "T", "status", "M1_fp64"))

@@ -52,13 +52,13 @@ UNIT = "spin-steps/s"
 GATHER_BYTES_PER_SPIN_STEP = 32   # one DRAM sector per random voxel lookup (mask + field record)
 USEFUL_BYTES_PER_SPIN_STEP = 5    # 1 B mask + 4 B field at the visited voxel
 SEED_BYTES_PER_SPIN = 2 * 624 * 4 + 6 * 4   # two mt19937 states + 6 ring/index words written
-# DRAM traffic per unit from ncu on the small SE case (profiles/kernels_small_se_300cubed_2e5spins.md),
+# DRAM traffic per unit from ncu on the small SE case (profiles/launches_small_se_300cubed_2e5spins.md),
 # scaled to a full launch by the units it processes (both grow in proportion)
-SEED_DRAM_BYTES_PER_SPIN = 4713.0
+SEED_DRAM_BYTES_PER_SPIN = 4704.0
 MT_BYTES_PER_SPIN_STEP = 3.82 * 8        # MT words drawn per step x (4 B read + 4 B write)
 WALK_FP64_OPS_PER_SPIN_STEP = 6          # x, y, z step multiplies and position additions
 FP64_PEAK_GFLOPS = 152 * 2 * 2070e6 / 1e9  # 2 FP64 lanes per clock per SM at 2070 MHz
-WALK_DRAM_BYTES_PER_SPIN_STEP = 26.0
+WALK_DRAM_BYTES_PER_SPIN_STEP = 24.5
 SEED_LANE_INST_PER_WORD = 7.7            # ncu, k_seed: lane instructions per regenerated MT word
 SEED_LIMITER = ("integer instruction issue (ncu: ALU pipe 83 %, issue 74 %, DRAM 2 %): "
                 "7.7 lane instructions per MT word, not HBM")

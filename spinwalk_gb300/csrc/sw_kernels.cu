@@ -247,11 +247,13 @@ __global__ void __launch_bounds__(32 * kJumpWarps, 6)
             h[i] = 0;
             A[i] = xs[(kJumpPer * lane + i) & M];
         }
-        for (uint32_t k0 = 0; k0 < (uint32_t)kMtDegreeDev; k0 += 2 * kJumpPer) {
+        // one block body per iteration (the next block's words move into A): the unrolled
+        // body is large, and two alternating copies of it stalled on instruction fetch
+        for (uint32_t k0 = 0; k0 < (uint32_t)kMtDegreeDev; k0 += kJumpPer) {
             generate_to(k0 + kJumpAhead);
             jump_block(h, A, B, xs, k0, lane, jump_bits(g, k0));
-            generate_to(k0 + kJumpPer + kJumpAhead);
-            jump_block(h, B, A, xs, k0 + kJumpPer, lane, jump_bits(g, k0 + kJumpPer));
+#pragma unroll
+            for (int m = 0; m < kJumpPer; m++) A[m] = B[m];
         }
         __syncwarp();
 #pragma unroll

@@ -1091,7 +1091,7 @@ def main():
     ap.add_argument("--walk-blocks-per-sm", type=int, default=None,
                     help="cap on the walk kernel's blocks per SM (0 = none)")
     ap.add_argument("--ring-steps", type=int, default=None,
-                    help="walk steps per refill/walk round (0 = default 256)")
+                    help="walk steps per refill/walk round (0 = default 512)")
     ap.add_argument("--jump-min-kwords", type=int, default=None,
                     help="seeding jumps ahead from this discard count (x 1024 words; 0 = default)")
     args = ap.parse_args()

@@ -340,7 +340,7 @@ int sw_last_timing(sw_timing *out);
  *                     src/sim/kernels.cu:87-88).
  *   ring_steps      : sw_sim / sw_sim_device / sw_sim_spins / sw_sim_signal: walk steps one
  *                     refill of a spin's Gaussian ring lasts (3 deviates each), i.e. the steps
- *                     of one refill/walk round and of one walk launch; 0 = default (256),
+ *                     of one refill/walk round and of one walk launch; 0 = default (512),
  *                     else 32 .. 4096. Longer rings mean fewer rounds and launches but more
  *                     ring memory (12 B per step per spin) between refill and walk.
  *   walk_blocks_per_sm : sw_sim / sw_sim_device: caps the walk launch at this many blocks per

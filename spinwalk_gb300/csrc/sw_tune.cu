@@ -220,7 +220,7 @@ extern "C" int sw_autotune(const sw_params *param, const sw_sequence *seq, const
     sw_tuning t = current_tuning();
     t.resort_interval = cand[bi].resort_interval;
     t.walk_block = cand[bi].walk_block;
-    t.ring_steps = cand[bi].ring_steps == def_steps ? 0u : cand[bi].ring_steps;
+    t.ring_steps = cand[bi].ring_steps;
     *best = t;
     if (table)
         for (uint32_t i = 0; i < std::min<size_t>(table_len, cand.size()); i++) table[i] = cand[i];

@@ -99,7 +99,7 @@ def test_autotune_measures_every_candidate_and_applies(tuning):
     fastest = min(table, key=lambda e: e["ms_per_round"])
     assert (best["resort_interval"], best["walk_block"]) == (fastest["resort_interval"],
                                                            fastest["walk_block"])
-    assert best["ring_steps"] == (0 if fastest["ring_steps"] == 256 else fastest["ring_steps"])
+    assert best["ring_steps"] == fastest["ring_steps"]
     assert _lib.get_tuning() == best
     _same(_lib.run(pr, fill=np.nan), want)
 
@@ -107,10 +107,10 @@ def test_autotune_measures_every_candidate_and_applies(tuning):
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", ["permeable", "se_multi_te", "lost_spins", "pgse_gradients",
                                   "trajectory", "three_substrates", "bssfp_phase_cycling"])
-@pytest.mark.parametrize("ring_steps", [32, 100, 512, 4096])
+@pytest.mark.parametrize("ring_steps", [32, 100, 256, 4096])
 def test_sim_results_independent_of_ring_steps(tuning, case, ring_steps):
     """Rounds of any length (the steps one refill of a spin's Gaussian ring lasts, an autotuner
-    candidate) give the results of the default 256-step rounds, in both generator flavours."""
+    candidate) give the results of the default rounds, in both generator flavours."""
     pr, _ = load_golden(case)
     for flavour in (0, 0x100):
         want = _lib.run(pr, precision=flavour, fill=np.nan)

@@ -777,6 +777,9 @@ def leg_served(args, rank=0, world=1):
     with ClockSampler(0) as clk:
         warm_s, warm_lat, warm_st = play_trace(eng, reqs, arrivals, submit)
     clocks = clk.summary()
+    # capacity: the same requests all submitted at once (the 20 / s trace offers less work per
+    # second than the engine can do, so its rate is bounded by the arrivals)
+    sat_s, sat_lat, sat_st = play_trace(eng, reqs, np.zeros(n_req), submit)
     # distinct seeds: the first requests of the trace, each with its own random 32-bit seed (what
     # SEED = 0 draws, simulation_parameters.cuh:233-234) and its own start positions, so no
     # request can use another's generator states
@@ -804,6 +807,10 @@ def leg_served(args, rank=0, world=1):
                      "latency_s": _lat(cold_lat), "seedings": cold_st["seedings"],
                      "note": "first pass of the trace on a new engine: every generator state "
                              "is computed inside the trace, when a request first needs it"},
+            "saturated": {"value": world * steps / sat_s, "makespan_s": sat_s,
+                          "latency_s": _lat(sat_lat),
+                          "note": "the same %d requests submitted at once: the engine's "
+                                  "capacity on this mix (latency is queueing)" % n_req},
             "distinct_seeds": {"value": world * dsteps / dist_s, "makespan_s": dist_s,
                                "requests": len(dreqs), "spin_steps": int(dsteps),
                                "spins": int(sum(p.params.n_spins for p in dreqs)),
@@ -951,6 +958,7 @@ def run_ours(args, world, rank, local):
         line["batched_over_plain"] = legs["batched"]["value"] / value
         line["served_over_plain"] = legs["served"]["value"] / value
         line["served_cold_over_plain"] = legs["served"]["cold"]["value"] / value
+        line["served_capacity_over_plain"] = legs["served"]["saturated"]["value"] / value
         line["tracks_over_plain"] = legs["tracks"]["value"] / value
         line["ratios_note"] = ("leg value / headline value (plain kernel on the spin-echo "
                                "workload); each leg also carries its ratio to the plain kernel "

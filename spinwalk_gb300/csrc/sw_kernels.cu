@@ -120,15 +120,24 @@ __global__ void __launch_bounds__(32 * kSeedWarps)
 // discard(z)) and g = x^J mod phi (host-computed, one per R), the state after J words is
 // h_j = XOR over k with g_k = 1 of x[k + j], j < 624, over the spin's own output sequence x.
 // One warp per spin: lane l accumulates h_j for the 21 words j = 21 l + i in registers; x lives
-// in a 1024-word ring in shared memory, generated 32 words at a time ahead of use. Each lane
-// slides a window of 42 registers (the current and the next block of 21 sequence words) along
-// x, so a step k reads one new word per lane instead of 21; the XOR of a window is a uniform
-// branch on g_k. The block of regeneration R is then h_1 .. h_623 plus one more word.
+// in a 1024-word ring in shared memory, generated 224 words at a time ahead of use. A block of
+// 21 steps k0 .. k0 + 20 needs x[k0 + 21 l + m], m < 42, in each lane: the window of step s is
+// m = s .. s + 20, and the XOR of a window is a uniform branch on g_k. The first 64 ring slots
+// are mirrored past its end, so that a lane's 42 words are read at one base address plus
+// immediate offsets (no per-word wrap). The block of regeneration R is then h_1 .. h_623 plus
+// one more word.
 // ------------------------------------------------------------------------------------------
 constexpr int kJumpWarps = 4;
 constexpr uint32_t kJumpRing = 1024;      // sequence words per warp in shared memory
+constexpr uint32_t kJumpMirror = 64;      // ring slots copied past the end
 constexpr int kJumpPer = 21;              // state words per lane: 32 x 21 = 672 >= 624
-constexpr uint32_t kJumpAhead = kJumpPer + kJumpPer * 31 + kJumpPer;   // sequence needed past k0
+constexpr int kJumpWin = 2 * kJumpPer;    // sequence words a lane reads per block
+constexpr uint32_t kJumpAhead = kJumpPer * 31 + kJumpWin;   // sequence needed past k0
+constexpr uint32_t kJumpGen = 224;        // words per generation: 7 per lane, all independent
+                                          // (x[n] reads x[n - 227] < the chunk's first word)
+static_assert(kJumpGen <= 227, "a generation chunk must not read its own words");
+static_assert(kJumpAhead + kJumpGen <= kJumpRing, "ring too short for the window");
+static_assert(kJumpWin <= (int)kJumpMirror, "mirror too short for one window");
 
 // Bits k0 .. k0 + 20 of the jump polynomial (624 words; bits past 19936 are zero).
 __device__ __forceinline__ uint32_t jump_bits(const uint32_t *__restrict__ g, uint32_t k0) {
@@ -144,74 +153,49 @@ __device__ __forceinline__ uint32_t xor3(uint32_t a, uint32_t b, uint32_t c) {
     return r;
 }
 
-// Steps k0 .. k0 + 20: cur holds x[k0 + 21 lane + m], nxt is loaded with the next block
-// x[k0 + 21 + 21 lane + m]; window element i of step t is cur[t + i] or nxt[t + i - 21]. The
-// steps go three at a time on their three polynomial bits: two windows are added with one
+// Steps T .. T + 2 of a block on their three polynomial bits: two windows are added with one
 // three-input xor, so a triple costs one operation per word on average instead of 1.5.
 template <int T>
-__device__ __forceinline__ uint32_t jw(const uint32_t (&cur)[kJumpPer], const uint32_t (&nxt)[kJumpPer],
-                                       int i) {
-    return (T + i < kJumpPer) ? cur[T + i] : nxt[T + i - kJumpPer];
-}
-
-template <int T>
-__device__ __forceinline__ void jump_triple(uint32_t (&h)[kJumpPer], const uint32_t (&cur)[kJumpPer],
-                                            const uint32_t (&nxt)[kJumpPer], uint32_t bits) {
+__device__ __forceinline__ void jump_triple(uint32_t (&h)[kJumpPer], const uint32_t (&W)[kJumpWin],
+                                            uint32_t bits) {
     switch (bits & 7u) {
     case 1:
 #pragma unroll
-        for (int i = 0; i < kJumpPer; i++) h[i] ^= jw<T>(cur, nxt, i);
+        for (int i = 0; i < kJumpPer; i++) h[i] ^= W[T + i];
         break;
     case 2:
 #pragma unroll
-        for (int i = 0; i < kJumpPer; i++) h[i] ^= jw<T + 1>(cur, nxt, i);
+        for (int i = 0; i < kJumpPer; i++) h[i] ^= W[T + 1 + i];
         break;
     case 4:
 #pragma unroll
-        for (int i = 0; i < kJumpPer; i++) h[i] ^= jw<T + 2>(cur, nxt, i);
+        for (int i = 0; i < kJumpPer; i++) h[i] ^= W[T + 2 + i];
         break;
     case 3:
 #pragma unroll
-        for (int i = 0; i < kJumpPer; i++) h[i] = xor3(h[i], jw<T>(cur, nxt, i), jw<T + 1>(cur, nxt, i));
+        for (int i = 0; i < kJumpPer; i++) h[i] = xor3(h[i], W[T + i], W[T + 1 + i]);
         break;
     case 5:
 #pragma unroll
-        for (int i = 0; i < kJumpPer; i++) h[i] = xor3(h[i], jw<T>(cur, nxt, i), jw<T + 2>(cur, nxt, i));
+        for (int i = 0; i < kJumpPer; i++) h[i] = xor3(h[i], W[T + i], W[T + 2 + i]);
         break;
     case 6:
 #pragma unroll
-        for (int i = 0; i < kJumpPer; i++)
-            h[i] = xor3(h[i], jw<T + 1>(cur, nxt, i), jw<T + 2>(cur, nxt, i));
+        for (int i = 0; i < kJumpPer; i++) h[i] = xor3(h[i], W[T + 1 + i], W[T + 2 + i]);
         break;
     case 7:
 #pragma unroll
-        for (int i = 0; i < kJumpPer; i++)
-            h[i] ^= xor3(jw<T>(cur, nxt, i), jw<T + 1>(cur, nxt, i), jw<T + 2>(cur, nxt, i));
+        for (int i = 0; i < kJumpPer; i++) h[i] ^= xor3(W[T + i], W[T + 1 + i], W[T + 2 + i]);
         break;
     default:
         break;
     }
 }
 
-__device__ __forceinline__ void jump_block(uint32_t (&h)[kJumpPer], const uint32_t (&cur)[kJumpPer],
-                                           uint32_t (&nxt)[kJumpPer], const uint32_t *xs,
-                                           uint32_t k0, int lane, uint32_t gb) {
-#pragma unroll
-    for (int m = 0; m < kJumpPer; m++)
-        nxt[m] = xs[(k0 + kJumpPer + kJumpPer * lane + m) & (kJumpRing - 1u)];
-    jump_triple<0>(h, cur, nxt, gb);
-    jump_triple<3>(h, cur, nxt, gb >> 3);
-    jump_triple<6>(h, cur, nxt, gb >> 6);
-    jump_triple<9>(h, cur, nxt, gb >> 9);
-    jump_triple<12>(h, cur, nxt, gb >> 12);
-    jump_triple<15>(h, cur, nxt, gb >> 15);
-    jump_triple<18>(h, cur, nxt, gb >> 18);
-}
-
 __global__ void __launch_bounds__(32 * kJumpWarps, 6)
     k_seed_jump(DevParams P, RngState G, const uint32_t *__restrict__ polys, uint64_t R_lo,
                 uint32_t spin_lo, uint32_t spin_hi) {
-    __shared__ uint32_t s_x[kJumpWarps][kJumpRing];
+    __shared__ uint32_t s_x[kJumpWarps][kJumpRing + kJumpMirror];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     uint32_t *xs = s_x[w];
     constexpr uint32_t M = kJumpRing - 1u;
@@ -223,37 +207,53 @@ __global__ void __launch_bounds__(32 * kJumpWarps, 6)
         if (lane == 0) {                             // mersenne_twister_engine::seed
             uint32_t x = (uint32_t)sd;
             xs[0] = x;
+            xs[kJumpRing] = x;
             for (uint32_t i = 1; i < kMtN; i++) {
                 x = 1812433253u * (x ^ (x >> 30)) + i;
                 xs[i] = x;
+                if (i < kJumpMirror) xs[kJumpRing + i] = x;
             }
         }
         __syncwarp();
         uint32_t gen = kMtN;                         // x[0 .. gen) are in the ring
+        // x[gen .. gen + 224): reads x[n - 624], x[n - 623], x[n - 227], all below gen; writes
+        // the slots of x[n - 1024], which no lane reads any more (a block reads from k0 on, and
+        // generation stops kJumpAhead + kJumpGen <= 1024 words past k0)
         auto generate_to = [&](uint32_t upto) {
             while (gen < upto) {
-                const uint32_t n = gen + lane;
-                const uint32_t v = mt_twist1(xs[(n - 624u) & M], xs[(n - 623u) & M], xs[(n - 227u) & M]);
+                uint32_t v[kJumpGen / 32];
+#pragma unroll
+                for (uint32_t c = 0; c < kJumpGen / 32; c++) {
+                    const uint32_t n = gen + 32 * c + lane;
+                    v[c] = mt_twist1_alu3(xs[(n - 624u) & M], xs[(n - 623u) & M], xs[(n - 227u) & M]);
+                }
+#pragma unroll
+                for (uint32_t c = 0; c < kJumpGen / 32; c++) {
+                    const uint32_t slot = (gen + 32 * c + lane) & M;
+                    xs[slot] = v[c];
+                    if (slot < kJumpMirror) xs[kJumpRing + slot] = v[c];
+                }
                 __syncwarp();
-                xs[n & M] = v;
-                __syncwarp();
-                gen += 32;
+                gen += kJumpGen;
             }
         };
-        uint32_t h[kJumpPer], A[kJumpPer], B[kJumpPer];
-        generate_to(kJumpPer * 32);
+        uint32_t h[kJumpPer];
 #pragma unroll
-        for (int i = 0; i < kJumpPer; i++) {
-            h[i] = 0;
-            A[i] = xs[(kJumpPer * lane + i) & M];
-        }
-        // one block body per iteration (the next block's words move into A): the unrolled
-        // body is large, and two alternating copies of it stalled on instruction fetch
+        for (int i = 0; i < kJumpPer; i++) h[i] = 0;
         for (uint32_t k0 = 0; k0 < (uint32_t)kMtDegreeDev; k0 += kJumpPer) {
             generate_to(k0 + kJumpAhead);
-            jump_block(h, A, B, xs, k0, lane, jump_bits(g, k0));
+            const uint32_t *wp = xs + ((k0 + kJumpPer * lane) & M);
+            uint32_t W[kJumpWin];
 #pragma unroll
-            for (int m = 0; m < kJumpPer; m++) A[m] = B[m];
+            for (int m = 0; m < kJumpWin; m++) W[m] = wp[m];
+            const uint32_t gb = jump_bits(g, k0);
+            jump_triple<0>(h, W, gb);
+            jump_triple<3>(h, W, gb >> 3);
+            jump_triple<6>(h, W, gb >> 6);
+            jump_triple<9>(h, W, gb >> 9);
+            jump_triple<12>(h, W, gb >> 12);
+            jump_triple<15>(h, W, gb >> 15);
+            jump_triple<18>(h, W, gb >> 18);
         }
         __syncwarp();
 #pragma unroll

@@ -1,6 +1,6 @@
 """Jump-ahead seeding: the state of mt19937(seed + spin) after discard(seed + spin)
 (src/sim/kernels.cu:82-88) computed through x^J mod phi instead of seed + spin generated words,
-for large discard counts (sw_mtjump.h, k_seed_jump; by default from 2304 x 1024 words).
+for large discard counts (sw_mtjump.h, k_seed_jump; by default from 1600 x 1024 words).
 
 CPU: the host polynomials against libstdc++'s own discard, at the edges of a regeneration and
 far out (a random 32-bit seed, the reference's SEED = 0 case). GPU: walks of high spin ids, of
@@ -14,7 +14,7 @@ from spinwalk_gb300.problem import Problem, cylinder_phantom
 from tests import oracle_lib
 from tests.helpers import bits_equal, m_close
 
-JUMP_MIN_Z = 2304 * 1024
+JUMP_MIN_Z = 1600 * 1024
 NEVER = 0xffffffff              # jump_min_kwords beyond any discard count: every spin discards
 
 

@@ -118,26 +118,54 @@ __global__ void __launch_bounds__(32 * kSeedWarps)
 // Seeding by jump-ahead (sw_mtjump.h): the same state as k_seed for spins whose discard count
 // z = seed + spin is large, in work independent of z. With J = 624 R - 1 (R regenerations of
 // discard(z)) and g = x^J mod phi (host-computed, one per R), the state after J words is
-// h_j = XOR over k with g_k = 1 of x[k + j], j < 624, over the spin's own output sequence x.
-// One warp per spin: lane l accumulates h_j for the 21 words j = 21 l + i in registers; x lives
-// in a 1024-word ring in shared memory, generated 224 words at a time ahead of use. A block of
-// 21 steps k0 .. k0 + 20 needs x[k0 + 21 l + m], m < 42, in each lane: the window of step s is
-// m = s .. s + 20, and the XOR of a window is a uniform branch on g_k. The first 64 ring slots
-// are mirrored past its end, so that a lane's 42 words are read at one base address plus
-// immediate offsets (no per-word wrap). The block of regeneration R is then h_1 .. h_623 plus
-// one more word.
+// h_j = XOR over k with g_k = 1 of x[k + j], j < 624, over the spin's own output sequence x:
+// a correlation of g with x, i.e. one 624 x 624 Hankel product per 624-step block of k.
+//
+// One level of Karatsuba splits each block product (outputs j = j' + 312 f, steps k = 624 a +
+// 312 e + r, f, e in {0, 1}) into three half-size products whose sums over the blocks are again
+// correlations:
+//   P1_j' = XOR over k in B of (g_(k-312) ^ g_k) x[k + j']
+//   P2_j' = XOR over k in A of g_k e[k + j'],   P3_j' = XOR over k in B of g_k e[k + j']
+//   h_j' = P1_j' ^ P2_j',   h_(312+j') = P1_j' ^ P3_j'                            (j' < 312)
+// with A, B the first and second halves of every 624-step block and e[i] = x[i] ^ x[i + 312]:
+// three correlations of 312 outputs over 9984 steps each, 3/4 of the direct XOR work.
+//
+// A thread block of three warps takes two spins that share R (hence g): warp w computes P_(w+1)
+// for both, lanes 0-15 for the first spin and 16-31 for the second, each lane the 21 outputs
+// j' = 21 l + i (16 x 21 = 336 >= 312) in registers. Each spin's x and e live in 1024-word rings
+// in shared memory; before block a the three warps produce x 624 words further (three rounds of
+// 208, which read only older words) and then e 624 words further, with a barrier after each
+// (the rings hold just the windows of one block), then run their 312 steps of the block: 15 groups of 21 steps (the last masked to 18), each group reading the
+// lane's 42 sequence words at one base address (the first 64 ring slots are mirrored past the
+// end) and adding windows on the polynomial's bits three at a time. The two spins' rings are 16
+// words apart modulo the 32 banks, so the two half-warps' reads do not conflict. The block of
+// regeneration R is then h_1 .. h_623 plus one more word.
 // ------------------------------------------------------------------------------------------
-constexpr int kJumpWarps = 4;
-constexpr uint32_t kJumpRing = 1024;      // sequence words per warp in shared memory
+constexpr int kJumpPer = 21;              // outputs per lane: 16 x 21 = 336 >= 312 per spin
+constexpr int kJumpWin = 2 * kJumpPer;    // sequence words a lane reads per group of 21 steps
+constexpr uint32_t kJumpRing = 1024;      // words per sequence ring
+constexpr uint32_t kJumpMask = kJumpRing - 1u;
 constexpr uint32_t kJumpMirror = 64;      // ring slots copied past the end
-constexpr int kJumpPer = 21;              // state words per lane: 32 x 21 = 672 >= 624
-constexpr int kJumpWin = 2 * kJumpPer;    // sequence words a lane reads per block
-constexpr uint32_t kJumpAhead = kJumpPer * 31 + kJumpWin;   // sequence needed past k0
-constexpr uint32_t kJumpGen = 224;        // words per generation: 7 per lane, all independent
-                                          // (x[n] reads x[n - 227] < the chunk's first word)
-static_assert(kJumpGen <= 227, "a generation chunk must not read its own words");
-static_assert(kJumpAhead + kJumpGen <= kJumpRing, "ring too short for the window");
+constexpr uint32_t kJumpStride = kJumpRing + kJumpMirror + 16;   // ring to ring: 16 mod 32 banks
+constexpr uint32_t kJumpXAhead = 1272;    // x is generated to 624 a + 1272 before block a
+constexpr uint32_t kJumpEAhead = 960;     // e to 624 a + 960 (the windows of block a reach there)
+constexpr uint32_t kJumpXFrom = 312;      // block a reads x from 624 a + 312 (P1), e from 624 a
+constexpr uint32_t kJumpRound = 208;      // x words per generation round (x[n] reads x[n - 227])
+constexpr int kJumpBlocksPerSm = 8;
+static_assert(kJumpStride % 32 == 16, "the second spin's rings must sit 16 banks over");
 static_assert(kJumpWin <= (int)kJumpMirror, "mirror too short for one window");
+static_assert(kJumpRound <= 227 && 3 * kJumpRound == kMtN, "three rounds per block");
+// Block a reads x[624 a + 312, 624 a + 962) and e[624 a, 624 a + 960); forming e[n] needs x[n]
+// and x[n + 312]. With x generated to 624 a + 1272 the ring holds x from 624 a + 248, and the
+// rounds before block a + 1 overwrite only x below 624 a + 872 (read by block a alone, done).
+static_assert(kJumpXAhead - kJumpRing <= kJumpXFrom, "x ring too short for block a");
+static_assert(kJumpXAhead - kJumpRing <= kJumpEAhead - kMtN + 312, "e formed from overwritten x");
+static_assert(kJumpEAhead <= kJumpRing, "e ring too short for block a");
+static_assert(kJumpEAhead + 312 <= kJumpXAhead, "e is formed from generated x only");
+// the last step of a block (624 a + 623) with the last padded output (335) reads 624 a + 958
+static_assert(kMtN - 1 + 16 * kJumpPer - 1 < (int)kJumpEAhead, "windows reach unformed e");
+constexpr uint32_t kJumpBlocks = (kMtDegreeDev + kMtN - 1) / kMtN;   // 32 blocks of 624 steps
+constexpr size_t kJumpSmem = 4 * kJumpStride * sizeof(uint32_t);
 
 // Bits k0 .. k0 + 20 of the jump polynomial (624 words; bits past 19936 are zero).
 __device__ __forceinline__ uint32_t jump_bits(const uint32_t *__restrict__ g, uint32_t k0) {
@@ -153,7 +181,7 @@ __device__ __forceinline__ uint32_t xor3(uint32_t a, uint32_t b, uint32_t c) {
     return r;
 }
 
-// Steps T .. T + 2 of a block on their three polynomial bits: two windows are added with one
+// Steps T .. T + 2 of a group on their three polynomial bits: two windows are added with one
 // three-input xor, so a triple costs one operation per word on average instead of 1.5.
 template <int T>
 __device__ __forceinline__ void jump_triple(uint32_t (&h)[kJumpPer], const uint32_t (&W)[kJumpWin],
@@ -192,94 +220,171 @@ __device__ __forceinline__ void jump_triple(uint32_t (&h)[kJumpPer], const uint3
     }
 }
 
-__global__ void __launch_bounds__(32 * kJumpWarps, 6)
+__device__ __forceinline__ void jump_put(uint32_t *ring, uint32_t n, uint32_t v) {
+    const uint32_t slot = n & kJumpMask;
+    ring[slot] = v;
+    if (slot < kJumpMirror) ring[kJumpRing + slot] = v;
+}
+
+// Spins [lo, hi) in pairs that share R: R changes where (seed + spin) % 624 == 1, so the range
+// splits into a head segment up to the first such spin and segments of 624 spins after it; each
+// segment is paired from its start (an odd segment leaves its last spin alone: both halves then
+// compute it and one writes). Pair p -> first spin and whether a second follows.
+struct JumpPairs {
+    uint32_t lo, hi, b0, head_pairs, n_pairs;
+    static JumpPairs make(uint64_t seed, uint32_t lo, uint32_t hi) {
+        JumpPairs q;
+        q.lo = lo;
+        q.hi = hi;
+        const uint32_t r = (uint32_t)((seed + lo) % kMtN);      // spin lo + (1 - r) mod 624
+        const uint64_t b0 = (uint64_t)lo + (r <= 1 ? 1 - r : kMtN + 1 - r);
+        q.b0 = (uint32_t)std::min<uint64_t>(b0, hi);
+        const uint32_t n0 = q.b0 - lo, rest = hi - q.b0;
+        q.head_pairs = (n0 + 1) / 2;
+        const uint32_t full = rest / kMtN, tail = rest % kMtN;
+        q.n_pairs = q.head_pairs + full * (kMtN / 2) + (tail + 1) / 2;
+        return q;
+    }
+    __device__ void pair(uint32_t p, uint32_t &s0, bool &two) const {
+        uint32_t end;
+        if (p < head_pairs) {
+            s0 = lo + 2 * p;
+            end = b0;
+        } else {
+            const uint32_t pp = p - head_pairs, seg = pp / (kMtN / 2);
+            const uint32_t base = b0 + seg * kMtN;
+            s0 = base + 2 * (pp % (kMtN / 2));
+            end = (uint32_t)min((uint64_t)hi, (uint64_t)base + kMtN);
+        }
+        two = s0 + 1 < end;
+    }
+};
+
+__global__ void __launch_bounds__(96, kJumpBlocksPerSm)
     k_seed_jump(DevParams P, RngState G, const uint32_t *__restrict__ polys, uint64_t R_lo,
-                uint32_t spin_lo, uint32_t spin_hi) {
-    __shared__ uint32_t s_x[kJumpWarps][kJumpRing + kJumpMirror];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t *xs = s_x[w];
-    constexpr uint32_t M = kJumpRing - 1u;
-    for (uint32_t spin = spin_lo + blockIdx.x * kJumpWarps + w; spin < spin_hi;
-         spin += gridDim.x * kJumpWarps) {
-        const uint64_t sd = P.seed + spin;
-        const uint32_t R = mt_discard_twists(sd);
+                JumpPairs pairs) {
+    extern __shared__ uint32_t s_jump[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, half = lane >> 4, hl = lane & 15;
+    const int t = threadIdx.x;
+    // rings: x of spin 0, x of spin 1, e of spin 0, e of spin 1
+    uint32_t *xr0 = s_jump, *xr1 = s_jump + kJumpStride;
+    uint32_t *er0 = s_jump + 2 * kJumpStride, *er1 = s_jump + 3 * kJumpStride;
+    for (uint32_t p = blockIdx.x; p < pairs.n_pairs; p += gridDim.x) {
+        uint32_t s0;
+        bool two;
+        pairs.pair(p, s0, two);
+        const uint32_t R = mt_discard_twists(P.seed + s0);
         const uint32_t *g = polys + (size_t)(R - R_lo) * kMtN;
-        if (lane == 0) {                             // mersenne_twister_engine::seed
-            uint32_t x = (uint32_t)sd;
-            xs[0] = x;
-            xs[kJumpRing] = x;
+        __syncthreads();                                 // the previous pair's reads are done
+        if (lane == 0 && w < 2) {                        // mersenne_twister_engine::seed
+            uint32_t *xr = w ? xr1 : xr0;
+            uint32_t x = (uint32_t)(P.seed + s0 + (w && two ? 1 : 0));
+            jump_put(xr, 0, x);
             for (uint32_t i = 1; i < kMtN; i++) {
                 x = 1812433253u * (x ^ (x >> 30)) + i;
-                xs[i] = x;
-                if (i < kJumpMirror) xs[kJumpRing + i] = x;
+                jump_put(xr, i, x);
             }
         }
-        __syncwarp();
-        uint32_t gen = kMtN;                         // x[0 .. gen) are in the ring
-        // x[gen .. gen + 224): reads x[n - 624], x[n - 623], x[n - 227], all below gen; writes
-        // the slots of x[n - 1024], which no lane reads any more (a block reads from k0 on, and
-        // generation stops kJumpAhead + kJumpGen <= 1024 words past k0)
-        auto generate_to = [&](uint32_t upto) {
-            while (gen < upto) {
-                uint32_t v[kJumpGen / 32];
-#pragma unroll
-                for (uint32_t c = 0; c < kJumpGen / 32; c++) {
-                    const uint32_t n = gen + 32 * c + lane;
-                    v[c] = mt_twist1_alu3(xs[(n - 624u) & M], xs[(n - 623u) & M], xs[(n - 227u) & M]);
-                }
-#pragma unroll
-                for (uint32_t c = 0; c < kJumpGen / 32; c++) {
-                    const uint32_t slot = (gen + 32 * c + lane) & M;
-                    xs[slot] = v[c];
-                    if (slot < kJumpMirror) xs[kJumpRing + slot] = v[c];
-                }
-                __syncwarp();
-                gen += kJumpGen;
+        // x[n] = f(x[n - 624], x[n - 623], x[n - 227]) for n in [from, to), to - from <= 227
+        auto x_round = [&](uint32_t from, uint32_t to) {
+            for (uint32_t i = t; i < 2 * (to - from); i += 96) {
+                uint32_t *xr = i < to - from ? xr0 : xr1;
+                const uint32_t n = from + (i < to - from ? i : i - (to - from));
+                jump_put(xr, n, mt_twist1_alu3(xr[(n - 624u) & kJumpMask], xr[(n - 623u) & kJumpMask],
+                                               xr[(n - 227u) & kJumpMask]));
             }
         };
+        // e[n] = x[n] ^ x[n + 312] for n in [from, to), both halves
+        auto e_form = [&](uint32_t from, uint32_t to) {
+            for (uint32_t i = t; i < 2 * (to - from); i += 96) {
+                const uint32_t m = to - from, n = from + (i < m ? i : i - m);
+                const uint32_t *xr = i < m ? xr0 : xr1;
+                jump_put(i < m ? er0 : er1, n, xr[n & kJumpMask] ^ xr[(n + 312u) & kJumpMask]);
+            }
+        };
+        // x to 1272 before block 0, and e[0, 624) while the x it reads is still in the ring
+        __syncthreads();
+        e_form(0, 312);
+        x_round(624, 832);
+        __syncthreads();
+        x_round(832, 1040);
+        __syncthreads();
+        e_form(312, 624);
+        x_round(1040, 1248);
+        __syncthreads();
+        x_round(1248, kJumpXAhead);
+        __syncthreads();
+        uint32_t e_done = kMtN;
         uint32_t h[kJumpPer];
 #pragma unroll
         for (int i = 0; i < kJumpPer; i++) h[i] = 0;
-        for (uint32_t k0 = 0; k0 < (uint32_t)kMtDegreeDev; k0 += kJumpPer) {
-            generate_to(k0 + kJumpAhead);
-            const uint32_t *wp = xs + ((k0 + kJumpPer * lane) & M);
-            uint32_t W[kJumpWin];
+        const uint32_t *seq = w == 0 ? (half ? xr1 : xr0) : (half ? er1 : er0);
+        for (uint32_t a = 0; a < kJumpBlocks; a++) {
+            const uint32_t xa = kMtN * a + kJumpXAhead - kMtN, ea = kMtN * a + kJumpEAhead;
+            if (a > 0) {                                 // x to 624 a + 1272 (block 0: above)
+                x_round(xa, xa + kJumpRound);
+                __syncthreads();
+                x_round(xa + kJumpRound, xa + 2 * kJumpRound);
+                __syncthreads();
+                x_round(xa + 2 * kJumpRound, xa + 3 * kJumpRound);
+                __syncthreads();
+            }
+            e_form(e_done, ea);                          // e to 624 a + 960
+            e_done = ea;
+            __syncthreads();
+            // this warp's 312 steps of block a: A (first half) for P2, B for P1 and P3
+            const uint32_t run = kMtN * a + (w == 1 ? 0u : 312u);
+            for (uint32_t u = 0; u < 312; u += kJumpPer) {
+                const uint32_t k0 = run + u;
+                uint32_t gb = jump_bits(g, k0);
+                if (w == 0) gb ^= jump_bits(g, k0 - 312);
+                if (u + kJumpPer > 312) gb &= (1u << (312 - u)) - 1u;
+                if (gb == 0) continue;
+                const uint32_t *wp = seq + ((k0 + kJumpPer * hl) & kJumpMask);
+                uint32_t W[kJumpWin];
 #pragma unroll
-            for (int m = 0; m < kJumpWin; m++) W[m] = wp[m];
-            const uint32_t gb = jump_bits(g, k0);
-            jump_triple<0>(h, W, gb);
-            jump_triple<3>(h, W, gb >> 3);
-            jump_triple<6>(h, W, gb >> 6);
-            jump_triple<9>(h, W, gb >> 9);
-            jump_triple<12>(h, W, gb >> 12);
-            jump_triple<15>(h, W, gb >> 15);
-            jump_triple<18>(h, W, gb >> 18);
+                for (int m = 0; m < kJumpWin; m++) W[m] = wp[m];
+                jump_triple<0>(h, W, gb);
+                jump_triple<3>(h, W, gb >> 3);
+                jump_triple<6>(h, W, gb >> 6);
+                jump_triple<9>(h, W, gb >> 9);
+                jump_triple<12>(h, W, gb >> 12);
+                jump_triple<15>(h, W, gb >> 15);
+                jump_triple<18>(h, W, gb >> 18);
+            }
+            __syncthreads();                             // block a's reads are done
         }
-        __syncwarp();
+        // P_(w+1) of spin `half` -> s_jump[(3 half + w) * 336 + j']
 #pragma unroll
-        for (int i = 0; i < kJumpPer; i++)
-            if (kJumpPer * lane + i < kMtN) xs[kJumpPer * lane + i] = h[i];
-        __syncwarp();
+        for (int i = 0; i < kJumpPer; i++) s_jump[(3 * half + w) * 336 + kJumpPer * hl + i] = h[i];
+        __syncthreads();
+        // h_j' = P1 ^ P2, h_(312+j') = P1 ^ P3 -> state words at 2048 + 624 sp + j
+        uint32_t *hs = s_jump + 2048;
+        for (uint32_t i = t; i < 2 * 624; i += 96) {
+            const uint32_t sp = i / 624, j = i % 624, jj = j % 312;
+            const uint32_t *Ps = s_jump + 3 * sp * 336;
+            hs[i] = Ps[jj] ^ Ps[(j < 312 ? 336 : 2 * 336) + jj];
+        }
+        __syncthreads();
         // block of regeneration R: x[624 R + q] = h_(q+1), q < 623, and one more twist word
-        uint32_t *gr = G.mt_r + (size_t)spin * kMtN, *gu = G.mt_u + (size_t)spin * kMtN;
-        for (int q = lane; q < kMtN - 1; q += 32) {
-            const uint32_t v = xs[q + 1];
-            gr[q] = v;
-            gu[q] = v;
+        for (uint32_t i = t; i < 2 * 624; i += 96) {
+            const uint32_t sp = i / 624, q = i % 624;
+            if (sp == 1 && !two) continue;
+            const uint32_t spin = s0 + sp;
+            const uint32_t *hp = hs + 624 * sp;
+            const uint32_t v = q < kMtN - 1 ? hp[q + 1] : mt_twist1(hp[0], hp[1], hp[397]);
+            G.mt_r[(size_t)spin * kMtN + q] = v;
+            G.mt_u[(size_t)spin * kMtN + q] = v;
+            if (q == 0) {
+                const uint32_t pos = (uint32_t)(P.seed + spin - (uint64_t)kMtN * (R - 1));
+                G.p_r[spin] = pos;
+                G.p_u[spin] = pos;
+                G.nhead[spin] = 0;
+                G.ncnt[spin] = 0;
+                G.uhead[spin] = 0;
+                G.ucnt[spin] = 0;
+            }
         }
-        if (lane == 0) {
-            const uint32_t v = mt_twist1(xs[0], xs[1], xs[397]);
-            gr[kMtN - 1] = v;
-            gu[kMtN - 1] = v;
-            const uint32_t p = (uint32_t)(sd - (uint64_t)kMtN * (R - 1));
-            G.p_r[spin] = p;
-            G.p_u[spin] = p;
-            G.nhead[spin] = 0;
-            G.ncnt[spin] = 0;
-            G.uhead[spin] = 0;
-            G.ucnt[spin] = 0;
-        }
-        __syncwarp();
     }
 }
 
@@ -1059,9 +1164,11 @@ cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo
     if (c > lo)
         k_seed<<<grid_for(((int64_t)c - lo + 1) / 2, kSeedWarps, 1 << 30), 32 * kSeedWarps, 0, st>>>(
             P, G, lo, c);
-    if (hi > c)
-        k_seed_jump<<<grid_for(hi - c, kJumpWarps, 152 * 6), 32 * kJumpWarps, 0, st>>>(
-            P, G, jt->polys, jt->R_lo, c, hi);
+    if (hi > c) {
+        const JumpPairs jp = JumpPairs::make(P.seed, c, hi);
+        const int grid = (int)std::min<uint32_t>(jp.n_pairs, 152 * kJumpBlocksPerSm);
+        k_seed_jump<<<grid, 96, kJumpSmem, st>>>(P, G, jt->polys, jt->R_lo, jp);
+    }
     return cudaGetLastError();
 }
 

@@ -60,8 +60,14 @@ WALK_FP64_OPS_PER_SPIN_STEP = 6          # x, y, z step multiplies and position 
 FP64_PEAK_GFLOPS = 152 * 2 * 2070e6 / 1e9  # 2 FP64 lanes per clock per SM at 2070 MHz
 WALK_DRAM_BYTES_PER_SPIN_STEP = 24.5
 SEED_LANE_INST_PER_WORD = 7.7            # ncu, k_seed: lane instructions per regenerated MT word
+# k_seed_jump: three correlations of 336 (padded) outputs over 32 x 15 groups of 21 steps, one
+# ALU lane operation per output word per triple of steps on average (a three-input xor adds two
+# windows), per spin
+JUMP_XOR_LANE_OPS_PER_SPIN = 3 * 336 * 32 * 15 * 21 / 3
 SEED_LIMITER = ("integer instruction issue (ncu: ALU pipe 83 %, issue 74 %, DRAM 2 %): "
                 "7.7 lane instructions per MT word, not HBM")
+JUMP_LIMITER = ("jump-ahead: integer ALU pipe (ncu: ALU 71 %, issue 59 %, DRAM 0.2 %) on the "
+                "xor work of three 312-output correlations per spin, not HBM")
 WALK_LIMITER = ("FP64 pipe (ncu: 64 %, 3 position additions + 3 step multiplies per step at 2 "
                 "lanes/clock/SM) and the latency of the voxel gather (issue 38 %, long-scoreboard "
                 "stalls, DRAM 10 %)")
@@ -880,19 +886,38 @@ def run_ours(args, world, rank, local):
                  "peak_source": peak_kind, "limiter": WALK_LIMITER}
     for rf in (seed_roof, walk_roof):
         rf["frac"] = rf["achieved"] / peak
-    # the seeding's own ceiling is instruction issue: the words its discards regenerate (624 per
+    # the seeding's own ceiling is instruction issue: the words the discards regenerate (624 per
     # regeneration, mt_discard_twists), at the measured instructions per word, against 4 warp
-    # instructions per SM clock
+    # instructions per SM clock; spins at or above the jump threshold are seeded by k_seed_jump
+    # instead, whose ceiling is the integer ALU pipe (16 lanes per clock per SM quarter) on its
+    # xor work. frac = the time both ideals would take / the stage's time.
+    from spinwalk_gb300 import abi
+    kw = tuning["applied"]["jump_min_kwords"] or abi.JUMP_MIN_KWORDS_DEFAULT
     z = int(p.seed) + np.arange(n, dtype=np.int64)
-    regen_words = float(624 * np.where(z > 0, 1 + (z - 1) // 624, 0).sum())
+    jumped = z >= kw * 1024
+    zd = z[~jumped]
+    regen_words = float(624 * np.where(zd > 0, 1 + (zd - 1) // 624, 0).sum())
+    n_jump = int(jumped.sum())
     sm_hz = (clocks.get("sm_mhz") or 2070.0) * 1e6 if clocks else 2070e6
     issue_peak = 152 * 4 * sm_hz
-    issued = regen_words * SEED_LANE_INST_PER_WORD / 32 / seed_launch_s
-    seed_roof["issue_roofline"] = {"achieved_warp_inst_per_s": issued, "peak": issue_peak,
-                                   "frac": issued / issue_peak, "regenerated_words": regen_words,
-                                   "note": "words x 7.7 lane instructions (ncu) / 32 per warp "
-                                           "instruction, against 4 warp instructions per SM "
-                                           "clock at the sampled SM clock"}
+    alu_peak = 152 * 64 * sm_hz
+    t_ideal = (regen_words * SEED_LANE_INST_PER_WORD / 32 / issue_peak +
+               n_jump * JUMP_XOR_LANE_OPS_PER_SPIN / alu_peak)
+    seed_roof["issue_roofline"] = {
+        "achieved_warp_inst_per_s": regen_words * SEED_LANE_INST_PER_WORD / 32 / seed_launch_s,
+        "peak": issue_peak, "frac": t_ideal / seed_launch_s, "regenerated_words": regen_words,
+        "jump_spins": n_jump, "jump_xor_lane_ops_per_spin": JUMP_XOR_LANE_OPS_PER_SPIN,
+        "alu_peak_lane_ops_per_s": alu_peak,
+        "note": "discarded words x 7.7 lane instructions (ncu) / 32 per warp instruction against "
+                "4 warp instructions per SM clock, plus jumped spins' xor lane operations against "
+                "64 ALU lanes per SM clock, at the sampled SM clock; frac = ideal time / stage time"}
+    if n_jump:
+        seed_roof["kernel"] = "k_seed + k_seed_jump" if regen_words else "k_seed_jump"
+        seed_roof["limiter"] = (("discards: " + SEED_LIMITER + "; ") if regen_words else "") + \
+            JUMP_LIMITER
+    if rng != abi.SW_RNG_MT19937:          # minstd: O(log) seeding per spin, no such ceiling
+        seed_roof.pop("issue_roofline")
+        seed_roof["kernel"] = "k_seed_minstd"
     roof = {"seed+init+pack": seed_roof, "walk": walk_roof}.get(dominant, walk_roof)
     # walk-only rate: the call's wall time minus its seeding stage (the kernel times of the two
     # halves of the rounds overlap, so their sum would overstate it)

@@ -335,7 +335,7 @@ int sw_last_timing(sw_timing *out);
  *   jump_min_kwords : seeding: spins whose discard count seed + spin reaches this many times
  *                     1024 words compute their state by jump-ahead (a polynomial over GF(2),
  *                     work independent of the count) instead of generating seed + spin words;
- *                     0 = default (1600, i.e. 1.64e6 words, where the two cost the same on
+ *                     0 = default (1408, i.e. 1.44e6 words, where the two cost the same on
  *                     GB300). No reference counterpart (the reference discards word by word,
  *                     src/sim/kernels.cu:87-88).
  *   ring_steps      : sw_sim / sw_sim_device / sw_sim_spins / sw_sim_signal: walk steps one

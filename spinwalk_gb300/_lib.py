@@ -229,7 +229,7 @@ def set_tuning(resort_interval=0, walk_block=256, seed_chunks=0, round_streams=0
                jump_min_kwords=0, ring_steps=0, walk_blocks_per_sm=0):
     """sw_set_tuning: Morton re-sort interval (walk rounds, 0 = never), walk block size, seed
     chunks of the seed/walk pipeline (0 = auto), round halves (0 = auto), the discard count
-    from which seeding jumps ahead (in 1024 words, 0 = default 1600) and the steps of one
+    from which seeding jumps ahead (in 1024 words, 0 = default 1408) and the steps of one
     refill/walk round (0 = default 512) and a cap on the walk's blocks per SM (0 = none) for
     every later call of this process. Results do not depend on it."""
     t = abi.SwTuning(resort_interval=int(resort_interval), walk_block=int(walk_block),

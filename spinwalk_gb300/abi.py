@@ -127,6 +127,10 @@ class SwEngineStats(C.Structure):
     ]
 
 
+# sw_tuning.jump_min_kwords = 0 means this many 1024-word units (include/spinwalk_gpu.h)
+JUMP_MIN_KWORDS_DEFAULT = 1408
+
+
 class SwTuning(C.Structure):
     _fields_ = [
         ("resort_interval", C.c_uint32),

@@ -18,9 +18,9 @@ constexpr uint32_t kUnifBuf = 128;               // uniform deviates for crossin
 constexpr uint32_t kStepsPerRound = kNormBuf / 3;  // longest walk of one refill/walk round
 // Seeding: by default, spins whose discard count seed + spin reaches this jump ahead
 // (k_seed_jump) instead of regenerating seed + spin words (k_seed); sw_tuning.jump_min_kwords
-// overrides it. Measured on GB300: the jump costs 0.39 us of the whole GPU per spin whatever the
-// count, the discard 1 / 4.2e12 s per word, so they break even near 1.64e6 words.
-constexpr uint64_t kJumpMinZ = 1600ull * 1024;
+// overrides it. Measured on GB300: the jump costs 0.34 us of the whole GPU per spin whatever the
+// count, the discard 1 / 4.2e12 s per word, so they break even near 1.44e6 words.
+constexpr uint64_t kJumpMinZ = 1408ull * 1024;
 constexpr int kMtDegreeDev = 19937;               // degree of mt19937's characteristic polynomial
 
 // Pooled Gaussian generators of a batch whose instances share the seed: one gen_r and one ring

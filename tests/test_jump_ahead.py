@@ -1,6 +1,6 @@
 """Jump-ahead seeding: the state of mt19937(seed + spin) after discard(seed + spin)
 (src/sim/kernels.cu:82-88) computed through x^J mod phi instead of seed + spin generated words,
-for large discard counts (sw_mtjump.h, k_seed_jump; by default from 1600 x 1024 words).
+for large discard counts (sw_mtjump.h, k_seed_jump; by default from 1408 x 1024 words).
 
 CPU: the host polynomials against libstdc++'s own discard, at the edges of a regeneration and
 far out (a random 32-bit seed, the reference's SEED = 0 case). GPU: walks of high spin ids, of
@@ -14,7 +14,7 @@ from spinwalk_gb300.problem import Problem, cylinder_phantom
 from tests import oracle_lib
 from tests.helpers import bits_equal, m_close
 
-JUMP_MIN_Z = 1600 * 1024
+JUMP_MIN_Z = 1408 * 1024
 NEVER = 0xffffffff              # jump_min_kwords beyond any discard count: every spin discards
 
 
@@ -153,3 +153,24 @@ def test_gpu_engine_jump_equals_discard(tuning):
             eng.close()
     for k in ("M1", "XYZ1", "T", "status"):
         assert bits_equal(outs[0][k], outs[1][k]), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("offset,count", [(0, 1), (623, 1), (622, 3), (620, 9), (1, 624),
+                                          (311, 625), (0, 1249)])
+def test_gpu_jump_pairs_at_regeneration_edges(tuning, offset, count):
+    """k_seed_jump seeds two spins that share R per thread block: R changes where
+    (seed + spin) % 624 == 1, so a range splits into segments of 624 spins paired from their
+    start. Ranges that begin or end at such an edge, single spins and odd segments (one spin
+    computed alone) seed the same by jump-ahead as by discard, bit for bit."""
+    seed = 5000
+    base = (1 - seed) % 624 + 624 * 2           # (seed + base) % 624 == 1
+    lo = base + offset
+    hi = lo + count
+    pr = _problem(hi + 5, seed)
+    tuning(jump_min_kwords=NEVER)
+    want = _lib.run_spins(pr, lo, hi)
+    tuning(jump_min_kwords=1)
+    got = _lib.run_spins(pr, lo, hi)
+    for k in ("M1", "XYZ1", "T", "status"):
+        assert bits_equal(got[k], want[k]), k

@@ -338,11 +338,13 @@ int sw_last_timing(sw_timing *out);
  *                     0 = default (1408, i.e. 1.44e6 words, where the two cost the same on
  *                     GB300). No reference counterpart (the reference discards word by word,
  *                     src/sim/kernels.cu:87-88).
- *   ring_steps      : sw_sim / sw_sim_device / sw_sim_spins / sw_sim_signal: walk steps one
- *                     refill of a spin's Gaussian ring lasts (3 deviates each), i.e. the steps
- *                     of one refill/walk round and of one walk launch; 0 = default (512),
- *                     else 32 .. 4096. Longer rings mean fewer rounds and launches but more
- *                     ring memory (12 B per step per spin) between refill and walk.
+ *   ring_steps      : sw_sim / sw_sim_device / sw_sim_spins / sw_sim_signal and the slots of
+ *                     engines created afterwards (sw_engine_create; sw_sim_batch instances that
+ *                     run as engine jobs): walk steps one refill of a spin's Gaussian ring
+ *                     lasts (3 deviates each), i.e. the steps of one refill/walk round and of
+ *                     one walk launch; 0 = default (512), else 32 .. 4096. Longer rings mean
+ *                     fewer rounds and launches but more ring memory (12 B per step per spin)
+ *                     between refill and walk.
  *   walk_blocks_per_sm : sw_sim / sw_sim_device: caps the walk launch at this many blocks per
  *                     SM, the blocks striding over the spins, so that the other half's refill
  *                     can run beside it on every SM; 0 = default (no cap, one thread per spin).

@@ -309,7 +309,7 @@ int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
         const bool t = timed < kMaxTimedChunks;
         cudaEvent_t *e = ev + 4 + 3 * timed;
         if (t) SW_CUDA(cudaEventRecord(e[0], st));
-        SW_CUDA(sw::launch_refill_range(P, L.G, L.S.flags, LT, lo, hi, st));
+        SW_CUDA(sw::launch_refill_range(P, L.G, L.S, LT, lo, hi, st));
         if (t) SW_CUDA(cudaEventRecord(e[1], st));
         if (tu.resort_interval && r % tu.resort_interval == 0) {
             sw::OrderState Qh = L.Q;                    // each half sorts with its own histogram

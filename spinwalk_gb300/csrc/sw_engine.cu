@@ -12,8 +12,9 @@
 //     one slot's capacity (spins are independent); slots run chunks of different jobs at the same
 //     time, so small jobs fill the GPU together and big ones never need more than a slot's memory.
 // A chunk is: stage inputs (pinned) -> copy its range of the seed cache -> k_init ->
-// ceil(steps / 64) refill/walk rounds issued without waiting (no spin can finish in fewer: a round
-// advances a spin by at most 64 time points) -> then one round at a time until the walk reports no
+// ceil(steps / ring steps) refill/walk rounds issued without waiting (no spin can finish in
+// fewer: a round advances a spin by at most the steps its Gaussian ring holds, the tuning's
+// ring_steps when the engine was created) -> then one round at a time until the walk reports no
 // active spin -> results back through the staging buffer. The host only polls events.
 //
 // Every job gives the results of its own sw_sim call, bit for bit (tests/test_engine.py).
@@ -47,7 +48,6 @@ namespace {
     } while (0)
 
 constexpr size_t kTableBytes = 1 << 20;        // per slot: RF / TE / gradient tables of a job
-using sw::kStepsPerRound;
 
 double now_s() {
     using clk = std::chrono::steady_clock;
@@ -151,6 +151,7 @@ struct Slot {
 struct sw_engine {
     std::mutex mu;
     int device = 0;
+    uint32_t nlen = sw::kNormBuf;            // Gaussian deviates per ring in every slot
     uint64_t budget = 0, used = 0;
     cudaStream_t seed_st = nullptr;
     uint32_t *seed_scratch = nullptr;        // ring counters written by k_seed, not needed here
@@ -300,7 +301,7 @@ ChunkView view(const Slot &s) {
     sw::RngState &G = v.G;
     G.mt_r = shift(G.mt_r, lo * sw::kMtN); G.mt_u = shift(G.mt_u, lo * sw::kMtN);
     G.p_r = shift(G.p_r, lo); G.p_u = shift(G.p_u, lo);
-    G.nbuf = shift(G.nbuf, lo * sw::kNormBuf); G.nhead = shift(G.nhead, lo); G.ncnt = shift(G.ncnt, lo);
+    G.nbuf = shift(G.nbuf, lo * G.nlen); G.nhead = shift(G.nhead, lo); G.ncnt = shift(G.ncnt, lo);
     G.ubuf = shift(G.ubuf, lo * sw::kUnifBuf); G.uhead = shift(G.uhead, lo); G.ucnt = shift(G.ucnt, lo);
     v.Q = s.L.Q;
     v.Q.order = shift(v.Q.order, lo);
@@ -391,7 +392,7 @@ int issue_rounds(sw_engine *E, Slot &s, uint64_t k, bool first) {
     const uint32_t ri = j.tuning.resort_interval;
     for (uint64_t r = 0; r < k; r++) {
         if (r + 1 == k) EN_CUDA(cudaMemsetAsync(s.L.active, 0, sizeof(uint32_t), s.st));
-        EN_CUDA(sw::launch_refill_range(j.P, v.G, v.S.flags, E->LT, s.lo, s.hi, s.st));
+        EN_CUDA(sw::launch_refill_range(j.P, v.G, v.S, E->LT, s.lo, s.hi, s.st));
         if (ri && (s.rounds + r) % ri == 0) {
             EN_CUDA(sw::launch_order(j.P, v.S, v.Q, s.lo, s.hi, s.st));
             E->launches += 3;
@@ -501,7 +502,8 @@ int pump(sw_engine *E, int &rc) {
         if (!pick) break;
         if ((rc = start_chunk(E, s, *pick))) return progress;
         const uint64_t steps = (uint64_t)pick->p.n_timepoints * (uint64_t)(pick->p.n_dummy_scan + 1);
-        if ((rc = issue_rounds(E, s, (steps + kStepsPerRound - 1) / kStepsPerRound, true))) return progress;
+        const uint64_t per_round = s.L.G.nlen / 3;
+        if ((rc = issue_rounds(E, s, (steps + per_round - 1) / per_round, true))) return progress;
         progress++;
     }
     return progress;
@@ -653,13 +655,14 @@ int engine_create(int device, uint32_t n_slots, uint32_t slot_spins, uint64_t bu
     size_t freeb = 0, total = 0;
     cudaMemGetInfo(&freeb, &total);
     E->budget = budget ? budget : (uint64_t)(freeb * 0.85);
+    E->nlen = ring_len(current_tuning());
     auto bad = [&](int code) { engine_free(E); return code; };
     if (cudaStreamCreateWithFlags(&E->seed_st, cudaStreamNonBlocking) != cudaSuccess)
         return bad(fail(SW_ERR_CUDA, "stream"));
     E->slots.resize(n_slots);
     for (Slot &s : E->slots) {
         s.cap = slot_spins;
-        Layout m = layout(nullptr, slot_spins, 0, kTableBytes, true);
+        Layout m = layout(nullptr, slot_spins, 0, kTableBytes, true, true, E->nlen);
         s.io_bytes = (size_t)slot_spins * 256 + (16 << 20);
         if (E->used + m.bytes + s.io_bytes > E->budget)
             return bad(fail(SW_ERR_NOMEM, "slots exceed the HBM budget"));
@@ -671,7 +674,7 @@ int engine_create(int device, uint32_t n_slots, uint32_t slot_spins, uint64_t bu
             cudaGetLastError();
             return bad(fail(SW_ERR_NOMEM, "slot buffers"));
         }
-        s.L = layout(s.ws, slot_spins, 0, kTableBytes, true);
+        s.L = layout(s.ws, slot_spins, 0, kTableBytes, true, true, E->nlen);
         E->used += m.bytes + s.io_bytes;
     }
     *out = E;
@@ -820,7 +823,8 @@ int acquire_call_engine(uint32_t slots, uint32_t slot_spins, sw_engine *&out) {
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxBatchDevices)
         return fail(SW_ERR_CUDA, "no current CUDA device");
     sw_engine *&E = g_batch_engine[dev];
-    if (E && (E->slots.size() < slots || E->slots[0].cap < slot_spins)) {
+    if (E && (E->slots.size() < slots || E->slots[0].cap < slot_spins ||
+              E->nlen != ring_len(current_tuning()))) {
         engine_free(E);
         E = nullptr;
     }

@@ -451,14 +451,31 @@ __device__ __forceinline__ float ms_uniform(uint32_t x) {
 
 // One warp per spin: lane l takes the (l+1)-th next engine output, 32 per pass. Tops up the
 // spin's Gaussian ring (and its uniform ring when at most half full).
+// Gaussian deviates a spin can still draw: three per remaining step of its walk (all scans to
+// come), plus 1/16 and 96 for rejected moves (a rejected crossing draws its step again). A
+// refill stops there instead of filling the whole ring: the last round of a short walk would
+// otherwise generate deviates nobody reads. A spin that draws more pauses and is topped up in
+// the next round, as when its ring runs out; the sequence it reads is the same either way.
+__device__ __forceinline__ uint32_t normals_left(const DevParams &P, const uint32_t *__restrict__ tp,
+                                                 const uint32_t *__restrict__ ds, uint32_t spin,
+                                                 uint32_t flags) {
+    const uint32_t d = ds[spin], t = (flags & kFlagStarted) ? tp[spin] : 0u;
+    if (d > P.n_dummy_scan) return 0u;
+    const uint64_t steps = (uint64_t)(P.n_dummy_scan - d) * P.n_timepoints +
+                           (t < P.n_timepoints ? P.n_timepoints - t : 0u);
+    const uint64_t n = 3 * steps + ((3 * steps) >> 4) + 96;
+    return n > 0xffffffffull ? 0xffffffffu : (uint32_t)n;
+}
+
 __device__ __forceinline__ void refill_spin_minstd(uint32_t spin, const RngState &G,
                                                    const uint32_t *__restrict__ ms_delta,
-                                                   int lane) {
+                                                   uint32_t cap, int lane) {
     const uint32_t nc = G.ncnt[spin], nh = G.nhead[spin], uc = G.ucnt[spin], nlen = G.nlen;
-    if (nc < nlen) {
+    const uint32_t fill = min(nlen, cap);
+    if (nc < fill) {
         uint32_t x = G.p_r[spin];
         float *nb = G.nbuf + (size_t)spin * nlen;
-        const uint32_t K = nlen - nc, wpos = nh + nc;
+        const uint32_t K = fill - nc, wpos = nh + nc;
         for (uint32_t b = 0; b < K; b += 32) {
             const uint32_t r = min(32u, K - b);
             if ((uint32_t)lane < r)
@@ -468,7 +485,7 @@ __device__ __forceinline__ void refill_spin_minstd(uint32_t spin, const RngState
         }
         if (lane == 0) {
             G.p_r[spin] = x;
-            G.ncnt[spin] = nlen;
+            G.ncnt[spin] = fill;
         }
     }
     if (uc <= kUnifBuf / 2) {
@@ -490,11 +507,13 @@ __device__ __forceinline__ void refill_spin_minstd(uint32_t spin, const RngState
 
 __global__ void __launch_bounds__(128)
     k_refill_minstd(DevParams P, RngState G, const uint32_t *__restrict__ flags,
+                    const uint32_t *__restrict__ tp, const uint32_t *__restrict__ ds,
                     const uint32_t *__restrict__ ms_delta, uint32_t spin_lo, uint32_t spin_hi) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (uint32_t spin = spin_lo + blockIdx.x * 4 + w; spin < spin_hi; spin += gridDim.x * 4) {
-        if (flags[spin] & kFlagDone) continue;
-        refill_spin_minstd(spin, G, ms_delta, lane);
+        const uint32_t f = flags[spin];
+        if (f & kFlagDone) continue;
+        refill_spin_minstd(spin, G, ms_delta, normals_left(P, tp, ds, spin, f), lane);
         __syncwarp();
     }
 }
@@ -671,9 +690,9 @@ __device__ __forceinline__ void refill_uniforms_mt(uint32_t *gst, uint32_t &p, f
 // gen_u. `s` is the warp's 624-word shared block.
 __device__ __forceinline__ void refill_spin_mt(uint32_t spin, const RngState &G,
                                                const LogfTables &L, const float *s_tab,
-                                               uint32_t *s, int lane) {
-    const uint32_t nc = G.ncnt[spin];
-    const uint32_t K = (G.nlen - nc) / 2;                   // pairs to add
+                                               uint32_t *s, uint32_t cap, int lane) {
+    const uint32_t nc = G.ncnt[spin], fill = min(G.nlen, cap);
+    const uint32_t K = fill > nc ? min((fill - nc + 1) / 2, (G.nlen - nc) / 2) : 0u;  // pairs
     if (K > 0) {
         uint32_t p = G.p_r[spin];
         refill_normals_mt(G.mt_r + (size_t)spin * kMtN, p, G.nbuf + (size_t)spin * G.nlen, G.nlen,
@@ -698,7 +717,8 @@ __device__ __forceinline__ void refill_spin_mt(uint32_t spin, const RngState &G,
 }
 
 __global__ void __launch_bounds__(32 * kRefillWarps)
-    k_refill(DevParams P, RngState G, const uint32_t *__restrict__ flags, LogfTables L,
+    k_refill(DevParams P, RngState G, const uint32_t *__restrict__ flags,
+             const uint32_t *__restrict__ tp, const uint32_t *__restrict__ ds, LogfTables L,
              uint32_t spin_lo, uint32_t spin_hi) {
     __shared__ float s_tab[192];
     __shared__ uint32_t s_mt[kRefillWarps][kMtN];
@@ -707,8 +727,9 @@ __global__ void __launch_bounds__(32 * kRefillWarps)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (uint32_t spin = spin_lo + blockIdx.x * kRefillWarps + w; spin < spin_hi;
          spin += gridDim.x * kRefillWarps) {
-        if (flags[spin] & kFlagDone) continue;
-        refill_spin_mt(spin, G, L, s_tab, s_mt[w], lane);
+        const uint32_t f = flags[spin];
+        if (f & kFlagDone) continue;
+        refill_spin_mt(spin, G, L, s_tab, s_mt[w], normals_left(P, tp, ds, spin, f), lane);
         __syncwarp();
     }
 }
@@ -1188,21 +1209,21 @@ cudaError_t launch_init_range(const DevParams &P, const DevTables &Tb, const uin
     return cudaGetLastError();
 }
 
-cudaError_t launch_refill(const DevParams &P, const RngState &G, const uint32_t *flags,
+cudaError_t launch_refill(const DevParams &P, const RngState &G, const SpinState &S,
                           const LogfTables &L, cudaStream_t st) {
-    return launch_refill_range(P, G, flags, L, 0, P.n_spins, st);
+    return launch_refill_range(P, G, S, L, 0, P.n_spins, st);
 }
 
-cudaError_t launch_refill_range(const DevParams &P, const RngState &G, const uint32_t *flags,
+cudaError_t launch_refill_range(const DevParams &P, const RngState &G, const SpinState &S,
                                 const LogfTables &L, uint32_t lo, uint32_t hi, cudaStream_t st) {
     if (hi <= lo) return cudaSuccess;
     if (P.rng == SW_RNG_MINSTD) {
-        k_refill_minstd<<<grid_for(hi - lo, 4, 152 * 64), 128, 0, st>>>(P, G, flags, L.ms_delta,
-                                                                         lo, hi);
+        k_refill_minstd<<<grid_for(hi - lo, 4, 152 * 64), 128, 0, st>>>(P, G, S.flags, S.tp, S.ds,
+                                                                         L.ms_delta, lo, hi);
         return cudaGetLastError();
     }
     k_refill<<<grid_for(hi - lo, kRefillWarps, 152 * 64), 32 * kRefillWarps, 0, st>>>(
-        P, G, flags, L, lo, hi);
+        P, G, S.flags, S.tp, S.ds, L, lo, hi);
     return cudaGetLastError();
 }
 

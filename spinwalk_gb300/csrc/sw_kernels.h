@@ -22,7 +22,9 @@ struct JumpTable {
 // their regeneration counts), the others by the plain discard.
 cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo, uint32_t hi,
                               cudaStream_t st, const JumpTable *jt = nullptr);
-cudaError_t launch_refill_range(const DevParams &P, const RngState &G, const uint32_t *flags,
+// Tops up the rings of the spins in [lo, hi) that are not done, each to what its remaining walk
+// can draw at most (S: flags, time point and scan of every spin).
+cudaError_t launch_refill_range(const DevParams &P, const RngState &G, const SpinState &S,
                                 const LogfTables &L, uint32_t lo, uint32_t hi, cudaStream_t st);
 // order: walk order of the spins (null = id order); block: threads per block (64..256);
 // max_blocks > 0 caps the grid (the blocks then stride over the spins).
@@ -54,7 +56,7 @@ cudaError_t launch_init_range(const DevParams &P, const DevTables &Tb, const uin
                               const float *M0, const float *XYZ0, const SpinState &S,
                               const Outputs &O, bool fp64_state, uint32_t lo, uint32_t hi,
                               cudaStream_t st);
-cudaError_t launch_refill(const DevParams &P, const RngState &G, const uint32_t *flags,
+cudaError_t launch_refill(const DevParams &P, const RngState &G, const SpinState &S,
                           const LogfTables &L, cudaStream_t st);
 cudaError_t launch_walk(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
                         const uint2 *vox, const SpinState &S, const RngState &G,

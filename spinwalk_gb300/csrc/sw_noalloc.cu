@@ -141,7 +141,7 @@ extern "C" int sw_sim_device_noalloc(const sw_params *p, const sw_sequence *q,
             return fail(SW_ERR_TIMEOUT, "walk did not finish");
         }
         NA_CUDA(cudaMemsetAsync(L.active, 0, sizeof(uint32_t), st));
-        NA_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
+        NA_CUDA(sw::launch_refill(P, L.G, L.S, LT, st));
         if (tu.resort_interval && round % tu.resort_interval == 0)
             NA_CUDA(sw::launch_order(P, L.S, L.Q, 0, P.n_spins, st));
         NA_CUDA(sw::launch_walk_range(SW_PREC_FP32, false, P, Tb, L.vox, L.S, L.G, O, L.active, 0,

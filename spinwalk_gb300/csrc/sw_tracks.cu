@@ -1166,7 +1166,7 @@ extern "C" int sw_sim_tracks(const sw_params *param, const sw_sequence *seq,
         const uint32_t lo = hb[hh], hi = hb[hh + 1];
         cudaStream_t s = C.st[hh];
         uint32_t *act = L.active + 2 * hh;
-        TR_CUDA(sw::launch_refill_range(P, L.G, L.S.flags, LT, lo, hi, s));
+        TR_CUDA(sw::launch_refill_range(P, L.G, L.S, LT, lo, hi, s));
         const unsigned gw = (hi - lo + 255) / 256, gb = (unsigned)(((size_t)ng * (hi - lo) + 255) / 256);
         if (NC > 1) {                              // gradient classes (FP32, no shadow)
             const bool kh = precision == SW_PREC_KAHAN;

@@ -158,7 +158,7 @@ extern "C" int sw_autotune(const sw_params *param, const sw_sequence *seq, const
         r = RoundEv{evi, evi + 1, evi + 2, evi + 3};
         evi += 4;
         TU_CUDA(cudaEventRecord(S.ev[r.er], st));
-        TU_CUDA(sw::launch_refill(P, L.G, L.S.flags, LT, st));
+        TU_CUDA(sw::launch_refill(P, L.G, L.S, LT, st));
         TU_CUDA(cudaEventRecord(S.ev[r.e0], st));
         if (sort) TU_CUDA(sw::launch_order(P, L.S, L.Q, 0, P.n_spins, st));
         TU_CUDA(cudaEventRecord(S.ev[r.e1], st));

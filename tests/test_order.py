@@ -121,6 +121,33 @@ def test_sim_results_independent_of_ring_steps(tuning, case, ring_steps):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("ring_steps", [32, 256, 1000])
+def test_engine_entry_points_independent_of_ring_steps(tuning, ring_steps):
+    """Engines take the ring length in force when they are created: sw_sim_spins and
+    sw_sim_signal (through the one-call engine) and a serving engine give the results of
+    sw_sim with the default rounds, bit for bit (the signal's sums up to their order)."""
+    pr, _ = load_golden("permeable")
+    want = _lib.run(pr, fill=np.nan)
+    want_sig = _lib.run_signal(pr)
+    n = pr.params.n_spins
+    tuning(0, 256, 0, 0, 0, ring_steps)
+    got = _lib.run_spins(pr, 0, n, fill=np.nan)
+    _same(got, want)
+    sig, cnt, status = _lib.run_signal(pr)
+    assert np.array_equal(cnt, want_sig[1]) and np.array_equal(status, want_sig[2])
+    # the sums are float atomics: their order, not their terms, may differ
+    assert np.allclose(sig, want_sig[0], rtol=1e-12, atol=1e-12 * max(1, int(cnt.max())))
+    eng = _lib.Engine(n_slots=2, slot_spins=max(1, n // 3))
+    try:
+        pid = eng.add_phantom(pr)
+        _, out = eng.submit(pr, pid, fill=np.nan)
+        assert all(rc == 0 for _, rc, _ in eng.run_all())
+        _same(out, want)
+    finally:
+        eng.close()
+
+
+@pytest.mark.gpu
 def test_dense_ring_steps_with_halves_resort_and_shadow(tuning):
     pr = _dense_problem(n_spins=150000)
     want = _lib.run(pr, precision=2, fp64_shadow=True, fill=np.nan)

@@ -216,6 +216,9 @@ int sw_logf_exception_count(uint64_t *count, uint64_t *wide);
  *   status    : [n_spins] SW_SPIN_* or NULL
  *   precision : SW_PREC_*; M1_fp64 (optional, [n_spins*n_TE*3] double) receives the FP64
  *               shadow magnetisation of the same walk when non-NULL.
+ * The GPU starts seeding the generators before the buffers are copied in (seeding reads none
+ * of them), so the copies overlap it; pinned host buffers copy fastest. The device workspace
+ * and the device copies of the buffers are kept per device for the next call, grown on demand.
  */
 int sw_sim(const sw_params *param, const sw_sequence *seq,
            const float *pFieldMap, const uint8_t *pMask,

@@ -212,6 +212,8 @@ struct DeviceCtx {
     uint32_t *d_logf_bitmap = nullptr;
     char *ws = nullptr;
     size_t ws_size = 0;
+    char *io = nullptr;                    // sw_sim: device copies of the caller's host buffers
+    size_t io_size = 0;
     uint32_t *h_active = nullptr;          // pinned
     std::vector<cudaEvent_t> ev;           // timing events: 4 call-level, then 3 per round
     cudaStream_t seed_st = nullptr;        // lowest priority: seeding of the chunks
@@ -274,22 +276,123 @@ std::vector<uint32_t> seed_chunks(const sw::DevParams &P, uint32_t C) {
     return b;
 }
 
+// One call between its set-up and its walk: workspace laid out, parameter tables uploaded on
+// the caller's stream, seeding launched on the context's seed stream.
+struct Call {
+    Layout L{};
+    sw::DevParams P{};
+    sw::DevTables Tb{};
+    sw::LogfTables LT{};
+    int precision = SW_PREC_FP32;          // SW_PREC_* alone
+    bool dbl = false;                      // FP64 state (FP64 arithmetic or the FP64 shadow)
+    uint32_t C = 1;                        // seed chunks
+    std::vector<uint32_t> b;               // their spin boundaries
+    uint32_t launches = 0;
+};
+
+// Waits for everything a call may have left on the context's streams (error paths).
+void drain(DeviceCtx &ctx) {
+    cudaStreamSynchronize(ctx.seed_st);
+    cudaStreamSynchronize(ctx.walk_st);
+    cudaStreamSynchronize(ctx.walk_st2);
+}
+
+// Set-up of a call and the launch of its seeding. The seeding reads nothing of the caller's
+// (generators depend only on seed + spin id) and writes only the context's workspace, so it is
+// not ordered after `st`: it runs while the caller's stream still produces the inputs, and while
+// sw_sim copies them from the host. Every call waits for its own work before it returns, so the
+// workspace is idle here.
+int begin_call(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, int precision,
+               bool fp64_shadow, cudaStream_t st, Call &c) {
+    g_timing = sw_timing{};
+    const size_t n = p->n_spins;
+    const bool bf16 = (precision & SW_FIELD_BF16) != 0;
+    const uint32_t rng = (uint32_t)precision & ~(uint32_t)(SW_PREC_MASK | SW_FIELD_BF16);
+    precision &= SW_PREC_MASK;
+    if (precision != SW_PREC_FP32 && precision != SW_PREC_FP64 && precision != SW_PREC_KAHAN)
+        return fail(SW_ERR_INVALID, "precision");
+    if (rng != SW_RNG_MT19937 && rng != SW_RNG_MINSTD) return fail(SW_ERR_INVALID, "generator flavour");
+    int rc = ensure_logf(ctx);
+    if (rc) return rc;
+    c.precision = precision;
+    c.dbl = precision == SW_PREC_FP64 || fp64_shadow;
+
+    TableImage im;
+    build_tables(p, q, im);
+    if (!im.complete()) return fail(SW_ERR_INVALID, "internal error: incomplete parameter tables");
+    const uint32_t nlen = ring_len(current_tuning());
+    Layout &L = c.L;
+    L = layout(nullptr, n, p->matrix_length, im.bytes.size(), c.dbl, rng == SW_RNG_MT19937, nlen);
+    if (L.bytes > ctx.ws_size) {
+        if (ctx.ws) {
+            SW_CUDA(cudaStreamSynchronize(st));
+            cudaFree(ctx.ws);
+            ctx.ws = nullptr;
+            ctx.ws_size = 0;
+        }
+        cudaError_t e = cudaMalloc(&ctx.ws, L.bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SW_ERR_NOMEM, "workspace of " + std::to_string(L.bytes >> 20) +
+                                          " MiB: " + cudaGetErrorString(e));
+        }
+        ctx.ws_size = L.bytes;
+    }
+    L = layout(ctx.ws, n, p->matrix_length, im.bytes.size(), c.dbl, rng == SW_RNG_MT19937, nlen);
+    // a pageable source: the copy has taken `im` by the time it returns
+    SW_CUDA(cudaMemcpyAsync(L.tables, im.bytes.data(), im.bytes.size(), cudaMemcpyHostToDevice, st));
+
+    c.P = dev_params(p, q);
+    c.P.rng = rng;
+    c.P.field_bf16 = bf16 ? 1 : 0;
+    c.Tb = dev_tables(im, L.tables);
+    c.LT = logf_tables(ctx);
+    if (rng == SW_RNG_MINSTD && !(c.LT.ms_delta = minstd_delta_table())) return SW_ERR_CUDA;
+
+    const sw_tuning tu = current_tuning();
+    // 0 = 1: on GB300 the co-resident seed and walk kernels slow each other down by about what
+    // the overlap saves (SE 1e6 spins: 194 ms per call with 1 chunk, 191 with 4, 198 with 8)
+    uint32_t C = tu.seed_chunks ? tu.seed_chunks : 1u;
+    c.C = std::min<uint32_t>(std::min<uint32_t>(C, kMaxSeedChunks), (uint32_t)n);
+    c.b = seed_chunks(c.P, c.C);
+    // high spin ids jump ahead instead of discarding (the previous call has finished with the
+    // table: every call waits for its work before it returns)
+    sw::JumpTable jt;
+    if (c.P.rng == SW_RNG_MT19937) {
+        const int rj = jump_table(c.P.seed, 0, c.P.n_spins, jump_min_z(tu), ctx.d_jump,
+                                  ctx.jump_words, jt);
+        if (rj) return rj;
+    }
+    cudaStream_t ss = ctx.seed_st;
+    SW_CUDA(cudaEventRecord(ctx.ev[0], ss));              // the call's first GPU work
+    // seeding of every chunk, each chunk bracketed by events (start, done)
+    for (uint32_t k = 0; k < c.C; k++) {
+        SW_CUDA(cudaEventRecord(ctx.pev[4 + 2 * k], ss));
+        SW_CUDA(sw::launch_seed_range(c.P, L.G, c.b[k], c.b[k + 1], ss, &jt));
+        SW_CUDA(cudaEventRecord(ctx.pev[5 + 2 * k], ss));
+        c.launches++;
+    }
+    return SW_OK;
+}
+
 // The walk of one call: the reference's per-spin loop over time points (kernels.cu:107-232) cut
 // into rounds of refill + walk, at which the generator rings are topped up.
 //
-// Pipeline: the spins are seeded in chunks of equal seeding cost on a low-priority stream; on a
-// high-priority stream each chunk, once seeded, is initialised and given the rounds that no spin
-// can finish sooner than (ceil(steps / 256)), so the walk of chunk c runs beside the seeding of
-// chunk c + 1 (the seed is integer-issue bound, the walk latency bound). Then rounds over all
-// spins until none is active. Adds kernel times and rounds to g_timing.
-int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
-                  const sw::DevParams &P, const sw::DevTables &Tb, const sw::LogfTables &LT,
-                  const Layout &L, const sw::Outputs &O, const float *d_M0, const float *d_XYZ0,
-                  uint32_t C, uint32_t &launches) {
+// Pipeline: the spins were seeded in chunks of equal seeding cost on a low-priority stream
+// (begin_call); on a high-priority stream each chunk, once seeded, is initialised and given the
+// rounds that no spin can finish sooner than (ceil(steps / ring steps)), so the walk of chunk c
+// runs beside the seeding of chunk c + 1 (the seed is integer-issue bound, the walk latency
+// bound). Then rounds over all spins until none is active. Adds kernel times and rounds to
+// g_timing.
+int walk_pipeline(DeviceCtx &ctx, const sw_params *p, Call &c, const sw::Outputs &O,
+                  const float *d_M0, const float *d_XYZ0) {
     cudaEvent_t *ev = ctx.ev.data();
-    cudaStream_t ss = ctx.seed_st;
+    const sw::DevParams &P = c.P;
+    const Layout &L = c.L;
+    const uint32_t C = c.C;
+    const std::vector<uint32_t> &b = c.b;
+    uint32_t &launches = c.launches;
     const sw_tuning tu = current_tuning();
-    const std::vector<uint32_t> b = seed_chunks(P, C);
     const uint64_t steps = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
     const uint64_t per_round = L.G.nlen / 3;      // steps a full ring lasts
     const uint64_t r0 = (steps + per_round - 1) / per_round;
@@ -309,7 +412,7 @@ int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
         const bool t = timed < kMaxTimedChunks;
         cudaEvent_t *e = ev + 4 + 3 * timed;
         if (t) SW_CUDA(cudaEventRecord(e[0], st));
-        SW_CUDA(sw::launch_refill_range(P, L.G, L.S, LT, lo, hi, st));
+        SW_CUDA(sw::launch_refill_range(P, L.G, L.S, c.LT, lo, hi, st));
         if (t) SW_CUDA(cudaEventRecord(e[1], st));
         if (tu.resort_interval && r % tu.resort_interval == 0) {
             sw::OrderState Qh = L.Q;                    // each half sorts with its own histogram
@@ -317,29 +420,15 @@ int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
             SW_CUDA(sw::launch_order(P, L.S, Qh, lo, hi, st));
             launches += 3;
         }
-        SW_CUDA(sw::launch_walk_range(precision, dbl, P, Tb, L.vox, L.S, L.G, O, L.active + 2 * h,
-                                      lo, hi, st, tu.resort_interval ? L.Q.order : nullptr,
+        SW_CUDA(sw::launch_walk_range(c.precision, c.dbl, P, c.Tb, L.vox, L.S, L.G, O,
+                                      L.active + 2 * h, lo, hi, st,
+                                      tu.resort_interval ? L.Q.order : nullptr,
                                       (int)tu.walk_block, walk_grid_cap(tu)));
         if (t) SW_CUDA(cudaEventRecord(e[2], st));
         if (t) timed++;
         launches += 2;
         return SW_OK;
     };
-    // high spin ids jump ahead instead of discarding (the previous call has finished with the
-    // table: every call waits for its work before it returns)
-    sw::JumpTable jt;
-    if (P.rng == SW_RNG_MT19937) {
-        const int rj = jump_table(P.seed, 0, P.n_spins, jump_min_z(tu), ctx.d_jump,
-                                  ctx.jump_words, jt);
-        if (rj) return rj;
-    }
-    // seeding of every chunk, each chunk bracketed by events (start, done)
-    for (uint32_t c = 0; c < C; c++) {
-        SW_CUDA(cudaEventRecord(ctx.pev[4 + 2 * c], ss));
-        SW_CUDA(sw::launch_seed_range(P, L.G, b[c], b[c + 1], ss, &jt));
-        SW_CUDA(cudaEventRecord(ctx.pev[5 + 2 * c], ss));
-        launches++;
-    }
     if (H == 2) {                          // the second stream starts after the call's pack
         SW_CUDA(cudaEventRecord(ctx.pev[2], ws[0]));
         SW_CUDA(cudaStreamWaitEvent(ws[1], ctx.pev[2], 0));
@@ -347,11 +436,12 @@ int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
     int rc;
     // the first r0 rounds (no spin can finish sooner) of each seeded piece, without waiting
     for (uint32_t h = 0; h < H; h++)
-        for (uint32_t c = 0; c < C; c++) {
-            const uint32_t lo = std::max(b[c], hb[h]), hi = std::min(b[c + 1], hb[h + 1]);
+        for (uint32_t k = 0; k < C; k++) {
+            const uint32_t lo = std::max(b[k], hb[h]), hi = std::min(b[k + 1], hb[h + 1]);
             if (hi <= lo) continue;
-            SW_CUDA(cudaStreamWaitEvent(ws[h], ctx.pev[5 + 2 * c], 0));
-            SW_CUDA(sw::launch_init_range(P, Tb, L.vox, d_M0, d_XYZ0, L.S, O, dbl, lo, hi, ws[h]));
+            SW_CUDA(cudaStreamWaitEvent(ws[h], ctx.pev[5 + 2 * k], 0));
+            SW_CUDA(sw::launch_init_range(P, c.Tb, L.vox, d_M0, d_XYZ0, L.S, O, c.dbl, lo, hi,
+                                          ws[h]));
             launches++;
             for (uint64_t r = 0; r < r0; r++)
                 if ((rc = round(h, lo, hi, r))) return rc;
@@ -384,12 +474,52 @@ int walk_pipeline(DeviceCtx &ctx, const sw_params *p, int precision, bool dbl,
         g_timing.refill_ms += a;
         g_timing.walk_ms += w;
     }
-    for (uint32_t c = 0; c < C; c++) {
+    for (uint32_t k = 0; k < C; k++) {
         float t = 0.f;
-        cudaEventElapsedTime(&t, ctx.pev[4 + 2 * c], ctx.pev[5 + 2 * c]);
+        cudaEventElapsedTime(&t, ctx.pev[4 + 2 * k], ctx.pev[5 + 2 * k]);
         g_timing.seed_ms += t;
     }
     g_timing.n_chunks += (uint32_t)(rounds + 1);
+    return SW_OK;
+}
+
+// The rest of a begun call, once its inputs are (or will be, in `st`'s order) on the device:
+// pack, label check, initial state and the rounds; joined back into `st`, waited for.
+int finish_call(DeviceCtx &ctx, Call &c, const sw_params *p, const float *d_field,
+                const uint8_t *d_mask, const float *d_M0, const float *d_XYZ0, float *d_M1,
+                float *d_XYZ1, uint8_t *d_T, int32_t *d_status, double *d_M1d, cudaStream_t st) {
+    const Layout &L = c.L;
+    sw::Outputs O{d_M1, d_M1d, d_XYZ1, d_T, d_status};
+    cudaEvent_t *ev = ctx.ev.data();
+    auto bail = [&](int code) { drain(ctx); return code; };
+#define SW_CUDA_B(call)                                                                    \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return bail(fail(SW_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_))); \
+    } while (0)
+    // the walk streams are ordered after the caller's stream (inputs, tables)
+    SW_CUDA_B(cudaEventRecord(ctx.pev[0], st));
+    SW_CUDA_B(cudaStreamWaitEvent(ctx.walk_st, ctx.pev[0], 0));
+    cudaStream_t ws = ctx.walk_st;
+    SW_CUDA_B(cudaMemsetAsync(L.active, 0, 2 * sizeof(uint32_t), ws));
+    SW_CUDA_B(sw::launch_pack(d_mask, p->fieldmap_exist ? d_field : nullptr, L.vox,
+                              p->matrix_length, p->n_substrate, L.active + 1, ws,
+                              c.P.field_bf16 != 0));
+    c.launches++;
+    SW_CUDA_B(cudaMemcpyAsync(ctx.h_active, L.active + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, ws));
+    SW_CUDA_B(cudaStreamSynchronize(ws));
+    if (*ctx.h_active != 0)
+        return bail(fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate"));
+    const int rc = walk_pipeline(ctx, p, c, O, d_M0, d_XYZ0);
+    if (rc) return bail(rc);
+    SW_CUDA_B(cudaEventRecord(ctx.pev[1], ws));
+    SW_CUDA_B(cudaStreamWaitEvent(st, ctx.pev[1], 0));
+    SW_CUDA_B(cudaEventRecord(ev[3], st));
+    SW_CUDA_B(cudaEventSynchronize(ev[3]));
+#undef SW_CUDA_B
+    cudaEventElapsedTime(&g_timing.total_ms, ev[0], ev[3]);
+    g_timing.n_launches = c.launches;
     return SW_OK;
 }
 
@@ -397,89 +527,18 @@ int run_device(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, const f
                const uint8_t *d_mask, const float *d_M0, const float *d_XYZ0, float *d_M1,
                float *d_XYZ1, uint8_t *d_T, int32_t *d_status, int precision, double *d_M1d,
                cudaStream_t st) {
-    g_timing = sw_timing{};
-    const size_t n = p->n_spins;
-    if (n == 0) return SW_OK;
-    const bool bf16 = (precision & SW_FIELD_BF16) != 0;
-    const uint32_t rng = (uint32_t)precision & ~(uint32_t)(SW_PREC_MASK | SW_FIELD_BF16);
-    precision &= SW_PREC_MASK;
-    if (precision != SW_PREC_FP32 && precision != SW_PREC_FP64 && precision != SW_PREC_KAHAN)
-        return fail(SW_ERR_INVALID, "precision");
-    if (rng != SW_RNG_MT19937 && rng != SW_RNG_MINSTD) return fail(SW_ERR_INVALID, "generator flavour");
-    int rc = ensure_logf(ctx);
-    if (rc) return rc;
-    const bool dbl = precision == SW_PREC_FP64 || d_M1d != nullptr;
-
-    TableImage im;
-    build_tables(p, q, im);
-    if (!im.complete()) return fail(SW_ERR_INVALID, "internal error: incomplete parameter tables");
-    const uint32_t nlen = ring_len(current_tuning());
-    Layout L = layout(nullptr, n, p->matrix_length, im.bytes.size(), dbl, rng == SW_RNG_MT19937,
-                      nlen);
-    if (L.bytes > ctx.ws_size) {
-        if (ctx.ws) {
-            SW_CUDA(cudaStreamSynchronize(st));
-            cudaFree(ctx.ws);
-            ctx.ws = nullptr;
-            ctx.ws_size = 0;
-        }
-        cudaError_t e = cudaMalloc(&ctx.ws, L.bytes);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return fail(SW_ERR_NOMEM, "workspace of " + std::to_string(L.bytes >> 20) +
-                                          " MiB: " + cudaGetErrorString(e));
-        }
-        ctx.ws_size = L.bytes;
+    if (p->n_spins == 0) {
+        g_timing = sw_timing{};
+        return SW_OK;
     }
-    L = layout(ctx.ws, n, p->matrix_length, im.bytes.size(), dbl, rng == SW_RNG_MT19937, nlen);
-    SW_CUDA(cudaMemcpyAsync(L.tables, im.bytes.data(), im.bytes.size(), cudaMemcpyHostToDevice, st));
-
-    sw::DevParams P = dev_params(p, q);
-    P.rng = rng;
-    P.field_bf16 = bf16 ? 1 : 0;
-    const sw::DevTables Tb = dev_tables(im, L.tables);
-    sw::LogfTables LT = logf_tables(ctx);
-    if (rng == SW_RNG_MINSTD && !(LT.ms_delta = minstd_delta_table())) return SW_ERR_CUDA;
-    sw::Outputs O{d_M1, d_M1d, d_XYZ1, d_T, d_status};
-    cudaEvent_t *ev = ctx.ev.data();
-    uint32_t launches = 0;
-
-    SW_CUDA(cudaEventRecord(ev[0], st));
-    // the call's work runs on the context's seed / walk streams, ordered after the caller's
-    // stream and joined back into it
-    SW_CUDA(cudaEventRecord(ctx.pev[0], st));
-    SW_CUDA(cudaStreamWaitEvent(ctx.seed_st, ctx.pev[0], 0));
-    SW_CUDA(cudaStreamWaitEvent(ctx.walk_st, ctx.pev[0], 0));
-    cudaStream_t ws = ctx.walk_st;
-    SW_CUDA(cudaMemsetAsync(L.active, 0, 2 * sizeof(uint32_t), ws));
-    SW_CUDA(sw::launch_pack(d_mask, p->fieldmap_exist ? d_field : nullptr, L.vox,
-                            p->matrix_length, p->n_substrate, L.active + 1, ws, bf16));
-    launches++;
-    SW_CUDA(cudaMemcpyAsync(ctx.h_active, L.active + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, ws));
-    SW_CUDA(cudaStreamSynchronize(ws));
-    if (*ctx.h_active != 0) {
-        SW_CUDA(cudaStreamSynchronize(ctx.seed_st));
-        return fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate");
-    }
-    const sw_tuning tu = current_tuning();
-    // 0 = 1: on GB300 the co-resident seed and walk kernels slow each other down by about what
-    // the overlap saves (SE 1e6 spins: 194 ms per call with 1 chunk, 191 with 4, 198 with 8)
-    uint32_t C = tu.seed_chunks ? tu.seed_chunks : 1u;
-    C = std::min<uint32_t>(std::min<uint32_t>(C, kMaxSeedChunks), (uint32_t)n);
-    rc = walk_pipeline(ctx, p, precision, dbl, P, Tb, LT, L, O, d_M0, d_XYZ0, C, launches);
+    Call c;
+    const int rc = begin_call(ctx, p, q, precision, d_M1d != nullptr, st, c);
     if (rc) {
-        cudaStreamSynchronize(ctx.seed_st);
-        cudaStreamSynchronize(ctx.walk_st);
-        cudaStreamSynchronize(ctx.walk_st2);
+        drain(ctx);
         return rc;
     }
-    SW_CUDA(cudaEventRecord(ctx.pev[1], ws));
-    SW_CUDA(cudaStreamWaitEvent(st, ctx.pev[1], 0));
-    SW_CUDA(cudaEventRecord(ev[3], st));
-    SW_CUDA(cudaEventSynchronize(ev[3]));
-    cudaEventElapsedTime(&g_timing.total_ms, ev[0], ev[3]);
-    g_timing.n_launches = launches;
-    return SW_OK;
+    return finish_call(ctx, c, p, d_field, d_mask, d_M0, d_XYZ0, d_M1, d_XYZ1, d_T, d_status,
+                       d_M1d, st);
 }
 
 DeviceCtx *current_ctx(int *dev_out) {
@@ -646,20 +705,41 @@ int sw_sim(const sw_params *param, const sw_sequence *seq, const float *pFieldMa
                  o_XYZ0 = slot(n * 12), o_M1 = slot(n * nte * 12), o_XYZ1 = slot(n * trj * 12),
                  o_T = slot(n * nte), o_st = slot(status ? n * 4 : 0),
                  o_M1d = slot(M1_fp64 ? n * nte * 24 : 0);
-    char *d = nullptr;
-    cudaError_t e = cudaMalloc(&d, off + 256);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return fail(SW_ERR_NOMEM, std::string("buffers: ") + cudaGetErrorString(e));
+    DeviceCtx *ctx = current_ctx(nullptr);
+    if (!ctx) return fail(SW_ERR_CUDA, "no current CUDA device");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    // the device copies of the caller's buffers live in the context's I/O region, grown on
+    // demand and kept for the next call like the workspace
+    if (off + 256 > ctx->io_size) {
+        if (ctx->io) cudaFree(ctx->io);
+        ctx->io = nullptr;
+        ctx->io_size = 0;
+        cudaError_t e = cudaMalloc(&ctx->io, off + 256);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SW_ERR_NOMEM, std::string("buffers: ") + cudaGetErrorString(e));
+        }
+        ctx->io_size = off + 256;
     }
-    auto done = [&](int code) { cudaFree(d); return code; };
+    char *d = ctx->io;
     cudaStream_t st = nullptr;
+    // the seeding starts first: it needs none of the inputs, so the host-to-device copies below
+    // (the phantom above all) run while the GPU seeds
+    Call c;
+    bool begun = false;
+    auto done = [&](int code) {
+        if (begun) drain(*ctx);
+        return code;
+    };
 #define SW_TRY(call)                                                                       \
     do {                                                                                   \
         cudaError_t e2 = (call);                                                           \
         if (e2 != cudaSuccess)                                                             \
             return done(fail(SW_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e2))); \
     } while (0)
+    if (int rc0 = begin_call(*ctx, param, seq, precision, M1_fp64 != nullptr, st, c))
+        return done(rc0);
+    begun = true;
     SW_TRY(cudaMemcpyAsync(d + o_mask, pMask, ml, cudaMemcpyHostToDevice, st));
     if (has_field) SW_TRY(cudaMemcpyAsync(d + o_field, pFieldMap, ml * 4, cudaMemcpyHostToDevice, st));
     SW_TRY(cudaMemcpyAsync(d + o_M0, M0, n * 12, cudaMemcpyHostToDevice, st));
@@ -672,15 +752,14 @@ int sw_sim(const sw_params *param, const sw_sequence *seq, const float *pFieldMa
     }
     SW_TRY(cudaMemcpyAsync(d + o_XYZ1, XYZ1, n * trj * 12, cudaMemcpyHostToDevice, st));
     if (M1_fp64) SW_TRY(cudaMemcpyAsync(d + o_M1d, M1_fp64, n * nte * 24, cudaMemcpyHostToDevice, st));
-    DeviceCtx *ctx = current_ctx(nullptr);
-    if (!ctx) return done(fail(SW_ERR_CUDA, "no current CUDA device"));
     {
-        std::lock_guard<std::mutex> lk(ctx->mu);
-        int rc2 = run_device(*ctx, param, seq, has_field ? (float *)(d + o_field) : nullptr,
-                             (uint8_t *)(d + o_mask), (float *)(d + o_M0), (float *)(d + o_XYZ0),
-                             (float *)(d + o_M1), (float *)(d + o_XYZ1), (uint8_t *)(d + o_T),
-                             status ? (int32_t *)(d + o_st) : nullptr, precision,
-                             M1_fp64 ? (double *)(d + o_M1d) : nullptr, st);
+        const int rc2 = finish_call(*ctx, c, param, has_field ? (float *)(d + o_field) : nullptr,
+                                    (uint8_t *)(d + o_mask), (float *)(d + o_M0),
+                                    (float *)(d + o_XYZ0), (float *)(d + o_M1),
+                                    (float *)(d + o_XYZ1), (uint8_t *)(d + o_T),
+                                    status ? (int32_t *)(d + o_st) : nullptr,
+                                    M1_fp64 ? (double *)(d + o_M1d) : nullptr, st);
+        begun = false;                     // finish_call drained on its own errors
         if (rc2) return done(rc2);
     }
     if (nte) {

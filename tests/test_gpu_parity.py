@@ -3,6 +3,8 @@
 Bar: trajectories (XYZ1), substrates at the echoes (T) and per-spin status are bit-exact;
 magnetisation within M_RTOL = 1e-5 of |M| (+1e-7 absolute) in the FP32 path.
 """
+import copy
+
 import numpy as np
 import pytest
 
@@ -173,6 +175,28 @@ def test_gpu_device_api_matches_host_api():
     assert bits_equal(d_XYZ1.cpu().numpy(), h["XYZ1"])
     assert bits_equal(d_T.cpu().numpy(), h["T"])
     assert np.array_equal(d_st.cpu().numpy(), h["status"])
+
+
+def test_gpu_host_call_after_refused_mask_matches():
+    """sw_sim launches its seeding before it copies the inputs in. A call refused afterwards (a
+    mask label >= n_substrate, found by the pack) leaves the device usable, and later calls,
+    of other sizes too (the device copies of the buffers are reused and grown), equal the ones
+    made before it bit for bit."""
+    pr, _ = load_golden("permeable")
+    big, _ = load_golden("se_multi_te")
+    a, a_big = _lib.run(pr), _lib.run(big)
+    bad = copy.copy(pr)
+    bad.mask = pr.mask.copy()
+    bad.mask.flat[0] = 7
+    with pytest.raises(_lib.SpinWalkError, match="substrate labels"):
+        _lib.run(bad)
+    b = _lib.run(pr)
+    b_big = _lib.run(big)
+    c = _lib.run(pr)
+    for k in ("M1", "XYZ1", "T", "status"):
+        assert bits_equal(a[k], b[k]), k
+        assert bits_equal(a[k], c[k]), k
+        assert bits_equal(a_big[k], b_big[k]), k
 
 
 def test_gpu_rejects_bad_arguments():

@@ -546,11 +546,12 @@ def c3_instances(rank=0, max_spins=None):
 
 
 def leg_batched(args, rank=0, world=1):
-    """Config 3 batched (sw_sim_batch: phantom packed once, generators seeded once for all 64
-    instances, instances in spin-range chunks on concurrent slots) against the same instances
-    run one sw_sim each. `value` is the device time of the whole call (CUDA events); `e2e` the
-    host time around it (staging copies included; every call uploads the phantom and seeds
-    again)."""
+    """Config 3 batched (sw_sim_batch: phantom packed once, pooled generator streams seeded once
+    for all 64 instances, every round one refill of the streams and one fused uniform-refill and
+    walk launch over all instances, replayed as a CUDA graph) against the same instances run one
+    sw_sim each. `value` is the whole call as the library times it (from its entry to its
+    return: phantom upload, seeding, rounds and the copies to and from the host staging);
+    `e2e` the host time around it from Python (the output arrays' allocation included)."""
     from spinwalk_gb300 import _lib
     probs, desc = c3_instances(rank, args.max_spins)
     tuning = apply_tuning(args, max(probs, key=lambda q: q.params.n_spins))
@@ -558,13 +559,16 @@ def leg_batched(args, rank=0, world=1):
     reps = max(3, min(args.steps, 5))
     for _ in range(max(3, min(args.warmup, 3))):
         _lib.run_batch(probs)
-    dev_ms, wall, launches = [], [], []
+    dev_ms, wall, launches, seed_ms, round_ms = [], [], [], [], []
     for _ in range(reps):
         t = time.perf_counter()
         _lib.run_batch(probs)
         wall.append(time.perf_counter() - t)
-        dev_ms.append(_lib.last_timing()["total_ms"])
-        launches.append(_lib.last_timing()["n_launches"])
+        lt = _lib.last_timing()
+        dev_ms.append(lt["total_ms"])
+        launches.append(lt["n_launches"])
+        seed_ms.append(lt["seed_ms"])
+        round_ms.append(lt["walk_ms"])
     plain_ms, plain_wall = 0.0, 0.0
     for p in probs:
         t = time.perf_counter()
@@ -578,6 +582,14 @@ def leg_batched(args, rank=0, world=1):
     err_idx = sorted({0, 1, 30, 31, 62, 63} | {int(np.argmax([p.params.n_spins for p in probs]))})
     return {"workload": desc["workload"], "value": value, "unit": UNIT,
             "ms_per_step": float(np.mean(dev_ms)), "steps": reps,
+            "stage_ms": {"seeding": float(np.mean(seed_ms)),
+                         "rounds": float(np.mean(round_ms)),
+                         "rest": float(np.mean(dev_ms) - np.mean(seed_ms) - np.mean(round_ms)),
+                         "note": "CUDA events on the batch's main stream; rest = the call's "
+                                 "wall time minus both (the phantom upload and the input "
+                                 "staging overlap the seeding; then the output copies to the "
+                                 "caller's buffers)"},
+            "rounds_instance_spin_steps_per_s": steps / (np.mean(round_ms) * 1e-3),
             "config": dict(desc, instance_spin_steps=int(steps)),
             "plain_one_call_per_instance": {"value": plain, "ms": plain_ms,
                                             "e2e_value": steps / plain_wall},

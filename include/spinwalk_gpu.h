@@ -226,8 +226,10 @@ int sw_sim(const sw_params *param, const sw_sequence *seq,
            float *M1, float *XYZ1, uint8_t *T, int32_t *status,
            int precision, double *M1_fp64);
 
-/* Same as sw_sim with DEVICE buffers (the cu_sim analogue). Asynchronous on `stream` except
- * for the small parameter-table uploads; sw_sync(stream) waits and reports errors. */
+/* Same as sw_sim with DEVICE buffers (the cu_sim analogue). The walk is ordered after the work
+ * already on `stream` (which may still be producing the inputs); the seeding, which reads none
+ * of them, starts at once beside it. The call returns once its own work has finished: between
+ * refill/walk rounds the host reads how many spins are still walking. */
 int sw_sim_device(const sw_params *param, const sw_sequence *seq,
                   const float *d_FieldMap, const uint8_t *d_Mask,
                   const float *d_M0, const float *d_XYZ0,

@@ -578,6 +578,7 @@ __global__ void k_init(DevParams P, DevTables Tb, const uint2 *__restrict__ vox,
 // Generator refill
 // ------------------------------------------------------------------------------------------
 constexpr int kRefillWarps = 4;
+static_assert(kRefillBatchSpins == 32u * kRefillWarps, "32 spins per warp in the batch refill");
 
 // Brings the spin's current 624-word block into shared memory (if it is not there yet),
 // regenerates it, and writes it back.
@@ -766,26 +767,58 @@ __global__ void __launch_bounds__(32 * kRefillWarps)
     }
 }
 
-// The crossing uniforms of one instance of a pooled batch: each walking spin's own gen_u ring,
-// topped up when at most half full (as k_refill does for them).
+// Instance of block b of a fused batch launch: the last descriptor whose first block is <= b
+// (descriptors in block order), found by thread 0 and shared with the block.
+template <bool WALK>
+__device__ __forceinline__ uint32_t batch_instance(const BatchInst *__restrict__ D, uint32_t n_inst,
+                                                   uint32_t *s_k) {
+    if (threadIdx.x == 0) {
+        uint32_t lo = 0, hi = n_inst;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            const uint32_t b0 = WALK ? D[mid].walk_block0 : D[mid].unif_block0;
+            if (b0 <= blockIdx.x) lo = mid; else hi = mid;
+        }
+        *s_k = lo;
+    }
+    __syncthreads();
+    return *s_k;
+}
+
+// The crossing uniforms of a pooled batch, every instance in one launch (each instance spin has
+// its own gen_u ring, topped up when at most half full, as k_refill does): block b covers
+// 32 * kRefillWarps consecutive spins of one instance, one warp per 32 of them. The warp reads
+// their counters together and tops up, one after the other, the rings of those that need it:
+// after the first round only spins that crossed substrates do, so most warps only look.
 __global__ void __launch_bounds__(32 * kRefillWarps)
-    k_refill_uniforms(RngState G, const uint32_t *__restrict__ flags, uint32_t spin_lo,
-                      uint32_t spin_hi) {
+    k_refill_uniforms_batch(const BatchInst *__restrict__ D, uint32_t n_inst) {
     __shared__ uint32_t s_mt[kRefillWarps][kMtN];
+    __shared__ uint32_t s_k;
+    const BatchInst &I = D[batch_instance<false>(D, n_inst, &s_k)];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (uint32_t spin = spin_lo + blockIdx.x * kRefillWarps + w; spin < spin_hi;
-         spin += gridDim.x * kRefillWarps) {
-        if (flags[spin] & kFlagDone) continue;
-        const uint32_t uc = G.ucnt[spin];
-        if (uc > kUnifBuf / 2) continue;
-        const uint32_t need = kUnifBuf - uc;
+    const uint32_t base = ((blockIdx.x - I.unif_block0) * kRefillWarps + w) * 32;
+    const uint32_t mine = base + lane;
+    const RngState &G = I.G;
+    bool needy = false;
+    uint32_t uc = 0;
+    if (mine < I.n_spins && !(I.S.flags[mine] & kFlagDone)) {
+        uc = G.ucnt[mine];
+        needy = uc <= kUnifBuf / 2;
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, needy);
+    while (todo) {
+        const int l = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const uint32_t spin = base + l;
+        const uint32_t c = __shfl_sync(0xffffffffu, uc, l);
+        const uint32_t need = kUnifBuf - c;
         uint32_t p = G.p_u[spin];
         refill_uniforms_mt<kUnifBuf>(G.mt_u + (size_t)spin * kMtN, p,
-                                     G.ubuf + (size_t)spin * kUnifBuf, G.uhead[spin] + uc, need,
+                                     G.ubuf + (size_t)spin * kUnifBuf, G.uhead[spin] + c, need,
                                      s_mt[w], lane);
         if (lane == 0) {
             G.p_u[spin] = p;
-            G.ucnt[spin] = uc + need;
+            G.ucnt[spin] = c + need;
         }
         __syncwarp();
     }
@@ -1109,17 +1142,21 @@ __global__ void __launch_bounds__(256, 4)
     if (lane == 0 && paused) atomicAdd(active, paused);
 }
 
-// The walk of one instance of a pooled batch: spins [spin_lo, spin_hi), generators from Q.
+// The walk of a pooled batch, every instance in one launch: block b walks 256 spins of one
+// instance (whose parameters, tables and state it reads from its descriptor), drawing their
+// steps from the pooled streams Q (G.nhead: the instance's read positions in them).
 template <int PREC, bool DBL>
 __global__ void __launch_bounds__(256, 4)
-    k_walk_pool(DevParams P, DevTables Tb, const uint2 *__restrict__ vox, SpinState S, RngState G,
-                Outputs O, PoolState Q, uint32_t *active, uint32_t spin_lo, uint32_t spin_hi) {
-    const uint32_t spin = spin_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    k_walk_batch(const BatchInst *__restrict__ D, uint32_t n_inst, const uint2 *__restrict__ vox,
+                 PoolState Q, uint32_t *active) {
+    __shared__ uint32_t s_k;
+    const BatchInst &I = D[batch_instance<true>(D, n_inst, &s_k)];
+    const uint32_t spin = (blockIdx.x - I.walk_block0) * 256 + threadIdx.x;
     bool still = false;
-    if (spin < spin_hi) {
-        const uint32_t flags = S.flags[spin];
+    if (spin < I.n_spins) {
+        const uint32_t flags = I.S.flags[spin];
         if (!(flags & kFlagDone))
-            still = walk_spin<PREC, DBL, true>(spin, flags, P, Tb, vox, S, G, O, Q);
+            still = walk_spin<PREC, DBL, true>(spin, flags, I.P, I.Tb, vox, I.S, I.G, I.O, Q);
     }
     const unsigned b = __ballot_sync(0xffffffffu, still);
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(active, (uint32_t)__popc(b));
@@ -1261,30 +1298,28 @@ cudaError_t launch_refill_pool(const PoolState &Q, const LogfTables &L, uint32_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_refill_uniforms(const RngState &G, const uint32_t *flags, uint32_t lo,
-                                   uint32_t hi, cudaStream_t st) {
-    if (hi <= lo) return cudaSuccess;
-    k_refill_uniforms<<<grid_for(hi - lo, kRefillWarps, 152 * 64), 32 * kRefillWarps, 0, st>>>(
-        G, flags, lo, hi);
+cudaError_t launch_refill_uniforms_batch(const BatchInst *D, uint32_t n_inst, uint32_t unif_blocks,
+                                         cudaStream_t st) {
+    if (!n_inst || !unif_blocks) return cudaSuccess;
+    k_refill_uniforms_batch<<<unif_blocks, 32 * kRefillWarps, 0, st>>>(D, n_inst);
     return cudaGetLastError();
 }
 
-cudaError_t launch_walk_pool_range(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
-                                   const uint2 *vox, const SpinState &S, const RngState &G,
-                                   const Outputs &O, const PoolState &Q, uint32_t *active,
-                                   uint32_t lo, uint32_t hi, cudaStream_t st) {
-    if (hi <= lo) return cudaSuccess;
-    const int g = grid_for(hi - lo, 256, 1 << 30);
+cudaError_t launch_walk_batch(int prec, bool dbl, const BatchInst *D, uint32_t n_inst,
+                              uint32_t walk_blocks, const uint2 *vox, const PoolState &Q,
+                              uint32_t *active, cudaStream_t st) {
+    if (!n_inst || !walk_blocks) return cudaSuccess;
+    const uint32_t g = walk_blocks;
     if (prec == SW_PREC_FP64)
-        k_walk_pool<SW_PREC_FP64, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, Q, active, lo, hi);
+        k_walk_batch<SW_PREC_FP64, true><<<g, 256, 0, st>>>(D, n_inst, vox, Q, active);
     else if (prec == SW_PREC_KAHAN && dbl)
-        k_walk_pool<SW_PREC_KAHAN, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, Q, active, lo, hi);
+        k_walk_batch<SW_PREC_KAHAN, true><<<g, 256, 0, st>>>(D, n_inst, vox, Q, active);
     else if (prec == SW_PREC_KAHAN)
-        k_walk_pool<SW_PREC_KAHAN, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, Q, active, lo, hi);
+        k_walk_batch<SW_PREC_KAHAN, false><<<g, 256, 0, st>>>(D, n_inst, vox, Q, active);
     else if (dbl)
-        k_walk_pool<SW_PREC_FP32, true><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, Q, active, lo, hi);
+        k_walk_batch<SW_PREC_FP32, true><<<g, 256, 0, st>>>(D, n_inst, vox, Q, active);
     else
-        k_walk_pool<SW_PREC_FP32, false><<<g, 256, 0, st>>>(P, Tb, vox, S, G, O, Q, active, lo, hi);
+        k_walk_batch<SW_PREC_FP32, false><<<g, 256, 0, st>>>(D, n_inst, vox, Q, active);
     return cudaGetLastError();
 }
 

@@ -33,17 +33,19 @@ cudaError_t launch_walk_range(int prec, bool dbl, const DevParams &P, const DevT
                               const Outputs &O, uint32_t *active, uint32_t lo, uint32_t hi,
                               cudaStream_t st, const uint32_t *order = nullptr, int block = 256,
                               int max_blocks = 0);
-// Pooled Gaussian generators of a batch (PoolState): refill of streams [0, n_streams), the
-// refill of one instance's own crossing uniforms, and its walk over spins [lo, hi) drawing from
-// the streams (G.nhead: the instance's read positions in them).
+// Pooled Gaussian generators of a batch (PoolState): refill of streams [0, n_streams).
 cudaError_t launch_refill_pool(const PoolState &Q, const LogfTables &L, uint32_t n_streams,
                                cudaStream_t st);
-cudaError_t launch_refill_uniforms(const RngState &G, const uint32_t *flags, uint32_t lo,
-                                   uint32_t hi, cudaStream_t st);
-cudaError_t launch_walk_pool_range(int prec, bool dbl, const DevParams &P, const DevTables &Tb,
-                                   const uint2 *vox, const SpinState &S, const RngState &G,
-                                   const Outputs &O, const PoolState &Q, uint32_t *active,
-                                   uint32_t lo, uint32_t hi, cudaStream_t st);
+// Spins per block of k_refill_uniforms_batch (32 per warp).
+constexpr uint32_t kRefillBatchSpins = 128;
+// The crossing-uniform refill and the walk of every instance of a pooled batch, one launch each:
+// D holds n_inst descriptors (device memory) whose block ranges tile [0, walk_blocks) and
+// [0, unif_blocks); each instance's results equal its own sw_sim run bit for bit.
+cudaError_t launch_refill_uniforms_batch(const BatchInst *D, uint32_t n_inst, uint32_t unif_blocks,
+                                         cudaStream_t st);
+cudaError_t launch_walk_batch(int prec, bool dbl, const BatchInst *D, uint32_t n_inst,
+                              uint32_t walk_blocks, const uint2 *vox, const PoolState &Q,
+                              uint32_t *active, cudaStream_t st);
 // Morton re-sort of spins [lo, hi) into Q.order (sw_order.cu).
 cudaError_t launch_order(const DevParams &P, const SpinState &S, const OrderState &Q,
                          uint32_t lo, uint32_t hi, cudaStream_t st);

@@ -15,9 +15,11 @@
 // first holds back), while with one pooled kind the slowest reader always gets a full ring.
 //
 // A round: k_refill_pool over the streams, then per instance its uniforms and its walk (one
-// launch each, on kWalkStreams streams); a stream's ring is topped up to the lowest read position
-// of the pairs that paused in the previous walk plus the ring length, so nothing unread is
-// overwritten. Results equal one sw_sim call per instance bit for bit (tests/test_batch.py).
+// launch each, on a branch of a CUDA graph captured once per call and launched once per round,
+// so that the instances' walks are independent graph nodes); a stream's ring is topped up to the
+// lowest read position of the pairs that paused in the previous walk plus the ring length, so
+// nothing unread is overwritten. Results equal one sw_sim call per instance bit for bit
+// (tests/test_batch.py).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,8 +40,6 @@ namespace {
 using namespace sw::api;
 
 constexpr int kMaxDevices = 64;
-constexpr int kWalkStreams = 8;
-
 struct PoolCtx {
     std::mutex mu;
     char *d = nullptr;                   // device workspace
@@ -48,9 +48,10 @@ struct PoolCtx {
     size_t h_bytes = 0;
     uint32_t *d_jump = nullptr;          // jump polynomials of the high spin ids
     size_t jump_words = 0;
-    cudaStream_t main = nullptr;         // pack, seeding, refills, copies
-    cudaStream_t walk[kWalkStreams] = {};
-    cudaEvent_t refilled = nullptr, walked[kWalkStreams] = {};
+    cudaStream_t main = nullptr;         // pack, seeding, rounds, copies
+    cudaStream_t side = nullptr;         // instance inputs and k_init, beside the seeding
+    cudaEvent_t side_done = nullptr;
+    cudaEvent_t stage[4] = {};           // timing: the seeding, then the rounds
     uint32_t *h_active = nullptr;        // pinned
     bool ready = false;
 };
@@ -74,27 +75,35 @@ int ensure_ctx(PoolCtx &c) {
     int lo = 0, hi = 0;
     PL_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     PL_CUDA(cudaStreamCreateWithPriority(&c.main, cudaStreamNonBlocking, hi));
-    for (auto &s : c.walk) PL_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, hi));
-    PL_CUDA(cudaEventCreateWithFlags(&c.refilled, cudaEventDisableTiming));
-    for (auto &e : c.walked) PL_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PL_CUDA(cudaStreamCreateWithPriority(&c.side, cudaStreamNonBlocking, hi));
+    PL_CUDA(cudaEventCreateWithFlags(&c.side_done, cudaEventDisableTiming));
+    for (auto &e : c.stage) PL_CUDA(cudaEventCreate(&e));
     PL_CUDA(cudaMallocHost(&c.h_active, sizeof(uint32_t)));
     c.ready = true;
     return SW_OK;
 }
 
-// Large host copies split across threads (one core copies about 10 GB/s).
-void par_copy(void *dst, const void *src, size_t bytes) {
-    constexpr size_t kPiece = 4 << 20;
-    if (bytes < 2 * kPiece) {
-        std::memcpy(dst, src, bytes);
-        return;
-    }
-    const int64_t pieces = (int64_t)((bytes + kPiece - 1) / kPiece);
-#pragma omp parallel for num_threads(8) schedule(static)
-    for (int64_t i = 0; i < pieces; i++) {
-        const size_t o = (size_t)i * kPiece, n = std::min(kPiece, bytes - o);
-        std::memcpy(static_cast<char *>(dst) + o, static_cast<const char *>(src) + o, n);
-    }
+// Host copies between the caller's buffers and the pinned staging, all of a call's arrays at
+// once: cut into pieces of 2 MiB and spread over every core (one core copies about 10 GB/s,
+// and most instances' arrays are too small to split on their own).
+struct CopyJob {
+    void *dst;
+    const void *src;
+    size_t bytes;
+};
+
+void par_copy_all(const std::vector<CopyJob> &jobs) {
+    constexpr size_t kPiece = 2 << 20;
+    std::vector<CopyJob> pieces;
+    for (const CopyJob &j : jobs)
+        for (size_t o = 0; o < j.bytes; o += kPiece)
+            pieces.push_back(CopyJob{static_cast<char *>(j.dst) + o,
+                                     static_cast<const char *>(j.src) + o,
+                                     std::min(kPiece, j.bytes - o)});
+    const int64_t np = (int64_t)pieces.size();
+    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(np, std::min(omp_get_num_procs(), 32)));
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 1)
+    for (int64_t i = 0; i < np; i++) std::memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes);
 }
 
 struct Inst {
@@ -142,6 +151,7 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
         c.take<uint32_t>(n_max * sw::kMtN);                  // mt_r
         for (int k = 0; k < 3; k++) c.take<uint32_t>(n_max);  // p_r nw nmin
         c.take<float>(n_max * sw::kPoolNorm);
+        c.take<sw::BatchInst>(n_items);                      // descriptors of the fused launches
         for (Inst &I : in) {
             const size_t n = I.n;
             I.tables = c.take<char>(I.im.bytes.size());
@@ -224,6 +234,15 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
     taken = true;
     int rc = ensure_ctx(X);
     if (rc) return rc;
+    // whichever way the call returns, nothing of it is left running on the context's streams
+    // (the next call reuses the workspace)
+    struct Drain {
+        PoolCtx &X;
+        ~Drain() {
+            cudaStreamSynchronize(X.main);
+            cudaStreamSynchronize(X.side);
+        }
+    } drain{X};
     const LogfTables LT = device_logf_tables();
     if (!LT.tab) return SW_ERR_CUDA;
     if (need > X.d_bytes) {
@@ -260,36 +279,14 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
     Q.nw = c2.take<uint32_t>(n_max);
     Q.nmin = c2.take<uint32_t>(n_max);
     Q.nbuf = c2.take<float>(n_max * sw::kPoolNorm);
+    sw::BatchInst *d_inst = c2.take<sw::BatchInst>(n_items);
     char *d_io = X.d + state_bytes;
     cudaStream_t ms = X.main;
     uint32_t launches = 0;
 
-    // ---- phantom (mask + field -> records), generator streams ----
-    {
-        uint8_t *d_mask = nullptr;
-        float *d_field = nullptr;
-        // the I/O region is free until the instances' inputs are staged: use it for the phantom
-        // upload when it is large enough, else a temporary allocation
-        const size_t ph_bytes = ml + (p0->fieldmap_exist ? ml * 4 : 0) + 512;
-        char *tmp = nullptr;
-        char *up = d_io;
-        if (ph_bytes > io) {
-            PL_CUDA(cudaMalloc(&tmp, ph_bytes));
-            up = tmp;
-        }
-        d_mask = reinterpret_cast<uint8_t *>(up);
-        if (p0->fieldmap_exist) d_field = reinterpret_cast<float *>(up + ((ml + 255) & ~size_t(255)));
-        PL_CUDA(cudaMemcpyAsync(d_mask, pMask, ml, cudaMemcpyHostToDevice, ms));
-        if (d_field) PL_CUDA(cudaMemcpyAsync(d_field, pFieldMap, ml * 4, cudaMemcpyHostToDevice, ms));
-        PL_CUDA(cudaMemsetAsync(cnt, 0, 4 * sizeof(uint32_t), ms));
-        PL_CUDA(sw::launch_pack(d_mask, d_field, vox, (int64_t)ml, p0->n_substrate, cnt + 1, ms, bf16));
-        launches++;
-        uint32_t bad = 0;
-        PL_CUDA(cudaMemcpyAsync(&bad, cnt + 1, 4, cudaMemcpyDeviceToHost, ms));
-        PL_CUDA(cudaStreamSynchronize(ms));
-        if (tmp) cudaFree(tmp);
-        if (bad) return fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate");
-    }
+    // ---- generator streams first (they read nothing of the call's inputs), then the phantom
+    // (mask + field -> records) beside them on the side stream ----
+    PL_CUDA(cudaEventRecord(X.stage[0], ms));
     sw::JumpTable jt;
     rc = jump_table(p0->seed, 0, (uint32_t)n_max, jump_min_z(current_tuning()), X.d_jump,
                     X.jump_words, jt);
@@ -307,6 +304,7 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
         Gs.nhead = Gs.uhead = Q.nw;
         Gs.ncnt = Gs.ucnt = Q.nmin;
         PL_CUDA(sw::launch_seed_range(Ps, Gs, 0, (uint32_t)n_max, ms, &jt));
+        PL_CUDA(cudaEventRecord(X.stage[1], ms));
         launches++;
         // each instance's gen_u starts from the same seeded state, before any refill moves it
         for (Inst &I : in) {
@@ -318,19 +316,69 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
             PL_CUDA(cudaMemsetAsync(I.G.ucnt, 0, I.n * 4, ms));
         }
     }
+    cudaStream_t w0 = X.side;
+    {
+        uint8_t *d_mask = nullptr;
+        float *d_field = nullptr;
+        // the I/O region is free until the instances' inputs are staged (uploaded later on the
+        // same stream): use it for the phantom upload when it is large enough, else a temporary
+        // allocation
+        const size_t ph_bytes = ml + (p0->fieldmap_exist ? ml * 4 : 0) + 512;
+        char *tmp = nullptr;
+        char *up = d_io;
+        auto bail = [&](int code) {          // the seeding is in flight on the main stream
+            cudaStreamSynchronize(ms);
+            cudaStreamSynchronize(w0);
+            if (tmp) cudaFree(tmp);
+            return code;
+        };
+        if (ph_bytes > io) {
+            const cudaError_t e = cudaMalloc(&tmp, ph_bytes);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                tmp = nullptr;
+                return bail(fail(SW_ERR_NOMEM, std::string("phantom upload: ") + cudaGetErrorString(e)));
+            }
+            up = tmp;
+        }
+        d_mask = reinterpret_cast<uint8_t *>(up);
+        if (p0->fieldmap_exist) d_field = reinterpret_cast<float *>(up + ((ml + 255) & ~size_t(255)));
+        cudaError_t e = cudaMemcpyAsync(d_mask, pMask, ml, cudaMemcpyHostToDevice, w0);
+        if (e == cudaSuccess && d_field)
+            e = cudaMemcpyAsync(d_field, pFieldMap, ml * 4, cudaMemcpyHostToDevice, w0);
+        if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, 4 * sizeof(uint32_t), w0);
+        if (e == cudaSuccess)
+            e = sw::launch_pack(d_mask, d_field, vox, (int64_t)ml, p0->n_substrate, cnt + 1, w0, bf16);
+        uint32_t bad = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, cnt + 1, 4, cudaMemcpyDeviceToHost, w0);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(w0);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return bail(fail(SW_ERR_CUDA, std::string("phantom: ") + cudaGetErrorString(e)));
+        }
+        launches++;
+        if (bad) return bail(fail(SW_ERR_INVALID, "the mask holds substrate labels >= n_substrate"));
+        if (tmp) {
+            cudaFree(tmp);
+            tmp = nullptr;
+        }
+    }
 
     // ---- instances: inputs (and the outputs' current contents) staged, uploaded, k_init ----
-    for (Inst &I : in) {
-        const sw_instance &it = *I.it;
-        par_copy(X.h + I.o_M0, it.M0, I.n * 12);
-        par_copy(X.h + I.o_XYZ0, it.XYZ0, I.n * 12);
-        if (I.nte) {
-            par_copy(X.h + I.o_M1, it.M1, I.n * I.nte * 12);
-            par_copy(X.h + I.o_T, it.T, I.n * I.nte);
+    {
+        std::vector<CopyJob> jobs;
+        for (Inst &I : in) {
+            const sw_instance &it = *I.it;
+            jobs.push_back({X.h + I.o_M0, it.M0, I.n * 12});
+            jobs.push_back({X.h + I.o_XYZ0, it.XYZ0, I.n * 12});
+            if (I.nte) {
+                jobs.push_back({X.h + I.o_M1, it.M1, I.n * I.nte * 12});
+                jobs.push_back({X.h + I.o_T, it.T, I.n * I.nte});
+            }
+            jobs.push_back({X.h + I.o_XYZ1, it.XYZ1, I.n * I.trj * 12});
         }
-        par_copy(X.h + I.o_XYZ1, it.XYZ1, I.n * I.trj * 12);
+        par_copy_all(jobs);
     }
-    cudaStream_t w0 = X.walk[0];
     PL_CUDA(cudaMemcpyAsync(d_io, X.h, io, cudaMemcpyHostToDevice, w0));
     std::vector<sw::DevTables> Tb(n_items);
     std::vector<sw::Outputs> O(n_items);
@@ -348,8 +396,8 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
                                       I.dbl, 0, (uint32_t)I.n, w0));
         launches++;
     }
-    PL_CUDA(cudaEventRecord(X.walked[0], w0));
-    PL_CUDA(cudaStreamWaitEvent(ms, X.walked[0], 0));
+    PL_CUDA(cudaEventRecord(X.side_done, w0));
+    PL_CUDA(cudaStreamWaitEvent(ms, X.side_done, 0));
 
     // ---- rounds ----
     uint64_t steps_max = 0, max_rounds = 64;
@@ -359,54 +407,113 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
         steps_max = std::max(steps_max, st);
         max_rounds = std::max<uint64_t>(max_rounds, 64 + st * (p->max_iterations + 2));
     }
+    // Descriptors of the walking instances for the fused launches, in block order.
+    std::vector<sw::BatchInst> desc;
+    uint32_t walk_blocks = 0, unif_blocks = 0;
+    for (uint32_t i = 0; i < n_items; i++) {
+        const Inst &I = in[i];
+        if (!I.n) continue;
+        sw::BatchInst b{};
+        b.P = I.P;
+        b.Tb = Tb[i];
+        b.S = I.S;
+        b.G = I.G;
+        b.O = O[i];
+        b.n_spins = (uint32_t)I.n;
+        b.walk_block0 = walk_blocks;
+        b.unif_block0 = unif_blocks;
+        walk_blocks += (uint32_t)((I.n + 255) / 256);
+        unif_blocks += (uint32_t)((I.n + sw::kRefillBatchSpins - 1) / sw::kRefillBatchSpins);
+        desc.push_back(b);
+    }
+    const uint32_t n_desc = (uint32_t)desc.size();
+    PL_CUDA(cudaMemcpyAsync(d_inst, desc.data(), n_desc * sizeof(sw::BatchInst),
+                            cudaMemcpyHostToDevice, ms));
+    // One round as a CUDA graph, captured once per call and launched once per round: the pooled
+    // refill of the Gaussian streams, then the crossing uniforms and the walk of every instance,
+    // each as one launch over all instances (blocks dealt out instance by instance). Every
+    // kernel reads its state from the workspace, so the same graph serves every round; results
+    // equal one sw_sim call per instance bit for bit.
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const uint32_t round_kernels = 3;
+    auto drop_graph = [&]() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    };
+    auto capture_round = [&]() -> int {
+        PL_CUDA(cudaStreamBeginCapture(ms, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        auto ok = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
+        ok(cudaMemsetAsync(cnt, 0, sizeof(uint32_t), ms));
+        ok(sw::launch_refill_pool(Q, LT, (uint32_t)n_max, ms));
+        ok(sw::launch_refill_uniforms_batch(d_inst, n_desc, unif_blocks, ms));
+        ok(sw::launch_walk_batch(prec, prec == SW_PREC_FP64, d_inst, n_desc, walk_blocks, vox, Q,
+                                 cnt, ms));
+        const cudaError_t ec = cudaStreamEndCapture(ms, &graph);
+        if (e == cudaSuccess) e = ec;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            drop_graph();
+            return fail(SW_ERR_CUDA, std::string("round graph: ") + cudaGetErrorString(e));
+        }
+        return SW_OK;
+    };
+    rc = capture_round();
+    if (rc) return rc;
+    PL_CUDA(cudaEventRecord(X.stage[2], ms));
     // every pair needs 3 deviates per step and a round gives at most kPoolNorm: no pair can
     // finish sooner than r0 rounds, which are issued without waiting
     const uint64_t r0 = std::max<uint64_t>(1, (3 * steps_max + sw::kPoolNorm - 1) / sw::kPoolNorm);
     uint64_t rounds = 0;
     for (;; rounds++) {
         if (rounds >= max_rounds) {
-            for (auto s : X.walk) cudaStreamSynchronize(s);
             cudaStreamSynchronize(ms);
+            drop_graph();
             return fail(SW_ERR_TIMEOUT, "walk did not finish");
         }
-        PL_CUDA(cudaMemsetAsync(cnt, 0, sizeof(uint32_t), ms));
-        PL_CUDA(sw::launch_refill_pool(Q, LT, (uint32_t)n_max, ms));
-        PL_CUDA(cudaEventRecord(X.refilled, ms));
-        launches++;
-        for (int k = 0; k < kWalkStreams; k++) PL_CUDA(cudaStreamWaitEvent(X.walk[k], X.refilled, 0));
-        for (uint32_t i = 0; i < n_items; i++) {
-            const Inst &I = in[i];
-            if (!I.n) continue;
-            cudaStream_t ws = X.walk[i % kWalkStreams];
-            PL_CUDA(sw::launch_refill_uniforms(I.G, I.S.flags, 0, (uint32_t)I.n, ws));
-            PL_CUDA(sw::launch_walk_pool_range(prec, I.dbl, I.P, Tb[i], vox, I.S, I.G, O[i], Q, cnt,
-                                               0, (uint32_t)I.n, ws));
-            launches += 2;
+        cudaError_t e = cudaGraphLaunch(exec, ms);
+        if (e == cudaSuccess && rounds + 1 >= r0) {
+            e = cudaMemcpyAsync(X.h_active, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, ms);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ms);
         }
-        for (int k = 0; k < kWalkStreams; k++) {
-            PL_CUDA(cudaEventRecord(X.walked[k], X.walk[k]));
-            PL_CUDA(cudaStreamWaitEvent(ms, X.walked[k], 0));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            cudaStreamSynchronize(ms);
+            drop_graph();
+            return fail(SW_ERR_CUDA, std::string("round: ") + cudaGetErrorString(e));
         }
-        if (rounds + 1 < r0) continue;
-        PL_CUDA(cudaMemcpyAsync(X.h_active, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, ms));
-        PL_CUDA(cudaStreamSynchronize(ms));
-        if (*X.h_active == 0) break;
+        if (rounds + 1 >= r0 && *X.h_active == 0) break;
     }
+    drop_graph();
+    launches += round_kernels * (uint32_t)(rounds + 1);
+    PL_CUDA(cudaEventRecord(X.stage[3], ms));
 
     // ---- outputs ----
     PL_CUDA(cudaMemcpyAsync(X.h + out_begin, d_io + out_begin, io - out_begin,
                             cudaMemcpyDeviceToHost, ms));
     PL_CUDA(cudaStreamSynchronize(ms));
-    for (Inst &I : in) {
-        const sw_instance &it = *I.it;
-        if (I.nte) {
-            par_copy(it.M1, X.h + I.o_M1, I.n * I.nte * 12);
-            par_copy(it.T, X.h + I.o_T, I.n * I.nte);
+    {
+        std::vector<CopyJob> jobs;
+        for (Inst &I : in) {
+            const sw_instance &it = *I.it;
+            if (I.nte) {
+                jobs.push_back({it.M1, X.h + I.o_M1, I.n * I.nte * 12});
+                jobs.push_back({it.T, X.h + I.o_T, I.n * I.nte});
+            }
+            jobs.push_back({it.XYZ1, X.h + I.o_XYZ1, I.n * I.trj * 12});
+            if (it.status) jobs.push_back({it.status, X.h + I.o_st, I.n * 4});
         }
-        par_copy(it.XYZ1, X.h + I.o_XYZ1, I.n * I.trj * 12);
-        if (it.status) par_copy(it.status, X.h + I.o_st, I.n * 4);
+        par_copy_all(jobs);
     }
     g_timing.n_chunks = (uint32_t)(rounds + 1);          // refill/walk rounds
     g_timing.n_launches = launches;
+    // stage times (CUDA events on the main stream): the seeding; the rounds (the pooled
+    // refills, uniforms and walks together); the call's wall time is set by the caller
+    cudaEventElapsedTime(&g_timing.seed_ms, X.stage[0], X.stage[1]);
+    cudaEventElapsedTime(&g_timing.walk_ms, X.stage[2], X.stage[3]);
     return SW_OK;
 }

@@ -135,6 +135,20 @@ struct Outputs {
     unsigned long long *cnt = nullptr;
 };
 
+// One instance of a fused batch launch (k_walk_batch, k_refill_uniforms_batch): what the
+// per-instance kernels take as parameters, read by each block from device memory. Blocks are
+// dealt out instance by instance: instance k owns the walk blocks [walk_block0, +ceil(n/256))
+// and the uniform-refill blocks [unif_block0, +ceil(n/128)).
+struct BatchInst {
+    DevParams P;
+    DevTables Tb;
+    SpinState S;
+    RngState G;
+    Outputs O;
+    uint32_t n_spins;
+    uint32_t walk_block0, unif_block0;
+};
+
 // Walk order of the spins (Morton re-sort, sw_order.cu). order and key are indexed by global
 // spin id like SpinState; hist has order_hist_words() counters.
 constexpr int kOrderMaxBitsPerAxis = 6;

@@ -1,6 +1,8 @@
 """sw_sim_batch: several instances on one phantom with one seeding of the generators (the scale
 loop of src/sim/monte_carlo.cu:273-337 and mixed sweeps). Every instance must equal its own
 sw_sim run bit for bit."""
+import copy
+
 import numpy as np
 import pytest
 
@@ -52,14 +54,15 @@ def test_batch_equals_one_run_per_instance():
 @pytest.mark.gpu
 def test_batch_counts_its_work():
     """One pack + one seeding of the pooled generator streams, k_init per instance, then rounds
-    of one refill of the streams and, per instance, a refill of its crossing uniforms and its
-    walk; at least one round."""
+    of three launches whatever the number of instances: the refill of the streams, the crossing
+    uniforms of every instance and the walk of every instance; at least one round."""
     probs = _instances()
     _lib.run_batch(probs)
     t = _lib.last_timing()
     busy = sum(1 for pr in probs if pr.params.n_spins)
+    assert busy > 1
     assert t["n_chunks"] >= 1
-    assert t["n_launches"] == 2 + busy + t["n_chunks"] * (1 + 2 * busy)
+    assert t["n_launches"] == 2 + busy + 3 * t["n_chunks"]
 
 
 def test_batch_rejects_mixed_seeds_and_phantoms():
@@ -128,5 +131,26 @@ def test_pooled_batch_with_jump_ahead_seeds_and_the_minstd_flavour():
     for k, (pr, b) in enumerate(zip(probs, batch)):
         if pr.params.n_spins:
             one = _lib.run(pr, precision=0x100)
+            for key in ("M1", "XYZ1", "T", "status"):
+                assert bits_equal(b[key], one[key]), (k, key)
+
+
+@pytest.mark.gpu
+def test_batch_refused_mask_then_batch_matches():
+    """The pooled batch seeds its generator streams before it uploads the phantom. A batch refused
+    afterwards (a mask label >= n_substrate, found by the pack) waits for that seeding, and the
+    next batch equals one run per instance bit for bit."""
+    probs = _instances()
+    bad = [copy.copy(pr) for pr in probs]
+    mask = probs[0].mask.copy()
+    mask.flat[0] = 9
+    for pr in bad:
+        pr.mask = mask
+    with pytest.raises(_lib.SpinWalkError, match="substrate labels"):
+        _lib.run_batch(bad)
+    batch = _lib.run_batch(probs)
+    for k, (pr, b) in enumerate(zip(probs, batch)):
+        if pr.params.n_spins:
+            one = _lib.run(pr)
             for key in ("M1", "XYZ1", "T", "status"):
                 assert bits_equal(b[key], one[key]), (k, key)

@@ -312,7 +312,9 @@ int sw_sim_device_noalloc(const sw_params *param, const sw_sequence *seq,
                           void *stream);
 
 /* Timing of the kernels launched by the last sw_sim / sw_sim_device call on this thread
- * (milliseconds, CUDA events on the launching stream): seeding, RNG refill, walk, total. */
+ * (milliseconds, CUDA events on the launching stream): seeding, RNG refill, walk, total. After
+ * sw_sim_batch with pooled generators: seed_ms the seeding of the streams, walk_ms all rounds
+ * (refills and walks together), refill_ms 0, total_ms the call's wall time. */
 typedef struct sw_timing {
     float seed_ms, refill_ms, walk_ms, total_ms;
     uint32_t n_chunks;       /* refill+walk rounds                                   */
@@ -411,7 +413,11 @@ typedef struct sw_instance {
  * depends only on seed + s (src/sim/kernels.cu:82-88), so the instances (which must share the
  * seed, phantom size, substrate count and fieldmap) start from prefixes of one seeding of the
  * largest instance. pFieldMap is in degrees per time step (already scaled, as for sw_sim).
- * No reference counterpart: the reference re-seeds every spin for every scale. */
+ * With the std::mt19937 generators, instances also share one Gaussian stream per spin id, and
+ * every refill/walk round is one launch of each kernel over all instances, replayed as a CUDA
+ * graph; above half the free device memory, and with SW_RNG_MINSTD, the instances run as jobs
+ * of an internal serving engine instead. No reference counterpart: the reference re-seeds every
+ * spin for every scale. */
 int sw_sim_batch(const sw_instance *items, uint32_t n_items, const float *pFieldMap,
                  const uint8_t *pMask, int precision);
 

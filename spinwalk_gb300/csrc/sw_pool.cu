@@ -434,15 +434,21 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
     // each as one launch over all instances (blocks dealt out instance by instance). Every
     // kernel reads its state from the workspace, so the same graph serves every round; results
     // equal one sw_sim call per instance bit for bit.
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
+    struct RoundGraph {                      // destroyed on every way out of the call
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        void drop() {
+            if (exec) cudaGraphExecDestroy(exec);
+            if (graph) cudaGraphDestroy(graph);
+            exec = nullptr;
+            graph = nullptr;
+        }
+        ~RoundGraph() { drop(); }
+    } rg;
+    cudaGraph_t &graph = rg.graph;
+    cudaGraphExec_t &exec = rg.exec;
     const uint32_t round_kernels = 3;
-    auto drop_graph = [&]() {
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        exec = nullptr;
-        graph = nullptr;
-    };
+    auto drop_graph = [&]() { rg.drop(); };
     auto capture_round = [&]() -> int {
         PL_CUDA(cudaStreamBeginCapture(ms, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = cudaSuccess;

@@ -292,10 +292,12 @@ def run(problem, precision=abi.SW_PREC_FP32, fp64_shadow=False, fill=0.0):
     return out
 
 
-def run_batch(problems, precision=abi.SW_PREC_FP32, fill=0.0):
+def run_batch(problems, precision=abi.SW_PREC_FP32, fill=0.0, outs=None):
     """sw_sim_batch over problem.Problem instances that share the phantom and the seed (the
-    phantom arrays of the first are used). Returns one output dict per instance, as run()."""
-    outs = [dict(zip(("M1", "XYZ1", "T", "status"), pr.outputs(fill))) for pr in problems]
+    phantom arrays of the first are used). Returns one output dict per instance, as run();
+    `outs` (the dicts of an earlier call on the same problems) are written again in place."""
+    if outs is None:
+        outs = [dict(zip(("M1", "XYZ1", "T", "status"), pr.outputs(fill))) for pr in problems]
     arr = (abi.SwInstance * len(problems))()
     for a, pr, o in zip(arr, problems, outs):
         a.param = C.pointer(pr.params)

@@ -59,8 +59,9 @@ __global__ void k_pack(const uint8_t *__restrict__ mask, const float *__restrict
 // bounds this kernel (integer pipes), not memory.
 constexpr int kSeedWarps = 4;
 
+template <bool FAN>
 __global__ void __launch_bounds__(32 * kSeedWarps)
-    k_seed(DevParams P, RngState G, uint32_t spin_lo, uint32_t spin_hi) {
+    k_seed(DevParams P, RngState G, uint32_t spin_lo, uint32_t spin_hi, SeedCopies F) {
     __shared__ uint32_t s_mt[2 * kSeedWarps][kMtN];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, half = lane >> 4, hl = lane & 15;
     uint32_t *s = s_mt[2 * w + half];
@@ -110,6 +111,27 @@ __global__ void __launch_bounds__(32 * kSeedWarps)
                 G.uhead[spin] = 0;
                 G.ucnt[spin] = 0;
             }
+        }
+        if (FAN) {              // further copies: staged in the half warp's block, stored coalesced
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+#pragma unroll
+                for (int j = 0; j < 13; j++) s[208 * k + 13 * hl + j] = b[k][j];
+            __syncwarp();
+            if (valid)
+                for (uint32_t d = 0; d < F.n; d++) {
+                    const SeedCopy c = F.d[d];
+                    if (spin >= c.n) continue;
+                    uint32_t *dst = c.mt + (size_t)spin * kMtN;
+                    for (int i = hl; i < kMtN; i += 16) dst[i] = s[i];
+                    if (hl == 0) {
+                        c.p[spin] = p;
+                        c.c0[spin] = 0;
+                        c.c1[spin] = 0;
+                        c.c2[spin] = 0;
+                    }
+                }
+            __syncwarp();       // the block is reseeded in the next pass
         }
     }
 }
@@ -260,9 +282,10 @@ struct JumpPairs {
     }
 };
 
+template <bool FAN>
 __global__ void __launch_bounds__(96, kJumpBlocksPerSm)
     k_seed_jump(DevParams P, RngState G, const uint32_t *__restrict__ polys, uint64_t R_lo,
-                JumpPairs pairs) {
+                JumpPairs pairs, SeedCopies F) {
     extern __shared__ uint32_t s_jump[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, half = lane >> 4, hl = lane & 15;
     const int t = threadIdx.x;
@@ -375,8 +398,8 @@ __global__ void __launch_bounds__(96, kJumpBlocksPerSm)
             const uint32_t v = q < kMtN - 1 ? hp[q + 1] : mt_twist1(hp[0], hp[1], hp[397]);
             G.mt_r[(size_t)spin * kMtN + q] = v;
             G.mt_u[(size_t)spin * kMtN + q] = v;
+            const uint32_t pos = (uint32_t)(P.seed + spin - (uint64_t)kMtN * (R - 1));
             if (q == 0) {
-                const uint32_t pos = (uint32_t)(P.seed + spin - (uint64_t)kMtN * (R - 1));
                 G.p_r[spin] = pos;
                 G.p_u[spin] = pos;
                 G.nhead[spin] = 0;
@@ -384,6 +407,18 @@ __global__ void __launch_bounds__(96, kJumpBlocksPerSm)
                 G.uhead[spin] = 0;
                 G.ucnt[spin] = 0;
             }
+            if (FAN)
+                for (uint32_t d = 0; d < F.n; d++) {
+                    const SeedCopy c = F.d[d];
+                    if (spin >= c.n) continue;
+                    c.mt[(size_t)spin * kMtN + q] = v;
+                    if (q == 0) {
+                        c.p[spin] = pos;
+                        c.c0[spin] = 0;
+                        c.c1[spin] = 0;
+                        c.c2[spin] = 0;
+                    }
+                }
         }
     }
 }
@@ -1204,7 +1239,7 @@ cudaError_t launch_seed(const DevParams &P, const RngState &G, cudaStream_t st) 
 }
 
 cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo, uint32_t hi,
-                              cudaStream_t st, const JumpTable *jt) {
+                              cudaStream_t st, const JumpTable *jt, SeedCopies fan) {
     if (hi <= lo) return cudaSuccess;
     if (P.rng == SW_RNG_MINSTD) {
         k_seed_minstd<<<grid_for(hi - lo, 256, 1 << 30), 256, 0, st>>>(P, G, lo, hi);
@@ -1219,13 +1254,20 @@ cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo
                        mt_discard_twists(P.seed + hi - 1) >= jt->R_hi))
             return cudaErrorInvalidValue;            // the table does not cover these spins
     }
-    if (c > lo)
-        k_seed<<<grid_for(((int64_t)c - lo + 1) / 2, kSeedWarps, 1 << 30), 32 * kSeedWarps, 0, st>>>(
-            P, G, lo, c);
+    if (c > lo) {
+        const int grid = grid_for(((int64_t)c - lo + 1) / 2, kSeedWarps, 1 << 30);
+        if (fan.n)
+            k_seed<true><<<grid, 32 * kSeedWarps, 0, st>>>(P, G, lo, c, fan);
+        else
+            k_seed<false><<<grid, 32 * kSeedWarps, 0, st>>>(P, G, lo, c, fan);
+    }
     if (hi > c) {
         const JumpPairs jp = JumpPairs::make(P.seed, c, hi);
         const int grid = (int)std::min<uint32_t>(jp.n_pairs, 152 * kJumpBlocksPerSm);
-        k_seed_jump<<<grid, 96, kJumpSmem, st>>>(P, G, jt->polys, jt->R_lo, jp);
+        if (fan.n)
+            k_seed_jump<true><<<grid, 96, kJumpSmem, st>>>(P, G, jt->polys, jt->R_lo, jp, fan);
+        else
+            k_seed_jump<false><<<grid, 96, kJumpSmem, st>>>(P, G, jt->polys, jt->R_lo, jp, fan);
     }
     return cudaGetLastError();
 }

@@ -18,10 +18,25 @@ struct JumpTable {
     uint64_t R_lo = 0, R_hi = 0;
     uint64_t z_min = ~0ull;
 };
+// Further destinations of the seeded state (a pooled batch: every instance's gen_u starts from
+// its stream's seeded state): spin s < n gets the 624 words in mt, its position in p and the
+// three ring counters c0, c1, c2 zeroed. d is a device array of n entries.
+struct SeedCopy {
+    uint32_t *mt, *p;
+    uint32_t *c0, *c1, *c2;
+    uint32_t n;
+};
+struct SeedCopies {
+    const SeedCopy *d = nullptr;
+    uint32_t n = 0;
+};
 // Spins with seed + spin >= jt->z_min are seeded by jump-ahead when jt is given (it must cover
-// their regeneration counts), the others by the plain discard.
+// their regeneration counts), the others by the plain discard. With `fan`, the seeding kernels
+// also store the state at those destinations (an instance of the kernels of its own: the
+// seeding without destinations compiles as if they did not exist).
 cudaError_t launch_seed_range(const DevParams &P, const RngState &G, uint32_t lo, uint32_t hi,
-                              cudaStream_t st, const JumpTable *jt = nullptr);
+                              cudaStream_t st, const JumpTable *jt = nullptr,
+                              SeedCopies fan = SeedCopies{});
 // Tops up the rings of the spins in [lo, hi) that are not done, each to what its remaining walk
 // can draw at most (S: flags, time point and scan of every spin).
 cudaError_t launch_refill_range(const DevParams &P, const RngState &G, const SpinState &S,

@@ -52,6 +52,7 @@ struct PoolCtx {
     cudaStream_t side = nullptr;         // instance inputs and k_init, beside the seeding
     cudaEvent_t side_done = nullptr;
     cudaEvent_t stage[4] = {};           // timing: the seeding, then the rounds
+    cudaEvent_t piece[8] = {};           // output read-back in pieces
     uint32_t *h_active = nullptr;        // pinned
     bool ready = false;
 };
@@ -78,6 +79,7 @@ int ensure_ctx(PoolCtx &c) {
     PL_CUDA(cudaStreamCreateWithPriority(&c.side, cudaStreamNonBlocking, hi));
     PL_CUDA(cudaEventCreateWithFlags(&c.side_done, cudaEventDisableTiming));
     for (auto &e : c.stage) PL_CUDA(cudaEventCreate(&e));
+    for (auto &e : c.piece) PL_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     PL_CUDA(cudaMallocHost(&c.h_active, sizeof(uint32_t)));
     c.ready = true;
     return SW_OK;
@@ -152,6 +154,7 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
         for (int k = 0; k < 3; k++) c.take<uint32_t>(n_max);  // p_r nw nmin
         c.take<float>(n_max * sw::kPoolNorm);
         c.take<sw::BatchInst>(n_items);                      // descriptors of the fused launches
+        c.take<sw::SeedCopy>(n_items);                       // gen_u of every instance
         for (Inst &I : in) {
             const size_t n = I.n;
             I.tables = c.take<char>(I.im.bytes.size());
@@ -280,6 +283,7 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
     Q.nmin = c2.take<uint32_t>(n_max);
     Q.nbuf = c2.take<float>(n_max * sw::kPoolNorm);
     sw::BatchInst *d_inst = c2.take<sw::BatchInst>(n_items);
+    sw::SeedCopy *d_fan = c2.take<sw::SeedCopy>(n_items);
     char *d_io = X.d + state_bytes;
     cudaStream_t ms = X.main;
     uint32_t launches = 0;
@@ -303,18 +307,19 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
         Gs.p_r = Gs.p_u = Q.p_r;
         Gs.nhead = Gs.uhead = Q.nw;
         Gs.ncnt = Gs.ucnt = Q.nmin;
-        PL_CUDA(sw::launch_seed_range(Ps, Gs, 0, (uint32_t)n_max, ms, &jt));
+        // each instance's gen_u starts from the same seeded state: the seeding kernels store it
+        // there as well, with the instance's read positions and uniform counters zeroed (their
+        // stores hide under the integer work of the seeding; 64 device copies afterwards would
+        // put ~10 ms of copying between the seeding and the first round)
+        std::vector<sw::SeedCopy> fan;
+        for (Inst &I : in)
+            if (I.n) fan.push_back({I.G.mt_u, I.G.p_u, I.G.nhead, I.G.uhead, I.G.ucnt, (uint32_t)I.n});
+        PL_CUDA(cudaMemcpyAsync(d_fan, fan.data(), fan.size() * sizeof(sw::SeedCopy),
+                                cudaMemcpyHostToDevice, ms));
+        PL_CUDA(sw::launch_seed_range(Ps, Gs, 0, (uint32_t)n_max, ms, &jt,
+                                      sw::SeedCopies{d_fan, (uint32_t)fan.size()}));
         PL_CUDA(cudaEventRecord(X.stage[1], ms));
         launches++;
-        // each instance's gen_u starts from the same seeded state, before any refill moves it
-        for (Inst &I : in) {
-            if (!I.n) continue;
-            PL_CUDA(cudaMemcpyAsync(I.G.mt_u, Q.mt_r, I.n * sw::kMtN * 4, cudaMemcpyDeviceToDevice, ms));
-            PL_CUDA(cudaMemcpyAsync(I.G.p_u, Q.p_r, I.n * 4, cudaMemcpyDeviceToDevice, ms));
-            PL_CUDA(cudaMemsetAsync(I.G.nhead, 0, I.n * 4, ms));
-            PL_CUDA(cudaMemsetAsync(I.G.uhead, 0, I.n * 4, ms));
-            PL_CUDA(cudaMemsetAsync(I.G.ucnt, 0, I.n * 4, ms));
-        }
     }
     cudaStream_t w0 = X.side;
     {
@@ -498,22 +503,42 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
     launches += round_kernels * (uint32_t)(rounds + 1);
     PL_CUDA(cudaEventRecord(X.stage[3], ms));
 
-    // ---- outputs ----
-    PL_CUDA(cudaMemcpyAsync(X.h + out_begin, d_io + out_begin, io - out_begin,
-                            cudaMemcpyDeviceToHost, ms));
-    PL_CUDA(cudaStreamSynchronize(ms));
+    // ---- outputs: read back in pieces of whole instances (their output sections are
+    // contiguous, in instance order); the host copies a piece into the caller's arrays while the
+    // next one is still on its way ----
     {
-        std::vector<CopyJob> jobs;
-        for (Inst &I : in) {
-            const sw_instance &it = *I.it;
-            if (I.nte) {
-                jobs.push_back({it.M1, X.h + I.o_M1, I.n * I.nte * 12});
-                jobs.push_back({it.T, X.h + I.o_T, I.n * I.nte});
-            }
-            jobs.push_back({it.XYZ1, X.h + I.o_XYZ1, I.n * I.trj * 12});
-            if (it.status) jobs.push_back({it.status, X.h + I.o_st, I.n * 4});
+        constexpr uint32_t kPieces = sizeof(X.piece) / sizeof(X.piece[0]);
+        const size_t out_bytes = io - out_begin;
+        std::vector<uint32_t> first(1, 0u);              // first instance of every piece
+        for (uint32_t i = 0; i < n_items && first.size() < kPieces; i++) {
+            const size_t end = in[i].o_st + in[i].n * 4;
+            if ((end - out_begin) * kPieces >= out_bytes * first.size() && i + 1 < n_items)
+                first.push_back(i + 1);
         }
-        par_copy_all(jobs);
+        first.push_back(n_items);
+        const uint32_t np = (uint32_t)first.size() - 1;
+        for (uint32_t k = 0; k < np; k++) {
+            const size_t a = in[first[k]].o_M1;
+            const size_t b = k + 1 < np ? in[first[k + 1]].o_M1 : io;
+            if (b > a)
+                PL_CUDA(cudaMemcpyAsync(X.h + a, d_io + a, b - a, cudaMemcpyDeviceToHost, ms));
+            PL_CUDA(cudaEventRecord(X.piece[k], ms));
+        }
+        for (uint32_t k = 0; k < np; k++) {
+            PL_CUDA(cudaEventSynchronize(X.piece[k]));
+            std::vector<CopyJob> jobs;
+            for (uint32_t i = first[k]; i < first[k + 1]; i++) {
+                const Inst &I = in[i];
+                const sw_instance &it = *I.it;
+                if (I.nte) {
+                    jobs.push_back({it.M1, X.h + I.o_M1, I.n * I.nte * 12});
+                    jobs.push_back({it.T, X.h + I.o_T, I.n * I.nte});
+                }
+                jobs.push_back({it.XYZ1, X.h + I.o_XYZ1, I.n * I.trj * 12});
+                if (it.status) jobs.push_back({it.status, X.h + I.o_st, I.n * 4});
+            }
+            par_copy_all(jobs);
+        }
     }
     g_timing.n_chunks = (uint32_t)(rounds + 1);          // refill/walk rounds
     g_timing.n_launches = launches;

@@ -14,12 +14,13 @@
 // (one spin waiting for uniforms a slower spin holds back, that one waiting for Gaussians the
 // first holds back), while with one pooled kind the slowest reader always gets a full ring.
 //
-// A round: k_refill_pool over the streams, then per instance its uniforms and its walk (one
-// launch each, on a branch of a CUDA graph captured once per call and launched once per round,
-// so that the instances' walks are independent graph nodes); a stream's ring is topped up to the
-// lowest read position of the pairs that paused in the previous walk plus the ring length, so
-// nothing unread is overwritten. Results equal one sw_sim call per instance bit for bit
-// (tests/test_batch.py).
+// A round: k_refill_pool over the streams, then the crossing uniforms and the walks of all
+// instances, one launch each over every instance (k_refill_uniforms_batch, k_walk_batch: blocks
+// dealt out instance by instance, per-instance descriptors in the workspace); the round is
+// captured once per call as a CUDA graph and launched once per round. A stream's ring is topped
+// up to the lowest read position of the pairs that paused in the previous walk plus the ring
+// length, so nothing unread is overwritten. Results equal one sw_sim call per instance bit for
+// bit (tests/test_batch.py).
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -311,6 +311,16 @@ int sw_sim_device_noalloc(const sw_params *param, const sw_sequence *seq,
                           float *d_M1, float *d_XYZ1, uint8_t *d_T, int32_t *d_status,
                           void *stream);
 
+/* Frees what the one-call entry points keep on the current device between calls: the device
+ * workspaces of sw_sim / sw_sim_device (generator state, rings, walk state), sw_sim's device
+ * copies of the caller's buffers, the pooled batch's workspace and pinned staging, and the
+ * internal engine of sw_sim_batch / sw_sim_spins / sw_sim_signal. They are otherwise kept until
+ * the process exits, grown to the largest call so far (about 12 KB per spin). The next call
+ * allocates again. Waits for a call running on another thread to finish; engines created with
+ * sw_engine_create, the logf table and the minstd deviate table are not touched. No counterpart
+ * in the reference (its driver frees its thrust vectors after every scale). */
+int sw_release_workspaces(void);
+
 /* Timing of the kernels launched by the last sw_sim / sw_sim_device call on this thread
  * (milliseconds, CUDA events on the launching stream): seeding, RNG refill, walk, total. After
  * sw_sim_batch with pooled generators: seed_ms the seeding of the streams, walk_ms all rounds

@@ -509,6 +509,11 @@ def debug_d2f(d_x, d_y, n, stream=None):
     check(lib().sw_debug_d2f(d_x, d_y, C.c_uint64(n), stream))
 
 
+def release_workspaces():
+    """sw_release_workspaces: frees the device memory the one-call entry points keep."""
+    check(lib().sw_release_workspaces())
+
+
 def debug_dadd(d_a, d_b, d_y, n, stream=None):
     check(lib().sw_debug_dadd(d_a, d_b, d_y, C.c_uint64(n), stream))
 

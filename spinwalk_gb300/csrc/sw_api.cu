@@ -659,6 +659,26 @@ int sw_device_count(int *count) {
     return SW_OK;
 }
 
+int sw_release_workspaces(void) {
+    int dev = 0;
+    DeviceCtx *ctx = current_ctx(&dev);
+    if (!ctx) return fail(SW_ERR_CUDA, "no current CUDA device");
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        if (ctx->ws) cudaFree(ctx->ws);
+        if (ctx->io) cudaFree(ctx->io);
+        if (ctx->d_jump) cudaFree(ctx->d_jump);
+        ctx->ws = ctx->io = nullptr;
+        ctx->d_jump = nullptr;
+        ctx->ws_size = ctx->io_size = ctx->jump_words = 0;
+    }
+    release_pool_memory(dev);
+    release_call_engine(dev);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(SW_ERR_CUDA, std::string("release: ") + cudaGetErrorString(e));
+    return SW_OK;
+}
+
 int sw_sync(void *stream) {
     SW_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
     return SW_OK;

@@ -89,6 +89,11 @@ int jump_table(uint64_t seed, uint32_t lo, uint32_t hi, uint64_t z_min, uint32_t
 int run_batch_pooled(const sw_instance *items, uint32_t n_items, const float *pFieldMap,
                      const uint8_t *pMask, int precision, bool &taken);
 
+// sw_release_workspaces, per part: the current device's batch pool (sw_pool.cu) and the engine
+// of the one-call entry points (sw_engine.cu); each waits for its lock, i.e. for a running call.
+void release_pool_memory(int dev);
+void release_call_engine(int dev);
+
 // Kernel timing of the last call on this thread (sw_last_timing).
 extern thread_local sw_timing g_timing;
 // Sets sw_last_error() for the calling thread and returns `code`.

@@ -873,6 +873,13 @@ int finish_call_engine(sw_engine *E, int rc) {
 }
 }  // namespace
 
+void sw::api::release_call_engine(int dev) {
+    if (dev < 0 || dev >= kMaxBatchDevices) return;
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    if (g_batch_engine[dev]) engine_free(g_batch_engine[dev]);
+    g_batch_engine[dev] = nullptr;
+}
+
 extern "C" {
 
 int sw_sim_batch(const sw_instance *items, uint32_t n_items, const float *pFieldMap,

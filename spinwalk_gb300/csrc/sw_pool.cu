@@ -125,6 +125,19 @@ struct Inst {
 
 }  // namespace
 
+void sw::api::release_pool_memory(int dev) {
+    if (dev < 0 || dev >= kMaxDevices) return;
+    PoolCtx &X = g_pool[dev];
+    std::lock_guard<std::mutex> lk(X.mu);
+    if (X.d) cudaFree(X.d);
+    if (X.h) cudaFreeHost(X.h);
+    if (X.d_jump) cudaFree(X.d_jump);
+    X.d = nullptr;
+    X.h = nullptr;
+    X.d_jump = nullptr;
+    X.d_bytes = X.h_bytes = X.jump_words = 0;
+}
+
 int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const float *pFieldMap,
                               const uint8_t *pMask, int precision, bool &taken) {
     taken = false;

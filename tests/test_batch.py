@@ -154,3 +154,25 @@ def test_batch_refused_mask_then_batch_matches():
             one = _lib.run(pr)
             for key in ("M1", "XYZ1", "T", "status"):
                 assert bits_equal(b[key], one[key]), (k, key)
+
+
+@pytest.mark.gpu
+def test_release_workspaces_frees_device_memory_and_calls_still_match():
+    """sw_release_workspaces gives back the device memory that sw_sim and sw_sim_batch keep
+    between calls; the calls after it allocate again and give the same results."""
+    torch = pytest.importorskip("torch")
+    probs = _instances()
+    a = _lib.run_batch(probs)
+    one = _lib.run(probs[0])
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    _lib.release_workspaces()
+    free_after = torch.cuda.mem_get_info()[0]
+    assert free_after > free_before
+    b = _lib.run_batch(probs)
+    again = _lib.run(probs[0])
+    for k, (pr, x, y) in enumerate(zip(probs, a, b)):
+        for key in ("M1", "XYZ1", "T", "status"):
+            assert bits_equal(x[key], y[key]), (k, key)
+    for key in ("M1", "XYZ1", "T", "status"):
+        assert bits_equal(one[key], again[key]), key

@@ -364,7 +364,9 @@ int sw_last_timing(sw_timing *out);
  *                     between refill and walk.
  *   walk_blocks_per_sm : sw_sim / sw_sim_device: caps the walk launch at this many blocks per
  *                     SM, the blocks striding over the spins, so that the other half's refill
- *                     can run beside it on every SM; 0 = default (no cap, one thread per spin).
+ *                     can run beside it on every SM; sw_sim_batch (pooled generators): the
+ *                     fused walk over all instances then runs as persistent blocks striding over
+ *                     the instances' blocks; 0 = default (no cap, one thread per spin).
  */
 typedef struct sw_tuning {
     uint32_t resort_interval;

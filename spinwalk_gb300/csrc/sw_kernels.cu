@@ -802,17 +802,17 @@ __global__ void __launch_bounds__(32 * kRefillWarps)
     }
 }
 
-// Instance of block b of a fused batch launch: the last descriptor whose first block is <= b
-// (descriptors in block order), found by thread 0 and shared with the block.
+// Instance of work block b of a fused batch launch: the last descriptor whose first block is
+// <= b (descriptors in block order), found by thread 0 and shared with the block.
 template <bool WALK>
 __device__ __forceinline__ uint32_t batch_instance(const BatchInst *__restrict__ D, uint32_t n_inst,
-                                                   uint32_t *s_k) {
+                                                   uint32_t b, uint32_t *s_k) {
     if (threadIdx.x == 0) {
         uint32_t lo = 0, hi = n_inst;
         while (hi - lo > 1) {
             const uint32_t mid = (lo + hi) >> 1;
             const uint32_t b0 = WALK ? D[mid].walk_block0 : D[mid].unif_block0;
-            if (b0 <= blockIdx.x) lo = mid; else hi = mid;
+            if (b0 <= b) lo = mid; else hi = mid;
         }
         *s_k = lo;
     }
@@ -829,7 +829,7 @@ __global__ void __launch_bounds__(32 * kRefillWarps)
     k_refill_uniforms_batch(const BatchInst *__restrict__ D, uint32_t n_inst) {
     __shared__ uint32_t s_mt[kRefillWarps][kMtN];
     __shared__ uint32_t s_k;
-    const BatchInst &I = D[batch_instance<false>(D, n_inst, &s_k)];
+    const BatchInst &I = D[batch_instance<false>(D, n_inst, blockIdx.x, &s_k)];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t base = ((blockIdx.x - I.unif_block0) * kRefillWarps + w) * 32;
     const uint32_t mine = base + lane;
@@ -1177,24 +1177,29 @@ __global__ void __launch_bounds__(256, 4)
     if (lane == 0 && paused) atomicAdd(active, paused);
 }
 
-// The walk of a pooled batch, every instance in one launch: block b walks 256 spins of one
+// The walk of a pooled batch, every instance in one launch: work block b walks 256 spins of one
 // instance (whose parameters, tables and state it reads from its descriptor), drawing their
-// steps from the pooled streams Q (G.nhead: the instance's read positions in them).
+// steps from the pooled streams Q (G.nhead: the instance's read positions in them). A grid
+// smaller than the work blocks makes it persistent: each block strides over them.
 template <int PREC, bool DBL>
 __global__ void __launch_bounds__(256, 4)
-    k_walk_batch(const BatchInst *__restrict__ D, uint32_t n_inst, const uint2 *__restrict__ vox,
-                 PoolState Q, uint32_t *active) {
+    k_walk_batch(const BatchInst *__restrict__ D, uint32_t n_inst, uint32_t walk_blocks,
+                 const uint2 *__restrict__ vox, PoolState Q, uint32_t *active) {
     __shared__ uint32_t s_k;
-    const BatchInst &I = D[batch_instance<true>(D, n_inst, &s_k)];
-    const uint32_t spin = (blockIdx.x - I.walk_block0) * 256 + threadIdx.x;
-    bool still = false;
-    if (spin < I.n_spins) {
-        const uint32_t flags = I.S.flags[spin];
-        if (!(flags & kFlagDone))
-            still = walk_spin<PREC, DBL, true>(spin, flags, I.P, I.Tb, vox, I.S, I.G, I.O, Q);
+    uint32_t paused = 0;
+    for (uint32_t b = blockIdx.x; b < walk_blocks; b += gridDim.x) {
+        __syncthreads();                             // s_k of the previous work block is read
+        const BatchInst &I = D[batch_instance<true>(D, n_inst, b, &s_k)];
+        const uint32_t spin = (b - I.walk_block0) * 256 + threadIdx.x;
+        bool still = false;
+        if (spin < I.n_spins) {
+            const uint32_t flags = I.S.flags[spin];
+            if (!(flags & kFlagDone))
+                still = walk_spin<PREC, DBL, true>(spin, flags, I.P, I.Tb, vox, I.S, I.G, I.O, Q);
+        }
+        paused += __popc(__ballot_sync(0xffffffffu, still));
     }
-    const unsigned b = __ballot_sync(0xffffffffu, still);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(active, (uint32_t)__popc(b));
+    if ((threadIdx.x & 31) == 0 && paused) atomicAdd(active, paused);
 }
 
 __global__ void k_debug_logf(const float *x, float *y, uint64_t n, LogfTables L) {
@@ -1349,19 +1354,21 @@ cudaError_t launch_refill_uniforms_batch(const BatchInst *D, uint32_t n_inst, ui
 
 cudaError_t launch_walk_batch(int prec, bool dbl, const BatchInst *D, uint32_t n_inst,
                               uint32_t walk_blocks, const uint2 *vox, const PoolState &Q,
-                              uint32_t *active, cudaStream_t st) {
+                              uint32_t *active, cudaStream_t st, int max_blocks) {
     if (!n_inst || !walk_blocks) return cudaSuccess;
-    const uint32_t g = walk_blocks;
+    const uint32_t g = max_blocks > 0 ? std::min<uint32_t>(walk_blocks, (uint32_t)max_blocks)
+                                      : walk_blocks;
+    const uint32_t wb = walk_blocks;
     if (prec == SW_PREC_FP64)
-        k_walk_batch<SW_PREC_FP64, true><<<g, 256, 0, st>>>(D, n_inst, vox, Q, active);
+        k_walk_batch<SW_PREC_FP64, true><<<g, 256, 0, st>>>(D, n_inst, wb, vox, Q, active);
     else if (prec == SW_PREC_KAHAN && dbl)
-        k_walk_batch<SW_PREC_KAHAN, true><<<g, 256, 0, st>>>(D, n_inst, vox, Q, active);
+        k_walk_batch<SW_PREC_KAHAN, true><<<g, 256, 0, st>>>(D, n_inst, wb, vox, Q, active);
     else if (prec == SW_PREC_KAHAN)
-        k_walk_batch<SW_PREC_KAHAN, false><<<g, 256, 0, st>>>(D, n_inst, vox, Q, active);
+        k_walk_batch<SW_PREC_KAHAN, false><<<g, 256, 0, st>>>(D, n_inst, wb, vox, Q, active);
     else if (dbl)
-        k_walk_batch<SW_PREC_FP32, true><<<g, 256, 0, st>>>(D, n_inst, vox, Q, active);
+        k_walk_batch<SW_PREC_FP32, true><<<g, 256, 0, st>>>(D, n_inst, wb, vox, Q, active);
     else
-        k_walk_batch<SW_PREC_FP32, false><<<g, 256, 0, st>>>(D, n_inst, vox, Q, active);
+        k_walk_batch<SW_PREC_FP32, false><<<g, 256, 0, st>>>(D, n_inst, wb, vox, Q, active);
     return cudaGetLastError();
 }
 

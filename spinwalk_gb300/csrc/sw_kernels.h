@@ -58,9 +58,10 @@ constexpr uint32_t kRefillBatchSpins = 128;
 // [0, unif_blocks); each instance's results equal its own sw_sim run bit for bit.
 cudaError_t launch_refill_uniforms_batch(const BatchInst *D, uint32_t n_inst, uint32_t unif_blocks,
                                          cudaStream_t st);
+// max_blocks > 0 caps the walk's grid (persistent blocks striding over the work blocks).
 cudaError_t launch_walk_batch(int prec, bool dbl, const BatchInst *D, uint32_t n_inst,
                               uint32_t walk_blocks, const uint2 *vox, const PoolState &Q,
-                              uint32_t *active, cudaStream_t st);
+                              uint32_t *active, cudaStream_t st, int max_blocks = 0);
 // Morton re-sort of spins [lo, hi) into Q.order (sw_order.cu).
 cudaError_t launch_order(const DevParams &P, const SpinState &S, const OrderState &Q,
                          uint32_t lo, uint32_t hi, cudaStream_t st);

@@ -476,7 +476,7 @@ int sw::api::run_batch_pooled(const sw_instance *items, uint32_t n_items, const 
         ok(sw::launch_refill_pool(Q, LT, (uint32_t)n_max, ms));
         ok(sw::launch_refill_uniforms_batch(d_inst, n_desc, unif_blocks, ms));
         ok(sw::launch_walk_batch(prec, prec == SW_PREC_FP64, d_inst, n_desc, walk_blocks, vox, Q,
-                                 cnt, ms));
+                                 cnt, ms, walk_grid_cap(current_tuning())));
         const cudaError_t ec = cudaStreamEndCapture(ms, &graph);
         if (e == cudaSuccess) e = ec;
         if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);

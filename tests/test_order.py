@@ -205,3 +205,23 @@ def test_dense_walk_grid_cap(tuning, cap):
     tuning(0, 256, 1, 2, 0, 0, cap)
     got = _lib.run(pr, precision=2, fp64_shadow=True, fill=np.nan)
     _same(got, want, ("M1", "XYZ1", "T", "status", "M1_fp64"))
+
+
+@pytest.mark.gpu
+def test_batch_persistent_walk_equals_default(tuning):
+    """With a cap on the walk's blocks per SM, the fused batch walk runs as persistent blocks that
+    stride over the instances' work blocks (here 4 x 47 work blocks on at most one block per SM);
+    every instance equals the uncapped batch bit for bit."""
+    probs = []
+    for k, s in enumerate((1.0, 0.8, 1.25, 1.1)):
+        pr = _dense_problem(n_spins=12000, TE_us=(3000, 9000), RF_FA=(90.0, 180.0),
+                            RF_PH=(0.0, 90.0), RF_us=(0, 4500))
+        s32 = np.float32(s)
+        pr.params.fov[0] = pr.params.fov[1] = pr.params.fov[2] = float(s32 * np.float32(32e-6))
+        pr.XYZ0 = (pr.XYZ0 * s32).astype(np.float32)
+        probs.append(pr)
+    want = _lib.run_batch(probs, fill=np.nan)
+    tuning(walk_blocks_per_sm=1)
+    got = _lib.run_batch(probs, fill=np.nan)
+    for a, b in zip(want, got):
+        _same(a, b)

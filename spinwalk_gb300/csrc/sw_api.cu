@@ -757,9 +757,9 @@ int sw_sim(const sw_params *param, const sw_sequence *seq, const float *pFieldMa
         if (e2 != cudaSuccess)                                                             \
             return done(fail(SW_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e2))); \
     } while (0)
+    begun = true;                          // from here an error return waits for the GPU
     if (int rc0 = begin_call(*ctx, param, seq, precision, M1_fp64 != nullptr, st, c))
         return done(rc0);
-    begun = true;
     SW_TRY(cudaMemcpyAsync(d + o_mask, pMask, ml, cudaMemcpyHostToDevice, st));
     if (has_field) SW_TRY(cudaMemcpyAsync(d + o_field, pFieldMap, ml * 4, cudaMemcpyHostToDevice, st));
     SW_TRY(cudaMemcpyAsync(d + o_M0, M0, n * 12, cudaMemcpyHostToDevice, st));

@@ -1153,7 +1153,9 @@ __device__ __forceinline__ bool walk_spin(const uint32_t spin, uint32_t flags, c
 }
 
 // 4 blocks of 256 per SM (64 registers): the walk is latency bound and its occupancy pays more
-// than the registers the compiler would otherwise take (SE walk 37.7 vs 44.0 ms at 78 registers)
+// than the registers the compiler would otherwise take (SE walk 37.7 vs 44.0 ms at 78 registers);
+// a fifth block (48 registers, 76 bytes of spills) is slower again (SE 75.3 -> 83.1 ms of walk
+// launch time per pass, GRE 1.11 -> 1.26 ms)
 template <int PREC, bool DBL>
 __global__ void __launch_bounds__(256, 4)
     k_walk(DevParams P, DevTables Tb, const uint2 *__restrict__ vox, SpinState S, RngState G,

@@ -177,6 +177,37 @@ def test_gpu_device_api_matches_host_api():
     assert np.array_equal(d_st.cpu().numpy(), h["status"])
 
 
+def test_gpu_device_call_waits_for_inputs_on_the_callers_stream():
+    """sw_sim_device starts seeding at once, but its walk is ordered after the caller's stream:
+    start positions, phantom and M0 that arrive late on that stream (after ~20 ms of other work
+    there) are the ones the walk reads."""
+    torch = pytest.importorskip("torch")
+    pr, _ = load_golden("se_multi_te")
+    h = _lib.run(pr)
+    n, nte = pr.params.n_spins, pr.n_te
+    dev = "cuda"
+    src = {k: torch.from_numpy(getattr(pr, k)).to(dev) for k in ("field", "mask", "M0", "XYZ0")}
+    dst = {k: torch.zeros_like(v) for k, v in src.items()}
+    d_M1 = torch.zeros((n, nte, 3), dtype=torch.float32, device=dev)
+    d_XYZ1 = torch.zeros((n, pr.traj_len, 3), dtype=torch.float32, device=dev)
+    d_T = torch.zeros((n, nte), dtype=torch.uint8, device=dev)
+    d_st = torch.zeros(n, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        torch.cuda._sleep(40_000_000)                # the caller's stream is busy for a while
+        for k in src:
+            dst[k].copy_(src[k])                     # then produces the inputs
+    _lib.run_device(pr, dst["field"].data_ptr(), dst["mask"].data_ptr(), dst["M0"].data_ptr(),
+                    dst["XYZ0"].data_ptr(), d_M1.data_ptr(), d_XYZ1.data_ptr(), d_T.data_ptr(),
+                    d_st.data_ptr(), stream=s.cuda_stream)
+    torch.cuda.synchronize()
+    assert bits_equal(d_XYZ1.cpu().numpy(), h["XYZ1"])
+    assert bits_equal(d_M1.cpu().numpy(), h["M1"])
+    assert bits_equal(d_T.cpu().numpy(), h["T"])
+    assert np.array_equal(d_st.cpu().numpy(), h["status"])
+
+
 def test_gpu_host_call_after_refused_mask_matches():
     """sw_sim launches its seeding before it copies the inputs in. A call refused afterwards (a
     mask label >= n_substrate, found by the pack) leaves the device usable, and later calls,

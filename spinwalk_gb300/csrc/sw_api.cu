@@ -292,6 +292,7 @@ struct Call {
 
 // Waits for everything a call may have left on the context's streams (error paths).
 void drain(DeviceCtx &ctx) {
+    if (!ctx.logf_ready) return;           // the streams are created with the tables
     cudaStreamSynchronize(ctx.seed_st);
     cudaStreamSynchronize(ctx.walk_st);
     cudaStreamSynchronize(ctx.walk_st2);

@@ -176,3 +176,39 @@ def test_release_workspaces_frees_device_memory_and_calls_still_match():
             assert bits_equal(x[key], y[key]), (k, key)
     for key in ("M1", "XYZ1", "T", "status"):
         assert bits_equal(one[key], again[key]), key
+
+
+@pytest.mark.gpu
+def test_batch_of_many_instances_with_empty_ones():
+    """Eighty instances (more than the batch reads back in pieces, some with no spins, first and
+    last among them) of different sizes, FoV scales and sequences: the fused launches find every
+    block's instance and every instance equals its own sw_sim run bit for bit."""
+    mask, field = _phantom()
+    xyz0 = _lib.initial_positions([FOV] * 3, 10, 400)
+    rng = np.random.default_rng(17)
+    gre = dict(TR_us=4050, TE_us=(2000, 4000), timestep_us=50)
+    se = dict(TR_us=4050, TE_us=(4000,), RF_FA=(90.0, 180.0), RF_PH=(0.0, 90.0),
+              RF_us=(0, 2000), timestep_us=50, pXY=[[1, 0.3], [0.2, 1]])
+    probs = []
+    for i in range(80):
+        n = 0 if i in (0, 33, 79) else int(rng.integers(1, 400))
+        s32 = np.float32(0.5 + 0.02 * i)
+        probs.append(Problem(mask, [float(s32 * np.float32(FOV))] * 3, field, n_spins=n, seed=10,
+                             XYZ0=(xyz0[:n] * s32).astype(np.float32), **(gre if i % 2 else se)))
+    batch = _lib.run_batch(probs, fill=np.nan)
+    for k, (pr, b) in enumerate(zip(probs, batch)):
+        if pr.params.n_spins == 0:
+            continue
+        one = _lib.run(pr, fill=np.nan)
+        for key in ("M1", "XYZ1", "T", "status"):
+            assert bits_equal(b[key], one[key]), (k, key)
+
+
+@pytest.mark.gpu
+def test_batch_of_one_instance():
+    """A batch of a single instance (one read-back piece) equals its sw_sim run."""
+    pr = _instances()[0]
+    b = _lib.run_batch([pr], fill=np.nan)[0]
+    one = _lib.run(pr, fill=np.nan)
+    for key in ("M1", "XYZ1", "T", "status"):
+        assert bits_equal(b[key], one[key]), key

@@ -946,8 +946,9 @@ def run_ours(args, world, rank, local):
     # walk-only rate: the call's wall time minus its seeding stage (the kernel times of the two
     # halves of the rounds overlap, so their sum would overstate it)
     walk_refill_s = ms / args.steps * 1e-3 - seed_ms / args.steps * 1e-3
+    overlapped = tuning["applied"]["seed_chunks"] > 1     # the seeding runs beside the walk
     secondary = {
-        "walk_only_spin_steps_per_s": spin_steps / walk_refill_s,
+        "walk_only_spin_steps_per_s": None if overlapped else spin_steps / walk_refill_s,
         "refill_mt_state_gbs": spin_steps * MT_BYTES_PER_SPIN_STEP / (refill_ms / args.steps * 1e-3) / 1e9,
         "walk_fp64_gflops": spin_steps * WALK_FP64_OPS_PER_SPIN_STEP / (walk_ms / args.steps * 1e-3) / 1e9,
         "fp64_peak_gflops": FP64_PEAK_GFLOPS,

@@ -342,11 +342,10 @@ int sw_last_timing(sw_timing *out);
  *   walk_block      : threads per block of the walk kernel: 64, 128 or 256
  *   seed_chunks     : sw_sim / sw_sim_device seed the spins in this many chunks of equal seeding
  *                     cost on a low-priority stream and walk each seeded chunk on a
- *                     high-priority stream meanwhile (1 = seed everything, then walk; at most
- *                     64). 0 = auto: 8 chunks when the walk is a sizeable share of the discards
- *                     (at least 2^19 spins, mt19937 with no spin jumping ahead, and
- *                     steps >= 2e-3 x (seed + n_spins / 2)), else 1; elsewhere the co-resident
- *                     kernels slow each other down by more than the overlap saves.
+ *                     high-priority stream meanwhile (0 or 1 = seed everything, then walk; at
+ *                     most 64). It pays only where the walk is a sizeable share of the discards
+ *                     (8 chunks on 1e6 spins of 2001 steps: 1.4 % faster); elsewhere the
+ *                     co-resident kernels slow each other down by more than the overlap saves.
  *   round_streams   : sw_sim / sw_sim_device run the refill/walk rounds of the spins as this
  *                     many independent halves on their own streams (1 = one, 2 = two, 0 = auto:
  *                     two from 2^17 spins on), so that one half's walk overlaps the other

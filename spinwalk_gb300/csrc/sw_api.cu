@@ -351,23 +351,12 @@ int begin_call(DeviceCtx &ctx, const sw_params *p, const sw_sequence *q, int pre
     if (rng == SW_RNG_MINSTD && !(c.LT.ms_delta = minstd_delta_table())) return SW_ERR_CUDA;
 
     const sw_tuning tu = current_tuning();
-    // 0 = auto: 8 chunks where the rounds are a sizeable share of the seeding, else 1. With the
-    // rounds as two halves, a seeded chunk's walk beside the next chunk's seeding saves a little
-    // more than the two kernels cost each other on a GB300 when the walk is at least about a
-    // third of the discards (SE, 1e6 spins, 2001 steps: 187.3 -> 184.7 ms per call with 8
-    // chunks, 187.0 with 4, 191.0 with 12); where it is less (2e6 spins of 801 steps: 495.9 ->
-    // 498.2 ms with 8) or the spins are few (2e5: 7.72 -> 8.81 ms; 1e5, 401 steps: 3.50 ->
-    // 5.78 ms with 4), one chunk stays faster. The walk's share is ~140 x steps / (seed + n/2)
-    // of the discards' time (a discarded word against a walk step, measured), so 8 chunks from
-    // steps / (seed + n/2) >= 2e-3 and 2^19 spins on; spins that jump ahead or the minstd
-    // generators have no long discards to hide.
-    uint32_t C = tu.seed_chunks;
-    if (C == 0) {
-        const uint64_t steps = (uint64_t)p->n_timepoints * (uint64_t)(p->n_dummy_scan + 1);
-        const double span = (double)p->seed + 0.5 * (double)n;
-        const bool long_discards = rng == SW_RNG_MT19937 && p->seed + n < jump_min_z(tu);
-        C = (long_discards && n >= (1u << 19) && (double)steps >= 2e-3 * span) ? 8u : 1u;
-    }
+    // 0 = 1. With the rounds as two halves, a seeded chunk's walk beside the next chunk's seeding
+    // gains only where the walk is a sizeable share of the discards (SE, 1e6 spins, 2001 steps:
+    // 187.3 -> 184.7 ms per call with 8 chunks, 191.0 with 12), and loses elsewhere (2e6 spins of
+    // 801 steps: 495.9 -> 498.2 ms; 2e5 spins: 7.72 -> 8.81 ms; 1e5 spins, 401 steps: 3.50 ->
+    // 5.78 ms with 4); callers with SE-like shapes can ask for 8.
+    const uint32_t C = tu.seed_chunks ? tu.seed_chunks : 1u;
     c.C = std::min<uint32_t>(std::min<uint32_t>(C, kMaxSeedChunks), (uint32_t)n);
     c.b = seed_chunks(c.P, c.C);
     // high spin ids jump ahead instead of discarding (the previous call has finished with the
